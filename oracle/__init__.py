@@ -1,0 +1,227 @@
+"""CPU oracle for the particle-to-volume path — TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this package,
+and only as the checker / the timed CPU baseline. The shipped GPU library never calls it.
+
+Two native libraries back it (both built by ``oracle/Makefile``):
+
+* ``_build/libp2v_oracle.so`` — our restatement of the reference algorithms (``p2v_oracle.cpp``), FP32
+  with the reference's operation order and FP64 for error judging.
+* ``_ref/libref_p2d.so`` — MegaMol's own ``plugins/datatools/src/ParticlesToDensity.cpp``, compiled
+  unmodified against ``oracle/shim`` and driven through its slots by ``ref_harness.cpp``. It exists only
+  where the reference tree was available at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libp2v_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_p2d.so")
+REFERENCE_TREE = os.environ.get("P2V_REFERENCE_TREE", "/root/reference")
+
+BUMP, GAUSS3 = 0, 1
+
+
+def build(with_reference: bool | None = None) -> None:
+    """Compile the restatement, and the reference module when its source tree is present."""
+    subprocess.run(["make", "-s", "-C", HERE, "restatement"], check=True)
+    if with_reference is None:
+        with_reference = os.path.isdir(os.path.join(REFERENCE_TREE, "plugins", "datatools"))
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_TREE}"], check=True)
+
+
+class _Grid(C.Structure):
+    _fields_ = [("bbox", C.c_float * 6), ("res", C.c_int32 * 3), ("cyclic", C.c_int32 * 3), ("sigma", C.c_float)]
+
+
+class _ConeParams(C.Structure):
+    _fields_ = [
+        ("bounds_min", C.c_float * 3), ("bounds_size", C.c_float * 3),
+        ("offset", C.c_float), ("strength", C.c_float), ("cone_length", C.c_float),
+        ("shortest_edge", C.c_float), ("max_lod", C.c_float),
+        ("steps", C.c_int32), ("early_exit", C.c_int32), ("border", C.c_int32),
+    ]
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build(with_reference=False)
+        _lib = C.CDLL(ORACLE_SO)
+        f = _lib
+        f.p2vo_density_f32.argtypes = [C.c_void_p, C.c_int64, C.POINTER(_Grid), C.c_int, C.c_int, C.c_void_p]
+        f.p2vo_density_f64.argtypes = [C.c_void_p, C.c_int64, C.POINTER(_Grid), C.c_int, C.c_int, C.c_void_p]
+        f.p2vo_normalize_minmax_f32.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_float),
+                                                C.POINTER(C.c_float)]
+        f.p2vo_mip_step_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32)]
+    return _lib
+
+
+def _grid(bbox, res, cyclic, sigma) -> _Grid:
+    g = _Grid()
+    g.bbox[:] = [float(v) for v in bbox]
+    g.res[:] = [int(v) for v in res]
+    g.cyclic[:] = [int(bool(v)) for v in cyclic]
+    g.sigma = float(sigma)
+    return g
+
+
+def _xyzr(xyzr) -> np.ndarray:
+    a = np.ascontiguousarray(xyzr, dtype=np.float32)
+    assert a.ndim == 2 and a.shape[1] == 4
+    return a
+
+
+def density_f32(xyzr, bbox, res, cyclic=(1, 1, 1), sigma=1.0, kernel=BUMP, nthreads=1) -> np.ndarray:
+    """FP32 restatement of createVolumeCPU (raw sums, no normalisation); shape (z, y, x)."""
+    a = _xyzr(xyzr)
+    out = np.zeros((res[2], res[1], res[0]), np.float32)
+    g = _grid(bbox, res, cyclic, sigma)
+    rc = lib().p2vo_density_f32(a.ctypes.data, a.shape[0], C.byref(g), kernel, nthreads, out.ctypes.data)
+    if rc:
+        raise ValueError("invalid grid")
+    return out
+
+
+def density_f64(xyzr, bbox, res, cyclic=(1, 1, 1), sigma=1.0, kernel=BUMP, nthreads=1) -> np.ndarray:
+    """FP64 restatement (the error judge); raw sums, shape (z, y, x)."""
+    a = _xyzr(xyzr)
+    out = np.zeros((res[2], res[1], res[0]), np.float64)
+    g = _grid(bbox, res, cyclic, sigma)
+    rc = lib().p2vo_density_f64(a.ctypes.data, a.shape[0], C.byref(g), kernel, nthreads, out.ctypes.data)
+    if rc:
+        raise ValueError("invalid grid")
+    return out
+
+
+def normalize_minmax_f32(vol: np.ndarray, apply: bool = True):
+    """ParticlesToDensity.cpp:669-682 in float; returns (volume, min, max)."""
+    v = np.ascontiguousarray(vol, dtype=np.float32).copy()
+    mn, mx = C.c_float(), C.c_float()
+    lib().p2vo_normalize_minmax_f32(v.ctypes.data, v.size, int(apply), C.byref(mn), C.byref(mx))
+    return v, mn.value, mx.value
+
+
+def normalize_f64(vol: np.ndarray, mode: str, n_particles: int = 0, spacing=(1.0, 1.0, 1.0)):
+    """FP64 normalisation: 'minmax' as the reference, 'mass' scales so sum(v)*dV equals n_particles."""
+    v = np.asarray(vol, np.float64)
+    if mode == "minmax":
+        mn, mx = v.min(), v.max()
+        return (v - mn) / (mx - mn), mn, mx
+    if mode == "mass":
+        dv = float(spacing[0]) * float(spacing[1]) * float(spacing[2])
+        s = v.sum(dtype=np.float64) * dv
+        out = v * (n_particles / s) if s > 0 else v.copy()
+        return out, out.min(), out.max()
+    return v.copy(), v.min(), v.max()
+
+
+def spacing_f64(bbox, res):
+    """Exact grid spacing of the reference grid, (right-left)/(res-1) per axis."""
+    return tuple(abs(float(bbox[a + 3]) - float(bbox[a])) / (res[a] - 1) for a in range(3))
+
+
+def mip_step_f64(src: np.ndarray) -> np.ndarray:
+    """One MDAO mip level (mdao_mipmap_compute_main.comp.glsl:8-26); arrays shaped (z, y, x)."""
+    s = np.ascontiguousarray(src, np.float64)
+    sd = (C.c_int32 * 3)(s.shape[2], s.shape[1], s.shape[0])
+    dd = (C.c_int32 * 3)(*[max(1, d // 2) for d in (s.shape[2], s.shape[1], s.shape[0])])
+    out = np.zeros((dd[2], dd[1], dd[0]), np.float64)
+    lib().p2vo_mip_step_f64(s.ctypes.data, sd, out.ctypes.data, dd)
+    return out
+
+
+# ------------------------------------------------------------------------------------------------
+# The reference's own module (compiled from the MegaMol tree)
+# ------------------------------------------------------------------------------------------------
+class _RefList(C.Structure):
+    _fields_ = [("vert_type", C.c_int), ("vert", C.c_void_p), ("vert_stride", C.c_uint32),
+                ("global_radius", C.c_float), ("count", C.c_uint64), ("icol", C.c_void_p), ("dir", C.c_void_p)]
+
+
+class _RefParams(C.Structure):
+    _fields_ = [("aggregator", C.c_int), ("sizex", C.c_int), ("sizey", C.c_int), ("sizez", C.c_int),
+                ("cyclX", C.c_int), ("cyclY", C.c_int), ("cyclZ", C.c_int), ("normalize", C.c_int),
+                ("surface", C.c_int), ("sigma", C.c_float)]
+
+
+class _RefResult(C.Structure):
+    _fields_ = [("resolution", C.c_uint64 * 3), ("components", C.c_uint64), ("slice_dists", C.c_float * 3),
+                ("origin", C.c_float * 3), ("extents", C.c_float * 3), ("min_value", C.c_double),
+                ("max_value", C.c_double), ("millis", C.c_double), ("needed_floats", C.c_uint64)]
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not reference_available():
+            raise FileNotFoundError("the reference ParticlesToDensity build (oracle/_ref) is not present")
+        _ref = C.CDLL(REF_SO)
+        _ref.ref_p2d_run.argtypes = [C.POINTER(_RefList), C.c_int, C.POINTER(C.c_float), C.POINTER(_RefParams),
+                                     C.c_void_p, C.c_uint64, C.POINTER(_RefResult)]
+        _ref.ref_p2d_run.restype = C.c_int
+    return _ref
+
+
+def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0, aggregator=0,
+                      surface=False):
+    """Run MegaMol's ParticlesToDensity once.
+
+    ``lists`` is a sequence of dicts with keys ``type`` (VertexDataType), ``data`` (numpy array whose
+    bytes are the vertex records), ``stride`` (bytes, 0 = packed), ``radius`` (global radius), ``count``
+    and optionally ``icol`` / ``dir``. Returns (volume (z,y,x) float32, metadata dict).
+    """
+    keep = []
+    arr = (_RefList * max(1, len(lists)))()
+    for i, L in enumerate(lists):
+        data = np.ascontiguousarray(L["data"])
+        keep.append(data)
+        icol = L.get("icol")
+        dr = L.get("dir")
+        if icol is not None:
+            icol = np.ascontiguousarray(icol, np.float32)
+            keep.append(icol)
+        if dr is not None:
+            dr = np.ascontiguousarray(dr, np.float32)
+            keep.append(dr)
+        arr[i] = _RefList(int(L["type"]), data.ctypes.data, int(L.get("stride", 0)), float(L.get("radius", 0.5)),
+                          int(L["count"]), icol.ctypes.data if icol is not None else None,
+                          dr.ctypes.data if dr is not None else None)
+    prm = _RefParams(int(aggregator), int(res[0]), int(res[1]), int(res[2]), int(bool(cyclic[0])),
+                     int(bool(cyclic[1])), int(bool(cyclic[2])), int(bool(normalize)), int(bool(surface)),
+                     float(sigma))
+    bb = (C.c_float * 6)(*[float(v) for v in bbox])
+    res_out = _RefResult()
+    comps = 3 if aggregator == 2 else 1
+    cap = int(res[0]) * int(res[1]) * int(res[2]) * comps
+    out = np.zeros(cap, np.float32)
+    rc = ref().ref_p2d_run(arr, len(lists), bb, C.byref(prm), out.ctypes.data, cap, C.byref(res_out))
+    if rc == 2:
+        cap = int(res_out.needed_floats)
+        out = np.zeros(cap, np.float32)
+        rc = ref().ref_p2d_run(arr, len(lists), bb, C.byref(prm), out.ctypes.data, cap, C.byref(res_out))
+    if rc != 0:
+        raise RuntimeError(f"reference ParticlesToDensity failed (rc={rc})")
+    r = [int(v) for v in res_out.resolution]
+    comps = int(res_out.components)
+    n = r[0] * r[1] * r[2] * comps
+    vol = out[:n].reshape((r[2], r[1], r[0]) if comps == 1 else (r[2], r[1], r[0], comps))
+    meta = dict(resolution=r, components=comps, slice_dists=list(res_out.slice_dists), origin=list(res_out.origin),
+                extents=list(res_out.extents), min_value=res_out.min_value, max_value=res_out.max_value,
+                millis=res_out.millis)
+    return vol, meta

@@ -1,0 +1,70 @@
+/*
+ * p2v_oracle.h — CPU restatement of MegaMol's particle-to-volume path, used ONLY as the checker.
+ *
+ * TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
+ * this library. The shipped GPU library never calls it.
+ *
+ * Every function restates a cited piece of the reference (paths relative to the MegaMol tree):
+ *  - density: plugins/datatools/src/ParticlesToDensity.cpp:389-747 (createVolumeCPU, bump rbf :472-476)
+ *  - MDAO mip: plugins/moldyn_gl/shaders/moldyn_gl/mdao_volume_generator/mdao_mipmap_compute_main.comp.glsl:8-26
+ *  - cone march: plugins/moldyn_gl/shaders/moldyn_gl/sphere_renderer/inc/mdao_deferred_fragment_ambocc.inc.glsl:9-60
+ *  - cone directions: plugins/moldyn_gl/src/rendering/SphereRenderer.cpp:2572-2587
+ *  - AOSphere deposit: plugins/pwdemos_gl/src/AOSphereRenderer.cpp:918-1021, sampling uniforms :489-514,
+ *    taps shaders/pwdemos_gl/AOSphere/snippets/mainaxes_vertex_2.glsl:1-9,
+ *    mainaxes_fragLightAO_evalAO.glsl:1-8, normals_fragLightAO_evalAO.glsl:1-4
+ *  - MDAO voxeliser: plugins/moldyn_gl/shaders/moldyn_gl/mdao_volume_generator/mdao_volume.geom.glsl:24-93,
+ *    mdao_volume.frag.glsl:9-76
+ *
+ * Parity status: density is pinned bit-exactly against the reference's own compiled
+ * ParticlesToDensity.cpp (see oracle/Makefile, target `ref`). The AO functions restate GLSL that
+ * cannot run here (no graphics stack): their parity is UNPINNED by any reference output.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Grid description shared by the density functions. bbox = {left, bottom, back, right, top, front}. */
+typedef struct {
+    float bbox[6];
+    int32_t res[3];
+    int32_t cyclic[3];
+    float sigma;
+} p2vo_grid;
+
+/* Kernel selector: 0 = reference bump rbf, 1 = Gaussian (sigma*r) cut at 3 sigma. */
+enum { P2VO_BUMP = 0, P2VO_GAUSS3 = 1 };
+
+/* FP32, same operation order as ParticlesToDensity::createVolumeCPU for aggregator 0. With
+ * nthreads == 1 the summation order is the particle order, as the reference with one OpenMP thread.
+ * With nthreads > 1 each thread owns a private grid and the grids are summed serially afterwards,
+ * like the reference (ParticlesToDensity.cpp:401-410,561,623-626). `xyzr` is n float4 records. */
+int p2vo_density_f32(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, float* out);
+
+/* FP64 restatement: the reference's integer decisions (cell, footprint, wrap) made with its float
+ * expressions, every value (node positions, distances, kernel) evaluated in double with the exact
+ * grid spacing (right-left)/(res-1). The GPU path is judged against this. */
+int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, double* out);
+
+/* MDAO 2x2x2 mip step, FP64: dst[i] = sum of the up-to-8 children clamped to the source size, / 8. */
+void p2vo_mip_step_f64(const double* src, const int32_t sdim[3], double* dst, const int32_t ddim[3]);
+
+/* Cone-marched AO per evaluation point (see p2v.h for the parameter meaning). levels[l] points to
+ * level l (dims ldims[3*l..]), FP64. dirs = ncones vec4 (xyz direction around +Y, w = cone width). */
+typedef struct {
+    float bounds_min[3];
+    float bounds_size[3];
+    float offset, strength, cone_length, shortest_edge, max_lod;
+    int32_t steps;      /* 0 = the reference's geometric stepping until cone_length */
+    int32_t early_exit; /* 1 = stop a cone once it exceeds 0.99, as the reference */
+    int32_t border;     /* 0 = CLAMP_TO_BORDER (0), 1 = CLAMP_TO_EDGE */
+} p2vo_cone_params;
+
+void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldims, int nlevels, const float* dirs, int ncones,
+    const p2vo_cone_params* cp, const float* pos, const float* nrm, int64_t n, double* ao);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,99 @@
+"""Generate golden density vectors from MegaMol's own ParticlesToDensity module.
+
+Runs the reference's unmodified plugins/datatools/src/ParticlesToDensity.cpp (compiled by
+``oracle/Makefile`` target ``ref`` into ``oracle/_ref``) on small seeded inputs and stores inputs,
+parameters and the reference output as ``tests/golden/p2d_<case>.npz``. The reference tree exists only
+on the development machine, so the fixtures are committed and the GPU tests read them from here.
+
+Usage:  python tests/golden/make_golden.py        (OMP_NUM_THREADS is forced to 1: the reference's
+        float sums then run in particle order, the order the CPU restatement reproduces bit-exactly)
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+os.environ["OMP_NUM_THREADS"] = "1"
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import numpy as np  # noqa: E402
+
+import oracle  # noqa: E402
+
+VERT_FLOAT_XYZ, VERT_FLOAT_XYZR, VERT_SHORT_XYZ, VERT_DOUBLE_XYZ = 1, 2, 3, 4
+
+
+def _case_uniform(rng, n, edge, r):
+    xyz = rng.uniform(0, edge, size=(n, 3)).astype(np.float32)
+    return [dict(type=VERT_FLOAT_XYZ, data=xyz, stride=0, radius=r, count=n)]
+
+
+def cases():
+    rng = np.random.default_rng(20240601)
+    out = {}
+    # 1. uniform, global radius, cyclic, sigma 1 (the reference defaults except the resolution)
+    out["uniform_cyclic"] = dict(lists=_case_uniform(rng, 6000, 30.0, 0.5), bbox=(0, 0, 0, 30, 30, 30),
+                                 res=(32, 32, 32), cyclic=(1, 1, 1), normalize=False, sigma=1.0)
+    # 2. the same kind of data, non-cyclic, min-max normalised (ParticlesToDensity.cpp:676-682)
+    out["uniform_open_norm"] = dict(lists=_case_uniform(rng, 6000, 30.0, 0.6), bbox=(0, 0, 0, 30, 30, 30),
+                                    res=(32, 24, 28), cyclic=(0, 0, 0), normalize=True, sigma=1.0)
+    # 3. per-particle radii, FLOAT_XYZR with a padded stride, sigma > 1 (footprint truncation)
+    n = 4000
+    rec = np.zeros((n, 5), np.float32)
+    rec[:, :3] = rng.uniform(-5, 25, size=(n, 3))
+    rec[:, 3] = rng.uniform(0.3, 1.4, size=n)
+    rec[:, 4] = 123.0
+    out["xyzr_stride_sigma2"] = dict(lists=[dict(type=VERT_FLOAT_XYZR, data=rec, stride=20, radius=0.0, count=n)],
+                                     bbox=(-5, -5, -5, 25, 25, 25), res=(30, 30, 30), cyclic=(1, 0, 1),
+                                     normalize=False, sigma=2.0)
+    # 4. several lists of different vertex types, particles partly outside the box, sigma < 1
+    xyz_d = rng.uniform(-2, 22, size=(2500, 3)).astype(np.float64)
+    xyz_s = rng.integers(0, 20, size=(1500, 3)).astype(np.uint16)
+    xyz_f = rng.uniform(0, 20, size=(2000, 3)).astype(np.float32)
+    out["multilist_types"] = dict(lists=[
+        dict(type=VERT_DOUBLE_XYZ, data=xyz_d, stride=0, radius=0.7, count=2500),
+        dict(type=VERT_SHORT_XYZ, data=xyz_s, stride=0, radius=0.9, count=1500),
+        dict(type=VERT_FLOAT_XYZ, data=xyz_f, stride=0, radius=0.45, count=2000),
+    ], bbox=(0, 0, 0, 20, 20, 20), res=(25, 21, 23), cyclic=(1, 1, 0), normalize=False, sigma=0.8)
+    # 5. footprint wider than the grid: cyclic wrap visits nodes several times (ParticlesToDensity.cpp:583-603)
+    out["wide_footprint_wrap"] = dict(lists=_case_uniform(rng, 300, 10.0, 3.1), bbox=(0, 0, 0, 10, 10, 10),
+                                      res=(6, 5, 7), cyclic=(1, 1, 1), normalize=False, sigma=1.0)
+    # 6. one particle exactly on a node and one at the box minimum (known-answer test)
+    one = np.array([[5.0, 5.0, 5.0], [0.0, 0.0, 0.0]], np.float32)
+    out["kat_two_particles"] = dict(lists=[dict(type=VERT_FLOAT_XYZ, data=one, stride=0, radius=1.0, count=2)],
+                                    bbox=(0, 0, 0, 10, 10, 10), res=(11, 11, 11), cyclic=(1, 1, 1),
+                                    normalize=False, sigma=1.0)
+    # 7. zero radius particles contribute nothing (ParticlesToDensity.cpp:523-524)
+    rec0 = np.zeros((500, 4), np.float32)
+    rec0[:, :3] = rng.uniform(0, 10, size=(500, 3))
+    rec0[:250, 3] = 0.0
+    rec0[250:, 3] = 0.8
+    out["zero_radius"] = dict(lists=[dict(type=VERT_FLOAT_XYZR, data=rec0, stride=0, radius=0.0, count=500)],
+                              bbox=(0, 0, 0, 10, 10, 10), res=(16, 16, 16), cyclic=(0, 0, 0), normalize=False,
+                              sigma=1.0)
+    return out
+
+
+def main():
+    oracle.build(with_reference=True)
+    for name, c in cases().items():
+        vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"])
+        d = dict(bbox=np.array(c["bbox"], np.float32), res=np.array(c["res"], np.int32),
+                 cyclic=np.array(c["cyclic"], np.int32), normalize=np.int32(c["normalize"]),
+                 sigma=np.float32(c["sigma"]), nlists=np.int32(len(c["lists"])), volume=vol,
+                 min_value=np.float64(meta["min_value"]), max_value=np.float64(meta["max_value"]),
+                 slice_dists=np.array(meta["slice_dists"], np.float32))
+        for i, L in enumerate(c["lists"]):
+            d[f"l{i}_type"] = np.int32(L["type"])
+            d[f"l{i}_data"] = np.ascontiguousarray(L["data"])
+            d[f"l{i}_stride"] = np.int32(L["stride"])
+            d[f"l{i}_radius"] = np.float32(L["radius"])
+            d[f"l{i}_count"] = np.int64(L["count"])
+        path = os.path.join(HERE, f"p2d_{name}.npz")
+        np.savez_compressed(path, **d)
+        print(f"{path}: volume {vol.shape} range [{vol.min():.6g}, {vol.max():.6g}]")
+
+
+if __name__ == "__main__":
+    main()
