@@ -1,0 +1,195 @@
+/*
+ * p2v.h — C ABI of the GB300-native particle-to-volume library (libp2v.so).
+ *
+ * Drop-in boundary for one MegaMol hot path: a MultiParticleDataCall frame in, a VolumetricDataCall
+ * density grid and a per-particle ambient-occlusion (AO) attribute out. The entry points replace:
+ *
+ *   p2v_set_params   <- the ParamSlots of datatools::ParticlesToDensity
+ *                       (plugins/datatools/src/ParticlesToDensity.cpp:59-152) plus the AO parameters of
+ *                       AOSphereRenderer (plugins/pwdemos_gl/src/AOSphereRenderer.cpp:83-124) and of the
+ *                       SphereRenderer MDAO mode (plugins/moldyn_gl/src/rendering/SphereRenderer.cpp:193-214)
+ *   p2v_run_frame    <- ParticlesToDensity::getDataCallback + createVolumeCPU
+ *                       (ParticlesToDensity.cpp:210-383, :389-747) and the AO evaluation of
+ *                       AOSphereRenderer / MDAO (see p2v_params.ao_mode)
+ *   p2v_volume       <- VolumetricMetadata_t + VolumetricDataCall::SetData
+ *                       (plugins/geometry_calls/include/geometry_calls/VolumetricDataCallTypes.h:32-134,
+ *                       VolumetricDataCall.h:285-288)
+ *   p2v_particle_list<- SimpleSphericalParticles vertex / direction / colour data
+ *                       (plugins/geometry_calls/include/geometry_calls/SimpleSphericalParticles.h:27-58,475-589)
+ *
+ * Conventions: every call returns a p2v_status; nothing throws across the boundary. A context is bound
+ * to one device and must be used by one host thread at a time. Output buffers are caller-allocated.
+ * Pointers flagged P2V_MEM_DEVICE are CUDA device pointers on the context's device.
+ */
+#ifndef P2V_H
+#define P2V_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define P2V_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define P2V_API __attribute__((visibility("default")))
+#else
+#define P2V_API
+#endif
+
+typedef enum p2v_status {
+    P2V_OK = 0,
+    P2V_EINVAL = 1,       /* invalid argument or parameter */
+    P2V_ENOMEM = 2,       /* device or host allocation failed */
+    P2V_ECUDA = 3,        /* a CUDA runtime call failed */
+    P2V_ETIMEOUT = 4,     /* a bounded device-side wait gave up (the results of that call are invalid) */
+    P2V_EDOMAIN = 5,      /* input outside the supported domain (see p2v_stats) */
+    P2V_EUNSUPPORTED = 6  /* parameter combination not implemented */
+} p2v_status;
+
+/* SimpleSphericalParticles::VertexDataType (SimpleSphericalParticles.h:27-33) */
+typedef enum p2v_vertex_type {
+    P2V_VERTDATA_NONE = 0,
+    P2V_VERTDATA_FLOAT_XYZ = 1,  /* global radius */
+    P2V_VERTDATA_FLOAT_XYZR = 2,
+    P2V_VERTDATA_SHORT_XYZ = 3,  /* unsigned short components, read as their integer value; global radius */
+    P2V_VERTDATA_DOUBLE_XYZ = 4  /* global radius */
+} p2v_vertex_type;
+
+typedef enum p2v_mem { P2V_MEM_HOST = 0, P2V_MEM_DEVICE = 1 } p2v_mem;
+
+/* Density kernel. BUMP is the reference's rbf exp(-1/(1-(d/eps)^2)), eps = sigma*r, with its
+ * footprint ceil(r/h) (ParticlesToDensity.cpp:472-476,573-575). GAUSS3 is a Gaussian of standard
+ * deviation sigma*r cut at 3 sigma, shifted by its value at the cut so it ends continuously at zero. */
+typedef enum p2v_kernel { P2V_KERNEL_BUMP = 0, P2V_KERNEL_GAUSS3 = 1 } p2v_kernel;
+
+/* AO evaluated per particle at the surface point p + r*n (n = the particle's normal). */
+typedef enum p2v_ao_mode {
+    P2V_AO_NONE = 0,
+    P2V_AO_CONE = 1,            /* cone march through a mip pyramid (MDAO evaluateAmbientOcclusion) */
+    P2V_AO_AOSPHERE_AXES = 2,   /* AOSphereRenderer main-axes mode: 6 taps combined by n^2 */
+    P2V_AO_AOSPHERE_NORMAL = 3, /* AOSphereRenderer normal-based mode: 1 tap along n */
+    P2V_AO_LEARNED = 4          /* MLP stand-in for CONE, cone-march fallback outside its training range */
+} p2v_ao_mode;
+
+/* Volume the cone march samples. */
+typedef enum p2v_ao_volume {
+    P2V_AOVOL_DENSITY = 0, /* the density grid of this call, times ao_volume_scale, saturated to [0,1] */
+    P2V_AOVOL_MDAO = 1     /* MDAO occupancy voxelisation (mdao_volume.geom/frag.glsl) */
+} p2v_ao_volume;
+
+typedef struct p2v_particle_list {
+    int32_t vertex_type;        /* p2v_vertex_type */
+    uint32_t vertex_stride;     /* bytes between records, 0 = packed */
+    const void* vertex_data;
+    uint64_t count;
+    float global_radius;
+    int32_t mem;                /* p2v_mem of vertex_data, normals and ao_out */
+    const float* normals;       /* optional: per-particle normal (DIRDATA_FLOAT_XYZ layout); AO modes need it */
+    uint32_t normal_stride;     /* bytes, 0 = packed (12) */
+    float* ao_out;              /* optional: per-particle AO (COLDATA_FLOAT_I), count floats */
+} p2v_particle_list;
+
+typedef struct p2v_frame {
+    float bbox[6];     /* ObjectSpaceBBox: left, bottom, back, right, top, front */
+    float clipbox[6];  /* ObjectSpaceClipBox (bounds of the AOSphere / MDAO AO volumes) */
+    uint32_t frame_id;
+    uint32_t list_count;
+    const p2v_particle_list* lists;
+} p2v_frame;
+
+typedef struct p2v_volume {
+    float* data;          /* out: resolution product * components floats, x fastest; may be NULL */
+    int32_t mem;          /* p2v_mem of data */
+    uint64_t capacity;    /* floats available at data */
+    /* filled by p2v_run_frame, as ParticlesToDensity::getDataCallback fills VolumetricMetadata_t
+     * (ParticlesToDensity.cpp:249-293) */
+    uint64_t resolution[3];
+    uint64_t components;
+    float slice_dists[3];
+    float origin[3];
+    float extents[3];
+    double min_value, max_value;
+    float bbox[6];        /* bounding box the grid spans (differs from the input with forSurfaceReconstruction) */
+    uint64_t data_hash;   /* bumped on every recomputation, as the module's datahash */
+} p2v_volume;
+
+typedef struct p2v_params {
+    uint32_t struct_size; /* sizeof(p2v_params); set by p2v_params_default */
+    /* --- ParticlesToDensity slots (ParticlesToDensity.cpp:59-152) --- */
+    int32_t aggregator;   /* 0 = PosToSingleCell_Volume (only 0 is implemented) */
+    int32_t sizex, sizey, sizez;
+    int32_t cyclX, cyclY, cyclZ;
+    int32_t normalize;    /* min-max to [0,1] after accumulation (ParticlesToDensity.cpp:676-682) */
+    float sigma;
+    int32_t forSurfaceReconstruction;
+    /* --- extensions --- */
+    int32_t kernel;         /* p2v_kernel */
+    int32_t mass_normalize; /* scale so that sum(grid) * voxel volume == particle count (FP64 sum); before `normalize` */
+    /* --- AO --- */
+    int32_t ao_mode;        /* p2v_ao_mode */
+    int32_t ao_volume;      /* p2v_ao_volume, for P2V_AO_CONE / P2V_AO_LEARNED */
+    float ao_volume_scale;  /* density -> occlusion scale for P2V_AOVOL_DENSITY */
+    int32_t ao_cones;       /* 3 = the MDAO direction set (SphereRenderer.cpp:2572-2587) */
+    int32_t ao_steps;       /* 0 = MDAO geometric stepping t += t*w until cone_length; >0 = that many samples */
+    int32_t ao_levels;      /* mip levels sampled (level 0 = the volume) */
+    float ao_apex_deg;      /* "ambient occlusion::apex" (50) */
+    float ao_offset;        /* "ambient occlusion::offset" (0.01) */
+    float ao_strength;      /* "ambient occlusion::strength" (1) */
+    float ao_cone_length;   /* "ambient occlusion::coneLength" (0.8), normalised volume coordinates */
+    int32_t ao_early_exit;  /* stop a cone at 0.99 occlusion, as the reference (1) */
+    int32_t mdao_volume_size; /* "ambient occlusion::volumeSize" (128): voxels along the longest edge */
+    int32_t mdao_unorm8;    /* store the MDAO volume and its mips as 8-bit UNORM like the reference's R8 */
+    /* AOSphereRenderer (AOSphereRenderer.cpp:83-124) */
+    int32_t aos_sizex, aos_sizey, aos_sizez; /* "vol::sizex/y/z" (32) including the 1-voxel border */
+    float aos_step_len;     /* "ao::stepLen" (0.5) */
+    float aos_gen_fac;      /* "vol::genFac" (1) */
+    float aos_eval_fac;     /* "ao::evalFac" (1) */
+    /* --- execution --- */
+    int32_t tile_x, tile_y, tile_z; /* density tile; 0 = chosen by the library */
+} p2v_params;
+
+typedef struct p2v_stats {
+    uint64_t particles_in;       /* records presented */
+    uint64_t particles_binned;   /* records that can contribute */
+    uint64_t particles_dropped;  /* NaN/Inf coordinates or radius, radius <= 0, or farther than 2^30 cells */
+    float radius_max;
+    int32_t cell_min[3], cell_max[3]; /* occupied cell range (floor((p-min)/h)) */
+    double mass_sum;             /* FP64 sum of the raw grid */
+    double ms_upload, ms_binning, ms_density, ms_normalize, ms_ao, ms_download, ms_total; /* CUDA events */
+    uint32_t device_error;       /* nonzero: a bounded device wait gave up (status P2V_ETIMEOUT) */
+    uint32_t ao_fallback;        /* learned AO: particles that fell back to the cone march */
+} p2v_stats;
+
+typedef struct p2v_ctx p2v_ctx;
+
+P2V_API int p2v_abi_version(void);
+P2V_API void p2v_params_default(p2v_params* p);
+
+P2V_API p2v_status p2v_create(p2v_ctx** ctx, int device);
+P2V_API void p2v_destroy(p2v_ctx* ctx);
+
+P2V_API p2v_status p2v_set_params(p2v_ctx* ctx, const p2v_params* p);
+/* Current parameters; forSurfaceReconstruction rewrites sizex/sizey as the reference module does. */
+P2V_API p2v_status p2v_get_params(const p2v_ctx* ctx, p2v_params* p);
+
+/* Compute the density grid (and AO when ao_mode != NONE) of one frame. Synchronous on `stream`
+ * (a cudaStream_t, NULL = the context's stream): on return `vol` is filled and every host output is
+ * written. Mirrors ParticlesToDensity::getDataCallback for IDX_GET_DATA. */
+P2V_API p2v_status p2v_run_frame(p2v_ctx* ctx, const p2v_frame* frame, p2v_volume* vol, void* stream);
+
+/* Device pointer of the last density grid (valid until the next call on this context); the reference's
+ * VolumetricDataCall cannot carry one, so this is an addition of this library. */
+P2V_API p2v_status p2v_get_device_volume(p2v_ctx* ctx, const float** dptr, uint64_t resolution[3]);
+
+P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
+/* Last error message of this context ("" if none); returns the message length. */
+P2V_API size_t p2v_get_last_error(const p2v_ctx* ctx, char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* P2V_H */

@@ -1,0 +1,471 @@
+// Cell binning: typed particle lists -> float4 xyzr records + cell keys, a stable LSD radix sort
+// (onesweep: one read and one write of the keys per 8-bit digit, decoupled look-back across tiles),
+// and the per-cell start table of the sorted order.
+//
+// Reference semantics (plugins/datatools/src/ParticlesToDensity.cpp):
+//   - particle components are read through SimpleSphericalParticles' accessors, i.e. converted to
+//     float with static_cast (SimpleSphericalParticles.h:86-130, Accessor.h:33-117); FLOAT_XYZ,
+//     DOUBLE_XYZ and SHORT_XYZ lists use the list's global radius (ParticlesToDensity.cpp:460-463,569-571)
+//   - the cell of a particle is (p - min) / sliceDist in float (:564-568).
+// The bin used for sorting is floor() of that quotient clamped to [-1, res] (one underflow and one
+// overflow bin per axis collect everything outside the box); the footprint decisions later use the
+// reference's truncation of the same quotient.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "p2v_common.cuh"
+#include "p2v_internal.h"
+
+namespace p2v {
+
+namespace {
+
+template<class T>
+__device__ __forceinline__ T load_unaligned(const uint8_t* p) {
+    T v;
+    uint8_t* d = reinterpret_cast<uint8_t*>(&v);
+#pragma unroll
+    for (int i = 0; i < (int) sizeof(T); ++i)
+        d[i] = p[i];
+    return v;
+}
+
+template<class T, bool ALIGNED>
+__device__ __forceinline__ float load_comp(const uint8_t* p) {
+    if (ALIGNED)
+        return static_cast<float>(*reinterpret_cast<const T*>(p));
+    return static_cast<float>(load_unaligned<T>(p));
+}
+
+__device__ __forceinline__ int32_t clamp_cell(float q) {
+    // floor of the cell quotient, clamped to +-2^30 so it always fits an int
+    float f = floorf(q);
+    f = fminf(fmaxf(f, -1073741824.0f), 1073741824.0f);
+    return static_cast<int32_t>(f);
+}
+
+__device__ __forceinline__ uint32_t lane_id() {
+    return threadIdx.x & 31u;
+}
+
+template<class T, int NC, bool ALIGNED>
+__global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, float4* __restrict__ xyzr,
+    uint32_t* __restrict__ keys, uint32_t* __restrict__ idx, FrameScalars* __restrict__ fs) {
+    __shared__ int32_t s_cmin[3][8], s_cmax[3][8];
+    __shared__ uint32_t s_rmax[8], s_drop[8];
+    const uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+    bool valid = false;
+    float r = 0.0f;
+    int32_t cell[3] = {INT32_MAX, INT32_MAX, INT32_MAX};
+    int32_t cellhi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    bool present = i < L.count;
+    if (present) {
+        const uint8_t* rec = L.data + i * L.stride;
+        float x = load_comp<T, ALIGNED>(rec);
+        float y = load_comp<T, ALIGNED>(rec + sizeof(T));
+        float z = load_comp<T, ALIGNED>(rec + 2 * sizeof(T));
+        r = NC == 4 ? load_comp<T, ALIGNED>(rec + 3 * sizeof(T)) : L.global_radius;
+        float p[3] = {x, y, z};
+        valid = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(r) && r > 0.0f;
+        uint32_t bin[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float q = (p[a] - g.minf[a]) / g.hf[a];
+            valid = valid && fabsf(q) < 1073741824.0f;
+            int32_t c = clamp_cell(q);
+            cell[a] = c;
+            int32_t b = c < -1 ? -1 : (c > g.s[a] ? g.s[a] : c);
+            bin[a] = static_cast<uint32_t>(b + 1);
+        }
+        uint32_t key = g.nbins;
+        if (valid)
+            key = (bin[2] * g.nb[1] + bin[1]) * g.nb[0] + bin[0];
+        const uint64_t o = L.offset + i;
+        xyzr[o] = make_float4(x, y, z, r);
+        keys[o] = key;
+        idx[o] = static_cast<uint32_t>(o);
+        if (valid) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                cellhi[a] = cell[a];
+        } else {
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                cell[a] = INT32_MAX;
+        }
+    }
+    // block reduction: one atomic per block and quantity
+    uint32_t rbits = valid ? __float_as_uint(r) : 0u;
+    uint32_t drop = (present && !valid) ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rbits = max(rbits, __shfl_xor_sync(0xffffffffu, rbits, o));
+        drop += __shfl_xor_sync(0xffffffffu, drop, o);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            cell[a] = min(cell[a], __shfl_xor_sync(0xffffffffu, cell[a], o));
+            cellhi[a] = max(cellhi[a], __shfl_xor_sync(0xffffffffu, cellhi[a], o));
+        }
+    }
+    const int w = threadIdx.x >> 5;
+    if (lane_id() == 0) {
+        s_rmax[w] = rbits;
+        s_drop[w] = drop;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s_cmin[a][w] = cell[a];
+            s_cmax[a][w] = cellhi[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int k = 1; k < nw; ++k) {
+            s_rmax[0] = max(s_rmax[0], s_rmax[k]);
+            s_drop[0] += s_drop[k];
+            for (int a = 0; a < 3; ++a) {
+                s_cmin[a][0] = min(s_cmin[a][0], s_cmin[a][k]);
+                s_cmax[a][0] = max(s_cmax[a][0], s_cmax[a][k]);
+            }
+        }
+        if (s_rmax[0])
+            atomicMax(&fs->rmax_bits, s_rmax[0]);
+        if (s_drop[0])
+            atomicAdd(&fs->n_dropped, s_drop[0]);
+        for (int a = 0; a < 3; ++a) {
+            if (s_cmin[a][0] != INT32_MAX)
+                atomicMin(&fs->cmin[a], s_cmin[a][0]);
+            if (s_cmax[a][0] != INT32_MIN)
+                atomicMax(&fs->cmax[a], s_cmax[a][0]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Onesweep LSD radix sort of (key, value) pairs, 8-bit digits.
+// ---------------------------------------------------------------------------------------------
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int SORT_ITEMS = 16;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 4096 keys per tile
+constexpr int RADIX = 256;
+constexpr uint32_t FLAG_AGG = 1u << 30;
+constexpr uint32_t FLAG_PRE = 2u << 30;
+constexpr uint32_t FLAG_MASK = 3u << 30;
+constexpr uint32_t COUNT_MASK = (1u << 30) - 1u;
+
+__global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n, int passes,
+    uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[4 * RADIX];
+    for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x)
+        sh[i] = 0;
+    __syncthreads();
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[j];
+        for (int p = 0; p < passes; ++p)
+            atomicAdd(&sh[p * RADIX + ((k >> (8 * p)) & 0xFFu)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x)
+        if (sh[i])
+            atomicAdd(&hist[i], sh[i]);
+}
+
+// Exclusive scan of each pass' digit histogram (one block of 256 threads).
+__global__ void radix_scan_kernel(uint32_t* hist, int passes) {
+    __shared__ uint32_t s[RADIX];
+    for (int p = 0; p < passes; ++p) {
+        uint32_t v = hist[p * RADIX + threadIdx.x];
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < RADIX; o <<= 1) {
+            uint32_t t = threadIdx.x >= (unsigned) o ? s[threadIdx.x - o] : 0u;
+            __syncthreads();
+            s[threadIdx.x] += t;
+            __syncthreads();
+        }
+        hist[p * RADIX + threadIdx.x] = s[threadIdx.x] - v;
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
+    return *reinterpret_cast<const volatile uint32_t*>(p);
+}
+
+__device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) {
+    *reinterpret_cast<volatile uint32_t*>(p) = v;
+}
+
+template<bool GATHER>
+__global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* __restrict__ keys_in,
+    const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
+    int shift, const uint32_t* __restrict__ digit_offsets, uint32_t* __restrict__ tile_counter,
+    uint32_t* __restrict__ status, uint32_t* __restrict__ err, const float4* __restrict__ xyzr_in,
+    float4* __restrict__ xyzr_out) {
+    __shared__ uint32_t s_keys[SORT_TILE];
+    __shared__ uint32_t s_vals[SORT_TILE];
+    __shared__ uint32_t s_whist[SORT_WARPS][RADIX];
+    __shared__ uint32_t s_base[RADIX];   // global destination of this tile's first item of each digit
+    __shared__ uint32_t s_local[RADIX];  // tile-local exclusive offset of each digit
+    __shared__ uint32_t s_scan[SORT_WARPS];
+    __shared__ uint32_t s_tile;
+
+    const int tid = threadIdx.x;
+    const int w = tid >> 5;
+    const uint32_t lane = lane_id();
+    if (tid == 0)
+        s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS)
+        (&s_whist[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * SORT_TILE;
+
+    // warp-striped load: item i of lane l of warp w is element base + w*32*ITEMS + i*32 + l, so the
+    // ranking order (i, lane) is the input order within the warp and warps follow each other.
+    uint32_t k[SORT_ITEMS], v[SORT_ITEMS], rk[SORT_ITEMS];
+    const uint32_t wbase = base + w * 32 * SORT_ITEMS;
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        k[i] = j < n ? keys_in[j] : 0u;
+        v[i] = j < n ? vals_in[j] : 0u;
+    }
+    const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        const bool valid = j < n;
+        const uint32_t d = (k[i] >> shift) & 0xFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : (RADIX + lane));
+        const uint32_t cnt = __popc(peers);
+        const uint32_t before = __popc(peers & lt_mask);
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t b = valid ? s_whist[w][d] : 0u;
+        __syncwarp();
+        if (valid && lane == leader)
+            s_whist[w][d] = b + cnt;
+        __syncwarp();
+        rk[i] = b + before;
+    }
+    __syncthreads();
+
+    // per digit: exclusive offsets over warps, and the tile count
+    const uint32_t d = tid;  // SORT_THREADS == RADIX
+    uint32_t run = 0;
+#pragma unroll
+    for (int ww = 0; ww < SORT_WARPS; ++ww) {
+        uint32_t c = s_whist[ww][d];
+        s_whist[ww][d] = run;
+        run += c;
+    }
+    const uint32_t count = run;
+    // publish the tile aggregate (or the inclusive prefix for tile 0) before looking back
+    uint32_t* my = status + (size_t) tile * RADIX + d;
+    if (tile == 0)
+        st_volatile(my, FLAG_PRE | count);
+    else
+        st_volatile(my, FLAG_AGG | count);
+    // tile-local exclusive scan over digits (block scan of `count`)
+    uint32_t incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t) o)
+            incl += t;
+    }
+    if (lane == 31)
+        s_scan[w] = incl;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int ww = 0; ww < w; ++ww)
+        wpre += s_scan[ww];
+    s_local[d] = wpre + incl - count;
+
+    // decoupled look-back for digit d
+    uint32_t excl = 0;
+    if (tile > 0) {
+        int32_t t = (int32_t) tile - 1;
+        uint32_t spins = 0;
+        while (t >= 0) {
+            uint32_t s = ld_volatile(status + (size_t) t * RADIX + d);
+            if ((s & FLAG_MASK) == 0u) {
+                if (++spins > SPIN_LIMIT) {
+                    atomicOr(err, ERR_LOOKBACK_TIMEOUT);
+                    break;
+                }
+                continue;
+            }
+            excl += s & COUNT_MASK;
+            if ((s & FLAG_MASK) == FLAG_PRE)
+                break;
+            --t;
+        }
+        st_volatile(my, FLAG_PRE | (excl + count));
+    }
+    s_base[d] = digit_offsets[d] + excl;
+    __syncthreads();
+
+    // stage the tile in digit order, then write runs of equal digits contiguously
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        if (j < n) {
+            const uint32_t dd = (k[i] >> shift) & 0xFFu;
+            const uint32_t lp = s_local[dd] + s_whist[w][dd] + rk[i];
+            s_keys[lp] = k[i];
+            s_vals[lp] = v[i];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = n - base < (uint32_t) SORT_TILE ? n - base : (uint32_t) SORT_TILE;
+    for (uint32_t j = tid; j < tile_n; j += SORT_THREADS) {
+        const uint32_t kk = s_keys[j];
+        const uint32_t dd = (kk >> shift) & 0xFFu;
+        const uint32_t dst = s_base[dd] + (j - s_local[dd]);
+        keys_out[dst] = kk;
+        const uint32_t vv = s_vals[j];
+        vals_out[dst] = vv;
+        if (GATHER)
+            xyzr_out[dst] = xyzr_in[vv];
+    }
+}
+
+// start[c] = first sorted position whose key is >= c, for c in [0, nbins]. Short gaps are filled by
+// the thread that sees them; gaps of 64 cells or more are queued for a block-wide fill.
+__global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t nbins,
+    uint32_t* __restrict__ start, uint4* __restrict__ gaps, uint32_t gap_cap, FrameScalars* __restrict__ fs) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+        const uint32_t lo = i == 0 ? 0u : keys[i - 1] + 1u;
+        uint32_t hi = i == n ? nbins : keys[i];
+        if (hi > nbins)
+            hi = nbins;
+        if (lo > hi)
+            continue;
+        if (hi - lo < 64u) {
+            for (uint32_t c = lo; c <= hi; ++c)
+                start[c] = i;
+        } else {
+            const uint32_t slot = atomicAdd(&fs->ngaps, 1u);
+            if (slot < gap_cap)
+                gaps[slot] = make_uint4(lo, hi, i, 0u);
+            else
+                atomicOr(&fs->error, ERR_GAP_OVERFLOW);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) cell_gap_fill_kernel(const uint4* __restrict__ gaps, uint32_t gap_cap,
+    uint32_t* __restrict__ start, const FrameScalars* __restrict__ fs) {
+    const uint32_t ng = min(fs->ngaps, gap_cap);
+    for (uint32_t g = blockIdx.x; g < ng; g += gridDim.x) {
+        const uint4 e = gaps[g];
+        for (uint32_t c = e.x + threadIdx.x; c <= e.y; c += blockDim.x)
+            start[c] = e.z;
+    }
+}
+
+__global__ void count_valid_kernel(const uint32_t* __restrict__ start, uint32_t nbins, FrameScalars* fs) {
+    fs->n_valid = start[nbins];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------------------------
+cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,
+    FrameScalars* fs, cudaStream_t st) {
+    if (L.count == 0)
+        return cudaSuccess;
+    const dim3 block(256);
+    const dim3 grid((unsigned) ((L.count + 255) / 256));
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(L.data);
+    switch (L.type) {
+    case 1: {  // FLOAT_XYZ
+        bool al = (addr % 4 == 0) && (L.stride % 4 == 0);
+        if (al)
+            pack_keys_kernel<float, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+        else
+            pack_keys_kernel<float, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+    } break;
+    case 2: {  // FLOAT_XYZR
+        bool al = (addr % 4 == 0) && (L.stride % 4 == 0);
+        if (al)
+            pack_keys_kernel<float, 4, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+        else
+            pack_keys_kernel<float, 4, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+    } break;
+    case 3: {  // SHORT_XYZ
+        bool al = (addr % 2 == 0) && (L.stride % 2 == 0);
+        if (al)
+            pack_keys_kernel<uint16_t, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+        else
+            pack_keys_kernel<uint16_t, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+    } break;
+    case 4: {  // DOUBLE_XYZ
+        bool al = (addr % 8 == 0) && (L.stride % 8 == 0);
+        if (al)
+            pack_keys_kernel<double, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+        else
+            pack_keys_kernel<double, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+    } break;
+    default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+size_t sort_status_words(uint32_t n) {
+    return (size_t) ceil_div(n, SORT_TILE) * RADIX;
+}
+
+int sort_passes(uint32_t max_key) {
+    int bits = 0;
+    while (bits < 32 && (max_key >> bits) != 0u)
+        ++bits;
+    return bits == 0 ? 1 : (bits + 7) / 8;
+}
+
+cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st) {
+    const int passes = sort_passes(max_key);
+    const uint32_t tiles = ceil_div(n, SORT_TILE);
+    cudaError_t e = cudaMemsetAsync(b.hist, 0, sizeof(uint32_t) * (4 * RADIX + 8), st);
+    if (e != cudaSuccess)
+        return e;
+    if (n == 0)
+        return cudaSuccess;
+    const unsigned hgrid = (unsigned) std::min<uint32_t>(ceil_div(n, 256 * 8), (uint32_t) sms * 4);
+    radix_hist_kernel<<<hgrid ? hgrid : 1, 256, 0, st>>>(b.keys[0], n, passes, b.hist);
+    radix_scan_kernel<<<1, RADIX, 0, st>>>(b.hist, passes);
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        e = cudaMemsetAsync(b.status, 0, sizeof(uint32_t) * (size_t) tiles * RADIX, st);
+        if (e != cudaSuccess)
+            return e;
+        uint32_t* counter = b.hist + 4 * RADIX + p;
+        const bool last = p == passes - 1;
+        if (last && b.xyzr_in != nullptr)
+            onesweep_kernel<true><<<tiles, SORT_THREADS, 0, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
+                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, b.xyzr_in, b.xyzr_out);
+        else
+            onesweep_kernel<false><<<tiles, SORT_THREADS, 0, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
+                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, nullptr, nullptr);
+        cur ^= 1;
+    }
+    b.result = cur;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_start(const uint32_t* keys, uint32_t n, uint32_t nbins, uint32_t* start, uint4* gaps,
+    uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st) {
+    const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n + 1, 256), sms * 8));
+    cell_start_kernel<<<grid, 256, 0, st>>>(keys, n, nbins, start, gaps, gap_cap, fs);
+    cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs);
+    count_valid_kernel<<<1, 1, 0, st>>>(start, nbins, fs);
+    return cudaGetLastError();
+}
+
+}  // namespace p2v

@@ -1,0 +1,494 @@
+// C ABI of libp2v: context, parameters and the per-frame pipeline
+// (pack + cell keys -> radix sort -> cell starts -> density gather -> statistics -> normalisation).
+//
+// Host-side semantics follow datatools::ParticlesToDensity (plugins/datatools/src/ParticlesToDensity.cpp):
+// parameter defaults (:59-152), the surface-reconstruction box adjustment modifyBBox (:749-799), the
+// grid geometry (:420-432) and the metadata it publishes (:249-293).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/p2v.h"
+#include "p2v_common.cuh"
+#include "p2v_internal.h"
+
+using namespace p2v;
+
+namespace {
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes)
+            return cudaSuccess;
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t cap = need + need / 4 + 256;
+        cudaError_t e = cudaMalloc(&ptr, cap);
+        if (e == cudaSuccess)
+            bytes = cap;
+        return e;
+    }
+    void release() {
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template<class T>
+    T* as() const {
+        return reinterpret_cast<T*>(ptr);
+    }
+};
+
+enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_COUNT };
+
+}  // namespace
+
+struct p2v_ctx {
+    int device = 0;
+    int sms = 152;
+    cudaStream_t own_stream = nullptr;
+    p2v_params prm{};
+    std::string err;
+    p2v_stats stats{};
+    uint64_t datahash = 0;
+
+    DevBuf raw, xyzr, xyzr_sorted, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
+    FrameScalars* h_scal = nullptr;  // pinned mirror
+    cudaEvent_t ev[EV_COUNT] = {};
+    const float* last_grid = nullptr;
+    uint64_t last_res[3] = {0, 0, 0};
+
+    p2v_status fail(p2v_status s, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return s;
+    }
+
+    p2v_status run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st);
+};
+
+namespace {
+
+// ParticlesToDensity::modifyBBox (ParticlesToDensity.cpp:749-799), in the same float arithmetic:
+// grow the box by 10% plus two voxels in z, make voxels cubic and rewrite sizex / sizey.
+void modify_bbox(float bb[6], int32_t& sx, int32_t& sy, int32_t sz) {
+    float rangeOSx = std::fabs(bb[3] - bb[0]), rangeOSy = std::fabs(bb[4] - bb[1]), rangeOSz = std::fabs(bb[5] - bb[2]);
+    float general_box_scaling = 1.1f;
+    float spacing = (rangeOSz * general_box_scaling) / sz;
+    float newDepth = (rangeOSz * general_box_scaling) + 2 * spacing;
+    spacing = newDepth / sz;
+    float newWidth = (rangeOSx * general_box_scaling) + 2 * spacing;
+    int resolutionX = static_cast<int>(newWidth / spacing);
+    float rest = newWidth / spacing - static_cast<float>(resolutionX);
+    newWidth += (1 - rest) * spacing;
+    resolutionX += 1;
+    sx = resolutionX;
+    float newHeight = (rangeOSy * general_box_scaling) + 2 * spacing;
+    int resolutionY = static_cast<int>(newHeight / spacing);
+    rest = newHeight / spacing - static_cast<float>(resolutionY);
+    newHeight += (1 - rest) * spacing;
+    resolutionY += 1;
+    sy = resolutionY;
+    float minOSx = bb[0], minOSy = bb[1], minOSz = bb[2], maxOSx = bb[3], maxOSy = bb[4], maxOSz = bb[5];
+    bb[0] = minOSx - (newWidth - rangeOSx) / 2;
+    bb[1] = minOSy - (newHeight - rangeOSy) / 2;
+    bb[2] = minOSz - (newDepth - rangeOSz) / 2;
+    bb[3] = maxOSx + (newWidth - rangeOSx) / 2;
+    bb[4] = maxOSy + (newHeight - rangeOSy) / 2;
+    bb[5] = maxOSz + (newDepth - rangeOSz) / 2;
+}
+
+uint32_t record_bytes(int type) {
+    switch (type) {
+    case P2V_VERTDATA_FLOAT_XYZ: return 12;
+    case P2V_VERTDATA_FLOAT_XYZR: return 16;
+    case P2V_VERTDATA_SHORT_XYZ: return 6;
+    case P2V_VERTDATA_DOUBLE_XYZ: return 24;
+    default: return 0;
+    }
+}
+
+}  // namespace
+
+p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st) {
+    P2V_CUDA_TRY(cudaSetDevice(device));
+    const p2v_params& P = prm;
+    if (P.aggregator != 0)
+        return fail(P2V_EUNSUPPORTED, "aggregator %d is not implemented (only PosToSingleCell_Volume)", P.aggregator);
+    if (!(P.sigma > 0.0f) || !std::isfinite(P.sigma))
+        return fail(P2V_EINVAL, "sigma must be a positive finite number");
+    if (P.kernel != P2V_KERNEL_BUMP && P.kernel != P2V_KERNEL_GAUSS3)
+        return fail(P2V_EINVAL, "unknown kernel %d", P.kernel);
+    if (fr->list_count > 0 && fr->lists == nullptr)
+        return fail(P2V_EINVAL, "frame has lists but no list array");
+
+    float bb[6];
+    std::memcpy(bb, fr->bbox, sizeof(bb));
+    int32_t res[3] = {P.sizex, P.sizey, P.sizez};
+    if (P.forSurfaceReconstruction) {
+        modify_bbox(bb, res[0], res[1], res[2]);
+        prm.sizex = res[0];
+        prm.sizey = res[1];
+    }
+    GridGeo g{};
+    uint64_t nb = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (res[a] < 2 || res[a] > 4096)
+            return fail(P2V_EINVAL, "size%c = %d: every resolution must lie in [2, 4096]", "xyz"[a], res[a]);
+        if (!std::isfinite(bb[a]) || !std::isfinite(bb[a + 3]))
+            return fail(P2V_EINVAL, "bounding box is not finite");
+        g.s[a] = res[a];
+        g.cyc[a] = (a == 0 ? P.cyclX : a == 1 ? P.cyclY : P.cyclZ) ? 1 : 0;
+        const float lo = bb[a], hi = bb[a + 3];
+        const float rangef = hi > lo ? hi - lo : lo - hi;  // vislib Cuboid::Width()
+        if (!(rangef > 0.0f))
+            return fail(P2V_EINVAL, "bounding box has zero extent along %c", "xyz"[a]);
+        g.minf[a] = lo;
+        g.hf[a] = rangef / static_cast<float>(res[a] - 1);
+        const double hd = std::fabs((double) hi - (double) lo) / (double) (res[a] - 1);
+        g.hhi[a] = (float) hd;
+        g.hlo[a] = (float) (hd - (double) g.hhi[a]);
+        g.nb[a] = (uint32_t) res[a] + 2u;
+        nb *= g.nb[a];
+    }
+    if (nb >= 0xFFFFFFF0ull)
+        return fail(P2V_EINVAL, "grid too large for 32-bit cell keys");
+    g.nbins = (uint32_t) nb;
+    g.sigma = P.sigma;
+    g.kernel = P.kernel;
+    const uint64_t V = (uint64_t) res[0] * res[1] * res[2];
+
+    uint64_t N = 0;
+    for (uint32_t l = 0; l < fr->list_count; ++l) {
+        const p2v_particle_list& L = fr->lists[l];
+        if (L.vertex_type == P2V_VERTDATA_NONE)
+            continue;
+        if (record_bytes(L.vertex_type) == 0)
+            return fail(P2V_EINVAL, "list %u: unknown vertex type %d", l, L.vertex_type);
+        if (L.count > 0 && L.vertex_data == nullptr)
+            return fail(P2V_EINVAL, "list %u: no vertex data", l);
+        N += L.count;
+    }
+    if (N >= (1ull << 30))
+        return fail(P2V_EINVAL, "%llu particles: at most 2^30 - 1 per frame", (unsigned long long) N);
+
+    // ---- buffers ----
+    const uint32_t n = (uint32_t) N;
+    const GatherConfig gc{8, 16, 16, 2048, 1024};
+    const uint32_t ntiles = gather_tile_count(gc, g);
+    const uint32_t gap_cap = g.nbins / 64 + 2;
+    P2V_CUDA_TRY(xyzr.ensure(sizeof(float4) * (N + 1)));
+    P2V_CUDA_TRY(xyzr_sorted.ensure(sizeof(float4) * (N + 1)));
+    P2V_CUDA_TRY(keys0.ensure(4 * (N + 1)));
+    P2V_CUDA_TRY(keys1.ensure(4 * (N + 1)));
+    P2V_CUDA_TRY(vals0.ensure(4 * (N + 1)));
+    P2V_CUDA_TRY(vals1.ensure(4 * (N + 1)));
+    P2V_CUDA_TRY(status.ensure(4 * (sort_status_words(n) + 256)));
+    P2V_CUDA_TRY(hist.ensure(4 * (4 * 256 + 8)));
+    P2V_CUDA_TRY(cstart.ensure(4 * ((size_t) g.nbins + 1)));
+    P2V_CUDA_TRY(gaps.ensure(sizeof(uint4) * gap_cap));
+    P2V_CUDA_TRY(tiles.ensure(sizeof(TileStats) * ntiles));
+    P2V_CUDA_TRY(scal.ensure(sizeof(FrameScalars)));
+    float* dgrid;
+    const bool direct = vol && vol->data && vol->mem == P2V_MEM_DEVICE && vol->capacity >= V;
+    if (direct) {
+        dgrid = vol->data;
+    } else {
+        P2V_CUDA_TRY(grid.ensure(sizeof(float) * V));
+        dgrid = grid.as<float>();
+    }
+    if (vol && vol->data && vol->capacity < V)
+        return fail(P2V_EINVAL, "output capacity %llu < %llu floats", (unsigned long long) vol->capacity,
+                    (unsigned long long) V);
+
+    FrameScalars init{};
+    for (int a = 0; a < 3; ++a) {
+        init.cmin[a] = INT32_MAX;
+        init.cmax[a] = INT32_MIN;
+    }
+    *h_scal = init;
+    FrameScalars* fs = scal.as<FrameScalars>();
+    P2V_CUDA_TRY(cudaEventRecord(ev[EV_START], st));
+    P2V_CUDA_TRY(cudaMemcpyAsync(fs, h_scal, sizeof(FrameScalars), cudaMemcpyHostToDevice, st));
+
+    // ---- upload + pack + keys ----
+    uint64_t raw_need = 0;
+    for (uint32_t l = 0; l < fr->list_count; ++l) {
+        const p2v_particle_list& L = fr->lists[l];
+        if (L.vertex_type == P2V_VERTDATA_NONE || L.count == 0 || L.mem == P2V_MEM_DEVICE)
+            continue;
+        const uint32_t stride = L.vertex_stride ? L.vertex_stride : record_bytes(L.vertex_type);
+        raw_need += (L.count - 1) * (uint64_t) stride + record_bytes(L.vertex_type) + 16;
+    }
+    if (raw_need)
+        P2V_CUDA_TRY(raw.ensure(raw_need));
+    uint64_t raw_off = 0, off = 0;
+    for (uint32_t l = 0; l < fr->list_count; ++l) {
+        const p2v_particle_list& L = fr->lists[l];
+        if (L.vertex_type == P2V_VERTDATA_NONE)
+            continue;
+        const uint32_t rb = record_bytes(L.vertex_type);
+        const uint32_t stride = L.vertex_stride ? L.vertex_stride : rb;
+        if (stride < rb)
+            return fail(P2V_EINVAL, "list %u: stride %u shorter than a record (%u)", l, stride, rb);
+        ListDesc d{};
+        d.stride = stride;
+        d.type = L.vertex_type;
+        d.global_radius = L.global_radius;
+        d.count = L.count;
+        d.offset = off;
+        if (L.count > 0) {
+            if (L.mem == P2V_MEM_DEVICE) {
+                d.data = static_cast<const uint8_t*>(L.vertex_data);
+            } else {
+                const uint64_t bytes = (L.count - 1) * (uint64_t) stride + rb;
+                uint8_t* dst = raw.as<uint8_t>() + raw_off;
+                P2V_CUDA_TRY(cudaMemcpyAsync(dst, L.vertex_data, bytes, cudaMemcpyHostToDevice, st));
+                d.data = dst;
+                raw_off += (bytes + 15) & ~uint64_t(15);
+            }
+        }
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
+        P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), vals0.as<uint32_t>(), fs, st));
+        off += L.count;
+    }
+    if (N == 0)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
+
+    // ---- sort + cell starts ----
+    SortBuffers sb{};
+    sb.keys[0] = keys0.as<uint32_t>();
+    sb.keys[1] = keys1.as<uint32_t>();
+    sb.vals[0] = vals0.as<uint32_t>();
+    sb.vals[1] = vals1.as<uint32_t>();
+    sb.hist = hist.as<uint32_t>();
+    sb.status = status.as<uint32_t>();
+    sb.err = &fs->error;
+    sb.xyzr_in = xyzr.as<float4>();
+    sb.xyzr_out = xyzr_sorted.as<float4>();
+    P2V_CUDA_TRY(launch_sort(sb, n, g.nbins, sms, st));
+    const uint32_t* skeys = sb.keys[sb.result];
+    P2V_CUDA_TRY(launch_cell_start(skeys, n, g.nbins, cstart.as<uint32_t>(), gaps.as<uint4>(), gap_cap, fs, sms, st));
+    P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
+
+    // ---- density ----
+    P2V_CUDA_TRY(launch_gather(gc, g, xyzr_sorted.as<float4>(), cstart.as<uint32_t>(), dgrid, tiles.as<TileStats>(), fs, st));
+    P2V_CUDA_TRY(cudaEventRecord(ev[EV_DENSITY], st));
+    const double voxel_volume = (double) g.hhi[0] * g.hhi[1] * g.hhi[2];
+    P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume, st));
+    P2V_CUDA_TRY(launch_normalize_modes(dgrid, V, fs, P.mass_normalize, P.normalize, sms, st));
+    P2V_CUDA_TRY(cudaEventRecord(ev[EV_NORM], st));
+    P2V_CUDA_TRY(cudaEventRecord(ev[EV_AO], st));
+
+    // ---- outputs ----
+    if (vol && vol->data && !direct)
+        P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * V,
+                                     vol->mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    P2V_CUDA_TRY(cudaMemcpyAsync(h_scal, fs, sizeof(FrameScalars), cudaMemcpyDeviceToHost, st));
+    P2V_CUDA_TRY(cudaEventRecord(ev[EV_DOWN], st));
+    P2V_CUDA_TRY(cudaStreamSynchronize(st));
+
+    const FrameScalars& hs = *h_scal;
+    last_grid = dgrid;
+    for (int a = 0; a < 3; ++a)
+        last_res[a] = (uint64_t) res[a];
+    stats = p2v_stats{};
+    stats.particles_in = N;
+    stats.particles_binned = hs.n_valid;
+    stats.particles_dropped = hs.n_dropped;
+    std::memcpy(&stats.radius_max, &hs.rmax_bits, sizeof(float));
+    for (int a = 0; a < 3; ++a) {
+        stats.cell_min[a] = hs.cmin[a];
+        stats.cell_max[a] = hs.cmax[a];
+    }
+    stats.mass_sum = hs.mass;
+    float ms;
+    cudaEventElapsedTime(&ms, ev[EV_START], ev[EV_UPLOAD]);
+    stats.ms_upload = ms;
+    cudaEventElapsedTime(&ms, ev[EV_UPLOAD], ev[EV_BIN]);
+    stats.ms_binning = ms;
+    cudaEventElapsedTime(&ms, ev[EV_BIN], ev[EV_DENSITY]);
+    stats.ms_density = ms;
+    cudaEventElapsedTime(&ms, ev[EV_DENSITY], ev[EV_NORM]);
+    stats.ms_normalize = ms;
+    cudaEventElapsedTime(&ms, ev[EV_NORM], ev[EV_AO]);
+    stats.ms_ao = ms;
+    cudaEventElapsedTime(&ms, ev[EV_AO], ev[EV_DOWN]);
+    stats.ms_download = ms;
+    cudaEventElapsedTime(&ms, ev[EV_START], ev[EV_DOWN]);
+    stats.ms_total = ms;
+    stats.device_error = hs.error;
+
+    if (vol) {
+        for (int a = 0; a < 3; ++a) {
+            vol->resolution[a] = (uint64_t) res[a];
+            const float rangef = std::fabs(bb[a + 3] - bb[a]);
+            vol->extents[a] = rangef;
+            vol->slice_dists[a] = rangef / static_cast<float>(res[a] - 1);
+            vol->origin[a] = bb[a];
+        }
+        std::memcpy(vol->bbox, bb, sizeof(bb));
+        vol->components = 1;
+        vol->min_value = hs.out_min;
+        vol->max_value = hs.out_max;
+        vol->data_hash = ++datahash;
+    }
+    if (hs.error & ERR_LOOKBACK_TIMEOUT)
+        return fail(P2V_ETIMEOUT, "radix sort look-back wait gave up (device error 0x%x)", hs.error);
+    if (hs.error)
+        return fail(P2V_EDOMAIN, "input outside the supported domain (device error 0x%x)", hs.error);
+    err.clear();
+    return P2V_OK;
+}
+
+extern "C" {
+
+int p2v_abi_version(void) {
+    return P2V_ABI_VERSION;
+}
+
+void p2v_params_default(p2v_params* p) {
+    if (!p)
+        return;
+    std::memset(p, 0, sizeof(*p));
+    p->struct_size = sizeof(p2v_params);
+    p->aggregator = 0;
+    p->sizex = p->sizey = p->sizez = 16;  // ParticlesToDensity.cpp:126-131
+    p->cyclX = p->cyclY = p->cyclZ = 1;   // :133-138
+    p->normalize = 1;                     // :140
+    p->sigma = 1.0f;                      // :143-144
+    p->forSurfaceReconstruction = 0;      // :147
+    p->kernel = P2V_KERNEL_BUMP;
+    p->mass_normalize = 0;
+    p->ao_mode = P2V_AO_NONE;
+    p->ao_volume = P2V_AOVOL_DENSITY;
+    p->ao_volume_scale = 1.0f;
+    p->ao_cones = 3;                      // SphereRenderer.cpp:2572-2587
+    p->ao_steps = 0;
+    p->ao_levels = 0;                     // 0: ceil(log2(volume size)) levels (SphereRenderer.cpp:2476)
+    p->ao_apex_deg = 50.0f;               // SphereRenderer.cpp:202
+    p->ao_offset = 0.01f;                 // :205
+    p->ao_strength = 1.0f;                // :208
+    p->ao_cone_length = 0.8f;             // :211
+    p->ao_early_exit = 1;
+    p->mdao_volume_size = 128;            // :199
+    p->mdao_unorm8 = 1;
+    p->aos_sizex = p->aos_sizey = p->aos_sizez = 32;  // AOSphereRenderer.cpp:83-124
+    p->aos_step_len = 0.5f;
+    p->aos_gen_fac = 1.0f;
+    p->aos_eval_fac = 1.0f;
+}
+
+p2v_status p2v_create(p2v_ctx** out, int device) {
+    if (!out)
+        return P2V_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return P2V_ECUDA;
+    auto* c = new (std::nothrow) p2v_ctx();
+    if (!c)
+        return P2V_ENOMEM;
+    c->device = device;
+    p2v_params_default(&c->prm);
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return P2V_ECUDA;
+    }
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    for (auto& e : c->ev)
+        cudaEventCreate(&e);
+    if (cudaMallocHost(&c->h_scal, sizeof(FrameScalars)) != cudaSuccess) {
+        p2v_destroy(c);
+        return P2V_ENOMEM;
+    }
+    *out = c;
+    return P2V_OK;
+}
+
+void p2v_destroy(p2v_ctx* c) {
+    if (!c)
+        return;
+    cudaSetDevice(c->device);
+    if (c->own_stream)
+        cudaStreamSynchronize(c->own_stream);
+    for (DevBuf* b : {&c->raw, &c->xyzr, &c->xyzr_sorted, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
+                      &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal})
+        b->release();
+    for (auto& e : c->ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (c->h_scal)
+        cudaFreeHost(c->h_scal);
+    if (c->own_stream)
+        cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+p2v_status p2v_set_params(p2v_ctx* c, const p2v_params* p) {
+    if (!c || !p)
+        return P2V_EINVAL;
+    if (p->struct_size != sizeof(p2v_params))
+        return c->fail(P2V_EINVAL, "p2v_params.struct_size %u != %zu (ABI mismatch)", p->struct_size, sizeof(p2v_params));
+    c->prm = *p;
+    return P2V_OK;
+}
+
+p2v_status p2v_get_params(const p2v_ctx* c, p2v_params* p) {
+    if (!c || !p)
+        return P2V_EINVAL;
+    *p = c->prm;
+    return P2V_OK;
+}
+
+p2v_status p2v_run_frame(p2v_ctx* c, const p2v_frame* fr, p2v_volume* vol, void* stream) {
+    if (!c || !fr)
+        return P2V_EINVAL;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    return c->run_frame(fr, vol, st);
+}
+
+p2v_status p2v_get_device_volume(p2v_ctx* c, const float** dptr, uint64_t resolution[3]) {
+    if (!c || !dptr)
+        return P2V_EINVAL;
+    if (!c->last_grid)
+        return c->fail(P2V_EINVAL, "no volume computed yet");
+    *dptr = c->last_grid;
+    if (resolution)
+        for (int a = 0; a < 3; ++a)
+            resolution[a] = c->last_res[a];
+    return P2V_OK;
+}
+
+p2v_status p2v_get_stats(const p2v_ctx* c, p2v_stats* st) {
+    if (!c || !st)
+        return P2V_EINVAL;
+    *st = c->stats;
+    return P2V_OK;
+}
+
+size_t p2v_get_last_error(const p2v_ctx* c, char* buf, size_t len) {
+    if (!c)
+        return 0;
+    if (buf && len) {
+        std::strncpy(buf, c->err.c_str(), len - 1);
+        buf[len - 1] = '\0';
+    }
+    return c->err.size();
+}
+
+}  // extern "C"

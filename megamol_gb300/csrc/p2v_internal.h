@@ -1,0 +1,60 @@
+// Internal launcher interfaces of libp2v (not part of the C ABI).
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "p2v_common.cuh"
+
+namespace p2v {
+
+// One particle list on the device, as the pack kernel reads it.
+struct ListDesc {
+    const uint8_t* data;
+    uint32_t stride;       // bytes, never 0 (packed stride filled in by the host)
+    int32_t type;          // p2v_vertex_type
+    float global_radius;
+    uint64_t count;
+    uint64_t offset;       // index of the list's first record in the frame arrays
+};
+
+struct SortBuffers {
+    uint32_t* keys[2];
+    uint32_t* vals[2];
+    uint32_t* hist;        // 4*256 digit histograms + 8 tile counters
+    uint32_t* status;      // look-back words, sort_status_words(n)
+    uint32_t* err;
+    const float4* xyzr_in; // gathered into sorted order by the last pass when non-null
+    float4* xyzr_out;
+    int result;            // index of the buffers holding the sorted output
+};
+
+cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,
+    FrameScalars* fs, cudaStream_t st);
+size_t sort_status_words(uint32_t n);
+int sort_passes(uint32_t max_key);
+cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st);
+cudaError_t launch_cell_start(const uint32_t* keys, uint32_t n, uint32_t nbins, uint32_t* start, uint4* gaps,
+    uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st);
+
+// Density gather configuration chosen on the host.
+struct GatherConfig {
+    int tx, ty, tz;        // nodes per tile
+    int smax;              // staged particles per chunk
+    int rmax;              // row-table entries per plane chunk
+};
+
+size_t gather_smem_bytes(const GatherConfig& c);
+cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* xyzr_sorted, const uint32_t* start,
+    float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st);
+uint32_t gather_tile_count(const GatherConfig& c, const GridGeo& g);
+// Reduce the tile statistics (fixed order, FP64 sum) and derive the normalisation of the grid.
+cudaError_t launch_finalize(const TileStats* tiles, uint32_t ntiles, FrameScalars* fs, int mass_normalize,
+    int minmax_normalize, double n_scale, double voxel_volume, cudaStream_t st);
+cudaError_t launch_normalize_modes(float* grid, uint64_t nvox, const FrameScalars* fs, int mass_normalize,
+    int minmax_normalize, int sms, cudaStream_t st);
+
+}  // namespace p2v

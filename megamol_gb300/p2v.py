@@ -1,0 +1,274 @@
+"""Python binding of libp2v (ctypes over the C ABI in include/p2v.h) and a host-side mirror of MegaMol's
+``datatools::ParticlesToDensity`` module.
+
+``ParticlesToDensity`` keeps the reference module's parameter names and meaning
+(plugins/datatools/src/ParticlesToDensity.cpp:59-152): ``aggregator``, ``sizex``/``sizey``/``sizez``,
+``cyclX``/``cyclY``/``cyclZ``, ``normalize``, ``sigma``, ``forSurfaceReconstruction``; ``get_data`` plays
+the role of the VolumetricDataCall GET_DATA callback (:210-304) and returns the volume together with the
+VolumetricMetadata_t fields the module publishes. Errors surface as ``P2VError`` (the reference returns
+false and logs; there is no silent fallback: without the compiled library or a GPU the calls raise).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Any, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libp2v.so")
+
+# enums of include/p2v.h
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EDOMAIN, EUNSUPPORTED = range(7)
+VERTDATA_NONE, VERTDATA_FLOAT_XYZ, VERTDATA_FLOAT_XYZR, VERTDATA_SHORT_XYZ, VERTDATA_DOUBLE_XYZ = range(5)
+MEM_HOST, MEM_DEVICE = 0, 1
+KERNEL_BUMP, KERNEL_GAUSS3 = 0, 1
+AO_NONE, AO_CONE, AO_AOSPHERE_AXES, AO_AOSPHERE_NORMAL, AO_LEARNED = range(5)
+AOVOL_DENSITY, AOVOL_MDAO = 0, 1
+STATUS_NAMES = {0: "P2V_OK", 1: "P2V_EINVAL", 2: "P2V_ENOMEM", 3: "P2V_ECUDA", 4: "P2V_ETIMEOUT", 5: "P2V_EDOMAIN",
+                6: "P2V_EUNSUPPORTED"}
+
+
+class P2VError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("aggregator", C.c_int32), ("sizex", C.c_int32), ("sizey", C.c_int32), ("sizez", C.c_int32),
+        ("cyclX", C.c_int32), ("cyclY", C.c_int32), ("cyclZ", C.c_int32), ("normalize", C.c_int32),
+        ("sigma", C.c_float), ("forSurfaceReconstruction", C.c_int32),
+        ("kernel", C.c_int32), ("mass_normalize", C.c_int32),
+        ("ao_mode", C.c_int32), ("ao_volume", C.c_int32), ("ao_volume_scale", C.c_float), ("ao_cones", C.c_int32),
+        ("ao_steps", C.c_int32), ("ao_levels", C.c_int32), ("ao_apex_deg", C.c_float), ("ao_offset", C.c_float),
+        ("ao_strength", C.c_float), ("ao_cone_length", C.c_float), ("ao_early_exit", C.c_int32),
+        ("mdao_volume_size", C.c_int32), ("mdao_unorm8", C.c_int32),
+        ("aos_sizex", C.c_int32), ("aos_sizey", C.c_int32), ("aos_sizez", C.c_int32),
+        ("aos_step_len", C.c_float), ("aos_gen_fac", C.c_float), ("aos_eval_fac", C.c_float),
+        ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("tile_z", C.c_int32),
+    ]
+
+
+class ParticleListC(C.Structure):
+    _fields_ = [("vertex_type", C.c_int32), ("vertex_stride", C.c_uint32), ("vertex_data", C.c_void_p),
+                ("count", C.c_uint64), ("global_radius", C.c_float), ("mem", C.c_int32),
+                ("normals", C.c_void_p), ("normal_stride", C.c_uint32), ("ao_out", C.c_void_p)]
+
+
+class FrameC(C.Structure):
+    _fields_ = [("bbox", C.c_float * 6), ("clipbox", C.c_float * 6), ("frame_id", C.c_uint32),
+                ("list_count", C.c_uint32), ("lists", C.POINTER(ParticleListC))]
+
+
+class VolumeC(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("mem", C.c_int32), ("capacity", C.c_uint64),
+                ("resolution", C.c_uint64 * 3), ("components", C.c_uint64), ("slice_dists", C.c_float * 3),
+                ("origin", C.c_float * 3), ("extents", C.c_float * 3), ("min_value", C.c_double),
+                ("max_value", C.c_double), ("bbox", C.c_float * 6), ("data_hash", C.c_uint64)]
+
+
+class StatsC(C.Structure):
+    _fields_ = [("particles_in", C.c_uint64), ("particles_binned", C.c_uint64), ("particles_dropped", C.c_uint64),
+                ("radius_max", C.c_float), ("cell_min", C.c_int32 * 3), ("cell_max", C.c_int32 * 3),
+                ("mass_sum", C.c_double), ("ms_upload", C.c_double), ("ms_binning", C.c_double),
+                ("ms_density", C.c_double), ("ms_normalize", C.c_double), ("ms_ao", C.c_double),
+                ("ms_download", C.c_double), ("ms_total", C.c_double), ("device_error", C.c_uint32),
+                ("ao_fallback", C.c_uint32)]
+
+
+# Every entry point include/p2v.h declares, with its ctypes signature.
+_SIGNATURES = {
+    "p2v_abi_version": ([], C.c_int),
+    "p2v_params_default": ([C.POINTER(Params)], None),
+    "p2v_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
+    "p2v_destroy": ([C.c_void_p], None),
+    "p2v_set_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
+    "p2v_get_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
+    "p2v_run_frame": ([C.c_void_p, C.POINTER(FrameC), C.POINTER(VolumeC), C.c_void_p], C.c_int),
+    "p2v_get_device_volume": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)], C.c_int),
+    "p2v_get_stats": ([C.c_void_p, C.POINTER(StatsC)], C.c_int),
+    "p2v_get_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_size_t),
+}
+
+_lib: Optional[C.CDLL] = None
+
+
+def library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libp2v.so. Raises if it has not been built: there is no fallback implementation."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} is missing: build it with `python -m megamol_gb300.build` "
+                                    "(the GPU path has no CPU fallback)")
+        lib = C.CDLL(path)
+        for name, (args, res) in _SIGNATURES.items():
+            f = getattr(lib, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = lib
+    return _lib
+
+
+def default_params() -> Params:
+    p = Params()
+    library().p2v_params_default(C.byref(p))
+    return p
+
+
+def _ptr(x) -> tuple[int, int]:
+    """(address, mem kind) of a numpy array or a CUDA torch tensor."""
+    if x is None:
+        return 0, MEM_HOST
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data, MEM_HOST
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr(), (MEM_DEVICE if getattr(x, "is_cuda", False) else MEM_HOST)
+    raise TypeError(f"unsupported buffer type {type(x)}")
+
+
+@dataclass
+class ParticleList:
+    """One SimpleSphericalParticles list: vertex data of `vertex_type` with `stride` bytes per record."""
+    data: Any
+    vertex_type: int = VERTDATA_FLOAT_XYZR
+    count: Optional[int] = None
+    stride: int = 0
+    global_radius: float = 0.5
+    normals: Any = None
+    normal_stride: int = 0
+    ao_out: Any = None
+
+    def n(self) -> int:
+        if self.count is not None:
+            return int(self.count)
+        comps = {1: 3, 2: 4, 3: 3, 4: 3}.get(self.vertex_type, 1)
+        if isinstance(self.data, np.ndarray) and self.stride == 0:
+            return self.data.size // comps
+        return int(self.data.shape[0])
+
+
+class Context:
+    """One libp2v context on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = library()
+        h = C.c_void_p()
+        st = self.lib.p2v_create(C.byref(h), int(device))
+        if st != OK:
+            raise P2VError(st, f"p2v_create(device={device}) failed (no CUDA device?)")
+        self.h = h
+        self.params = default_params()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.p2v_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != OK:
+            buf = C.create_string_buffer(1024)
+            self.lib.p2v_get_last_error(self.h, buf, 1024)
+            raise P2VError(st, buf.value.decode(errors="replace"))
+
+    def set_params(self, **kw) -> None:
+        for k, v in kw.items():
+            if not hasattr(self.params, k):
+                raise AttributeError(f"unknown parameter {k}")
+            setattr(self.params, k, v)
+        self._check(self.lib.p2v_set_params(self.h, C.byref(self.params)))
+
+    def get_params(self) -> Params:
+        p = Params()
+        self._check(self.lib.p2v_get_params(self.h, C.byref(p)))
+        return p
+
+    def run_frame(self, lists: Sequence[ParticleList], bbox, out=None, clipbox=None, stream: int = 0,
+                  frame_id: int = 0) -> dict:
+        """Run one frame. `out` is a host numpy float32 array or a CUDA float32 tensor (or None)."""
+        arr = (ParticleListC * max(1, len(lists)))()
+        for i, L in enumerate(lists):
+            dp, mem = _ptr(L.data)
+            npp, _ = _ptr(L.normals)
+            ap, _ = _ptr(L.ao_out)
+            arr[i] = ParticleListC(int(L.vertex_type), int(L.stride), dp, L.n(), float(L.global_radius), mem,
+                                   npp or None, int(L.normal_stride), ap or None)
+        fr = FrameC()
+        fr.bbox[:] = [float(v) for v in bbox]
+        fr.clipbox[:] = [float(v) for v in (clipbox if clipbox is not None else bbox)]
+        fr.frame_id = frame_id
+        fr.list_count = len(lists)
+        fr.lists = arr
+        vol = VolumeC()
+        if out is not None:
+            op, omem = _ptr(out)
+            vol.data = op
+            vol.mem = omem
+            vol.capacity = int(out.size if isinstance(out, np.ndarray) else out.numel())
+        self._check(self.lib.p2v_run_frame(self.h, C.byref(fr), C.byref(vol), C.c_void_p(stream)))
+        return dict(resolution=list(vol.resolution), components=int(vol.components),
+                    slice_dists=list(vol.slice_dists), origin=list(vol.origin), extents=list(vol.extents),
+                    min_value=vol.min_value, max_value=vol.max_value, bbox=list(vol.bbox), data_hash=vol.data_hash)
+
+    def stats(self) -> dict:
+        s = StatsC()
+        self._check(self.lib.p2v_get_stats(self.h, C.byref(s)))
+        return {k: (list(getattr(s, k)) if k in ("cell_min", "cell_max") else getattr(s, k)) for k, _ in s._fields_}
+
+    def device_volume(self):
+        p = C.c_void_p()
+        res = (C.c_uint64 * 3)()
+        self._check(self.lib.p2v_get_device_volume(self.h, C.byref(p), res))
+        return p.value, list(res)
+
+
+class ParticlesToDensity:
+    """Host-side mirror of datatools::ParticlesToDensity (ParticlesToDensity.h:32-145): same parameter
+    slots, same outputs, computed on the GPU through libp2v."""
+
+    SLOTS = ("aggregator", "sizex", "sizey", "sizez", "cyclX", "cyclY", "cyclZ", "normalize", "sigma",
+             "forSurfaceReconstruction")
+
+    def __init__(self, device: int = 0, **params):
+        self.ctx = Context(device)
+        self.ctx.set_params(**params)
+        self.metadata: dict = {}
+
+    def set(self, **params) -> None:
+        self.ctx.set_params(**params)
+
+    def param(self, name: str):
+        return getattr(self.ctx.get_params(), name)
+
+    def get_data(self, lists: Sequence[ParticleList], bbox, clipbox=None, out=None):
+        """VolumetricDataCall GET_DATA: returns (volume, metadata). The volume is a (z, y, x) float32 array
+        (or the given `out`)."""
+        p = self.ctx.get_params()
+        res = [p.sizex, p.sizey, p.sizez]
+        host_out = out
+        if out is None:
+            if p.forSurfaceReconstruction:
+                # the resolution is only known after the box adjustment: compute into the device buffer
+                meta = self.ctx.run_frame(lists, bbox, None, clipbox)
+                res = meta["resolution"]
+                host_out = np.empty(res[2] * res[1] * res[0], np.float32)
+                meta = self.ctx.run_frame(lists, bbox, host_out, clipbox)
+                self.metadata = meta
+                return host_out.reshape(res[2], res[1], res[0]), meta
+            host_out = np.empty(res[2] * res[1] * res[0], np.float32)
+        meta = self.ctx.run_frame(lists, bbox, host_out, clipbox)
+        self.metadata = meta
+        if isinstance(host_out, np.ndarray):
+            r = meta["resolution"]
+            return host_out.reshape(r[2], r[1], r[0]), meta
+        return host_out, meta

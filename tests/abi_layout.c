@@ -1,0 +1,22 @@
+/* Prints sizeof/offsetof of the C ABI structs as JSON, so the test suite can check the Python ctypes
+ * mirror (megamol_gb300/p2v.py) against the header the library was compiled with. */
+#include <stddef.h>
+#include <stdio.h>
+
+#include "p2v.h"
+
+#define F(T, m) printf("\"%s.%s\": %zu, ", #T, #m, offsetof(T, m))
+#define S(T) printf("\"%s\": %zu, ", #T, sizeof(T))
+
+int main(void) {
+    printf("{");
+    S(p2v_params); S(p2v_particle_list); S(p2v_frame); S(p2v_volume); S(p2v_stats);
+    F(p2v_params, sigma); F(p2v_params, kernel); F(p2v_params, ao_mode); F(p2v_params, aos_eval_fac);
+    F(p2v_params, tile_z);
+    F(p2v_particle_list, count); F(p2v_particle_list, mem); F(p2v_particle_list, ao_out);
+    F(p2v_frame, frame_id); F(p2v_frame, lists);
+    F(p2v_volume, resolution); F(p2v_volume, min_value); F(p2v_volume, data_hash);
+    F(p2v_stats, mass_sum); F(p2v_stats, ms_total); F(p2v_stats, ao_fallback);
+    printf("\"end\": 0}\n");
+    return 0;
+}
