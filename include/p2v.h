@@ -65,6 +65,12 @@ typedef enum p2v_mem { P2V_MEM_HOST = 0, P2V_MEM_DEVICE = 1 } p2v_mem;
  * deviation sigma*r cut at 3 sigma, shifted by its value at the cut so it ends continuously at zero. */
 typedef enum p2v_kernel { P2V_KERNEL_BUMP = 0, P2V_KERNEL_GAUSS3 = 1 } p2v_kernel;
 
+/* Voxel accumulation. EXACT: every FP32 contribution is rounded to a multiple of 2^-40 and summed in
+ * 64-bit integers, i.e. the exact, order-independent sum, rounded once to FP32 (particle-major scatter
+ * into shared-memory tiles; the fast path). KAHAN: each voxel gathers its contributions in cell order
+ * with a Kahan-compensated FP32 sum (node-major). Both are deterministic run to run. */
+typedef enum p2v_accumulate { P2V_ACCUM_EXACT = 0, P2V_ACCUM_KAHAN = 1 } p2v_accumulate;
+
 /* AO evaluated per particle at the surface point p + r*n (n = the particle's normal). */
 typedef enum p2v_ao_mode {
     P2V_AO_NONE = 0,
@@ -128,6 +134,7 @@ typedef struct p2v_params {
     /* --- extensions --- */
     int32_t kernel;         /* p2v_kernel */
     int32_t mass_normalize; /* scale so that sum(grid) * voxel volume == particle count (FP64 sum); before `normalize` */
+    int32_t accumulate;     /* p2v_accumulate: how each voxel sums its FP32 contributions */
     /* --- AO --- */
     int32_t ao_mode;        /* p2v_ao_mode */
     int32_t ao_volume;      /* p2v_ao_volume, for P2V_AO_CONE / P2V_AO_LEARNED */

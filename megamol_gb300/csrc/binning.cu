@@ -16,6 +16,7 @@
 
 #include "p2v_common.cuh"
 #include "p2v_internal.h"
+#include "particle_record.cuh"
 
 namespace p2v {
 
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
     const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
     int shift, const uint32_t* __restrict__ digit_offsets, uint32_t* __restrict__ tile_counter,
     uint32_t* __restrict__ status, uint32_t* __restrict__ err, const float4* __restrict__ xyzr_in,
-    float4* __restrict__ xyzr_out) {
+    float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo) {
     __shared__ uint32_t s_keys[SORT_TILE];
     __shared__ uint32_t s_vals[SORT_TILE];
     __shared__ uint32_t s_whist[SORT_WARPS][RADIX];
@@ -328,8 +329,14 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
         keys_out[dst] = kk;
         const uint32_t vv = s_vals[j];
         vals_out[dst] = vv;
-        if (GATHER)
-            xyzr_out[dst] = xyzr_in[vv];
+        if (GATHER) {
+            // last pass: emit the particle's gather record in sorted order
+            float4 A;
+            int4 B;
+            make_record(xyzr_in[vv], geo, A, B);
+            rec_a[dst] = A;
+            rec_b[dst] = B;
+        }
     }
 }
 
@@ -449,10 +456,12 @@ cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, c
         const bool last = p == passes - 1;
         if (last && b.xyzr_in != nullptr)
             onesweep_kernel<true><<<tiles, SORT_THREADS, 0, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
-                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, b.xyzr_in, b.xyzr_out);
+                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, b.xyzr_in, b.rec_a,
+                b.rec_b, b.geo);
         else
             onesweep_kernel<false><<<tiles, SORT_THREADS, 0, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
-                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, nullptr, nullptr);
+                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, nullptr, nullptr, nullptr,
+                b.geo);
         cur ^= 1;
     }
     b.result = cur;

@@ -62,7 +62,7 @@ struct p2v_ctx {
     p2v_stats stats{};
     uint64_t datahash = 0;
 
-    DevBuf raw, xyzr, xyzr_sorted, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
+    DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
     FrameScalars* h_scal = nullptr;  // pinned mirror
     cudaEvent_t ev[EV_COUNT] = {};
     const float* last_grid = nullptr;
@@ -162,6 +162,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
         const double hd = std::fabs((double) hi - (double) lo) / (double) (res[a] - 1);
         g.hhi[a] = (float) hd;
         g.hlo[a] = (float) (hd - (double) g.hhi[a]);
+        g.ihh[a] = (float) (1.0 / (double) g.hhi[a]);
         g.nb[a] = (uint32_t) res[a] + 2u;
         nb *= g.nb[a];
     }
@@ -188,11 +189,21 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
 
     // ---- buffers ----
     const uint32_t n = (uint32_t) N;
-    const GatherConfig gc{8, 16, 16, 2048, 1024};
+    GatherConfig gc{};
+    if (P.accumulate == P2V_ACCUM_KAHAN) {
+        gc = GatherConfig{GATHER_KAHAN, 8, 16, 16, 2048, 1024};
+    } else if (P.accumulate == P2V_ACCUM_EXACT) {
+        gc = GatherConfig{GATHER_EXACT, 16, 16, 16, 0, 1024};
+        if (P.tile_x > 0 || P.tile_y > 0 || P.tile_z > 0)
+            gc = GatherConfig{GATHER_EXACT, P.tile_x, P.tile_y, P.tile_z, 0, 1024};
+    } else {
+        return fail(P2V_EINVAL, "unknown accumulate mode %d", P.accumulate);
+    }
     const uint32_t ntiles = gather_tile_count(gc, g);
     const uint32_t gap_cap = g.nbins / 64 + 2;
     P2V_CUDA_TRY(xyzr.ensure(sizeof(float4) * (N + 1)));
-    P2V_CUDA_TRY(xyzr_sorted.ensure(sizeof(float4) * (N + 1)));
+    P2V_CUDA_TRY(rec_a.ensure(sizeof(float4) * (N + 1)));
+    P2V_CUDA_TRY(rec_b.ensure(sizeof(int4) * (N + 1)));
     P2V_CUDA_TRY(keys0.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(keys1.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals0.ensure(4 * (N + 1)));
@@ -279,14 +290,23 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     sb.status = status.as<uint32_t>();
     sb.err = &fs->error;
     sb.xyzr_in = xyzr.as<float4>();
-    sb.xyzr_out = xyzr_sorted.as<float4>();
+    sb.rec_a = rec_a.as<float4>();
+    sb.rec_b = rec_b.as<int4>();
+    sb.geo = g;
     P2V_CUDA_TRY(launch_sort(sb, n, g.nbins, sms, st));
     const uint32_t* skeys = sb.keys[sb.result];
     P2V_CUDA_TRY(launch_cell_start(skeys, n, g.nbins, cstart.as<uint32_t>(), gaps.as<uint4>(), gap_cap, fs, sms, st));
     P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
 
     // ---- density ----
-    P2V_CUDA_TRY(launch_gather(gc, g, xyzr_sorted.as<float4>(), cstart.as<uint32_t>(), dgrid, tiles.as<TileStats>(), fs, st));
+    {
+        const cudaError_t ge = launch_gather(gc, g, rec_a.as<float4>(), rec_b.as<int4>(), cstart.as<uint32_t>(), dgrid,
+                                             tiles.as<TileStats>(), fs, st);
+        if (ge == cudaErrorInvalidValue)
+            return fail(P2V_EUNSUPPORTED, "density tile %dx%dx%d is not compiled for accumulate=%d", gc.tx, gc.ty,
+                        gc.tz, P.accumulate);
+        P2V_CUDA_TRY(ge);
+    }
     P2V_CUDA_TRY(cudaEventRecord(ev[EV_DENSITY], st));
     const double voxel_volume = (double) g.hhi[0] * g.hhi[1] * g.hhi[2];
     P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume, st));
@@ -374,6 +394,7 @@ void p2v_params_default(p2v_params* p) {
     p->forSurfaceReconstruction = 0;      // :147
     p->kernel = P2V_KERNEL_BUMP;
     p->mass_normalize = 0;
+    p->accumulate = P2V_ACCUM_EXACT;
     p->ao_mode = P2V_AO_NONE;
     p->ao_volume = P2V_AOVOL_DENSITY;
     p->ao_volume_scale = 1.0f;
@@ -426,7 +447,7 @@ void p2v_destroy(p2v_ctx* c) {
     cudaSetDevice(c->device);
     if (c->own_stream)
         cudaStreamSynchronize(c->own_stream);
-    for (DevBuf* b : {&c->raw, &c->xyzr, &c->xyzr_sorted, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
+    for (DevBuf* b : {&c->raw, &c->xyzr, &c->rec_a, &c->rec_b, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
                       &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal})
         b->release();
     for (auto& e : c->ev)

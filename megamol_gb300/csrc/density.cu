@@ -16,6 +16,7 @@
 
 #include "p2v_common.cuh"
 #include "p2v_internal.h"
+#include "particle_record.cuh"
 
 namespace p2v {
 
@@ -26,53 +27,41 @@ constexpr int GATHER_TY = 16;
 constexpr int GATHER_TZ = 16;
 constexpr int MAX_IMAGES = 8;  // cyclic images per axis a tile may visit
 
-__device__ __forceinline__ int64_t floor_div(int64_t a, int64_t b) {
-    int64_t q = a / b;
-    return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
-}
-
-__device__ __forceinline__ int64_t ceil_div_i(int64_t a, int64_t b) {
-    return -floor_div(-a, b);
-}
-
-// Fractional position of coordinate p relative to cell cf, in units of the exact spacing
-// (hhi + hlo): ((p - min) / h) - cf, accurate to ~1e-7 absolute without FP64.
-__device__ __forceinline__ float frac_in_cell(float p, float minf, float hhi, float hlo, int cf) {
-    // two-sum: p - minf = ah + al exactly
-    const float ah = p - minf;
-    const float bb = ah - p;
-    const float al = (p - (ah - bb)) + (-minf - bb);
-    const float q0 = ah / hhi;
-    float rem = __fmaf_rn(-q0, hhi, ah);  // exact remainder of the rounded quotient
-    rem = rem + al - q0 * hlo;
-    return (q0 - static_cast<float>(cf)) + rem / hhi;
+// floor(a / b) for b > 0
+__device__ __forceinline__ int floor_div(int a, int b) {
+    const int q = a / b;
+    return (a % b != 0 && a < 0) ? q - 1 : q;
 }
 
 struct Extent {
-    int L[3], H[3];  // rows [u - L, u + H] of cell bins can hold candidates of node u
-    int F[3];        // largest footprint half-width (bump)
+    int L[3], H[3];     // cell-bin rows [u - L, u + H] can hold candidates of node u
+    int klo[3], khi[3]; // cyclic images of the tile to visit
+    float eps2_max;
+    int ok;
 };
 
 template<int TX, int TY, int TZ>
-__global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const float4* __restrict__ xyzr,
-    const uint32_t* __restrict__ start, float* __restrict__ grid, TileStats* __restrict__ tiles,
-    FrameScalars* __restrict__ fs, int smax, int rmax) {
+__global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const float4* __restrict__ rec_a,
+    const int4* __restrict__ rec_b, const uint32_t* __restrict__ start, float* __restrict__ grid,
+    TileStats* __restrict__ tiles, FrameScalars* __restrict__ fs, int smax, int rmax) {
     constexpr int NT = TY * TZ;
     extern __shared__ __align__(16) unsigned char smem[];
     float* acc_s = reinterpret_cast<float*>(smem);                      // [TX][NT]
     float* acc_c = acc_s + TX * NT;                                      // [TX][NT]
-    float4* sp = reinterpret_cast<float4*>(acc_c + TX * NT);             // [smax] phi xyz, eps^2
-    uint4* sm = reinterpret_cast<uint4*>(sp + smax);                     // [smax] boxes, cells, inv
+    float4* sp = reinterpret_cast<float4*>(acc_c + TX * NT);             // [smax] phi xyz, support^2
+    uint4* sm = reinterpret_cast<uint4*>(sp + smax);                     // [smax] boxes, cells, kernel scale
     uint32_t* row_beg = reinterpret_cast<uint32_t*>(sm + smax);          // [rmax]
     uint32_t* row_off = row_beg + rmax;                                  // [rmax + 1]
     __shared__ double s_dsum[NT / 32];
     __shared__ float s_fmin[NT / 32], s_fmax[NT / 32];
+    __shared__ Extent s_ex;
 
     const int t = threadIdx.x;
     const int ty = t % TY;
     const int tz = t / TY;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
     const bool row_in = (y0 + ty < g.s[1]) && (z0 + tz < g.s[2]);
+    const int T3[3] = {TX, TY, TZ};
 
 #pragma unroll
     for (int k = 0; k < TX; ++k) {
@@ -80,56 +69,57 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
         acc_c[k * NT + t] = 0.0f;
     }
 
-    const float rmax_r = __uint_as_float(fs->rmax_bits);
     const bool bump = g.kernel == 0;
-    const float E45 = expf(-4.5f);
-    if (rmax_r > 0.0f) {
-        // ---- candidate extents from the largest radius ----
+    const float E45 = __expf(-4.5f);
+    // ---- candidate extents from the largest radius, once per CTA ----
+    if (t == 0) {
+        const float rmax_r = __uint_as_float(fs->rmax_bits);
         Extent ex;
+        ex.ok = rmax_r > 0.0f;
         const float eps_max = bump ? g.sigma * rmax_r : 3.0f * (g.sigma * rmax_r);
-        int64_t klo[3], khi[3];
-        const int T3[3] = {TX, TY, TZ};
+        // enlarged slightly so rounding never prunes a contributing cell row
+        ex.eps2_max = eps_max * eps_max * 1.0001f;
         const int o3[3] = {x0, y0, z0};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
+        for (int a = 0; a < 3 && ex.ok; ++a) {
             int E = static_cast<int>(ceilf(eps_max / g.hhi[a] + 1e-3f));
             E = E < 1 ? 1 : E;
-            int F = bump ? static_cast<int>(fminf(ceilf(rmax_r / g.hf[a]), 268435456.0f)) : E;
-            ex.F[a] = F;
+            const int F = bump ? static_cast<int>(fminf(ceilf(rmax_r / g.hf[a]), 255.0f)) : E;
             ex.L[a] = bump ? min(E, F + 1) : E;
             ex.H[a] = bump ? min(E - 1, F) : E - 1;
             if (ex.L[a] > 100) {  // staged cell offsets are kept in 8 bits
-                if (t == 0)
-                    atomicOr(&fs->error, ERR_WINDOW_TOO_WIDE);
+                atomicOr(&fs->error, ERR_WINDOW_TOO_WIDE);
                 ex.L[a] = 100;
                 ex.H[a] = min(ex.H[a], 100);
             }
             if (g.cyc[a]) {
-                const int64_t s = g.s[a];
-                klo[a] = ceil_div_i((int64_t) fs->cmin[a] - o3[a] - T3[a] + 1 - ex.H[a], s);
-                khi[a] = floor_div((int64_t) fs->cmax[a] - o3[a] + ex.L[a], s);
-                if (khi[a] - klo[a] + 1 > MAX_IMAGES) {
-                    if (t == 0)
-                        atomicOr(&fs->error, ERR_WINDOW_TOO_WIDE);
-                    khi[a] = klo[a] + MAX_IMAGES - 1;
+                const int s = g.s[a];
+                // images k with [o + k s - L, o + T - 1 + k s + H] meeting the occupied cells
+                ex.klo[a] = -floor_div(-(fs->cmin[a] - o3[a] - T3[a] + 1 - ex.H[a]), s);
+                ex.khi[a] = floor_div(fs->cmax[a] - o3[a] + ex.L[a], s);
+                if (ex.khi[a] - ex.klo[a] + 1 > MAX_IMAGES) {
+                    atomicOr(&fs->error, ERR_WINDOW_TOO_WIDE);
+                    ex.khi[a] = ex.klo[a] + MAX_IMAGES - 1;
                 }
             } else {
-                klo[a] = 0;
-                khi[a] = 0;
+                ex.klo[a] = 0;
+                ex.khi[a] = 0;
             }
         }
+        s_ex = ex;
+    }
+    __syncthreads();
+    const Extent ex = s_ex;
 
-        for (int64_t kz = klo[2]; kz <= khi[2]; ++kz)
-            for (int64_t ky = klo[1]; ky <= khi[1]; ++ky)
-                for (int64_t kx = klo[0]; kx <= khi[0]; ++kx) {
-                    const int u0[3] = {x0 + (int) (kx * g.s[0]), y0 + (int) (ky * g.s[1]), z0 + (int) (kz * g.s[2])};
+    if (ex.ok) {
+        for (int kz = ex.klo[2]; kz <= ex.khi[2]; ++kz)
+            for (int ky = ex.klo[1]; ky <= ex.khi[1]; ++ky)
+                for (int kx = ex.klo[0]; kx <= ex.khi[0]; ++kx) {
+                    const int u0[3] = {x0 + kx * g.s[0], y0 + ky * g.s[1], z0 + kz * g.s[2]};
                     int wlo[3], whi[3];
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
-                        wlo[a] = max(u0[a] - ex.L[a], -1);
-                        wlo[a] = min(wlo[a], g.s[a]);
-                        whi[a] = min(u0[a] + T3[a] - 1 + ex.H[a], g.s[a]);
-                        whi[a] = max(whi[a], -1);
+                        wlo[a] = min(max(u0[a] - ex.L[a], -1), g.s[a]);
+                        whi[a] = max(min(u0[a] + T3[a] - 1 + ex.H[a], g.s[a]), -1);
                     }
                     const int nwy = whi[1] - wlo[1] + 1;
                     const int nwz = whi[2] - wlo[2] + 1;
@@ -139,10 +129,14 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                         continue;
                     }
                     const int planes_per_chunk = rmax / nwy;
-                    // this thread's node (unwrapped) and its relevant rows
+                    // This thread's node row (unwrapped) and its candidate cell rows. Each end is first
+                    // clamped to the bin range [-1, s]: bins -1 and s hold every particle beyond the box,
+                    // so a row range lying wholly outside maps onto them.
                     const int uy = u0[1] + ty, uz = u0[2] + tz;
-                    const int ry_lo = max(uy - ex.L[1], wlo[1]), ry_hi = min(uy + ex.H[1], whi[1]);
-                    const int rz_lo = max(uz - ex.L[2], wlo[2]), rz_hi = min(uz + ex.H[2], whi[2]);
+                    const int ry_lo = max(min(max(uy - ex.L[1], -1), g.s[1]), wlo[1]);
+                    const int ry_hi = min(max(min(uy + ex.H[1], g.s[1]), -1), whi[1]);
+                    const int rz_lo = max(min(max(uz - ex.L[2], -1), g.s[2]), wlo[2]);
+                    const int rz_hi = min(max(min(uz + ex.H[2], g.s[2]), -1), whi[2]);
                     const uint32_t bx_lo = (uint32_t) (wlo[0] + 1), bx_end = (uint32_t) (whi[0] + 2);
 
                     for (int pz0 = 0; pz0 < nwz; pz0 += planes_per_chunk) {
@@ -160,7 +154,7 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                             row_off[r + 1] = e - b;
                         }
                         __syncthreads();
-                        // exclusive scan of the row counts (single warp, rows are few)
+                        // exclusive scan of the row counts (one warp)
                         if (t < 32) {
                             uint32_t carry = 0;
                             for (int base = 0; base < nrows; base += 32) {
@@ -185,10 +179,10 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                             const uint32_t cn = min((uint32_t) smax, total - cb);
                             if (cb > 0)
                                 __syncthreads();  // previous chunk fully consumed
-                            // ---- stage: coalesced float4 loads of the chunk's particles ----
+                            // ---- stage: coalesced 16-byte loads of the chunk's particle records ----
                             for (uint32_t si = t; si < cn; si += NT) {
                                 const uint32_t f = cb + si;
-                                int lo = 0, hi = nrows;  // find row r with row_off[r] <= f < row_off[r+1]
+                                int lo = 0, hi = nrows;  // row r with row_off[r] <= f < row_off[r+1]
                                 while (hi - lo > 1) {
                                     const int mid = (lo + hi) >> 1;
                                     if (row_off[mid] <= f)
@@ -197,37 +191,36 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                                         hi = mid;
                                 }
                                 const uint32_t j = row_beg[lo] + (f - row_off[lo]);
-                                const float4 p = xyzr[j];
-                                const float pc[3] = {p.x, p.y, p.z};
-                                const float r = p.w;
+                                const float4 A = rec_a[j];
+                                const int4 B = rec_b[j];
+                                const float phi[3] = {A.x, A.y, A.z};
+                                const int cf[3] = {B.x, B.y, B.z};
+                                const uint32_t meta = (uint32_t) B.w;
+                                const float r = A.w;
                                 const float eps = bump ? g.sigma * r : 3.0f * (g.sigma * r);
-                                float phi[3];
                                 int blo[3], bhi[3], crel[3];
                                 bool empty = false;
 #pragma unroll
                                 for (int a = 0; a < 3; ++a) {
-                                    const float q = (pc[a] - g.minf[a]) / g.hf[a];
-                                    const int ct = static_cast<int>(q);          // reference cell
-                                    const int cf = static_cast<int>(floorf(q));  // bin cell
-                                    phi[a] = frac_in_cell(pc[a], g.minf[a], g.hhi[a], g.hlo[a], cf);
-                                    const int64_t cr = (int64_t) cf - u0[a];
+                                    const int cr = cf[a] - u0[a];
                                     const float pos = static_cast<float>(cr) + phi[a];
-                                    const float eh = eps / g.hhi[a];
-                                    int64_t lo_a = (int64_t) floorf(pos - eh);
-                                    int64_t hi_a = (int64_t) ceilf(pos + eh);
+                                    const float eh = eps * g.ihh[a];
+                                    // nodes k with |k - pos| < eps / h; a node the rounding drops lies at
+                                    // the edge of the support, where the kernel is zero
+                                    int lo_a = static_cast<int>(floorf(pos - eh)) + 1;
+                                    int hi_a = static_cast<int>(ceilf(pos + eh)) - 1;
                                     if (bump) {
-                                        const int64_t f = (int64_t) fminf(ceilf(r / g.hf[a]), 268435456.0f);
-                                        const int64_t ctr = (int64_t) ct - u0[a];
+                                        const int f = (int) ((meta >> (8 * a)) & 0xFFu);
+                                        const int ctr = cr + (int) ((meta >> (24 + a)) & 1u);
                                         lo_a = max(lo_a, ctr - f);
                                         hi_a = min(hi_a, ctr + f);
                                     }
-                                    lo_a = max(lo_a, (int64_t) 0);
-                                    hi_a = min(hi_a, (int64_t) T3[a] - 1);
-                                    if (lo_a > hi_a)
-                                        empty = true;
-                                    blo[a] = (int) lo_a;
-                                    bhi[a] = (int) hi_a;
-                                    crel[a] = (int) max(min(cr, (int64_t) 120), (int64_t) -120);
+                                    lo_a = max(lo_a, 0);
+                                    hi_a = min(hi_a, T3[a] - 1);
+                                    empty = empty || lo_a > hi_a;
+                                    blo[a] = lo_a;
+                                    bhi[a] = hi_a;
+                                    crel[a] = max(min(cr, 120), -120);
                                 }
                                 uint4 m;
                                 if (empty) {
@@ -245,11 +238,11 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                                 float eps2, inv;
                                 if (bump) {
                                     eps2 = eps * eps;
-                                    inv = 1.0f / eps2;
+                                    inv = __frcp_rn(eps2);
                                 } else {
                                     const float sg = g.sigma * r;
                                     eps2 = 9.0f * sg * sg;
-                                    inv = 1.0f / (2.0f * sg * sg);
+                                    inv = __frcp_rn(2.0f * sg * sg);
                                 }
                                 m.w = __float_as_uint(inv);
                                 sp[si] = make_float4(phi[0], phi[1], phi[2], eps2);
@@ -260,7 +253,16 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                             if (row_in) {
                                 const int zr_lo = max(rz_lo, wlo[2] + pz0), zr_hi = min(rz_hi, wlo[2] + pz1 - 1);
                                 for (int zz = zr_lo; zz <= zr_hi; ++zz) {
+                                    // smallest z distance from this node row to cell row zz
+                                    const int oz = zz - uz;
+                                    const float gz = oz > 0 ? oz * g.hhi[2] : (oz < -1 ? (-oz - 1) * g.hhi[2] : 0.0f);
                                     for (int yy = ry_lo; yy <= ry_hi; ++yy) {
+                                        const int oy = yy - uy;
+                                        const float gy = oy > 0 ? oy * g.hhi[1] : (oy < -1 ? (-oy - 1) * g.hhi[1] : 0.0f);
+                                        // bins -1 and s hold particles from arbitrarily far away: never pruned
+                                        if (gy * gy + gz * gz >= ex.eps2_max && yy >= 0 && yy < g.s[1] && zz >= 0 &&
+                                            zz < g.s[2])
+                                            continue;
                                         const int r = (zz - wlo[2] - pz0) * nwy + (yy - wlo[1]);
                                         uint32_t a0 = row_off[r], a1 = row_off[r + 1];
                                         a0 = max(a0, cb);
@@ -289,12 +291,15 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                                                 const float d2 = __fmaf_rn(dx, dx, dyz);
                                                 if (!(d2 < P.w))
                                                     continue;
+                                                // __frcp_rn is the correctly rounded reciprocal; __expf's
+                                                // relative error stays below 1e-6 over the argument range
+                                                // that yields values above 1e-7 of the kernel maximum.
                                                 float v;
                                                 if (bump) {
                                                     const float w = __fmaf_rn(-d2, inv, 1.0f);
-                                                    v = w > 0.0f ? expf(-1.0f / w) : 0.0f;
+                                                    v = w > 0.0f ? __expf(-__frcp_rn(w)) : 0.0f;
                                                 } else {
-                                                    v = fmaxf(expf(-d2 * inv) - E45, 0.0f);
+                                                    v = fmaxf(__expf(-d2 * inv) - E45, 0.0f);
                                                 }
                                                 float* ps = acc_s + k * NT + t;
                                                 float* pcmp = acc_c + k * NT + t;
@@ -347,7 +352,322 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
             vmin = fminf(vmin, s_fmin[w]);
             vmax = fmaxf(vmax, s_fmax[w]);
         }
-        // warp 0's values are already in dsum/vmin/vmax of lane 0
+        TileStats ts;
+        ts.sum = dsum;
+        ts.vmin = vmin;
+        ts.vmax = vmax;
+        tiles[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = ts;
+    }
+}
+
+// Candidate extents and cyclic images of one tile (shared by both gather kernels).
+__device__ __forceinline__ Extent tile_extent(const GridGeo& g, FrameScalars* fs, const int o3[3], const int T3[3]) {
+    const bool bump = g.kernel == 0;
+    const float rmax_r = __uint_as_float(fs->rmax_bits);
+    Extent ex;
+    ex.ok = rmax_r > 0.0f;
+    const float eps_max = bump ? g.sigma * rmax_r : 3.0f * (g.sigma * rmax_r);
+    ex.eps2_max = eps_max * eps_max * 1.0001f;
+    for (int a = 0; a < 3 && ex.ok; ++a) {
+        int E = static_cast<int>(ceilf(eps_max / g.hhi[a] + 1e-3f));
+        E = E < 1 ? 1 : E;
+        const int F = bump ? static_cast<int>(fminf(ceilf(rmax_r / g.hf[a]), 255.0f)) : E;
+        ex.L[a] = bump ? min(E, F + 1) : E;
+        ex.H[a] = bump ? min(E - 1, F) : E - 1;
+        if (ex.L[a] > 100) {
+            atomicOr(&fs->error, ERR_WINDOW_TOO_WIDE);
+            ex.L[a] = 100;
+            ex.H[a] = min(ex.H[a], 100);
+        }
+        if (g.cyc[a]) {
+            const int s = g.s[a];
+            ex.klo[a] = -floor_div(-(fs->cmin[a] - o3[a] - T3[a] + 1 - ex.H[a]), s);
+            ex.khi[a] = floor_div(fs->cmax[a] - o3[a] + ex.L[a], s);
+            if (ex.khi[a] - ex.klo[a] + 1 > MAX_IMAGES) {
+                atomicOr(&fs->error, ERR_WINDOW_TOO_WIDE);
+                ex.khi[a] = ex.klo[a] + MAX_IMAGES - 1;
+            }
+        } else {
+            ex.klo[a] = 0;
+            ex.khi[a] = 0;
+        }
+    }
+    return ex;
+}
+
+// One particle's node box as the warp-level walk needs it (held in registers, then published to
+// shared memory field by field so that lanes reading different particles never conflict on a bank).
+struct WarpPart {
+    float d0[3];       // (box corner - particle) in cells, per axis
+    float eps2, inv;   // squared support and kernel scale
+    float iby;         // 1/by for decoding a box-local row index
+    int bx, by;        // box extents in x and y
+    int node0;         // tile index of the box corner
+};
+constexpr int WP_FIELDS = 9;
+
+// Fixed-point scale of the exact accumulation: contributions are rounded to multiples of 2^-40 and
+// summed as 64-bit integers, so every voxel holds the exact sum of its rounded FP32 contributions,
+// independent of the order in which particles arrive.
+constexpr float FIX_SCALE = 1099511627776.0f;  // 2^40
+constexpr float FIX_INV = 9.094947017729282e-13f;  // 2^-40
+
+// Particle-major gather with exact, order-independent accumulation. A CTA owns a tile of TX*TY*TZ
+// nodes held as 64-bit fixed-point sums in shared memory; for every cyclic image of the tile it walks
+// the sorted particle records of the surrounding cell rows (coalesced 16-byte loads), and each thread
+// adds its particle's kernel values to the nodes of the particle's footprint that lie in the tile.
+template<int TX, int TY, int TZ, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, const float4* __restrict__ rec_a,
+    const int4* __restrict__ rec_b, const uint32_t* __restrict__ start, float* __restrict__ grid,
+    TileStats* __restrict__ tiles, FrameScalars* __restrict__ fs, int rmax) {
+    constexpr int NN = TX * TY * TZ;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);  // [NN]
+    uint32_t* row_beg = reinterpret_cast<uint32_t*>(acc + NN);               // [rmax]
+    uint32_t* row_off = row_beg + rmax;                                      // [rmax + 1]
+    __shared__ double s_dsum[NT / 32];
+    __shared__ float s_fmin[NT / 32], s_fmax[NT / 32];
+    __shared__ Extent s_ex;
+    __shared__ uint32_t s_part[WP_FIELDS][NT];
+    __shared__ uint32_t s_pre[NT + 32];
+
+    const int t = threadIdx.x;
+    const uint32_t lane = t & 31u;
+    const uint32_t warp = t >> 5;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    const int T3[3] = {TX, TY, TZ};
+    const int o3[3] = {x0, y0, z0};
+    for (int n = t; n < NN; n += NT)
+        acc[n] = 0ull;
+    const bool bump = g.kernel == 0;
+    const float E45 = __expf(-4.5f);
+    if (t == 0)
+        s_ex = tile_extent(g, fs, o3, T3);
+    __syncthreads();
+    const Extent ex = s_ex;
+
+    if (ex.ok) {
+        for (int kz = ex.klo[2]; kz <= ex.khi[2]; ++kz)
+            for (int ky = ex.klo[1]; ky <= ex.khi[1]; ++ky)
+                for (int kx = ex.klo[0]; kx <= ex.khi[0]; ++kx) {
+                    const int u0[3] = {x0 + kx * g.s[0], y0 + ky * g.s[1], z0 + kz * g.s[2]};
+                    int wlo[3], whi[3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        wlo[a] = min(max(u0[a] - ex.L[a], -1), g.s[a]);
+                        whi[a] = max(min(u0[a] + T3[a] - 1 + ex.H[a], g.s[a]), -1);
+                    }
+                    const int nwy = whi[1] - wlo[1] + 1;
+                    const int nwz = whi[2] - wlo[2] + 1;
+                    if (nwy > rmax) {
+                        if (t == 0)
+                            atomicOr(&fs->error, ERR_STAGE_OVERFLOW);
+                        continue;
+                    }
+                    const int planes_per_chunk = rmax / nwy;
+                    const uint32_t bx_lo = (uint32_t) (wlo[0] + 1), bx_end = (uint32_t) (whi[0] + 2);
+                    for (int pz0 = 0; pz0 < nwz; pz0 += planes_per_chunk) {
+                        const int pz1 = min(nwz, pz0 + planes_per_chunk);
+                        const int nrows = (pz1 - pz0) * nwy;
+                        __syncthreads();
+                        for (int r = t; r < nrows; r += NT) {
+                            const int zz = wlo[2] + pz0 + r / nwy;
+                            const int yy = wlo[1] + r % nwy;
+                            const uint32_t rowkey = ((uint32_t) (zz + 1) * g.nb[1] + (uint32_t) (yy + 1)) * g.nb[0];
+                            const uint32_t b = start[rowkey + bx_lo];
+                            row_beg[r] = b;
+                            row_off[r + 1] = start[rowkey + bx_end] - b;
+                        }
+                        __syncthreads();
+                        if (t < 32) {
+                            uint32_t carry = 0;
+                            for (int base = 0; base < nrows; base += 32) {
+                                const int r = base + t;
+                                uint32_t v = r < nrows ? row_off[r + 1] : 0u;
+#pragma unroll
+                                for (int o = 1; o < 32; o <<= 1) {
+                                    uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+                                    if (t >= o)
+                                        v += u;
+                                }
+                                if (r < nrows)
+                                    row_off[r + 1] = carry + v;
+                                carry += __shfl_sync(0xffffffffu, v, 31);
+                            }
+                            if (t == 0)
+                                row_off[0] = 0;
+                        }
+                        __syncthreads();
+                        const uint32_t total = row_off[nrows];
+                        // Each warp takes 32 consecutive records; every lane derives its particle's node
+                        // box, then the warp walks the concatenated boxes 32 nodes at a time (a warp-level
+                        // load-balanced search), so all lanes test nodes in lockstep.
+                        for (uint32_t base = warp * 32; base < total; base += NT) {
+                            const uint32_t f = base + lane;
+                            uint32_t nb = 0;
+                            WarpPart wp;
+                            if (f < total) {
+                                int lo = 0, hi = nrows;  // row r with row_off[r] <= f < row_off[r+1]
+                                while (hi - lo > 1) {
+                                    const int mid = (lo + hi) >> 1;
+                                    if (row_off[mid] <= f)
+                                        lo = mid;
+                                    else
+                                        hi = mid;
+                                }
+                                const uint32_t j = row_beg[lo] + (f - row_off[lo]);
+                                const float4 A = rec_a[j];
+                                const int4 B = rec_b[j];
+                                const float phi[3] = {A.x, A.y, A.z};
+                                const int cf[3] = {B.x, B.y, B.z};
+                                const uint32_t meta = (uint32_t) B.w;
+                                const float r = A.w;
+                                const float eps = bump ? g.sigma * r : 3.0f * (g.sigma * r);
+                                int blo[3], bw[3];
+                                bool empty = false;
+#pragma unroll
+                                for (int a = 0; a < 3; ++a) {
+                                    const int cr = cf[a] - u0[a];
+                                    const float pos = static_cast<float>(cr) + phi[a];
+                                    const float eh = eps * g.ihh[a];
+                                    // nodes k with |k - pos| < eps / h; a node the rounding drops lies at
+                                    // the edge of the support, where the kernel is zero
+                                    int lo_a = static_cast<int>(floorf(pos - eh)) + 1;
+                                    int hi_a = static_cast<int>(ceilf(pos + eh)) - 1;
+                                    if (bump) {
+                                        const int fa = (int) ((meta >> (8 * a)) & 0xFFu);
+                                        const int ctr = cr + (int) ((meta >> (24 + a)) & 1u);
+                                        lo_a = max(lo_a, ctr - fa);
+                                        hi_a = min(hi_a, ctr + fa);
+                                    }
+                                    lo_a = max(lo_a, 0);
+                                    hi_a = min(hi_a, T3[a] - 1);
+                                    empty = empty || lo_a > hi_a;
+                                    blo[a] = lo_a;
+                                    bw[a] = hi_a - lo_a + 1;
+                                    // node offset from the particle, in cells: (k - cr) - phi = (k - lo) + d0
+                                    wp.d0[a] = static_cast<float>(lo_a - cr) - phi[a];
+                                }
+                                if (!empty) {
+                                    nb = (uint32_t) (bw[1] * bw[2]);  // x-rows of the box
+                                    if (bump) {
+                                        wp.eps2 = eps * eps;
+                                        wp.inv = __frcp_rn(wp.eps2);
+                                    } else {
+                                        const float sg = g.sigma * r;
+                                        wp.eps2 = 9.0f * sg * sg;
+                                        wp.inv = __frcp_rn(2.0f * sg * sg);
+                                    }
+                                    wp.bx = bw[0];
+                                    wp.by = bw[1];
+                                    wp.node0 = (blo[2] * TY + blo[1]) * TX + blo[0];
+                                    wp.iby = 1.0f / (float) bw[1];
+                                }
+                            }
+                            // exclusive prefix of the row counts over the warp
+                            uint32_t incl = nb;
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                                if (lane >= (uint32_t) o)
+                                    incl += u;
+                            }
+                            const uint32_t wtotal = __shfl_sync(0xffffffffu, incl, 31);
+                            if (wtotal == 0)
+                                continue;
+                            const int wl = warp * 32 + lane;
+                            s_part[0][wl] = __float_as_uint(wp.d0[0]);
+                            s_part[1][wl] = __float_as_uint(wp.d0[1]);
+                            s_part[2][wl] = __float_as_uint(wp.d0[2]);
+                            s_part[3][wl] = __float_as_uint(wp.eps2);
+                            s_part[4][wl] = __float_as_uint(wp.inv);
+                            s_part[5][wl] = __float_as_uint(wp.iby);
+                            s_part[6][wl] = (uint32_t) wp.bx;
+                            s_part[7][wl] = (uint32_t) wp.by;
+                            s_part[8][wl] = (uint32_t) wp.node0;
+                            s_pre[wl] = incl - nb;
+                            __syncwarp();
+                            const uint32_t* pre = s_pre + warp * 32;
+                            for (uint32_t j0 = 0; j0 < wtotal; j0 += 32) {
+                                const uint32_t jj = j0 + lane;
+                                if (jj < wtotal) {
+                                    // owner: the last lane whose prefix is <= jj (its box is non-empty)
+                                    int o = 0;
+#pragma unroll
+                                    for (int step = 16; step > 0; step >>= 1)
+                                        if (pre[o + step] <= jj)
+                                            o += step;
+                                    const int ow = warp * 32 + o;
+                                    const int local = (int) (jj - pre[o]);
+                                    const int by = (int) s_part[7][ow];
+                                    const int zl = (int) ((static_cast<float>(local) + 0.5f) * __uint_as_float(s_part[5][ow]));
+                                    const int yl = local - zl * by;
+                                    const float dy = g.hhi[1] * (static_cast<float>(yl) + __uint_as_float(s_part[1][ow]));
+                                    const float dz = g.hhi[2] * (static_cast<float>(zl) + __uint_as_float(s_part[2][ow]));
+                                    const float dyz = __fmaf_rn(dy, dy, dz * dz);
+                                    const float eps2 = __uint_as_float(s_part[3][ow]);
+                                    if (dyz < eps2) {
+                                        const float inv = __uint_as_float(s_part[4][ow]);
+                                        const float d0x = __uint_as_float(s_part[0][ow]);
+                                        const int bx = (int) s_part[6][ow];
+                                        unsigned long long* row = acc + (int) s_part[8][ow] + (zl * TY + yl) * TX;
+                                        for (int xl = 0; xl < bx; ++xl) {
+                                            const float dx = g.hhi[0] * (static_cast<float>(xl) + d0x);
+                                            const float d2 = __fmaf_rn(dx, dx, dyz);
+                                            if (!(d2 < eps2))
+                                                continue;
+                                            // __frcp_rn is the correctly rounded reciprocal; __expf's relative
+                                            // error stays below 1e-6 where the kernel exceeds 1e-7 of its peak
+                                            float v;
+                                            if (bump) {
+                                                const float w = __fmaf_rn(-d2, inv, 1.0f);
+                                                v = w > 0.0f ? __expf(-__frcp_rn(w)) : 0.0f;
+                                            } else {
+                                                v = fmaxf(__expf(-d2 * inv) - E45, 0.0f);
+                                            }
+                                            atomicAdd(row + xl, (unsigned long long) __float2ull_rn(v * FIX_SCALE));
+                                        }
+                                    }
+                                }
+                            }
+                            __syncwarp();
+                        }
+                    }
+                }
+    }
+    __syncthreads();
+
+    // ---- write the tile (x fastest, coalesced) and its statistics ----
+    double dsum = 0.0;
+    float vmin = INFINITY, vmax = -INFINITY;
+    for (int n = t; n < NN; n += NT) {
+        const int x = n % TX, y = (n / TX) % TY, z = n / (TX * TY);
+        if (x0 + x < g.s[0] && y0 + y < g.s[1] && z0 + z < g.s[2]) {
+            const float v = __ull2float_rn(acc[n]) * FIX_INV;
+            grid[((size_t) (z0 + z) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)] = v;
+            dsum += (double) v;
+            vmin = fminf(vmin, v);
+            vmax = fmaxf(vmax, v);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+        vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    }
+    if ((t & 31) == 0) {
+        s_dsum[t >> 5] = dsum;
+        s_fmin[t >> 5] = vmin;
+        s_fmax[t >> 5] = vmax;
+    }
+    __syncthreads();
+    if (t == 0) {
+        for (int w = 1; w < NT / 32; ++w) {
+            dsum += s_dsum[w];
+            vmin = fminf(vmin, s_fmin[w]);
+            vmax = fmaxf(vmax, s_fmax[w]);
+        }
         TileStats ts;
         ts.sum = dsum;
         ts.vmin = vmin;
@@ -432,6 +752,8 @@ __global__ void __launch_bounds__(256) normalize_kernel(float* __restrict__ grid
 }  // namespace
 
 size_t gather_smem_bytes(const GatherConfig& c) {
+    if (c.mode == GATHER_EXACT)
+        return (size_t) c.tx * c.ty * c.tz * sizeof(unsigned long long) + (size_t) (2 * c.rmax + 1) * sizeof(uint32_t);
     return (size_t) 2 * c.tx * c.ty * c.tz * sizeof(float) + (size_t) c.smax * (sizeof(float4) + sizeof(uint4)) +
            (size_t) (2 * c.rmax + 1) * sizeof(uint32_t);
 }
@@ -440,17 +762,42 @@ uint32_t gather_tile_count(const GatherConfig& c, const GridGeo& g) {
     return ceil_div(g.s[0], c.tx) * ceil_div(g.s[1], c.ty) * ceil_div(g.s[2], c.tz);
 }
 
-cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* xyzr_sorted, const uint32_t* start,
-    float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st) {
+namespace {
+template<class K>
+cudaError_t launch_tiles(K kern, const GatherConfig& c, const GridGeo& g, int nt, size_t smem, cudaStream_t st,
+    const float4* rec_a, const int4* rec_b, const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    if (e != cudaSuccess)
+        return e;
+    dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), ceil_div(g.s[2], c.tz));
+    kern<<<grd, nt, smem, st>>>(g, rec_a, rec_b, start, grid, tiles, fs, c.rmax);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* rec_a, const int4* rec_b,
+    const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st) {
+    const size_t smem = gather_smem_bytes(c);
+    if (c.mode == GATHER_EXACT) {
+        if (c.tx == 16 && c.ty == 16 && c.tz == 16)
+            return launch_tiles(gather_fixed_kernel<16, 16, 16, 256>, c, g, 256, smem, st, rec_a, rec_b, start, grid,
+                                tiles, fs);
+        if (c.tx == 16 && c.ty == 8 && c.tz == 8)
+            return launch_tiles(gather_fixed_kernel<16, 8, 8, 256>, c, g, 256, smem, st, rec_a, rec_b, start, grid,
+                                tiles, fs);
+        if (c.tx == 32 && c.ty == 16 && c.tz == 8)
+            return launch_tiles(gather_fixed_kernel<32, 16, 8, 512>, c, g, 512, smem, st, rec_a, rec_b, start, grid,
+                                tiles, fs);
+        return cudaErrorInvalidValue;
+    }
     if (c.tx != GATHER_TX || c.ty != GATHER_TY || c.tz != GATHER_TZ)
         return cudaErrorInvalidValue;
-    const size_t smem = gather_smem_bytes(c);
     auto kern = gather_kernel<GATHER_TX, GATHER_TY, GATHER_TZ>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess)
         return e;
     dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), ceil_div(g.s[2], c.tz));
-    kern<<<grd, c.ty * c.tz, smem, st>>>(g, xyzr_sorted, start, grid, tiles, fs, c.smax, c.rmax);
+    kern<<<grd, c.ty * c.tz, smem, st>>>(g, rec_a, rec_b, start, grid, tiles, fs, c.smax, c.rmax);
     return cudaGetLastError();
 }
 

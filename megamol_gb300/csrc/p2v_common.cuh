@@ -22,6 +22,7 @@ struct GridGeo {
     float minf[3];       // bbox min (reference origin)
     float hf[3];         // reference spacing: float(range) / float(res-1)
     float hhi[3], hlo[3];// exact spacing (right-left)/(res-1) as an unevaluated float sum
+    float ihh[3];        // 1 / hhi
     float sigma;
     int32_t kernel;      // 0 bump, 1 gauss3
     uint32_t nb[3];      // bins per axis = res + 2 (underflow and overflow bins)

@@ -27,8 +27,10 @@ struct SortBuffers {
     uint32_t* hist;        // 4*256 digit histograms + 8 tile counters
     uint32_t* status;      // look-back words, sort_status_words(n)
     uint32_t* err;
-    const float4* xyzr_in; // gathered into sorted order by the last pass when non-null
-    float4* xyzr_out;
+    const float4* xyzr_in; // when non-null the last pass writes every particle's gather record
+    float4* rec_a;         // (particle_record.cuh) in sorted order
+    int4* rec_b;
+    GridGeo geo;
     int result;            // index of the buffers holding the sorted output
 };
 
@@ -41,14 +43,17 @@ cudaError_t launch_cell_start(const uint32_t* keys, uint32_t n, uint32_t nbins, 
     uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st);
 
 // Density gather configuration chosen on the host.
+enum GatherMode { GATHER_EXACT = 0, GATHER_KAHAN = 1 };
 struct GatherConfig {
+    int mode;              // GatherMode
     int tx, ty, tz;        // nodes per tile
     int smax;              // staged particles per chunk
     int rmax;              // row-table entries per plane chunk
 };
 
 size_t gather_smem_bytes(const GatherConfig& c);
-cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* xyzr_sorted, const uint32_t* start,
+cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* rec_a, const int4* rec_b,
+    const uint32_t* start,
     float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st);
 uint32_t gather_tile_count(const GatherConfig& c, const GridGeo& g);
 // Reduce the tile statistics (fixed order, FP64 sum) and derive the normalisation of the grid.

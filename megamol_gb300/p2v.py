@@ -25,6 +25,7 @@ OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EDOMAIN, EUNSUPPORTED = range(7)
 VERTDATA_NONE, VERTDATA_FLOAT_XYZ, VERTDATA_FLOAT_XYZR, VERTDATA_SHORT_XYZ, VERTDATA_DOUBLE_XYZ = range(5)
 MEM_HOST, MEM_DEVICE = 0, 1
 KERNEL_BUMP, KERNEL_GAUSS3 = 0, 1
+ACCUM_EXACT, ACCUM_KAHAN = 0, 1
 AO_NONE, AO_CONE, AO_AOSPHERE_AXES, AO_AOSPHERE_NORMAL, AO_LEARNED = range(5)
 AOVOL_DENSITY, AOVOL_MDAO = 0, 1
 STATUS_NAMES = {0: "P2V_OK", 1: "P2V_EINVAL", 2: "P2V_ENOMEM", 3: "P2V_ECUDA", 4: "P2V_ETIMEOUT", 5: "P2V_EDOMAIN",
@@ -43,7 +44,7 @@ class Params(C.Structure):
         ("aggregator", C.c_int32), ("sizex", C.c_int32), ("sizey", C.c_int32), ("sizez", C.c_int32),
         ("cyclX", C.c_int32), ("cyclY", C.c_int32), ("cyclZ", C.c_int32), ("normalize", C.c_int32),
         ("sigma", C.c_float), ("forSurfaceReconstruction", C.c_int32),
-        ("kernel", C.c_int32), ("mass_normalize", C.c_int32),
+        ("kernel", C.c_int32), ("mass_normalize", C.c_int32), ("accumulate", C.c_int32),
         ("ao_mode", C.c_int32), ("ao_volume", C.c_int32), ("ao_volume_scale", C.c_float), ("ao_cones", C.c_int32),
         ("ao_steps", C.c_int32), ("ao_levels", C.c_int32), ("ao_apex_deg", C.c_float), ("ao_offset", C.c_float),
         ("ao_strength", C.c_float), ("ao_cone_length", C.c_float), ("ao_early_exit", C.c_int32),

@@ -27,10 +27,10 @@ def ctx():
 
 
 def run(ctx, lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0, kernel=p2v.KERNEL_BUMP, mass=False,
-        out=None):
+        out=None, accumulate=p2v.ACCUM_EXACT):
     ctx.set_params(sizex=int(res[0]), sizey=int(res[1]), sizez=int(res[2]), cyclX=int(cyclic[0]),
                    cyclY=int(cyclic[1]), cyclZ=int(cyclic[2]), normalize=int(bool(normalize)), sigma=float(sigma),
-                   kernel=kernel, mass_normalize=int(mass), forSurfaceReconstruction=0)
+                   kernel=kernel, mass_normalize=int(mass), forSurfaceReconstruction=0, accumulate=accumulate)
     if out is None:
         out = np.full(int(res[0]) * int(res[1]) * int(res[2]), np.nan, np.float32)
     meta = ctx.run_frame(lists, bbox, out)
@@ -49,10 +49,15 @@ def golden_lists(c):
                              global_radius=L["radius"]) for L in c["lists"]]
 
 
+ACCUM = [p2v.ACCUM_EXACT, p2v.ACCUM_KAHAN]
+
+
+@pytest.mark.parametrize("accumulate", ACCUM)
 @pytest.mark.parametrize("name", G.golden_names())
-def test_golden_vs_reference_and_fp64(ctx, name):
+def test_golden_vs_reference_and_fp64(ctx, name, accumulate):
     c = G.load(name)
-    vol, meta = run(ctx, golden_lists(c), c["bbox"], c["res"], c["cyclic"], bool(c["normalize"]), float(c["sigma"]))
+    vol, meta = run(ctx, golden_lists(c), c["bbox"], c["res"], c["cyclic"], bool(c["normalize"]), float(c["sigma"]),
+                    accumulate=accumulate)
     ref = c["volume"]
     xyzr = G.case_xyzr(c)
     v64 = oracle.density_f64(xyzr, c["bbox"], c["res"], c["cyclic"], float(c["sigma"]), oracle.BUMP, NT)
@@ -68,12 +73,19 @@ def test_golden_vs_reference_and_fp64(ctx, name):
         assert abs(meta["max_value"] - float(c["max_value"])) <= 2e-5 * abs(float(c["max_value"]))
 
 
-def test_deterministic_bitwise(ctx):
+@pytest.mark.parametrize("accumulate", ACCUM)
+def test_deterministic_bitwise(ctx, accumulate):
     f = synth.uniform(n=200_000, edge=60.0, res=96, seed=3)
     L = [p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)]
-    a, _ = run(ctx, L, f.bbox, f.res)
-    b, _ = run(ctx, L, f.bbox, f.res)
+    a, _ = run(ctx, L, f.bbox, f.res, accumulate=accumulate)
+    b, _ = run(ctx, L, f.bbox, f.res, accumulate=accumulate)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    # the exact mode is independent of the particle order: shuffle the input and compare bitwise
+    if accumulate == p2v.ACCUM_EXACT:
+        perm = np.random.default_rng(0).permutation(f.n)
+        c, _ = run(ctx, [p2v.ParticleList(np.ascontiguousarray(f.xyzr[perm]), p2v.VERTDATA_FLOAT_XYZR)], f.bbox,
+                   f.res, accumulate=accumulate)
+        assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
 
 
 def test_device_buffers_match_host_buffers(ctx):
@@ -126,7 +138,8 @@ def test_empty_frame(ctx):
     assert np.all(np.isnan(vol))
 
 
-def test_out_of_box_particles_open_and_cyclic(ctx):
+@pytest.mark.parametrize("accumulate", ACCUM)
+def test_out_of_box_particles_open_and_cyclic(ctx, accumulate):
     rng = np.random.default_rng(8)
     x = np.zeros((8000, 4), np.float32)
     x[:, :3] = rng.uniform(-6, 26, size=(8000, 3))
@@ -134,7 +147,7 @@ def test_out_of_box_particles_open_and_cyclic(ctx):
     for cyc in [(0, 0, 0), (1, 1, 1), (0, 1, 0)]:
         for sigma in (1.0, 1.7):
             vol, _ = run(ctx, [p2v.ParticleList(x, p2v.VERTDATA_FLOAT_XYZR)], (0, 0, 0, 20, 20, 20), (21, 18, 23),
-                         cyc, sigma=sigma)
+                         cyc, sigma=sigma, accumulate=accumulate)
             v64 = oracle.density_f64(x, (0, 0, 0, 20, 20, 20), (21, 18, 23), cyc, sigma, oracle.BUMP, NT)
             assert maxrel(vol, v64) <= 1e-6, (cyc, sigma)
 
@@ -154,11 +167,11 @@ def test_surface_reconstruction_box(ctx):
     assert abs(sd[0] - sd[2]) < 0.2 * sd[2]
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_lj_liquid_full_size(ctx, seed):
+@pytest.mark.parametrize("seed,accumulate", [(0, p2v.ACCUM_EXACT), (1, p2v.ACCUM_KAHAN)])
+def test_lj_liquid_full_size(ctx, seed, accumulate):
     """The headline workload at full size (4M particles, 256^3), against the FP64 oracle."""
     f = synth.lj_liquid(seed=2 + seed)
-    vol, meta = run(ctx, [p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, f.res)
+    vol, meta = run(ctx, [p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, f.res, accumulate=accumulate)
     v64 = oracle.density_f64(f.xyzr, f.bbox, f.res, (1, 1, 1), 1.0, oracle.BUMP, NT)
     err = maxrel(vol, v64)
     assert err <= 1e-6, err
