@@ -128,9 +128,28 @@ def profile_traffic(name: str):
     return None
 
 
+AO_PARAMS = dict(ao_mode=1, ao_volume=0, ao_volume_scale=1.0, ao_cones=8, ao_steps=32, ao_levels=3, ao_apex_deg=50.0,
+                 ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1)
+AO_SAMPLE = 50_000  # particles in the CPU AO sample
+
+
+def setup_frame(ctx, f):
+    """Density once (untimed) to derive the workload's normals: unit vectors down the density gradient."""
+    from megamol_gb300 import p2v, synth
+
+    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], cyclX=1, cyclY=1, cyclZ=1, normalize=1, sigma=1.0,
+                   kernel=p2v.KERNEL_BUMP, ao_mode=p2v.AO_NONE)
+    V = f.res[0] * f.res[1] * f.res[2]
+    vol = np.empty(V, np.float32)
+    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
+    nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
+    ctx.set_params(**AO_PARAMS)
+    return vol.reshape(f.res[2], f.res[1], f.res[0]), nrm
+
+
 def cpu_reference_density(f, nthreads: int):
     """Time the reference's CPU density (the compiled ParticlesToDensity module when present, else the
-    FP32 restatement with the same OpenMP structure) on one frame; returns (seconds, kind)."""
+    FP32 restatement with the same OpenMP structure) on one frame; returns (seconds, kind, grid)."""
     import oracle
 
     os.environ["OMP_NUM_THREADS"] = str(nthreads)
@@ -138,11 +157,43 @@ def cpu_reference_density(f, nthreads: int):
         xyzr = np.ascontiguousarray(f.xyzr)
         L = [dict(type=2, data=xyzr, stride=0, radius=0.0, count=f.n)]
         t0 = time.perf_counter()
-        oracle.reference_density(L, f.bbox, f.res, (1, 1, 1), False, 1.0)
-        return time.perf_counter() - t0, "reference"
+        vol, _ = oracle.reference_density(L, f.bbox, f.res, (1, 1, 1), True, 1.0)
+        return time.perf_counter() - t0, "reference", vol
     t0 = time.perf_counter()
-    oracle.density_f32(f.xyzr, f.bbox, f.res, (1, 1, 1), 1.0, oracle.BUMP, nthreads)
-    return time.perf_counter() - t0, "port"
+    vol = oracle.density_f32(f.xyzr, f.bbox, f.res, (1, 1, 1), 1.0, oracle.BUMP, nthreads)
+    vol, _, _ = oracle.normalize_minmax_f32(vol)
+    return time.perf_counter() - t0, "port", vol
+
+
+def cpu_cone_ao(f, grid, nrm, sample: int):
+    """Time the CPU cone march (restatement of the MDAO shader, OpenMP) on `sample` particles; returns
+    seconds for the sample."""
+    import oracle
+
+    h = oracle.spacing_f64(f.bbox, f.res)
+    bmin = [f.bbox[a] - 0.5 * h[a] for a in range(3)]
+    bsize = [f.res[a] * h[a] for a in range(3)]
+    lv = oracle.mip_chain_f64(grid, AO_PARAMS["ao_levels"], AO_PARAMS["ao_volume_scale"])
+    dirs = oracle.cone_dirs(AO_PARAMS["ao_cones"], np.deg2rad(np.float32(AO_PARAMS["ao_apex_deg"])))
+    idx = np.linspace(0, f.n - 1, sample).astype(np.int64)
+    t0 = time.perf_counter()
+    oracle.cone_ao_f64(lv, dirs, f.xyzr[idx], nrm[idx], bmin, bsize, offset=AO_PARAMS["ao_offset"],
+                       strength=AO_PARAMS["ao_strength"], cone_length=AO_PARAMS["ao_cone_length"],
+                       shortest_edge=float(min(f.res)), max_lod=float(AO_PARAMS["ao_levels"] - 1),
+                       steps=AO_PARAMS["ao_steps"], early_exit=1, border=0, sat_scale=AO_PARAMS["ao_volume_scale"])
+    return time.perf_counter() - t0
+
+
+def cpu_pipeline(f, nthreads, grid=None, nrm=None):
+    """CPU particles/s of density + plain cone AO: the density stage on the full frame, the AO stage on a
+    sample of AO_SAMPLE particles scaled to the frame."""
+    from megamol_gb300 import synth
+
+    dt_d, kind, vol = cpu_reference_density(f, nthreads)
+    if nrm is None:
+        nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
+    dt_ao = cpu_cone_ao(f, vol, nrm, AO_SAMPLE) * (f.n / AO_SAMPLE)
+    return f.n / (dt_d + dt_ao), kind, dt_d, dt_ao
 
 
 def run_reference(args):
@@ -151,21 +202,26 @@ def run_reference(args):
         return
     f, desc = make_workload(args.workload)
     nthreads = os.cpu_count() or 1
+    from megamol_gb300 import synth
+
+    _, _, vol = cpu_reference_density(f, nthreads)
+    nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
     for _ in range(max(0, args.warmup)):
-        cpu_reference_density(f, nthreads)
-    times = []
-    kind = "port"
+        cpu_pipeline(f, nthreads, nrm=nrm)
+    vals, kind = [], "port"
+    tot = 0.0
     for _ in range(args.steps):
-        dt, kind = cpu_reference_density(f, nthreads)
-        times.append(dt)
-    tot = sum(times)
+        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm)
+        vals.append(v)
+        tot += dt_d + dt_ao
     value = f.n * args.steps / tot
     line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference", "config": desc,
+            "impl": "reference", "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip"),
             "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": kind,
-                             "sample": f"full frame ({f.n} particles, density only) per step"},
+                             "sample": f"density on the full frame ({f.n} particles) + cone AO on {AO_SAMPLE} "
+                                       "particles scaled to the frame, per step"},
             "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -184,14 +240,15 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     f, desc = make_workload(args.workload, rank)
     ctx = p2v.Context(dev)
-    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], cyclX=1, cyclY=1, cyclZ=1, normalize=0, sigma=1.0,
-                   kernel=p2v.KERNEL_BUMP)
+    grid0, nrm = setup_frame(ctx, f)
     V = f.res[0] * f.res[1] * f.res[2]
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     d_in = torch.from_numpy(f.xyzr).to(dev)
+    d_nrm = torch.from_numpy(nrm).to(dev)
+    d_ao = torch.empty(f.n, dtype=torch.float32, device=dev)
     d_out = torch.empty(V, dtype=torch.float32, device=dev)
-    dev_lists = [p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n)]
+    dev_lists = [p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=d_nrm, ao_out=d_ao)]
 
     def barrier():
         if ws > 1:
@@ -204,9 +261,7 @@ def run_ours(args):
     stage = {"ms_binning": 0.0, "ms_density": 0.0, "ms_normalize": 0.0, "ms_ao": 0.0}
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    gi, _, _ = dist_info()
-    sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(dev)).split(",")[0]) if os.environ.get(
-        "CUDA_VISIBLE_DEVICES", "").replace(",", "").isdigit() else dev)
+    sampler = ClockSampler(dev)
     barrier()
     torch.cuda.synchronize()
     with sampler:
@@ -230,8 +285,10 @@ def run_ours(args):
 
     # ---- end to end through the public API, host buffers ----
     h_in = torch.from_numpy(f.xyzr).pin_memory()
+    h_nrm = torch.from_numpy(nrm).pin_memory()
+    h_ao = torch.empty(f.n, dtype=torch.float32).pin_memory()
     h_out = torch.empty(V, dtype=torch.float32).pin_memory()
-    host_lists = [p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n)]
+    host_lists = [p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=h_nrm, ao_out=h_ao)]
     for _ in range(2):
         ctx.run_frame(host_lists, f.bbox, h_out, stream=sp)
     e2e_steps = max(3, args.steps // 2)
@@ -250,39 +307,50 @@ def run_ours(args):
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * 16),
-           "d2h_bytes_per_step": int(V * 4), "ms_per_step": e2e_ms}
+    e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * (16 + 12)),
+           "d2h_bytes_per_step": int(V * 4 + f.n * 4), "ms_per_step": e2e_ms}
 
-    # ---- roofline of the dominant kernel (density gather) ----
+    # ---- roofline of the dominant kernel ----
     peak, peak_kind = peaks()
     nb = (f.res[0] + 2) * (f.res[1] + 2) * (f.res[2] + 2)
+    per = {k: v / args.steps for k, v in stage.items()}
     gather_bytes = f.n * 16 + V * 4 + nb * 4
-    gather_ms = stage["ms_density"] / args.steps
-    bin_ms = stage["ms_binning"] / args.steps
-    achieved = gather_bytes / (gather_ms * 1e-3) / 1e9
-    traffic = profile_traffic("density_gather_lj_liquid_4M.md") if args.workload == "lj_liquid_4M" else None
-    roofline = {"bound": "hbm", "kernel": "p2v::gather_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes": gather_bytes, "ms_per_launch": gather_ms,
-                "stages_ms": {"binning": bin_ms, "density": gather_ms,
-                              "normalize": stage["ms_normalize"] / args.steps}}
+    lv_bytes, d = 0, list(f.res)
+    for _ in range(AO_PARAMS["ao_levels"]):
+        lv_bytes += d[0] * d[1] * d[2] * 4
+        d = [max(1, x // 2) for x in d]
+    ao_bytes = f.n * (16 + 12 + 4) + lv_bytes
+    if per["ms_ao"] >= per["ms_density"]:
+        dom = ("p2v::cone_ao_kernel (+ mip levels)", ao_bytes, per["ms_ao"], "cone_ao_lj_liquid_4M.md")
+    else:
+        dom = ("p2v::gather_fixed_kernel", gather_bytes, per["ms_density"], "density_gather_lj_liquid_4M.md")
+    achieved = dom[1] / (dom[2] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": profile_traffic(dom[3]) if args.workload == "lj_liquid_4M" else None,
+                "algorithmic_bytes": dom[1], "ms_per_launch": dom[2],
+                "stages_ms": {"binning": per["ms_binning"], "density": per["ms_density"],
+                              "normalize": per["ms_normalize"], "ao": per["ms_ao"]},
+                "density_gather": {"algorithmic_bytes": gather_bytes, "ms": per["ms_density"],
+                                   "frac": gather_bytes / (per["ms_density"] * 1e-3) / 1e9 / peak}}
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu = None
     if rank == 0 and ws == 1:
         nthreads = os.cpu_count() or 1
-        dt, kind = cpu_reference_density(f, nthreads)
-        cpu = {"value": f.n / dt, "unit": "particles/s", "cores": nthreads, "kind": kind,
-               "sample": f"one full frame ({f.n} particles, density only)"}
+        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm)
+        cpu = {"value": v, "unit": "particles/s", "cores": nthreads, "kind": kind,
+               "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + cone AO on {AO_SAMPLE} "
+                         f"particles scaled to the frame ({dt_ao:.2f} s)"}
 
     passes = 4
-    launches_per_step = 1 + 2 + passes + 3 + 2
+    launches_per_step = 2 + 2 + passes + 3 + 1 + 2 + (AO_PARAMS["ao_levels"] - 1) + 1
     if rank == 0:
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(desc, l2="per-step working set ~0.5 GB > 126 MB L2 (no flush)",
-                               stage="density only (AO not yet in the pipeline)"),
+                "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip, gradient normals",
+                               l2="per-step working set ~0.6 GB > 126 MB L2 (no flush)"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)

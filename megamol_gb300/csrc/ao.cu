@@ -1,0 +1,304 @@
+// Per-particle ambient occlusion: the MDAO mip pyramid and cone march, and the AOSphereRenderer volume.
+//
+// Reference shaders (all GLSL, restated here as CUDA; the GL sampler semantics are written out by hand):
+//   mip build   plugins/moldyn_gl/shaders/moldyn_gl/mdao_volume_generator/mdao_mipmap_compute_main.comp.glsl:8-26
+//   cone march  plugins/moldyn_gl/shaders/moldyn_gl/sphere_renderer/inc/mdao_deferred_fragment_ambocc.inc.glsl:9-60
+//   AOSphere    plugins/pwdemos_gl/src/AOSphereRenderer.cpp:918-1021 (deposit), :489-514 (uniforms),
+//               shaders/pwdemos_gl/AOSphere/snippets/mainaxes_vertex_2.glsl:1-9, mainaxes_fragLightAO_evalAO.glsl:1-8,
+//               normals_fragLightAO_evalAO.glsl:1-4
+// AO is evaluated once per particle at its surface point p + r * n along the particle's normal n.
+// Particles are processed in cell-sorted order so neighbouring threads sample neighbouring texels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "ao_internal.h"
+#include "p2v_common.cuh"
+
+namespace p2v {
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// mip pyramid: level l+1 voxel = sum of the children 2g .. min(2g+1, N-1), divided by 8 always
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) mip_level_kernel(const float* __restrict__ src, int sx, int sy, int sz,
+    float* __restrict__ dst, int dx, int dy, int dz, float sat_scale) {
+    const int64_t n = (int64_t) dx * dy * dz;
+    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
+        const int x = (int) (i % dx);
+        const int y = (int) ((i / dx) % dy);
+        const int z = (int) (i / ((int64_t) dx * dy));
+        const int x1 = min(2 * x + 1, sx - 1), y1 = min(2 * y + 1, sy - 1), z1 = min(2 * z + 1, sz - 1);
+        float acc = 0.0f;
+        for (int zz = 2 * z; zz <= z1; ++zz)
+            for (int yy = 2 * y; yy <= y1; ++yy)
+                for (int xx = 2 * x; xx <= x1; ++xx) {
+                    float v = __ldg(src + ((int64_t) zz * sy + yy) * sx + xx);
+                    if (sat_scale > 0.0f)
+                        v = fminf(fmaxf(v * sat_scale, 0.0f), 1.0f);
+                    acc += v;
+                }
+        dst[i] = acc * 0.125f;
+    }
+}
+
+using Level = ConeLevel;
+
+// GL LINEAR filtering with texel centres at (i + 0.5) / N. border: 0 = CLAMP_TO_BORDER (0 outside),
+// 1 = CLAMP_TO_EDGE. sat > 0 saturates level-0 texels (the level-0 texture holds clamp(v*sat, 0, 1)).
+__device__ __forceinline__ float tex_fetch(const Level& L, int x, int y, int z, int border, float sat) {
+    if (border == 0) {
+        if ((unsigned) x >= (unsigned) L.d[0] || (unsigned) y >= (unsigned) L.d[1] || (unsigned) z >= (unsigned) L.d[2])
+            return 0.0f;
+    } else {
+        x = min(max(x, 0), L.d[0] - 1);
+        y = min(max(y, 0), L.d[1] - 1);
+        z = min(max(z, 0), L.d[2] - 1);
+    }
+    float v = __ldg(L.v + ((int64_t) z * L.d[1] + y) * L.d[0] + x);
+    if (sat > 0.0f)
+        v = fminf(fmaxf(v * sat, 0.0f), 1.0f);
+    return v;
+}
+
+__device__ __forceinline__ float trilinear(const Level& L, float ux, float uy, float uz, int border, float sat) {
+    const float cx = ux * L.fd[0] - 0.5f, cy = uy * L.fd[1] - 0.5f, cz = uz * L.fd[2] - 0.5f;
+    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
+    const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
+    const float fx = cx - fx0, fy = cy - fy0, fz = cz - fz0;
+    const float c000 = tex_fetch(L, x0, y0, z0, border, sat), c100 = tex_fetch(L, x0 + 1, y0, z0, border, sat);
+    const float c010 = tex_fetch(L, x0, y0 + 1, z0, border, sat), c110 = tex_fetch(L, x0 + 1, y0 + 1, z0, border, sat);
+    const float c001 = tex_fetch(L, x0, y0, z0 + 1, border, sat), c101 = tex_fetch(L, x0 + 1, y0, z0 + 1, border, sat);
+    const float c011 = tex_fetch(L, x0, y0 + 1, z0 + 1, border, sat);
+    const float c111 = tex_fetch(L, x0 + 1, y0 + 1, z0 + 1, border, sat);
+    const float c00 = c000 + fx * (c100 - c000), c10 = c010 + fx * (c110 - c010);
+    const float c01 = c001 + fx * (c101 - c001), c11 = c011 + fx * (c111 - c011);
+    const float c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
+    return c0 + fz * (c1 - c0);
+}
+
+// Surface point and unit normal of particle `o`.
+__device__ __forceinline__ bool surface_point(const float4 p, const float4 nrm, float x[3], float n[3]) {
+    const float l2 = nrm.x * nrm.x + nrm.y * nrm.y + nrm.z * nrm.z;
+    if (!(l2 > 0.0f))
+        return false;
+    const float il = rsqrtf(l2);
+    n[0] = nrm.x * il;
+    n[1] = nrm.y * il;
+    n[2] = nrm.z * il;
+    x[0] = p.x + p.w * n[0];
+    x[1] = p.y + p.w * n[1];
+    x[2] = p.z + p.w * n[2];
+    return true;
+}
+
+__global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, float* __restrict__ ao) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t o = order ? order[i] : i;
+    const float4 p = xyzr[o];
+    const float4 nv = nrm[o];
+    float x[3], nn[3];
+    if (!surface_point(p, nv, x, nn)) {
+        ao[o] = 1.0f;  // no normal: no occlusion
+        return;
+    }
+    // frame (mdao_deferred_fragment_ambocc.inc.glsl:18-21): new_y = n, new_x = cross(n, normalize(objPos)),
+    // new_z = cross(new_x, new_y)
+    float xn[3] = {x[0], x[1], x[2]};
+    const float xl2 = xn[0] * xn[0] + xn[1] * xn[1] + xn[2] * xn[2];
+    if (xl2 > 0.0f) {
+        const float il = rsqrtf(xl2);
+        xn[0] *= il;
+        xn[1] *= il;
+        xn[2] *= il;
+    } else {
+        xn[0] = 1.0f;
+        xn[1] = xn[2] = 0.0f;
+    }
+    const float ex[3] = {nn[1] * xn[2] - nn[2] * xn[1], nn[2] * xn[0] - nn[0] * xn[2], nn[0] * xn[1] - nn[1] * xn[0]};
+    const float ez[3] = {ex[1] * nn[2] - ex[2] * nn[1], ex[2] * nn[0] - ex[0] * nn[2], ex[0] * nn[1] - ex[1] * nn[0]};
+    const float u[3] = {(x[0] - cp.bmin[0]) * cp.ibsize[0], (x[1] - cp.bmin[1]) * cp.ibsize[1],
+                        (x[2] - cp.bmin[2]) * cp.ibsize[2]};
+    float ambient = 0.0f;
+    for (int c = 0; c < cp.ncones; ++c) {
+        const float4 cd = cp.dirs[c];
+        const float dir[3] = {ex[0] * cd.x + nn[0] * cd.y + ez[0] * cd.z, ex[1] * cd.x + nn[1] * cd.y + ez[1] * cd.z,
+                              ex[2] * cd.x + nn[2] * cd.y + ez[2] * cd.z};
+        float acc = 0.0f;
+        for (int k = 0; k < cp.nsteps; ++k) {
+            const float t = cp.t[k];
+            const float lod = cp.lod[k];
+            const float qx = u[0] + t * dir[0], qy = u[1] + t * dir[1], qz = u[2] + t * dir[2];
+            const int l0 = min((int) lod, cp.nlevels - 1);
+            const float fr = lod - (float) l0;
+            float vis = trilinear(cp.lv[l0], qx, qy, qz, cp.border, l0 == 0 ? cp.sat : 0.0f);
+            if (fr > 0.0f && l0 + 1 < cp.nlevels)
+                vis = (1.0f - fr) * vis + fr * trilinear(cp.lv[l0 + 1], qx, qy, qz, cp.border, 0.0f);
+            acc += (1.0f - acc) * vis;
+            if (cp.early_exit && acc > 0.99f)
+                break;
+        }
+        ambient += acc;
+    }
+    ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+}
+
+// ---------------------------------------------------------------------------------------------
+// AOSphere volume: nearest inner voxel, (4/3 pi r^3 / voxel volume) * genFac, summed exactly in
+// 64-bit fixed point (2^-32) so the result does not depend on the particle order.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) aosphere_deposit_kernel(const AOSphereParams ap, const float4* __restrict__ xyzr,
+    uint32_t n, unsigned long long* __restrict__ acc) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const float4 p = xyzr[i];
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(p.w) && p.w > 0.0f))
+        return;
+    const float pc[3] = {p.x, p.y, p.z};
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // AOSphereRenderer.cpp:964-980: int(((p - min) / range) * s_inner), clamped to [0, s_inner - 1]
+        const float q = ((pc[a] - ap.minOS[a]) / ap.rangeOS[a]) * static_cast<float>(ap.si[a]);
+        int v = (int) fminf(fmaxf(q, -2147483520.0f), 2147483520.0f);
+        c[a] = v < 0 ? 0 : (v >= ap.si[a] ? ap.si[a] - 1 : v);
+    }
+    const float spVol = 4.0f / 3.0f * 3.14159265358979f * p.w * p.w * p.w;
+    const float val = (spVol / ap.voxel_vol) * ap.gen_fac;
+    const int64_t idx = (c[0] + 1) + ((int64_t) (c[1] + 1) + (int64_t) (c[2] + 1) * ap.s[1]) * ap.s[0];
+    atomicAdd(acc + idx, (unsigned long long) __float2ull_rn(val * 4294967296.0f));
+}
+
+__global__ void __launch_bounds__(256) fixed_to_float_kernel(const unsigned long long* __restrict__ acc, int64_t n,
+    float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x)
+        out[i] = (float) ((double) acc[i] * 2.3283064365386963e-10);
+}
+
+__global__ void __launch_bounds__(128) aosphere_ao_kernel(const AOSphereParams ap, const float* __restrict__ tex,
+    const uint32_t* __restrict__ order, const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n,
+    int mode, float* __restrict__ ao) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t o = order ? order[i] : i;
+    const float4 p = xyzr[o];
+    const float4 nv = nrm[o];
+    float x[3], nn[3];
+    if (!surface_point(p, nv, x, nn)) {
+        ao[o] = 1.0f;
+        return;
+    }
+    Level T;
+    T.v = tex;
+    for (int a = 0; a < 3; ++a) {
+        T.d[a] = ap.s[a];
+        T.fd[a] = (float) ap.s[a];
+    }
+    if (mode == 0) {
+        // taps at p +- (r + aoSampDist) along each axis, combined by n^2 (main axes)
+        const float pc[3] = {p.x, p.y, p.z};
+        float aop[3], aod[3];
+        for (int a = 0; a < 3; ++a) {
+            aop[a] = (pc[a] - ap.origin[a]) / ap.ext[a];
+            aod[a] = (p.w + ap.sampd[a]) / ap.ext[a];
+        }
+        float acc = 0.0f;
+        for (int a = 0; a < 3; ++a) {
+            float q[3] = {aop[0], aop[1], aop[2]};
+            q[a] += nn[a] > 0.0f ? aod[a] : -aod[a];
+            const float tap = 1.0f - trilinear(T, q[0], q[1], q[2], 1, 0.0f) * ap.eval_fac;
+            acc += nn[a] * nn[a] * tap;
+        }
+        ao[o] = acc;
+    } else {
+        float q[3];
+        for (int a = 0; a < 3; ++a)
+            q[a] = (x[a] + nn[a] * ap.sampd[a] - ap.origin[a]) / ap.ext[a];
+        ao[o] = 1.0f - trilinear(T, q[0], q[1], q[2], 1, 0.0f) * ap.eval_fac;
+    }
+}
+
+__global__ void __launch_bounds__(256) pack_normals_kernel(const uint8_t* __restrict__ src, uint32_t stride,
+    uint64_t count, uint64_t offset, float4* __restrict__ nrm, int aligned) {
+    const uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+    if (i >= count)
+        return;
+    const uint8_t* r = src + i * stride;
+    float v[3];
+    if (aligned) {
+        const float* f = reinterpret_cast<const float*>(r);
+        v[0] = f[0];
+        v[1] = f[1];
+        v[2] = f[2];
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            uint32_t b = (uint32_t) r[4 * c] | ((uint32_t) r[4 * c + 1] << 8) | ((uint32_t) r[4 * c + 2] << 16) |
+                         ((uint32_t) r[4 * c + 3] << 24);
+            v[c] = __uint_as_float(b);
+        }
+    }
+    nrm[offset + i] = make_float4(v[0], v[1], v[2], 0.0f);
+}
+
+}  // namespace
+
+cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int nlevels, float* const* out,
+    int (*dims)[3], int sms, cudaStream_t st) {
+    const float* src = l0;
+    int sd[3] = {d0[0], d0[1], d0[2]};
+    for (int l = 1; l < nlevels; ++l) {
+        int dd[3] = {max(1, sd[0] / 2), max(1, sd[1] / 2), max(1, sd[2] / 2)};
+        const int64_t nv = (int64_t) dd[0] * dd[1] * dd[2];
+        const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((nv + 255) / 256, (int64_t) sms * 32));
+        mip_level_kernel<<<grd, 256, 0, st>>>(src, sd[0], sd[1], sd[2], out[l], dd[0], dd[1], dd[2],
+                                              l == 1 ? sat_scale : 0.0f);
+        for (int a = 0; a < 3; ++a)
+            dims[l][a] = dd[a];
+        src = out[l];
+        for (int a = 0; a < 3; ++a)
+            sd[a] = dd[a];
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
+    uint32_t n, float* ao, cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, ao);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc, float* tex, const uint32_t* order, const float4* nrm, int mode, float* ao,
+    int sms, cudaStream_t st) {
+    const int64_t nv = (int64_t) ap.s[0] * ap.s[1] * ap.s[2];
+    cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * nv, st);
+    if (e != cudaSuccess)
+        return e;
+    if (n > 0)
+        aosphere_deposit_kernel<<<ceil_div(n, 256), 256, 0, st>>>(ap, xyzr, n, acc);
+    const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((nv + 255) / 256, (int64_t) sms * 16));
+    fixed_to_float_kernel<<<grd, 256, 0, st>>>(acc, nv, tex);
+    if (n > 0)
+        aosphere_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(ap, tex, order, xyzr, nrm, n, mode, ao);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,
+    cudaStream_t st) {
+    if (count == 0)
+        return cudaSuccess;
+    const int aligned = (reinterpret_cast<uintptr_t>(src) % 4 == 0) && (stride % 4 == 0);
+    pack_normals_kernel<<<(unsigned) ((count + 255) / 256), 256, 0, st>>>(static_cast<const uint8_t*>(src), stride,
+                                                                         count, offset, nrm, aligned);
+    return cudaGetLastError();
+}
+
+}  // namespace p2v

@@ -1,0 +1,49 @@
+// Internal interfaces of the AO stage of libp2v (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace p2v {
+
+constexpr int MAX_CONES = 16;
+constexpr int MAX_STEPS = 256;
+constexpr int MAX_LEVELS = 12;
+
+struct ConeLevel {
+    const float* v;
+    int d[3];
+    float fd[3];
+};
+
+// Everything the cone march needs, passed by value (kernel parameter space).
+struct ConeParams {
+    float bmin[3], ibsize[3];      // volume bounds (normalised coordinates u = (x - bmin) * ibsize)
+    float strength;
+    float sat;                     // level-0 texel = clamp(v * sat, 0, 1); 0 = raw
+    int border;                    // 0 = CLAMP_TO_BORDER, 1 = CLAMP_TO_EDGE
+    int early_exit;
+    int ncones, nsteps, nlevels;
+    float4 dirs[MAX_CONES];        // xyz around +Y, w = cone width
+    float t[MAX_STEPS], lod[MAX_STEPS];
+    ConeLevel lv[MAX_LEVELS];
+};
+
+struct AOSphereParams {
+    int s[3], si[3];               // texture size with border, inner size
+    float minOS[3], rangeOS[3];    // clip box
+    float voxel_vol, gen_fac, eval_fac;
+    float origin[3], ext[3], sampd[3];  // posOrigin, posExtents, aoSampDist
+};
+
+cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int nlevels, float* const* out,
+    int (*dims)[3], int sms, cudaStream_t st);
+cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
+    uint32_t n, float* ao, cudaStream_t st);
+cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc,
+    float* tex, const uint32_t* order, const float4* nrm, int mode, float* ao, int sms, cudaStream_t st);
+cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,
+    cudaStream_t st);
+
+}  // namespace p2v

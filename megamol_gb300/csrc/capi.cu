@@ -15,6 +15,7 @@
 
 #include "../../include/p2v.h"
 #include "p2v_common.cuh"
+#include "ao_internal.h"
 #include "p2v_internal.h"
 
 using namespace p2v;
@@ -63,6 +64,7 @@ struct p2v_ctx {
     uint64_t datahash = 0;
 
     DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
+    DevBuf nrm, ao, mips, aos_acc, aos_tex;
     FrameScalars* h_scal = nullptr;  // pinned mirror
     cudaEvent_t ev[EV_COUNT] = {};
     const float* last_grid = nullptr;
@@ -79,6 +81,8 @@ struct p2v_ctx {
     }
 
     p2v_status run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st);
+    p2v_status run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
+                      const uint32_t* order, cudaStream_t st);
 };
 
 namespace {
@@ -110,6 +114,49 @@ void modify_bbox(float bb[6], int32_t& sx, int32_t& sy, int32_t sz) {
     bb[3] = maxOSx + (newWidth - rangeOSx) / 2;
     bb[4] = maxOSy + (newHeight - rangeOSy) / 2;
     bb[5] = maxOSz + (newDepth - rangeOSz) / 2;
+}
+
+// SphereRenderer::generate3ConeDirections (SphereRenderer.cpp:2572-2587) for K = 3; other K use the
+// same ring construction with the circumradius of a regular K-gon of that edge length.
+void cone_directions(int K, float apex, float4* out) {
+    const float edge = 2.0f * std::tan(0.5f * apex);
+    const float height = std::sqrt(1.0f - edge * edge / 12.0f);
+    const float radius = K == 3 ? std::sqrt(3.0f) / 3.0f * edge : edge / (2.0f * std::sin(3.14159265358979f / K));
+    for (int i = 0; i < K; ++i) {
+        const float angle = static_cast<float>(i) / static_cast<float>(K) * 2.0f * 3.14159265358979f;
+        float c[3] = {std::cos(angle) * radius, height, std::sin(angle) * radius};
+        const float l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        out[i] = make_float4(c[0] / l, c[1] / l, c[2] / l, edge);
+    }
+}
+
+// Sample distances and mip levels along a cone (mdao_deferred_fragment_ambocc.inc.glsl:35-51): t starts at
+// offset + 1e-4 and grows by t*w until cone_length, or (steps > 0) follows a geometric sequence of that
+// many samples ending below cone_length. lod = clamp(log2(t * w * shortestEdge), 0, maxLod).
+int cone_steps(float offset, float cone_length, int steps, float w, float shortest, float max_lod, float* t,
+               float* lod, int cap) {
+    int n = 0;
+    float tt = offset + 0.0001f;
+    float gq = 0.0f;
+    if (steps > 0)
+        gq = std::pow(cone_length / tt, 1.0f / static_cast<float>(steps));
+    while (n < cap) {
+        float l = std::log2(tt * w * shortest);
+        l = std::min(std::max(l, 0.0f), max_lod);
+        t[n] = tt;
+        lod[n] = l;
+        ++n;
+        if (steps > 0) {
+            if (n >= steps)
+                break;
+            tt = tt * gq;
+        } else {
+            tt += tt * w;
+            if (!(tt < cone_length))
+                break;
+        }
+    }
+    return n;
 }
 
 uint32_t record_bytes(int type) {
@@ -244,6 +291,10 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
             continue;
         const uint32_t stride = L.vertex_stride ? L.vertex_stride : record_bytes(L.vertex_type);
         raw_need += (L.count - 1) * (uint64_t) stride + record_bytes(L.vertex_type) + 16;
+        if (P.ao_mode != P2V_AO_NONE && L.normals != nullptr) {
+            const uint32_t ns = L.normal_stride ? L.normal_stride : 12u;
+            raw_need += (L.count - 1) * (uint64_t) ns + 12 + 16;
+        }
     }
     if (raw_need)
         P2V_CUDA_TRY(raw.ensure(raw_need));
@@ -279,6 +330,37 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     }
     if (N == 0)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
+    // ---- normals for AO ----
+    const bool want_ao = P.ao_mode != P2V_AO_NONE;
+    if (want_ao) {
+        P2V_CUDA_TRY(nrm.ensure(sizeof(float4) * (N + 1)));
+        P2V_CUDA_TRY(ao.ensure(sizeof(float) * (N + 1)));
+        uint64_t noff = 0;
+        for (uint32_t l = 0; l < fr->list_count; ++l) {
+            const p2v_particle_list& L = fr->lists[l];
+            if (L.vertex_type == P2V_VERTDATA_NONE)
+                continue;
+            if (L.count > 0 && L.normals == nullptr)
+                return fail(P2V_EINVAL, "list %u: AO needs per-particle normals", l);
+            if (L.count > 0) {
+                const uint32_t ns = L.normal_stride ? L.normal_stride : 12u;
+                if (ns < 12u)
+                    return fail(P2V_EINVAL, "list %u: normal stride %u < 12", l, ns);
+                const void* src = L.normals;
+                if (L.mem != P2V_MEM_DEVICE) {
+                    const uint64_t bytes = (L.count - 1) * (uint64_t) ns + 12;
+                    P2V_CUDA_TRY(raw.ensure(raw_off + bytes + 16));
+                    // raw may have been reallocated: only grow it before any upload is queued
+                    uint8_t* dst = raw.as<uint8_t>() + raw_off;
+                    P2V_CUDA_TRY(cudaMemcpyAsync(dst, L.normals, bytes, cudaMemcpyHostToDevice, st));
+                    src = dst;
+                    raw_off += (bytes + 15) & ~uint64_t(15);
+                }
+                P2V_CUDA_TRY(launch_pack_normals(src, ns, L.count, noff, nrm.as<float4>(), st));
+            }
+            noff += L.count;
+        }
+    }
 
     // ---- sort + cell starts ----
     SortBuffers sb{};
@@ -312,12 +394,30 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume, st));
     P2V_CUDA_TRY(launch_normalize_modes(dgrid, V, fs, P.mass_normalize, P.normalize, sms, st));
     P2V_CUDA_TRY(cudaEventRecord(ev[EV_NORM], st));
+    if (want_ao) {
+        const p2v_status as = run_ao(fr, g, dgrid, bb, n, sb.vals[sb.result], st);
+        if (as != P2V_OK)
+            return as;
+    }
     P2V_CUDA_TRY(cudaEventRecord(ev[EV_AO], st));
 
     // ---- outputs ----
     if (vol && vol->data && !direct)
         P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * V,
                                      vol->mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (want_ao) {
+        uint64_t aoff = 0;
+        for (uint32_t l = 0; l < fr->list_count; ++l) {
+            const p2v_particle_list& L = fr->lists[l];
+            if (L.vertex_type == P2V_VERTDATA_NONE)
+                continue;
+            if (L.ao_out && L.count > 0)
+                P2V_CUDA_TRY(cudaMemcpyAsync(L.ao_out, ao.as<float>() + aoff, sizeof(float) * L.count,
+                                             L.mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                             st));
+            aoff += L.count;
+        }
+    }
     P2V_CUDA_TRY(cudaMemcpyAsync(h_scal, fs, sizeof(FrameScalars), cudaMemcpyDeviceToHost, st));
     P2V_CUDA_TRY(cudaEventRecord(ev[EV_DOWN], st));
     P2V_CUDA_TRY(cudaStreamSynchronize(st));
@@ -373,6 +473,99 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
         return fail(P2V_EDOMAIN, "input outside the supported domain (device error 0x%x)", hs.error);
     err.clear();
     return P2V_OK;
+}
+
+p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
+                           const uint32_t* order, cudaStream_t st) {
+    const p2v_params& P = prm;
+    if (P.ao_mode == P2V_AO_CONE) {
+        if (P.ao_volume != P2V_AOVOL_DENSITY)
+            return fail(P2V_EUNSUPPORTED, "ao_volume %d is not implemented for the cone march", P.ao_volume);
+        if (P.ao_cones < 1 || P.ao_cones > MAX_CONES)
+            return fail(P2V_EINVAL, "ao_cones must lie in [1, %d]", MAX_CONES);
+        ConeParams cp{};
+        int smax = std::max(g.s[0], std::max(g.s[1], g.s[2]));
+        int smin = std::min(g.s[0], std::min(g.s[1], g.s[2]));
+        int L = P.ao_levels > 0 ? P.ao_levels : (int) std::ceil(std::log2((double) smax));
+        L = std::max(1, std::min(L, MAX_LEVELS));
+        // the density grid is node-centred: as a texture it spans [min - h/2, max + h/2]
+        for (int a = 0; a < 3; ++a) {
+            const double hd = std::fabs((double) bb[a + 3] - (double) bb[a]) / (double) (g.s[a] - 1);
+            cp.bmin[a] = (float) ((double) bb[a] - 0.5 * hd);
+            cp.ibsize[a] = (float) (1.0 / (g.s[a] * hd));
+        }
+        cp.strength = P.ao_strength;
+        cp.sat = P.ao_volume_scale;
+        cp.border = 0;  // CLAMP_TO_BORDER (MDAOVolumeGenerator.cpp:58-60)
+        cp.early_exit = P.ao_early_exit ? 1 : 0;
+        cp.ncones = P.ao_cones;
+        cone_directions(P.ao_cones, P.ao_apex_deg * 3.14159265358979f / 180.0f, cp.dirs);
+        cp.nsteps = cone_steps(P.ao_offset, P.ao_cone_length, P.ao_steps, cp.dirs[0].w, (float) smin,
+                               (float) (L - 1), cp.t, cp.lod, MAX_STEPS);
+        if (P.ao_steps > MAX_STEPS || (P.ao_steps <= 0 && cp.nsteps >= MAX_STEPS))
+            return fail(P2V_EUNSUPPORTED, "more than %d samples per cone", MAX_STEPS);
+        cp.nlevels = L;
+        // level 0 is the density grid itself (saturated on the fly); levels 1.. are built here
+        size_t need = 0;
+        int d[MAX_LEVELS][3];
+        for (int a = 0; a < 3; ++a)
+            d[0][a] = g.s[a];
+        for (int l = 1; l < L; ++l) {
+            for (int a = 0; a < 3; ++a)
+                d[l][a] = std::max(1, d[l - 1][a] / 2);
+            need += (size_t) d[l][0] * d[l][1] * d[l][2];
+        }
+        P2V_CUDA_TRY(mips.ensure(sizeof(float) * (need + 1)));
+        float* lvp[MAX_LEVELS];
+        lvp[0] = const_cast<float*>(dgrid);
+        size_t off = 0;
+        for (int l = 1; l < L; ++l) {
+            lvp[l] = mips.as<float>() + off;
+            off += (size_t) d[l][0] * d[l][1] * d[l][2];
+        }
+        int dims[MAX_LEVELS][3];
+        P2V_CUDA_TRY(launch_mip_levels(dgrid, g.s, cp.sat, L, lvp, dims, sms, st));
+        for (int l = 0; l < L; ++l) {
+            cp.lv[l].v = lvp[l];
+            for (int a = 0; a < 3; ++a) {
+                cp.lv[l].d[a] = d[l][a];
+                cp.lv[l].fd[a] = (float) d[l][a];
+            }
+        }
+        P2V_CUDA_TRY(launch_cone_ao(cp, order, xyzr.as<float4>(), nrm.as<float4>(), n, ao.as<float>(), st));
+        return P2V_OK;
+    }
+    if (P.ao_mode == P2V_AO_AOSPHERE_AXES || P.ao_mode == P2V_AO_AOSPHERE_NORMAL) {
+        AOSphereParams ap{};
+        const int sz3[3] = {P.aos_sizex, P.aos_sizey, P.aos_sizez};
+        for (int a = 0; a < 3; ++a) {
+            if (sz3[a] < 3 || sz3[a] > 2048)
+                return fail(P2V_EINVAL, "aos_size%c must lie in [3, 2048]", "xyz"[a]);
+            ap.s[a] = sz3[a];
+            ap.si[a] = sz3[a] - 2;
+            ap.minOS[a] = fr->clipbox[a];
+            ap.rangeOS[a] = std::fabs(fr->clipbox[a + 3] - fr->clipbox[a]);
+            if (!(ap.rangeOS[a] > 0.0f))
+                return fail(P2V_EINVAL, "clip box has zero extent along %c", "xyz"[a]);
+            // AOSphereRenderer.cpp:496-513
+            const float ext = ap.rangeOS[a] / (1.0f - 2.0f / static_cast<float>(sz3[a]));
+            ap.ext[a] = ext;
+            ap.origin[a] = ap.minOS[a] - ext / static_cast<float>(sz3[a]);
+            ap.sampd[a] = P.aos_step_len * (ap.rangeOS[a] / static_cast<float>(sz3[a]));
+        }
+        ap.voxel_vol = (ap.rangeOS[0] / static_cast<float>(ap.si[0])) * (ap.rangeOS[1] / static_cast<float>(ap.si[1])) *
+                       (ap.rangeOS[2] / static_cast<float>(ap.si[2]));
+        ap.gen_fac = P.aos_gen_fac;
+        ap.eval_fac = P.aos_eval_fac;
+        const size_t nv = (size_t) ap.s[0] * ap.s[1] * ap.s[2];
+        P2V_CUDA_TRY(aos_acc.ensure(sizeof(unsigned long long) * nv));
+        P2V_CUDA_TRY(aos_tex.ensure(sizeof(float) * nv));
+        P2V_CUDA_TRY(launch_aosphere(ap, xyzr.as<float4>(), n, aos_acc.as<unsigned long long>(), aos_tex.as<float>(),
+                                     order, nrm.as<float4>(), P.ao_mode == P2V_AO_AOSPHERE_AXES ? 0 : 1,
+                                     ao.as<float>(), sms, st));
+        return P2V_OK;
+    }
+    return fail(P2V_EUNSUPPORTED, "ao_mode %d is not implemented", P.ao_mode);
 }
 
 extern "C" {
@@ -448,7 +641,8 @@ void p2v_destroy(p2v_ctx* c) {
     if (c->own_stream)
         cudaStreamSynchronize(c->own_stream);
     for (DevBuf* b : {&c->raw, &c->xyzr, &c->rec_a, &c->rec_b, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
-                      &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal})
+                      &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal, &c->nrm, &c->ao, &c->mips,
+                      &c->aos_acc, &c->aos_tex})
         b->release();
     for (auto& e : c->ev)
         if (e)

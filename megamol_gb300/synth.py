@@ -138,3 +138,45 @@ def random_normals(n: int, seed: int = 7) -> np.ndarray:
     v = rng.normal(size=(n, 3))
     v /= np.linalg.norm(v, axis=1, keepdims=True)
     return v.astype(np.float32)
+
+
+def gradient_normals(xyzr: np.ndarray, grid: np.ndarray, bbox, cyclic=True, seed: int = 11) -> np.ndarray:
+    """Unit normals pointing down the local density gradient (outward from dense regions): -grad(rho)
+    by central differences on the node grid (periodic when `cyclic`), trilinearly interpolated at each
+    particle. Particles where the gradient vanishes get a seeded random direction."""
+    g = np.asarray(grid, np.float32)
+    sz, sy, sx = g.shape
+    lo = np.array(bbox[:3], np.float64)
+    hi = np.array(bbox[3:], np.float64)
+    h = (hi - lo) / (np.array([sx, sy, sz]) - 1)
+    grads = []
+    for axis, ha in ((2, h[0]), (1, h[1]), (0, h[2])):
+        if cyclic:
+            d = (np.roll(g, -1, axis) - np.roll(g, 1, axis)) / (2 * ha)
+        else:
+            d = np.gradient(g, ha, axis=axis)
+        grads.append(d.astype(np.float32))
+    u = (xyzr[:, :3].astype(np.float64) - lo) / h
+    u = np.clip(u, 0, np.array([sx, sy, sz]) - 1 - 1e-6)
+    i0 = np.floor(u).astype(np.int64)
+    f = (u - i0).astype(np.float32)
+    i1 = np.minimum(i0 + 1, np.array([sx, sy, sz]) - 1)
+    out = np.zeros((xyzr.shape[0], 3), np.float32)
+    for c, G in enumerate(grads):
+        acc = np.zeros(xyzr.shape[0], np.float32)
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    w = (f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1]) * \
+                        (f[:, 2] if dz else 1 - f[:, 2])
+                    ix = i1[:, 0] if dx else i0[:, 0]
+                    iy = i1[:, 1] if dy else i0[:, 1]
+                    iz = i1[:, 2] if dz else i0[:, 2]
+                    acc += w * G[iz, iy, ix]
+        out[:, c] = -acc
+    n = np.linalg.norm(out, axis=1, keepdims=True)
+    bad = (n[:, 0] <= 1e-12) | ~np.isfinite(n[:, 0])
+    if bad.any():
+        out[bad] = random_normals(int(bad.sum()), seed)
+        n[bad] = 1.0
+    return (out / n).astype(np.float32)

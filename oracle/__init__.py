@@ -45,7 +45,7 @@ class _ConeParams(C.Structure):
         ("bounds_min", C.c_float * 3), ("bounds_size", C.c_float * 3),
         ("offset", C.c_float), ("strength", C.c_float), ("cone_length", C.c_float),
         ("shortest_edge", C.c_float), ("max_lod", C.c_float),
-        ("steps", C.c_int32), ("early_exit", C.c_int32), ("border", C.c_int32),
+        ("steps", C.c_int32), ("early_exit", C.c_int32), ("border", C.c_int32), ("sat_scale", C.c_float),
     ]
 
 
@@ -65,6 +65,15 @@ def lib() -> C.CDLL:
         f.p2vo_normalize_minmax_f32.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_float),
                                                 C.POINTER(C.c_float)]
         f.p2vo_mip_step_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32)]
+        f.p2vo_cone_dirs.argtypes = [C.c_int, C.c_float, C.c_void_p]
+        f.p2vo_cone_steps.argtypes = [C.POINTER(_ConeParams), C.c_float, C.c_void_p, C.c_void_p, C.c_int]
+        f.p2vo_cone_steps.restype = C.c_int
+        f.p2vo_cone_ao_f64.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_int32), C.c_int, C.c_void_p, C.c_int,
+                                       C.POINTER(_ConeParams), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        f.p2vo_aosphere_volume_f64.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                                               C.c_float, C.c_void_p]
+        f.p2vo_aosphere_ao_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float,
+                                           C.c_float, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
     return _lib
 
 
@@ -225,3 +234,81 @@ def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma
                 extents=list(res_out.extents), min_value=res_out.min_value, max_value=res_out.max_value,
                 millis=res_out.millis)
     return vol, meta
+
+
+# ------------------------------------------------------------------------------------------------
+# AO restatements
+# ------------------------------------------------------------------------------------------------
+def cone_dirs(k: int, apex_rad: float) -> np.ndarray:
+    out = np.zeros((k, 4), np.float32)
+    lib().p2vo_cone_dirs(k, float(apex_rad), out.ctypes.data)
+    return out
+
+
+def _cone_params(bounds_min, bounds_size, offset=0.01, strength=1.0, cone_length=0.8, shortest_edge=128.0,
+                 max_lod=6.0, steps=0, early_exit=1, border=0, sat_scale=0.0) -> _ConeParams:
+    cp = _ConeParams()
+    cp.bounds_min[:] = [float(v) for v in bounds_min]
+    cp.bounds_size[:] = [float(v) for v in bounds_size]
+    cp.offset, cp.strength, cp.cone_length = float(offset), float(strength), float(cone_length)
+    cp.shortest_edge, cp.max_lod = float(shortest_edge), float(max_lod)
+    cp.steps, cp.early_exit, cp.border, cp.sat_scale = int(steps), int(early_exit), int(border), float(sat_scale)
+    return cp
+
+
+def cone_steps(w: float, **kw):
+    cp = _cone_params((0, 0, 0), (1, 1, 1), **kw)
+    t = np.zeros(1024, np.float32)
+    lod = np.zeros(1024, np.float32)
+    n = lib().p2vo_cone_steps(C.byref(cp), float(w), t.ctypes.data, lod.ctypes.data, 1024)
+    return t[:n], lod[:n]
+
+
+def mip_chain_f64(l0: np.ndarray, nlevels: int, sat_scale: float = 0.0):
+    """Levels 0..nlevels-1 of the MDAO pyramid. Level 0 is returned raw (cone_ao_f64 saturates it with
+    the same sat_scale); level 1 is built from the saturated texels clamp(v*scale, 0, 1)."""
+    raw = np.asarray(l0, np.float64)
+    base = np.clip(raw * sat_scale, 0.0, 1.0) if sat_scale > 0 else raw
+    levels = [raw]
+    cur = base
+    for _ in range(1, nlevels):
+        cur = mip_step_f64(cur)
+        levels.append(cur)
+    return levels
+
+
+def cone_ao_f64(levels, dirs, xyzr, normals, bounds_min, bounds_size, **kw) -> np.ndarray:
+    """Cone-marched AO per particle (FP64). `levels` are (z, y, x) arrays; level 0 raw (the kernel applies
+    sat_scale to it), the others as mip_chain_f64 builds them."""
+    lv = [np.ascontiguousarray(L, np.float64) for L in levels]
+    ptrs = (C.c_void_p * len(lv))(*[L.ctypes.data for L in lv])
+    dims = (C.c_int32 * (3 * len(lv)))(*[d for L in lv for d in (L.shape[2], L.shape[1], L.shape[0])])
+    d = np.ascontiguousarray(dirs, np.float32)
+    x = _xyzr(xyzr)
+    nrm = np.ascontiguousarray(normals, np.float32)
+    out = np.zeros(x.shape[0], np.float64)
+    cp = _cone_params(bounds_min, bounds_size, **kw)
+    lib().p2vo_cone_ao_f64(ptrs, dims, len(lv), d.ctypes.data, d.shape[0], C.byref(cp), x.ctypes.data,
+                           nrm.ctypes.data, x.shape[0], out.ctypes.data)
+    return out
+
+
+def aosphere_volume_f64(xyzr, clip, s, gen_fac=1.0) -> np.ndarray:
+    x = _xyzr(xyzr)
+    tex = np.zeros((s[2], s[1], s[0]), np.float64)
+    cl = (C.c_float * 6)(*[float(v) for v in clip])
+    ss = (C.c_int32 * 3)(*[int(v) for v in s])
+    lib().p2vo_aosphere_volume_f64(x.ctypes.data, x.shape[0], cl, ss, float(gen_fac), tex.ctypes.data)
+    return tex
+
+
+def aosphere_ao_f64(tex, clip, xyzr, normals, mode=0, step_len=0.5, eval_fac=1.0) -> np.ndarray:
+    t = np.ascontiguousarray(tex, np.float64)
+    x = _xyzr(xyzr)
+    nrm = np.ascontiguousarray(normals, np.float32)
+    out = np.zeros(x.shape[0], np.float64)
+    cl = (C.c_float * 6)(*[float(v) for v in clip])
+    ss = (C.c_int32 * 3)(t.shape[2], t.shape[1], t.shape[0])
+    lib().p2vo_aosphere_ao_f64(t.ctypes.data, ss, cl, float(step_len), float(eval_fac), x.ctypes.data, nrm.ctypes.data,
+                               x.shape[0], int(mode), out.ctypes.data)
+    return out

@@ -261,3 +261,241 @@ extern "C" void p2vo_mip_step_f64(const double* src, const int32_t sd[3], double
                 dst[x + (y + int64_t(z) * dd[1]) * dd[0]] = acc / 8.0;
             }
 }
+
+/* ------------------------------------------------------------------------------------------------
+ * AO restatements
+ * ---------------------------------------------------------------------------------------------- */
+namespace {
+
+struct Vol {
+    const double* v;
+    int d[3];
+};
+
+// Texel fetch with GL wrap semantics: border (0 outside) or edge (clamped index).
+inline double fetch(const Vol& L, int x, int y, int z, int border) {
+    if (border == 0) {
+        if (x < 0 || y < 0 || z < 0 || x >= L.d[0] || y >= L.d[1] || z >= L.d[2])
+            return 0.0;
+    } else {
+        x = std::min(std::max(x, 0), L.d[0] - 1);
+        y = std::min(std::max(y, 0), L.d[1] - 1);
+        z = std::min(std::max(z, 0), L.d[2] - 1);
+    }
+    return L.v[x + (y + int64_t(z) * L.d[1]) * L.d[0]];
+}
+
+// GL LINEAR filtering at normalised coordinate u: texel centres at (i + 0.5) / N.
+inline double trilinear(const Vol& L, const double u[3], int border) {
+    double c[3], f[3];
+    int i0[3];
+    for (int a = 0; a < 3; ++a) {
+        c[a] = u[a] * L.d[a] - 0.5;
+        i0[a] = (int) std::floor(c[a]);
+        f[a] = c[a] - i0[a];
+    }
+    double acc = 0.0;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                double w = (dx ? f[0] : 1 - f[0]) * (dy ? f[1] : 1 - f[1]) * (dz ? f[2] : 1 - f[2]);
+                if (w != 0.0)
+                    acc += w * fetch(L, i0[0] + dx, i0[1] + dy, i0[2] + dz, border);
+            }
+    return acc;
+}
+
+inline void normalize3(double v[3]) {
+    double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] /= l;
+    v[1] /= l;
+    v[2] /= l;
+}
+
+inline void cross3(const double a[3], const double b[3], double o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+}  // namespace
+
+extern "C" void p2vo_cone_dirs(int K, float apex, float* out) {
+    // SphereRenderer.cpp:2572-2587 for K = 3; a regular K-gon ring of the same edge length otherwise.
+    const float edge = 2.0f * std::tan(0.5f * apex);
+    const float height = std::sqrt(1.0f - edge * edge / 12.0f);
+    const float radius = K == 3 ? std::sqrt(3.0f) / 3.0f * edge : edge / (2.0f * std::sin(3.14159265358979f / K));
+    for (int i = 0; i < K; ++i) {
+        const float angle = static_cast<float>(i) / static_cast<float>(K) * 2.0f * 3.14159265358979f;
+        float c[3] = {std::cos(angle) * radius, height, std::sin(angle) * radius};
+        const float l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        out[4 * i + 0] = c[0] / l;
+        out[4 * i + 1] = c[1] / l;
+        out[4 * i + 2] = c[2] / l;
+        out[4 * i + 3] = edge;
+    }
+}
+
+extern "C" int p2vo_cone_steps(const p2vo_cone_params* cp, float w, float* t, float* lod, int cap) {
+    int n = 0;
+    float tt = cp->offset + 0.0001f;
+    float g = 0.0f;
+    if (cp->steps > 0)
+        g = std::pow(cp->cone_length / tt, 1.0f / static_cast<float>(cp->steps));
+    while (n < cap) {
+        float l = std::log2(tt * w * cp->shortest_edge);
+        l = std::min(std::max(l, 0.0f), cp->max_lod);
+        t[n] = tt;
+        lod[n] = l;
+        ++n;
+        if (cp->steps > 0) {
+            if (n >= cp->steps)
+                break;
+            tt = tt * g;
+        } else {
+            tt += tt * w;  // mdao_deferred_fragment_ambocc.inc.glsl:50
+            if (!(tt < cp->cone_length))
+                break;
+        }
+    }
+    return n;
+}
+
+extern "C" void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldims, int nlevels, const float* dirs,
+    int ncones, const p2vo_cone_params* cp, const float* xyzr, const float* nrm, int64_t n, double* ao) {
+    std::vector<Vol> L(nlevels);
+    for (int l = 0; l < nlevels; ++l)
+        L[l] = Vol{levels[l], {ldims[3 * l], ldims[3 * l + 1], ldims[3 * l + 2]}};
+    std::vector<double> sat0;
+    if (cp->sat_scale > 0.0f) {  // the level-0 texture holds clamp(v * scale, 0, 1)
+        const int64_t nv = int64_t(L[0].d[0]) * L[0].d[1] * L[0].d[2];
+        sat0.resize(nv);
+        for (int64_t i = 0; i < nv; ++i)
+            sat0[i] = std::min(1.0, std::max(0.0, L[0].v[i] * (double) cp->sat_scale));
+        L[0].v = sat0.data();
+    }
+    std::vector<float> ts(256), lods(256);
+    const int ns = p2vo_cone_steps(cp, dirs[3], ts.data(), lods.data(), 256);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const float* p = xyzr + 4 * i;
+        double nn[3] = {nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]};
+        const double nl = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        if (!(nl > 0.0)) {
+            ao[i] = 1.0;  // no normal: no occlusion
+            continue;
+        }
+        for (double& c : nn)
+            c /= nl;
+        // evaluation point on the sphere surface along the normal
+        double x[3] = {p[0] + p[3] * nn[0], p[1] + p[3] * nn[1], p[2] + p[3] * nn[2]};
+        // frame: new_y = n, new_x = cross(new_y, normalize(objPos)), new_z = cross(new_x, new_y) (:18-21)
+        double xn[3] = {x[0], x[1], x[2]};
+        const double xl = std::sqrt(xn[0] * xn[0] + xn[1] * xn[1] + xn[2] * xn[2]);
+        if (xl > 0.0) {
+            for (double& c : xn)
+                c /= xl;
+        } else {
+            xn[0] = 1.0;
+            xn[1] = xn[2] = 0.0;
+        }
+        double ex[3], ez[3];
+        cross3(nn, xn, ex);
+        cross3(ex, nn, ez);
+        double u[3];
+        for (int a = 0; a < 3; ++a)
+            u[a] = (x[a] - (double) cp->bounds_min[a]) / (double) cp->bounds_size[a];
+        double ambient = 0.0;
+        for (int c = 0; c < ncones; ++c) {
+            const float* cd = dirs + 4 * c;
+            double dir[3];
+            for (int a = 0; a < 3; ++a)
+                dir[a] = ex[a] * cd[0] + nn[a] * cd[1] + ez[a] * cd[2];
+            double acc = 0.0;
+            for (int k = 0; k < ns; ++k) {
+                const double t = ts[k];
+                const double lod = lods[k];
+                double q[3] = {u[0] + t * dir[0], u[1] + t * dir[1], u[2] + t * dir[2]};
+                const int l0 = (int) std::floor(lod);
+                const double fr = lod - l0;
+                double vis = trilinear(L[std::min(l0, nlevels - 1)], q, cp->border);
+                if (fr > 0.0 && l0 + 1 < nlevels)
+                    vis = (1.0 - fr) * vis + fr * trilinear(L[l0 + 1], q, cp->border);
+                acc += (1.0 - acc) * vis;
+                if (cp->early_exit && acc > 0.99)
+                    break;
+            }
+            ambient += acc;
+        }
+        ao[i] = 1.0 - std::min(1.0, std::max(0.0, (double) cp->strength * ambient / ncones));
+    }
+}
+
+extern "C" void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3],
+    float gen_fac, double* tex) {
+    // AOSphereRenderer.cpp:918-1021: inner grid s-2, cell decisions in float as the reference
+    const int sx = s[0] - 2, sy = s[1] - 2, sz = s[2] - 2;
+    const float minOS[3] = {clip[0], clip[1], clip[2]};
+    const float rangeOS[3] = {std::fabs(clip[3] - clip[0]), std::fabs(clip[4] - clip[1]), std::fabs(clip[5] - clip[2])};
+    const int si[3] = {sx, sy, sz};
+    const double voxelVol = ((double) rangeOS[0] / sx) * ((double) rangeOS[1] / sy) * ((double) rangeOS[2] / sz);
+    std::memset(tex, 0, sizeof(double) * (size_t) s[0] * s[1] * s[2]);
+    for (int64_t i = 0; i < n; ++i) {
+        const float* p = xyzr + 4 * i;
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+            int v = static_cast<int>(((p[a] - minOS[a]) / rangeOS[a]) * static_cast<float>(si[a]));
+            c[a] = v < 0 ? 0 : (v >= si[a] ? si[a] - 1 : v);
+        }
+        const double r = p[3];
+        const double spVol = 4.0 / 3.0 * 3.14159265358979323846 * r * r * r;
+        tex[(c[0] + 1) + ((c[1] + 1) + int64_t(c[2] + 1) * s[1]) * s[0]] += spVol / voxelVol * gen_fac;
+    }
+}
+
+extern "C" void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], const float clip[6], float step_len,
+    float eval_fac, const float* xyzr, const float* nrm, int64_t n, int mode, double* ao) {
+    // uniforms of AOSphereRenderer::renderParticles (AOSphereRenderer.cpp:489-514)
+    double origin[3], ext[3], sampd[3];
+    for (int a = 0; a < 3; ++a) {
+        const double range = std::fabs((double) clip[a + 3] - (double) clip[a]);
+        ext[a] = range / (1.0 - 2.0 / s[a]);
+        origin[a] = (double) clip[a] - ext[a] / s[a];
+        sampd[a] = (double) step_len * (range / s[a]);
+    }
+    Vol T{tex, {s[0], s[1], s[2]}};
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const float* p = xyzr + 4 * i;
+        double nn[3] = {nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]};
+        const double nl = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        if (!(nl > 0.0)) {
+            ao[i] = 1.0;
+            continue;
+        }
+        for (double& c : nn)
+            c /= nl;
+        if (mode == 0) {
+            // mainaxes_vertex_2.glsl:1-9 and mainaxes_fragLightAO_evalAO.glsl:1-8
+            double aop[3], aod[3];
+            for (int a = 0; a < 3; ++a) {
+                aop[a] = (p[a] - origin[a]) / ext[a];
+                aod[a] = ((double) p[3] + sampd[a]) / ext[a];
+            }
+            double acc = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                double q[3] = {aop[0], aop[1], aop[2]};
+                q[a] += nn[a] > 0.0 ? aod[a] : -aod[a];
+                const double tap = 1.0 - trilinear(T, q, 1) * eval_fac;
+                acc += nn[a] * nn[a] * tap;
+            }
+            ao[i] = acc;
+        } else {
+            // normals_fragLightAO_evalAO.glsl:1-4 at the surface point p + r n
+            double q[3];
+            for (int a = 0; a < 3; ++a)
+                q[a] = ((p[a] + p[3] * nn[a]) + nn[a] * sampd[a] - origin[a]) / ext[a];
+            ao[i] = 1.0 - trilinear(T, q, 1) * eval_fac;
+        }
+    }
+}

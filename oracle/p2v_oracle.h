@@ -51,19 +51,39 @@ int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g, int kerne
 /* MDAO 2x2x2 mip step, FP64: dst[i] = sum of the up-to-8 children clamped to the source size, / 8. */
 void p2vo_mip_step_f64(const double* src, const int32_t sdim[3], double* dst, const int32_t ddim[3]);
 
-/* Cone-marched AO per evaluation point (see p2v.h for the parameter meaning). levels[l] points to
- * level l (dims ldims[3*l..]), FP64. dirs = ncones vec4 (xyz direction around +Y, w = cone width). */
+/* Cone-marched AO (MDAO evaluateAmbientOcclusion, mdao_deferred_fragment_ambocc.inc.glsl:9-60).
+ * levels[l] is mip level l in FP64 (dims ldims[3l..3l+2], x fastest). The sample positions use the
+ * step table of p2vo_cone_steps (float, shared with the GPU so loop lengths agree); everything else is
+ * evaluated in double. */
 typedef struct {
     float bounds_min[3];
     float bounds_size[3];
     float offset, strength, cone_length, shortest_edge, max_lod;
-    int32_t steps;      /* 0 = the reference's geometric stepping until cone_length */
+    int32_t steps;      /* 0 = the reference's geometric stepping t += t*w until cone_length */
     int32_t early_exit; /* 1 = stop a cone once it exceeds 0.99, as the reference */
     int32_t border;     /* 0 = CLAMP_TO_BORDER (0), 1 = CLAMP_TO_EDGE */
+    float sat_scale;    /* level-0 texel = clamp(v * sat_scale, 0, 1); <= 0 keeps v */
 } p2vo_cone_params;
 
+/* Cone directions around +Y (vec4: xyz direction, w = cone width 2 tan(apex/2)); K = 3 is
+ * SphereRenderer::generate3ConeDirections (SphereRenderer.cpp:2572-2587), other K the same ring
+ * construction with the K-gon circumradius. Float, as the reference. */
+void p2vo_cone_dirs(int K, float apex_rad, float* out4);
+
+/* Step table (t, lod) of one cone of width w; returns the number of samples (<= cap). */
+int p2vo_cone_steps(const p2vo_cone_params* cp, float w, float* t, float* lod, int cap);
+
 void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldims, int nlevels, const float* dirs, int ncones,
-    const p2vo_cone_params* cp, const float* pos, const float* nrm, int64_t n, double* ao);
+    const p2vo_cone_params* cp, const float* xyzr, const float* nrm, int64_t n, double* ao);
+
+/* AOSphereRenderer volume deposit (AOSphereRenderer.cpp:918-1021): s = "vol::size" including the
+ * 1-voxel zero border; tex gets (4/3 pi r^3 / voxel volume) * genFac in the inner voxel of each particle. */
+void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3], float gen_fac,
+    double* tex);
+/* AOSphere sampling: mode 0 = main axes (mainaxes_vertex_2.glsl + mainaxes_fragLightAO_evalAO.glsl),
+ * mode 1 = normal tap (normals_fragLightAO_evalAO.glsl), uniforms as AOSphereRenderer.cpp:489-514. */
+void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], const float clip[6], float step_len, float eval_fac,
+    const float* xyzr, const float* nrm, int64_t n, int mode, double* ao);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,123 @@
+"""GPU tests of the AO stage through the C ABI, against the FP64 oracle restatement of the reference's
+GLSL (MDAO cone march, AOSphereRenderer taps). The density grid the GPU produced is handed to the oracle,
+so these tests isolate the AO arithmetic.
+
+Bars: cone march RMS error <= 1e-5 and max error <= 2e-3 (the reference's early exit at 0.99 is a
+discontinuity: a sample that sits on the threshold in one precision and not the other changes the cone's
+occlusion by at most (1 - 0.99) times one sample); AOSphere max error <= 1e-5."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from megamol_gb300 import build as nbuild
+from megamol_gb300 import p2v, synth
+
+pytestmark = pytest.mark.gpu
+NT = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    nbuild.build()
+    c = p2v.Context(0)
+    yield c
+    c.close()
+
+
+def frame(n=30_000, edge=30.0, res=40, seed=21):
+    f = synth.uniform(n=n, edge=edge, res=res, seed=seed)
+    f.xyzr[:, 3] = np.random.default_rng(seed).uniform(0.4, 0.8, f.n).astype(np.float32)
+    return f
+
+
+def run_ao(ctx, f, normals, **params):
+    # every parameter is set on each call: the context is shared by the tests of this module
+    base = dict(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], normalize=1, sigma=1.0, cyclX=1, cyclY=1, cyclZ=1,
+                accumulate=p2v.ACCUM_EXACT, forSurfaceReconstruction=0, mass_normalize=0, kernel=p2v.KERNEL_BUMP,
+                ao_volume=p2v.AOVOL_DENSITY, ao_volume_scale=1.0, ao_cones=3, ao_steps=0, ao_levels=0,
+                ao_apex_deg=50.0, ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1)
+    base.update(params)
+    ctx.set_params(**base)
+    ao = np.full(f.n, np.nan, np.float32)
+    vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
+    L = p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=np.ascontiguousarray(normals), ao_out=ao)
+    meta = ctx.run_frame([L], f.bbox, vol)
+    return ao, vol.reshape(f.res[2], f.res[1], f.res[0]), meta
+
+
+def cone_oracle(f, vol, normals, cones, steps, levels, apex=50.0, offset=0.01, strength=1.0, cone_length=0.8,
+                scale=1.0, early_exit=1):
+    h = oracle.spacing_f64(f.bbox, f.res)
+    bmin = [f.bbox[a] - 0.5 * h[a] for a in range(3)]
+    bsize = [f.res[a] * h[a] for a in range(3)]
+    lv = oracle.mip_chain_f64(vol, levels, scale)
+    dirs = oracle.cone_dirs(cones, np.deg2rad(np.float32(apex)))
+    return oracle.cone_ao_f64(lv, dirs, f.xyzr, normals, bmin, bsize, offset=offset, strength=strength,
+                              cone_length=cone_length, shortest_edge=float(min(f.res)), max_lod=float(levels - 1),
+                              steps=steps, early_exit=early_exit, border=0, sat_scale=scale)
+
+
+@pytest.mark.parametrize("cones,steps,levels", [(3, 0, 6), (8, 32, 3), (8, 16, 4)])
+def test_cone_ao_vs_fp64(ctx, cones, steps, levels):
+    f = frame()
+    nrm = synth.random_normals(f.n, 5)
+    ao, vol, _ = run_ao(ctx, f, nrm, ao_mode=p2v.AO_CONE, ao_cones=cones, ao_steps=steps, ao_levels=levels)
+    ref = cone_oracle(f, vol, nrm, cones, steps, levels)
+    d = np.abs(ao.astype(np.float64) - ref)
+    assert np.isfinite(ao).all()
+    assert np.sqrt(np.mean(d ** 2)) <= 1e-5, np.sqrt(np.mean(d ** 2))
+    assert d.max() <= 2e-3, d.max()
+    assert 0.0 <= ao.min() and ao.max() <= 1.0
+
+
+def test_cone_ao_no_early_exit_is_smooth(ctx):
+    """Without the early exit the march has no discontinuity: max error is at float rounding level."""
+    f = frame(n=10_000, seed=22)
+    nrm = synth.random_normals(f.n, 6)
+    ao, vol, _ = run_ao(ctx, f, nrm, ao_mode=p2v.AO_CONE, ao_cones=8, ao_steps=32, ao_levels=3, ao_early_exit=0)
+    ref = cone_oracle(f, vol, nrm, 8, 32, 3, early_exit=0)
+    assert np.abs(ao - ref).max() <= 2e-5
+
+
+def test_cone_ao_empty_volume_is_unoccluded(ctx):
+    f = frame(n=2000, seed=23)
+    nrm = synth.random_normals(f.n, 7)
+    ao, vol, _ = run_ao(ctx, f, nrm, ao_mode=p2v.AO_CONE, ao_cones=3, ao_volume_scale=1e-30, normalize=0)
+    assert np.allclose(ao, 1.0, atol=1e-6)
+
+
+def test_zero_normal_means_no_occlusion(ctx):
+    f = frame(n=5000, seed=24)
+    nrm = synth.random_normals(f.n, 8)
+    nrm[::7] = 0.0
+    ao, _, _ = run_ao(ctx, f, nrm, ao_mode=p2v.AO_CONE, ao_cones=3)
+    assert np.all(ao[::7] == 1.0)
+
+
+@pytest.mark.parametrize("mode", [p2v.AO_AOSPHERE_AXES, p2v.AO_AOSPHERE_NORMAL])
+def test_aosphere_vs_fp64(ctx, mode):
+    f = frame(n=20_000, seed=25)
+    nrm = synth.random_normals(f.n, 9)
+    s = (24, 20, 28)
+    ao, _, _ = run_ao(ctx, f, nrm, ao_mode=mode, aos_sizex=s[0], aos_sizey=s[1], aos_sizez=s[2], aos_step_len=0.5,
+                      aos_gen_fac=1.0, aos_eval_fac=1.0)
+    tex = oracle.aosphere_volume_f64(f.xyzr, f.bbox, s, 1.0)
+    ref = oracle.aosphere_ao_f64(tex, f.bbox, f.xyzr, nrm, 0 if mode == p2v.AO_AOSPHERE_AXES else 1, 0.5, 1.0)
+    d = np.abs(ao.astype(np.float64) - ref)
+    assert d.max() <= 1e-5 * max(1.0, np.abs(ref).max()), d.max()
+
+
+def test_gradient_normals_ao_pipeline_lj_small(ctx):
+    """A small LJ-liquid frame with gradient normals (the headline workload's normal definition)."""
+    f = synth.lj_liquid(cells=24, res=64, seed=31)
+    ctx.set_params(sizex=64, sizey=64, sizez=64, normalize=1, ao_mode=p2v.AO_NONE)
+    vol = np.empty(64 ** 3, np.float32)
+    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
+    nrm = synth.gradient_normals(f.xyzr, vol.reshape(64, 64, 64), f.bbox)
+    ao, vol2, _ = run_ao(ctx, f, nrm, ao_mode=p2v.AO_CONE, ao_cones=8, ao_steps=32, ao_levels=3)
+    assert np.array_equal(vol2.reshape(-1), vol)
+    ref = cone_oracle(f, vol2, nrm, 8, 32, 3)
+    d = np.abs(ao - ref)
+    assert np.sqrt(np.mean(d ** 2)) <= 1e-5 and d.max() <= 2e-3
