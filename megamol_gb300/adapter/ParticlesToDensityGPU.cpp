@@ -1,0 +1,348 @@
+/*
+ * ParticlesToDensityGPU — see the header. The callback structure follows
+ * ParticlesToDensity::getDataCallback / getExtentCallback (ParticlesToDensity.cpp:163-304); the volume and
+ * AO are computed by p2v_run_frame.
+ */
+#include "ParticlesToDensityGPU.h"
+
+#include <algorithm>
+#include <limits>
+
+#include "mmcore/param/BoolParam.h"
+#include "mmcore/param/EnumParam.h"
+#include "mmcore/param/FloatParam.h"
+#include "mmcore/param/IntParam.h"
+#include "mmcore/utility/log/Log.h"
+
+using namespace megamol;
+using namespace megamol::p2v_gb300;
+using core::param::BoolParam;
+using core::param::EnumParam;
+using core::param::FloatParam;
+using core::param::IntParam;
+
+ParticlesToDensityGPU::ParticlesToDensityGPU()
+        : aggregatorSlot("aggregator", "algorithm for the aggregation")
+        , xResSlot("sizex", "The size of the volume in numbers of voxels")
+        , yResSlot("sizey", "The size of the volume in numbers of voxels")
+        , zResSlot("sizez", "The size of the volume in numbers of voxels")
+        , cyclXSlot("cyclX", "Considers cyclic boundary conditions in X direction")
+        , cyclYSlot("cyclY", "Considers cyclic boundary conditions in Y direction")
+        , cyclZSlot("cyclZ", "Considers cyclic boundary conditions in Z direction")
+        , normalizeSlot("normalize", "Normalize the output volume")
+        , sigmaSlot("sigma", "Sigma for Gauss in multiple of rad")
+        , surfaceSlot("forSurfaceReconstruction", "Set true if this volume is used for surface reconstruction")
+        , kernelSlot("kernel", "Density kernel: reference bump, or Gaussian cut at 3 sigma")
+        , massNormSlot("massNormalize", "Scale the grid so that it integrates to the particle count")
+        , aoModeSlot("ao::mode", "Per-particle ambient occlusion")
+        , aoConesSlot("ao::cones", "Number of cones")
+        , aoStepsSlot("ao::steps", "Samples per cone (0 = geometric steps until the cone length)")
+        , aoLevelsSlot("ao::levels", "Mip levels (0 = log2 of the longest edge)")
+        , aoApexSlot("ao::apex", "Cone apex angle in degrees")
+        , aoOffsetSlot("ao::offset", "Offset from the surface")
+        , aoStrengthSlot("ao::strength", "Strength")
+        , aoConeLengthSlot("ao::coneLength", "Cone length")
+        , outDataSlot("outData", "Provides a density volume for the particles")
+        , outAOSlot("outAO", "Provides the particles with their ambient occlusion as intensity colour")
+        , inDataSlot("inData", "Takes the particle data") {
+    auto* ep = new EnumParam(0);
+    ep->SetTypePair(0, "PosToSingleCell_Volume");
+    aggregatorSlot << ep;
+    MakeSlotAvailable(&aggregatorSlot);
+    xResSlot << new IntParam(16);
+    MakeSlotAvailable(&xResSlot);
+    yResSlot << new IntParam(16);
+    MakeSlotAvailable(&yResSlot);
+    zResSlot << new IntParam(16);
+    MakeSlotAvailable(&zResSlot);
+    cyclXSlot.SetParameter(new BoolParam(true));
+    MakeSlotAvailable(&cyclXSlot);
+    cyclYSlot.SetParameter(new BoolParam(true));
+    MakeSlotAvailable(&cyclYSlot);
+    cyclZSlot.SetParameter(new BoolParam(true));
+    MakeSlotAvailable(&cyclZSlot);
+    normalizeSlot << new BoolParam(true);
+    MakeSlotAvailable(&normalizeSlot);
+    sigmaSlot << new FloatParam(1.0f, std::numeric_limits<float>::min(), std::numeric_limits<float>::max());
+    MakeSlotAvailable(&sigmaSlot);
+    surfaceSlot << new BoolParam(false);
+    MakeSlotAvailable(&surfaceSlot);
+
+    auto* kp = new EnumParam(P2V_KERNEL_BUMP);
+    kp->SetTypePair(P2V_KERNEL_BUMP, "Bump (reference)");
+    kp->SetTypePair(P2V_KERNEL_GAUSS3, "Gaussian, 3 sigma");
+    kernelSlot << kp;
+    MakeSlotAvailable(&kernelSlot);
+    massNormSlot << new BoolParam(false);
+    MakeSlotAvailable(&massNormSlot);
+    auto* am = new EnumParam(P2V_AO_NONE);
+    am->SetTypePair(P2V_AO_NONE, "None");
+    am->SetTypePair(P2V_AO_CONE, "Cone march (MDAO)");
+    am->SetTypePair(P2V_AO_AOSPHERE_AXES, "AOSphere main axes");
+    am->SetTypePair(P2V_AO_AOSPHERE_NORMAL, "AOSphere normal");
+    am->SetTypePair(P2V_AO_LEARNED, "Learned (MLP, cone-march fallback)");
+    aoModeSlot << am;
+    MakeSlotAvailable(&aoModeSlot);
+    aoConesSlot << new IntParam(3, 1, 16);
+    MakeSlotAvailable(&aoConesSlot);
+    aoStepsSlot << new IntParam(0, 0, 256);
+    MakeSlotAvailable(&aoStepsSlot);
+    aoLevelsSlot << new IntParam(0, 0, 12);
+    MakeSlotAvailable(&aoLevelsSlot);
+    aoApexSlot << new FloatParam(50.0f, 1.0f, 90.0f);
+    MakeSlotAvailable(&aoApexSlot);
+    aoOffsetSlot << new FloatParam(0.01f, 0.0f, 0.2f);
+    MakeSlotAvailable(&aoOffsetSlot);
+    aoStrengthSlot << new FloatParam(1.0f, 0.1f, 20.0f);
+    MakeSlotAvailable(&aoStrengthSlot);
+    aoConeLengthSlot << new FloatParam(0.8f, 0.01f, 1.0f);
+    MakeSlotAvailable(&aoConeLengthSlot);
+
+    using VDC = geocalls::VolumetricDataCall;
+    outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_GET_DATA),
+        &ParticlesToDensityGPU::getDataCallback);
+    outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_GET_EXTENTS),
+        &ParticlesToDensityGPU::getExtentCallback);
+    outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_GET_METADATA),
+        &ParticlesToDensityGPU::getExtentCallback);
+    outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_START_ASYNC),
+        &ParticlesToDensityGPU::dummyCallback);
+    outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_STOP_ASYNC),
+        &ParticlesToDensityGPU::dummyCallback);
+    outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_TRY_GET_DATA),
+        &ParticlesToDensityGPU::dummyCallback);
+    MakeSlotAvailable(&outDataSlot);
+
+    using MPDC = geocalls::MultiParticleDataCall;
+    outAOSlot.SetCallback(MPDC::ClassName(), MPDC::FunctionName(0), &ParticlesToDensityGPU::getAODataCallback);
+    outAOSlot.SetCallback(MPDC::ClassName(), MPDC::FunctionName(1), &ParticlesToDensityGPU::getAOExtentCallback);
+    MakeSlotAvailable(&outAOSlot);
+
+    inDataSlot.SetCompatibleCall<geocalls::MultiParticleDataCallDescription>();
+    MakeSlotAvailable(&inDataSlot);
+}
+
+ParticlesToDensityGPU::~ParticlesToDensityGPU() {
+    Release();
+}
+
+bool ParticlesToDensityGPU::create() {
+    // one GPU, device 0, as MegaMol's CUDA service creates its context (frontend/services/cuda/CUDA_Service.cpp:30-56)
+    if (p2v_create(&ctx, 0) != P2V_OK) {
+        core::utility::log::Log::DefaultLog.WriteError("ParticlesToDensityGPU: no CUDA device for libp2v");
+        return false;
+    }
+    return true;
+}
+
+void ParticlesToDensityGPU::release() {
+    p2v_destroy(ctx);
+    ctx = nullptr;
+}
+
+bool ParticlesToDensityGPU::anythingDirty() const {
+    for (auto* s : {&aggregatorSlot, &xResSlot, &yResSlot, &zResSlot, &cyclXSlot, &cyclYSlot, &cyclZSlot,
+             &normalizeSlot, &sigmaSlot, &kernelSlot, &massNormSlot, &aoModeSlot, &aoConesSlot, &aoStepsSlot,
+             &aoLevelsSlot, &aoApexSlot, &aoOffsetSlot, &aoStrengthSlot, &aoConeLengthSlot})
+        if (s->IsDirty())
+            return true;
+    return false;
+}
+
+void ParticlesToDensityGPU::resetDirty() {
+    for (auto* s : {&aggregatorSlot, &xResSlot, &yResSlot, &zResSlot, &cyclXSlot, &cyclYSlot, &cyclZSlot,
+             &normalizeSlot, &sigmaSlot, &kernelSlot, &massNormSlot, &aoModeSlot, &aoConesSlot, &aoStepsSlot,
+             &aoLevelsSlot, &aoApexSlot, &aoOffsetSlot, &aoStrengthSlot, &aoConeLengthSlot})
+        s->ResetDirty();
+}
+
+bool ParticlesToDensityGPU::getExtentCallback(core::Call& c) {
+    auto* out = dynamic_cast<geocalls::VolumetricDataCall*>(&c);
+    auto* in = inDataSlot.CallAs<geocalls::MultiParticleDataCall>();
+    if (out == nullptr || in == nullptr)
+        return false;
+    in->SetFrameID(out->FrameID(), true);
+    if (!(*in)(1))
+        return false;
+    out->AccessBoundingBoxes().SetObjectSpaceBBox(in->GetBoundingBoxes().ObjectSpaceBBox());
+    out->AccessBoundingBoxes().SetObjectSpaceClipBox(in->GetBoundingBoxes().ObjectSpaceClipBox());
+    out->AccessBoundingBoxes().MakeScaledWorld(1.0f);
+    out->SetFrameCount(in->FrameCount());
+    return true;
+}
+
+bool ParticlesToDensityGPU::dummyCallback(core::Call&) {
+    return true;
+}
+
+bool ParticlesToDensityGPU::pullFrame(geocalls::MultiParticleDataCall* in, unsigned int frame) {
+    do { // ParticlesToDensity.cpp:222-232
+        in->SetFrameID(frame, true);
+        if (!(*in)(1) || !(*in)(0)) {
+            core::utility::log::Log::DefaultLog.WriteError("ParticlesToDensityGPU: unable to get frame %u", frame);
+            return false;
+        }
+    } while (in->FrameID() != frame);
+    if (time != in->FrameID() || inDataHash != in->DataHash() || anythingDirty()) {
+        if (!recompute(in))
+            return false;
+        time = in->FrameID();
+        inDataHash = in->DataHash();
+        ++dataHash;
+        resetDirty();
+    }
+    return true;
+}
+
+bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
+    p2v_params prm;
+    p2v_params_default(&prm);
+    prm.aggregator = aggregatorSlot.Param<EnumParam>()->Value();
+    prm.sizex = xResSlot.Param<IntParam>()->Value();
+    prm.sizey = yResSlot.Param<IntParam>()->Value();
+    prm.sizez = zResSlot.Param<IntParam>()->Value();
+    prm.cyclX = cyclXSlot.Param<BoolParam>()->Value();
+    prm.cyclY = cyclYSlot.Param<BoolParam>()->Value();
+    prm.cyclZ = cyclZSlot.Param<BoolParam>()->Value();
+    prm.normalize = normalizeSlot.Param<BoolParam>()->Value();
+    prm.sigma = sigmaSlot.Param<FloatParam>()->Value();
+    prm.forSurfaceReconstruction = surfaceSlot.Param<BoolParam>()->Value();
+    prm.kernel = kernelSlot.Param<EnumParam>()->Value();
+    prm.mass_normalize = massNormSlot.Param<BoolParam>()->Value();
+    prm.ao_mode = aoModeSlot.Param<EnumParam>()->Value();
+    prm.ao_cones = aoConesSlot.Param<IntParam>()->Value();
+    prm.ao_steps = aoStepsSlot.Param<IntParam>()->Value();
+    prm.ao_levels = aoLevelsSlot.Param<IntParam>()->Value();
+    prm.ao_apex_deg = aoApexSlot.Param<FloatParam>()->Value();
+    prm.ao_offset = aoOffsetSlot.Param<FloatParam>()->Value();
+    prm.ao_strength = aoStrengthSlot.Param<FloatParam>()->Value();
+    prm.ao_cone_length = aoConeLengthSlot.Param<FloatParam>()->Value();
+    if (p2v_set_params(ctx, &prm) != P2V_OK)
+        return false;
+
+    const unsigned int nl = in->GetParticleListCount();
+    std::vector<p2v_particle_list> lists(nl);
+    ao.resize(nl);
+    for (unsigned int i = 0; i < nl; ++i) {
+        auto& p = in->AccessParticles(i);
+        p2v_particle_list& L = lists[i];
+        L = p2v_particle_list{};
+        L.vertex_type = static_cast<int32_t>(p.GetVertexDataType());
+        L.vertex_data = p.GetVertexData();
+        L.vertex_stride = p.GetVertexDataStride();
+        L.count = p.GetCount();
+        L.global_radius = p.GetGlobalRadius();
+        L.mem = P2V_MEM_HOST;
+        if (prm.ao_mode != P2V_AO_NONE) {
+            L.normals = static_cast<const float*>(p.GetDirData());
+            L.normal_stride = p.GetDirDataStride();
+            ao[i].resize(p.GetCount());
+            L.ao_out = ao[i].data();
+        }
+    }
+    p2v_frame fr{};
+    const auto& bb = in->AccessBoundingBoxes().ObjectSpaceBBox();
+    const auto& cb = in->AccessBoundingBoxes().ObjectSpaceClipBox();
+    const float box[6] = {bb.Left(), bb.Bottom(), bb.Back(), bb.Right(), bb.Top(), bb.Front()};
+    const float clip[6] = {cb.Left(), cb.Bottom(), cb.Back(), cb.Right(), cb.Top(), cb.Front()};
+    std::copy(box, box + 6, fr.bbox);
+    std::copy(clip, clip + 6, fr.clipbox);
+    fr.frame_id = in->FrameID();
+    fr.list_count = nl;
+    fr.lists = lists.data();
+
+    // the grid size is only final after the surface-reconstruction box adjustment: ask the library first
+    p2v_volume v{};
+    if (prm.forSurfaceReconstruction) {
+        if (p2v_run_frame(ctx, &fr, &v, nullptr) != P2V_OK)
+            return false;
+    } else {
+        v.resolution[0] = prm.sizex;
+        v.resolution[1] = prm.sizey;
+        v.resolution[2] = prm.sizez;
+    }
+    volume.resize(v.resolution[0] * v.resolution[1] * v.resolution[2]);
+    v.data = volume.data();
+    v.mem = P2V_MEM_HOST;
+    v.capacity = volume.size();
+    if (p2v_run_frame(ctx, &fr, &v, nullptr) != P2V_OK) {
+        char msg[512];
+        p2v_get_last_error(ctx, msg, sizeof(msg));
+        core::utility::log::Log::DefaultLog.WriteError("ParticlesToDensityGPU: %s", msg);
+        return false;
+    }
+    if (prm.forSurfaceReconstruction) {
+        // mirror the parameter rewrite of modifyBBox (ParticlesToDensity.cpp:772,779)
+        xResSlot.Param<IntParam>()->SetValue(static_cast<int>(v.resolution[0]), false);
+        yResSlot.Param<IntParam>()->SetValue(static_cast<int>(v.resolution[1]), false);
+    }
+    metadata.Components = 1;
+    metadata.GridType = geocalls::CARTESIAN;
+    metadata.ScalarType = geocalls::FLOATING_POINT;
+    metadata.ScalarLength = sizeof(float);
+    metadata.NumberOfFrames = 1;
+    for (int a = 0; a < 3; ++a) {
+        metadata.Resolution[a] = v.resolution[a];
+        metadata.Extents[a] = v.extents[a];
+        metadata.Origin[a] = v.origin[a];
+        sliceDists[a] = v.slice_dists[a];
+        metadata.SliceDists[a] = &sliceDists[a];
+        metadata.IsUniform[a] = true;
+    }
+    minValue = v.min_value;
+    maxValue = v.max_value;
+    metadata.MinValues = &minValue;
+    metadata.MaxValues = &maxValue;
+    return true;
+}
+
+bool ParticlesToDensityGPU::getDataCallback(core::Call& c) {
+    auto* in = inDataSlot.CallAs<geocalls::MultiParticleDataCall>();
+    auto* out = dynamic_cast<geocalls::VolumetricDataCall*>(&c);
+    if (in == nullptr || out == nullptr)
+        return false;
+    if (!pullFrame(in, out->FrameID()))
+        return false;
+    out->SetFrameID(time);
+    out->SetData(volume.data());
+    out->SetMetadata(&metadata);
+    out->SetDataHash(dataHash);
+    return true;
+}
+
+bool ParticlesToDensityGPU::getAOExtentCallback(core::Call& c) {
+    auto* out = dynamic_cast<geocalls::MultiParticleDataCall*>(&c);
+    auto* in = inDataSlot.CallAs<geocalls::MultiParticleDataCall>();
+    if (out == nullptr || in == nullptr)
+        return false;
+    in->SetFrameID(out->FrameID(), true);
+    if (!(*in)(1))
+        return false;
+    out->AccessBoundingBoxes().SetObjectSpaceBBox(in->GetBoundingBoxes().ObjectSpaceBBox());
+    out->AccessBoundingBoxes().SetObjectSpaceClipBox(in->GetBoundingBoxes().ObjectSpaceClipBox());
+    out->SetFrameCount(in->FrameCount());
+    return true;
+}
+
+bool ParticlesToDensityGPU::getAODataCallback(core::Call& c) {
+    auto* out = dynamic_cast<geocalls::MultiParticleDataCall*>(&c);
+    auto* in = inDataSlot.CallAs<geocalls::MultiParticleDataCall>();
+    if (out == nullptr || in == nullptr || aoModeSlot.Param<EnumParam>()->Value() == P2V_AO_NONE)
+        return false;
+    if (!pullFrame(in, out->FrameID()))
+        return false;
+    out->SetFrameID(time);
+    out->SetDataHash(dataHash);
+    out->SetParticleListCount(in->GetParticleListCount());
+    for (unsigned int i = 0; i < in->GetParticleListCount(); ++i) {
+        auto& src = in->AccessParticles(i);
+        auto& dst = out->AccessParticles(i);
+        dst.SetCount(src.GetCount());
+        dst.SetGlobalRadius(src.GetGlobalRadius());
+        dst.SetVertexData(src.GetVertexDataType(), src.GetVertexData(), src.GetVertexDataStride());
+        dst.SetDirData(src.GetDirDataType(), src.GetDirData(), src.GetDirDataStride());
+        dst.SetColourData(geocalls::SimpleSphericalParticles::COLDATA_FLOAT_I, ao[i].data());
+        dst.SetColourMapIndexValues(0.0f, 1.0f);
+    }
+    return true;
+}

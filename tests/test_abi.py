@@ -84,3 +84,18 @@ def test_create_without_device_fails_cleanly(lib):
     h = C.c_void_p()
     assert lib.p2v_create(C.byref(h), 0) == p2v.ECUDA
     assert not h.value
+
+
+def test_megamol_adapter_compiles_against_reference_headers():
+    """The drop-in module (megamol_gb300/adapter) compiles against MegaMol's own geometry_calls and
+    vislib headers, with the oracle's stand-ins for the core headers. Needs the MegaMol source tree."""
+    import oracle
+
+    ref = oracle.REFERENCE_TREE
+    if not os.path.isdir(os.path.join(ref, "plugins", "geometry_calls")):
+        pytest.skip("MegaMol source tree not present")
+    src = os.path.join(ROOT, "megamol_gb300", "adapter", "ParticlesToDensityGPU.cpp")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "oracle", "shim"), "-I",
+                        os.path.join(ROOT, "include"), "-I", os.path.join(ref, "plugins", "geometry_calls", "include"),
+                        "-I", os.path.join(ref, "vislib", "include"), src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
