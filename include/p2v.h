@@ -170,6 +170,33 @@ typedef struct p2v_stats {
     uint32_t ao_fallback;        /* learned AO: particles that fell back to the cone march */
 } p2v_stats;
 
+/* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle:
+ * mip levels 1 and 2 of the AO volume, each a 4x4x4 stencil of trilinear samples one texel apart centred
+ * on the surface point, then the unit normal (P2V_MLP_INPUTS values); network 131 -> 64 -> 64 -> 1 with
+ * SiLU, SiLU, sigmoid. Parameter vector: W1[64][131], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define P2V_MLP_INPUTS 131
+#define P2V_MLP_HIDDEN 64
+#define P2V_MLP_PARAMS 12673
+
+typedef struct p2v_train_params {
+    uint32_t struct_size;   /* sizeof(p2v_train_params); set by p2v_train_params_default */
+    int32_t epochs;
+    int32_t batch;
+    float lr, beta1, beta2, eps;   /* Adam */
+    float lr_decay;         /* lr multiplied by this after every epoch */
+    float val_fraction;     /* pairs held out for validation */
+    float range_margin;     /* fallback when a feature leaves [lo - m(hi-lo), hi + m(hi-lo)] of the training pairs */
+    uint64_t seed;          /* initialisation and batch order */
+} p2v_train_params;
+
+typedef struct p2v_train_report {
+    uint64_t pairs_train, pairs_val;
+    int32_t steps;
+    float final_loss;       /* training MSE of the last epoch's last batch */
+    float val_rmse, val_max_err;   /* FP32 network vs cone-march targets on the held-out pairs */
+    double ms;
+} p2v_train_report;
+
 typedef struct p2v_ctx p2v_ctx;
 
 P2V_API int p2v_abi_version(void);
@@ -194,6 +221,30 @@ P2V_API p2v_status p2v_get_device_volume(p2v_ctx* ctx, const float** dptr, uint6
 P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
 /* Last error message of this context ("" if none); returns the message length. */
 P2V_API size_t p2v_get_last_error(const p2v_ctx* ctx, char* buf, size_t len);
+
+/* ---- learned AO ---- */
+P2V_API void p2v_train_params_default(p2v_train_params* tp);
+/* Run the frame with the plain cone march (current AO parameters, ao_mode forced to P2V_AO_CONE) and add
+ * up to max_pairs (feature, cone-march AO) pairs, drawn uniformly with `seed`, to the training set.
+ * *total receives the training-set size. The frame's lists must carry normals. */
+P2V_API p2v_status p2v_mlp_collect(p2v_ctx* ctx, const p2v_frame* frame, uint32_t max_pairs, uint64_t seed,
+                                   uint64_t* total);
+P2V_API p2v_status p2v_mlp_clear(p2v_ctx* ctx);
+/* Train the MLP on the collected pairs with FP32 forward/backward kernels and Adam. */
+P2V_API p2v_status p2v_mlp_train(p2v_ctx* ctx, const p2v_train_params* tp, p2v_train_report* rep);
+/* Flat binary file: header (magic, version, sizes, seed, Adam step), FP32 parameters, Adam moments,
+ * feature ranges. */
+P2V_API p2v_status p2v_mlp_save(p2v_ctx* ctx, const char* path);
+P2V_API p2v_status p2v_mlp_load(p2v_ctx* ctx, const char* path);
+/* FP32 parameters (P2V_MLP_PARAMS values). Setting them clears the feature ranges (no fallback). */
+P2V_API p2v_status p2v_mlp_get_weights(p2v_ctx* ctx, float* out, uint64_t count);
+P2V_API p2v_status p2v_mlp_set_weights(p2v_ctx* ctx, const float* in, uint64_t count);
+/* One forward + backward pass of the training kernels on n given pairs (host arrays): gradient of
+ * mean((y - t)^2) with respect to the parameters, and the loss. */
+P2V_API p2v_status p2v_mlp_gradients(p2v_ctx* ctx, const float* x, const float* t, uint32_t n, float* grad,
+                                     float* loss);
+/* Tensor-core (BF16 x BF16 -> FP32) inference on n given feature rows (host arrays). */
+P2V_API p2v_status p2v_mlp_infer(p2v_ctx* ctx, const float* x, uint32_t n, float* y);
 
 #ifdef __cplusplus
 }

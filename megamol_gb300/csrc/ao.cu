@@ -95,8 +95,11 @@ __device__ __forceinline__ bool surface_point(const float4 p, const float4 nrm, 
 }
 
 __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
-    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, float* __restrict__ ao) {
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, const uint32_t* __restrict__ n_dev,
+    float* __restrict__ ao) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev != nullptr)
+        n = min(n, *n_dev);
     if (i >= n)
         return;
     const uint32_t o = order ? order[i] : i;
@@ -269,10 +272,10 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
 }
 
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
-    uint32_t n, float* ao, cudaStream_t st) {
+    uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st) {
     if (n == 0)
         return cudaSuccess;
-    cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, ao);
+    cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
     return cudaGetLastError();
 }
 

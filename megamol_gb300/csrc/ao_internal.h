@@ -28,6 +28,7 @@ struct ConeParams {
     float4 dirs[MAX_CONES];        // xyz around +Y, w = cone width
     float t[MAX_STEPS], lod[MAX_STEPS];
     ConeLevel lv[MAX_LEVELS];
+    int stencil_level;             // learned AO: first of the two mip levels its stencil reads
 };
 
 struct AOSphereParams {
@@ -39,8 +40,9 @@ struct AOSphereParams {
 
 cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int nlevels, float* const* out,
     int (*dims)[3], int sms, cudaStream_t st);
+// n_dev (nullable): device-side particle count, at most n (the cone march of the learned-AO fallback list)
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
-    uint32_t n, float* ao, cudaStream_t st);
+    uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st);
 cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc,
     float* tex, const uint32_t* order, const float4* nrm, int mode, float* ao, int sms, cudaStream_t st);
 cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,

@@ -4,18 +4,24 @@
 // Host-side semantics follow datatools::ParticlesToDensity (plugins/datatools/src/ParticlesToDensity.cpp):
 // parameter defaults (:59-152), the surface-reconstruction box adjustment modifyBBox (:749-799), the
 // grid geometry (:420-432) and the metadata it publishes (:249-293).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <numeric>
+#include <random>
 #include <string>
 #include <vector>
 
 #include "../../include/p2v.h"
 #include "p2v_common.cuh"
 #include "ao_internal.h"
+#include "mlp_internal.h"
 #include "p2v_internal.h"
 
 using namespace p2v;
@@ -65,9 +71,22 @@ struct p2v_ctx {
 
     DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
     DevBuf nrm, ao, mips, aos_acc, aos_tex;
+    // learned AO
+    DevBuf mlp_P, mlp_m, mlp_v, mlp_g, mlp_part, mlp_ploss, mlp_loss, mlp_w1h, mlp_w2h, mlp_lo, mlp_hi, mlp_idx,
+        mlp_y, fb_list;
+    DevBuf tX, tT;                       // collected training pairs
+    uint64_t t_pairs = 0, t_cap = 0;
+    std::vector<uint32_t> t_valid;       // indices of pairs with features
+    std::vector<float> t_host_T;         // targets on the host (validation error)
+    bool mlp_ready = false, mlp_has_range = false;
+    int mlp_level = -1;                  // stencil base level the network was trained on
+    int mlp_step = 0;
+    uint64_t mlp_seed = 0;
+    ConeParams last_cp{};
     FrameScalars* h_scal = nullptr;  // pinned mirror
     cudaEvent_t ev[EV_COUNT] = {};
     const float* last_grid = nullptr;
+    const uint32_t* last_order = nullptr;  // sorted position -> particle index of the last frame
     uint64_t last_res[3] = {0, 0, 0};
 
     p2v_status fail(p2v_status s, const char* fmt, ...) {
@@ -83,6 +102,9 @@ struct p2v_ctx {
     p2v_status run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st);
     p2v_status run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
                       const uint32_t* order, cudaStream_t st);
+    p2v_status build_cone(const GridGeo& g, const float* dgrid, const float bb[6], ConeParams& cp, cudaStream_t st);
+    p2v_status mlp_alloc();
+    void mlp_init_params(uint64_t seed, float bias3);
 };
 
 namespace {
@@ -424,6 +446,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
 
     const FrameScalars& hs = *h_scal;
     last_grid = dgrid;
+    last_order = sb.vals[sb.result];
     for (int a = 0; a < 3; ++a)
         last_res[a] = (uint64_t) res[a];
     stats = p2v_stats{};
@@ -452,6 +475,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     cudaEventElapsedTime(&ms, ev[EV_START], ev[EV_DOWN]);
     stats.ms_total = ms;
     stats.device_error = hs.error;
+    stats.ao_fallback = hs.ao_fallback;
 
     if (vol) {
         for (int a = 0; a < 3; ++a) {
@@ -475,64 +499,109 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     return P2V_OK;
 }
 
+p2v_status p2v_ctx::build_cone(const GridGeo& g, const float* dgrid, const float bb[6], ConeParams& cp,
+                               cudaStream_t st) {
+    const p2v_params& P = prm;
+    if (P.ao_volume != P2V_AOVOL_DENSITY)
+        return fail(P2V_EUNSUPPORTED, "ao_volume %d is not implemented for the cone march", P.ao_volume);
+    if (P.ao_cones < 1 || P.ao_cones > MAX_CONES)
+        return fail(P2V_EINVAL, "ao_cones must lie in [1, %d]", MAX_CONES);
+    cp = ConeParams{};
+    const int smax = std::max(g.s[0], std::max(g.s[1], g.s[2]));
+    const int smin = std::min(g.s[0], std::min(g.s[1], g.s[2]));
+    int L = P.ao_levels > 0 ? P.ao_levels : (int) std::ceil(std::log2((double) smax));
+    L = std::max(1, std::min(L, MAX_LEVELS));
+    // the density grid is node-centred: as a texture it spans [min - h/2, max + h/2]
+    for (int a = 0; a < 3; ++a) {
+        const double hd = std::fabs((double) bb[a + 3] - (double) bb[a]) / (double) (g.s[a] - 1);
+        cp.bmin[a] = (float) ((double) bb[a] - 0.5 * hd);
+        cp.ibsize[a] = (float) (1.0 / (g.s[a] * hd));
+    }
+    cp.strength = P.ao_strength;
+    cp.sat = P.ao_volume_scale;
+    cp.border = 0;  // CLAMP_TO_BORDER (MDAOVolumeGenerator.cpp:58-60)
+    cp.early_exit = P.ao_early_exit ? 1 : 0;
+    cp.ncones = P.ao_cones;
+    cone_directions(P.ao_cones, P.ao_apex_deg * 3.14159265358979f / 180.0f, cp.dirs);
+    cp.nsteps = cone_steps(P.ao_offset, P.ao_cone_length, P.ao_steps, cp.dirs[0].w, (float) smin, (float) (L - 1),
+                           cp.t, cp.lod, MAX_STEPS);
+    if (P.ao_steps > MAX_STEPS || (P.ao_steps <= 0 && cp.nsteps >= MAX_STEPS))
+        return fail(P2V_EUNSUPPORTED, "more than %d samples per cone", MAX_STEPS);
+    cp.nlevels = L;
+    // the learned AO's stencil reads the two levels the cone's first sample blends
+    cp.stencil_level = std::max(0, std::min((int) std::floor(cp.lod[0]), L - 2));
+    // level 0 is the density grid itself (saturated on the fly); levels 1.. are built here
+    size_t need = 0;
+    int d[MAX_LEVELS][3];
+    for (int a = 0; a < 3; ++a)
+        d[0][a] = g.s[a];
+    for (int l = 1; l < L; ++l) {
+        for (int a = 0; a < 3; ++a)
+            d[l][a] = std::max(1, d[l - 1][a] / 2);
+        need += (size_t) d[l][0] * d[l][1] * d[l][2];
+    }
+    P2V_CUDA_TRY(mips.ensure(sizeof(float) * (need + 1)));
+    float* lvp[MAX_LEVELS];
+    lvp[0] = const_cast<float*>(dgrid);
+    size_t off = 0;
+    for (int l = 1; l < L; ++l) {
+        lvp[l] = mips.as<float>() + off;
+        off += (size_t) d[l][0] * d[l][1] * d[l][2];
+    }
+    int dims[MAX_LEVELS][3];
+    P2V_CUDA_TRY(launch_mip_levels(dgrid, g.s, cp.sat, L, lvp, dims, sms, st));
+    for (int l = 0; l < L; ++l) {
+        cp.lv[l].v = lvp[l];
+        for (int a = 0; a < 3; ++a) {
+            cp.lv[l].d[a] = d[l][a];
+            cp.lv[l].fd[a] = (float) d[l][a];
+        }
+    }
+    last_cp = cp;
+    return P2V_OK;
+}
+
 p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
                            const uint32_t* order, cudaStream_t st) {
     const p2v_params& P = prm;
     if (P.ao_mode == P2V_AO_CONE) {
-        if (P.ao_volume != P2V_AOVOL_DENSITY)
-            return fail(P2V_EUNSUPPORTED, "ao_volume %d is not implemented for the cone march", P.ao_volume);
-        if (P.ao_cones < 1 || P.ao_cones > MAX_CONES)
-            return fail(P2V_EINVAL, "ao_cones must lie in [1, %d]", MAX_CONES);
         ConeParams cp{};
-        int smax = std::max(g.s[0], std::max(g.s[1], g.s[2]));
-        int smin = std::min(g.s[0], std::min(g.s[1], g.s[2]));
-        int L = P.ao_levels > 0 ? P.ao_levels : (int) std::ceil(std::log2((double) smax));
-        L = std::max(1, std::min(L, MAX_LEVELS));
-        // the density grid is node-centred: as a texture it spans [min - h/2, max + h/2]
-        for (int a = 0; a < 3; ++a) {
-            const double hd = std::fabs((double) bb[a + 3] - (double) bb[a]) / (double) (g.s[a] - 1);
-            cp.bmin[a] = (float) ((double) bb[a] - 0.5 * hd);
-            cp.ibsize[a] = (float) (1.0 / (g.s[a] * hd));
-        }
-        cp.strength = P.ao_strength;
-        cp.sat = P.ao_volume_scale;
-        cp.border = 0;  // CLAMP_TO_BORDER (MDAOVolumeGenerator.cpp:58-60)
-        cp.early_exit = P.ao_early_exit ? 1 : 0;
-        cp.ncones = P.ao_cones;
-        cone_directions(P.ao_cones, P.ao_apex_deg * 3.14159265358979f / 180.0f, cp.dirs);
-        cp.nsteps = cone_steps(P.ao_offset, P.ao_cone_length, P.ao_steps, cp.dirs[0].w, (float) smin,
-                               (float) (L - 1), cp.t, cp.lod, MAX_STEPS);
-        if (P.ao_steps > MAX_STEPS || (P.ao_steps <= 0 && cp.nsteps >= MAX_STEPS))
-            return fail(P2V_EUNSUPPORTED, "more than %d samples per cone", MAX_STEPS);
-        cp.nlevels = L;
-        // level 0 is the density grid itself (saturated on the fly); levels 1.. are built here
-        size_t need = 0;
-        int d[MAX_LEVELS][3];
-        for (int a = 0; a < 3; ++a)
-            d[0][a] = g.s[a];
-        for (int l = 1; l < L; ++l) {
-            for (int a = 0; a < 3; ++a)
-                d[l][a] = std::max(1, d[l - 1][a] / 2);
-            need += (size_t) d[l][0] * d[l][1] * d[l][2];
-        }
-        P2V_CUDA_TRY(mips.ensure(sizeof(float) * (need + 1)));
-        float* lvp[MAX_LEVELS];
-        lvp[0] = const_cast<float*>(dgrid);
-        size_t off = 0;
-        for (int l = 1; l < L; ++l) {
-            lvp[l] = mips.as<float>() + off;
-            off += (size_t) d[l][0] * d[l][1] * d[l][2];
-        }
-        int dims[MAX_LEVELS][3];
-        P2V_CUDA_TRY(launch_mip_levels(dgrid, g.s, cp.sat, L, lvp, dims, sms, st));
-        for (int l = 0; l < L; ++l) {
-            cp.lv[l].v = lvp[l];
-            for (int a = 0; a < 3; ++a) {
-                cp.lv[l].d[a] = d[l][a];
-                cp.lv[l].fd[a] = (float) d[l][a];
-            }
-        }
-        P2V_CUDA_TRY(launch_cone_ao(cp, order, xyzr.as<float4>(), nrm.as<float4>(), n, ao.as<float>(), st));
+        const p2v_status bs = build_cone(g, dgrid, bb, cp, st);
+        if (bs != P2V_OK)
+            return bs;
+        P2V_CUDA_TRY(launch_cone_ao(cp, order, xyzr.as<float4>(), nrm.as<float4>(), n, nullptr, ao.as<float>(), st));
+        return P2V_OK;
+    }
+    if (P.ao_mode == P2V_AO_LEARNED) {
+        if (!mlp_ready)
+            return fail(P2V_EINVAL, "learned AO: no trained network (p2v_mlp_train or p2v_mlp_load first)");
+        ConeParams cp{};
+        const p2v_status bs = build_cone(g, dgrid, bb, cp, st);
+        if (bs != P2V_OK)
+            return bs;
+        if (cp.nlevels < 2)
+            return fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
+        if (mlp_level >= 0)
+            cp.stencil_level = std::min(mlp_level, cp.nlevels - 2);
+        P2V_CUDA_TRY(fb_list.ensure(sizeof(uint32_t) * ((size_t) n + 1)));
+        FrameScalars* fs = scal.as<FrameScalars>();
+        MlpInferArgs a{};
+        a.P = mlp_P.as<float>();
+        a.w1h = mlp_w1h.as<__nv_bfloat16>();
+        a.w2h = mlp_w2h.as<__nv_bfloat16>();
+        a.lo = mlp_has_range ? mlp_lo.as<float>() : nullptr;
+        a.hi = mlp_has_range ? mlp_hi.as<float>() : nullptr;
+        a.n = n;
+        a.order = order;
+        a.xyzr = xyzr.as<float4>();
+        a.nrm = nrm.as<float4>();
+        a.y = ao.as<float>();
+        a.fallback = fb_list.as<uint32_t>();
+        a.nfallback = &fs->ao_fallback;
+        P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
+        // the plain cone march for every particle whose stencil left the training range
+        P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), xyzr.as<float4>(), nrm.as<float4>(), n,
+                                    &fs->ao_fallback, ao.as<float>(), st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_AOSPHERE_AXES || P.ao_mode == P2V_AO_AOSPHERE_NORMAL) {
@@ -567,6 +636,58 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
     }
     return fail(P2V_EUNSUPPORTED, "ao_mode %d is not implemented", P.ao_mode);
 }
+
+p2v_status p2v_ctx::mlp_alloc() {
+    P2V_CUDA_TRY(mlp_P.ensure(sizeof(float) * MLP_NPARAM));
+    P2V_CUDA_TRY(mlp_m.ensure(sizeof(float) * MLP_NPARAM));
+    P2V_CUDA_TRY(mlp_v.ensure(sizeof(float) * MLP_NPARAM));
+    P2V_CUDA_TRY(mlp_g.ensure(sizeof(float) * MLP_NPARAM));
+    P2V_CUDA_TRY(mlp_loss.ensure(sizeof(float) * 4));
+    P2V_CUDA_TRY(mlp_w1h.ensure(sizeof(__nv_bfloat16) * MLP_H * MLP_KP));
+    P2V_CUDA_TRY(mlp_w2h.ensure(sizeof(__nv_bfloat16) * MLP_H * MLP_H));
+    P2V_CUDA_TRY(mlp_lo.ensure(sizeof(float) * MLP_IN));
+    P2V_CUDA_TRY(mlp_hi.ensure(sizeof(float) * MLP_IN));
+    return P2V_OK;
+}
+
+// Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases, last bias `bias3`; Adam state cleared.
+void p2v_ctx::mlp_init_params(uint64_t seed, float bias3) {
+    std::vector<float> h(MLP_NPARAM, 0.0f);
+    std::mt19937_64 rng(seed);
+    auto fill = [&](int off, int count, int fan_in) {
+        std::uniform_real_distribution<float> u(-1.0f / std::sqrt((float) fan_in), 1.0f / std::sqrt((float) fan_in));
+        for (int k = 0; k < count; ++k)
+            h[off + k] = u(rng);
+    };
+    fill(OFF_W1, MLP_H * MLP_IN, MLP_IN);
+    fill(OFF_W2, MLP_H * MLP_H, MLP_H);
+    fill(OFF_W3, MLP_H, MLP_H);
+    h[OFF_B3] = bias3;
+    cudaMemcpy(mlp_P.ptr, h.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
+    cudaMemset(mlp_m.ptr, 0, sizeof(float) * MLP_NPARAM);
+    cudaMemset(mlp_v.ptr, 0, sizeof(float) * MLP_NPARAM);
+    mlp_step = 0;
+    mlp_seed = seed;
+}
+
+namespace {
+// Grow a device buffer keeping its first `used` bytes.
+cudaError_t grow_keep(DevBuf& b, size_t need, size_t used) {
+    if (need <= b.bytes)
+        return cudaSuccess;
+    DevBuf nb;
+    cudaError_t e = nb.ensure(need);
+    if (e != cudaSuccess)
+        return e;
+    if (used && b.ptr)
+        e = cudaMemcpy(nb.ptr, b.ptr, used, cudaMemcpyDeviceToDevice);
+    b.release();
+    b = nb;
+    return e;
+}
+
+constexpr char MLP_MAGIC[8] = {'P', '2', 'V', 'M', 'L', 'P', '0', '1'};
+}  // namespace
 
 extern "C" {
 
@@ -642,7 +763,9 @@ void p2v_destroy(p2v_ctx* c) {
         cudaStreamSynchronize(c->own_stream);
     for (DevBuf* b : {&c->raw, &c->xyzr, &c->rec_a, &c->rec_b, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
                       &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal, &c->nrm, &c->ao, &c->mips,
-                      &c->aos_acc, &c->aos_tex})
+                      &c->aos_acc, &c->aos_tex, &c->mlp_P, &c->mlp_m, &c->mlp_v, &c->mlp_g, &c->mlp_part,
+                      &c->mlp_ploss, &c->mlp_loss, &c->mlp_w1h, &c->mlp_w2h, &c->mlp_lo, &c->mlp_hi, &c->mlp_idx,
+                      &c->mlp_y, &c->fb_list, &c->tX, &c->tT})
         b->release();
     for (auto& e : c->ev)
         if (e)
@@ -704,6 +827,368 @@ size_t p2v_get_last_error(const p2v_ctx* c, char* buf, size_t len) {
         buf[len - 1] = '\0';
     }
     return c->err.size();
+}
+
+}  // extern "C"
+
+extern "C" {
+
+void p2v_train_params_default(p2v_train_params* tp) {
+    if (!tp)
+        return;
+    std::memset(tp, 0, sizeof(*tp));
+    tp->struct_size = sizeof(p2v_train_params);
+    tp->epochs = 16;
+    tp->batch = 4096;
+    tp->lr = 3e-3f;
+    tp->beta1 = 0.9f;
+    tp->beta2 = 0.999f;
+    tp->eps = 1e-8f;
+    tp->lr_decay = 0.8f;
+    tp->val_fraction = 0.05f;
+    tp->range_margin = 0.05f;
+    tp->seed = 12345;
+}
+
+p2v_status p2v_mlp_clear(p2v_ctx* c) {
+    if (!c)
+        return P2V_EINVAL;
+    c->t_pairs = 0;
+    c->mlp_level = -1;
+    c->t_valid.clear();
+    c->t_host_T.clear();
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, uint64_t seed, uint64_t* total) {
+    if (!c || !fr)
+        return P2V_EINVAL;
+    const p2v_params saved = c->prm;
+    c->prm.ao_mode = P2V_AO_CONE;
+    p2v_status st = c->run_frame(fr, nullptr, c->own_stream);
+    c->prm = saved;
+    if (st != P2V_OK)
+        return st;
+    const uint32_t nvalid = (uint32_t) c->stats.particles_binned;
+    const uint32_t nsel = std::min(max_pairs, nvalid);
+    if (c->last_cp.nlevels < 2)
+        return c->fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
+    // the first frame fixes the stencil levels of the training set; later frames use the same levels
+    if (c->t_pairs == 0 || c->mlp_level < 0)
+        c->mlp_level = c->last_cp.stencil_level;
+    c->last_cp.stencil_level = std::min(c->mlp_level, c->last_cp.nlevels - 2);
+    if (nsel > 0) {
+        std::vector<uint32_t> sel(nvalid);
+        std::iota(sel.begin(), sel.end(), 0u);
+        if (nsel < nvalid) {
+            std::mt19937_64 rng(seed);
+            for (uint32_t i = 0; i < nsel; ++i) {
+                std::uniform_int_distribution<uint32_t> d(i, nvalid - 1);
+                std::swap(sel[i], sel[d(rng)]);
+            }
+            sel.resize(nsel);
+            std::sort(sel.begin(), sel.end());
+        }
+        if (cudaSetDevice(c->device) != cudaSuccess)
+            return c->fail(P2V_ECUDA, "cudaSetDevice failed");
+        const uint64_t newp = c->t_pairs + nsel;
+        if (grow_keep(c->tX, sizeof(float) * newp * MLP_IN, sizeof(float) * c->t_pairs * MLP_IN) != cudaSuccess ||
+            grow_keep(c->tT, sizeof(float) * newp, sizeof(float) * c->t_pairs) != cudaSuccess ||
+            c->mlp_idx.ensure(sizeof(uint32_t) * (nsel + 4)) != cudaSuccess)
+            return c->fail(P2V_ENOMEM, "training buffer of %llu pairs", (unsigned long long) newp);
+        uint32_t* d_sel = c->mlp_idx.as<uint32_t>();
+        uint32_t* d_kept = d_sel + nsel;
+        cudaMemcpyAsync(d_sel, sel.data(), sizeof(uint32_t) * nsel, cudaMemcpyHostToDevice, c->own_stream);
+        cudaMemsetAsync(d_kept, 0, sizeof(uint32_t), c->own_stream);
+        cudaError_t e = launch_mlp_collect(c->last_cp, c->last_order, d_sel, nsel, c->xyzr.as<float4>(),
+                                           c->nrm.as<float4>(), c->ao.as<float>(),
+                                           c->tX.as<float>() + c->t_pairs * MLP_IN, c->tT.as<float>() + c->t_pairs,
+                                           d_kept, c->own_stream);
+        if (e != cudaSuccess)
+            return c->fail(P2V_ECUDA, "collect: %s", cudaGetErrorString(e));
+        std::vector<float> ht(nsel);
+        cudaMemcpyAsync(ht.data(), c->tT.as<float>() + c->t_pairs, sizeof(float) * nsel, cudaMemcpyDeviceToHost,
+                        c->own_stream);
+        if ((e = cudaStreamSynchronize(c->own_stream)) != cudaSuccess)
+            return c->fail(P2V_ECUDA, "collect: %s", cudaGetErrorString(e));
+        c->t_host_T.resize(newp);
+        for (uint32_t i = 0; i < nsel; ++i) {
+            c->t_host_T[c->t_pairs + i] = ht[i];
+            if (ht[i] >= 0.0f)
+                c->t_valid.push_back((uint32_t) (c->t_pairs + i));
+        }
+        c->t_pairs = newp;
+    }
+    if (total)
+        *total = c->t_valid.size();
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_train(p2v_ctx* c, const p2v_train_params* tp, p2v_train_report* rep) {
+    if (!c || !tp)
+        return P2V_EINVAL;
+    if (tp->struct_size != sizeof(p2v_train_params))
+        return c->fail(P2V_EINVAL, "p2v_train_params.struct_size mismatch");
+    if (tp->epochs < 1 || tp->batch < 1 || tp->batch > (1 << 20) || !(tp->lr > 0.0f))
+        return c->fail(P2V_EINVAL, "invalid training parameters");
+    if (c->t_valid.size() < 2)
+        return c->fail(P2V_EINVAL, "no training pairs (p2v_mlp_collect first)");
+    const auto t0 = std::chrono::steady_clock::now();
+    if (cudaSetDevice(c->device) != cudaSuccess)
+        return c->fail(P2V_ECUDA, "cudaSetDevice failed");
+    p2v_status ps = c->mlp_alloc();
+    if (ps != P2V_OK)
+        return ps;
+    std::vector<uint32_t> all = c->t_valid;
+    std::mt19937_64 rng(tp->seed);
+    std::shuffle(all.begin(), all.end(), rng);
+    size_t nval = (size_t) std::floor(tp->val_fraction * (double) all.size());
+    nval = std::min(nval, all.size() - 1);
+    std::vector<uint32_t> val(all.begin(), all.begin() + nval), train(all.begin() + nval, all.end());
+    std::sort(val.begin(), val.end());
+    double mean = 0.0;
+    for (uint32_t i : train)
+        mean += c->t_host_T[i];
+    mean /= (double) train.size();
+    mean = std::min(std::max(mean, 1e-3), 1.0 - 1e-3);
+    c->mlp_init_params(tp->seed, (float) std::log(mean / (1.0 - mean)));
+
+    const int batch = tp->batch;
+    const int nblk = (batch + 31) / 32;
+    if (c->mlp_idx.ensure(sizeof(uint32_t) * (train.size() + val.size() + 8)) != cudaSuccess ||
+        c->mlp_part.ensure(sizeof(float) * (size_t) nblk * MLP_NPARAM) != cudaSuccess ||
+        c->mlp_ploss.ensure(sizeof(float) * nblk) != cudaSuccess ||
+        c->mlp_y.ensure(sizeof(float) * (val.size() + 1)) != cudaSuccess)
+        return c->fail(P2V_ENOMEM, "training buffers");
+    uint32_t* d_idx = c->mlp_idx.as<uint32_t>();
+    uint32_t* d_val = d_idx + train.size();
+    cudaStream_t st = c->own_stream;
+    // feature ranges of the training pairs (the learned path falls back outside them)
+    cudaMemcpyAsync(d_idx, train.data(), sizeof(uint32_t) * train.size(), cudaMemcpyHostToDevice, st);
+    cudaError_t e = launch_mlp_range(c->tX.as<float>(), d_idx, (uint32_t) train.size(), tp->range_margin,
+                                     c->mlp_lo.as<float>(), c->mlp_hi.as<float>(), st);
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "range: %s", cudaGetErrorString(e));
+    float lr = tp->lr;
+    int steps = 0;
+    for (int ep = 0; ep < tp->epochs; ++ep) {
+        std::mt19937_64 er(tp->seed + 1 + (uint64_t) ep);
+        std::shuffle(train.begin(), train.end(), er);
+        cudaMemcpyAsync(d_idx, train.data(), sizeof(uint32_t) * train.size(), cudaMemcpyHostToDevice, st);
+        for (size_t b0 = 0; b0 < train.size(); b0 += (size_t) batch) {
+            const int nb = (int) std::min<size_t>((size_t) batch, train.size() - b0);
+            e = launch_mlp_train_step(c->mlp_P.as<float>(), c->tX.as<float>(), c->tT.as<float>(), d_idx + b0, nb,
+                                      c->mlp_part.as<float>(), c->mlp_ploss.as<float>(), c->mlp_g.as<float>(),
+                                      c->mlp_loss.as<float>(), st);
+            if (e == cudaSuccess)
+                e = launch_mlp_adam(c->mlp_P.as<float>(), c->mlp_g.as<float>(), c->mlp_m.as<float>(),
+                                    c->mlp_v.as<float>(), lr, tp->beta1, tp->beta2, tp->eps, ++c->mlp_step, st);
+            if (e != cudaSuccess)
+                return c->fail(P2V_ECUDA, "train step: %s", cudaGetErrorString(e));
+            ++steps;
+        }
+        lr *= tp->lr_decay;
+    }
+    float last_loss = 0.0f;
+    cudaMemcpyAsync(&last_loss, c->mlp_loss.ptr, sizeof(float), cudaMemcpyDeviceToHost, st);
+    const size_t last_nb = train.size() % (size_t) batch ? train.size() % (size_t) batch : (size_t) batch;
+    float val_rmse = 0.0f, val_max = 0.0f;
+    if (!val.empty()) {
+        cudaMemcpyAsync(d_val, val.data(), sizeof(uint32_t) * val.size(), cudaMemcpyHostToDevice, st);
+        launch_mlp_forward_f32(c->mlp_P.as<float>(), c->tX.as<float>(), d_val, (uint32_t) val.size(),
+                               c->mlp_y.as<float>(), st);
+        std::vector<float> y(val.size());
+        cudaMemcpyAsync(y.data(), c->mlp_y.ptr, sizeof(float) * val.size(), cudaMemcpyDeviceToHost, st);
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return c->fail(P2V_ECUDA, "validation: %s", cudaGetErrorString(e));
+        double se = 0.0;
+        for (size_t k = 0; k < val.size(); ++k) {
+            const double d = (double) y[k] - c->t_host_T[val[k]];
+            se += d * d;
+            val_max = std::max(val_max, (float) std::fabs(d));
+        }
+        val_rmse = (float) std::sqrt(se / (double) val.size());
+    }
+    e = launch_mlp_pack(c->mlp_P.as<float>(), c->mlp_w1h.as<__nv_bfloat16>(), c->mlp_w2h.as<__nv_bfloat16>(), st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "pack: %s", cudaGetErrorString(e));
+    c->mlp_ready = true;
+    c->mlp_has_range = true;
+    if (rep) {
+        rep->pairs_train = train.size();
+        rep->pairs_val = val.size();
+        rep->steps = steps;
+        rep->final_loss = last_loss / (float) last_nb;
+        rep->val_rmse = val_rmse;
+        rep->val_max_err = val_max;
+        rep->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_get_weights(p2v_ctx* c, float* out, uint64_t count) {
+    if (!c || !out || count < (uint64_t) MLP_NPARAM)
+        return P2V_EINVAL;
+    if (!c->mlp_P.ptr)
+        return c->fail(P2V_EINVAL, "no network");
+    cudaSetDevice(c->device);
+    if (cudaMemcpy(out, c->mlp_P.ptr, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return c->fail(P2V_ECUDA, "copy failed");
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_set_weights(p2v_ctx* c, const float* in, uint64_t count) {
+    if (!c || !in || count < (uint64_t) MLP_NPARAM)
+        return P2V_EINVAL;
+    cudaSetDevice(c->device);
+    p2v_status ps = c->mlp_alloc();
+    if (ps != P2V_OK)
+        return ps;
+    if (cudaMemcpy(c->mlp_P.ptr, in, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice) != cudaSuccess ||
+        launch_mlp_pack(c->mlp_P.as<float>(), c->mlp_w1h.as<__nv_bfloat16>(), c->mlp_w2h.as<__nv_bfloat16>(),
+                        nullptr) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess)
+        return c->fail(P2V_ECUDA, "set weights failed");
+    cudaMemset(c->mlp_m.ptr, 0, sizeof(float) * MLP_NPARAM);
+    cudaMemset(c->mlp_v.ptr, 0, sizeof(float) * MLP_NPARAM);
+    c->mlp_step = 0;
+    c->mlp_ready = true;
+    c->mlp_has_range = false;
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_gradients(p2v_ctx* c, const float* x, const float* t, uint32_t n, float* grad, float* loss) {
+    if (!c || !x || !t || !grad || n == 0 || !c->mlp_P.ptr)
+        return P2V_EINVAL;
+    cudaSetDevice(c->device);
+    const int nblk = (int) ((n + 31) / 32);
+    DevBuf dx, dt, di;
+    if (dx.ensure(sizeof(float) * (size_t) n * MLP_IN) != cudaSuccess || dt.ensure(sizeof(float) * n) != cudaSuccess ||
+        di.ensure(sizeof(uint32_t) * n) != cudaSuccess ||
+        c->mlp_part.ensure(sizeof(float) * (size_t) nblk * MLP_NPARAM) != cudaSuccess ||
+        c->mlp_ploss.ensure(sizeof(float) * nblk) != cudaSuccess) {
+        dx.release();
+        dt.release();
+        di.release();
+        return c->fail(P2V_ENOMEM, "gradient buffers");
+    }
+    std::vector<uint32_t> idx(n);
+    std::iota(idx.begin(), idx.end(), 0u);
+    cudaMemcpy(dx.ptr, x, sizeof(float) * (size_t) n * MLP_IN, cudaMemcpyHostToDevice);
+    cudaMemcpy(dt.ptr, t, sizeof(float) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(di.ptr, idx.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+    cudaError_t e = launch_mlp_train_step(c->mlp_P.as<float>(), dx.as<float>(), dt.as<float>(), di.as<uint32_t>(),
+                                          (int) n, c->mlp_part.as<float>(), c->mlp_ploss.as<float>(),
+                                          c->mlp_g.as<float>(), c->mlp_loss.as<float>(), nullptr);
+    float l = 0.0f;
+    if (e == cudaSuccess)
+        e = cudaMemcpy(grad, c->mlp_g.ptr, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&l, c->mlp_loss.ptr, sizeof(float), cudaMemcpyDeviceToHost);
+    dx.release();
+    dt.release();
+    di.release();
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "gradients: %s", cudaGetErrorString(e));
+    if (loss)
+        *loss = l / (float) n;
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_infer(p2v_ctx* c, const float* x, uint32_t n, float* y) {
+    if (!c || !x || !y || n == 0)
+        return P2V_EINVAL;
+    if (!c->mlp_ready)
+        return c->fail(P2V_EINVAL, "no trained network");
+    cudaSetDevice(c->device);
+    DevBuf dx, dy;
+    if (dx.ensure(sizeof(float) * (size_t) n * MLP_IN) != cudaSuccess || dy.ensure(sizeof(float) * n) != cudaSuccess) {
+        dx.release();
+        dy.release();
+        return c->fail(P2V_ENOMEM, "inference buffers");
+    }
+    cudaMemcpy(dx.ptr, x, sizeof(float) * (size_t) n * MLP_IN, cudaMemcpyHostToDevice);
+    MlpInferArgs a{};
+    a.P = c->mlp_P.as<float>();
+    a.w1h = c->mlp_w1h.as<__nv_bfloat16>();
+    a.w2h = c->mlp_w2h.as<__nv_bfloat16>();
+    a.n = n;
+    a.X = dx.as<float>();
+    a.y = dy.as<float>();
+    cudaError_t e = launch_mlp_infer(a, c->last_cp, true, c->sms, nullptr);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(y, dy.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    dx.release();
+    dy.release();
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "infer: %s", cudaGetErrorString(e));
+    return P2V_OK;
+}
+
+p2v_status p2v_mlp_save(p2v_ctx* c, const char* path) {
+    if (!c || !path || !c->mlp_ready)
+        return c ? c->fail(P2V_EINVAL, "no trained network to save") : P2V_EINVAL;
+    cudaSetDevice(c->device);
+    std::vector<float> P(MLP_NPARAM), m(MLP_NPARAM), v(MLP_NPARAM), lo(MLP_IN, -INFINITY), hi(MLP_IN, INFINITY);
+    cudaMemcpy(P.data(), c->mlp_P.ptr, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost);
+    cudaMemcpy(m.data(), c->mlp_m.ptr, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost);
+    cudaMemcpy(v.data(), c->mlp_v.ptr, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost);
+    if (c->mlp_has_range) {
+        cudaMemcpy(lo.data(), c->mlp_lo.ptr, sizeof(float) * MLP_IN, cudaMemcpyDeviceToHost);
+        cudaMemcpy(hi.data(), c->mlp_hi.ptr, sizeof(float) * MLP_IN, cudaMemcpyDeviceToHost);
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f)
+        return c->fail(P2V_EINVAL, "cannot open %s", path);
+    const int32_t hdr[7] = {1, MLP_IN, MLP_H, MLP_NPARAM, c->mlp_step, c->mlp_has_range ? 1 : 0, c->mlp_level};
+    bool ok = std::fwrite(MLP_MAGIC, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
+              std::fwrite(&c->mlp_seed, sizeof(uint64_t), 1, f) == 1 &&
+              std::fwrite(P.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
+              std::fwrite(m.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
+              std::fwrite(v.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
+              std::fwrite(lo.data(), sizeof(float), MLP_IN, f) == (size_t) MLP_IN &&
+              std::fwrite(hi.data(), sizeof(float), MLP_IN, f) == (size_t) MLP_IN;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? P2V_OK : c->fail(P2V_EINVAL, "write to %s failed", path);
+}
+
+p2v_status p2v_mlp_load(p2v_ctx* c, const char* path) {
+    if (!c || !path)
+        return P2V_EINVAL;
+    FILE* f = std::fopen(path, "rb");
+    if (!f)
+        return c->fail(P2V_EINVAL, "cannot open %s", path);
+    char magic[8];
+    int32_t hdr[7];
+    uint64_t seed = 0;
+    std::vector<float> P(MLP_NPARAM), m(MLP_NPARAM), v(MLP_NPARAM), lo(MLP_IN), hi(MLP_IN);
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, MLP_MAGIC, 8) == 0 &&
+              std::fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == 1 && hdr[1] == MLP_IN && hdr[2] == MLP_H &&
+              hdr[3] == MLP_NPARAM && std::fread(&seed, sizeof(uint64_t), 1, f) == 1 &&
+              std::fread(P.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
+              std::fread(m.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
+              std::fread(v.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
+              std::fread(lo.data(), sizeof(float), MLP_IN, f) == (size_t) MLP_IN &&
+              std::fread(hi.data(), sizeof(float), MLP_IN, f) == (size_t) MLP_IN;
+    std::fclose(f);
+    if (!ok)
+        return c->fail(P2V_EINVAL, "%s is not a p2v MLP file of this version", path);
+    p2v_status ps = p2v_mlp_set_weights(c, P.data(), MLP_NPARAM);
+    if (ps != P2V_OK)
+        return ps;
+    cudaMemcpy(c->mlp_m.ptr, m.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->mlp_v.ptr, v.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
+    c->mlp_step = hdr[4];
+    c->mlp_seed = seed;
+    c->mlp_has_range = hdr[5] != 0;
+    c->mlp_level = hdr[6];
+    if (c->mlp_has_range) {
+        cudaMemcpy(c->mlp_lo.ptr, lo.data(), sizeof(float) * MLP_IN, cudaMemcpyHostToDevice);
+        cudaMemcpy(c->mlp_hi.ptr, hi.data(), sizeof(float) * MLP_IN, cudaMemcpyHostToDevice);
+    }
+    return P2V_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,57 @@
+// Internal interfaces of the learned-AO MLP (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "ao_internal.h"
+
+namespace p2v {
+
+constexpr int MLP_IN = 131;   // 2 levels x 64 stencil samples + 3 normal components
+constexpr int MLP_KP = 144;   // input padded to a multiple of the MMA K (16)
+constexpr int MLP_H = 64;
+// parameter vector: W1[H][IN], b1[H], W2[H][H], b2[H], w3[H], b3
+constexpr int OFF_W1 = 0;
+constexpr int OFF_B1 = OFF_W1 + MLP_H * MLP_IN;
+constexpr int OFF_W2 = OFF_B1 + MLP_H;
+constexpr int OFF_B2 = OFF_W2 + MLP_H * MLP_H;
+constexpr int OFF_W3 = OFF_B2 + MLP_H;
+constexpr int OFF_B3 = OFF_W3 + MLP_H;
+constexpr int MLP_NPARAM = OFF_B3 + 1;
+
+struct MlpInferArgs {
+    const float* P;                 // FP32 parameters (biases, last layer)
+    const __nv_bfloat16* w1h;       // [H][KP] BF16
+    const __nv_bfloat16* w2h;       // [H][H] BF16
+    const float* lo;                // per-feature training range (nullable: no range check)
+    const float* hi;
+    uint32_t n;
+    // extracted features (inference on particles)
+    const uint32_t* order;          // sorted position -> particle index
+    const float4* xyzr;
+    const float4* nrm;
+    // given features (tests)
+    const float* X;
+    float* y;                       // output, indexed by particle (or by row for given features)
+    uint32_t* fallback;             // particle indices whose features left the training range (nullable)
+    uint32_t* nfallback;
+};
+
+size_t mlp_train_smem_bytes();
+cudaError_t launch_mlp_collect(const ConeParams& cp, const uint32_t* order, const uint32_t* sel, uint32_t nsel,
+    const float4* xyzr, const float4* nrm, const float* ao, float* X, float* T, uint32_t* kept, cudaStream_t st);
+cudaError_t launch_mlp_train_step(const float* P, const float* X, const float* T, const uint32_t* idx, int nbatch,
+    float* partial, float* partial_loss, float* grad, float* loss, cudaStream_t st);
+cudaError_t launch_mlp_adam(float* P, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+    int step, cudaStream_t st);
+cudaError_t launch_mlp_forward_f32(const float* P, const float* X, const uint32_t* idx, uint32_t n, float* y,
+    cudaStream_t st);
+cudaError_t launch_mlp_range(const float* X, const uint32_t* idx, uint32_t n, float margin, float* lo, float* hi,
+    cudaStream_t st);
+cudaError_t launch_mlp_pack(const float* P, __nv_bfloat16* w1h, __nv_bfloat16* w2h, cudaStream_t st);
+cudaError_t launch_mlp_infer(const MlpInferArgs& a, const ConeParams& cp, bool features_in, int sms, cudaStream_t st);
+
+}  // namespace p2v

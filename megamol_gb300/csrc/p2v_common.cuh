@@ -38,7 +38,7 @@ struct FrameScalars {
     uint32_t n_valid;
     uint32_t error;         // ERR_* bits
     uint32_t ngaps;
-    uint32_t pad;
+    uint32_t ao_fallback;   // learned AO: particles handed to the cone march
     double mass;            // FP64 sum of the raw grid
     float vmin, vmax;       // raw grid min / max
     float out_min, out_max; // after normalisation

@@ -82,6 +82,19 @@ class StatsC(C.Structure):
                 ("ao_fallback", C.c_uint32)]
 
 
+class TrainParams(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float), ("lr_decay", C.c_float),
+                ("val_fraction", C.c_float), ("range_margin", C.c_float), ("seed", C.c_uint64)]
+
+
+class TrainReport(C.Structure):
+    _fields_ = [("pairs_train", C.c_uint64), ("pairs_val", C.c_uint64), ("steps", C.c_int32),
+                ("final_loss", C.c_float), ("val_rmse", C.c_float), ("val_max_err", C.c_float), ("ms", C.c_double)]
+
+
+MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 131, 64, 12673
+
 # Every entry point include/p2v.h declares, with its ctypes signature.
 _SIGNATURES = {
     "p2v_abi_version": ([], C.c_int),
@@ -94,6 +107,17 @@ _SIGNATURES = {
     "p2v_get_device_volume": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)], C.c_int),
     "p2v_get_stats": ([C.c_void_p, C.POINTER(StatsC)], C.c_int),
     "p2v_get_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_size_t),
+    "p2v_train_params_default": ([C.POINTER(TrainParams)], None),
+    "p2v_mlp_collect": ([C.c_void_p, C.POINTER(FrameC), C.c_uint32, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+    "p2v_mlp_clear": ([C.c_void_p], C.c_int),
+    "p2v_mlp_train": ([C.c_void_p, C.POINTER(TrainParams), C.POINTER(TrainReport)], C.c_int),
+    "p2v_mlp_save": ([C.c_void_p, C.c_char_p], C.c_int),
+    "p2v_mlp_load": ([C.c_void_p, C.c_char_p], C.c_int),
+    "p2v_mlp_get_weights": ([C.c_void_p, C.c_void_p, C.c_uint64], C.c_int),
+    "p2v_mlp_set_weights": ([C.c_void_p, C.c_void_p, C.c_uint64], C.c_int),
+    "p2v_mlp_gradients": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)],
+                          C.c_int),
+    "p2v_mlp_infer": ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int),
 }
 
 _lib: Optional[C.CDLL] = None
@@ -193,6 +217,73 @@ class Context:
         p = Params()
         self._check(self.lib.p2v_get_params(self.h, C.byref(p)))
         return p
+
+    def _frame(self, lists, bbox, clipbox=None, frame_id=0):
+        arr = (ParticleListC * max(1, len(lists)))()
+        for i, L in enumerate(lists):
+            dp, mem = _ptr(L.data)
+            npp, _ = _ptr(L.normals)
+            ap, _ = _ptr(L.ao_out)
+            arr[i] = ParticleListC(int(L.vertex_type), int(L.stride), dp, L.n(), float(L.global_radius), mem,
+                                   npp or None, int(L.normal_stride), ap or None)
+        fr = FrameC()
+        fr.bbox[:] = [float(v) for v in bbox]
+        fr.clipbox[:] = [float(v) for v in (clipbox if clipbox is not None else bbox)]
+        fr.frame_id = frame_id
+        fr.list_count = len(lists)
+        fr.lists = arr
+        return fr, arr
+
+    # ---- learned AO ----
+    def mlp_collect(self, lists, bbox, max_pairs: int, seed: int = 0, clipbox=None) -> int:
+        fr, keep = self._frame(lists, bbox, clipbox)
+        total = C.c_uint64()
+        self._check(self.lib.p2v_mlp_collect(self.h, C.byref(fr), int(max_pairs), int(seed), C.byref(total)))
+        return int(total.value)
+
+    def mlp_clear(self):
+        self._check(self.lib.p2v_mlp_clear(self.h))
+
+    def mlp_train(self, **kw) -> dict:
+        tp = TrainParams()
+        self.lib.p2v_train_params_default(C.byref(tp))
+        for k, v in kw.items():
+            if not hasattr(tp, k):
+                raise AttributeError(f"unknown training parameter {k}")
+            setattr(tp, k, v)
+        rep = TrainReport()
+        self._check(self.lib.p2v_mlp_train(self.h, C.byref(tp), C.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in rep._fields_}
+
+    def mlp_save(self, path: str):
+        self._check(self.lib.p2v_mlp_save(self.h, path.encode()))
+
+    def mlp_load(self, path: str):
+        self._check(self.lib.p2v_mlp_load(self.h, path.encode()))
+
+    def mlp_get_weights(self) -> np.ndarray:
+        w = np.zeros(MLP_PARAMS, np.float32)
+        self._check(self.lib.p2v_mlp_get_weights(self.h, w.ctypes.data, w.size))
+        return w
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        self._check(self.lib.p2v_mlp_set_weights(self.h, w.ctypes.data, w.size))
+
+    def mlp_gradients(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        self._check(self.lib.p2v_mlp_gradients(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], g.ctypes.data,
+                                               C.byref(loss)))
+        return g, loss.value
+
+    def mlp_infer(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros(x.shape[0], np.float32)
+        self._check(self.lib.p2v_mlp_infer(self.h, x.ctypes.data, x.shape[0], y.ctypes.data))
+        return y
 
     def run_frame(self, lists: Sequence[ParticleList], bbox, out=None, clipbox=None, stream: int = 0,
                   frame_id: int = 0) -> dict:

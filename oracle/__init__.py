@@ -74,6 +74,8 @@ def lib() -> C.CDLL:
                                                C.c_float, C.c_void_p]
         f.p2vo_aosphere_ao_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float,
                                            C.c_float, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
+        f.p2vo_mlp_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_double),
+                                   C.c_void_p]
     return _lib
 
 
@@ -312,3 +314,22 @@ def aosphere_ao_f64(tex, clip, xyzr, normals, mode=0, step_len=0.5, eval_fac=1.0
     lib().p2vo_aosphere_ao_f64(t.ctypes.data, ss, cl, float(step_len), float(eval_fac), x.ctypes.data, nrm.ctypes.data,
                                x.shape[0], int(mode), out.ctypes.data)
     return out
+
+
+MLP_IN, MLP_HIDDEN = 131, 64
+MLP_NPARAM = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
+
+
+def mlp_f64(params, x, t=None, grads=True):
+    """FP64 forward (+ backward) of the learned-AO MLP; returns (loss, y, grads)."""
+    p = np.ascontiguousarray(params, np.float64)
+    assert p.size == MLP_NPARAM
+    xx = np.ascontiguousarray(x, np.float32)
+    n = xx.shape[0]
+    tt = np.ascontiguousarray(t, np.float32) if t is not None else None
+    y = np.zeros(n, np.float64)
+    g = np.zeros(MLP_NPARAM, np.float64) if grads else None
+    loss = C.c_double()
+    lib().p2vo_mlp_f64(p.ctypes.data, xx.ctypes.data, tt.ctypes.data if tt is not None else None, n,
+                       g.ctypes.data if g is not None else None, C.byref(loss), y.ctypes.data)
+    return loss.value, y, g

@@ -499,3 +499,80 @@ extern "C" void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], cons
         }
     }
 }
+
+/* ------------------------------------------------------------------------------------------------
+ * Learned-AO MLP, FP64 forward and backward (the check of the GPU training kernels)
+ * ---------------------------------------------------------------------------------------------- */
+extern "C" void p2vo_mlp_f64(const double* P, const float* x, const float* t, int64_t n, double* grads, double* loss,
+    double* y) {
+    const int IN = 131, H = 64;
+    const double* W1 = P;
+    const double* b1 = W1 + H * IN;
+    const double* W2 = b1 + H;
+    const double* b2 = W2 + H * H;
+    const double* w3 = b2 + H;
+    const double b3 = w3[H];
+    const int64_t np = (int64_t) H * IN + H + H * H + H + H + 1;
+    std::vector<double> g(grads ? np : 0, 0.0);
+    double L = 0.0;
+    std::vector<double> a1(H), h1(H), a2(H), h2(H), dh2(H), da2(H), dh1(H), da1(H);
+    auto sig = [](double v) { return 1.0 / (1.0 + std::exp(-v)); };
+    for (int64_t s = 0; s < n; ++s) {
+        const float* xs = x + s * IN;
+        for (int j = 0; j < H; ++j) {
+            double acc = b1[j];
+            for (int i = 0; i < IN; ++i)
+                acc += W1[j * IN + i] * xs[i];
+            a1[j] = acc;
+            h1[j] = acc * sig(acc);
+        }
+        for (int j = 0; j < H; ++j) {
+            double acc = b2[j];
+            for (int i = 0; i < H; ++i)
+                acc += W2[j * H + i] * h1[i];
+            a2[j] = acc;
+            h2[j] = acc * sig(acc);
+        }
+        double z = b3;
+        for (int j = 0; j < H; ++j)
+            z += w3[j] * h2[j];
+        const double ys = sig(z);
+        if (y)
+            y[s] = ys;
+        const double e = ys - (t ? t[s] : 0.0);
+        L += e * e;
+        if (!grads)
+            continue;
+        const double dz = 2.0 * e / n * ys * (1.0 - ys);
+        double* gW1 = g.data();
+        double* gb1 = gW1 + H * IN;
+        double* gW2 = gb1 + H;
+        double* gb2 = gW2 + H * H;
+        double* gw3 = gb2 + H;
+        for (int j = 0; j < H; ++j) {
+            gw3[j] += dz * h2[j];
+            dh2[j] = dz * w3[j];
+            const double sg = sig(a2[j]);
+            da2[j] = dh2[j] * sg * (1.0 + a2[j] * (1.0 - sg));
+            gb2[j] += da2[j];
+            for (int i = 0; i < H; ++i)
+                gW2[j * H + i] += da2[j] * h1[i];
+        }
+        gw3[H] += dz;
+        for (int i = 0; i < H; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < H; ++j)
+                acc += da2[j] * W2[j * H + i];
+            dh1[i] = acc;
+            const double sg = sig(a1[i]);
+            da1[i] = acc * sg * (1.0 + a1[i] * (1.0 - sg));
+            gb1[i] += da1[i];
+            for (int k = 0; k < IN; ++k)
+                gW1[i * IN + k] += da1[i] * xs[k];
+        }
+    }
+    if (loss)
+        *loss = n ? L / n : 0.0;
+    if (grads)
+        std::memcpy(grads, g.data(), sizeof(double) * np);
+}
