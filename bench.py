@@ -226,6 +226,53 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def train_learned_ao(ctx, f_main):
+    """Train the learned AO on cone-march pairs of other frames: LJ-liquid frames (seeds 3 and 4,
+    500,000 pairs each) and ten uniform 100k-particle frames of the small plain-method workload."""
+    from megamol_gb300 import p2v, synth
+
+    ctx.mlp_clear()
+    total = 0
+    frames = [(synth.lj_liquid(seed=s), 500_000) for s in (3, 4)]
+    frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000) for k in range(10)]
+    for k, (f, npairs) in enumerate(frames):
+        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1)
+        vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
+        ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
+        nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
+        ctx.set_params(**AO_PARAMS)
+        total = ctx.mlp_collect([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm)], f.bbox, npairs,
+                                seed=100 + k)
+    rep = ctx.mlp_train(seed=7)
+    ctx.set_params(sizex=f_main.res[0], sizey=f_main.res[1], sizez=f_main.res[2], normalize=1, **AO_PARAMS)
+    return total, rep
+
+
+def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, sampler=None):
+    """Device time per step (CUDA events on the launching stream) and per-stage times from the library."""
+    for _ in range(warmup):
+        ctx.run_frame(lists, bbox, out, stream=stream.cuda_stream)
+    stage = {"ms_binning": 0.0, "ms_density": 0.0, "ms_normalize": 0.0, "ms_ao": 0.0, "ao_fallback": 0}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.__enter__()
+    ev0.record(stream)
+    for _ in range(steps):
+        ctx.run_frame(lists, bbox, out, stream=stream.cuda_stream)
+        st = ctx.stats()
+        for k in stage:
+            stage[k] += st[k]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.__exit__()
+    barrier()
+    return ev0.elapsed_time(ev1) / steps, {k: v / steps for k, v in stage.items()}
+
+
 def run_ours(args):
     import torch
 
@@ -240,10 +287,10 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     f, desc = make_workload(args.workload, rank)
     ctx = p2v.Context(dev)
+    pairs, train_rep = train_learned_ao(ctx, f)
     grid0, nrm = setup_frame(ctx, f)
     V = f.res[0] * f.res[1] * f.res[2]
     stream = torch.cuda.Stream()
-    sp = stream.cuda_stream
     d_in = torch.from_numpy(f.xyzr).to(dev)
     d_nrm = torch.from_numpy(nrm).to(dev)
     d_ao = torch.empty(f.n, dtype=torch.float32, device=dev)
@@ -255,33 +302,33 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
-    # ---- device-resident throughput ----
-    for _ in range(args.warmup):
-        ctx.run_frame(dev_lists, f.bbox, d_out, stream=sp)
-    stage = {"ms_binning": 0.0, "ms_density": 0.0, "ms_normalize": 0.0, "ms_ao": 0.0}
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    def max_over_ranks(x):
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([x], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    # ---- plain cone-march pipeline ----
+    ctx.set_params(ao_mode=p2v.AO_CONE)
+    ms_plain, st_plain = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier)
+    ms_plain = max_over_ranks(ms_plain)
+    ao_plain = d_ao.cpu().numpy().copy()
+    # ---- learned-AO pipeline (MLP, cone-march fallback) ----
+    ctx.set_params(ao_mode=p2v.AO_LEARNED)
     sampler = ClockSampler(dev)
-    barrier()
-    torch.cuda.synchronize()
-    with sampler:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            ctx.run_frame(dev_lists, f.bbox, d_out, stream=sp)
-            st = ctx.stats()
-            for k in stage:
-                stage[k] += st[k]
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * f.n / (ms * 1e-3)
+    ms_learn, st_learn = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier,
+                                       sampler)
+    ms_learn = max_over_ranks(ms_learn)
+    ao_learn = d_ao.cpu().numpy()
+    rmse = float(np.sqrt(np.mean((ao_learn.astype(np.float64) - ao_plain) ** 2)))
     clocks = sampler.summary()
+    use_learned = rmse <= 0.02
+    mode = p2v.AO_LEARNED if use_learned else p2v.AO_CONE
+    ms, st = (ms_learn, st_learn) if use_learned else (ms_plain, st_plain)
+    ctx.set_params(ao_mode=mode)
+    value = ws * f.n / (ms * 1e-3)
 
     # ---- end to end through the public API, host buffers ----
     h_in = torch.from_numpy(f.xyzr).pin_memory()
@@ -289,50 +336,35 @@ def run_ours(args):
     h_ao = torch.empty(f.n, dtype=torch.float32).pin_memory()
     h_out = torch.empty(V, dtype=torch.float32).pin_memory()
     host_lists = [p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=h_nrm, ao_out=h_ao)]
-    for _ in range(2):
-        ctx.run_frame(host_lists, f.bbox, h_out, stream=sp)
     e2e_steps = max(3, args.steps // 2)
-    barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        ctx.run_frame(host_lists, f.bbox, h_out, stream=sp)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms, _ = time_pipeline(ctx, host_lists, f.bbox, h_out, e2e_steps, 2, stream, torch, barrier)
+    e2e_ms = max_over_ranks(e2e_ms)
     e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * (16 + 12)),
            "d2h_bytes_per_step": int(V * 4 + f.n * 4), "ms_per_step": e2e_ms}
 
-    # ---- roofline of the dominant kernel ----
+    # ---- roofline of the dominant kernel of the measured pipeline ----
     peak, peak_kind = peaks()
     nb = (f.res[0] + 2) * (f.res[1] + 2) * (f.res[2] + 2)
-    per = {k: v / args.steps for k, v in stage.items()}
     gather_bytes = f.n * 16 + V * 4 + nb * 4
     lv_bytes, d = 0, list(f.res)
     for _ in range(AO_PARAMS["ao_levels"]):
         lv_bytes += d[0] * d[1] * d[2] * 4
         d = [max(1, x // 2) for x in d]
     ao_bytes = f.n * (16 + 12 + 4) + lv_bytes
-    if per["ms_ao"] >= per["ms_density"]:
-        dom = ("p2v::cone_ao_kernel (+ mip levels)", ao_bytes, per["ms_ao"], "cone_ao_lj_liquid_4M.md")
+    ao_name = "p2v::mlp_infer_kernel (+ mip levels, fallback cone march)" if use_learned else \
+        "p2v::cone_ao_kernel (+ mip levels)"
+    if st["ms_ao"] >= st["ms_density"]:
+        dom = (ao_name, ao_bytes, st["ms_ao"], "learned_ao_lj_liquid_4M.md" if use_learned else "cone_ao_lj_liquid_4M.md")
     else:
-        dom = ("p2v::gather_fixed_kernel", gather_bytes, per["ms_density"], "density_gather_lj_liquid_4M.md")
+        dom = ("p2v::gather_fixed_kernel", gather_bytes, st["ms_density"], "density_gather_lj_liquid_4M.md")
     achieved = dom[1] / (dom[2] * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": profile_traffic(dom[3]) if args.workload == "lj_liquid_4M" else None,
                 "algorithmic_bytes": dom[1], "ms_per_launch": dom[2],
-                "stages_ms": {"binning": per["ms_binning"], "density": per["ms_density"],
-                              "normalize": per["ms_normalize"], "ao": per["ms_ao"]},
-                "density_gather": {"algorithmic_bytes": gather_bytes, "ms": per["ms_density"],
-                                   "frac": gather_bytes / (per["ms_density"] * 1e-3) / 1e9 / peak}}
+                "stages_ms": {k: st[k] for k in ("ms_binning", "ms_density", "ms_normalize", "ms_ao")},
+                "density_gather": {"algorithmic_bytes": gather_bytes, "ms": st["ms_density"],
+                                   "frac": gather_bytes / (st["ms_density"] * 1e-3) / 1e9 / peak}}
 
     # ---- CPU baseline (rank 0, N=1 only) ----
     cpu = None
@@ -340,19 +372,30 @@ def run_ours(args):
         nthreads = os.cpu_count() or 1
         v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm)
         cpu = {"value": v, "unit": "particles/s", "cores": nthreads, "kind": kind,
-               "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + cone AO on {AO_SAMPLE} "
+               "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on {AO_SAMPLE} "
                          f"particles scaled to the frame ({dt_ao:.2f} s)"}
 
     passes = 4
-    launches_per_step = 2 + 2 + passes + 3 + 1 + 2 + (AO_PARAMS["ao_levels"] - 1) + 1
+    launches_density = 2 + 2 + passes + 3 + 1 + 2
+    launches_ao = (AO_PARAMS["ao_levels"] - 1) + (2 if use_learned else 1)
     if rank == 0:
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip, gradient normals",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP: bf16 x bf16 -> f32)", "data": "synthetic",
+                "config": dict(desc, ao=("learned AO (MLP 131-64-64-1, BF16 tensor cores) with cone-march fallback"
+                                         if use_learned else "plain cone march") +
+                                        ", 8 cones x 32 steps, 3-level mip, gradient normals",
                                l2="per-step working set ~0.6 GB > 126 MB L2 (no flush)"),
+                "learned_vs_plain": {"plain_particles_per_s": ws * f.n / (ms_plain * 1e-3), "plain_ms": ms_plain,
+                                     "learned_particles_per_s": ws * f.n / (ms_learn * 1e-3), "learned_ms": ms_learn,
+                                     "speedup": ms_plain / ms_learn, "ao_rmse_learned_vs_plain": rmse,
+                                     "ao_max_err": float(np.abs(ao_learn - ao_plain).max()),
+                                     "fallback_particles": int(st_learn["ao_fallback"]),
+                                     "plain_ao_ms": st_plain["ms_ao"], "learned_ao_ms": st_learn["ms_ao"],
+                                     "training": {"pairs": pairs, "val_rmse": train_rep["val_rmse"],
+                                                  "steps": train_rep["steps"], "ms": train_rep["ms"]}},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches_per_step * args.steps, "clocks": clocks}
+                "gpu_launches": (launches_density + launches_ao) * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
