@@ -246,6 +246,22 @@ P2V_API p2v_status p2v_mlp_gradients(p2v_ctx* ctx, const float* x, const float* 
 /* Tensor-core (BF16 x BF16 -> FP32) inference on n given feature rows (host arrays). */
 P2V_API p2v_status p2v_mlp_infer(p2v_ctx* ctx, const float* x, uint32_t n, float* y);
 
+/* ---- allocation-free AOSphere AO ----
+ * No counterpart in the reference. For callers that cannot allocate device memory while computing AO
+ * (a renderer recording its frame into a CUDA graph, a host that fixed the library's memory budget up
+ * front, or a frame callback where cudaMalloc would stall the device). It computes what p2v_run_frame
+ * computes for ao_mode P2V_AO_AOSPHERE_AXES / P2V_AO_AOSPHERE_NORMAL, from caller-provided device
+ * buffers only: xyzr = count float4 (x, y, z, radius), normals = count float4 (x, y, z, unused),
+ * ao_out = count floats, clipbox = ObjectSpaceClipBox, vol_size = "vol::sizex/y/z" including the border.
+ * Its scratch is a static device array of P2V_NOALLOC_MAX_VOXELS voxels (3 MB, held by every GPU that
+ * loads the library); larger volumes are rejected with P2V_EINVAL. The first call on a device looks up
+ * that array's address (make it before any stream capture). Calls share the array: calls that overlap on
+ * the GPU race. Asynchronous on `stream` (a cudaStream_t, NULL = the legacy default stream). */
+#define P2V_NOALLOC_MAX_VOXELS (64 * 64 * 64)
+P2V_API p2v_status p2v_aosphere_ao_noalloc(const float* xyzr, const float* normals, uint64_t count,
+                                           const float clipbox[6], const int32_t vol_size[3], float step_len,
+                                           float gen_fac, float eval_fac, int32_t mode, float* ao_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

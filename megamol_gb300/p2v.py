@@ -118,6 +118,8 @@ _SIGNATURES = {
     "p2v_mlp_gradients": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)],
                           C.c_int),
     "p2v_mlp_infer": ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int),
+    "p2v_aosphere_ao_noalloc": ([C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                                 C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
 }
 
 _lib: Optional[C.CDLL] = None
