@@ -248,8 +248,9 @@ def train_learned_ao(ctx, f_main):
     return total, rep
 
 
-def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, sampler=None):
-    """Device time per step (CUDA events on the launching stream) and per-stage times from the library."""
+def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, sampler=None, tag="timed"):
+    """Device time per step (CUDA events on the launching stream) and per-stage times from the library.
+    The timed steps run inside an NVTX range named `tag` (profilers can restrict themselves to it)."""
     for _ in range(warmup):
         ctx.run_frame(lists, bbox, out, stream=stream.cuda_stream)
     stage = {"ms_binning": 0.0, "ms_density": 0.0, "ms_normalize": 0.0, "ms_ao": 0.0, "ao_fallback": 0}
@@ -259,6 +260,7 @@ def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, 
     torch.cuda.synchronize()
     if sampler:
         sampler.__enter__()
+    torch.cuda.nvtx.range_push(tag)
     ev0.record(stream)
     for _ in range(steps):
         ctx.run_frame(lists, bbox, out, stream=stream.cuda_stream)
@@ -267,6 +269,7 @@ def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, 
             stage[k] += st[k]
     ev1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     if sampler:
         sampler.__exit__()
     barrier()
@@ -312,14 +315,15 @@ def run_ours(args):
 
     # ---- plain cone-march pipeline ----
     ctx.set_params(ao_mode=p2v.AO_CONE)
-    ms_plain, st_plain = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier)
+    ms_plain, st_plain = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier,
+                                       tag="plain")
     ms_plain = max_over_ranks(ms_plain)
     ao_plain = d_ao.cpu().numpy().copy()
     # ---- learned-AO pipeline (MLP, cone-march fallback) ----
     ctx.set_params(ao_mode=p2v.AO_LEARNED)
     sampler = ClockSampler(dev)
     ms_learn, st_learn = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier,
-                                       sampler)
+                                       sampler, tag="learned")
     ms_learn = max_over_ranks(ms_learn)
     ao_learn = d_ao.cpu().numpy()
     rmse = float(np.sqrt(np.mean((ao_learn.astype(np.float64) - ao_plain) ** 2)))
@@ -337,7 +341,7 @@ def run_ours(args):
     h_out = torch.empty(V, dtype=torch.float32).pin_memory()
     host_lists = [p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=h_nrm, ao_out=h_ao)]
     e2e_steps = max(3, args.steps // 2)
-    e2e_ms, _ = time_pipeline(ctx, host_lists, f.bbox, h_out, e2e_steps, 2, stream, torch, barrier)
+    e2e_ms, _ = time_pipeline(ctx, host_lists, f.bbox, h_out, e2e_steps, 2, stream, torch, barrier, tag="e2e")
     e2e_ms = max_over_ranks(e2e_ms)
     e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * (16 + 12)),
            "d2h_bytes_per_step": int(V * 4 + f.n * 4), "ms_per_step": e2e_ms}

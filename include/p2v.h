@@ -141,7 +141,8 @@ typedef struct p2v_params {
     float ao_volume_scale;  /* density -> occlusion scale for P2V_AOVOL_DENSITY */
     int32_t ao_cones;       /* 3 = the MDAO direction set (SphereRenderer.cpp:2572-2587) */
     int32_t ao_steps;       /* 0 = MDAO geometric stepping t += t*w until cone_length; >0 = that many samples */
-    int32_t ao_levels;      /* mip levels sampled (level 0 = the volume) */
+    int32_t ao_levels;      /* mip levels sampled (level 0 = the volume); 0 = density: ceil(log2(longest edge)),
+                               MDAO: maxLod + 1 = ceil(log2(mdao_volume_size)) (SphereRenderer.cpp:2476) */
     float ao_apex_deg;      /* "ambient occlusion::apex" (50) */
     float ao_offset;        /* "ambient occlusion::offset" (0.01) */
     float ao_strength;      /* "ambient occlusion::strength" (1) */
@@ -217,6 +218,14 @@ P2V_API p2v_status p2v_run_frame(p2v_ctx* ctx, const p2v_frame* frame, p2v_volum
 /* Device pointer of the last density grid (valid until the next call on this context); the reference's
  * VolumetricDataCall cannot carry one, so this is an addition of this library. */
 P2V_API p2v_status p2v_get_device_volume(p2v_ctx* ctx, const float** dptr, uint64_t resolution[3]);
+
+/* Level `level` of the last cone-march pyramid (P2V_AO_CONE / P2V_AO_LEARNED): level 0 is the density grid
+ * (before the ao_volume_scale saturation) or the MDAO occupancy volume, whose R8 texture the reference
+ * keeps in GL (MDAOVolumeGenerator::GetVolumeTextureHandle, MDAOVolumeGenerator.cpp:46-48). dims receives
+ * the level's size (x, y, z); with out == NULL only dims is written. Otherwise copies the texels (x fastest)
+ * into out (host or device memory per mem, capacity in floats). Synchronises the device. */
+P2V_API p2v_status p2v_get_ao_volume(p2v_ctx* ctx, int32_t level, float* out, uint64_t capacity, int32_t mem,
+                                     int32_t dims[3]);
 
 P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
 /* Last error message of this context ("" if none); returns the message length. */

@@ -24,13 +24,23 @@ namespace {
 // mip pyramid: level l+1 voxel = sum of the children 2g .. min(2g+1, N-1), divided by 8 always
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) mip_level_kernel(const float* __restrict__ src, int sx, int sy, int sz,
-    float* __restrict__ dst, int dx, int dy, int dz, float sat_scale) {
+    float* __restrict__ dst, int dx, int dy, int dz, float sat_scale, int quantize) {
     const int64_t n = (int64_t) dx * dy * dz;
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
         const int x = (int) (i % dx);
         const int y = (int) ((i / dx) % dy);
         const int z = (int) (i / ((int64_t) dx * dy));
         const int x1 = min(2 * x + 1, sx - 1), y1 = min(2 * y + 1, sy - 1), z1 = min(2 * z + 1, sz - 1);
+        if (quantize) {
+            // R8 levels: children as 8-bit integers, the /8 rule rounded half up, stored as k/255
+            int k = 0;
+            for (int zz = 2 * z; zz <= z1; ++zz)
+                for (int yy = 2 * y; yy <= y1; ++yy)
+                    for (int xx = 2 * x; xx <= x1; ++xx)
+                        k += __float2int_rn(__ldg(src + ((int64_t) zz * sy + yy) * sx + xx) * 255.0f);
+            dst[i] = __fdiv_rn((float) ((k + 4) >> 3), 255.0f);
+            continue;
+        }
         float acc = 0.0f;
         for (int zz = 2 * z; zz <= z1; ++zz)
             for (int yy = 2 * y; yy <= y1; ++yy)
@@ -57,49 +67,115 @@ __device__ __forceinline__ float tex_fetch(const Level& L, int x, int y, int z, 
         y = min(max(y, 0), L.d[1] - 1);
         z = min(max(z, 0), L.d[2] - 1);
     }
-    float v = __ldg(L.v + ((int64_t) z * L.d[1] + y) * L.d[0] + x);
-    if (sat > 0.0f)
-        v = fminf(fmaxf(v * sat, 0.0f), 1.0f);
-    return v;
+    const float v = __ldg(L.v + ((int64_t) z * L.d[1] + y) * L.d[0] + x);
+    return sat > 0.0f ? fminf(fmaxf(v * sat, 0.0f), 1.0f) : v;
 }
 
+__device__ __forceinline__ float lerp_rn(float a, float b, float w) {
+    return __fmaf_rn(w, __fsub_rn(b, a), a);
+}
+
+__device__ __forceinline__ float saturate_if(float v, float sat) {
+    return sat > 0.0f ? fminf(fmaxf(v * sat, 0.0f), 1.0f) : v;
+}
+
+// One GL LINEAR sample. When the 2x2x2 block lies inside the level (the common case) the eight texels are
+// read from one base pointer without per-texel checks; the host keeps every level below 2^31 texels so the
+// offsets fit in 32 bits.
 __device__ __forceinline__ float trilinear(const Level& L, float ux, float uy, float uz, int border, float sat) {
-    const float cx = ux * L.fd[0] - 0.5f, cy = uy * L.fd[1] - 0.5f, cz = uz * L.fd[2] - 0.5f;
+    // explicitly rounded operations: every kernel that inlines this gets the same bits
+    const float cx = __fmaf_rn(ux, L.fd[0], -0.5f), cy = __fmaf_rn(uy, L.fd[1], -0.5f);
+    const float cz = __fmaf_rn(uz, L.fd[2], -0.5f);
     const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
     const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
-    const float fx = cx - fx0, fy = cy - fy0, fz = cz - fz0;
-    const float c000 = tex_fetch(L, x0, y0, z0, border, sat), c100 = tex_fetch(L, x0 + 1, y0, z0, border, sat);
-    const float c010 = tex_fetch(L, x0, y0 + 1, z0, border, sat), c110 = tex_fetch(L, x0 + 1, y0 + 1, z0, border, sat);
-    const float c001 = tex_fetch(L, x0, y0, z0 + 1, border, sat), c101 = tex_fetch(L, x0 + 1, y0, z0 + 1, border, sat);
-    const float c011 = tex_fetch(L, x0, y0 + 1, z0 + 1, border, sat);
-    const float c111 = tex_fetch(L, x0 + 1, y0 + 1, z0 + 1, border, sat);
-    const float c00 = c000 + fx * (c100 - c000), c10 = c010 + fx * (c110 - c010);
-    const float c01 = c001 + fx * (c101 - c001), c11 = c011 + fx * (c111 - c011);
-    const float c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
-    return c0 + fz * (c1 - c0);
+    const float fx = __fsub_rn(cx, fx0), fy = __fsub_rn(cy, fy0), fz = __fsub_rn(cz, fz0);
+    float c000, c100, c010, c110, c001, c101, c011, c111;
+    if (x0 >= 0 && y0 >= 0 && z0 >= 0 && x0 + 1 < L.d[0] && y0 + 1 < L.d[1] && z0 + 1 < L.d[2]) {
+        const int sy = L.d[0], sz = L.d[0] * L.d[1];
+        const float* b = L.v + ((z0 * L.d[1] + y0) * L.d[0] + x0);
+        c000 = saturate_if(__ldg(b), sat);
+        c100 = saturate_if(__ldg(b + 1), sat);
+        c010 = saturate_if(__ldg(b + sy), sat);
+        c110 = saturate_if(__ldg(b + sy + 1), sat);
+        c001 = saturate_if(__ldg(b + sz), sat);
+        c101 = saturate_if(__ldg(b + sz + 1), sat);
+        c011 = saturate_if(__ldg(b + sz + sy), sat);
+        c111 = saturate_if(__ldg(b + sz + sy + 1), sat);
+    } else {
+        c000 = tex_fetch(L, x0, y0, z0, border, sat);
+        c100 = tex_fetch(L, x0 + 1, y0, z0, border, sat);
+        c010 = tex_fetch(L, x0, y0 + 1, z0, border, sat);
+        c110 = tex_fetch(L, x0 + 1, y0 + 1, z0, border, sat);
+        c001 = tex_fetch(L, x0, y0, z0 + 1, border, sat);
+        c101 = tex_fetch(L, x0 + 1, y0, z0 + 1, border, sat);
+        c011 = tex_fetch(L, x0, y0 + 1, z0 + 1, border, sat);
+        c111 = tex_fetch(L, x0 + 1, y0 + 1, z0 + 1, border, sat);
+    }
+    const float c00 = lerp_rn(c000, c100, fx), c10 = lerp_rn(c010, c110, fx);
+    const float c01 = lerp_rn(c001, c101, fx), c11 = lerp_rn(c011, c111, fx);
+    const float c0 = lerp_rn(c00, c10, fy), c1 = lerp_rn(c01, c11, fy);
+    return lerp_rn(c0, c1, fz);
 }
 
 // Surface point and unit normal of particle `o`.
 __device__ __forceinline__ bool surface_point(const float4 p, const float4 nrm, float x[3], float n[3]) {
-    const float l2 = nrm.x * nrm.x + nrm.y * nrm.y + nrm.z * nrm.z;
+    const float l2 = __fmaf_rn(nrm.z, nrm.z, __fmaf_rn(nrm.y, nrm.y, __fmul_rn(nrm.x, nrm.x)));
     if (!(l2 > 0.0f))
         return false;
     const float il = rsqrtf(l2);
-    n[0] = nrm.x * il;
-    n[1] = nrm.y * il;
-    n[2] = nrm.z * il;
-    x[0] = p.x + p.w * n[0];
-    x[1] = p.y + p.w * n[1];
-    x[2] = p.z + p.w * n[2];
+    n[0] = __fmul_rn(nrm.x, il);
+    n[1] = __fmul_rn(nrm.y, il);
+    n[2] = __fmul_rn(nrm.z, il);
+    x[0] = __fmaf_rn(p.w, n[0], p.x);
+    x[1] = __fmaf_rn(p.w, n[1], p.y);
+    x[2] = __fmaf_rn(p.w, n[2], p.z);
     return true;
 }
 
+__device__ __forceinline__ void cross_rn(const float a[3], const float b[3], float out[3]) {
+    out[0] = __fsub_rn(__fmul_rn(a[1], b[2]), __fmul_rn(a[2], b[1]));
+    out[1] = __fsub_rn(__fmul_rn(a[2], b[0]), __fmul_rn(a[0], b[2]));
+    out[2] = __fsub_rn(__fmul_rn(a[0], b[1]), __fmul_rn(a[1], b[0]));
+}
+
+// One cone of the MDAO march (mdao_deferred_fragment_ambocc.inc.glsl:30-51) from normalised point u.
+__device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const float u[3], const float ex[3],
+                                            const float nn[3], const float ez[3]) {
+    const float4 cd = cp.dirs[c];
+    float dir[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        dir[a] = __fmaf_rn(ez[a], cd.z, __fmaf_rn(nn[a], cd.y, __fmul_rn(ex[a], cd.x)));
+    float acc = 0.0f;
+    for (int k = 0; k < cp.nsteps; ++k) {
+        const float t = cp.t[k];
+        const float lod = cp.lod[k];
+        const float qx = __fmaf_rn(t, dir[0], u[0]), qy = __fmaf_rn(t, dir[1], u[1]), qz = __fmaf_rn(t, dir[2], u[2]);
+        const int l0 = min((int) lod, cp.nlevels - 1);
+        const float fr = __fsub_rn(lod, (float) l0);
+        float vis = trilinear(cp.lv[l0], qx, qy, qz, cp.border, l0 == 0 ? cp.sat : 0.0f);
+        if (fr > 0.0f && l0 + 1 < cp.nlevels)
+            vis = __fmaf_rn(fr, trilinear(cp.lv[l0 + 1], qx, qy, qz, cp.border, 0.0f), __fmul_rn(1.0f - fr, vis));
+        acc = __fmaf_rn(1.0f - acc, vis, acc);
+        if (cp.early_exit && acc > 0.99f)
+            break;
+    }
+    return acc;
+}
+
+// G lanes per particle: G = 1 marches all cones in one thread (throughput: millions of particles); G > 1
+// spreads the cones over G lanes (latency: the short fallback list of the learned AO). The cone sum is
+// formed in cone order either way, so both give the same bits.
+template <int G>
 __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
     const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, const uint32_t* __restrict__ n_dev,
     float* __restrict__ ao) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = gt / G;
+    const int sub = (int) (gt % G);
     if (n_dev != nullptr)
         n = min(n, *n_dev);
+    // whole groups leave together (the group's lanes share i), so the shuffles below see full groups
     if (i >= n)
         return;
     const uint32_t o = order ? order[i] : i;
@@ -107,46 +183,41 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
     const float4 nv = nrm[o];
     float x[3], nn[3];
     if (!surface_point(p, nv, x, nn)) {
-        ao[o] = 1.0f;  // no normal: no occlusion
+        if (sub == 0)
+            ao[o] = 1.0f;  // no normal: no occlusion
         return;
     }
     // frame (mdao_deferred_fragment_ambocc.inc.glsl:18-21): new_y = n, new_x = cross(n, normalize(objPos)),
     // new_z = cross(new_x, new_y)
     float xn[3] = {x[0], x[1], x[2]};
-    const float xl2 = xn[0] * xn[0] + xn[1] * xn[1] + xn[2] * xn[2];
+    const float xl2 = __fmaf_rn(xn[2], xn[2], __fmaf_rn(xn[1], xn[1], __fmul_rn(xn[0], xn[0])));
     if (xl2 > 0.0f) {
         const float il = rsqrtf(xl2);
-        xn[0] *= il;
-        xn[1] *= il;
-        xn[2] *= il;
+        xn[0] = __fmul_rn(xn[0], il);
+        xn[1] = __fmul_rn(xn[1], il);
+        xn[2] = __fmul_rn(xn[2], il);
     } else {
         xn[0] = 1.0f;
         xn[1] = xn[2] = 0.0f;
     }
-    const float ex[3] = {nn[1] * xn[2] - nn[2] * xn[1], nn[2] * xn[0] - nn[0] * xn[2], nn[0] * xn[1] - nn[1] * xn[0]};
-    const float ez[3] = {ex[1] * nn[2] - ex[2] * nn[1], ex[2] * nn[0] - ex[0] * nn[2], ex[0] * nn[1] - ex[1] * nn[0]};
-    const float u[3] = {(x[0] - cp.bmin[0]) * cp.ibsize[0], (x[1] - cp.bmin[1]) * cp.ibsize[1],
-                        (x[2] - cp.bmin[2]) * cp.ibsize[2]};
+    float ex[3], ez[3];
+    cross_rn(nn, xn, ex);
+    cross_rn(ex, nn, ez);
+    const float u[3] = {__fmul_rn(__fsub_rn(x[0], cp.bmin[0]), cp.ibsize[0]),
+                        __fmul_rn(__fsub_rn(x[1], cp.bmin[1]), cp.ibsize[1]),
+                        __fmul_rn(__fsub_rn(x[2], cp.bmin[2]), cp.ibsize[2])};
     float ambient = 0.0f;
-    for (int c = 0; c < cp.ncones; ++c) {
-        const float4 cd = cp.dirs[c];
-        const float dir[3] = {ex[0] * cd.x + nn[0] * cd.y + ez[0] * cd.z, ex[1] * cd.x + nn[1] * cd.y + ez[1] * cd.z,
-                              ex[2] * cd.x + nn[2] * cd.y + ez[2] * cd.z};
-        float acc = 0.0f;
-        for (int k = 0; k < cp.nsteps; ++k) {
-            const float t = cp.t[k];
-            const float lod = cp.lod[k];
-            const float qx = u[0] + t * dir[0], qy = u[1] + t * dir[1], qz = u[2] + t * dir[2];
-            const int l0 = min((int) lod, cp.nlevels - 1);
-            const float fr = lod - (float) l0;
-            float vis = trilinear(cp.lv[l0], qx, qy, qz, cp.border, l0 == 0 ? cp.sat : 0.0f);
-            if (fr > 0.0f && l0 + 1 < cp.nlevels)
-                vis = (1.0f - fr) * vis + fr * trilinear(cp.lv[l0 + 1], qx, qy, qz, cp.border, 0.0f);
-            acc += (1.0f - acc) * vis;
-            if (cp.early_exit && acc > 0.99f)
-                break;
-        }
-        ambient += acc;
+    if (G == 1) {
+        for (int c = 0; c < cp.ncones; ++c)
+            ambient += march_cone(cp, c, u, ex, nn, ez);
+    } else {
+        // lane `sub` marches cone sub (G >= ncones); the group's first lane adds them up in cone order
+        const float a = sub < cp.ncones ? march_cone(cp, sub, u, ex, nn, ez) : 0.0f;
+        const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << ((threadIdx.x & 31) / G * G);
+        for (int c = 0; c < cp.ncones; ++c)
+            ambient += __shfl_sync(gmask, a, c, G);
+        if (sub != 0)
+            return;
     }
     ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
 }
@@ -252,8 +323,8 @@ __global__ void __launch_bounds__(256) pack_normals_kernel(const uint8_t* __rest
 
 }  // namespace
 
-cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int nlevels, float* const* out,
-    int (*dims)[3], int sms, cudaStream_t st) {
+cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int quantize, int nlevels,
+    float* const* out, int (*dims)[3], int sms, cudaStream_t st) {
     const float* src = l0;
     int sd[3] = {d0[0], d0[1], d0[2]};
     for (int l = 1; l < nlevels; ++l) {
@@ -261,7 +332,7 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
         const int64_t nv = (int64_t) dd[0] * dd[1] * dd[2];
         const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((nv + 255) / 256, (int64_t) sms * 32));
         mip_level_kernel<<<grd, 256, 0, st>>>(src, sd[0], sd[1], sd[2], out[l], dd[0], dd[1], dd[2],
-                                              l == 1 ? sat_scale : 0.0f);
+                                              l == 1 ? sat_scale : 0.0f, quantize);
         for (int a = 0; a < 3; ++a)
             dims[l][a] = dd[a];
         src = out[l];
@@ -275,7 +346,21 @@ cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const fl
     uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st) {
     if (n == 0)
         return cudaSuccess;
-    cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+    if (n_dev == nullptr) {
+        cone_ao_kernel<1><<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+    } else {
+        // a device-side count (the learned AO's fallback list) is usually tiny: spread the cones over lanes
+        // and size the grid for the list's capacity n, most of whose threads leave at once
+        const int g = cp.ncones <= 4 ? 4 : (cp.ncones <= 8 ? 8 : 16);
+        const uint64_t threads = (uint64_t) n * g;
+        const unsigned grd = (unsigned) ((threads + 127) / 128);
+        if (g == 4)
+            cone_ao_kernel<4><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+        else if (g == 8)
+            cone_ao_kernel<8><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+        else
+            cone_ao_kernel<16><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+    }
     return cudaGetLastError();
 }
 

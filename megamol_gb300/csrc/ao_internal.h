@@ -38,8 +38,21 @@ struct AOSphereParams {
     float origin[3], ext[3], sampd[3];  // posOrigin, posExtents, aoSampDist
 };
 
-cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int nlevels, float* const* out,
-    int (*dims)[3], int sms, cudaStream_t st);
+// MDAO occupancy volume geometry (uniforms of mdao_volume.geom/frag.glsl, MDAOVolumeGenerator.cpp:141-165)
+struct MdaoParams {
+    float bmin[3], inv[3], fd[3], cell[3];  // inBoundsMin, inBoundsSizeInverse, inVolumeSize, cellSize
+    float cell_vol, ps_scale, sphere_k;     // cell volume, point-size scale (geom:43), 4/3 * 3.14152
+    float half_vp[2];                       // half the slice viewport
+    int d[3];
+    int unorm8;                             // 1 = R8 texel values k/255, 0 = unquantised fractions
+};
+
+// quantize = 1: the levels are R8 textures (texels k/255; out = ((sum k + 4) / 8) / 255)
+cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int quantize, int nlevels,
+    float* const* out, int (*dims)[3], int sms, cudaStream_t st);
+// acc: scratch of 4 (unorm8) or 8 bytes per voxel; vol: level 0 of the MDAO volume (x fastest)
+cudaError_t launch_mdao_volume(const MdaoParams& mp, const uint32_t* order, const float4* xyzr, uint32_t n,
+    void* acc, float* vol, int sms, cudaStream_t st);
 // n_dev (nullable): device-side particle count, at most n (the cone march of the learned-AO fallback list)
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
     uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st);

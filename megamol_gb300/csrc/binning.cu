@@ -12,6 +12,7 @@
 // reference's truncation of the same quotient.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "p2v_common.cuh"
@@ -50,55 +51,53 @@ __device__ __forceinline__ uint32_t lane_id() {
     return threadIdx.x & 31u;
 }
 
+// Grid-stride over the list: each thread packs several particles and keeps running reductions, so the
+// frame-wide maxima and counts cost one atomic per block rather than per 256 particles.
 template<class T, int NC, bool ALIGNED>
 __global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, float4* __restrict__ xyzr,
     uint32_t* __restrict__ keys, uint32_t* __restrict__ idx, FrameScalars* __restrict__ fs) {
     __shared__ int32_t s_cmin[3][8], s_cmax[3][8];
     __shared__ uint32_t s_rmax[8], s_drop[8];
-    const uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
-    bool valid = false;
-    float r = 0.0f;
     int32_t cell[3] = {INT32_MAX, INT32_MAX, INT32_MAX};
     int32_t cellhi[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
-    bool present = i < L.count;
-    if (present) {
+    uint32_t rbits = 0u, drop = 0u;
+    const uint64_t step = (uint64_t) gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < L.count; i += step) {
         const uint8_t* rec = L.data + i * L.stride;
-        float x = load_comp<T, ALIGNED>(rec);
-        float y = load_comp<T, ALIGNED>(rec + sizeof(T));
-        float z = load_comp<T, ALIGNED>(rec + 2 * sizeof(T));
-        r = NC == 4 ? load_comp<T, ALIGNED>(rec + 3 * sizeof(T)) : L.global_radius;
-        float p[3] = {x, y, z};
-        valid = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(r) && r > 0.0f;
+        const float x = load_comp<T, ALIGNED>(rec);
+        const float y = load_comp<T, ALIGNED>(rec + sizeof(T));
+        const float z = load_comp<T, ALIGNED>(rec + 2 * sizeof(T));
+        const float r = NC == 4 ? load_comp<T, ALIGNED>(rec + 3 * sizeof(T)) : L.global_radius;
+        const float p[3] = {x, y, z};
+        bool valid = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(r) && r > 0.0f;
         uint32_t bin[3];
+        int32_t c[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            float q = (p[a] - g.minf[a]) / g.hf[a];
+            const float q = (p[a] - g.minf[a]) / g.hf[a];
             valid = valid && fabsf(q) < 1073741824.0f;
-            int32_t c = clamp_cell(q);
-            cell[a] = c;
-            int32_t b = c < -1 ? -1 : (c > g.s[a] ? g.s[a] : c);
+            c[a] = clamp_cell(q);
+            const int32_t b = c[a] < -1 ? -1 : (c[a] > g.s[a] ? g.s[a] : c[a]);
             bin[a] = static_cast<uint32_t>(b + 1);
         }
         uint32_t key = g.nbins;
-        if (valid)
+        if (valid) {
             key = (bin[2] * g.nb[1] + bin[1]) * g.nb[0] + bin[0];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                cell[a] = min(cell[a], c[a]);
+                cellhi[a] = max(cellhi[a], c[a]);
+            }
+            rbits = max(rbits, __float_as_uint(r));
+        } else {
+            ++drop;
+        }
         const uint64_t o = L.offset + i;
         xyzr[o] = make_float4(x, y, z, r);
         keys[o] = key;
         idx[o] = static_cast<uint32_t>(o);
-        if (valid) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-                cellhi[a] = cell[a];
-        } else {
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-                cell[a] = INT32_MAX;
-        }
     }
     // block reduction: one atomic per block and quantity
-    uint32_t rbits = valid ? __float_as_uint(r) : 0u;
-    uint32_t drop = (present && !valid) ? 1u : 0u;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         rbits = max(rbits, __shfl_xor_sync(0xffffffffu, rbits, o));
@@ -388,7 +387,8 @@ cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, 
     if (L.count == 0)
         return cudaSuccess;
     const dim3 block(256);
-    const dim3 grid((unsigned) ((L.count + 255) / 256));
+    // about 8 particles per thread; at most 64 resident-sized blocks per SM
+    const dim3 grid((unsigned) std::max<uint64_t>(1, std::min<uint64_t>((L.count + 2047) / 2048, 152ull * 64)));
     const uintptr_t addr = reinterpret_cast<uintptr_t>(L.data);
     switch (L.type) {
     case 1: {  // FLOAT_XYZ

@@ -70,7 +70,7 @@ struct p2v_ctx {
     uint64_t datahash = 0;
 
     DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
-    DevBuf nrm, ao, mips, aos_acc, aos_tex;
+    DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol;
     // learned AO
     DevBuf mlp_P, mlp_m, mlp_v, mlp_g, mlp_part, mlp_ploss, mlp_loss, mlp_w1h, mlp_w2h, mlp_lo, mlp_hi, mlp_idx,
         mlp_y, fb_list;
@@ -102,7 +102,8 @@ struct p2v_ctx {
     p2v_status run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st);
     p2v_status run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
                       const uint32_t* order, cudaStream_t st);
-    p2v_status build_cone(const GridGeo& g, const float* dgrid, const float bb[6], ConeParams& cp, cudaStream_t st);
+    p2v_status build_cone(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
+                          const uint32_t* order, ConeParams& cp, cudaStream_t st);
     p2v_status mlp_alloc();
     void mlp_init_params(uint64_t seed, float bias3);
 };
@@ -493,48 +494,125 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     }
     if (hs.error & ERR_LOOKBACK_TIMEOUT)
         return fail(P2V_ETIMEOUT, "radix sort look-back wait gave up (device error 0x%x)", hs.error);
+    if (hs.error & ERR_MMA_TIMEOUT)
+        return fail(P2V_ETIMEOUT, "tensor-core MMA wait gave up (device error 0x%x)", hs.error);
     if (hs.error)
         return fail(P2V_EDOMAIN, "input outside the supported domain (device error 0x%x)", hs.error);
     err.clear();
     return P2V_OK;
 }
 
-p2v_status p2v_ctx::build_cone(const GridGeo& g, const float* dgrid, const float bb[6], ConeParams& cp,
-                               cudaStream_t st) {
+// MDAO volume size for a clip box (SphereRenderer.cpp:2463-2476): the longest edge gets vol_size voxels,
+// x is rounded up to a multiple of 4; Cuboid edges are absolute and Dimension::Scale multiplies in double.
+void mdao_dims(const float clip[6], int vol_size, int dims[3], float& shortest, float& max_lod) {
+    float size[3];
+    for (int a = 0; a < 3; ++a)
+        size[a] = std::fabs(clip[a + 3] - clip[a]);
+    const float w = size[0], h = size[1], d = size[2];
+    const float longest = ((w > h) && (w > d)) ? w : ((h > d) ? h : d);
+    const double f = static_cast<double>(static_cast<float>(vol_size) / longest);
+    float dm[3];
+    for (int a = 0; a < 3; ++a)
+        dm[a] = static_cast<float>(f * static_cast<double>(size[a]));
+    dm[0] = std::ceil(dm[0] / 4.0f) * 4.0f;
+    dm[1] = std::ceil(dm[1]);
+    dm[2] = std::ceil(dm[2]);
+    for (int a = 0; a < 3; ++a)
+        dims[a] = static_cast<int>(dm[a]);
+    shortest = std::min(dm[0], std::min(dm[1], dm[2]));
+    max_lod = std::ceil(std::log2(static_cast<float>(vol_size))) - 1.0f;
+}
+
+p2v_status p2v_ctx::build_cone(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
+                               uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st) {
     const p2v_params& P = prm;
-    if (P.ao_volume != P2V_AOVOL_DENSITY)
-        return fail(P2V_EUNSUPPORTED, "ao_volume %d is not implemented for the cone march", P.ao_volume);
+    if (P.ao_volume != P2V_AOVOL_DENSITY && P.ao_volume != P2V_AOVOL_MDAO)
+        return fail(P2V_EINVAL, "ao_volume %d is not a p2v_ao_volume", P.ao_volume);
     if (P.ao_cones < 1 || P.ao_cones > MAX_CONES)
         return fail(P2V_EINVAL, "ao_cones must lie in [1, %d]", MAX_CONES);
     cp = ConeParams{};
-    const int smax = std::max(g.s[0], std::max(g.s[1], g.s[2]));
-    const int smin = std::min(g.s[0], std::min(g.s[1], g.s[2]));
-    int L = P.ao_levels > 0 ? P.ao_levels : (int) std::ceil(std::log2((double) smax));
-    L = std::max(1, std::min(L, MAX_LEVELS));
-    // the density grid is node-centred: as a texture it spans [min - h/2, max + h/2]
-    for (int a = 0; a < 3; ++a) {
-        const double hd = std::fabs((double) bb[a + 3] - (double) bb[a]) / (double) (g.s[a] - 1);
-        cp.bmin[a] = (float) ((double) bb[a] - 0.5 * hd);
-        cp.ibsize[a] = (float) (1.0 / (g.s[a] * hd));
+    const bool mdao = P.ao_volume == P2V_AOVOL_MDAO;
+    int d0[3];
+    float shortest = 0.0f, max_lod = 0.0f;
+    int L = 0;
+    const float* level0 = dgrid;
+    if (mdao) {
+        // the occupancy voxelisation of the clip box (MDAOVolumeGenerator); its texture spans the clip box
+        if (P.mdao_volume_size < 1 || P.mdao_volume_size > 4096)
+            return fail(P2V_EINVAL, "mdao_volume_size must lie in [1, 4096]");
+        for (int a = 0; a < 3; ++a)
+            if (!(std::fabs(fr->clipbox[a + 3] - fr->clipbox[a]) > 0.0f) ||
+                !std::isfinite(fr->clipbox[a]) || !std::isfinite(fr->clipbox[a + 3]))
+                return fail(P2V_EINVAL, "clip box must have a finite, non-zero extent along %c (MDAO volume)",
+                            "xyz"[a]);
+        mdao_dims(fr->clipbox, P.mdao_volume_size, d0, shortest, max_lod);
+        const uint64_t nv = (uint64_t) d0[0] * d0[1] * d0[2];
+        if (nv > (1ull << 31))
+            return fail(P2V_EINVAL, "MDAO volume %dx%dx%d is too large", d0[0], d0[1], d0[2]);
+        MdaoParams mp{};
+        for (int a = 0; a < 3; ++a) {
+            const float size = std::fabs(fr->clipbox[a + 3] - fr->clipbox[a]);
+            mp.bmin[a] = fr->clipbox[a];
+            mp.inv[a] = 1.0f / size;
+            mp.fd[a] = static_cast<float>(d0[a]);
+            mp.d[a] = d0[a];
+            mp.cell[a] = 1.0f / (mp.fd[a] * mp.inv[a]);
+            cp.bmin[a] = mp.bmin[a];
+            cp.ibsize[a] = mp.inv[a];
+        }
+        mp.cell_vol = (mp.cell[0] * mp.cell[1]) * mp.cell[2];
+        mp.ps_scale = std::max(mp.inv[0] * mp.fd[0], mp.inv[1] * mp.fd[1]);
+        mp.sphere_k = 4.0f / 3.0f * 3.14152f;
+        mp.half_vp[0] = 0.5f * mp.fd[0];
+        mp.half_vp[1] = 0.5f * mp.fd[1];
+        mp.unorm8 = P.mdao_unorm8 ? 1 : 0;
+        P2V_CUDA_TRY(mdao_acc.ensure((mp.unorm8 ? 4 : 8) * nv));
+        P2V_CUDA_TRY(mdao_vol.ensure(sizeof(float) * nv));
+        P2V_CUDA_TRY(launch_mdao_volume(mp, order, xyzr.as<float4>(), n, mdao_acc.ptr, mdao_vol.as<float>(), sms, st));
+        level0 = mdao_vol.as<float>();
+        // the reference's texture holds every level down to 1x1x1; the lod clamp is maxLod
+        const int smax = std::max(d0[0], std::max(d0[1], d0[2]));
+        const int full = (int) std::floor(std::log2((double) smax)) + 1;
+        L = P.ao_levels > 0 ? P.ao_levels : std::min(full, (int) max_lod + 1);
+        L = std::max(1, std::min(L, MAX_LEVELS));
+        max_lod = std::min(max_lod, (float) (L - 1));
+        cp.sat = 0.0f;
+    } else {
+        for (int a = 0; a < 3; ++a)
+            d0[a] = g.s[a];
+        const int smax = std::max(g.s[0], std::max(g.s[1], g.s[2]));
+        shortest = (float) std::min(g.s[0], std::min(g.s[1], g.s[2]));
+        L = P.ao_levels > 0 ? P.ao_levels : (int) std::ceil(std::log2((double) smax));
+        L = std::max(1, std::min(L, MAX_LEVELS));
+        max_lod = (float) (L - 1);
+        // the density grid is node-centred: as a texture it spans [min - h/2, max + h/2]
+        for (int a = 0; a < 3; ++a) {
+            const double hd = std::fabs((double) bb[a + 3] - (double) bb[a]) / (double) (g.s[a] - 1);
+            cp.bmin[a] = (float) ((double) bb[a] - 0.5 * hd);
+            cp.ibsize[a] = (float) (1.0 / (g.s[a] * hd));
+        }
+        cp.sat = P.ao_volume_scale;
     }
     cp.strength = P.ao_strength;
-    cp.sat = P.ao_volume_scale;
     cp.border = 0;  // CLAMP_TO_BORDER (MDAOVolumeGenerator.cpp:58-60)
     cp.early_exit = P.ao_early_exit ? 1 : 0;
     cp.ncones = P.ao_cones;
     cone_directions(P.ao_cones, P.ao_apex_deg * 3.14159265358979f / 180.0f, cp.dirs);
-    cp.nsteps = cone_steps(P.ao_offset, P.ao_cone_length, P.ao_steps, cp.dirs[0].w, (float) smin, (float) (L - 1),
-                           cp.t, cp.lod, MAX_STEPS);
+    cp.nsteps = cone_steps(P.ao_offset, P.ao_cone_length, P.ao_steps, cp.dirs[0].w, shortest, max_lod, cp.t, cp.lod,
+                           MAX_STEPS);
     if (P.ao_steps > MAX_STEPS || (P.ao_steps <= 0 && cp.nsteps >= MAX_STEPS))
         return fail(P2V_EUNSUPPORTED, "more than %d samples per cone", MAX_STEPS);
     cp.nlevels = L;
     // the learned AO's stencil reads the two levels the cone's first sample blends
     cp.stencil_level = std::max(0, std::min((int) std::floor(cp.lod[0]), L - 2));
-    // level 0 is the density grid itself (saturated on the fly); levels 1.. are built here
+    // the samplers address texels with 32-bit offsets
+    if ((uint64_t) d0[0] * d0[1] * d0[2] >= (1ull << 31))
+        return fail(P2V_EUNSUPPORTED, "AO volume %dx%dx%d exceeds 2^31 texels", d0[0], d0[1], d0[2]);
+    // level 0 is the density grid (saturated on the fly) or the MDAO volume; levels 1.. are built here
     size_t need = 0;
     int d[MAX_LEVELS][3];
     for (int a = 0; a < 3; ++a)
-        d[0][a] = g.s[a];
+        d[0][a] = d0[a];
     for (int l = 1; l < L; ++l) {
         for (int a = 0; a < 3; ++a)
             d[l][a] = std::max(1, d[l - 1][a] / 2);
@@ -542,14 +620,14 @@ p2v_status p2v_ctx::build_cone(const GridGeo& g, const float* dgrid, const float
     }
     P2V_CUDA_TRY(mips.ensure(sizeof(float) * (need + 1)));
     float* lvp[MAX_LEVELS];
-    lvp[0] = const_cast<float*>(dgrid);
+    lvp[0] = const_cast<float*>(level0);
     size_t off = 0;
     for (int l = 1; l < L; ++l) {
         lvp[l] = mips.as<float>() + off;
         off += (size_t) d[l][0] * d[l][1] * d[l][2];
     }
     int dims[MAX_LEVELS][3];
-    P2V_CUDA_TRY(launch_mip_levels(dgrid, g.s, cp.sat, L, lvp, dims, sms, st));
+    P2V_CUDA_TRY(launch_mip_levels(level0, d0, cp.sat, mdao && P.mdao_unorm8 ? 1 : 0, L, lvp, dims, sms, st));
     for (int l = 0; l < L; ++l) {
         cp.lv[l].v = lvp[l];
         for (int a = 0; a < 3; ++a) {
@@ -566,7 +644,7 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
     const p2v_params& P = prm;
     if (P.ao_mode == P2V_AO_CONE) {
         ConeParams cp{};
-        const p2v_status bs = build_cone(g, dgrid, bb, cp, st);
+        const p2v_status bs = build_cone(fr, g, dgrid, bb, n, order, cp, st);
         if (bs != P2V_OK)
             return bs;
         P2V_CUDA_TRY(launch_cone_ao(cp, order, xyzr.as<float4>(), nrm.as<float4>(), n, nullptr, ao.as<float>(), st));
@@ -576,7 +654,7 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
         if (!mlp_ready)
             return fail(P2V_EINVAL, "learned AO: no trained network (p2v_mlp_train or p2v_mlp_load first)");
         ConeParams cp{};
-        const p2v_status bs = build_cone(g, dgrid, bb, cp, st);
+        const p2v_status bs = build_cone(fr, g, dgrid, bb, n, order, cp, st);
         if (bs != P2V_OK)
             return bs;
         if (cp.nlevels < 2)
@@ -598,6 +676,7 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
         a.y = ao.as<float>();
         a.fallback = fb_list.as<uint32_t>();
         a.nfallback = &fs->ao_fallback;
+        a.err = &fs->error;
         P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
         // the plain cone march for every particle whose stencil left the training range
         P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), xyzr.as<float4>(), nrm.as<float4>(), n,
@@ -763,7 +842,7 @@ void p2v_destroy(p2v_ctx* c) {
         cudaStreamSynchronize(c->own_stream);
     for (DevBuf* b : {&c->raw, &c->xyzr, &c->rec_a, &c->rec_b, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
                       &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal, &c->nrm, &c->ao, &c->mips,
-                      &c->aos_acc, &c->aos_tex, &c->mlp_P, &c->mlp_m, &c->mlp_v, &c->mlp_g, &c->mlp_part,
+                      &c->aos_acc, &c->aos_tex, &c->mdao_acc, &c->mdao_vol, &c->mlp_P, &c->mlp_m, &c->mlp_v, &c->mlp_g, &c->mlp_part,
                       &c->mlp_ploss, &c->mlp_loss, &c->mlp_w1h, &c->mlp_w2h, &c->mlp_lo, &c->mlp_hi, &c->mlp_idx,
                       &c->mlp_y, &c->fb_list, &c->tX, &c->tT})
         b->release();
@@ -809,6 +888,38 @@ p2v_status p2v_get_device_volume(p2v_ctx* c, const float** dptr, uint64_t resolu
     if (resolution)
         for (int a = 0; a < 3; ++a)
             resolution[a] = c->last_res[a];
+    return P2V_OK;
+}
+
+p2v_status p2v_get_ao_volume(p2v_ctx* c, int32_t level, float* out, uint64_t capacity, int32_t mem,
+                             int32_t dims[3]) {
+    if (!c || level < 0)
+        return P2V_EINVAL;
+    const ConeParams& cp = c->last_cp;
+    if (cp.nlevels < 1 || !cp.lv[0].v)
+        return c->fail(P2V_EINVAL, "no cone-march volume computed yet");
+    if (level >= cp.nlevels)
+        return c->fail(P2V_EINVAL, "level %d does not exist (the last pyramid has %d levels)", level, cp.nlevels);
+    const ConeLevel& L = cp.lv[level];
+    if (dims)
+        for (int a = 0; a < 3; ++a)
+            dims[a] = L.d[a];
+    if (!out)
+        return P2V_OK;
+    const uint64_t nv = (uint64_t) L.d[0] * L.d[1] * L.d[2];
+    if (capacity < nv)
+        return c->fail(P2V_EINVAL, "output capacity %llu < %llu texels", (unsigned long long) capacity,
+                       (unsigned long long) nv);
+    if (mem != P2V_MEM_HOST && mem != P2V_MEM_DEVICE)
+        return c->fail(P2V_EINVAL, "mem must be P2V_MEM_HOST or P2V_MEM_DEVICE");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, L.v, sizeof(float) * nv,
+                       mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "AO volume copy failed: %s", cudaGetErrorString(e));
     return P2V_OK;
 }
 
@@ -1104,12 +1215,16 @@ p2v_status p2v_mlp_infer(p2v_ctx* c, const float* x, uint32_t n, float* y) {
         return c->fail(P2V_EINVAL, "no trained network");
     cudaSetDevice(c->device);
     DevBuf dx, dy;
-    if (dx.ensure(sizeof(float) * (size_t) n * MLP_IN) != cudaSuccess || dy.ensure(sizeof(float) * n) != cudaSuccess) {
+    // dy holds the n outputs and, after them, the kernel's error word
+    if (dx.ensure(sizeof(float) * (size_t) n * MLP_IN) != cudaSuccess ||
+        dy.ensure(sizeof(float) * ((size_t) n + 1)) != cudaSuccess) {
         dx.release();
         dy.release();
         return c->fail(P2V_ENOMEM, "inference buffers");
     }
-    cudaMemcpy(dx.ptr, x, sizeof(float) * (size_t) n * MLP_IN, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(dx.ptr, x, sizeof(float) * (size_t) n * MLP_IN, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemset(dy.as<float>() + n, 0, sizeof(uint32_t));
     MlpInferArgs a{};
     a.P = c->mlp_P.as<float>();
     a.w1h = c->mlp_w1h.as<__nv_bfloat16>();
@@ -1117,13 +1232,20 @@ p2v_status p2v_mlp_infer(p2v_ctx* c, const float* x, uint32_t n, float* y) {
     a.n = n;
     a.X = dx.as<float>();
     a.y = dy.as<float>();
-    cudaError_t e = launch_mlp_infer(a, c->last_cp, true, c->sms, nullptr);
+    a.err = reinterpret_cast<uint32_t*>(dy.as<float>() + n);
+    if (e == cudaSuccess)
+        e = launch_mlp_infer(a, c->last_cp, true, c->sms, nullptr);
+    uint32_t derr = 0;
     if (e == cudaSuccess)
         e = cudaMemcpy(y, dy.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&derr, a.err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
     dx.release();
     dy.release();
     if (e != cudaSuccess)
         return c->fail(P2V_ECUDA, "infer: %s", cudaGetErrorString(e));
+    if (derr & ERR_MMA_TIMEOUT)
+        return c->fail(P2V_ETIMEOUT, "tensor-core MMA wait gave up (device error 0x%x)", derr);
     return P2V_OK;
 }
 

@@ -6,8 +6,9 @@
 // continuously with the point), then the unit normal. Network 131 -> 64 -> 64 -> 1, SiLU, SiLU, sigmoid.
 // Training: FP32 forward/backward kernels per CTA with a fixed-order reduction of the per-CTA gradients,
 // then Adam; pairs come from the plain cone march. Inference: BF16 weights and features, FP32 accumulation
-// on the tensor cores (mma.sync m16n8k16), bias/activations in FP32 registers. A particle whose features
-// leave the training range (per feature, with a margin) falls back to the cone march.
+// on the 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM), bias/activations in FP32. A
+// particle whose features leave the training range (per feature, with a margin) falls back to the cone
+// march.
 // No reference counterpart: the reference evaluates AO only by the GLSL cone march / AOSphere taps.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -27,6 +28,11 @@ __device__ __forceinline__ float silu(float a) {
     return a / (1.0f + __expf(-a));
 }
 
+// inference: fast division (2 ulp) instead of the IEEE quotient
+__device__ __forceinline__ float silu_fast(float a) {
+    return __fdividef(a, 1.0f + __expf(-a));
+}
+
 __device__ __forceinline__ float sigmoidf_(float a) {
     return 1.0f / (1.0f + __expf(-a));
 }
@@ -37,13 +43,13 @@ __device__ __forceinline__ float lv_fetch(const ConeLevel& L, int x, int y, int 
     return __ldg(L.v + ((int64_t) z * L.d[1] + y) * L.d[0] + x);
 }
 
-// 4x4x4 trilinear samples of level L at texel-spaced offsets (k - 1.5) around normalised point u;
-// out[(kz*4 + ky)*4 + kx]. The samples share one 5x5x5 block of texels and one set of weights.
-__device__ __forceinline__ void stencil64(const ConeLevel& L, float ux, float uy, float uz, float* out) {
-    const float cx = ux * L.fd[0] - 2.0f, cy = uy * L.fd[1] - 2.0f, cz = uz * L.fd[2] - 2.0f;
-    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
-    const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
-    const float fx = cx - fx0, fy = cy - fy0, fz = cz - fz0;
+// The 5x5x5 texel block of a stencil: FAST = inside the level (rows read from one base pointer), else
+// every texel is bounds-checked (CLAMP_TO_BORDER). emit(m, a, b) receives samples 2m and 2m+1.
+template<bool FAST, class Emit>
+__device__ __forceinline__ void stencil_block(const ConeLevel& L, int x0, int y0, int z0, float fx, float fy, float fz,
+                                              Emit& emit) {
+    const int sy = L.d[0], sz = L.d[0] * L.d[1];
+    const float* base = FAST ? L.v + ((z0 * L.d[1] + y0) * L.d[0] + x0) : nullptr;
     float prev[16];
 #pragma unroll
     for (int zz = 0; zz < 5; ++zz) {
@@ -52,9 +58,16 @@ __device__ __forceinline__ void stencil64(const ConeLevel& L, float ux, float uy
 #pragma unroll
         for (int yy = 0; yy < 5; ++yy) {
             float t[5];
+            if (FAST) {
+                const float* row = base + zz * sz + yy * sy;
 #pragma unroll
-            for (int xx = 0; xx < 5; ++xx)
-                t[xx] = lv_fetch(L, x0 + xx, y0 + yy, z0 + zz);
+                for (int xx = 0; xx < 5; ++xx)
+                    t[xx] = __ldg(row + xx);
+            } else {
+#pragma unroll
+                for (int xx = 0; xx < 5; ++xx)
+                    t[xx] = lv_fetch(L, x0 + xx, y0 + yy, z0 + zz);
+            }
             float rowc[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k)
@@ -70,13 +83,28 @@ __device__ __forceinline__ void stencil64(const ConeLevel& L, float ux, float uy
         }
         if (zz > 0) {
 #pragma unroll
-            for (int k = 0; k < 16; ++k)
-                out[(zz - 1) * 16 + k] = prev[k] + fz * (cur[k] - prev[k]);
+            for (int j = 0; j < 8; ++j)
+                emit((zz - 1) * 8 + j, prev[2 * j] + fz * (cur[2 * j] - prev[2 * j]),
+                     prev[2 * j + 1] + fz * (cur[2 * j + 1] - prev[2 * j + 1]));
         }
 #pragma unroll
         for (int k = 0; k < 16; ++k)
             prev[k] = cur[k];
     }
+}
+
+// 4x4x4 trilinear samples of level L at texel-spaced offsets (k - 1.5) around normalised point u, in the
+// order (kz*4 + ky)*4 + kx. The samples share one 5x5x5 block of texels and one set of weights.
+template<class Emit>
+__device__ __forceinline__ void stencil64(const ConeLevel& L, float ux, float uy, float uz, Emit&& emit) {
+    const float cx = ux * L.fd[0] - 2.0f, cy = uy * L.fd[1] - 2.0f, cz = uz * L.fd[2] - 2.0f;
+    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
+    const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
+    const float fx = cx - fx0, fy = cy - fy0, fz = cz - fz0;
+    if (x0 >= 0 && y0 >= 0 && z0 >= 0 && x0 + 4 < L.d[0] && y0 + 4 < L.d[1] && z0 + 4 < L.d[2])
+        stencil_block<true>(L, x0, y0, z0, fx, fy, fz, emit);
+    else
+        stencil_block<false>(L, x0, y0, z0, fx, fy, fz, emit);
 }
 
 // Surface point (normalised volume coordinates) and unit normal; false for a zero normal.
@@ -111,16 +139,15 @@ __global__ void __launch_bounds__(128) mlp_collect_kernel(const ConeParams cp, c
         T[i] = -1.0f;  // marks a pair without features; compacted away on the host side
         return;
     }
-    float f[64];
     float* x = X + (size_t) i * MLP_IN;
-    stencil64(cp.lv[cp.stencil_level], u[0], u[1], u[2], f);
-#pragma unroll
-    for (int k = 0; k < 64; ++k)
-        x[k] = f[k];
-    stencil64(cp.lv[cp.stencil_level + 1], u[0], u[1], u[2], f);
-#pragma unroll
-    for (int k = 0; k < 64; ++k)
-        x[64 + k] = f[k];
+    stencil64(cp.lv[cp.stencil_level], u[0], u[1], u[2], [&](int m, float a, float b) {
+        x[2 * m] = a;
+        x[2 * m + 1] = b;
+    });
+    stencil64(cp.lv[cp.stencil_level + 1], u[0], u[1], u[2], [&](int m, float a, float b) {
+        x[64 + 2 * m] = a;
+        x[64 + 2 * m + 1] = b;
+    });
     x[128] = n[0];
     x[129] = n[1];
     x[130] = n[2];
@@ -341,12 +368,8 @@ __global__ void __launch_bounds__(256) mlp_range_kernel(const float* __restrict_
 }
 
 // ---------------------------------------------------------------------------------------------
-// inference: BF16 tensor cores (mma.sync m16n8k16, FP32 accumulate)
+// inference weights: BF16 copies of W1 (K padded to 144 with zeros) and W2
 // ---------------------------------------------------------------------------------------------
-constexpr int W1P = 152;  // smem row pitch (bf16) of W1 and of the feature tile: conflict-free fragment loads
-constexpr int W2P = 72;
-constexpr int IWARPS = 4;
-
 __global__ void mlp_pack_kernel(const float* __restrict__ P, __nv_bfloat16* __restrict__ w1h,
     __nv_bfloat16* __restrict__ w2h) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < MLP_H * MLP_KP; k += gridDim.x * blockDim.x) {
@@ -357,66 +380,218 @@ __global__ void mlp_pack_kernel(const float* __restrict__ P, __nv_bfloat16* __re
         w2h[k] = __float2bfloat16_rn(P[OFF_W2 + k]);
 }
 
-__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-    uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// FEATURES_IN: features given in global memory (tests); else extracted from the mip levels.
+// ---------------------------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05). One CTA of 256 threads takes 128 particles per
+// tile. Threads t and t + 128 extract the two stencil levels of particle t straight into the A tile (BF16,
+// canonical no-swizzle K-major layout in shared memory); one thread issues the layer-1 MMAs (M = 128,
+// N = 64, K = 144) into 64 TMEM columns and commits them to an mbarrier. The epilogue reads TMEM
+// (warp w: lanes 32 (w % 4).., columns 32 (w / 4)..), adds the bias, applies SiLU and writes the hidden
+// layer back into the A tile as layer 2's A operand; layer 2 (K = 64) reuses the TMEM columns, and its
+// epilogue finishes layer 3 (64 -> 1) in FP32 with the sigmoid. The accumulators never occupy registers,
+// so three CTAs (24 warps) stay resident per SM to hide the stencil loads' latency. Every mbarrier wait
+// is bounded: on timeout the CTA records ERR_MMA_TIMEOUT, drains its MMAs (bounded) and frees TMEM.
+// ---------------------------------------------------------------------------------------------
+namespace tc {
+constexpr int THREADS = 256;
+constexpr int M = 128;                         // particles per tile (MMA M, TMEM lanes)
+constexpr int KCH1 = MLP_KP / 8;               // 16-byte core-matrix columns of layer 1's K (18)
+constexpr int KCH2 = MLP_H / 8;                // of layer 2's K (8)
+constexpr int SBO1 = KCH1 * 128;               // bytes between 8-row core-matrix groups, layer 1
+constexpr int SBO2 = KCH2 * 128;               // layer 2
+constexpr int A_BYTES = (M / 8) * SBO1;        // 36864: features; later the hidden layer (16384 B)
+constexpr int W1_BYTES = (MLP_H / 8) * SBO1;   // 18432
+constexpr int W2_BYTES = (MLP_H / 8) * SBO2;   // 8192
+constexpr int DYN_SMEM = A_BYTES + W1_BYTES + W2_BYTES;
+constexpr uint32_t TMEM_COLS = 64;
+constexpr uint32_t WAIT_LIMIT = 1u << 20;
+// instruction descriptor, kind::f16: D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12), both K-major,
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t) (MLP_H >> 3) << 17) |
+                           ((uint32_t) (M >> 4) << 24);
+}  // namespace tc
+
+// byte offset of element (row, k) in the canonical K-major layout: 8x8 BF16 core matrices of 128 B (row r
+// of a core matrix at 16 r), core matrices along K 128 B apart, 8-row groups `sbo` bytes apart
+__device__ __forceinline__ uint32_t canon_off(int row, int k, int sbo) {
+    return (uint32_t) ((row >> 3) * sbo + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start address, leading (K) byte offset, stride (8-row) byte offset,
+// bits 46-48 = 0b001, base offset 0, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t) ((saddr >> 4) & 0x3FFFu) | ((uint64_t) ((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t) ((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(tc::IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// bounded wait for phase `phase` of an mbarrier; false when the budget ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (uint32_t i = 0; i < tc::WAIT_LIMIT; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
+
+// 32 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+          "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+          "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+        v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint8_t* p, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+    *reinterpret_cast<uint4*>(p) = make_uint4(a, b, c, d);
+}
+
 template<bool FEATURES_IN>
-__global__ void __launch_bounds__(IWARPS * 32) mlp_infer_kernel(const MlpInferArgs args, const ConeParams cp) {
-    __shared__ __align__(16) __nv_bfloat16 sW1[MLP_H * W1P];
-    __shared__ __align__(16) __nv_bfloat16 sW2[MLP_H * W2P];
-    __shared__ __align__(16) __nv_bfloat16 sA[IWARPS][16 * W1P];
-    __shared__ float sB1[MLP_H], sB2[MLP_H], sW3[MLP_H], sLo[MLP_IN], sHi[MLP_IN];
+__global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    uint8_t* sA = tc_smem;
+    uint8_t* sW1 = tc_smem + tc::A_BYTES;
+    uint8_t* sW2 = sW1 + tc::W1_BYTES;
+    __shared__ float sB1[MLP_H], sB2[MLP_H], sW3[MLP_H];
+    __shared__ __align__(8) float2 sRange[MLP_KP / 2][2];
+    __shared__ __align__(8) uint64_t s_mbar;
+    __shared__ uint32_t s_tmem;
+    __shared__ float s_part[tc::M];
+    __shared__ uint32_t s_flag[tc::M];
+
     const int t = threadIdx.x;
-    for (int k = t; k < MLP_H * MLP_KP; k += blockDim.x)
-        sW1[(k / MLP_KP) * W1P + k % MLP_KP] = args.w1h[k];
-    for (int k = t; k < MLP_H * MLP_H; k += blockDim.x)
-        sW2[(k / MLP_H) * W2P + k % MLP_H] = args.w2h[k];
-    for (int k = t; k < MLP_H; k += blockDim.x) {
+    const int row = t & (tc::M - 1), half = t >> 7;
+    const int q = (t >> 5) & 3;
+    // weights into the canonical layout (16-byte chunks: 8 consecutive k of one output neuron)
+    for (int i = t; i < MLP_H * tc::KCH1; i += tc::THREADS) {
+        const int n = i / tc::KCH1, c = i % tc::KCH1;
+        *reinterpret_cast<uint4*>(sW1 + canon_off(n, 8 * c, tc::SBO1)) =
+            *reinterpret_cast<const uint4*>(args.w1h + n * MLP_KP + 8 * c);
+    }
+    for (int i = t; i < MLP_H * tc::KCH2; i += tc::THREADS) {
+        const int n = i / tc::KCH2, c = i % tc::KCH2;
+        *reinterpret_cast<uint4*>(sW2 + canon_off(n, 8 * c, tc::SBO2)) =
+            *reinterpret_cast<const uint4*>(args.w2h + n * MLP_H + 8 * c);
+    }
+    for (int k = t; k < MLP_H; k += tc::THREADS) {
         sB1[k] = args.P[OFF_B1 + k];
         sB2[k] = args.P[OFF_B2 + k];
         sW3[k] = args.P[OFF_W3 + k];
     }
-    for (int k = t; k < MLP_IN; k += blockDim.x) {
-        sLo[k] = args.lo ? args.lo[k] : -INFINITY;
-        sHi[k] = args.hi ? args.hi[k] : INFINITY;
+    for (int w = t; w < MLP_KP / 2; w += tc::THREADS) {
+        float lo[2], hi[2];
+        for (int e = 0; e < 2; ++e) {
+            const int k = 2 * w + e;
+            lo[e] = (args.lo && k < MLP_IN) ? args.lo[k] : -INFINITY;
+            hi[e] = (args.hi && k < MLP_IN) ? args.hi[k] : INFINITY;
+        }
+        sRange[w][0] = make_float2(lo[0], lo[1]);
+        sRange[w][1] = make_float2(hi[0], hi[1]);
     }
+    const uint32_t mbar = smem_u32(&s_mbar);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (t < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                     "r"(tc::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();  // the weight tiles were written by ordinary stores; the MMA reads them
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const uint32_t taddr = tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) (32 * half);
+    const uint32_t a_s = smem_u32(sA), w1_s = smem_u32(sW1), w2_s = smem_u32(sW2);
     const float b3 = args.P[OFF_B3];
-    const int warp = t >> 5, lane = t & 31;
-    const int g = lane >> 2, tg = lane & 3;
-    __nv_bfloat16* A = sA[warp];
-    const uint32_t ntiles = (args.n + 15) / 16;
-    for (uint32_t tile = blockIdx.x * IWARPS + warp; tile < ntiles; tile += gridDim.x * IWARPS) {
-        const uint32_t base = tile * 16;
-        // ---- features: lane pair (2p, 2p+1) builds particle p's row; lane 2p+l does level l+1 ----
-        const int pl = lane >> 1, lev = lane & 1;
-        const uint32_t pi = base + pl;
-        bool out_of_range = false;
+    const bool check = args.lo != nullptr && args.hi != nullptr;
+    uint32_t phase = 0;
+    bool failed = false;
+    const uint32_t ntiles = (args.n + tc::M - 1) / tc::M;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t pi = tile * tc::M + row;
         bool valid = pi < args.n;
+        bool oor = false;
         uint32_t o = 0;
+        // ---- features: this thread's half of row `row` ----
         if (FEATURES_IN) {
-            for (int k = lev; k < MLP_KP; k += 2) {
-                float v = 0.0f;
-                if (valid && k < MLP_IN) {
-                    v = args.X[(size_t) pi * MLP_IN + k];
-                    out_of_range |= !(v >= sLo[k] && v <= sHi[k]);
+            // half h writes k in [72 h, 72 h + 72)
+#pragma unroll 1
+            for (int c = 0; c < tc::KCH1 / 2; ++c) {
+                const int k0 = 8 * (c + half * (tc::KCH1 / 2));
+                uint32_t pk[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float v2[2];
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) {
+                        const int k = k0 + 2 * e + b;
+                        float v = 0.0f;
+                        if (valid && k < MLP_IN) {
+                            v = args.X[(size_t) pi * MLP_IN + k];
+                            if (check) {
+                                const float2 lo = sRange[k >> 1][0], hi = sRange[k >> 1][1];
+                                oor |= !(v >= (b ? lo.y : lo.x) && v <= (b ? hi.y : hi.x));
+                            }
+                        }
+                        v2[b] = v;
+                    }
+                    pk[e] = pack_bf16(v2[0], v2[1]);
                 }
-                A[pl * W1P + k] = __float2bfloat16_rn(v);
+                st_shared_v4(sA + canon_off(row, k0, tc::SBO1), pk[0], pk[1], pk[2], pk[3]);
             }
         } else {
-            float f[64];
             float u[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
             if (valid) {
                 o = args.order[pi];
@@ -424,127 +599,124 @@ __global__ void __launch_bounds__(IWARPS * 32) mlp_infer_kernel(const MlpInferAr
                 valid = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f &&
                         mlp_point(cp, p, args.nrm[o], u, nn);
             }
+            uint8_t* arow = sA + canon_off(row, 64 * half, tc::SBO1);
+            const float2(*rng)[2] = sRange + 32 * half;
+            uint32_t pk[4];
+            auto emit = [&](int m, float a, float b) {
+                pk[m & 3] = pack_bf16(a, b);
+                if ((m & 3) == 3)
+                    st_shared_v4(arow + (m >> 2) * 128, pk[0], pk[1], pk[2], pk[3]);
+                if (check) {
+                    const float2 lo = rng[m][0], hi = rng[m][1];
+                    oor |= !(a >= lo.x && a <= hi.x && b >= lo.y && b <= hi.y);
+                }
+            };
             if (valid) {
-                stencil64(cp.lv[cp.stencil_level + lev], u[0], u[1], u[2], f);
+                stencil64(cp.lv[cp.stencil_level + half], u[0], u[1], u[2], emit);
             } else {
 #pragma unroll
-                for (int k = 0; k < 64; ++k)
-                    f[k] = 0.0f;
+                for (int c = 0; c < 8; ++c)
+                    st_shared_v4(arow + c * 128, 0u, 0u, 0u, 0u);
             }
-#pragma unroll
-            for (int k = 0; k < 64; ++k) {
-                const int fi = lev * 64 + k;
-                out_of_range |= valid && !(f[k] >= sLo[fi] && f[k] <= sHi[fi]);
-                A[pl * W1P + fi] = __float2bfloat16_rn(f[k]);
-            }
-            if (lev == 0) {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    out_of_range |= valid && !(nn[c] >= sLo[128 + c] && nn[c] <= sHi[128 + c]);
-                    A[pl * W1P + 128 + c] = __float2bfloat16_rn(nn[c]);
-                }
+            // features 128..143: the normal and zero padding (chunk 16 on half 0, chunk 17 on half 1)
+            if (half == 0) {
+                st_shared_v4(sA + canon_off(row, 128, tc::SBO1), pack_bf16(nn[0], nn[1]), pack_bf16(nn[2], 0.0f), 0u,
+                             0u);
+                if (valid && check)
+                    oor |= !(nn[0] >= sRange[64][0].x && nn[0] <= sRange[64][1].x && nn[1] >= sRange[64][0].y &&
+                             nn[1] <= sRange[64][1].y && nn[2] >= sRange[65][0].x && nn[2] <= sRange[65][1].x);
             } else {
-                for (int k = 131; k < MLP_KP; ++k)
-                    A[pl * W1P + k] = __float2bfloat16_rn(0.0f);
+                st_shared_v4(sA + canon_off(row, 136, tc::SBO1), 0u, 0u, 0u, 0u);
             }
+            oor = oor && valid;
         }
-        // every lane must execute each shuffle (full mask): no short-circuit around them
-        const bool partner_oor = __shfl_xor_sync(0xffffffffu, out_of_range, 1);
-        const bool partner_valid = __shfl_xor_sync(0xffffffffu, valid, 1);
-        out_of_range = out_of_range || partner_oor;
-        const bool pvalid = valid || partner_valid;
-        __syncwarp();
-        // ---- layer 1: [16 x 144] x [144 x 64] ----
-        float acc[8][4];
+        if (half == 1)
+            s_flag[row] = oor ? 1u : 0u;
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (half == 0)
+            oor = oor || s_flag[row] != 0u;
+        // ---- layer 1: D[128 x 64] = A[128 x 144] W1^T ----
+        if (t == 0) {
+            tc_fence_after();
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+            for (int kk = 0; kk < tc::KCH1 / 2; ++kk)
+                umma_bf16(tmem, umma_desc(a_s + 256u * kk, 128u, tc::SBO1), umma_desc(w1_s + 256u * kk, 128u, tc::SBO1),
+                          kk > 0 ? 1u : 0u);
+            umma_commit(mbar);
+        }
+        failed = !mbar_wait(mbar, phase);
+        phase ^= 1u;
+        tc_fence_after();
+        if (__syncthreads_or(failed))
+            break;
+        float v[32];
+        tmem_ld32(taddr, v);
+        // hidden layer 1 -> A tile (K = 64 layout): columns 32 half .. 32 half + 31 of row `row`
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                acc[nt][e] = 0.0f;
+        for (int c = 0; c < 4; ++c) {
+            uint32_t pk[4];
 #pragma unroll
-        for (int kk = 0; kk < MLP_KP / 16; ++kk) {
-            const int c0 = 16 * kk + 2 * tg;
-            const uint32_t a0 = *reinterpret_cast<const uint32_t*>(&A[g * W1P + c0]);
-            const uint32_t a1 = *reinterpret_cast<const uint32_t*>(&A[(g + 8) * W1P + c0]);
-            const uint32_t a2 = *reinterpret_cast<const uint32_t*>(&A[g * W1P + c0 + 8]);
-            const uint32_t a3 = *reinterpret_cast<const uint32_t*>(&A[(g + 8) * W1P + c0 + 8]);
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                const __nv_bfloat16* wr = sW1 + (8 * nt + g) * W1P + c0;
-                mma_bf16(acc[nt], a0, a1, a2, a3, *reinterpret_cast<const uint32_t*>(wr),
-                         *reinterpret_cast<const uint32_t*>(wr + 8));
+            for (int e = 0; e < 4; ++e) {
+                const int j = 8 * c + 2 * e;
+                pk[e] = pack_bf16(silu_fast(v[j] + sB1[32 * half + j]), silu_fast(v[j + 1] + sB1[32 * half + j + 1]));
             }
+            st_shared_v4(sA + canon_off(row, 32 * half + 8 * c, tc::SBO2), pk[0], pk[1], pk[2], pk[3]);
         }
-        // ---- bias + SiLU; the accumulator layout of two n-tiles is the A layout of one k-step ----
-        uint32_t h[4][4];
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // ---- layer 2: D[128 x 64] = H[128 x 64] W2^T (same TMEM columns) ----
+        if (t == 0) {
+            tc_fence_after();
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const int col = 8 * nt + 2 * tg;
-            const float v0 = silu(acc[nt][0] + sB1[col]), v1 = silu(acc[nt][1] + sB1[col + 1]);
-            const float v2 = silu(acc[nt][2] + sB1[col]), v3 = silu(acc[nt][3] + sB1[col + 1]);
-            h[nt >> 1][(nt & 1) * 2 + 0] = pack_bf16(v0, v1);
-            h[nt >> 1][(nt & 1) * 2 + 1] = pack_bf16(v2, v3);
+            for (int kk = 0; kk < tc::KCH2 / 2; ++kk)
+                umma_bf16(tmem, umma_desc(a_s + 256u * kk, 128u, tc::SBO2), umma_desc(w2_s + 256u * kk, 128u, tc::SBO2),
+                          kk > 0 ? 1u : 0u);
+            umma_commit(mbar);
         }
-        // ---- layer 2: [16 x 64] x [64 x 64] ----
+        failed = !mbar_wait(mbar, phase);
+        phase ^= 1u;
+        tc_fence_after();
+        if (__syncthreads_or(failed))
+            break;
+        tmem_ld32(taddr, v);
+        // ---- layer 3 (64 -> 1) in FP32: each half sums its 32 columns ----
+        float z = 0.0f;
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                acc[nt][e] = 0.0f;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            const int c0 = 16 * kk + 2 * tg;
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                const __nv_bfloat16* wr = sW2 + (8 * nt + g) * W2P + c0;
-                // A regs: a0 = (row g, k c0..), a1 = (row g+8), a2 = (row g, k c0+8..), a3 = (row g+8, ..)
-                mma_bf16(acc[nt], h[kk][0], h[kk][1], h[kk][2], h[kk][3], *reinterpret_cast<const uint32_t*>(wr),
-                         *reinterpret_cast<const uint32_t*>(wr + 8));
-            }
-        }
-        // ---- layer 3 (64 -> 1) in FP32 on the CUDA cores, sigmoid ----
-        float zlo = 0.0f, zhi = 0.0f;
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const int col = 8 * nt + 2 * tg;
-            zlo = fmaf(silu(acc[nt][0] + sB2[col]), sW3[col], zlo);
-            zlo = fmaf(silu(acc[nt][1] + sB2[col + 1]), sW3[col + 1], zlo);
-            zhi = fmaf(silu(acc[nt][2] + sB2[col]), sW3[col], zhi);
-            zhi = fmaf(silu(acc[nt][3] + sB2[col + 1]), sW3[col + 1], zhi);
-        }
-        zlo += __shfl_xor_sync(0xffffffffu, zlo, 1);
-        zlo += __shfl_xor_sync(0xffffffffu, zlo, 2);
-        zhi += __shfl_xor_sync(0xffffffffu, zhi, 1);
-        zhi += __shfl_xor_sync(0xffffffffu, zhi, 2);
-        // flags and output index of rows g and g+8 live on lanes 2g and 2(g+8)
-        const bool oor_lo = __shfl_sync(0xffffffffu, out_of_range, 2 * g);
-        const bool oor_hi = __shfl_sync(0xffffffffu, out_of_range, (2 * (g + 8)) & 31);
-        const bool val_lo = __shfl_sync(0xffffffffu, pvalid, 2 * g);
-        const bool val_hi = __shfl_sync(0xffffffffu, pvalid, (2 * (g + 8)) & 31);
-        const uint32_t o_lo = __shfl_sync(0xffffffffu, o, 2 * g);
-        const uint32_t o_hi = __shfl_sync(0xffffffffu, o, (2 * (g + 8)) & 31);
-        if (tg == 0) {
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const uint32_t row = base + g + 8 * half;
-                if (row >= args.n)
-                    continue;
-                const float y = sigmoidf_((half ? zhi : zlo) + b3);
-                const bool oor = half ? oor_hi : oor_lo;
-                const bool vv = half ? val_hi : val_lo;
-                const uint32_t oo = FEATURES_IN ? row : (half ? o_hi : o_lo);
-                if (!FEATURES_IN && !vv) {
-                    args.y[oo] = 1.0f;  // no normal / invalid particle: unoccluded, as the cone march
-                } else if (oor && args.fallback) {
-                    args.fallback[atomicAdd(args.nfallback, 1u)] = oo;
-                    if (FEATURES_IN)
-                        args.y[oo] = y;
-                } else {
+        for (int j = 0; j < 32; ++j)
+            z = fmaf(silu_fast(v[j] + sB2[32 * half + j]), sW3[32 * half + j], z);
+        if (half == 1)
+            s_part[row] = z;
+        tc_fence_before();
+        __syncthreads();
+        if (half == 0 && pi < args.n) {
+            const float y = sigmoidf_(z + s_part[row] + b3);
+            const uint32_t oo = FEATURES_IN ? pi : o;
+            if (!FEATURES_IN && !valid) {
+                args.y[oo] = 1.0f;  // no normal / invalid particle: unoccluded, as the cone march
+            } else if (oor && args.fallback) {
+                args.fallback[atomicAdd(args.nfallback, 1u)] = oo;
+                if (FEATURES_IN)
                     args.y[oo] = y;
-                }
+            } else {
+                args.y[oo] = y;
             }
         }
-        __syncwarp();
+    }
+    if (failed) {
+        if (t == 0 && args.err)
+            atomicOr(args.err, ERR_MMA_TIMEOUT);
+        // drain: the phase that timed out may still complete; wait for it once more (bounded)
+        mbar_wait(mbar, phase ^ 1u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (t < 32) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc::TMEM_COLS)
+                     : "memory");
     }
 }
 
@@ -604,13 +776,21 @@ cudaError_t launch_mlp_pack(const float* P, __nv_bfloat16* w1h, __nv_bfloat16* w
 cudaError_t launch_mlp_infer(const MlpInferArgs& a, const ConeParams& cp, bool features_in, int sms, cudaStream_t st) {
     if (a.n == 0)
         return cudaSuccess;
-    const uint32_t ntiles = (a.n + 15) / 16;
-    const unsigned grid = (unsigned) std::min<uint32_t>(ceil_div(ntiles, IWARPS), (uint32_t) sms * 8);
-    if (features_in)
-        mlp_infer_kernel<true><<<grid, IWARPS * 32, 0, st>>>(a, cp);
-    else
-        mlp_infer_kernel<false><<<grid, IWARPS * 32, 0, st>>>(a, cp);
-    return cudaGetLastError();
+    static_assert(tc::DYN_SMEM <= 227 * 1024, "tensor-core tile does not fit in shared memory");
+    const uint32_t ntiles = (a.n + tc::M - 1) / tc::M;
+    // three resident CTAs per SM (shared memory allows three; 3 x 64 TMEM columns of 512): one wave
+    const unsigned grid = (unsigned) std::min<uint32_t>(ntiles, (uint32_t) sms * 3);
+    cudaError_t e;
+    if (features_in) {
+        e = cudaFuncSetAttribute(mlp_infer_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::DYN_SMEM);
+        if (e == cudaSuccess)
+            mlp_infer_tc_kernel<true><<<grid, tc::THREADS, tc::DYN_SMEM, st>>>(a, cp);
+    } else {
+        e = cudaFuncSetAttribute(mlp_infer_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::DYN_SMEM);
+        if (e == cudaSuccess)
+            mlp_infer_tc_kernel<false><<<grid, tc::THREADS, tc::DYN_SMEM, st>>>(a, cp);
+    }
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace p2v

@@ -38,6 +38,7 @@ struct MlpInferArgs {
     float* y;                       // output, indexed by particle (or by row for given features)
     uint32_t* fallback;             // particle indices whose features left the training range (nullable)
     uint32_t* nfallback;
+    uint32_t* err;                  // ERR_* bits (the tensor-core kernel's bounded waits)
 };
 
 size_t mlp_train_smem_bytes();

@@ -10,6 +10,7 @@ constexpr uint32_t ERR_LOOKBACK_TIMEOUT = 1u;  // radix-sort decoupled look-back
 constexpr uint32_t ERR_GAP_OVERFLOW = 2u;      // cell-start long-gap list overflowed
 constexpr uint32_t ERR_STAGE_OVERFLOW = 4u;    // density tile window exceeded the staging tables
 constexpr uint32_t ERR_WINDOW_TOO_WIDE = 8u;   // footprint wider than the supported tile window
+constexpr uint32_t ERR_MMA_TIMEOUT = 16u;      // a tensor-core MMA completion wait gave up
 
 // Bounded spin budget for device-side waits: a wait that exceeds it records an error and gives up.
 constexpr uint32_t SPIN_LIMIT = 1u << 22;

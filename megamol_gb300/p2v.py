@@ -105,6 +105,8 @@ _SIGNATURES = {
     "p2v_get_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
     "p2v_run_frame": ([C.c_void_p, C.POINTER(FrameC), C.POINTER(VolumeC), C.c_void_p], C.c_int),
     "p2v_get_device_volume": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)], C.c_int),
+    "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
+                          C.c_int),
     "p2v_get_stats": ([C.c_void_p, C.POINTER(StatsC)], C.c_int),
     "p2v_get_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_size_t),
     "p2v_train_params_default": ([C.POINTER(TrainParams)], None),
@@ -324,6 +326,14 @@ class Context:
         res = (C.c_uint64 * 3)()
         self._check(self.lib.p2v_get_device_volume(self.h, C.byref(p), res))
         return p.value, list(res)
+
+    def ao_volume(self, level: int = 0) -> np.ndarray:
+        """Level `level` of the last cone-march pyramid as a (z, y, x) float32 host array."""
+        dims = (C.c_int32 * 3)()
+        self._check(self.lib.p2v_get_ao_volume(self.h, int(level), None, 0, MEM_HOST, dims))
+        out = np.empty((dims[2], dims[1], dims[0]), np.float32)
+        self._check(self.lib.p2v_get_ao_volume(self.h, int(level), out.ctypes.data, out.size, MEM_HOST, dims))
+        return out
 
 
 class ParticlesToDensity:

@@ -74,6 +74,11 @@ def lib() -> C.CDLL:
                                                C.c_float, C.c_void_p]
         f.p2vo_aosphere_ao_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float,
                                            C.c_float, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
+        f.p2vo_mdao_dims.argtypes = [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float)]
+        f.p2vo_mdao_volume_f32.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                                           C.c_int, C.c_void_p]
+        f.p2vo_mdao_mip_u8.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_int32)]
         f.p2vo_mlp_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.POINTER(C.c_double),
                                    C.c_void_p]
     return _lib
@@ -318,6 +323,35 @@ def aosphere_ao_f64(tex, clip, xyzr, normals, mode=0, step_len=0.5, eval_fac=1.0
 
 MLP_IN, MLP_HIDDEN = 131, 64
 MLP_NPARAM = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
+
+
+def mdao_dims(clip, vol_size: int):
+    """MDAO volume size for a clip box: (dims (x, y, z), shortest edge, max lod)."""
+    c = (C.c_float * 6)(*[float(v) for v in clip])
+    d = (C.c_int32 * 3)()
+    sh, ml = C.c_float(), C.c_float()
+    lib().p2vo_mdao_dims(c, int(vol_size), d, C.byref(sh), C.byref(ml))
+    return (int(d[0]), int(d[1]), int(d[2])), float(sh.value), float(ml.value)
+
+
+def mdao_volume_f32(xyzr, clip, dims, unorm8: bool = True) -> np.ndarray:
+    """MDAO occupancy volume, (z, y, x) float32: k/255 per voxel (unorm8) or min(1, sum of fractions)."""
+    x = _xyzr(xyzr)
+    c = (C.c_float * 6)(*[float(v) for v in clip])
+    d = (C.c_int32 * 3)(*[int(v) for v in dims])
+    out = np.zeros((dims[2], dims[1], dims[0]), np.float32)
+    lib().p2vo_mdao_volume_f32(x.ctypes.data, x.shape[0], c, d, int(bool(unorm8)), out.ctypes.data)
+    return out
+
+
+def mdao_mip_u8(src: np.ndarray) -> np.ndarray:
+    """One R8 mip step (integer /8 rule, rounded half up) of a (z, y, x) float32 volume of k/255 values."""
+    s = np.ascontiguousarray(src, np.float32)
+    sd = (C.c_int32 * 3)(s.shape[2], s.shape[1], s.shape[0])
+    dd = (C.c_int32 * 3)(max(1, s.shape[2] // 2), max(1, s.shape[1] // 2), max(1, s.shape[0] // 2))
+    out = np.zeros((dd[2], dd[1], dd[0]), np.float32)
+    lib().p2vo_mdao_mip_u8(s.ctypes.data, sd, out.ctypes.data, dd)
+    return out
 
 
 def mlp_f64(params, x, t=None, grads=True):

@@ -576,3 +576,194 @@ extern "C" void p2vo_mlp_f64(const double* P, const float* x, const float* t, in
     if (grads)
         std::memcpy(grads, g.data(), sizeof(double) * np);
 }
+
+/* ------------------------------------------------------------------------------------------------
+ * MDAO occupancy volume. FP32 throughout, in the shaders' operation order, compiled without fused
+ * multiply-adds, so the GPU voxeliser (which uses explicitly rounded operations) matches it bit for bit.
+ * ---------------------------------------------------------------------------------------------- */
+extern "C" void p2vo_mdao_dims(const float clip[6], int vol_size, int32_t dims[3], float* shortest, float* max_lod) {
+    // SphereRenderer.cpp:2463-2476; Cuboid::Width/Height/Depth are absolute edge lengths and
+    // Dimension::Scale multiplies in double (AbstractDimensionImpl.h:183-187)
+    float size[3];
+    for (int a = 0; a < 3; ++a)
+        size[a] = clip[a + 3] > clip[a] ? clip[a + 3] - clip[a] : clip[a] - clip[a + 3];
+    const float w = size[0], h = size[1], d = size[2];
+    const float longest = ((w > h) && (w > d)) ? w : ((h > d) ? h : d);  // AbstractCuboid.h:412-417
+    const double f = static_cast<double>(static_cast<float>(vol_size) / longest);
+    float dm[3];
+    for (int a = 0; a < 3; ++a)
+        dm[a] = static_cast<float>(f * static_cast<double>(size[a]));
+    dm[0] = std::ceil(dm[0] / 4.0f) * 4.0f;
+    dm[1] = std::ceil(dm[1]);
+    dm[2] = std::ceil(dm[2]);
+    for (int a = 0; a < 3; ++a)
+        dims[a] = static_cast<int32_t>(dm[a]);
+    *shortest = std::min(dm[0], std::min(dm[1], dm[2]));
+    *max_lod = std::ceil(std::log2(static_cast<float>(vol_size))) - 1.0f;
+}
+
+namespace {
+
+struct MdaoGeo {
+    float bmin[3], inv[3], fd[3], cell[3];
+    float cell_vol, ps_scale, sphere_k, half_vp[2];
+    int d[3];
+};
+
+MdaoGeo mdao_geo(const float clip[6], const int32_t dims[3]) {
+    MdaoGeo g{};
+    for (int a = 0; a < 3; ++a) {
+        const float size = clip[a + 3] > clip[a] ? clip[a + 3] - clip[a] : clip[a] - clip[a + 3];
+        g.bmin[a] = clip[a];             // StartInsertion: inBoundsMin (MDAOVolumeGenerator.cpp:147-148)
+        g.inv[a] = 1.0f / size;          // inBoundsSizeInverse (:141-144)
+        g.fd[a] = static_cast<float>(dims[a]);
+        g.d[a] = dims[a];
+        g.cell[a] = 1.0f / (g.fd[a] * g.inv[a]);  // frag:20
+    }
+    g.cell_vol = (g.cell[0] * g.cell[1]) * g.cell[2];                                 // frag:58
+    g.ps_scale = std::max(g.inv[0] * g.fd[0], g.inv[1] * g.fd[1]);                    // geom:43
+    g.sphere_k = 4.0f / 3.0f * 3.14152f;                                              // frag:57 (sic)
+    g.half_vp[0] = 0.5f * g.fd[0];  // viewport = one slice (MDAOVolumeGenerator.cpp:165)
+    g.half_vp[1] = 0.5f * g.fd[1];
+    return g;
+}
+
+inline float mdao_dot(const float* v) {
+    return (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+}
+
+// mdao_volume.frag.glsl:17-76 for voxel (i, j, layer) and a sphere with centre c (relative to inBoundsMin)
+// and squared radius w2; -1 = discarded fragment.
+float mdao_fragment(const MdaoGeo& g, int i, int j, int layer, const float c[3], float w2) {
+    const float cm[3] = {static_cast<float>(i) * g.cell[0], static_cast<float>(j) * g.cell[1],
+                         static_cast<float>(layer) * g.cell[2]};
+    float lo[3], hi[3], fp[3], cp[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = cm[a] - c[a];
+        hi[a] = (cm[a] - c[a]) + g.cell[a];
+        fp[a] = std::max(std::fabs(lo[a]), std::fabs(hi[a]));
+        cp[a] = std::min(std::fabs(lo[a]), std::fabs(hi[a]));
+    }
+    if (mdao_dot(cp) - w2 > 0.0f)
+        return -1.0f;
+    if (mdao_dot(fp) - w2 < 0.0f)
+        return 1.0f;
+    const float radius = std::sqrt(w2);
+    if (lo[0] <= -radius && lo[1] <= -radius && lo[2] <= -radius && hi[0] >= radius && hi[1] >= radius &&
+        hi[2] >= radius)
+        return (g.sphere_k * w2 * radius) / g.cell_vol;
+    int hits = 0;
+    for (int x = 0; x < 3; ++x)
+        for (int y = 0; y < 3; ++y)
+            for (int z = 0; z < 3; ++z) {
+                const int k[3] = {x, y, z};
+                float t[3];
+                for (int a = 0; a < 3; ++a)
+                    t[a] = (cm[a] + (g.cell[a] * static_cast<float>(k[a])) * 0.5f) - c[a];
+                if (mdao_dot(t) - w2 < 0.0f)
+                    ++hits;
+            }
+    return static_cast<float>(hits) / 27.0f;
+}
+
+// Covered pixel range of a point of `size` pixels centred at window coordinate `wc`: pixel centres
+// i + 0.5 in [wc - size/2, wc + size/2), clipped to [0, n). For |wc|, size < 2^22 both subtractions of
+// 0.5 are exact, so the ceilings give the first centre at or above each bound.
+void mdao_point_span(float wc, float size, int n, int& i0, int& i1) {
+    const float lo = wc - 0.5f * size, hi = wc + 0.5f * size;
+    const float a = std::min(std::max(std::ceil(lo - 0.5f), 0.0f), static_cast<float>(n));
+    const float b = std::min(std::max(std::ceil(hi - 0.5f), 0.0f), static_cast<float>(n));
+    i0 = static_cast<int>(a);
+    i1 = static_cast<int>(b);
+}
+
+}  // namespace
+
+extern "C" void p2vo_mdao_volume_f32(const float* xyzr, int64_t n, const float clip[6], const int32_t dims[3],
+    int unorm8, float* out) {
+    const MdaoGeo g = mdao_geo(clip, dims);
+    const int64_t nv = (int64_t) dims[0] * dims[1] * dims[2];
+    std::vector<uint64_t> acc((size_t) nv, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t k = 0; k < n; ++k) {
+        const float* p = xyzr + 4 * k;
+        const float r = p[3];
+        float np[3], c[3];
+        bool inside = true;
+        for (int a = 0; a < 3; ++a) {
+            np[a] = (p[a] - g.bmin[a]) * g.inv[a];  // geom:87
+            const float ndc = np[a] * 2.0f - 1.0f;  // geom:94; a point is clipped by its centre vertex
+            inside = inside && (ndc >= -1.0f && ndc <= 1.0f);
+            c[a] = p[a] - g.bmin[a];                // geom:45
+        }
+        if (!inside)
+            continue;
+        const float w2 = r * r;
+        const float xw = (np[0] * 2.0f - 1.0f) * g.half_vp[0] + g.half_vp[0];  // viewport transform
+        const float yw = (np[1] * 2.0f - 1.0f) * g.half_vp[1] + g.half_vp[1];
+        auto emit = [&](int layer, float disk) {  // geom:39-49 + rasterisation of the point
+            if (layer < 0 || layer >= g.d[2])
+                return;
+            // gl_PointSize = int(2 ceil(disk * scale)), at least one pixel; sizes beyond 2^22 pixels cover
+            // the whole slice anyway and are capped so the span arithmetic stays exact
+            const float ps = std::max(std::min(2.0f * std::ceil(disk * g.ps_scale), 4194304.0f), 1.0f);
+            int x0, x1, y0, y1;
+            mdao_point_span(xw, ps, g.d[0], x0, x1);
+            mdao_point_span(yw, ps, g.d[1], y0, y1);
+            for (int j = y0; j < y1; ++j)
+                for (int i = x0; i < x1; ++i) {
+                    float f = mdao_fragment(g, i, j, layer, c, w2);
+                    if (f < 0.0f)
+                        continue;
+                    f = std::min(std::max(f, 0.0f), 1.0f);  // UNORM colour clamp before blending
+                    const uint64_t q = unorm8 ? (uint64_t) std::nearbyint(f * 255.0f)
+                                              : (uint64_t) std::llrint((double) (f * 4294967296.0f));
+                    const int64_t v = (int64_t) i + ((int64_t) j + (int64_t) layer * g.d[1]) * g.d[0];
+#pragma omp atomic
+                    acc[(size_t) v] += q;
+                }
+        };
+        // geom:91-107
+        // slices beyond the volume's depth emit layers outside it: cap the count there
+        const int numSlices =
+            static_cast<int>(std::min(std::ceil(r * g.inv[2] * g.fd[2]), static_cast<float>(g.d[2] + 1)));
+        const float zs = np[2] * g.fd[2];
+        const int centerLayer = static_cast<int>(std::floor(zs));
+        emit(centerLayer, r);
+        const float sliceThickness = 1.0f / g.fd[2];
+        const float zOffset = (zs - std::floor(zs)) / g.fd[2];
+        for (int side = 0; side < 2; ++side) {  // geom:54-72, negative then positive hemisphere
+            const int step = side == 0 ? -1 : 1;
+            const float offset = side == 0 ? zOffset : sliceThickness - zOffset;
+            for (int i = 1; i <= numSlices; ++i) {
+                const float dist = (static_cast<float>(i - 1) / g.fd[2] + offset) / g.inv[2];
+                const float nsq = r * r - dist * dist;
+                if (nsq < 0.0f)
+                    break;
+                emit(centerLayer + step * i, std::sqrt(nsq));
+            }
+        }
+    }
+    for (int64_t v = 0; v < nv; ++v) {
+        if (unorm8)
+            out[v] = static_cast<float>(std::min<uint64_t>(acc[(size_t) v], 255)) / 255.0f;
+        else
+            out[v] = acc[(size_t) v] >= (1ull << 32) ? 1.0f
+                                                     : static_cast<float>(acc[(size_t) v]) * (1.0f / 4294967296.0f);
+    }
+}
+
+extern "C" void p2vo_mdao_mip_u8(const float* src, const int32_t sd[3], float* dst, const int32_t dd[3]) {
+    for (int z = 0; z < dd[2]; ++z)
+        for (int y = 0; y < dd[1]; ++y)
+            for (int x = 0; x < dd[0]; ++x) {
+                int sum = 0;
+                const int x1 = std::min(2 * x + 1, sd[0] - 1), y1 = std::min(2 * y + 1, sd[1] - 1),
+                          z1 = std::min(2 * z + 1, sd[2] - 1);
+                for (int zz = 2 * z; zz <= z1; ++zz)
+                    for (int yy = 2 * y; yy <= y1; ++yy)
+                        for (int xx = 2 * x; xx <= x1; ++xx)
+                            sum += (int) std::lrint(src[xx + (yy + int64_t(zz) * sd[1]) * sd[0]] * 255.0f);
+                dst[x + (y + int64_t(z) * dd[1]) * dd[0]] = static_cast<float>((sum + 4) / 8) / 255.0f;
+            }
+}

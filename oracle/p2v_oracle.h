@@ -91,6 +91,22 @@ void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], const float cli
 void p2vo_mlp_f64(const double* params, const float* x, const float* t, int64_t n, double* grads, double* loss,
     double* y);
 
+/* MDAO occupancy volume (the AO volume of moldyn_gl::SphereRenderer's MDAO mode).
+ * Dimensions (SphereRenderer.cpp:2463-2476): longest clip-box edge -> vol_size voxels, x rounded up to a
+ * multiple of 4; shortest = min(dims); max_lod = ceil(log2(vol_size)) - 1. */
+void p2vo_mdao_dims(const float clip[6], int vol_size, int32_t dims[3], float* shortest, float* max_lod);
+/* Voxelisation (mdao_volume.vert.glsl:9-14, mdao_volume.geom.glsl:24-93, mdao_volume.frag.glsl:9-76) with
+ * the additive blend of MDAOVolumeGenerator.cpp:151-153 into an R8 texture: each voxel receives, per
+ * covering sphere, the fragment value q = round(clamp(frac, 0, 1) * 255) and keeps min(255, sum q); out =
+ * that / 255 (unorm8 = 1). unorm8 = 0 keeps the fractions unquantised: out = min(1, sum of clamp(frac))
+ * summed in 2^-32 fixed point. FP32 with the shaders' operation order, no fused multiply-adds.
+ * xyzr holds the particles to insert (radius = w). */
+void p2vo_mdao_volume_f32(const float* xyzr, int64_t n, const float clip[6], const int32_t dims[3], int unorm8,
+    float* out);
+/* One MDAO mip step of an R8 volume (mdao_mipmap_compute_main.comp.glsl:8-26 with an R8 store): children
+ * as 8-bit integers k, out = ((sum k + 4) / 8) / 255 (the /8 rule, rounded half up). */
+void p2vo_mdao_mip_u8(const float* src, const int32_t sdim[3], float* dst, const int32_t ddim[3]);
+
 #ifdef __cplusplus
 }
 #endif
