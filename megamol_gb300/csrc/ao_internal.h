@@ -29,6 +29,8 @@ struct ConeParams {
     float t[MAX_STEPS], lod[MAX_STEPS];
     ConeLevel lv[MAX_LEVELS];
     int stencil_level;             // learned AO: first of the two mip levels its stencil reads
+    unsigned long long stex[2];    // learned AO: FP16 layered textures of those two levels (bilinear per slice)
+    float sinv[2][3];              // their inverse sizes (texel spacing in normalised coordinates)
 };
 
 struct AOSphereParams {

@@ -75,6 +75,7 @@ struct p2v_ctx {
     DevBuf mlp_P, mlp_m, mlp_v, mlp_g, mlp_part, mlp_ploss, mlp_loss, mlp_w1h, mlp_w2h, mlp_lo, mlp_hi, mlp_idx,
         mlp_y, fb_list;
     DevBuf tX, tT;                       // collected training pairs
+    StencilTex stex[2];                  // the learned AO's two stencil levels as textures
     uint64_t t_pairs = 0, t_cap = 0;
     std::vector<uint32_t> t_valid;       // indices of pairs with features
     std::vector<float> t_host_T;         // targets on the host (validation error)
@@ -105,6 +106,7 @@ struct p2v_ctx {
     p2v_status build_cone(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
                           const uint32_t* order, ConeParams& cp, cudaStream_t st);
     p2v_status mlp_alloc();
+    p2v_status prepare_stencil(ConeParams& cp, cudaStream_t st);
     void mlp_init_params(uint64_t seed, float bias3);
 };
 
@@ -639,6 +641,21 @@ p2v_status p2v_ctx::build_cone(const p2v_frame* fr, const GridGeo& g, const floa
     return P2V_OK;
 }
 
+// Copy the learned AO's two stencil levels into their textures (level 0 of a density volume saturated as
+// the cone march sees it) and hand the texture objects to the kernels.
+p2v_status p2v_ctx::prepare_stencil(ConeParams& cp, cudaStream_t st) {
+    for (int h = 0; h < 2; ++h) {
+        const int l = cp.stencil_level + h;
+        const ConeLevel& L = cp.lv[l];
+        P2V_CUDA_TRY(stex[h].ensure(L.d));
+        P2V_CUDA_TRY(launch_fill_stencil_tex(L, l == 0 ? cp.sat : 0.0f, stex[h], st));
+        cp.stex[h] = stex[h].tex;
+        for (int a = 0; a < 3; ++a)
+            cp.sinv[h][a] = 1.0f / L.fd[a];
+    }
+    return P2V_OK;
+}
+
 p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
                            const uint32_t* order, cudaStream_t st) {
     const p2v_params& P = prm;
@@ -661,6 +678,9 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
             return fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
         if (mlp_level >= 0)
             cp.stencil_level = std::min(mlp_level, cp.nlevels - 2);
+        const p2v_status ps = prepare_stencil(cp, st);
+        if (ps != P2V_OK)
+            return ps;
         P2V_CUDA_TRY(fb_list.ensure(sizeof(uint32_t) * ((size_t) n + 1)));
         FrameScalars* fs = scal.as<FrameScalars>();
         MlpInferArgs a{};
@@ -846,6 +866,8 @@ void p2v_destroy(p2v_ctx* c) {
                       &c->mlp_ploss, &c->mlp_loss, &c->mlp_w1h, &c->mlp_w2h, &c->mlp_lo, &c->mlp_hi, &c->mlp_idx,
                       &c->mlp_y, &c->fb_list, &c->tX, &c->tT})
         b->release();
+    c->stex[0].release();
+    c->stex[1].release();
     for (auto& e : c->ev)
         if (e)
             cudaEventDestroy(e);
@@ -989,6 +1011,9 @@ p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, 
         c->mlp_level = c->last_cp.stencil_level;
     c->last_cp.stencil_level = std::min(c->mlp_level, c->last_cp.nlevels - 2);
     if (nsel > 0) {
+        const p2v_status ps = c->prepare_stencil(c->last_cp, c->own_stream);
+        if (ps != P2V_OK)
+            return ps;
         std::vector<uint32_t> sel(nvalid);
         std::iota(sel.begin(), sel.end(), 0u);
         if (nsel < nvalid) {

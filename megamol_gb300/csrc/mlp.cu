@@ -11,6 +11,7 @@
 // march.
 // No reference counterpart: the reference evaluates AO only by the GLSL cone march / AOSphere taps.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,55 +38,48 @@ __device__ __forceinline__ float sigmoidf_(float a) {
     return 1.0f / (1.0f + __expf(-a));
 }
 
-__device__ __forceinline__ float lv_fetch(const ConeLevel& L, int x, int y, int z) {
-    if ((unsigned) x >= (unsigned) L.d[0] || (unsigned) y >= (unsigned) L.d[1] || (unsigned) z >= (unsigned) L.d[2])
-        return 0.0f;  // CLAMP_TO_BORDER, as the cone march samples
-    return __ldg(L.v + ((int64_t) z * L.d[1] + y) * L.d[0] + x);
-}
-
-// The 5x5x5 texel block of a stencil: FAST = inside the level (rows read from one base pointer), else
-// every texel is bounds-checked (CLAMP_TO_BORDER). emit(m, a, b) receives samples 2m and 2m+1.
-template<bool FAST, class Emit>
-__device__ __forceinline__ void stencil_block(const ConeLevel& L, int x0, int y0, int z0, float fx, float fy, float fz,
-                                              Emit& emit) {
-    const int sy = L.d[0], sz = L.d[0] * L.d[1];
-    const float* base = FAST ? L.v + ((z0 * L.d[1] + y0) * L.d[0] + x0) : nullptr;
+// 4x4x4 trilinear samples of one mip level at texel-spaced offsets (k - 1.5) around normalised point u.
+// The level is a layered 2D texture (one layer per z slice, FP16 texels, GL LINEAR in x and y with
+// CLAMP_TO_BORDER): the texture units filter the 16 (x, y) positions bilinearly on each of the five z
+// slices the stencil spans, and the z interpolation runs in FP32 (slices outside the level read 0, the
+// border). emit(kz, v) receives the 16 samples of z row kz, in the order ky*4 + kx. The features feed a
+// BF16 network, so the texture filter's 8-bit weight fractions sit below the features' own rounding;
+// training pairs are extracted by the same code.
+template<class Emit>
+__device__ __forceinline__ void stencil64(unsigned long long tex, const float inv[3], int nz, float ux, float uy,
+                                          float uz, Emit&& emit) {
+    float px[4], py[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        px[k] = fmaf((float) k - 1.5f, inv[0], ux);
+        py[k] = fmaf((float) k - 1.5f, inv[1], uy);
+    }
+    const float cz = uz * (float) nz - 2.0f;
+    const float fz0 = floorf(cz);
+    const float fz = cz - fz0;
+    const int z0 = (int) fz0;
     float prev[16];
-#pragma unroll
-    for (int zz = 0; zz < 5; ++zz) {
+#pragma unroll 1
+    for (int s = 0; s < 5; ++s) {
+        const int layer = z0 + s;
         float cur[16];
-        float rowp[4];
+        if (layer >= 0 && layer < nz) {
 #pragma unroll
-        for (int yy = 0; yy < 5; ++yy) {
-            float t[5];
-            if (FAST) {
-                const float* row = base + zz * sz + yy * sy;
+            for (int ky = 0; ky < 4; ++ky)
 #pragma unroll
-                for (int xx = 0; xx < 5; ++xx)
-                    t[xx] = __ldg(row + xx);
-            } else {
+                for (int kx = 0; kx < 4; ++kx)
+                    cur[ky * 4 + kx] = tex2DLayered<float>((cudaTextureObject_t) tex, px[kx], py[ky], layer);
+        } else {
 #pragma unroll
-                for (int xx = 0; xx < 5; ++xx)
-                    t[xx] = lv_fetch(L, x0 + xx, y0 + yy, z0 + zz);
-            }
-            float rowc[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                rowc[k] = t[k] + fx * (t[k + 1] - t[k]);
-            if (yy > 0) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    cur[(yy - 1) * 4 + k] = rowp[k] + fy * (rowc[k] - rowp[k]);
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                rowp[k] = rowc[k];
+            for (int k = 0; k < 16; ++k)
+                cur[k] = 0.0f;
         }
-        if (zz > 0) {
+        if (s > 0) {
+            float v[16];
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-                emit((zz - 1) * 8 + j, prev[2 * j] + fz * (cur[2 * j] - prev[2 * j]),
-                     prev[2 * j + 1] + fz * (cur[2 * j + 1] - prev[2 * j + 1]));
+            for (int k = 0; k < 16; ++k)
+                v[k] = prev[k] + fz * (cur[k] - prev[k]);
+            emit(s - 1, v);
         }
 #pragma unroll
         for (int k = 0; k < 16; ++k)
@@ -93,18 +87,17 @@ __device__ __forceinline__ void stencil_block(const ConeLevel& L, int x0, int y0
     }
 }
 
-// 4x4x4 trilinear samples of level L at texel-spaced offsets (k - 1.5) around normalised point u, in the
-// order (kz*4 + ky)*4 + kx. The samples share one 5x5x5 block of texels and one set of weights.
-template<class Emit>
-__device__ __forceinline__ void stencil64(const ConeLevel& L, float ux, float uy, float uz, Emit&& emit) {
-    const float cx = ux * L.fd[0] - 2.0f, cy = uy * L.fd[1] - 2.0f, cz = uz * L.fd[2] - 2.0f;
-    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
-    const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
-    const float fx = cx - fx0, fy = cy - fy0, fz = cz - fz0;
-    if (x0 >= 0 && y0 >= 0 && z0 >= 0 && x0 + 4 < L.d[0] && y0 + 4 < L.d[1] && z0 + 4 < L.d[2])
-        stencil_block<true>(L, x0, y0, z0, fx, fy, fz, emit);
-    else
-        stencil_block<false>(L, x0, y0, z0, fx, fy, fz, emit);
+__global__ void __launch_bounds__(256) fill_stencil_tex_kernel(const float* __restrict__ src, int dx, int dy, int dz,
+                                                               float sat, unsigned long long surf) {
+    const int64_t n = (int64_t) dx * dy * dz;
+    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
+        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), z = (int) (i / ((int64_t) dx * dy));
+        float v = src[i];
+        if (sat > 0.0f)
+            v = fminf(fmaxf(v * sat, 0.0f), 1.0f);
+        surf2DLayeredwrite(__half_as_ushort(__float2half_rn(v)), (cudaSurfaceObject_t) surf, x * (int) sizeof(__half), y,
+                           z);
+    }
 }
 
 // Surface point (normalised volume coordinates) and unit normal; false for a zero normal.
@@ -140,14 +133,13 @@ __global__ void __launch_bounds__(128) mlp_collect_kernel(const ConeParams cp, c
         return;
     }
     float* x = X + (size_t) i * MLP_IN;
-    stencil64(cp.lv[cp.stencil_level], u[0], u[1], u[2], [&](int m, float a, float b) {
-        x[2 * m] = a;
-        x[2 * m + 1] = b;
-    });
-    stencil64(cp.lv[cp.stencil_level + 1], u[0], u[1], u[2], [&](int m, float a, float b) {
-        x[64 + 2 * m] = a;
-        x[64 + 2 * m + 1] = b;
-    });
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        stencil64(cp.stex[h], cp.sinv[h], cp.lv[cp.stencil_level + h].d[2], u[0], u[1], u[2],
+                  [&](int kz, const float* v) {
+                      for (int k = 0; k < 16; ++k)
+                          x[64 * h + 16 * kz + k] = v[k];
+                  });
     x[128] = n[0];
     x[129] = n[1];
     x[130] = n[2];
@@ -501,7 +493,9 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
     uint8_t* sW1 = tc_smem + tc::A_BYTES;
     uint8_t* sW2 = sW1 + tc::W1_BYTES;
     __shared__ float sB1[MLP_H], sB2[MLP_H], sW3[MLP_H];
-    __shared__ __align__(8) float2 sRange[MLP_KP / 2][2];
+    // training range per feature pair, rounded outward to BF16 (the features are checked as the BF16 values
+    // the network sees)
+    __shared__ __nv_bfloat162 sLo2[MLP_KP / 2], sHi2[MLP_KP / 2];
     __shared__ __align__(8) uint64_t s_mbar;
     __shared__ uint32_t s_tmem;
     __shared__ float s_part[tc::M];
@@ -533,8 +527,8 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
             lo[e] = (args.lo && k < MLP_IN) ? args.lo[k] : -INFINITY;
             hi[e] = (args.hi && k < MLP_IN) ? args.hi[k] : INFINITY;
         }
-        sRange[w][0] = make_float2(lo[0], lo[1]);
-        sRange[w][1] = make_float2(hi[0], hi[1]);
+        sLo2[w] = __halves2bfloat162(__float2bfloat16_rd(lo[0]), __float2bfloat16_rd(lo[1]));
+        sHi2[w] = __halves2bfloat162(__float2bfloat16_ru(hi[0]), __float2bfloat16_ru(hi[1]));
     }
     const uint32_t mbar = smem_u32(&s_mbar);
     if (t == 0) {
@@ -565,6 +559,7 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
         bool oor = false;
         uint32_t o = 0;
         // ---- features: this thread's half of row `row` ----
+        auto in_range = [&](int w, __nv_bfloat162 v2) { return __hble2(sLo2[w], v2) && __hble2(v2, sHi2[w]); };
         if (FEATURES_IN) {
             // half h writes k in [72 h, 72 h + 72)
 #pragma unroll 1
@@ -573,21 +568,13 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
                 uint32_t pk[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
-                    float v2[2];
-#pragma unroll
-                    for (int b = 0; b < 2; ++b) {
-                        const int k = k0 + 2 * e + b;
-                        float v = 0.0f;
-                        if (valid && k < MLP_IN) {
-                            v = args.X[(size_t) pi * MLP_IN + k];
-                            if (check) {
-                                const float2 lo = sRange[k >> 1][0], hi = sRange[k >> 1][1];
-                                oor |= !(v >= (b ? lo.y : lo.x) && v <= (b ? hi.y : hi.x));
-                            }
-                        }
-                        v2[b] = v;
-                    }
-                    pk[e] = pack_bf16(v2[0], v2[1]);
+                    const int k = k0 + 2 * e;
+                    const float a = (valid && k < MLP_IN) ? args.X[(size_t) pi * MLP_IN + k] : 0.0f;
+                    const float b = (valid && k + 1 < MLP_IN) ? args.X[(size_t) pi * MLP_IN + k + 1] : 0.0f;
+                    const __nv_bfloat162 v2 = __floats2bfloat162_rn(a, b);
+                    if (check && valid)
+                        oor |= !in_range(k >> 1, v2);
+                    pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
                 }
                 st_shared_v4(sA + canon_off(row, k0, tc::SBO1), pk[0], pk[1], pk[2], pk[3]);
             }
@@ -600,19 +587,24 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
                         mlp_point(cp, p, args.nrm[o], u, nn);
             }
             uint8_t* arow = sA + canon_off(row, 64 * half, tc::SBO1);
-            const float2(*rng)[2] = sRange + 32 * half;
-            uint32_t pk[4];
-            auto emit = [&](int m, float a, float b) {
-                pk[m & 3] = pack_bf16(a, b);
-                if ((m & 3) == 3)
-                    st_shared_v4(arow + (m >> 2) * 128, pk[0], pk[1], pk[2], pk[3]);
-                if (check) {
-                    const float2 lo = rng[m][0], hi = rng[m][1];
-                    oor |= !(a >= lo.x && a <= hi.x && b >= lo.y && b <= hi.y);
-                }
-            };
             if (valid) {
-                stencil64(cp.lv[cp.stencil_level + half], u[0], u[1], u[2], emit);
+                // z row kz of the stencil = two 16-byte chunks of the A row
+                stencil64(cp.stex[half], cp.sinv[half], cp.lv[cp.stencil_level + half].d[2], u[0], u[1], u[2],
+                          [&](int kz, const float* v) {
+#pragma unroll
+                              for (int c = 0; c < 2; ++c) {
+                                  uint32_t pk[4];
+#pragma unroll
+                                  for (int e = 0; e < 4; ++e) {
+                                      const __nv_bfloat162 v2 =
+                                          __floats2bfloat162_rn(v[8 * c + 2 * e], v[8 * c + 2 * e + 1]);
+                                      if (check)
+                                          oor |= !in_range(32 * half + 8 * kz + 4 * c + e, v2);
+                                      pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
+                                  }
+                                  st_shared_v4(arow + (2 * kz + c) * 128, pk[0], pk[1], pk[2], pk[3]);
+                              }
+                          });
             } else {
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
@@ -620,11 +612,12 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
             }
             // features 128..143: the normal and zero padding (chunk 16 on half 0, chunk 17 on half 1)
             if (half == 0) {
-                st_shared_v4(sA + canon_off(row, 128, tc::SBO1), pack_bf16(nn[0], nn[1]), pack_bf16(nn[2], 0.0f), 0u,
-                             0u);
+                const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
+                const __nv_bfloat162 n2 = __floats2bfloat162_rn(nn[2], 0.0f);
+                st_shared_v4(sA + canon_off(row, 128, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
+                             *reinterpret_cast<const uint32_t*>(&n2), 0u, 0u);
                 if (valid && check)
-                    oor |= !(nn[0] >= sRange[64][0].x && nn[0] <= sRange[64][1].x && nn[1] >= sRange[64][0].y &&
-                             nn[1] <= sRange[64][1].y && nn[2] >= sRange[65][0].x && nn[2] <= sRange[65][1].x);
+                    oor |= !(in_range(64, n01) && in_range(65, n2));
             } else {
                 st_shared_v4(sA + canon_off(row, 136, tc::SBO1), 0u, 0u, 0u, 0u);
             }
@@ -724,6 +717,63 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
 
 size_t mlp_train_smem_bytes() {
     return sizeof(float) * (MLP_H * MLP_IN + MLP_H * MLP_H + TS * MLP_IN + 6 * TS * MLP_H + TS);
+}
+
+cudaError_t StencilTex::ensure(const int dims[3]) {
+    if (arr && d[0] == dims[0] && d[1] == dims[1] && d[2] == dims[2])
+        return cudaSuccess;
+    release();
+    cudaChannelFormatDesc fmt = cudaCreateChannelDescHalf();
+    // one layer per z slice
+    cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2]),
+                                      cudaArrayLayered | cudaArraySurfaceLoadStore);
+    if (e != cudaSuccess) {
+        arr = nullptr;
+        return e;
+    }
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td{};
+    for (int a = 0; a < 3; ++a)
+        td.addressMode[a] = cudaAddressModeBorder;  // CLAMP_TO_BORDER with border colour 0
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    cudaTextureObject_t to = 0;
+    cudaSurfaceObject_t so = 0;
+    if ((e = cudaCreateTextureObject(&to, &rd, &td, nullptr)) != cudaSuccess ||
+        (e = cudaCreateSurfaceObject(&so, &rd)) != cudaSuccess) {
+        if (to)
+            cudaDestroyTextureObject(to);
+        cudaFreeArray(arr);
+        arr = nullptr;
+        return e;
+    }
+    tex = to;
+    surf = so;
+    for (int a = 0; a < 3; ++a)
+        d[a] = dims[a];
+    return cudaSuccess;
+}
+
+void StencilTex::release() {
+    if (tex)
+        cudaDestroyTextureObject((cudaTextureObject_t) tex);
+    if (surf)
+        cudaDestroySurfaceObject((cudaSurfaceObject_t) surf);
+    if (arr)
+        cudaFreeArray(arr);
+    arr = nullptr;
+    tex = surf = 0;
+    d[0] = d[1] = d[2] = 0;
+}
+
+cudaError_t launch_fill_stencil_tex(const ConeLevel& L, float sat, const StencilTex& t, cudaStream_t st) {
+    const int64_t n = (int64_t) L.d[0] * L.d[1] * L.d[2];
+    const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    fill_stencil_tex_kernel<<<grd, 256, 0, st>>>(L.v, L.d[0], L.d[1], L.d[2], sat, t.surf);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_mlp_collect(const ConeParams& cp, const uint32_t* order, const uint32_t* sel, uint32_t nsel,

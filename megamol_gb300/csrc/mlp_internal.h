@@ -41,6 +41,20 @@ struct MlpInferArgs {
     uint32_t* err;                  // ERR_* bits (the tensor-core kernel's bounded waits)
 };
 
+// One mip level of the AO volume as an FP16 layered 2D texture, one layer per z slice (CLAMP_TO_BORDER,
+// linear filtering in x and y, normalised coordinates), written through a surface. The learned AO's
+// stencil samples it with the texture units.
+struct StencilTex {
+    cudaArray_t arr = nullptr;
+    unsigned long long tex = 0;   // cudaTextureObject_t
+    unsigned long long surf = 0;  // cudaSurfaceObject_t
+    int d[3] = {0, 0, 0};
+    cudaError_t ensure(const int dims[3]);
+    void release();
+};
+// copy level L (level-0 saturation `sat` applied when > 0) into the texture
+cudaError_t launch_fill_stencil_tex(const ConeLevel& L, float sat, const StencilTex& t, cudaStream_t st);
+
 size_t mlp_train_smem_bytes();
 cudaError_t launch_mlp_collect(const ConeParams& cp, const uint32_t* order, const uint32_t* sel, uint32_t nsel,
     const float4* xyzr, const float4* nrm, const float* ao, float* X, float* T, uint32_t* kept, cudaStream_t st);
