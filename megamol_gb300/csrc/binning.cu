@@ -143,49 +143,76 @@ __global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, f
 }
 
 // ---------------------------------------------------------------------------------------------
-// Onesweep LSD radix sort of (key, value) pairs, 8-bit digits.
+// Onesweep LSD radix sort of (key, value) pairs with 8- or 9-bit digits: a key of B bits takes
+// ceil(B / 9) passes (a 256^3 grid's 25-bit bin keys take 9 + 8 + 8 bits, three passes).
 // ---------------------------------------------------------------------------------------------
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
 constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 4096 keys per tile
-constexpr int RADIX = 256;
+constexpr int MAX_RADIX = 512;
+constexpr int MAX_PASSES = 4;
+constexpr int HIST_WORDS = MAX_PASSES * MAX_RADIX;    // digit histograms, pass p at p * MAX_RADIX
 constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_PRE = 2u << 30;
 constexpr uint32_t FLAG_MASK = 3u << 30;
 constexpr uint32_t COUNT_MASK = (1u << 30) - 1u;
 
-__global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n, int passes,
+struct SortPlan {
+    int passes;
+    int shift[MAX_PASSES];
+    int bits[MAX_PASSES];
+};
+
+SortPlan sort_plan(uint32_t max_key) {
+    int nb = 0;
+    while (nb < 32 && (max_key >> nb) != 0u)
+        ++nb;
+    nb = std::max(nb, 1);
+    SortPlan pl{};
+    pl.passes = (nb + 8) / 9;
+    // the first (nb - 8 * passes) passes take 9 bits, the others 8
+    int nine = std::max(0, nb - 8 * pl.passes);
+    int sh = 0;
+    for (int p = 0; p < pl.passes; ++p) {
+        pl.bits[p] = p < nine ? 9 : 8;
+        pl.shift[p] = sh;
+        sh += pl.bits[p];
+    }
+    return pl;
+}
+
+__global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan pl,
     uint32_t* __restrict__ hist) {
-    __shared__ uint32_t sh[4 * RADIX];
-    for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x)
+    __shared__ uint32_t sh[HIST_WORDS];
+    for (int i = threadIdx.x; i < HIST_WORDS; i += blockDim.x)
         sh[i] = 0;
     __syncthreads();
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t k = keys[j];
-        for (int p = 0; p < passes; ++p)
-            atomicAdd(&sh[p * RADIX + ((k >> (8 * p)) & 0xFFu)], 1u);
+        for (int p = 0; p < pl.passes; ++p)
+            atomicAdd(&sh[p * MAX_RADIX + ((k >> pl.shift[p]) & ((1u << pl.bits[p]) - 1u))], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x)
+    for (int i = threadIdx.x; i < pl.passes * MAX_RADIX; i += blockDim.x)
         if (sh[i])
             atomicAdd(&hist[i], sh[i]);
 }
 
-// Exclusive scan of each pass' digit histogram (one block of 256 threads).
-__global__ void radix_scan_kernel(uint32_t* hist, int passes) {
-    __shared__ uint32_t s[RADIX];
+// Exclusive scan of each pass' digit histogram (one block of MAX_RADIX threads).
+__global__ void __launch_bounds__(MAX_RADIX) radix_scan_kernel(uint32_t* hist, int passes) {
+    __shared__ uint32_t s[MAX_RADIX];
     for (int p = 0; p < passes; ++p) {
-        uint32_t v = hist[p * RADIX + threadIdx.x];
+        const uint32_t v = hist[p * MAX_RADIX + threadIdx.x];
         s[threadIdx.x] = v;
         __syncthreads();
-        for (int o = 1; o < RADIX; o <<= 1) {
-            uint32_t t = threadIdx.x >= (unsigned) o ? s[threadIdx.x - o] : 0u;
+        for (int o = 1; o < MAX_RADIX; o <<= 1) {
+            const uint32_t t = threadIdx.x >= (unsigned) o ? s[threadIdx.x - o] : 0u;
             __syncthreads();
             s[threadIdx.x] += t;
             __syncthreads();
         }
-        hist[p * RADIX + threadIdx.x] = s[threadIdx.x] - v;
+        hist[p * MAX_RADIX + threadIdx.x] = s[threadIdx.x] - v;
         __syncthreads();
     }
 }
@@ -198,17 +225,25 @@ __device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) {
     *reinterpret_cast<volatile uint32_t*>(p) = v;
 }
 
-template<bool GATHER>
-__global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* __restrict__ keys_in,
+// One pass over digit (key >> shift) & (RADIX - 1). Tiles are taken in launch order from a counter; each
+// tile ranks its keys stably (warp match on the digit, per-warp digit counters), publishes its digit
+// counts, resolves its global offsets by decoupled look-back (bounded spins), stages the tile in digit
+// order in shared memory and writes runs of equal digits contiguously.
+template<bool GATHER, int BITS>
+__global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_t* __restrict__ keys_in,
     const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
     int shift, const uint32_t* __restrict__ digit_offsets, uint32_t* __restrict__ tile_counter,
     uint32_t* __restrict__ status, uint32_t* __restrict__ err, const float4* __restrict__ xyzr_in,
     float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo) {
-    __shared__ uint32_t s_keys[SORT_TILE];
-    __shared__ uint32_t s_vals[SORT_TILE];
-    __shared__ uint32_t s_whist[SORT_WARPS][RADIX];
-    __shared__ uint32_t s_base[RADIX];   // global destination of this tile's first item of each digit
-    __shared__ uint32_t s_local[RADIX];  // tile-local exclusive offset of each digit
+    constexpr int RADIX = 1 << BITS;
+    constexpr uint32_t DMASK = RADIX - 1u;
+    constexpr int DPT = RADIX / SORT_THREADS;  // digits per thread in the per-digit phases
+    extern __shared__ __align__(16) uint32_t sort_smem[];
+    uint32_t* s_keys = sort_smem;                                                  // [SORT_TILE]
+    uint32_t* s_vals = s_keys + SORT_TILE;                                         // [SORT_TILE]
+    uint32_t(*s_whist)[RADIX] = reinterpret_cast<uint32_t(*)[RADIX]>(s_vals + SORT_TILE);  // [SORT_WARPS][RADIX]
+    uint32_t* s_base = s_vals + SORT_TILE + SORT_WARPS * RADIX;  // global destination of each digit's first item
+    uint32_t* s_local = s_base + RADIX;                          // tile-local exclusive offset of each digit
     __shared__ uint32_t s_scan[SORT_WARPS];
     __shared__ uint32_t s_tile;
 
@@ -238,7 +273,7 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
     for (int i = 0; i < SORT_ITEMS; ++i) {
         const uint32_t j = wbase + i * 32 + lane;
         const bool valid = j < n;
-        const uint32_t d = (k[i] >> shift) & 0xFFu;
+        const uint32_t d = (k[i] >> shift) & DMASK;
         const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : (RADIX + lane));
         const uint32_t cnt = __popc(peers);
         const uint32_t before = __popc(peers & lt_mask);
@@ -252,27 +287,29 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
     }
     __syncthreads();
 
-    // per digit: exclusive offsets over warps, and the tile count
-    const uint32_t d = tid;  // SORT_THREADS == RADIX
-    uint32_t run = 0;
+    // per digit (thread tid owns digits tid*DPT .. tid*DPT + DPT-1): exclusive offsets over warps, counts
+    uint32_t count[DPT];
+    uint32_t tsum = 0;
 #pragma unroll
-    for (int ww = 0; ww < SORT_WARPS; ++ww) {
-        uint32_t c = s_whist[ww][d];
-        s_whist[ww][d] = run;
-        run += c;
+    for (int e = 0; e < DPT; ++e) {
+        const int d = tid * DPT + e;
+        uint32_t run = 0;
+#pragma unroll
+        for (int ww = 0; ww < SORT_WARPS; ++ww) {
+            const uint32_t c = s_whist[ww][d];
+            s_whist[ww][d] = run;
+            run += c;
+        }
+        count[e] = run;
+        tsum += run;
+        // publish the tile aggregate (or the inclusive prefix for tile 0) before looking back
+        st_volatile(status + (size_t) tile * RADIX + d, (tile == 0 ? FLAG_PRE : FLAG_AGG) | run);
     }
-    const uint32_t count = run;
-    // publish the tile aggregate (or the inclusive prefix for tile 0) before looking back
-    uint32_t* my = status + (size_t) tile * RADIX + d;
-    if (tile == 0)
-        st_volatile(my, FLAG_PRE | count);
-    else
-        st_volatile(my, FLAG_AGG | count);
-    // tile-local exclusive scan over digits (block scan of `count`)
-    uint32_t incl = count;
+    // tile-local exclusive scan over digits (block scan of the per-thread digit sums)
+    uint32_t incl = tsum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (uint32_t) o)
             incl += t;
     }
@@ -282,30 +319,39 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
     uint32_t wpre = 0;
     for (int ww = 0; ww < w; ++ww)
         wpre += s_scan[ww];
-    s_local[d] = wpre + incl - count;
-
-    // decoupled look-back for digit d
-    uint32_t excl = 0;
-    if (tile > 0) {
-        int32_t t = (int32_t) tile - 1;
-        uint32_t spins = 0;
-        while (t >= 0) {
-            uint32_t s = ld_volatile(status + (size_t) t * RADIX + d);
-            if ((s & FLAG_MASK) == 0u) {
-                if (++spins > SPIN_LIMIT) {
-                    atomicOr(err, ERR_LOOKBACK_TIMEOUT);
-                    break;
-                }
-                continue;
-            }
-            excl += s & COUNT_MASK;
-            if ((s & FLAG_MASK) == FLAG_PRE)
-                break;
-            --t;
-        }
-        st_volatile(my, FLAG_PRE | (excl + count));
+    uint32_t run = wpre + incl - tsum;
+#pragma unroll
+    for (int e = 0; e < DPT; ++e) {
+        s_local[tid * DPT + e] = run;
+        run += count[e];
     }
-    s_base[d] = digit_offsets[d] + excl;
+
+    // decoupled look-back per digit
+#pragma unroll
+    for (int e = 0; e < DPT; ++e) {
+        const int d = tid * DPT + e;
+        uint32_t excl = 0;
+        if (tile > 0) {
+            int32_t t = (int32_t) tile - 1;
+            uint32_t spins = 0;
+            while (t >= 0) {
+                const uint32_t sv = ld_volatile(status + (size_t) t * RADIX + d);
+                if ((sv & FLAG_MASK) == 0u) {
+                    if (++spins > SPIN_LIMIT) {
+                        atomicOr(err, ERR_LOOKBACK_TIMEOUT);
+                        break;
+                    }
+                    continue;
+                }
+                excl += sv & COUNT_MASK;
+                if ((sv & FLAG_MASK) == FLAG_PRE)
+                    break;
+                --t;
+            }
+            st_volatile(status + (size_t) tile * RADIX + d, FLAG_PRE | (excl + count[e]));
+        }
+        s_base[d] = digit_offsets[d] + excl;
+    }
     __syncthreads();
 
     // stage the tile in digit order, then write runs of equal digits contiguously
@@ -313,7 +359,7 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
     for (int i = 0; i < SORT_ITEMS; ++i) {
         const uint32_t j = wbase + i * 32 + lane;
         if (j < n) {
-            const uint32_t dd = (k[i] >> shift) & 0xFFu;
+            const uint32_t dd = (k[i] >> shift) & DMASK;
             const uint32_t lp = s_local[dd] + s_whist[w][dd] + rk[i];
             s_keys[lp] = k[i];
             s_vals[lp] = v[i];
@@ -323,7 +369,7 @@ __global__ void __launch_bounds__(SORT_THREADS) onesweep_kernel(const uint32_t* 
     const uint32_t tile_n = n - base < (uint32_t) SORT_TILE ? n - base : (uint32_t) SORT_TILE;
     for (uint32_t j = tid; j < tile_n; j += SORT_THREADS) {
         const uint32_t kk = s_keys[j];
-        const uint32_t dd = (kk >> shift) & 0xFFu;
+        const uint32_t dd = (kk >> shift) & DMASK;
         const uint32_t dst = s_base[dd] + (j - s_local[dd]);
         keys_out[dst] = kk;
         const uint32_t vv = s_vals[j];
@@ -426,42 +472,63 @@ cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, 
 }
 
 size_t sort_status_words(uint32_t n) {
-    return (size_t) ceil_div(n, SORT_TILE) * RADIX;
+    return (size_t) ceil_div(n, SORT_TILE) * MAX_RADIX;
+}
+
+size_t sort_hist_words() {
+    return HIST_WORDS + 8;
 }
 
 int sort_passes(uint32_t max_key) {
-    int bits = 0;
-    while (bits < 32 && (max_key >> bits) != 0u)
-        ++bits;
-    return bits == 0 ? 1 : (bits + 7) / 8;
+    return sort_plan(max_key).passes;
+}
+
+template<bool GATHER, int BITS>
+cudaError_t launch_onesweep_bits(uint32_t tiles, SortBuffers& b, int cur, uint32_t n, int shift, const uint32_t* offs,
+                                 uint32_t* counter, cudaStream_t st) {
+    constexpr int RADIX = 1 << BITS;
+    const int smem = (int) sizeof(uint32_t) * (2 * SORT_TILE + SORT_WARPS * RADIX + 2 * RADIX);
+    const cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<GATHER, BITS>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess)
+        return e;
+    onesweep_kernel<GATHER, BITS><<<tiles, SORT_THREADS, smem, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
+        b.vals[cur ^ 1], n, shift, offs, counter, b.status, b.err, GATHER ? b.xyzr_in : nullptr,
+        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, b.geo);
+    return cudaSuccess;
+}
+
+template<bool GATHER>
+cudaError_t launch_onesweep(int bits, uint32_t tiles, SortBuffers& b, int cur, uint32_t n, int shift,
+                            const uint32_t* offs, uint32_t* counter, cudaStream_t st) {
+    return bits == 9 ? launch_onesweep_bits<GATHER, 9>(tiles, b, cur, n, shift, offs, counter, st)
+                     : launch_onesweep_bits<GATHER, 8>(tiles, b, cur, n, shift, offs, counter, st);
 }
 
 cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st) {
-    const int passes = sort_passes(max_key);
+    const SortPlan pl = sort_plan(max_key);
     const uint32_t tiles = ceil_div(n, SORT_TILE);
-    cudaError_t e = cudaMemsetAsync(b.hist, 0, sizeof(uint32_t) * (4 * RADIX + 8), st);
+    cudaError_t e = cudaMemsetAsync(b.hist, 0, sizeof(uint32_t) * sort_hist_words(), st);
     if (e != cudaSuccess)
         return e;
     if (n == 0)
         return cudaSuccess;
     const unsigned hgrid = (unsigned) std::min<uint32_t>(ceil_div(n, 256 * 8), (uint32_t) sms * 4);
-    radix_hist_kernel<<<hgrid ? hgrid : 1, 256, 0, st>>>(b.keys[0], n, passes, b.hist);
-    radix_scan_kernel<<<1, RADIX, 0, st>>>(b.hist, passes);
+    radix_hist_kernel<<<hgrid ? hgrid : 1, 256, 0, st>>>(b.keys[0], n, pl, b.hist);
+    radix_scan_kernel<<<1, MAX_RADIX, 0, st>>>(b.hist, pl.passes);
     int cur = 0;
-    for (int p = 0; p < passes; ++p) {
-        e = cudaMemsetAsync(b.status, 0, sizeof(uint32_t) * (size_t) tiles * RADIX, st);
+    for (int p = 0; p < pl.passes; ++p) {
+        e = cudaMemsetAsync(b.status, 0, sizeof(uint32_t) * (size_t) tiles * ((size_t) 1 << pl.bits[p]), st);
         if (e != cudaSuccess)
             return e;
-        uint32_t* counter = b.hist + 4 * RADIX + p;
-        const bool last = p == passes - 1;
+        uint32_t* counter = b.hist + HIST_WORDS + p;
+        const bool last = p == pl.passes - 1;
         if (last && b.xyzr_in != nullptr)
-            onesweep_kernel<true><<<tiles, SORT_THREADS, 0, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
-                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, b.xyzr_in, b.rec_a,
-                b.rec_b, b.geo);
+            e = launch_onesweep<true>(pl.bits[p], tiles, b, cur, n, pl.shift[p], b.hist + p * MAX_RADIX, counter, st);
         else
-            onesweep_kernel<false><<<tiles, SORT_THREADS, 0, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
-                b.vals[cur ^ 1], n, 8 * p, b.hist + p * RADIX, counter, b.status, b.err, nullptr, nullptr, nullptr,
-                b.geo);
+            e = launch_onesweep<false>(pl.bits[p], tiles, b, cur, n, pl.shift[p], b.hist + p * MAX_RADIX, counter, st);
+        if (e != cudaSuccess)
+            return e;
         cur ^= 1;
     }
     b.result = cur;

@@ -281,7 +281,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     P2V_CUDA_TRY(vals0.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals1.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(status.ensure(4 * (sort_status_words(n) + 256)));
-    P2V_CUDA_TRY(hist.ensure(4 * (4 * 256 + 8)));
+    P2V_CUDA_TRY(hist.ensure(4 * sort_hist_words()));
     P2V_CUDA_TRY(cstart.ensure(4 * ((size_t) g.nbins + 1)));
     P2V_CUDA_TRY(gaps.ensure(sizeof(uint4) * gap_cap));
     P2V_CUDA_TRY(tiles.ensure(sizeof(TileStats) * ntiles));

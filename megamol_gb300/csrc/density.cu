@@ -406,11 +406,12 @@ struct WarpPart {
 };
 constexpr int WP_FIELDS = 9;
 
-// Fixed-point scale of the exact accumulation: contributions are rounded to multiples of 2^-40 and
-// summed as 64-bit integers, so every voxel holds the exact sum of its rounded FP32 contributions,
-// independent of the order in which particles arrive.
-constexpr float FIX_SCALE = 1099511627776.0f;  // 2^40
-constexpr float FIX_INV = 9.094947017729282e-13f;  // 2^-40
+// Fixed-point scale of the exact accumulation: contributions (all below 1) are rounded to multiples of
+// 2^-32 and summed as 64-bit integers held in two 32-bit words per node (a 32-bit shared-memory atomic on
+// the low word; the thread whose add wraps it carries into the high word), so every voxel holds the exact
+// sum of its rounded FP32 contributions, independent of the order in which particles arrive.
+constexpr float FIX_SCALE = 4294967296.0f;          // 2^32
+constexpr float FIX_INV = 2.3283064365386963e-10f;  // 2^-32
 
 // Particle-major gather with exact, order-independent accumulation. A CTA owns a tile of TX*TY*TZ
 // nodes held as 64-bit fixed-point sums in shared memory; for every cyclic image of the tile it walks
@@ -422,8 +423,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     TileStats* __restrict__ tiles, FrameScalars* __restrict__ fs, int rmax) {
     constexpr int NN = TX * TY * TZ;
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem);  // [NN]
-    uint32_t* row_beg = reinterpret_cast<uint32_t*>(acc + NN);               // [rmax]
+    uint32_t* acc_lo = reinterpret_cast<uint32_t*>(smem);  // [NN] low words of the fixed-point sums
+    uint32_t* acc_hi = acc_lo + NN;                        // [NN] high words
+    uint32_t* row_beg = acc_hi + NN;                        // [rmax]
     uint32_t* row_off = row_beg + rmax;                                      // [rmax + 1]
     __shared__ double s_dsum[NT / 32];
     __shared__ float s_fmin[NT / 32], s_fmax[NT / 32];
@@ -437,8 +439,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
     const int T3[3] = {TX, TY, TZ};
     const int o3[3] = {x0, y0, z0};
-    for (int n = t; n < NN; n += NT)
-        acc[n] = 0ull;
+    for (int n = t; n < NN; n += NT) {
+        acc_lo[n] = 0u;
+        acc_hi[n] = 0u;
+    }
     const bool bump = g.kernel == 0;
     const float E45 = __expf(-4.5f);
     if (t == 0)
@@ -610,7 +614,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                         const float inv = __uint_as_float(s_part[4][ow]);
                                         const float d0x = __uint_as_float(s_part[0][ow]);
                                         const int bx = (int) s_part[6][ow];
-                                        unsigned long long* row = acc + (int) s_part[8][ow] + (zl * TY + yl) * TX;
+                                        const int row = (int) s_part[8][ow] + (zl * TY + yl) * TX;
                                         for (int xl = 0; xl < bx; ++xl) {
                                             const float dx = g.hhi[0] * (static_cast<float>(xl) + d0x);
                                             const float d2 = __fmaf_rn(dx, dx, dyz);
@@ -625,7 +629,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                             } else {
                                                 v = fmaxf(__expf(-d2 * inv) - E45, 0.0f);
                                             }
-                                            atomicAdd(row + xl, (unsigned long long) __float2ull_rn(v * FIX_SCALE));
+                                            const uint32_t q = __float2uint_rn(v * FIX_SCALE);
+                                            if (q != 0u) {
+                                                const uint32_t old = atomicAdd(acc_lo + row + xl, q);
+                                                if (old + q < old)
+                                                    atomicAdd(acc_hi + row + xl, 1u);
+                                            }
                                         }
                                     }
                                 }
@@ -643,7 +652,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     for (int n = t; n < NN; n += NT) {
         const int x = n % TX, y = (n / TX) % TY, z = n / (TX * TY);
         if (x0 + x < g.s[0] && y0 + y < g.s[1] && z0 + z < g.s[2]) {
-            const float v = __ull2float_rn(acc[n]) * FIX_INV;
+            const float v = __ull2float_rn(((unsigned long long) acc_hi[n] << 32) | acc_lo[n]) * FIX_INV;
             grid[((size_t) (z0 + z) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)] = v;
             dsum += (double) v;
             vmin = fminf(vmin, v);

@@ -24,7 +24,7 @@ struct ListDesc {
 struct SortBuffers {
     uint32_t* keys[2];
     uint32_t* vals[2];
-    uint32_t* hist;        // 4*256 digit histograms + 8 tile counters
+    uint32_t* hist;        // digit histograms + tile counters, sort_hist_words()
     uint32_t* status;      // look-back words, sort_status_words(n)
     uint32_t* err;
     const float4* xyzr_in; // when non-null the last pass writes every particle's gather record
@@ -37,6 +37,7 @@ struct SortBuffers {
 cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,
     FrameScalars* fs, cudaStream_t st);
 size_t sort_status_words(uint32_t n);
+size_t sort_hist_words();
 int sort_passes(uint32_t max_key);
 cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st);
 cudaError_t launch_cell_start(const uint32_t* keys, uint32_t n, uint32_t nbins, uint32_t* start, uint4* gaps,
