@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 1
+#define P2V_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -156,7 +156,10 @@ typedef struct p2v_params {
     float aos_gen_fac;      /* "vol::genFac" (1) */
     float aos_eval_fac;     /* "ao::evalFac" (1) */
     /* --- execution --- */
-    int32_t tile_x, tile_y, tile_z; /* density tile; 0 = chosen by the library */
+    int32_t tile_x, tile_y, tile_z; /* density tile; 0 = the autotuned tile (p2v_autotune_batch) or 16^3 */
+    int32_t batch_lanes;    /* p2v_run_batch: concurrent frame pipelines; 0 = the autotuned count or 4 */
+    int32_t batch_graph;    /* p2v_run_batch: capture the batch as a CUDA graph and replay it while the batch's
+                               shape (frames, sizes, pointers, parameters) repeats (1) */
 } p2v_params;
 
 typedef struct p2v_stats {
@@ -230,6 +233,41 @@ P2V_API p2v_status p2v_get_ao_volume(p2v_ctx* ctx, int32_t level, float* out, ui
 P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
 /* Last error message of this context ("" if none); returns the message length. */
 P2V_API size_t p2v_get_last_error(const p2v_ctx* ctx, char* buf, size_t len);
+
+/* ---- batched frames ----
+ * No counterpart in the reference, whose ParticlesToDensity computes one frame per GET_DATA call. A batch
+ * runs many frames (a trajectory's, of uneven particle counts and grid sizes) with the current parameters:
+ * the frames are spread over batch_lanes concurrent pipelines (largest first, onto the least-loaded lane),
+ * nothing waits for the device until the whole batch is queued, and with batch_graph the queued batch is
+ * captured once as a CUDA graph and replayed by one launch while its shape repeats. Each frame's results
+ * equal those of p2v_run_frame on the same frame bit for bit. */
+typedef struct p2v_batch_item {
+    const p2v_frame* frame;
+    p2v_volume* volume;  /* the frame's grid and metadata; NULL or data == NULL: not returned */
+    int32_t size[3];     /* grid resolution of this frame; 0 = the parameters' sizex / sizey / sizez */
+} p2v_batch_item;
+
+/* stats (nullable) receives count per-frame statistics (stage times are not split per frame in a batch:
+ * p2v_get_stats afterwards reports the whole batch's device time in ms_total). */
+P2V_API p2v_status p2v_run_batch(p2v_ctx* ctx, const p2v_batch_item* items, uint32_t count, p2v_stats* stats,
+                                 void* stream);
+
+#define P2V_TUNE_MAX 32
+typedef struct p2v_tune_report {
+    uint32_t struct_size;
+    int32_t tile[3];                  /* chosen density tile (exact accumulation) */
+    int32_t lanes;                    /* chosen batch_lanes */
+    float ms_best;                    /* device time of one batch with the chosen configuration */
+    int32_t candidates;
+    int32_t cand_tile[P2V_TUNE_MAX][3];
+    int32_t cand_lanes[P2V_TUNE_MAX];
+    float cand_ms[P2V_TUNE_MAX];
+} p2v_tune_report;
+
+/* Time every compiled density tile x lane count on this batch (CUDA events, one warm-up run each) and keep
+ * the fastest for later calls whose tile_x / batch_lanes are 0. rep (nullable) receives the table. */
+P2V_API p2v_status p2v_autotune_batch(p2v_ctx* ctx, const p2v_batch_item* items, uint32_t count,
+                                      p2v_tune_report* rep);
 
 /* ---- learned AO ---- */
 P2V_API void p2v_train_params_default(p2v_train_params* tp);

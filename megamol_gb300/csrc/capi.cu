@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <random>
 #include <string>
@@ -58,6 +59,76 @@ struct DevBuf {
 
 enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_COUNT };
 
+// Scratch of one frame pipeline: every device buffer a frame touches, the stage timing events and the
+// pinned mirror of the frame scalars. A context owns one pipe for p2v_run_frame and one per lane of
+// p2v_run_batch; frames on different pipes may run concurrently.
+struct Pipe {
+    DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
+    DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list;
+    StencilTex stex[2];                    // the learned AO's two stencil levels as textures
+    cudaEvent_t ev[EV_COUNT] = {};
+    FrameScalars* h_scal = nullptr;        // pinned mirror of the last frame's scalars
+    cudaStream_t stream = nullptr;         // the stream of a batch lane
+    ConeParams last_cp{};
+    const float* last_grid = nullptr;
+    const uint32_t* last_order = nullptr;  // sorted position -> particle index of the last frame
+    uint64_t last_res[3] = {0, 0, 0};
+
+    cudaError_t init(bool with_stream) {
+        for (auto& e : ev) {
+            const cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess)
+                return r;
+        }
+        if (with_stream) {
+            const cudaError_t r = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+            if (r != cudaSuccess)
+                return r;
+        }
+        return cudaMallocHost(&h_scal, sizeof(FrameScalars));
+    }
+    void release() {
+        if (stream)
+            cudaStreamSynchronize(stream);
+        for (DevBuf* b : {&raw, &xyzr, &rec_a, &rec_b, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
+                          &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list})
+            b->release();
+        stex[0].release();
+        stex[1].release();
+        for (auto& e : ev)
+            if (e)
+                cudaEventDestroy(e);
+        if (h_scal)
+            cudaFreeHost(h_scal);
+        if (stream)
+            cudaStreamDestroy(stream);
+        h_scal = nullptr;
+        stream = nullptr;
+        last_grid = nullptr;
+        last_order = nullptr;
+    }
+};
+
+// Host-side state of a frame between its enqueue and its completion.
+struct FrameJob {
+    uint64_t N = 0;
+    int32_t res[3] = {0, 0, 0};
+    float bb[6] = {};
+    const float* dgrid = nullptr;
+    const uint32_t* order = nullptr;
+    FrameScalars* h_out = nullptr;  // pinned slot that receives the frame's scalars
+    bool timed = false;             // stage events were recorded
+};
+
+__global__ void init_scalars_kernel(FrameScalars* fs) {
+    FrameScalars z{};
+    for (int a = 0; a < 3; ++a) {
+        z.cmin[a] = INT32_MAX;
+        z.cmax[a] = INT32_MIN;
+    }
+    *fs = z;
+}
+
 }  // namespace
 
 struct p2v_ctx {
@@ -69,13 +140,24 @@ struct p2v_ctx {
     p2v_stats stats{};
     uint64_t datahash = 0;
 
-    DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
-    DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol;
+    Pipe main;                                  // p2v_run_frame
+    std::vector<std::unique_ptr<Pipe>> lanes;   // p2v_run_batch
+    // batches: pinned per-frame scalars, fork/join events, the captured graph and the shape it was captured for
+    FrameScalars* b_scal = nullptr;
+    size_t b_scal_cap = 0;
+    std::vector<cudaEvent_t> b_events;
+    cudaEvent_t b_t0 = nullptr, b_t1 = nullptr;
+    cudaGraphExec_t b_exec = nullptr;
+    std::vector<uint8_t> b_graph_sig, b_eager_sig;
+    std::vector<FrameJob> b_jobs;
+    std::vector<int> b_lane_of;
+    // autotuned choices (0 = none)
+    int tuned_tile[3] = {0, 0, 0};
+    int tuned_lanes = 0;
     // learned AO
     DevBuf mlp_P, mlp_m, mlp_v, mlp_g, mlp_part, mlp_ploss, mlp_loss, mlp_w1h, mlp_w2h, mlp_lo, mlp_hi, mlp_idx,
-        mlp_y, fb_list;
+        mlp_y;
     DevBuf tX, tT;                       // collected training pairs
-    StencilTex stex[2];                  // the learned AO's two stencil levels as textures
     uint64_t t_pairs = 0, t_cap = 0;
     std::vector<uint32_t> t_valid;       // indices of pairs with features
     std::vector<float> t_host_T;         // targets on the host (validation error)
@@ -83,12 +165,6 @@ struct p2v_ctx {
     int mlp_level = -1;                  // stencil base level the network was trained on
     int mlp_step = 0;
     uint64_t mlp_seed = 0;
-    ConeParams last_cp{};
-    FrameScalars* h_scal = nullptr;  // pinned mirror
-    cudaEvent_t ev[EV_COUNT] = {};
-    const float* last_grid = nullptr;
-    const uint32_t* last_order = nullptr;  // sorted position -> particle index of the last frame
-    uint64_t last_res[3] = {0, 0, 0};
 
     p2v_status fail(p2v_status s, const char* fmt, ...) {
         char buf[512];
@@ -101,12 +177,23 @@ struct p2v_ctx {
     }
 
     p2v_status run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st);
-    p2v_status run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
-                      const uint32_t* order, cudaStream_t st);
-    p2v_status build_cone(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
-                          const uint32_t* order, ConeParams& cp, cudaStream_t st);
+    p2v_status enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol, cudaStream_t st, FrameScalars* h_out,
+                             bool timed, FrameJob& job);
+    p2v_status finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol, p2v_stats& out);
+    p2v_status run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
+                      uint32_t n, const uint32_t* order, cudaStream_t st);
+    p2v_status build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
+                          uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st);
     p2v_status mlp_alloc();
-    p2v_status prepare_stencil(ConeParams& cp, cudaStream_t st);
+    p2v_status prepare_stencil(Pipe& pp, ConeParams& cp, cudaStream_t st);
+    p2v_status run_batch(const p2v_batch_item* items, uint32_t count, p2v_stats* out, cudaStream_t st,
+                         bool allow_graph, float* ms_out);
+    void drop_graph() {
+        if (b_exec)
+            cudaGraphExecDestroy(b_exec);
+        b_exec = nullptr;
+        b_graph_sig.clear();
+    }
     void mlp_init_params(uint64_t seed, float bias3);
 };
 
@@ -198,6 +285,23 @@ uint32_t record_bytes(int type) {
 
 p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st) {
     P2V_CUDA_TRY(cudaSetDevice(device));
+    FrameJob job;
+    const p2v_status es = enqueue_frame(main, fr, vol, st, main.h_scal, true, job);
+    if (es != P2V_OK)
+        return es;
+    P2V_CUDA_TRY(cudaStreamSynchronize(st));
+    return finish_frame(main, job, vol, stats);
+}
+
+// Validate the frame and queue its whole pipeline on `st` using the buffers of `pp`; the frame scalars are
+// copied to the pinned slot h_out at the end. Nothing here waits for the device.
+p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol, cudaStream_t st,
+                                  FrameScalars* h_out, bool timed, FrameJob& job) {
+    DevBuf &raw = pp.raw, &xyzr = pp.xyzr, &rec_a = pp.rec_a, &rec_b = pp.rec_b, &keys0 = pp.keys0,
+           &keys1 = pp.keys1, &vals0 = pp.vals0, &vals1 = pp.vals1, &status = pp.status, &hist = pp.hist,
+           &cstart = pp.cstart, &gaps = pp.gaps, &grid = pp.grid, &tiles = pp.tiles, &scal = pp.scal, &nrm = pp.nrm,
+           &ao = pp.ao;
+    cudaEvent_t* ev = pp.ev;
     const p2v_params& P = prm;
     if (P.aggregator != 0)
         return fail(P2V_EUNSUPPORTED, "aggregator %d is not implemented (only PosToSingleCell_Volume)", P.aggregator);
@@ -268,6 +372,8 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
         gc = GatherConfig{GATHER_EXACT, 16, 16, 16, 0, 1024};
         if (P.tile_x > 0 || P.tile_y > 0 || P.tile_z > 0)
             gc = GatherConfig{GATHER_EXACT, P.tile_x, P.tile_y, P.tile_z, 0, 1024};
+        else if (tuned_tile[0] > 0)
+            gc = GatherConfig{GATHER_EXACT, tuned_tile[0], tuned_tile[1], tuned_tile[2], 0, 1024};
     } else {
         return fail(P2V_EINVAL, "unknown accumulate mode %d", P.accumulate);
     }
@@ -298,15 +404,10 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
         return fail(P2V_EINVAL, "output capacity %llu < %llu floats", (unsigned long long) vol->capacity,
                     (unsigned long long) V);
 
-    FrameScalars init{};
-    for (int a = 0; a < 3; ++a) {
-        init.cmin[a] = INT32_MAX;
-        init.cmax[a] = INT32_MIN;
-    }
-    *h_scal = init;
     FrameScalars* fs = scal.as<FrameScalars>();
-    P2V_CUDA_TRY(cudaEventRecord(ev[EV_START], st));
-    P2V_CUDA_TRY(cudaMemcpyAsync(fs, h_scal, sizeof(FrameScalars), cudaMemcpyHostToDevice, st));
+    if (timed)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_START], st));
+    init_scalars_kernel<<<1, 1, 0, st>>>(fs);
 
     // ---- upload + pack + keys ----
     uint64_t raw_need = 0;
@@ -349,11 +450,15 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
                 raw_off += (bytes + 15) & ~uint64_t(15);
             }
         }
+        if (timed)
+            if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
         P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), vals0.as<uint32_t>(), fs, st));
         off += L.count;
     }
     if (N == 0)
+        if (timed)
+            if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
     // ---- normals for AO ----
     const bool want_ao = P.ao_mode != P2V_AO_NONE;
@@ -403,7 +508,8 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     P2V_CUDA_TRY(launch_sort(sb, n, g.nbins, sms, st));
     const uint32_t* skeys = sb.keys[sb.result];
     P2V_CUDA_TRY(launch_cell_start(skeys, n, g.nbins, cstart.as<uint32_t>(), gaps.as<uint4>(), gap_cap, fs, sms, st));
-    P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
+    if (timed)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
 
     // ---- density ----
     {
@@ -414,17 +520,20 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
                         gc.tz, P.accumulate);
         P2V_CUDA_TRY(ge);
     }
-    P2V_CUDA_TRY(cudaEventRecord(ev[EV_DENSITY], st));
+    if (timed)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_DENSITY], st));
     const double voxel_volume = (double) g.hhi[0] * g.hhi[1] * g.hhi[2];
     P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume, st));
     P2V_CUDA_TRY(launch_normalize_modes(dgrid, V, fs, P.mass_normalize, P.normalize, sms, st));
-    P2V_CUDA_TRY(cudaEventRecord(ev[EV_NORM], st));
+    if (timed)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_NORM], st));
     if (want_ao) {
-        const p2v_status as = run_ao(fr, g, dgrid, bb, n, sb.vals[sb.result], st);
+        const p2v_status as = run_ao(pp, fr, g, dgrid, bb, n, sb.vals[sb.result], st);
         if (as != P2V_OK)
             return as;
     }
-    P2V_CUDA_TRY(cudaEventRecord(ev[EV_AO], st));
+    if (timed)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_AO], st));
 
     // ---- outputs ----
     if (vol && vol->data && !direct)
@@ -443,13 +552,33 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
             aoff += L.count;
         }
     }
-    P2V_CUDA_TRY(cudaMemcpyAsync(h_scal, fs, sizeof(FrameScalars), cudaMemcpyDeviceToHost, st));
-    P2V_CUDA_TRY(cudaEventRecord(ev[EV_DOWN], st));
-    P2V_CUDA_TRY(cudaStreamSynchronize(st));
+    P2V_CUDA_TRY(cudaMemcpyAsync(h_out, fs, sizeof(FrameScalars), cudaMemcpyDeviceToHost, st));
+    if (timed)
+        P2V_CUDA_TRY(cudaEventRecord(ev[EV_DOWN], st));
+    job.N = N;
+    for (int a = 0; a < 3; ++a)
+        job.res[a] = res[a];
+    std::memcpy(job.bb, bb, sizeof(bb));
+    job.dgrid = dgrid;
+    job.order = sb.vals[sb.result];
+    job.h_out = h_out;
+    job.timed = timed;
+    return P2V_OK;
+}
 
-    const FrameScalars& hs = *h_scal;
+// Statistics, metadata and error status of a completed frame (its stream has been synchronised).
+p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol, p2v_stats& stats) {
+    const uint64_t N = job.N;
+    const int32_t* res = job.res;
+    const float* bb = job.bb;
+    const float* dgrid = job.dgrid;
+    cudaEvent_t* ev = pp.ev;
+    auto& last_grid = pp.last_grid;
+    auto& last_order = pp.last_order;
+    auto& last_res = pp.last_res;
+    const FrameScalars& hs = *job.h_out;
     last_grid = dgrid;
-    last_order = sb.vals[sb.result];
+    last_order = job.order;
     for (int a = 0; a < 3; ++a)
         last_res[a] = (uint64_t) res[a];
     stats = p2v_stats{};
@@ -462,7 +591,8 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
         stats.cell_max[a] = hs.cmax[a];
     }
     stats.mass_sum = hs.mass;
-    float ms;
+    float ms = 0.0f;
+    if (job.timed) {
     cudaEventElapsedTime(&ms, ev[EV_START], ev[EV_UPLOAD]);
     stats.ms_upload = ms;
     cudaEventElapsedTime(&ms, ev[EV_UPLOAD], ev[EV_BIN]);
@@ -477,6 +607,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
     stats.ms_download = ms;
     cudaEventElapsedTime(&ms, ev[EV_START], ev[EV_DOWN]);
     stats.ms_total = ms;
+    }
     stats.device_error = hs.error;
     stats.ao_fallback = hs.ao_fallback;
 
@@ -488,7 +619,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
             vol->slice_dists[a] = rangef / static_cast<float>(res[a] - 1);
             vol->origin[a] = bb[a];
         }
-        std::memcpy(vol->bbox, bb, sizeof(bb));
+        std::memcpy(vol->bbox, bb, sizeof(float) * 6);
         vol->components = 1;
         vol->min_value = hs.out_min;
         vol->max_value = hs.out_max;
@@ -525,8 +656,9 @@ void mdao_dims(const float clip[6], int vol_size, int dims[3], float& shortest, 
     max_lod = std::ceil(std::log2(static_cast<float>(vol_size))) - 1.0f;
 }
 
-p2v_status p2v_ctx::build_cone(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
-                               uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st) {
+p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid,
+                               const float bb[6], uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st) {
+    DevBuf &xyzr = pp.xyzr, &mips = pp.mips, &mdao_acc = pp.mdao_acc, &mdao_vol = pp.mdao_vol;
     const p2v_params& P = prm;
     if (P.ao_volume != P2V_AOVOL_DENSITY && P.ao_volume != P2V_AOVOL_MDAO)
         return fail(P2V_EINVAL, "ao_volume %d is not a p2v_ao_volume", P.ao_volume);
@@ -637,13 +769,14 @@ p2v_status p2v_ctx::build_cone(const p2v_frame* fr, const GridGeo& g, const floa
             cp.lv[l].fd[a] = (float) d[l][a];
         }
     }
-    last_cp = cp;
+    pp.last_cp = cp;
     return P2V_OK;
 }
 
 // Copy the learned AO's two stencil levels into their textures (level 0 of a density volume saturated as
 // the cone march sees it) and hand the texture objects to the kernels.
-p2v_status p2v_ctx::prepare_stencil(ConeParams& cp, cudaStream_t st) {
+p2v_status p2v_ctx::prepare_stencil(Pipe& pp, ConeParams& cp, cudaStream_t st) {
+    StencilTex* stex = pp.stex;
     for (int h = 0; h < 2; ++h) {
         const int l = cp.stencil_level + h;
         const ConeLevel& L = cp.lv[l];
@@ -656,12 +789,14 @@ p2v_status p2v_ctx::prepare_stencil(ConeParams& cp, cudaStream_t st) {
     return P2V_OK;
 }
 
-p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6], uint32_t n,
-                           const uint32_t* order, cudaStream_t st) {
+p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
+                           uint32_t n, const uint32_t* order, cudaStream_t st) {
+    DevBuf &xyzr = pp.xyzr, &nrm = pp.nrm, &ao = pp.ao, &scal = pp.scal, &fb_list = pp.fb_list,
+           &aos_acc = pp.aos_acc, &aos_tex = pp.aos_tex;
     const p2v_params& P = prm;
     if (P.ao_mode == P2V_AO_CONE) {
         ConeParams cp{};
-        const p2v_status bs = build_cone(fr, g, dgrid, bb, n, order, cp, st);
+        const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st);
         if (bs != P2V_OK)
             return bs;
         P2V_CUDA_TRY(launch_cone_ao(cp, order, xyzr.as<float4>(), nrm.as<float4>(), n, nullptr, ao.as<float>(), st));
@@ -671,14 +806,14 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
         if (!mlp_ready)
             return fail(P2V_EINVAL, "learned AO: no trained network (p2v_mlp_train or p2v_mlp_load first)");
         ConeParams cp{};
-        const p2v_status bs = build_cone(fr, g, dgrid, bb, n, order, cp, st);
+        const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st);
         if (bs != P2V_OK)
             return bs;
         if (cp.nlevels < 2)
             return fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
         if (mlp_level >= 0)
             cp.stencil_level = std::min(mlp_level, cp.nlevels - 2);
-        const p2v_status ps = prepare_stencil(cp, st);
+        const p2v_status ps = prepare_stencil(pp, cp, st);
         if (ps != P2V_OK)
             return ps;
         P2V_CUDA_TRY(fb_list.ensure(sizeof(uint32_t) * ((size_t) n + 1)));
@@ -734,6 +869,215 @@ p2v_status p2v_ctx::run_ao(const p2v_frame* fr, const GridGeo& g, const float* d
         return P2V_OK;
     }
     return fail(P2V_EUNSUPPORTED, "ao_mode %d is not implemented", P.ao_mode);
+}
+
+namespace {
+
+void sig_put(std::vector<uint8_t>& v, const void* p, size_t n) {
+    const uint8_t* b = static_cast<const uint8_t*>(p);
+    v.insert(v.end(), b, b + n);
+}
+
+// true when host memory p can take part in a captured graph's copies (pinned, or device / managed)
+bool graph_safe_host(const void* p) {
+    if (!p)
+        return true;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type != cudaMemoryTypeUnregistered;
+}
+
+}  // namespace
+
+// A batch: frames sorted by work (particles plus a share of the grid) and dealt, largest first, to the
+// least-loaded of L lanes; every lane queues its frames on its own stream, forked from and joined back into
+// `st`. When the batch's shape (every pointer, count, size and parameter) equals that of the previous eager
+// run, the queueing is captured as a CUDA graph (all buffers already have their sizes, so nothing is
+// allocated during capture) and later calls with the same shape replay it with a single launch.
+p2v_status p2v_ctx::run_batch(const p2v_batch_item* items, uint32_t count, p2v_stats* out, cudaStream_t st,
+                              bool allow_graph, float* ms_out) {
+    P2V_CUDA_TRY(cudaSetDevice(device));
+    if (count == 0)
+        return P2V_OK;
+    if (!items)
+        return fail(P2V_EINVAL, "no batch items");
+    int L = prm.batch_lanes > 0 ? prm.batch_lanes : (tuned_lanes > 0 ? tuned_lanes : 4);
+    L = std::max(1, std::min(L, 16));
+    L = (int) std::min<uint32_t>((uint32_t) L, count);
+    while ((int) lanes.size() < L) {
+        auto pp = std::make_unique<Pipe>();
+        if (pp->init(true) != cudaSuccess) {
+            pp->release();
+            return fail(P2V_ECUDA, "batch lane creation failed");
+        }
+        lanes.push_back(std::move(pp));
+    }
+    while ((int) b_events.size() < L + 1) {
+        cudaEvent_t e;
+        P2V_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b_events.push_back(e);
+    }
+    if (!b_t0) {
+        P2V_CUDA_TRY(cudaEventCreate(&b_t0));
+        P2V_CUDA_TRY(cudaEventCreate(&b_t1));
+    }
+    if (b_scal_cap < count) {
+        if (b_scal) {
+            P2V_CUDA_TRY(cudaStreamSynchronize(st));
+            cudaFreeHost(b_scal);
+            b_scal = nullptr;
+        }
+        P2V_CUDA_TRY(cudaMallocHost(&b_scal, sizeof(FrameScalars) * count));
+        b_scal_cap = count;
+        drop_graph();  // the graph copies into the old slots
+    }
+    // ---- schedule ----
+    std::vector<uint32_t> byw(count);
+    std::vector<double> work(count);
+    bool pinned = true;
+    for (uint32_t f = 0; f < count; ++f) {
+        const p2v_batch_item& it = items[f];
+        if (!it.frame)
+            return fail(P2V_EINVAL, "batch item %u has no frame", f);
+        uint64_t n = 0;
+        for (uint32_t l = 0; l < it.frame->list_count; ++l) {
+            const p2v_particle_list& Lst = it.frame->lists[l];
+            n += Lst.count;
+            if (Lst.mem != P2V_MEM_DEVICE)
+                pinned = pinned && graph_safe_host(Lst.vertex_data) && graph_safe_host(Lst.normals) &&
+                         graph_safe_host(Lst.ao_out);
+        }
+        const int32_t sz[3] = {it.size[0] > 0 ? it.size[0] : prm.sizex, it.size[1] > 0 ? it.size[1] : prm.sizey,
+                               it.size[2] > 0 ? it.size[2] : prm.sizez};
+        work[f] = (double) n + 0.25 * (double) sz[0] * sz[1] * sz[2];
+        if (it.volume && it.volume->data && it.volume->mem != P2V_MEM_DEVICE)
+            pinned = pinned && graph_safe_host(it.volume->data);
+        byw[f] = f;
+    }
+    std::stable_sort(byw.begin(), byw.end(), [&](uint32_t a, uint32_t b) { return work[a] > work[b]; });
+    std::vector<int> lane_of(count);
+    std::vector<double> load(L, 0.0);
+    for (uint32_t k = 0; k < count; ++k) {
+        const int l = (int) (std::min_element(load.begin(), load.end()) - load.begin());
+        lane_of[byw[k]] = l;
+        load[l] += work[byw[k]];
+    }
+    // ---- shape signature ----
+    std::vector<uint8_t> sig;
+    sig_put(sig, &prm, sizeof(prm));
+    sig_put(sig, tuned_tile, sizeof(tuned_tile));
+    sig_put(sig, &L, sizeof(L));
+    sig_put(sig, &st, sizeof(st));
+    for (uint32_t f = 0; f < count; ++f) {
+        const p2v_batch_item& it = items[f];
+        sig_put(sig, it.size, sizeof(it.size));
+        sig_put(sig, it.frame->bbox, sizeof(it.frame->bbox));
+        sig_put(sig, it.frame->clipbox, sizeof(it.frame->clipbox));
+        sig_put(sig, &it.frame->list_count, sizeof(it.frame->list_count));
+        for (uint32_t l = 0; l < it.frame->list_count; ++l)
+            sig_put(sig, &it.frame->lists[l], sizeof(p2v_particle_list));
+        const p2v_volume* v = it.volume;
+        const void* vd = v ? v->data : nullptr;
+        const int32_t vm = v ? v->mem : -1;
+        const uint64_t vc = v ? v->capacity : 0;
+        sig_put(sig, &vd, sizeof(vd));
+        sig_put(sig, &vm, sizeof(vm));
+        sig_put(sig, &vc, sizeof(vc));
+    }
+    const bool use_graph = allow_graph && prm.batch_graph != 0 && pinned;
+    const bool replay = use_graph && b_exec && sig == b_graph_sig;
+    P2V_CUDA_TRY(cudaEventRecord(b_t0, st));
+    if (replay) {
+        P2V_CUDA_TRY(cudaGraphLaunch(b_exec, st));
+    } else {
+        const bool capture = use_graph && sig == b_eager_sig;
+        if (capture) {
+            drop_graph();
+            P2V_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        }
+        b_jobs.assign(count, FrameJob{});
+        p2v_status es = P2V_OK;
+        cudaError_t ce = cudaEventRecord(b_events[L], st);
+        for (int l = 0; l < L && ce == cudaSuccess; ++l)
+            ce = cudaStreamWaitEvent(lanes[l]->stream, b_events[L], 0);
+        const p2v_params saved = prm;
+        for (uint32_t k = 0; k < count && ce == cudaSuccess && es == P2V_OK; ++k) {
+            const uint32_t f = byw[k];
+            const p2v_batch_item& it = items[f];
+            if (it.size[0] > 0)
+                prm.sizex = it.size[0];
+            if (it.size[1] > 0)
+                prm.sizey = it.size[1];
+            if (it.size[2] > 0)
+                prm.sizez = it.size[2];
+            Pipe& pp = *lanes[lane_of[f]];
+            es = enqueue_frame(pp, it.frame, it.volume, pp.stream, b_scal + f, false, b_jobs[f]);
+            prm = saved;
+        }
+        for (int l = 0; l < L && ce == cudaSuccess; ++l) {
+            ce = cudaEventRecord(b_events[l], lanes[l]->stream);
+            if (ce == cudaSuccess)
+                ce = cudaStreamWaitEvent(st, b_events[l], 0);
+        }
+        if (capture) {
+            cudaGraph_t g = nullptr;
+            const cudaError_t ee = cudaStreamEndCapture(st, &g);
+            if (es == P2V_OK && ce == cudaSuccess && ee == cudaSuccess) {
+                ce = cudaGraphInstantiate(&b_exec, g, 0);
+                if (ce == cudaSuccess) {
+                    b_graph_sig = sig;
+                    ce = cudaGraphLaunch(b_exec, st);
+                } else {
+                    b_exec = nullptr;
+                }
+            } else if (ce == cudaSuccess) {
+                ce = ee;
+            }
+            if (g)
+                cudaGraphDestroy(g);
+        } else {
+            b_eager_sig = sig;
+        }
+        if (es != P2V_OK) {
+            cudaStreamSynchronize(st);
+            return es;
+        }
+        P2V_CUDA_TRY(ce);
+        b_lane_of = lane_of;
+    }
+    P2V_CUDA_TRY(cudaEventRecord(b_t1, st));
+    P2V_CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, b_t0, b_t1);
+    if (ms_out)
+        *ms_out = ms;
+    // ---- per-frame results ----
+    p2v_status first_err = P2V_OK;
+    std::string first_msg;
+    uint64_t parts = 0;
+    for (uint32_t f = 0; f < count; ++f) {
+        p2v_stats fsx{};
+        const p2v_status fs = finish_frame(*lanes[b_lane_of[f]], b_jobs[f], items[f].volume, fsx);
+        parts += fsx.particles_in;
+        if (out)
+            out[f] = fsx;
+        if (fs != P2V_OK && first_err == P2V_OK) {
+            first_err = fs;
+            first_msg = err;
+        }
+    }
+    stats = p2v_stats{};
+    stats.particles_in = parts;
+    stats.ms_total = ms;
+    if (first_err != P2V_OK) {
+        err = first_msg;
+        return first_err;
+    }
+    err.clear();
+    return P2V_OK;
 }
 
 p2v_status p2v_ctx::mlp_alloc() {
@@ -825,6 +1169,8 @@ void p2v_params_default(p2v_params* p) {
     p->aos_step_len = 0.5f;
     p->aos_gen_fac = 1.0f;
     p->aos_eval_fac = 1.0f;
+    p->batch_lanes = 0;
+    p->batch_graph = 1;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {
@@ -844,9 +1190,7 @@ p2v_status p2v_create(p2v_ctx** out, int device) {
         return P2V_ECUDA;
     }
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
-    for (auto& e : c->ev)
-        cudaEventCreate(&e);
-    if (cudaMallocHost(&c->h_scal, sizeof(FrameScalars)) != cudaSuccess) {
+    if (c->main.init(false) != cudaSuccess) {
         p2v_destroy(c);
         return P2V_ENOMEM;
     }
@@ -860,19 +1204,22 @@ void p2v_destroy(p2v_ctx* c) {
     cudaSetDevice(c->device);
     if (c->own_stream)
         cudaStreamSynchronize(c->own_stream);
-    for (DevBuf* b : {&c->raw, &c->xyzr, &c->rec_a, &c->rec_b, &c->keys0, &c->keys1, &c->vals0, &c->vals1, &c->status,
-                      &c->hist, &c->cstart, &c->gaps, &c->grid, &c->tiles, &c->scal, &c->nrm, &c->ao, &c->mips,
-                      &c->aos_acc, &c->aos_tex, &c->mdao_acc, &c->mdao_vol, &c->mlp_P, &c->mlp_m, &c->mlp_v, &c->mlp_g, &c->mlp_part,
-                      &c->mlp_ploss, &c->mlp_loss, &c->mlp_w1h, &c->mlp_w2h, &c->mlp_lo, &c->mlp_hi, &c->mlp_idx,
-                      &c->mlp_y, &c->fb_list, &c->tX, &c->tT})
+    c->drop_graph();
+    for (auto e : c->b_events)
+        cudaEventDestroy(e);
+    if (c->b_t0)
+        cudaEventDestroy(c->b_t0);
+    if (c->b_t1)
+        cudaEventDestroy(c->b_t1);
+    if (c->b_scal)
+        cudaFreeHost(c->b_scal);
+    c->main.release();
+    for (auto& l : c->lanes)
+        l->release();
+    c->lanes.clear();
+    for (DevBuf* b : {&c->mlp_P, &c->mlp_m, &c->mlp_v, &c->mlp_g, &c->mlp_part, &c->mlp_ploss, &c->mlp_loss,
+                      &c->mlp_w1h, &c->mlp_w2h, &c->mlp_lo, &c->mlp_hi, &c->mlp_idx, &c->mlp_y, &c->tX, &c->tT})
         b->release();
-    c->stex[0].release();
-    c->stex[1].release();
-    for (auto& e : c->ev)
-        if (e)
-            cudaEventDestroy(e);
-    if (c->h_scal)
-        cudaFreeHost(c->h_scal);
     if (c->own_stream)
         cudaStreamDestroy(c->own_stream);
     delete c;
@@ -901,15 +1248,85 @@ p2v_status p2v_run_frame(p2v_ctx* c, const p2v_frame* fr, p2v_volume* vol, void*
     return c->run_frame(fr, vol, st);
 }
 
+p2v_status p2v_run_batch(p2v_ctx* c, const p2v_batch_item* items, uint32_t count, p2v_stats* stats, void* stream) {
+    if (!c || (count > 0 && !items))
+        return P2V_EINVAL;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    return c->run_batch(items, count, stats, st, true, nullptr);
+}
+
+p2v_status p2v_autotune_batch(p2v_ctx* c, const p2v_batch_item* items, uint32_t count, p2v_tune_report* rep) {
+    if (!c || count == 0 || !items)
+        return P2V_EINVAL;
+    if (rep && rep->struct_size != sizeof(p2v_tune_report))
+        return c->fail(P2V_EINVAL, "p2v_tune_report.struct_size %u != %zu", rep->struct_size, sizeof(p2v_tune_report));
+    if (c->prm.accumulate != P2V_ACCUM_EXACT)
+        return c->fail(P2V_EUNSUPPORTED, "the autotuner chooses tiles of the exact accumulation");
+    static const int tiles[][3] = {{16, 16, 16}, {16, 8, 8}, {32, 16, 8}};
+    static const int lane_opts[] = {1, 2, 4, 8};
+    const p2v_params saved = c->prm;
+    const int saved_tile[3] = {c->tuned_tile[0], c->tuned_tile[1], c->tuned_tile[2]};
+    const int saved_lanes = c->tuned_lanes;
+    float best = INFINITY;
+    int bt = -1, bl = -1, nc = 0;
+    p2v_status st = P2V_OK;
+    for (int t = 0; t < 3 && st == P2V_OK; ++t)
+        for (int l : lane_opts) {
+            c->prm.tile_x = c->prm.tile_y = c->prm.tile_z = 0;
+            c->prm.batch_lanes = l;
+            c->tuned_tile[0] = tiles[t][0];
+            c->tuned_tile[1] = tiles[t][1];
+            c->tuned_tile[2] = tiles[t][2];
+            float ms = 0.0f;
+            st = c->run_batch(items, count, nullptr, c->own_stream, false, nullptr);  // warm-up, sizes buffers
+            if (st == P2V_OK)
+                st = c->run_batch(items, count, nullptr, c->own_stream, false, &ms);
+            if (st != P2V_OK)
+                break;
+            if (rep && nc < P2V_TUNE_MAX) {
+                for (int a = 0; a < 3; ++a)
+                    rep->cand_tile[nc][a] = tiles[t][a];
+                rep->cand_lanes[nc] = l;
+                rep->cand_ms[nc] = ms;
+            }
+            ++nc;
+            if (ms < best) {
+                best = ms;
+                bt = t;
+                bl = l;
+            }
+        }
+    c->prm = saved;
+    if (st != P2V_OK || bt < 0) {
+        c->tuned_tile[0] = saved_tile[0];
+        c->tuned_tile[1] = saved_tile[1];
+        c->tuned_tile[2] = saved_tile[2];
+        c->tuned_lanes = saved_lanes;
+        return st != P2V_OK ? st : c->fail(P2V_ECUDA, "autotune measured nothing");
+    }
+    for (int a = 0; a < 3; ++a)
+        c->tuned_tile[a] = tiles[bt][a];
+    c->tuned_lanes = bl;
+    c->drop_graph();
+    if (rep) {
+        for (int a = 0; a < 3; ++a)
+            rep->tile[a] = tiles[bt][a];
+        rep->lanes = bl;
+        rep->ms_best = best;
+        rep->candidates = std::min(nc, P2V_TUNE_MAX);
+    }
+    return P2V_OK;
+}
+
 p2v_status p2v_get_device_volume(p2v_ctx* c, const float** dptr, uint64_t resolution[3]) {
     if (!c || !dptr)
         return P2V_EINVAL;
-    if (!c->last_grid)
+    if (!c->main.last_grid)
         return c->fail(P2V_EINVAL, "no volume computed yet");
-    *dptr = c->last_grid;
+    *dptr = c->main.last_grid;
     if (resolution)
         for (int a = 0; a < 3; ++a)
-            resolution[a] = c->last_res[a];
+            resolution[a] = c->main.last_res[a];
     return P2V_OK;
 }
 
@@ -917,7 +1334,7 @@ p2v_status p2v_get_ao_volume(p2v_ctx* c, int32_t level, float* out, uint64_t cap
                              int32_t dims[3]) {
     if (!c || level < 0)
         return P2V_EINVAL;
-    const ConeParams& cp = c->last_cp;
+    const ConeParams& cp = c->main.last_cp;
     if (cp.nlevels < 1 || !cp.lv[0].v)
         return c->fail(P2V_EINVAL, "no cone-march volume computed yet");
     if (level >= cp.nlevels)
@@ -1004,14 +1421,14 @@ p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, 
         return st;
     const uint32_t nvalid = (uint32_t) c->stats.particles_binned;
     const uint32_t nsel = std::min(max_pairs, nvalid);
-    if (c->last_cp.nlevels < 2)
+    if (c->main.last_cp.nlevels < 2)
         return c->fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
     // the first frame fixes the stencil levels of the training set; later frames use the same levels
     if (c->t_pairs == 0 || c->mlp_level < 0)
-        c->mlp_level = c->last_cp.stencil_level;
-    c->last_cp.stencil_level = std::min(c->mlp_level, c->last_cp.nlevels - 2);
+        c->mlp_level = c->main.last_cp.stencil_level;
+    c->main.last_cp.stencil_level = std::min(c->mlp_level, c->main.last_cp.nlevels - 2);
     if (nsel > 0) {
-        const p2v_status ps = c->prepare_stencil(c->last_cp, c->own_stream);
+        const p2v_status ps = c->prepare_stencil(c->main, c->main.last_cp, c->own_stream);
         if (ps != P2V_OK)
             return ps;
         std::vector<uint32_t> sel(nvalid);
@@ -1036,8 +1453,8 @@ p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, 
         uint32_t* d_kept = d_sel + nsel;
         cudaMemcpyAsync(d_sel, sel.data(), sizeof(uint32_t) * nsel, cudaMemcpyHostToDevice, c->own_stream);
         cudaMemsetAsync(d_kept, 0, sizeof(uint32_t), c->own_stream);
-        cudaError_t e = launch_mlp_collect(c->last_cp, c->last_order, d_sel, nsel, c->xyzr.as<float4>(),
-                                           c->nrm.as<float4>(), c->ao.as<float>(),
+        cudaError_t e = launch_mlp_collect(c->main.last_cp, c->main.last_order, d_sel, nsel, c->main.xyzr.as<float4>(),
+                                           c->main.nrm.as<float4>(), c->main.ao.as<float>(),
                                            c->tX.as<float>() + c->t_pairs * MLP_IN, c->tT.as<float>() + c->t_pairs,
                                            d_kept, c->own_stream);
         if (e != cudaSuccess)
@@ -1259,7 +1676,7 @@ p2v_status p2v_mlp_infer(p2v_ctx* c, const float* x, uint32_t n, float* y) {
     a.y = dy.as<float>();
     a.err = reinterpret_cast<uint32_t*>(dy.as<float>() + n);
     if (e == cudaSuccess)
-        e = launch_mlp_infer(a, c->last_cp, true, c->sms, nullptr);
+        e = launch_mlp_infer(a, c->main.last_cp, true, c->sms, nullptr);
     uint32_t derr = 0;
     if (e == cudaSuccess)
         e = cudaMemcpy(y, dy.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost);

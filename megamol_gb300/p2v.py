@@ -52,6 +52,7 @@ class Params(C.Structure):
         ("aos_sizex", C.c_int32), ("aos_sizey", C.c_int32), ("aos_sizez", C.c_int32),
         ("aos_step_len", C.c_float), ("aos_gen_fac", C.c_float), ("aos_eval_fac", C.c_float),
         ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("tile_z", C.c_int32),
+        ("batch_lanes", C.c_int32), ("batch_graph", C.c_int32),
     ]
 
 
@@ -64,6 +65,19 @@ class ParticleListC(C.Structure):
 class FrameC(C.Structure):
     _fields_ = [("bbox", C.c_float * 6), ("clipbox", C.c_float * 6), ("frame_id", C.c_uint32),
                 ("list_count", C.c_uint32), ("lists", C.POINTER(ParticleListC))]
+
+
+class BatchItemC(C.Structure):
+    _fields_ = [("frame", C.c_void_p), ("volume", C.c_void_p), ("size", C.c_int32 * 3)]
+
+
+TUNE_MAX = 32
+
+
+class TuneReportC(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("tile", C.c_int32 * 3), ("lanes", C.c_int32), ("ms_best", C.c_float),
+                ("candidates", C.c_int32), ("cand_tile", (C.c_int32 * 3) * TUNE_MAX),
+                ("cand_lanes", C.c_int32 * TUNE_MAX), ("cand_ms", C.c_float * TUNE_MAX)]
 
 
 class VolumeC(C.Structure):
@@ -105,6 +119,8 @@ _SIGNATURES = {
     "p2v_get_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
     "p2v_run_frame": ([C.c_void_p, C.POINTER(FrameC), C.POINTER(VolumeC), C.c_void_p], C.c_int),
     "p2v_get_device_volume": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)], C.c_int),
+    "p2v_run_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p], C.c_int),
+    "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
                           C.c_int),
     "p2v_get_stats": ([C.c_void_p, C.POINTER(StatsC)], C.c_int),
@@ -315,6 +331,50 @@ class Context:
         return dict(resolution=list(vol.resolution), components=int(vol.components),
                     slice_dists=list(vol.slice_dists), origin=list(vol.origin), extents=list(vol.extents),
                     min_value=vol.min_value, max_value=vol.max_value, bbox=list(vol.bbox), data_hash=vol.data_hash)
+
+    # ---- batches ----
+    def _batch(self, frames):
+        """frames: sequence of dicts with keys lists, bbox, and optionally out, size, clipbox. Returns the
+        ctypes objects (kept alive by the caller) and the item array."""
+        keep, vols = [], []
+        items = (BatchItemC * max(1, len(frames)))()
+        for i, f in enumerate(frames):
+            fr, arr = self._frame(f["lists"], f["bbox"], f.get("clipbox"), i)
+            vol = VolumeC()
+            out = f.get("out")
+            if out is not None:
+                op, omem = _ptr(out)
+                vol.data = op
+                vol.mem = omem
+                vol.capacity = int(out.size if isinstance(out, np.ndarray) else out.numel())
+            keep += [fr, arr, vol]
+            vols.append(vol)
+            size = f.get("size", (0, 0, 0))
+            items[i] = BatchItemC(C.cast(C.pointer(fr), C.c_void_p), C.cast(C.pointer(vol), C.c_void_p),
+                                  (C.c_int32 * 3)(*[int(v) for v in size]))
+        return keep, vols, items
+
+    def run_batch(self, frames, stream: int = 0):
+        """Run a batch of frames (see _batch); returns per-frame metadata dicts and per-frame stats."""
+        keep, vols, items = self._batch(frames)
+        st = (StatsC * max(1, len(frames)))()
+        self._check(self.lib.p2v_run_batch(self.h, C.cast(items, C.c_void_p), len(frames), C.cast(st, C.c_void_p),
+                                           C.c_void_p(stream)))
+        meta = [dict(resolution=list(v.resolution), min_value=v.min_value, max_value=v.max_value,
+                     slice_dists=list(v.slice_dists), origin=list(v.origin), data_hash=v.data_hash) for v in vols]
+        stats = [{k: (list(getattr(x, k)) if k in ("cell_min", "cell_max") else getattr(x, k))
+                  for k, _ in x._fields_} for x in st[:len(frames)]]
+        return meta, stats
+
+    def autotune_batch(self, frames) -> dict:
+        keep, vols, items = self._batch(frames)
+        rep = TuneReportC()
+        rep.struct_size = C.sizeof(TuneReportC)
+        self._check(self.lib.p2v_autotune_batch(self.h, C.cast(items, C.c_void_p), len(frames), C.byref(rep)))
+        n = rep.candidates
+        return dict(tile=list(rep.tile), lanes=rep.lanes, ms_best=rep.ms_best,
+                    candidates=[dict(tile=list(rep.cand_tile[k]), lanes=rep.cand_lanes[k], ms=rep.cand_ms[k])
+                                for k in range(n)])
 
     def stats(self) -> dict:
         s = StatsC()

@@ -11,8 +11,11 @@
 int main(void) {
     printf("{");
     S(p2v_params); S(p2v_particle_list); S(p2v_frame); S(p2v_volume); S(p2v_stats);
+    S(p2v_batch_item); S(p2v_tune_report);
     F(p2v_params, sigma); F(p2v_params, kernel); F(p2v_params, ao_mode); F(p2v_params, aos_eval_fac);
-    F(p2v_params, tile_z);
+    F(p2v_params, tile_z); F(p2v_params, batch_graph);
+    F(p2v_batch_item, volume); F(p2v_batch_item, size);
+    F(p2v_tune_report, ms_best); F(p2v_tune_report, cand_lanes); F(p2v_tune_report, cand_ms);
     F(p2v_particle_list, count); F(p2v_particle_list, mem); F(p2v_particle_list, ao_out);
     F(p2v_frame, frame_id); F(p2v_frame, lists);
     F(p2v_volume, resolution); F(p2v_volume, min_value); F(p2v_volume, data_hash);
