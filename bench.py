@@ -407,10 +407,119 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batch_bench(args):
+    """Batched-trajectory workload: 64 frames of 1-8 Gaussian blobs, particle counts log-uniform in
+    [50k, 2M], grids 64^3-256^3 matched to extent, density + plain cone AO (8 cones x 32 steps, 3 levels,
+    gradient normals). One step = the whole batch through p2v_run_batch (one CUDA-graph launch); the
+    autotuner picks the density tile and the lane count first. Also reported: the same frames one
+    p2v_run_frame call after another, and the batch without its graph."""
+    import torch
+
+    from megamol_gb300 import p2v, synth
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.cuda.current_device()
+    traj = synth.trajectory(frames=64, seed=3 + 1000 * rank)
+    ctx = p2v.Context(dev)
+    # setup (untimed): gradient normals from each frame's own density
+    frames_dev, frames_host, total = [], [], 0
+    for f in traj:
+        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1)
+        vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
+        ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
+        nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
+        V = f.res[0] * f.res[1] * f.res[2]
+        d_in = torch.from_numpy(f.xyzr).to(dev)
+        d_n = torch.from_numpy(nrm).to(dev)
+        d_ao = torch.empty(f.n, dtype=torch.float32, device=dev)
+        d_out = torch.empty(V, dtype=torch.float32, device=dev)
+        frames_dev.append(dict(lists=[p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=d_n,
+                                                       ao_out=d_ao)], bbox=f.bbox, out=d_out, size=f.res))
+        h_in = torch.from_numpy(f.xyzr).pin_memory()
+        h_n = torch.from_numpy(nrm).pin_memory()
+        h_ao = torch.empty(f.n, dtype=torch.float32).pin_memory()
+        h_out = torch.empty(V, dtype=torch.float32).pin_memory()
+        frames_host.append(dict(lists=[p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=h_n,
+                                                        ao_out=h_ao)], bbox=f.bbox, out=h_out, size=f.res))
+        total += f.n
+    ctx.set_params(normalize=1, batch_graph=1, tile_x=0, tile_y=0, tile_z=0, batch_lanes=0, **AO_PARAMS)
+    tune = ctx.autotune_batch(frames_dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(frames, steps, warmup, graph=True):
+        ctx.set_params(batch_graph=1 if graph else 0)
+        for _ in range(warmup):
+            ctx.run_batch(frames)
+        barrier()
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(steps):
+            ctx.run_batch(frames)
+            t.append(ctx.stats()["ms_total"])
+        torch.cuda.synchronize()
+        barrier()
+        return sum(t) / len(t)
+
+    sampler = ClockSampler(dev)
+    sampler.__enter__()
+    ms = timed(frames_dev, args.steps, max(args.warmup, 3))
+    sampler.__exit__()
+    ms_eager = timed(frames_dev, max(3, args.steps // 4), 2, graph=False)
+    ms_e2e = timed(frames_host, max(3, args.steps // 2), 3)
+    # the same frames one p2v_run_frame after another (stream-synchronous per frame)
+    seq = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for fd in frames_dev:
+            ctx.set_params(sizex=fd["size"][0], sizey=fd["size"][1], sizez=fd["size"][2])
+            ctx.run_frame(fd["lists"], fd["bbox"], fd["out"])
+        torch.cuda.synchronize()
+        seq.append((time.perf_counter() - t0) * 1e3)
+    ms_seq = min(seq)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms, ms_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, ms_e2e = float(t[0]), float(t[1])
+    h2d = sum(f.n * (16 + 12) for f in traj)
+    d2h = sum(f.n * 4 + f.res[0] * f.res[1] * f.res[2] * 4 for f in traj)
+    if rank == 0:
+        line = {"metric": "particles/s density+AO (batched trajectory)", "value": ws * total / (ms * 1e-3),
+                "unit": "particles/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "trajectory_64", "frames": len(traj), "particles": total,
+                           "particles_per_frame": "log-uniform [50k, 2M]", "grids": sorted({f.res[0] for f in traj}),
+                           "ao": "plain cone march, 8 cones x 32 steps, 3-level mip, gradient normals",
+                           "l2": "per-step working set several GB > 126 MB L2 (no flush)"},
+                "batch": {"autotuned_tile": tune["tile"], "autotuned_lanes": tune["lanes"],
+                          "ms_graph": ms, "ms_eager": ms_eager, "ms_frame_by_frame": ms_seq,
+                          "speedup_vs_frame_by_frame": ms_seq / ms},
+                "e2e": {"value": ws * total / (ms_e2e * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
+                "gpu_launches": None, "clocks": sampler.summary()}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "trajectory_64":
+        run_batch_bench(args)
     else:
         run_ours(args)
 
