@@ -355,7 +355,7 @@ def run_ours(args):
         lv_bytes += d[0] * d[1] * d[2] * 4
         d = [max(1, x // 2) for x in d]
     ao_bytes = f.n * (16 + 12 + 4) + lv_bytes
-    ao_name = "p2v::mlp_infer_kernel (+ mip levels, fallback cone march)" if use_learned else \
+    ao_name = "p2v::mlp_infer_tc_kernel (+ mip levels, stencil textures, fallback cone march)" if use_learned else \
         "p2v::cone_ao_kernel (+ mip levels)"
     if st["ms_ao"] >= st["ms_density"]:
         dom = (ao_name, ao_bytes, st["ms_ao"], "learned_ao_lj_liquid_4M.md" if use_learned else "cone_ao_lj_liquid_4M.md")
@@ -379,9 +379,13 @@ def run_ours(args):
                "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on {AO_SAMPLE} "
                          f"particles scaled to the frame ({dt_ao:.2f} s)"}
 
-    passes = 4
-    launches_density = 2 + 2 + passes + 3 + 1 + 2
-    launches_ao = (AO_PARAMS["ao_levels"] - 1) + (2 if use_learned else 1)
+    # kernels per frame: scalar init, pack, digit histogram + scan, the radix passes (9/8-bit digits over the
+    # bin keys), cell starts (3), gather, finalize + normalise; AO: normals, mips, then the cone march or
+    # stencil textures (2) + tensor-core inference + fallback cone march
+    key_bits = int(nb).bit_length()
+    passes = (key_bits + 8) // 9
+    launches_density = 1 + 1 + 2 + passes + 3 + 1 + 2
+    launches_ao = 1 + (AO_PARAMS["ao_levels"] - 1) + (4 if use_learned else 1)
     if rank == 0:
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,

@@ -230,6 +230,16 @@ P2V_API p2v_status p2v_get_device_volume(p2v_ctx* ctx, const float** dptr, uint6
 P2V_API p2v_status p2v_get_ao_volume(p2v_ctx* ctx, int32_t level, float* out, uint64_t capacity, int32_t mem,
                                      int32_t dims[3]);
 
+/* The binning of the last p2v_run_frame (replaces ParticlesToDensity.cpp:561-568, which computes each
+ * particle's cell on the fly): the bin keys in sorted order, the stable sort permutation (sorted position ->
+ * particle index over the concatenated lists) and the first sorted position of every bin (nbins + 1
+ * entries). A bin is the particle's floor cell per axis clamped to [-1, size] (one underflow and one
+ * overflow bin per axis), key = (bz * (sy + 2) + by) * (sx + 2) + bx with b = cell + 1; particles with
+ * non-finite coordinates or radius <= 0 carry key nbins and sort last. Any output pointer may be NULL;
+ * count and nbins (nullable) receive the sizes. Synchronises the device. */
+P2V_API p2v_status p2v_get_binning(p2v_ctx* ctx, uint32_t* keys, uint32_t* order, uint64_t capacity,
+                                   uint32_t* cell_start, uint64_t start_capacity, uint32_t* count, uint32_t* nbins);
+
 P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
 /* Last error message of this context ("" if none); returns the message length. */
 P2V_API size_t p2v_get_last_error(const p2v_ctx* ctx, char* buf, size_t len);

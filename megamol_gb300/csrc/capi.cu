@@ -72,6 +72,8 @@ struct Pipe {
     ConeParams last_cp{};
     const float* last_grid = nullptr;
     const uint32_t* last_order = nullptr;  // sorted position -> particle index of the last frame
+    const uint32_t* last_keys = nullptr;   // sorted bin keys of the last frame
+    uint32_t last_n = 0, last_nbins = 0;
     uint64_t last_res[3] = {0, 0, 0};
 
     cudaError_t init(bool with_stream) {
@@ -116,6 +118,8 @@ struct FrameJob {
     float bb[6] = {};
     const float* dgrid = nullptr;
     const uint32_t* order = nullptr;
+    const uint32_t* keys = nullptr;
+    uint32_t nbins = 0;
     FrameScalars* h_out = nullptr;  // pinned slot that receives the frame's scalars
     bool timed = false;             // stage events were recorded
 };
@@ -561,6 +565,8 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     std::memcpy(job.bb, bb, sizeof(bb));
     job.dgrid = dgrid;
     job.order = sb.vals[sb.result];
+    job.keys = skeys;
+    job.nbins = g.nbins;
     job.h_out = h_out;
     job.timed = timed;
     return P2V_OK;
@@ -579,6 +585,9 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
     const FrameScalars& hs = *job.h_out;
     last_grid = dgrid;
     last_order = job.order;
+    pp.last_keys = job.keys;
+    pp.last_n = (uint32_t) job.N;
+    pp.last_nbins = job.nbins;
     for (int a = 0; a < 3; ++a)
         last_res[a] = (uint64_t) res[a];
     stats = p2v_stats{};
@@ -1359,6 +1368,37 @@ p2v_status p2v_get_ao_volume(p2v_ctx* c, int32_t level, float* out, uint64_t cap
                        mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
     if (e != cudaSuccess)
         return c->fail(P2V_ECUDA, "AO volume copy failed: %s", cudaGetErrorString(e));
+    return P2V_OK;
+}
+
+p2v_status p2v_get_binning(p2v_ctx* c, uint32_t* keys, uint32_t* order, uint64_t capacity, uint32_t* cell_start,
+                           uint64_t start_capacity, uint32_t* count, uint32_t* nbins) {
+    if (!c)
+        return P2V_EINVAL;
+    const Pipe& pp = c->main;
+    if (!pp.last_keys)
+        return c->fail(P2V_EINVAL, "no frame binned yet");
+    if (count)
+        *count = pp.last_n;
+    if (nbins)
+        *nbins = pp.last_nbins;
+    if ((keys || order) && capacity < pp.last_n)
+        return c->fail(P2V_EINVAL, "capacity %llu < %u particles", (unsigned long long) capacity, pp.last_n);
+    if (cell_start && start_capacity < (uint64_t) pp.last_nbins + 1)
+        return c->fail(P2V_EINVAL, "start capacity %llu < %u bins + 1", (unsigned long long) start_capacity,
+                       pp.last_nbins);
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && keys && pp.last_n)
+        e = cudaMemcpy(keys, pp.last_keys, sizeof(uint32_t) * pp.last_n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && order && pp.last_n)
+        e = cudaMemcpy(order, pp.last_order, sizeof(uint32_t) * pp.last_n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && cell_start)
+        e = cudaMemcpy(cell_start, pp.cstart.ptr, sizeof(uint32_t) * ((size_t) pp.last_nbins + 1),
+                       cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "binning copy failed: %s", cudaGetErrorString(e));
     return P2V_OK;
 }
 

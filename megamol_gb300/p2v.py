@@ -123,6 +123,8 @@ _SIGNATURES = {
     "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
                           C.c_int),
+    "p2v_get_binning": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
+                         C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)], C.c_int),
     "p2v_get_stats": ([C.c_void_p, C.POINTER(StatsC)], C.c_int),
     "p2v_get_last_error": ([C.c_void_p, C.c_char_p, C.c_size_t], C.c_size_t),
     "p2v_train_params_default": ([C.POINTER(TrainParams)], None),
@@ -386,6 +388,17 @@ class Context:
         res = (C.c_uint64 * 3)()
         self._check(self.lib.p2v_get_device_volume(self.h, C.byref(p), res))
         return p.value, list(res)
+
+    def binning(self):
+        """(sorted keys, sort permutation, cell starts) of the last frame, as host arrays."""
+        n, nb = C.c_uint32(), C.c_uint32()
+        self._check(self.lib.p2v_get_binning(self.h, None, None, 0, None, 0, C.byref(n), C.byref(nb)))
+        keys = np.empty(n.value, np.uint32)
+        order = np.empty(n.value, np.uint32)
+        start = np.empty(nb.value + 1, np.uint32)
+        self._check(self.lib.p2v_get_binning(self.h, keys.ctypes.data, order.ctypes.data, keys.size,
+                                             start.ctypes.data, start.size, None, None))
+        return keys, order, start
 
     def ao_volume(self, level: int = 0) -> np.ndarray:
         """Level `level` of the last cone-march pyramid as a (z, y, x) float32 host array."""

@@ -325,6 +325,40 @@ MLP_IN, MLP_HIDDEN = 131, 64
 MLP_NPARAM = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
 
 
+def bin_keys(xyzr, bbox, res) -> tuple[np.ndarray, int]:
+    """Bin key of every particle (numpy restatement in FP32, the reference's cell expression of
+    ParticlesToDensity.cpp:561-568: cell = (p - min) / h with h = |max - min| / (res - 1) in float). The bin is
+    floor(cell) clamped to [-1, res] per axis (one underflow and one overflow bin), key =
+    (bz * (sy + 2) + by) * (sx + 2) + bx with b = bin + 1; particles with non-finite coordinates or radius,
+    radius <= 0 or a cell beyond 2^30 get key nbins. Returns (keys, nbins)."""
+    x = np.asarray(xyzr, np.float32).reshape(-1, 4)
+    nb = [int(r) + 2 for r in res]
+    nbins = nb[0] * nb[1] * nb[2]
+    valid = np.isfinite(x).all(1) & (x[:, 3] > 0)
+    b = []
+    with np.errstate(invalid="ignore", over="ignore"):
+        for a in range(3):
+            lo, hi = np.float32(bbox[a]), np.float32(bbox[a + 3])
+            h = np.float32(abs(hi - lo)) / np.float32(res[a] - 1)
+            q = (x[:, a] - lo) / h
+            valid &= np.abs(q) < np.float32(2.0 ** 30)
+            c = np.floor(np.where(np.isfinite(q), q, 0.0)).astype(np.int64)
+            b.append(np.clip(c, -1, int(res[a])) + 1)
+    keys = (b[2] * nb[1] + b[1]) * nb[0] + b[0]
+    keys = np.where(valid, keys, nbins).astype(np.uint32)
+    return keys, nbins
+
+
+def binning(xyzr, bbox, res):
+    """Stable sort of the bin keys (np.argsort kind="stable"): (sorted keys, permutation, cell starts of the
+    nbins + 1 bins)."""
+    keys, nbins = bin_keys(xyzr, bbox, res)
+    order = np.argsort(keys, kind="stable").astype(np.uint32)
+    sk = keys[order]
+    start = np.searchsorted(sk, np.arange(nbins + 1, dtype=np.int64), side="left").astype(np.uint32)
+    return sk, order, start
+
+
 def mdao_dims(clip, vol_size: int):
     """MDAO volume size for a clip box: (dims (x, y, z), shortest edge, max lod)."""
     c = (C.c_float * 6)(*[float(v) for v in clip])

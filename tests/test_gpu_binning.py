@@ -1,0 +1,72 @@
+"""GPU test of the cell binning: the radix sort of the bin keys must equal a CPU stable sort bit for bit
+(sorted keys, permutation and cell starts), for ordinary, ragged, out-of-box, invalid and crowded inputs
+and at the full LJ-liquid size (4,000,000 particles, 256^3 grid, 25-bit keys, three digit passes)."""
+import numpy as np
+import pytest
+
+import oracle
+from megamol_gb300 import build as nbuild
+from megamol_gb300 import p2v, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    nbuild.build()
+    c = p2v.Context(0)
+    yield c
+    c.close()
+
+
+def check(ctx, xyzr, bbox, res, lists=None):
+    ctx.set_params(sizex=res[0], sizey=res[1], sizez=res[2], ao_mode=p2v.AO_NONE, normalize=0,
+                   forSurfaceReconstruction=0)
+    ctx.run_frame(lists or [p2v.ParticleList(xyzr, p2v.VERTDATA_FLOAT_XYZR)], bbox, None)
+    keys, order, start = ctx.binning()
+    rk, ro, rs = oracle.binning(xyzr, bbox, res)
+    assert np.array_equal(keys, rk)
+    assert np.array_equal(order, ro)
+    assert np.array_equal(start, rs)
+
+
+def test_uniform_frame(ctx):
+    f = synth.uniform(n=200_000, edge=50.0, res=64, seed=3)
+    check(ctx, f.xyzr, f.bbox, f.res)
+
+
+def test_out_of_box_invalid_and_crowded(ctx):
+    rng = np.random.default_rng(4)
+    n = 150_000
+    x = np.empty((n, 4), np.float32)
+    x[:, :3] = rng.uniform(-20, 60, (n, 3))       # a third outside the box: underflow / overflow bins
+    x[:, 3] = rng.uniform(0.2, 1.0, n)
+    x[::11, :3] = np.float32(17.25)                # one crowded cell (~14k particles)
+    x[5::97, 3] = 0.0                              # invalid radius
+    x[7::101, 1] = np.nan                          # invalid coordinate
+    check(ctx, x, (0.0, 0.0, 0.0, 40.0, 40.0, 40.0), (48, 40, 56))
+
+
+def test_ragged_sizes(ctx):
+    rng = np.random.default_rng(5)
+    for n in (1, 31, 4095, 4096, 4097, 70_001):
+        x = np.concatenate([rng.uniform(0, 10, (n, 3)), np.full((n, 1), 0.5)], 1).astype(np.float32)
+        check(ctx, x, (0, 0, 0, 10, 10, 10), (20, 20, 20))
+
+
+def test_mixed_list_types(ctx):
+    rng = np.random.default_rng(6)
+    a = rng.uniform(0, 30, (5000, 3)).astype(np.float64)
+    b = rng.integers(0, 30, (3000, 3)).astype(np.uint16)
+    c = np.concatenate([rng.uniform(0, 30, (4000, 3)), np.full((4000, 1), 0.7)], 1).astype(np.float32)
+    lists = [p2v.ParticleList(a, p2v.VERTDATA_DOUBLE_XYZ, global_radius=0.5),
+             p2v.ParticleList(b, p2v.VERTDATA_SHORT_XYZ, global_radius=0.6),
+             p2v.ParticleList(c, p2v.VERTDATA_FLOAT_XYZR)]
+    packed = np.concatenate([np.column_stack([a.astype(np.float32), np.full(len(a), 0.5, np.float32)]),
+                             np.column_stack([b.astype(np.float32), np.full(len(b), 0.6, np.float32)]), c])
+    check(ctx, packed, (0, 0, 0, 30, 30, 30), (33, 30, 31), lists=lists)
+
+
+def test_lj_liquid_full_size(ctx):
+    f = synth.lj_liquid(seed=2)
+    check(ctx, f.xyzr, f.bbox, f.res)
