@@ -40,10 +40,10 @@ struct AOSphereParams {
     float origin[3], ext[3], sampd[3];  // posOrigin, posExtents, aoSampDist
 };
 
-// MDAO occupancy volume geometry (uniforms of mdao_volume.geom/frag.glsl, MDAOVolumeGenerator.cpp:141-165)
+// MDAO occupancy volume geometry (uniforms of mdao_volume.geom/frag.glsl, MDAOVolumeGenerator.cpp:139-164)
 struct MdaoParams {
     float bmin[3], inv[3], fd[3], cell[3];  // inBoundsMin, inBoundsSizeInverse, inVolumeSize, cellSize
-    float cell_vol, ps_scale, sphere_k;     // cell volume, point-size scale (geom:43), 4/3 * 3.14152
+    float cell_vol, ps_scale, sphere_k;     // cell volume, point-size scale (mdao_volume.geom.glsl:28), 4/3 * 3.14152
     float half_vp[2];                       // half the slice viewport
     int d[3];
     int unorm8;                             // 1 = R8 texel values k/255, 0 = unquantised fractions

@@ -31,7 +31,7 @@ __device__ __forceinline__ float dot3_rn(float x, float y, float z) {
     return __fadd_rn(__fadd_rn(sq_rn(x), sq_rn(y)), sq_rn(z));
 }
 
-// mdao_volume.frag.glsl:17-76 for voxel (i, j, layer) and a sphere with centre c relative to inBoundsMin and
+// mdao_volume.frag.glsl:9-76 for voxel (i, j, layer) and a sphere with centre c relative to inBoundsMin and
 // squared radius w2. Returns -1 for a discarded fragment.
 __device__ float mdao_fragment(const MdaoParams& mp, int i, int j, int layer, float cx, float cy, float cz,
                                float w2) {
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) mdao_voxelise_kernel(const MdaoParams mp,
     for (uint32_t k = warp; k < n; k += nwarps) {
         const float4 p = __ldg(xyzr + (order ? __ldg(order + k) : k));
         const float r = p.w;
-        // mdao_volume.geom.glsl:87-107; every lane evaluates the same sphere, so branches are warp-uniform
+        // mdao_volume.geom.glsl:72-92; every lane evaluates the same sphere, so branches are warp-uniform
         const float npx = __fmul_rn(__fsub_rn(p.x, mp.bmin[0]), mp.inv[0]);
         const float npy = __fmul_rn(__fsub_rn(p.y, mp.bmin[1]), mp.inv[1]);
         const float npz = __fmul_rn(__fsub_rn(p.z, mp.bmin[2]), mp.inv[2]);

@@ -614,16 +614,16 @@ MdaoGeo mdao_geo(const float clip[6], const int32_t dims[3]) {
     MdaoGeo g{};
     for (int a = 0; a < 3; ++a) {
         const float size = clip[a + 3] > clip[a] ? clip[a + 3] - clip[a] : clip[a] - clip[a + 3];
-        g.bmin[a] = clip[a];             // StartInsertion: inBoundsMin (MDAOVolumeGenerator.cpp:147-148)
-        g.inv[a] = 1.0f / size;          // inBoundsSizeInverse (:141-144)
+        g.bmin[a] = clip[a];             // StartInsertion: inBoundsMin (MDAOVolumeGenerator.cpp:145-146)
+        g.inv[a] = 1.0f / size;          // inBoundsSizeInverse (:139-143)
         g.fd[a] = static_cast<float>(dims[a]);
         g.d[a] = dims[a];
-        g.cell[a] = 1.0f / (g.fd[a] * g.inv[a]);  // frag:20
+        g.cell[a] = 1.0f / (g.fd[a] * g.inv[a]);  // mdao_volume.frag.glsl:12
     }
-    g.cell_vol = (g.cell[0] * g.cell[1]) * g.cell[2];                                 // frag:58
-    g.ps_scale = std::max(g.inv[0] * g.fd[0], g.inv[1] * g.fd[1]);                    // geom:43
-    g.sphere_k = 4.0f / 3.0f * 3.14152f;                                              // frag:57 (sic)
-    g.half_vp[0] = 0.5f * g.fd[0];  // viewport = one slice (MDAOVolumeGenerator.cpp:165)
+    g.cell_vol = (g.cell[0] * g.cell[1]) * g.cell[2];                                 // frag:50
+    g.ps_scale = std::max(g.inv[0] * g.fd[0], g.inv[1] * g.fd[1]);                    // mdao_volume.geom.glsl:28
+    g.sphere_k = 4.0f / 3.0f * 3.14152f;                                              // frag:49 (sic)
+    g.half_vp[0] = 0.5f * g.fd[0];  // viewport = one slice (MDAOVolumeGenerator.cpp:164)
     g.half_vp[1] = 0.5f * g.fd[1];
     return g;
 }
@@ -632,7 +632,7 @@ inline float mdao_dot(const float* v) {
     return (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
 }
 
-// mdao_volume.frag.glsl:17-76 for voxel (i, j, layer) and a sphere with centre c (relative to inBoundsMin)
+// mdao_volume.frag.glsl:9-76 for voxel (i, j, layer) and a sphere with centre c (relative to inBoundsMin)
 // and squared radius w2; -1 = discarded fragment.
 float mdao_fragment(const MdaoGeo& g, int i, int j, int layer, const float c[3], float w2) {
     const float cm[3] = {static_cast<float>(i) * g.cell[0], static_cast<float>(j) * g.cell[1],
@@ -691,17 +691,17 @@ extern "C" void p2vo_mdao_volume_f32(const float* xyzr, int64_t n, const float c
         float np[3], c[3];
         bool inside = true;
         for (int a = 0; a < 3; ++a) {
-            np[a] = (p[a] - g.bmin[a]) * g.inv[a];  // geom:87
-            const float ndc = np[a] * 2.0f - 1.0f;  // geom:94; a point is clipped by its centre vertex
+            np[a] = (p[a] - g.bmin[a]) * g.inv[a];  // geom:72
+            const float ndc = np[a] * 2.0f - 1.0f;  // geom:79; a point is clipped by its centre vertex
             inside = inside && (ndc >= -1.0f && ndc <= 1.0f);
-            c[a] = p[a] - g.bmin[a];                // geom:45
+            c[a] = p[a] - g.bmin[a];                // geom:30
         }
         if (!inside)
             continue;
         const float w2 = r * r;
         const float xw = (np[0] * 2.0f - 1.0f) * g.half_vp[0] + g.half_vp[0];  // viewport transform
         const float yw = (np[1] * 2.0f - 1.0f) * g.half_vp[1] + g.half_vp[1];
-        auto emit = [&](int layer, float disk) {  // geom:39-49 + rasterisation of the point
+        auto emit = [&](int layer, float disk) {  // geom:24-34 + rasterisation of the point
             if (layer < 0 || layer >= g.d[2])
                 return;
             // gl_PointSize = int(2 ceil(disk * scale)), at least one pixel; sizes beyond 2^22 pixels cover
@@ -723,7 +723,7 @@ extern "C" void p2vo_mdao_volume_f32(const float* xyzr, int64_t n, const float c
                     acc[(size_t) v] += q;
                 }
         };
-        // geom:91-107
+        // geom:76-92
         // slices beyond the volume's depth emit layers outside it: cap the count there
         const int numSlices =
             static_cast<int>(std::min(std::ceil(r * g.inv[2] * g.fd[2]), static_cast<float>(g.d[2] + 1)));
@@ -732,7 +732,7 @@ extern "C" void p2vo_mdao_volume_f32(const float* xyzr, int64_t n, const float c
         emit(centerLayer, r);
         const float sliceThickness = 1.0f / g.fd[2];
         const float zOffset = (zs - std::floor(zs)) / g.fd[2];
-        for (int side = 0; side < 2; ++side) {  // geom:54-72, negative then positive hemisphere
+        for (int side = 0; side < 2; ++side) {  // geom:39-57, negative then positive hemisphere
             const int step = side == 0 ? -1 : 1;
             const float offset = side == 0 ? zOffset : sliceThickness - zOffset;
             for (int i = 1; i <= numSlices; ++i) {
