@@ -55,10 +55,34 @@ def make_workload(name: str, rank: int = 0):
                     jitter=0.08, radii="U[0.4,0.6]", kernel="bump sigma=1 (reference rbf)", cyclic=True)
         return f, desc
     if name == "uniform_100k":
+        # the small plain-method case: Gaussian sigma = radius cut at 3 sigma
         f = synth.uniform(n=100_000, seed=1 + rank)
-        desc = dict(workload="uniform_100k", particles=f.n, grid=list(f.res), radius=0.5, kernel="bump sigma=1")
+        desc = dict(workload="uniform_100k", particles=f.n, grid=list(f.res), radius=0.5,
+                    kernel="gauss3 sigma=r (cut at 3 sigma)", cyclic=True)
+        return f, desc
+    if name == "uniform_16M":
+        # the learned-AO inference set: 16M particles of the small case's structure, box scaled to keep the
+        # number density and the voxel size
+        n = 16_000_000
+        scale = (n / 100_000) ** (1.0 / 3.0)
+        f = synth.uniform(n=n, edge=100.0 * scale, res=int(round(128 * scale)), seed=1 + rank)
+        desc = dict(workload="uniform_16M", particles=f.n, grid=list(f.res), radius=0.5,
+                    kernel="bump sigma=1 (reference rbf)", cyclic=True)
+        return f, desc
+    if name == "mixed_phase_64M":
+        f = synth.mixed_phase(seed=5 + rank)
+        desc = dict(workload="mixed_phase_64M", particles=f.n, grid=list(f.res),
+                    phases="FCC slab (a=1.12, jitter 0.05) + uniform gas at 1/20 density",
+                    radii="0.5/0.8/1.2 in 6:3:1", kernel="bump sigma=1 (reference rbf)", cyclic=True)
         return f, desc
     raise SystemExit(f"unknown workload {name}")
+
+
+def density_params(desc: dict) -> dict:
+    from megamol_gb300 import p2v
+
+    gauss = desc["kernel"].startswith("gauss3")
+    return dict(kernel=p2v.KERNEL_GAUSS3 if gauss else p2v.KERNEL_BUMP, sigma=1.0)
 
 
 class ClockSampler:
@@ -133,12 +157,13 @@ AO_PARAMS = dict(ao_mode=1, ao_volume=0, ao_volume_scale=1.0, ao_cones=8, ao_ste
 AO_SAMPLE = 50_000  # particles in the CPU AO sample
 
 
-def setup_frame(ctx, f):
+def setup_frame(ctx, f, dparams=None):
     """Density once (untimed) to derive the workload's normals: unit vectors down the density gradient."""
     from megamol_gb300 import p2v, synth
 
-    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], cyclX=1, cyclY=1, cyclZ=1, normalize=1, sigma=1.0,
-                   kernel=p2v.KERNEL_BUMP, ao_mode=p2v.AO_NONE)
+    dp = dparams or dict(kernel=p2v.KERNEL_BUMP, sigma=1.0)
+    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], cyclX=1, cyclY=1, cyclZ=1, normalize=1,
+                   ao_mode=p2v.AO_NONE, **dp)
     V = f.res[0] * f.res[1] * f.res[2]
     vol = np.empty(V, np.float32)
     ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
@@ -147,20 +172,21 @@ def setup_frame(ctx, f):
     return vol.reshape(f.res[2], f.res[1], f.res[0]), nrm
 
 
-def cpu_reference_density(f, nthreads: int):
+def cpu_reference_density(f, nthreads: int, kernel: int = 0):
     """Time the reference's CPU density (the compiled ParticlesToDensity module when present, else the
-    FP32 restatement with the same OpenMP structure) on one frame; returns (seconds, kind, grid)."""
+    FP32 restatement with the same OpenMP structure) on one frame; returns (seconds, kind, grid). The
+    reference has only its bump rbf: the 3-sigma Gaussian is timed with the restatement."""
     import oracle
 
     os.environ["OMP_NUM_THREADS"] = str(nthreads)
-    if oracle.reference_available():
+    if oracle.reference_available() and kernel == oracle.BUMP:
         xyzr = np.ascontiguousarray(f.xyzr)
         L = [dict(type=2, data=xyzr, stride=0, radius=0.0, count=f.n)]
         t0 = time.perf_counter()
         vol, _ = oracle.reference_density(L, f.bbox, f.res, (1, 1, 1), True, 1.0)
         return time.perf_counter() - t0, "reference", vol
     t0 = time.perf_counter()
-    vol = oracle.density_f32(f.xyzr, f.bbox, f.res, (1, 1, 1), 1.0, oracle.BUMP, nthreads)
+    vol = oracle.density_f32(f.xyzr, f.bbox, f.res, (1, 1, 1), 1.0, kernel, nthreads)
     vol, _, _ = oracle.normalize_minmax_f32(vol)
     return time.perf_counter() - t0, "port", vol
 
@@ -184,12 +210,12 @@ def cpu_cone_ao(f, grid, nrm, sample: int):
     return time.perf_counter() - t0
 
 
-def cpu_pipeline(f, nthreads, grid=None, nrm=None):
+def cpu_pipeline(f, nthreads, grid=None, nrm=None, kernel: int = 0):
     """CPU particles/s of density + plain cone AO: the density stage on the full frame, the AO stage on a
     sample of AO_SAMPLE particles scaled to the frame."""
     from megamol_gb300 import synth
 
-    dt_d, kind, vol = cpu_reference_density(f, nthreads)
+    dt_d, kind, vol = cpu_reference_density(f, nthreads, kernel)
     if nrm is None:
         nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
     dt_ao = cpu_cone_ao(f, vol, nrm, AO_SAMPLE) * (f.n / AO_SAMPLE)
@@ -200,18 +226,23 @@ def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
         return
+    if args.workload == "trajectory_64":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm times single frames; "
+                          "run it on the default workload"}), flush=True)
+        return
     f, desc = make_workload(args.workload)
+    kern = density_params(desc)["kernel"]
     nthreads = os.cpu_count() or 1
     from megamol_gb300 import synth
 
-    _, _, vol = cpu_reference_density(f, nthreads)
+    _, _, vol = cpu_reference_density(f, nthreads, kern)
     nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
     for _ in range(max(0, args.warmup)):
-        cpu_pipeline(f, nthreads, nrm=nrm)
+        cpu_pipeline(f, nthreads, nrm=nrm, kernel=kern)
     vals, kind = [], "port"
     tot = 0.0
     for _ in range(args.steps):
-        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm)
+        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm, kernel=kern)
         vals.append(v)
         tot += dt_d + dt_ao
     value = f.n * args.steps / tot
@@ -226,17 +257,24 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def train_learned_ao(ctx, f_main):
-    """Train the learned AO on cone-march pairs of other frames: LJ-liquid frames (seeds 3 and 4,
-    500,000 pairs each) and ten uniform 100k-particle frames of the small plain-method workload."""
+def train_learned_ao(ctx, f_main, dparams=None, workload: str = "lj_liquid_4M"):
+    """Train the learned AO on cone-march pairs of other frames. LJ liquid: two other LJ frames (seeds 3
+    and 4, 500,000 pairs each) and ten uniform 100k-particle frames of the small plain-method workload.
+    Other workloads: other seeds of the same workload (the cone length is a fraction of the volume, so the
+    network must see the box geometry it infers on): two frames of 1,000,000 pairs, one for the 64M frame."""
     from megamol_gb300 import p2v, synth
 
     ctx.mlp_clear()
     total = 0
-    frames = [(synth.lj_liquid(seed=s), 500_000) for s in (3, 4)]
-    frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000) for k in range(10)]
+    if workload == "lj_liquid_4M":
+        frames = [(synth.lj_liquid(seed=s), 500_000) for s in (3, 4)]
+        frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000) for k in range(10)]
+    else:
+        kk = (100,) if workload == "mixed_phase_64M" else (100, 101)
+        frames = [(make_workload(workload, rank=k)[0], 1_000_000) for k in kk]
     for k, (f, npairs) in enumerate(frames):
-        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1)
+        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1,
+                       **(dparams or {}))
         vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
         ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
         nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
@@ -290,8 +328,9 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     f, desc = make_workload(args.workload, rank)
     ctx = p2v.Context(dev)
-    pairs, train_rep = train_learned_ao(ctx, f)
-    grid0, nrm = setup_frame(ctx, f)
+    dparams = density_params(desc)
+    pairs, train_rep = train_learned_ao(ctx, f, dparams, args.workload)
+    grid0, nrm = setup_frame(ctx, f, dparams)
     V = f.res[0] * f.res[1] * f.res[2]
     stream = torch.cuda.Stream()
     d_in = torch.from_numpy(f.xyzr).to(dev)
@@ -374,7 +413,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1:
         nthreads = os.cpu_count() or 1
-        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm)
+        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm, kernel=dparams["kernel"])
         cpu = {"value": v, "unit": "particles/s", "cores": nthreads, "kind": kind,
                "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on {AO_SAMPLE} "
                          f"particles scaled to the frame ({dt_ao:.2f} s)"}
@@ -433,7 +472,8 @@ def run_batch_bench(args):
     # setup (untimed): gradient normals from each frame's own density
     frames_dev, frames_host, total = [], [], 0
     for f in traj:
-        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1)
+        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1,
+                       **(dparams or {}))
         vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
         ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
         nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
