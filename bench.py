@@ -191,6 +191,10 @@ def cpu_reference_density(f, nthreads: int, kernel: int = 0):
     return time.perf_counter() - t0, "port", vol
 
 
+def ao_sample(f) -> int:
+    return AO_SAMPLE if f.res[0] * f.res[1] * f.res[2] <= 256 ** 3 else AO_SAMPLE // 10
+
+
 def cpu_cone_ao(f, grid, nrm, sample: int):
     """Time the CPU cone march (restatement of the MDAO shader, OpenMP) on `sample` particles; returns
     seconds for the sample."""
@@ -212,13 +216,15 @@ def cpu_cone_ao(f, grid, nrm, sample: int):
 
 def cpu_pipeline(f, nthreads, grid=None, nrm=None, kernel: int = 0):
     """CPU particles/s of density + plain cone AO: the density stage on the full frame, the AO stage on a
-    sample of AO_SAMPLE particles scaled to the frame."""
+    sample of particles scaled to the frame (AO_SAMPLE, a tenth of that above 256^3 voxels, so the CPU leg
+    stays within about half a minute)."""
     from megamol_gb300 import synth
 
     dt_d, kind, vol = cpu_reference_density(f, nthreads, kernel)
     if nrm is None:
         nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
-    dt_ao = cpu_cone_ao(f, vol, nrm, AO_SAMPLE) * (f.n / AO_SAMPLE)
+    sample = ao_sample(f)
+    dt_ao = cpu_cone_ao(f, vol, nrm, sample) * (f.n / sample)
     return f.n / (dt_d + dt_ao), kind, dt_d, dt_ao
 
 
@@ -251,7 +257,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference", "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip"),
             "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": kind,
-                             "sample": f"density on the full frame ({f.n} particles) + cone AO on {AO_SAMPLE} "
+                             "sample": f"density on the full frame ({f.n} particles) + cone AO on {ao_sample(f)} "
                                        "particles scaled to the frame, per step"},
             "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -269,6 +275,8 @@ def train_learned_ao(ctx, f_main, dparams=None, workload: str = "lj_liquid_4M"):
     if workload == "lj_liquid_4M":
         frames = [(synth.lj_liquid(seed=s), 500_000) for s in (3, 4)]
         frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000) for k in range(10)]
+    elif workload == "uniform_100k":
+        frames = [(make_workload(workload, rank=100 + k)[0], 100_000) for k in range(12)]
     else:
         kk = (100,) if workload == "mixed_phase_64M" else (100, 101)
         frames = [(make_workload(workload, rank=k)[0], 1_000_000) for k in kk]
@@ -415,8 +423,8 @@ def run_ours(args):
         nthreads = os.cpu_count() or 1
         v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm, kernel=dparams["kernel"])
         cpu = {"value": v, "unit": "particles/s", "cores": nthreads, "kind": kind,
-               "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on {AO_SAMPLE} "
-                         f"particles scaled to the frame ({dt_ao:.2f} s)"}
+               "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on "
+                         f"{ao_sample(f)} particles scaled to the frame ({dt_ao:.2f} s)"}
 
     # kernels per frame: scalar init, pack, digit histogram + scan, the radix passes (9/8-bit digits over the
     # bin keys), cell starts (3), gather, finalize + normalise; AO: normals, mips, then the cone march or

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 2
+#define P2V_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -86,16 +86,34 @@ typedef enum p2v_ao_volume {
     P2V_AOVOL_MDAO = 1     /* MDAO occupancy voxelisation (mdao_volume.geom/frag.glsl) */
 } p2v_ao_volume;
 
+/* Colour data types, values of SimpleSphericalParticles::ColourDataType (SimpleSphericalParticles.h:41-50). */
+typedef enum p2v_colour_type {
+    P2V_COLDATA_NONE = 0,        /* global colour */
+    P2V_COLDATA_UINT8_RGB = 1,
+    P2V_COLDATA_UINT8_RGBA = 2,
+    P2V_COLDATA_FLOAT_RGB = 3,
+    P2V_COLDATA_FLOAT_RGBA = 4,
+    P2V_COLDATA_FLOAT_I = 5,
+    P2V_COLDATA_USHORT_RGBA = 6,
+    P2V_COLDATA_DOUBLE_I = 7
+} p2v_colour_type;
+
 typedef struct p2v_particle_list {
     int32_t vertex_type;        /* p2v_vertex_type */
     uint32_t vertex_stride;     /* bytes between records, 0 = packed */
     const void* vertex_data;
     uint64_t count;
     float global_radius;
-    int32_t mem;                /* p2v_mem of vertex_data, normals and ao_out */
-    const float* normals;       /* optional: per-particle normal (DIRDATA_FLOAT_XYZ layout); AO modes need it */
+    int32_t mem;                /* p2v_mem of vertex_data, normals, colour_data and ao_out */
+    const float* normals;       /* optional: per-particle direction (DIRDATA_FLOAT_XYZ layout): the AO modes'
+                                   normals, the vector aggregator's directions */
     uint32_t normal_stride;     /* bytes, 0 = packed (12) */
     float* ao_out;              /* optional: per-particle AO (COLDATA_FLOAT_I), count floats */
+    int32_t colour_type;        /* p2v_colour_type of colour_data (the intensity aggregator reads its first
+                                   channel, as SimpleSphericalParticles' GetCRAcc) */
+    uint32_t colour_stride;     /* bytes, 0 = packed */
+    const void* colour_data;
+    uint8_t global_colour[4];   /* RGBA for P2V_COLDATA_NONE (channel value / 255 as the intensity) */
 } p2v_particle_list;
 
 typedef struct p2v_frame {
@@ -278,6 +296,42 @@ typedef struct p2v_tune_report {
  * the fastest for later calls whose tile_x / batch_lanes are 0. rep (nullable) receives the table. */
 P2V_API p2v_status p2v_autotune_batch(p2v_ctx* ctx, const p2v_batch_item* items, uint32_t count,
                                       p2v_tune_report* rep);
+
+/* ---- MMPLD files ----
+ * The reader of MegaMol's particle list files (plugins/moldyn/src/io/MMPLDDataSource.cpp:50-220, header
+ * :335-420): versions 1.0-1.3, a frame table of file offsets, per frame a timestamp (1.2+) and lists of
+ * interleaved vertex + colour records with a global radius / colour, an intensity range and (1.3) a per-list
+ * box. Frames are read with positional reads, so several threads may read different frames of one open
+ * file at once. The caller provides the frame buffer (host memory; a pinned buffer from p2v_host_alloc lets
+ * p2v_run_frame upload it asynchronously); the lists point into it. */
+typedef struct p2v_mmpld p2v_mmpld;
+
+typedef struct p2v_mmpld_info {
+    uint32_t version;   /* 100..103 */
+    uint32_t frames;
+    float bbox[6];
+    float clipbox[6];
+} p2v_mmpld_info;
+
+typedef struct p2v_mmpld_list_info {
+    float intensity_range[2];  /* colour map index values (FLOAT_I / DOUBLE_I lists; else 0, 1) */
+    float bbox[6];             /* the list's box (version 1.3), else the file's */
+    uint32_t clusters;         /* version 1.1 cluster count (the cluster data are skipped) */
+} p2v_mmpld_list_info;
+
+P2V_API p2v_status p2v_mmpld_open(const char* path, p2v_mmpld** file, p2v_mmpld_info* info);
+P2V_API void p2v_mmpld_close(p2v_mmpld* file);
+/* Bytes of frame `frame` (the buffer p2v_mmpld_read_frame needs). */
+P2V_API p2v_status p2v_mmpld_frame_size(p2v_mmpld* file, uint32_t frame, uint64_t* bytes);
+/* Read frame `frame` into buffer and describe its lists: at most max_lists entries of lists (mem = host,
+ * pointers into buffer) and list_info (nullable); *nlists receives the frame's list count, *timestamp (nullable)
+ * its time (the frame index before version 1.2). Lists without vertex data keep P2V_VERTDATA_NONE. */
+P2V_API p2v_status p2v_mmpld_read_frame(p2v_mmpld* file, uint32_t frame, void* buffer, uint64_t capacity,
+                                        p2v_particle_list* lists, p2v_mmpld_list_info* list_info, uint32_t max_lists,
+                                        uint32_t* nlists, float* timestamp);
+/* Pinned host memory for frame buffers (cudaMallocHost / cudaFreeHost). */
+P2V_API void* p2v_host_alloc(uint64_t bytes);
+P2V_API void p2v_host_free(void* ptr);
 
 /* ---- learned AO ---- */
 P2V_API void p2v_train_params_default(p2v_train_params* tp);

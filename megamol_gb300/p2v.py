@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(HERE, "_lib", "libp2v.so")
 # enums of include/p2v.h
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EDOMAIN, EUNSUPPORTED = range(7)
 VERTDATA_NONE, VERTDATA_FLOAT_XYZ, VERTDATA_FLOAT_XYZR, VERTDATA_SHORT_XYZ, VERTDATA_DOUBLE_XYZ = range(5)
+(COLDATA_NONE, COLDATA_UINT8_RGB, COLDATA_UINT8_RGBA, COLDATA_FLOAT_RGB, COLDATA_FLOAT_RGBA, COLDATA_FLOAT_I,
+ COLDATA_USHORT_RGBA, COLDATA_DOUBLE_I) = range(8)
 MEM_HOST, MEM_DEVICE = 0, 1
 KERNEL_BUMP, KERNEL_GAUSS3 = 0, 1
 ACCUM_EXACT, ACCUM_KAHAN = 0, 1
@@ -59,7 +61,18 @@ class Params(C.Structure):
 class ParticleListC(C.Structure):
     _fields_ = [("vertex_type", C.c_int32), ("vertex_stride", C.c_uint32), ("vertex_data", C.c_void_p),
                 ("count", C.c_uint64), ("global_radius", C.c_float), ("mem", C.c_int32),
-                ("normals", C.c_void_p), ("normal_stride", C.c_uint32), ("ao_out", C.c_void_p)]
+                ("normals", C.c_void_p), ("normal_stride", C.c_uint32), ("ao_out", C.c_void_p),
+                ("colour_type", C.c_int32), ("colour_stride", C.c_uint32), ("colour_data", C.c_void_p),
+                ("global_colour", C.c_uint8 * 4)]
+
+
+class MmpldInfoC(C.Structure):
+    _fields_ = [("version", C.c_uint32), ("frames", C.c_uint32), ("bbox", C.c_float * 6),
+                ("clipbox", C.c_float * 6)]
+
+
+class MmpldListInfoC(C.Structure):
+    _fields_ = [("intensity_range", C.c_float * 2), ("bbox", C.c_float * 6), ("clusters", C.c_uint32)]
 
 
 class FrameC(C.Structure):
@@ -119,6 +132,13 @@ _SIGNATURES = {
     "p2v_get_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
     "p2v_run_frame": ([C.c_void_p, C.POINTER(FrameC), C.POINTER(VolumeC), C.c_void_p], C.c_int),
     "p2v_get_device_volume": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64)], C.c_int),
+    "p2v_mmpld_open": ([C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(MmpldInfoC)], C.c_int),
+    "p2v_mmpld_close": ([C.c_void_p], None),
+    "p2v_mmpld_frame_size": ([C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)], C.c_int),
+    "p2v_mmpld_read_frame": ([C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32,
+                              C.POINTER(C.c_uint32), C.POINTER(C.c_float)], C.c_int),
+    "p2v_host_alloc": ([C.c_uint64], C.c_void_p),
+    "p2v_host_free": ([C.c_void_p], None),
     "p2v_run_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p], C.c_int),
     "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
@@ -168,9 +188,11 @@ def default_params() -> Params:
 
 
 def _ptr(x) -> tuple[int, int]:
-    """(address, mem kind) of a numpy array or a CUDA torch tensor."""
+    """(address, mem kind) of a numpy array, a CUDA torch tensor or a raw host address."""
     if x is None:
         return 0, MEM_HOST
+    if isinstance(x, int):
+        return x, MEM_HOST
     if isinstance(x, np.ndarray):
         return x.ctypes.data, MEM_HOST
     if hasattr(x, "data_ptr"):
@@ -189,6 +211,19 @@ class ParticleList:
     normals: Any = None
     normal_stride: int = 0
     ao_out: Any = None
+    colour: Any = None            # colour data of colour_type (SimpleSphericalParticles colour layouts)
+    colour_type: int = 0          # COLDATA_*
+    colour_stride: int = 0
+    global_colour: tuple = (255, 255, 255, 255)
+
+    def to_c(self) -> "ParticleListC":
+        dp, mem = _ptr(self.data)
+        npp, _ = _ptr(self.normals)
+        ap, _ = _ptr(self.ao_out)
+        cp, _ = _ptr(self.colour)
+        return ParticleListC(int(self.vertex_type), int(self.stride), dp, self.n(), float(self.global_radius), mem,
+                             npp or None, int(self.normal_stride), ap or None, int(self.colour_type),
+                             int(self.colour_stride), cp or None, (C.c_uint8 * 4)(*self.global_colour))
 
     def n(self) -> int:
         if self.count is not None:
@@ -197,6 +232,60 @@ class ParticleList:
         if isinstance(self.data, np.ndarray) and self.stride == 0:
             return self.data.size // comps
         return int(self.data.shape[0])
+
+
+class Mmpld:
+    """An MMPLD file read through libp2v (p2v_mmpld_*): header info and frames as ParticleLists that point
+    into a frame buffer (pinned host memory when `pinned`)."""
+
+    def __init__(self, path: str):
+        self.lib = library()
+        h = C.c_void_p()
+        info = MmpldInfoC()
+        st = self.lib.p2v_mmpld_open(str(path).encode(), C.byref(h), C.byref(info))
+        if st != OK:
+            raise P2VError(st, f"cannot open MMPLD file {path}")
+        self.h = h
+        self.version, self.frames = info.version, info.frames
+        self.bbox, self.clipbox = list(info.bbox), list(info.clipbox)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.p2v_mmpld_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def frame_size(self, frame: int) -> int:
+        b = C.c_uint64()
+        st = self.lib.p2v_mmpld_frame_size(self.h, int(frame), C.byref(b))
+        if st != OK:
+            raise P2VError(st, f"frame {frame}")
+        return b.value
+
+    def read(self, frame: int, max_lists: int = 64):
+        """(lists, list infos, timestamp, buffer): the ParticleLists reference `buffer` (keep it alive)."""
+        size = self.frame_size(frame)
+        buf = np.empty(max(size, 1), np.uint8)
+        lists = (ParticleListC * max_lists)()
+        infos = (MmpldListInfoC * max_lists)()
+        n = C.c_uint32()
+        ts = C.c_float()
+        st = self.lib.p2v_mmpld_read_frame(self.h, int(frame), buf.ctypes.data, buf.size, C.cast(lists, C.c_void_p),
+                                           C.cast(infos, C.c_void_p), max_lists, C.byref(n), C.byref(ts))
+        if st != OK:
+            raise P2VError(st, f"cannot read frame {frame}")
+        out = []
+        for k in range(min(n.value, max_lists)):
+            L = lists[k]
+            out.append(ParticleList(data=int(L.vertex_data or 0), vertex_type=L.vertex_type, count=L.count,
+                                    stride=L.vertex_stride, global_radius=L.global_radius,
+                                    colour=int(L.colour_data or 0) or None, colour_type=L.colour_type,
+                                    colour_stride=L.colour_stride, global_colour=tuple(L.global_colour)))
+        inf = [dict(intensity_range=list(infos[k].intensity_range), bbox=list(infos[k].bbox),
+                    clusters=infos[k].clusters) for k in range(min(n.value, max_lists))]
+        return out, inf, ts.value, buf
 
 
 class Context:
@@ -243,11 +332,7 @@ class Context:
     def _frame(self, lists, bbox, clipbox=None, frame_id=0):
         arr = (ParticleListC * max(1, len(lists)))()
         for i, L in enumerate(lists):
-            dp, mem = _ptr(L.data)
-            npp, _ = _ptr(L.normals)
-            ap, _ = _ptr(L.ao_out)
-            arr[i] = ParticleListC(int(L.vertex_type), int(L.stride), dp, L.n(), float(L.global_radius), mem,
-                                   npp or None, int(L.normal_stride), ap or None)
+            arr[i] = L.to_c()
         fr = FrameC()
         fr.bbox[:] = [float(v) for v in bbox]
         fr.clipbox[:] = [float(v) for v in (clipbox if clipbox is not None else bbox)]
@@ -312,11 +397,7 @@ class Context:
         """Run one frame. `out` is a host numpy float32 array or a CUDA float32 tensor (or None)."""
         arr = (ParticleListC * max(1, len(lists)))()
         for i, L in enumerate(lists):
-            dp, mem = _ptr(L.data)
-            npp, _ = _ptr(L.normals)
-            ap, _ = _ptr(L.ao_out)
-            arr[i] = ParticleListC(int(L.vertex_type), int(L.stride), dp, L.n(), float(L.global_radius), mem,
-                                   npp or None, int(L.normal_stride), ap or None)
+            arr[i] = L.to_c()
         fr = FrameC()
         fr.bbox[:] = [float(v) for v in bbox]
         fr.clipbox[:] = [float(v) for v in (clipbox if clipbox is not None else bbox)]
