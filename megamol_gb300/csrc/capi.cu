@@ -64,7 +64,7 @@ enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_C
 // p2v_run_batch; frames on different pipes may run concurrently.
 struct Pipe {
     DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
-    DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list;
+    DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list, wts, wsorted, wsum;
     StencilTex stex[2];                    // the learned AO's two stencil levels as textures
     cudaEvent_t ev[EV_COUNT] = {};
     FrameScalars* h_scal = nullptr;        // pinned mirror of the last frame's scalars
@@ -93,7 +93,8 @@ struct Pipe {
         if (stream)
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &rec_b, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
-                          &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list})
+                          &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
+                          &wts, &wsorted, &wsum})
             b->release();
         stex[0].release();
         stex[1].release();
@@ -120,6 +121,7 @@ struct FrameJob {
     const uint32_t* order = nullptr;
     const uint32_t* keys = nullptr;
     uint32_t nbins = 0;
+    int components = 1;
     FrameScalars* h_out = nullptr;  // pinned slot that receives the frame's scalars
     bool timed = false;             // stage events were recorded
 };
@@ -130,6 +132,7 @@ __global__ void init_scalars_kernel(FrameScalars* fs) {
         z.cmin[a] = INT32_MAX;
         z.cmax[a] = INT32_MIN;
     }
+    z.dmin_bits = 0x7f7fffffu;  // FLT_MAX, as the vector aggregator's minDens starts
     *fs = z;
 }
 
@@ -275,6 +278,20 @@ int cone_steps(float offset, float cone_length, int steps, float w, float shorte
     return n;
 }
 
+// bytes of one colour record (SimpleSphericalParticles.h:124-175); 0 = no per-particle colour
+uint32_t colour_bytes(int type) {
+    switch (type) {
+    case P2V_COLDATA_UINT8_RGB: return 3;
+    case P2V_COLDATA_UINT8_RGBA: return 4;
+    case P2V_COLDATA_FLOAT_RGB: return 12;
+    case P2V_COLDATA_FLOAT_RGBA: return 16;
+    case P2V_COLDATA_FLOAT_I: return 4;
+    case P2V_COLDATA_USHORT_RGBA: return 8;
+    case P2V_COLDATA_DOUBLE_I: return 8;
+    default: return 0;
+    }
+}
+
 uint32_t record_bytes(int type) {
     switch (type) {
     case P2V_VERTDATA_FLOAT_XYZ: return 12;
@@ -307,8 +324,19 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
            &ao = pp.ao;
     cudaEvent_t* ev = pp.ev;
     const p2v_params& P = prm;
-    if (P.aggregator != 0)
-        return fail(P2V_EUNSUPPORTED, "aggregator %d is not implemented (only PosToSingleCell_Volume)", P.aggregator);
+    // aggregator: 0 PosToSingleCell_Volume, 1 IColToSingleCell_Volume, 2 IVecToSingleCell_Volume
+    // (ParticlesToDensity.cpp:78-81)
+    if (P.aggregator < 0 || P.aggregator > 2)
+        return fail(P2V_EINVAL, "aggregator %d is not 0, 1 or 2", P.aggregator);
+    const int agg = P.aggregator;
+    const int wnc = agg == 1 ? 1 : (agg == 2 ? 3 : 0);      // weights per particle
+    const int comps = agg == 2 ? 3 : 1;                       // volume components
+    if (agg != 0 && P.accumulate != P2V_ACCUM_EXACT)
+        return fail(P2V_EUNSUPPORTED, "aggregator %d needs the exact accumulation", agg);
+    if (agg != 0 && P.mass_normalize)
+        return fail(P2V_EINVAL, "mass normalisation applies to the density aggregator only");
+    if (agg == 2 && P.ao_mode != P2V_AO_NONE && P.ao_volume == P2V_AOVOL_DENSITY)
+        return fail(P2V_EUNSUPPORTED, "the cone-march AO of a density volume needs a scalar grid (aggregator 0/1)");
     if (!(P.sigma > 0.0f) || !std::isfinite(P.sigma))
         return fail(P2V_EINVAL, "sigma must be a positive finite number");
     if (P.kernel != P2V_KERNEL_BUMP && P.kernel != P2V_KERNEL_GAUSS3)
@@ -352,6 +380,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     g.sigma = P.sigma;
     g.kernel = P.kernel;
     const uint64_t V = (uint64_t) res[0] * res[1] * res[2];
+    const uint64_t VC = V * (uint64_t) comps;
 
     uint64_t N = 0;
     for (uint32_t l = 0; l < fr->list_count; ++l) {
@@ -397,16 +426,22 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     P2V_CUDA_TRY(tiles.ensure(sizeof(TileStats) * ntiles));
     P2V_CUDA_TRY(scal.ensure(sizeof(FrameScalars)));
     float* dgrid;
-    const bool direct = vol && vol->data && vol->mem == P2V_MEM_DEVICE && vol->capacity >= V;
+    const bool direct = vol && vol->data && vol->mem == P2V_MEM_DEVICE && vol->capacity >= VC;
     if (direct) {
         dgrid = vol->data;
     } else {
-        P2V_CUDA_TRY(grid.ensure(sizeof(float) * V));
+        P2V_CUDA_TRY(grid.ensure(sizeof(float) * VC));
         dgrid = grid.as<float>();
     }
-    if (vol && vol->data && vol->capacity < V)
+    if (vol && vol->data && vol->capacity < VC)
         return fail(P2V_EINVAL, "output capacity %llu < %llu floats", (unsigned long long) vol->capacity,
-                    (unsigned long long) V);
+                    (unsigned long long) VC);
+    if (wnc) {
+        P2V_CUDA_TRY(pp.wts.ensure(sizeof(float) * wnc * (N + 1)));
+        P2V_CUDA_TRY(pp.wsorted.ensure(sizeof(float) * wnc * (N + 1)));
+        if (agg == 2)
+            P2V_CUDA_TRY(pp.wsum.ensure(sizeof(float) * V));
+    }
 
     FrameScalars* fs = scal.as<FrameScalars>();
     if (timed)
@@ -421,9 +456,13 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
             continue;
         const uint32_t stride = L.vertex_stride ? L.vertex_stride : record_bytes(L.vertex_type);
         raw_need += (L.count - 1) * (uint64_t) stride + record_bytes(L.vertex_type) + 16;
-        if (P.ao_mode != P2V_AO_NONE && L.normals != nullptr) {
+        if ((P.ao_mode != P2V_AO_NONE || agg == 2) && L.normals != nullptr) {
             const uint32_t ns = L.normal_stride ? L.normal_stride : 12u;
-            raw_need += (L.count - 1) * (uint64_t) ns + 12 + 16;
+            raw_need += 2 * ((L.count - 1) * (uint64_t) ns + 12 + 16);
+        }
+        if (agg == 1 && L.colour_data != nullptr && colour_bytes(L.colour_type) > 0) {
+            const uint32_t cs = L.colour_stride ? L.colour_stride : colour_bytes(L.colour_type);
+            raw_need += (L.count - 1) * (uint64_t) cs + colour_bytes(L.colour_type) + 16;
         }
     }
     if (raw_need)
@@ -496,6 +535,44 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         }
     }
 
+    // ---- weights of the intensity / vector aggregators ----
+    if (wnc) {
+        uint64_t woff = 0;
+        for (uint32_t l = 0; l < fr->list_count; ++l) {
+            const p2v_particle_list& L = fr->lists[l];
+            if (L.vertex_type == P2V_VERTDATA_NONE)
+                continue;
+            if (L.count > 0) {
+                WeightSource ws{};
+                ws.count = L.count;
+                ws.offset = woff;
+                const void* src = agg == 1 ? L.colour_data : static_cast<const void*>(L.normals);
+                uint32_t rb = agg == 1 ? colour_bytes(L.colour_type) : 12u;
+                uint32_t stride = agg == 1 ? (L.colour_stride ? L.colour_stride : rb) : (L.normal_stride ? L.normal_stride : 12u);
+                if (agg == 2 && src == nullptr)
+                    return fail(P2V_EINVAL, "list %u: the vector aggregator needs directions (normals)", l);
+                if (agg == 1 && (src == nullptr || rb == 0)) {
+                    src = nullptr;  // the global colour's red channel, normalised (Accessor_Val<uchar, true>)
+                    ws.global_i = static_cast<float>(L.global_colour[0]) / static_cast<float>(255);
+                }
+                if (src != nullptr && L.mem != P2V_MEM_DEVICE) {
+                    const uint64_t bytes = (L.count - 1) * (uint64_t) stride + rb;
+                    uint8_t* dst = raw.as<uint8_t>() + raw_off;
+                    if (raw_off + bytes > raw.bytes)
+                        return fail(P2V_EINVAL, "list %u: weight data larger than the staging buffer", l);
+                    P2V_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+                    src = dst;
+                    raw_off += (bytes + 15) & ~uint64_t(15);
+                }
+                ws.data = static_cast<const uint8_t*>(src);
+                ws.stride = stride;
+                ws.ctype = L.colour_type;
+                P2V_CUDA_TRY(launch_pack_weights(ws, wnc, pp.wts.as<float>(), fs, sms, st));
+            }
+            woff += L.count;
+        }
+    }
+
     // ---- sort + cell starts ----
     SortBuffers sb{};
     sb.keys[0] = keys0.as<uint32_t>();
@@ -516,19 +593,48 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
 
     // ---- density ----
+    if (wnc)
+        P2V_CUDA_TRY(launch_permute_weights(sb.vals[sb.result], pp.wts.as<float>(), pp.wsorted.as<float>(), n, wnc, sms,
+                                            st));
     {
-        const cudaError_t ge = launch_gather(gc, g, rec_a.as<float4>(), rec_b.as<int4>(), cstart.as<uint32_t>(), dgrid,
-                                             tiles.as<TileStats>(), fs, st);
-        if (ge == cudaErrorInvalidValue)
-            return fail(P2V_EUNSUPPORTED, "density tile %dx%dx%d is not compiled for accumulate=%d", gc.tx, gc.ty,
-                        gc.tz, P.accumulate);
-        P2V_CUDA_TRY(ge);
+        // aggregator 0: the density; 1: the intensity-weighted sums; 2: three direction-weighted passes into
+        // the interleaved vector volume and the plain kernel sums (the weights) into wsum
+        const int passes = agg == 2 ? 4 : 1;
+        for (int pass = 0; pass < passes; ++pass) {
+            GatherWeights gw{};
+            float* out = dgrid;
+            if (agg == 1) {
+                gw.mode = GatherWeights::FIXED;
+                gw.w = pp.wsorted.as<float>();
+            } else if (agg == 2 && pass < 3) {
+                gw.mode = GatherWeights::DOUBLE;
+                gw.w = pp.wsorted.as<float>() + pass;
+                gw.wstride = 3;
+                gw.ostride = 3;
+                out = dgrid + pass;
+            } else if (agg == 2) {
+                gw.mode = GatherWeights::DOUBLE;  // the weights: plain kernel sums in FP64
+                out = pp.wsum.as<float>();
+            }
+            const cudaError_t ge = launch_gather(gc, g, rec_a.as<float4>(), rec_b.as<int4>(), cstart.as<uint32_t>(),
+                                                 out, tiles.as<TileStats>(), fs, st, gw);
+            if (ge == cudaErrorInvalidValue)
+                return fail(P2V_EUNSUPPORTED, "density tile %dx%dx%d is not compiled for accumulate=%d", gc.tx, gc.ty,
+                            gc.tz, P.accumulate);
+            P2V_CUDA_TRY(ge);
+        }
     }
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_DENSITY], st));
     const double voxel_volume = (double) g.hhi[0] * g.hhi[1] * g.hhi[2];
-    P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume, st));
-    P2V_CUDA_TRY(launch_normalize_modes(dgrid, V, fs, P.mass_normalize, P.normalize, sms, st));
+    if (agg == 2) {
+        P2V_CUDA_TRY(launch_vector_finish(dgrid, pp.wsum.as<float>(), (int64_t) V, fs, P.normalize, sms, st));
+        P2V_CUDA_TRY(launch_normalize_modes(dgrid, VC, fs, 0, P.normalize, sms, st));
+    } else {
+        P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume,
+                                     st));
+        P2V_CUDA_TRY(launch_normalize_modes(dgrid, V, fs, P.mass_normalize, P.normalize, sms, st));
+    }
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_NORM], st));
     if (want_ao) {
@@ -541,7 +647,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
 
     // ---- outputs ----
     if (vol && vol->data && !direct)
-        P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * V,
+        P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * VC,
                                      vol->mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
     if (want_ao) {
         uint64_t aoff = 0;
@@ -567,6 +673,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     job.order = sb.vals[sb.result];
     job.keys = skeys;
     job.nbins = g.nbins;
+    job.components = comps;
     job.h_out = h_out;
     job.timed = timed;
     return P2V_OK;
@@ -629,7 +736,7 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
             vol->origin[a] = bb[a];
         }
         std::memcpy(vol->bbox, bb, sizeof(float) * 6);
-        vol->components = 1;
+        vol->components = (uint64_t) job.components;
         vol->min_value = hs.out_min;
         vol->max_value = hs.out_max;
         vol->data_hash = ++datahash;

@@ -403,8 +403,9 @@ struct WarpPart {
     float iby;         // 1/by for decoding a box-local row index
     int bx, by;        // box extents in x and y
     int node0;         // tile index of the box corner
+    float w;           // the particle's weight (the weighted aggregators)
 };
-constexpr int WP_FIELDS = 9;
+constexpr int WP_FIELDS = 10;
 
 // Fixed-point scale of the exact accumulation: contributions (all below 1) are rounded to multiples of
 // 2^-32 and summed as 64-bit integers held in two 32-bit words per node (a 32-bit shared-memory atomic on
@@ -417,14 +418,31 @@ constexpr float FIX_INV = 2.3283064365386963e-10f;  // 2^-32
 // nodes held as 64-bit fixed-point sums in shared memory; for every cyclic image of the tile it walks
 // the sorted particle records of the surrounding cell rows (coalesced 16-byte loads), and each thread
 // adds its particle's kernel values to the nodes of the particle's footprint that lie in the tile.
-template<int TX, int TY, int TZ, int NT>
+//
+// ACC selects the accumulation:
+//   ACC_EXACT   the density: contributions < 1 in 2^-32 fixed point (see above);
+//   ACC_FIXED_W the intensity aggregator (ParticlesToDensity.cpp:509-519): contribution = kernel value times
+//               the particle's weight w (wts[j * wstride], sorted order), rounded to a multiple of 1 / wscale
+//               with wscale = 2^31 / 2^ceil(log2 max|w|) and summed as a signed 64-bit integer (exact, order
+//               independent; absolute resolution 2^-31 of the largest weight);
+//   ACC_DOUBLE  the vector aggregator's direction and weight sums (:492-508): FP64 shared-memory atomics of
+//               the FP32 contributions. Its finish divides two sums, so small sums need relative accuracy
+//               (a fixed-point quantum would erase voxels reached only by kernel tails); the sums depend on
+//               the arrival order only at the 1e-16 level, below the final rounding to FP32.
+// The result is written with stride ostride.
+constexpr int ACC_EXACT = 0, ACC_FIXED_W = 1, ACC_DOUBLE = 2;
+template<int TX, int TY, int TZ, int NT, int ACC>
 __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, const float4* __restrict__ rec_a,
     const int4* __restrict__ rec_b, const uint32_t* __restrict__ start, float* __restrict__ grid,
-    TileStats* __restrict__ tiles, FrameScalars* __restrict__ fs, int rmax) {
+    TileStats* __restrict__ tiles, FrameScalars* __restrict__ fs, int rmax, const float* __restrict__ wts,
+    int wstride, int ostride) {
     constexpr int NN = TX * TY * TZ;
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* acc_lo = reinterpret_cast<uint32_t*>(smem);  // [NN] low words of the fixed-point sums
     uint32_t* acc_hi = acc_lo + NN;                        // [NN] high words
+    unsigned long long* acc64 = reinterpret_cast<unsigned long long*>(smem);  // [NN] ACC_FIXED_W sums (same bytes)
+    double* accd = reinterpret_cast<double*>(smem);                          // [NN] ACC_DOUBLE sums (same bytes)
+    constexpr bool WEIGHTED = ACC != ACC_EXACT;
     uint32_t* row_beg = acc_hi + NN;                        // [rmax]
     uint32_t* row_off = row_beg + rmax;                                      // [rmax + 1]
     __shared__ double s_dsum[NT / 32];
@@ -445,6 +463,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     }
     const bool bump = g.kernel == 0;
     const float E45 = __expf(-4.5f);
+    float wscale = 1.0f, winv = 1.0f;
+    if (ACC == ACC_FIXED_W) {
+        const float wmax = __uint_as_float(fs->wmax_bits);
+        if (wmax > 0.0f) {
+            int e;
+            frexpf(wmax, &e);  // wmax <= 2^e
+            e = max(e, -90);
+            wscale = ldexpf(1.0f, 31 - e);
+            winv = ldexpf(1.0f, e - 31);
+        }
+    }
     if (t == 0)
         s_ex = tile_extent(g, fs, o3, T3);
     __syncthreads();
@@ -566,6 +595,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                     wp.by = bw[1];
                                     wp.node0 = (blo[2] * TY + blo[1]) * TX + blo[0];
                                     wp.iby = 1.0f / (float) bw[1];
+                                    if (WEIGHTED)
+                                        wp.w = wts ? __ldg(wts + (size_t) j * wstride) : 1.0f;
                                 }
                             }
                             // exclusive prefix of the row counts over the warp
@@ -589,6 +620,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                             s_part[6][wl] = (uint32_t) wp.bx;
                             s_part[7][wl] = (uint32_t) wp.by;
                             s_part[8][wl] = (uint32_t) wp.node0;
+                            if (WEIGHTED)
+                                s_part[9][wl] = __float_as_uint(wp.w);
                             s_pre[wl] = incl - nb;
                             __syncwarp();
                             const uint32_t* pre = s_pre + warp * 32;
@@ -615,6 +648,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                         const float d0x = __uint_as_float(s_part[0][ow]);
                                         const int bx = (int) s_part[6][ow];
                                         const int row = (int) s_part[8][ow] + (zl * TY + yl) * TX;
+                                        const float pw = WEIGHTED ? __uint_as_float(s_part[9][ow]) : 0.0f;
                                         for (int xl = 0; xl < bx; ++xl) {
                                             const float dx = g.hhi[0] * (static_cast<float>(xl) + d0x);
                                             const float d2 = __fmaf_rn(dx, dx, dyz);
@@ -629,11 +663,21 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                             } else {
                                                 v = fmaxf(__expf(-d2 * inv) - E45, 0.0f);
                                             }
-                                            const uint32_t q = __float2uint_rn(v * FIX_SCALE);
-                                            if (q != 0u) {
-                                                const uint32_t old = atomicAdd(acc_lo + row + xl, q);
-                                                if (old + q < old)
-                                                    atomicAdd(acc_hi + row + xl, 1u);
+                                            if (ACC == ACC_FIXED_W) {
+                                                const long long q = __float2ll_rn(__fmul_rn(__fmul_rn(v, pw), wscale));
+                                                if (q != 0)
+                                                    atomicAdd(acc64 + row + xl, (unsigned long long) q);
+                                            } else if (ACC == ACC_DOUBLE) {
+                                                const float c = __fmul_rn(v, pw);  // rbf * val, in float
+                                                if (c != 0.0f)
+                                                    atomicAdd(accd + row + xl, (double) c);
+                                            } else {
+                                                const uint32_t q = __float2uint_rn(v * FIX_SCALE);
+                                                if (q != 0u) {
+                                                    const uint32_t old = atomicAdd(acc_lo + row + xl, q);
+                                                    if (old + q < old)
+                                                        atomicAdd(acc_hi + row + xl, 1u);
+                                                }
                                             }
                                         }
                                     }
@@ -652,8 +696,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     for (int n = t; n < NN; n += NT) {
         const int x = n % TX, y = (n / TX) % TY, z = n / (TX * TY);
         if (x0 + x < g.s[0] && y0 + y < g.s[1] && z0 + z < g.s[2]) {
-            const float v = __ull2float_rn(((unsigned long long) acc_hi[n] << 32) | acc_lo[n]) * FIX_INV;
-            grid[((size_t) (z0 + z) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)] = v;
+            const float v = ACC == ACC_FIXED_W ? __ll2float_rn((long long) acc64[n]) * winv
+                            : ACC == ACC_DOUBLE ? __double2float_rn(accd[n])
+                                                : __ull2float_rn(((unsigned long long) acc_hi[n] << 32) | acc_lo[n]) * FIX_INV;
+            grid[(((size_t) (z0 + z) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)) * (size_t) ostride] = v;
             dsum += (double) v;
             vmin = fminf(vmin, v);
             vmax = fmaxf(vmax, v);
@@ -774,31 +820,46 @@ uint32_t gather_tile_count(const GatherConfig& c, const GridGeo& g) {
 namespace {
 template<class K>
 cudaError_t launch_tiles(K kern, const GatherConfig& c, const GridGeo& g, int nt, size_t smem, cudaStream_t st,
-    const float4* rec_a, const int4* rec_b, const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs) {
+    const float4* rec_a, const int4* rec_b, const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs,
+    const GatherWeights& w) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess)
         return e;
     dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), ceil_div(g.s[2], c.tz));
-    kern<<<grd, nt, smem, st>>>(g, rec_a, rec_b, start, grid, tiles, fs, c.rmax);
+    kern<<<grd, nt, smem, st>>>(g, rec_a, rec_b, start, grid, tiles, fs, c.rmax, w.w, w.wstride,
+                                w.ostride > 0 ? w.ostride : 1);
     return cudaGetLastError();
+}
+
+template<int W>
+cudaError_t launch_exact(const GatherConfig& c, const GridGeo& g, size_t smem, cudaStream_t st, const float4* rec_a,
+    const int4* rec_b, const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs,
+    const GatherWeights& w) {
+    if (c.tx == 16 && c.ty == 16 && c.tz == 16)
+        return launch_tiles(gather_fixed_kernel<16, 16, 16, 256, W>, c, g, 256, smem, st, rec_a, rec_b, start, grid,
+                            tiles, fs, w);
+    if (c.tx == 16 && c.ty == 8 && c.tz == 8)
+        return launch_tiles(gather_fixed_kernel<16, 8, 8, 256, W>, c, g, 256, smem, st, rec_a, rec_b, start, grid,
+                            tiles, fs, w);
+    if (c.tx == 32 && c.ty == 16 && c.tz == 8)
+        return launch_tiles(gather_fixed_kernel<32, 16, 8, 512, W>, c, g, 512, smem, st, rec_a, rec_b, start, grid,
+                            tiles, fs, w);
+    return cudaErrorInvalidValue;
 }
 }  // namespace
 
 cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* rec_a, const int4* rec_b,
-    const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st) {
+    const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st, const GatherWeights& w) {
     const size_t smem = gather_smem_bytes(c);
     if (c.mode == GATHER_EXACT) {
-        if (c.tx == 16 && c.ty == 16 && c.tz == 16)
-            return launch_tiles(gather_fixed_kernel<16, 16, 16, 256>, c, g, 256, smem, st, rec_a, rec_b, start, grid,
-                                tiles, fs);
-        if (c.tx == 16 && c.ty == 8 && c.tz == 8)
-            return launch_tiles(gather_fixed_kernel<16, 8, 8, 256>, c, g, 256, smem, st, rec_a, rec_b, start, grid,
-                                tiles, fs);
-        if (c.tx == 32 && c.ty == 16 && c.tz == 8)
-            return launch_tiles(gather_fixed_kernel<32, 16, 8, 512>, c, g, 512, smem, st, rec_a, rec_b, start, grid,
-                                tiles, fs);
-        return cudaErrorInvalidValue;
+        if (w.mode == GatherWeights::DOUBLE)
+            return launch_exact<ACC_DOUBLE>(c, g, smem, st, rec_a, rec_b, start, grid, tiles, fs, w);
+        if (w.mode == GatherWeights::FIXED)
+            return launch_exact<ACC_FIXED_W>(c, g, smem, st, rec_a, rec_b, start, grid, tiles, fs, w);
+        return launch_exact<ACC_EXACT>(c, g, smem, st, rec_a, rec_b, start, grid, tiles, fs, w);
     }
+    if (w.mode != GatherWeights::DENSITY)
+        return cudaErrorInvalidValue;  // the weighted aggregators use the particle-major gather
     if (c.tx != GATHER_TX || c.ty != GATHER_TY || c.tz != GATHER_TZ)
         return cudaErrorInvalidValue;
     auto kern = gather_kernel<GATHER_TX, GATHER_TY, GATHER_TZ>;

@@ -52,10 +52,38 @@ struct GatherConfig {
     int rmax;              // row-table entries per plane chunk
 };
 
+// Accumulation and per-particle weights of one gather pass: DENSITY (exact fixed point), FIXED (the
+// intensity aggregator: weights w[j * wstride] in sorted order, signed fixed point), DOUBLE (the vector
+// aggregator: FP64 sums of weights w, or of the plain kernel values when w == nullptr). The output grid is
+// written with stride ostride (3 for one component of a vector volume).
+struct GatherWeights {
+    enum Mode { DENSITY = 0, FIXED = 1, DOUBLE = 2 };
+    int mode = DENSITY;
+    const float* w = nullptr;
+    int wstride = 1;
+    int ostride = 1;
+};
+
+// Per-particle weight source of one list for the intensity (nc = 1: first colour channel) or vector
+// (nc = 3: DIRDATA_FLOAT_XYZ) aggregator; data == nullptr with nc = 1: every particle has global_i.
+struct WeightSource {
+    const uint8_t* data = nullptr;
+    uint32_t stride = 0;
+    int ctype = 0;          // p2v_colour_type
+    float global_i = 0.0f;
+    uint64_t count = 0, offset = 0;
+};
+cudaError_t launch_pack_weights(const WeightSource& src, int nc, float* w, FrameScalars* fs, int sms, cudaStream_t st);
+cudaError_t launch_permute_weights(const uint32_t* order, const float* win, float* wout, uint32_t n, int nc, int sms,
+                                   cudaStream_t st);
+// vol3 /= weight sums, density range into fs, normalisation constants (ParticlesToDensity.cpp:628-682)
+cudaError_t launch_vector_finish(float* vol3, const float* wsum, int64_t V, FrameScalars* fs, int minmax_normalize,
+                                 int sms, cudaStream_t st);
+
 size_t gather_smem_bytes(const GatherConfig& c);
 cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* rec_a, const int4* rec_b,
-    const uint32_t* start,
-    float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st);
+    const uint32_t* start, float* grid, TileStats* tiles, FrameScalars* fs, cudaStream_t st,
+    const GatherWeights& w = GatherWeights{});
 uint32_t gather_tile_count(const GatherConfig& c, const GridGeo& g);
 // Reduce the tile statistics (fixed order, FP64 sum) and derive the normalisation of the grid.
 cudaError_t launch_finalize(const TileStats* tiles, uint32_t ntiles, FrameScalars* fs, int mass_normalize,

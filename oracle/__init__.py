@@ -74,6 +74,12 @@ def lib() -> C.CDLL:
                                                C.c_float, C.c_void_p]
         f.p2vo_aosphere_ao_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float,
                                            C.c_float, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
+        f.p2vo_density_weighted_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.POINTER(_Grid), C.c_int,
+                                                C.c_int, C.c_void_p]
+        f.p2vo_density_weighted_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int64, C.POINTER(_Grid), C.c_int,
+                                                C.c_int, C.c_void_p]
+        f.p2vo_vector_finish_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_float),
+                                             C.POINTER(C.c_float)]
         f.p2vo_mdao_dims.argtypes = [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_float),
                                      C.POINTER(C.c_float)]
         f.p2vo_mdao_volume_f32.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
@@ -119,6 +125,30 @@ def density_f64(xyzr, bbox, res, cyclic=(1, 1, 1), sigma=1.0, kernel=BUMP, nthre
     if rc:
         raise ValueError("invalid grid")
     return out
+
+
+def density_weighted(xyzr, w, bbox, res, cyclic=(1, 1, 1), sigma=1.0, kernel=BUMP, nthreads=1, fp64=False):
+    """Weighted createVolumeCPU sums (the intensity aggregator with w of shape (n,), one direction component
+    per column of w of shape (n, nc) for the vector aggregator); returns (z, y, x) or (z, y, x, nc)."""
+    a = _xyzr(xyzr)
+    wa = np.ascontiguousarray(w, np.float32)
+    nc = 1 if wa.ndim == 1 else wa.shape[1]
+    dt = np.float64 if fp64 else np.float32
+    out = np.zeros((res[2], res[1], res[0], nc), dt)
+    g = _grid(bbox, res, cyclic, sigma)
+    fn = lib().p2vo_density_weighted_f64 if fp64 else lib().p2vo_density_weighted_f32
+    if fn(a.ctypes.data, wa.ctypes.data, nc, a.shape[0], C.byref(g), kernel, nthreads, out.ctypes.data):
+        raise ValueError("invalid grid")
+    return out[..., 0] if nc == 1 else out
+
+
+def vector_finish_f32(vol3: np.ndarray, weights: np.ndarray, normalize: bool):
+    """The vector aggregator's finish in float (ParticlesToDensity.cpp:628-682); returns (volume, min, max)."""
+    v = np.ascontiguousarray(vol3, np.float32).copy()
+    w = np.ascontiguousarray(weights, np.float32)
+    mn, mx = C.c_float(), C.c_float()
+    lib().p2vo_vector_finish_f32(v.ctypes.data, w.ctypes.data, w.size, int(bool(normalize)), C.byref(mn), C.byref(mx))
+    return v, mn.value, mx.value
 
 
 def normalize_minmax_f32(vol: np.ndarray, apply: bool = True):

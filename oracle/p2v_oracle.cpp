@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include <omp.h>
@@ -125,13 +126,17 @@ void for_particles(int64_t n, int T, std::vector<std::vector<Acc>>& grids, Body 
 
 } // namespace
 
-extern "C" int p2vo_density_f32(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, float* out) {
+// FP32 createVolumeCPU (ParticlesToDensity.cpp:389-626): with w == nullptr the density (aggregator 0,
+// volOp :520-528); with nc weights per particle the intensity (nc = 1, :509-519) or one direction component
+// per pass of the vector aggregator (:492-508): vol += rbf(dis, sigma * rad) * val, in float.
+static int density_f32_impl(const float* xyzr, const float* w, int nc, int64_t n, const p2vo_grid* g, int kernel,
+                            int nthreads, float* out) {
     Geo G;
     if (!make_geo(g, G))
         return 1;
     const int64_t V = int64_t(G.s[0]) * G.s[1] * G.s[2];
     const int T = std::max(1, nthreads);
-    std::vector<std::vector<float>> grids(T, std::vector<float>(V, 0.0f));
+    std::vector<std::vector<float>> grids(T, std::vector<float>(V * nc, 0.0f));
     const float sigma = g->sigma;
     for_particles(n, T, grids, [&](int64_t j, std::vector<float>& vol) {
         const float* p = xyzr + 4 * j;
@@ -162,26 +167,41 @@ extern "C" int p2vo_density_f32(const float* xyzr, int64_t n, const p2vo_grid* g
                     if (rad == 0.0f) // volOp returns early (ParticlesToDensity.cpp:523-524)
                         continue;
                     float v = kernel == P2VO_BUMP ? rbf_f32(std::sqrt(d2), sigma * rad) : gauss3_f32(d2, sigma * rad);
-                    vol[wx + (wy + int64_t(wz) * G.s[1]) * G.s[0]] += v;
+                    const int64_t idx = wx + (wy + int64_t(wz) * G.s[1]) * G.s[0];
+                    if (!w)
+                        vol[idx] += v;
+                    else
+                        for (int c = 0; c < nc; ++c)
+                            vol[idx * nc + c] += v * w[j * nc + c];
                 }
             }
         }
     });
     // Serial reduction of the thread grids (ParticlesToDensity.cpp:623-626).
     for (int t = 1; t < T; ++t)
-        for (int64_t i = 0; i < V; ++i)
+        for (int64_t i = 0; i < V * nc; ++i)
             grids[0][i] = grids[t][i] + grids[0][i];
-    std::memcpy(out, grids[0].data(), V * sizeof(float));
+    std::memcpy(out, grids[0].data(), V * nc * sizeof(float));
     return 0;
 }
 
-extern "C" int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, double* out) {
+extern "C" int p2vo_density_f32(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, float* out) {
+    return density_f32_impl(xyzr, nullptr, 1, n, g, kernel, nthreads, out);
+}
+
+extern "C" int p2vo_density_weighted_f32(const float* xyzr, const float* w, int nc, int64_t n, const p2vo_grid* g,
+                                         int kernel, int nthreads, float* out) {
+    return density_f32_impl(xyzr, w, nc, n, g, kernel, nthreads, out);
+}
+
+static int density_f64_impl(const float* xyzr, const float* w, int nc, int64_t n, const p2vo_grid* g, int kernel,
+                            int nthreads, double* out) {
     Geo G;
     if (!make_geo(g, G))
         return 1;
     const int64_t V = int64_t(G.s[0]) * G.s[1] * G.s[2];
     const int T = std::max(1, nthreads);
-    std::vector<std::vector<double>> grids(T, std::vector<double>(V, 0.0));
+    std::vector<std::vector<double>> grids(T, std::vector<double>(V * nc, 0.0));
     const float sigma = g->sigma;
     for_particles(n, T, grids, [&](int64_t j, std::vector<double>& vol) {
         const float* p = xyzr + 4 * j;
@@ -215,17 +235,58 @@ extern "C" int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g
                     } else {
                         v = gauss3_f64(d2, eps);
                     }
-                    vol[wx + (wy + int64_t(wz) * G.s[1]) * G.s[0]] += v;
+                    const int64_t idx = wx + (wy + int64_t(wz) * G.s[1]) * G.s[0];
+                    if (!w)
+                        vol[idx] += v;
+                    else
+                        for (int c = 0; c < nc; ++c)
+                            vol[idx * nc + c] += v * static_cast<double>(w[j * nc + c]);
                 }
             }
         }
     });
     for (int t = 1; t < T; ++t)
-        for (int64_t i = 0; i < V; ++i)
+        for (int64_t i = 0; i < V * nc; ++i)
             grids[0][i] += grids[t][i];
-    std::memcpy(out, grids[0].data(), V * sizeof(double));
+    std::memcpy(out, grids[0].data(), V * nc * sizeof(double));
     return 0;
 }
+
+extern "C" int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, double* out) {
+    return density_f64_impl(xyzr, nullptr, 1, n, g, kernel, nthreads, out);
+}
+
+extern "C" int p2vo_density_weighted_f64(const float* xyzr, const float* w, int nc, int64_t n, const p2vo_grid* g,
+                                         int kernel, int nthreads, double* out) {
+    return density_f64_impl(xyzr, w, nc, n, g, kernel, nthreads, out);
+}
+
+// The vector aggregator's finish (ParticlesToDensity.cpp:628-682), float as the reference: every voxel's
+// direction sum divided by its weight sum (1 where that is 0), density = |v|, min / max over the densities
+// (max starting at 0), then with `normalize` all three components mapped by (a - min) * (1 / (max - min)).
+extern "C" void p2vo_vector_finish_f32(float* vol3, const float* weights, int64_t V, int normalize, float* out_min,
+                                       float* out_max) {
+    float maxD = 0.0f, minD = std::numeric_limits<float>::max();
+    for (int64_t i = 0; i < V; ++i) {
+        const float wv = weights[i] == 0.0f ? 1.0f : weights[i];
+        vol3[i * 3 + 0] /= wv;
+        vol3[i * 3 + 1] /= wv;
+        vol3[i * 3 + 2] /= wv;
+        const float d = std::sqrt(vol3[i * 3 + 0] * vol3[i * 3 + 0] + vol3[i * 3 + 1] * vol3[i * 3 + 1] +
+                                  vol3[i * 3 + 2] * vol3[i * 3 + 2]);
+        maxD = std::max(maxD, d);
+        minD = std::min(minD, d);
+    }
+    *out_min = minD;
+    *out_max = maxD;
+    if (normalize) {
+        const float rcp = 1.0f / (maxD - minD);
+        for (int64_t i = 0; i < 3 * V; ++i)
+            vol3[i] = (vol3[i] - minD) * rcp;
+    }
+}
+
+
 
 // ParticlesToDensity.cpp:669-682: min/max over the grid, then (v - min) * (1 / (max - min)) in float.
 extern "C" void p2vo_normalize_minmax_f32(float* v, int64_t n, int apply, float* out_min, float* out_max) {

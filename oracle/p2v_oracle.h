@@ -48,6 +48,17 @@ int p2vo_density_f32(const float* xyzr, int64_t n, const p2vo_grid* g, int kerne
  * grid spacing (right-left)/(res-1). The GPU path is judged against this. */
 int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, double* out);
 
+/* Weighted createVolumeCPU: nc weights per particle (w[j * nc + c]); out holds nc interleaved components.
+ * nc = 1 with intensities: the IColToSingleCell aggregator; the direction components: the
+ * IVecToSingleCell aggregator's sums (its weight grid is the plain density). */
+int p2vo_density_weighted_f32(const float* xyzr, const float* w, int nc, int64_t n, const p2vo_grid* g, int kernel,
+    int nthreads, float* out);
+int p2vo_density_weighted_f64(const float* xyzr, const float* w, int nc, int64_t n, const p2vo_grid* g, int kernel,
+    int nthreads, double* out);
+/* The vector aggregator's finish in float (ParticlesToDensity.cpp:628-682), in place on vol3 (3 per voxel). */
+void p2vo_vector_finish_f32(float* vol3, const float* weights, int64_t V, int normalize, float* out_min,
+    float* out_max);
+
 /* MDAO 2x2x2 mip step, FP64: dst[i] = sum of the up-to-8 children clamped to the source size, / 8. */
 void p2vo_mip_step_f64(const double* src, const int32_t sdim[3], double* dst, const int32_t ddim[3]);
 

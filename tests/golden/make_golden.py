@@ -75,8 +75,62 @@ def cases():
     return out
 
 
+def agg_cases():
+    """The intensity (aggregator 1) and vector (aggregator 2) aggregators; colour data are COLDATA_FLOAT_I and
+    directions DIRDATA_FLOAT_XYZ, the types the reference harness passes through."""
+    rng = np.random.default_rng(20240917)
+    out = {}
+    xyz = rng.uniform(0, 24, size=(5000, 3)).astype(np.float32)
+    out["icol_cyclic"] = dict(aggregator=1, lists=[dict(type=VERT_FLOAT_XYZ, data=xyz, stride=0, radius=0.8,
+                                                        count=5000, icol=rng.uniform(-1, 3, 5000).astype(np.float32))],
+                              bbox=(0, 0, 0, 24, 24, 24), res=(26, 24, 25), cyclic=(1, 1, 1), normalize=False,
+                              sigma=1.0)
+    rec = np.zeros((4000, 4), np.float32)
+    rec[:, :3] = rng.uniform(-2, 22, size=(4000, 3))
+    rec[:, 3] = rng.uniform(0.4, 1.2, size=4000)
+    out["icol_open_norm"] = dict(aggregator=1, lists=[dict(type=VERT_FLOAT_XYZR, data=rec, stride=0, radius=0.0,
+                                                           count=4000, icol=rng.uniform(0, 5, 4000).astype(np.float32))],
+                                 bbox=(0, 0, 0, 20, 20, 20), res=(21, 23, 20), cyclic=(0, 0, 0), normalize=True,
+                                 sigma=1.0)
+    xyz2 = rng.uniform(0, 20, size=(4500, 3)).astype(np.float32)
+    out["ivec_cyclic"] = dict(aggregator=2, lists=[dict(type=VERT_FLOAT_XYZ, data=xyz2, stride=0, radius=0.9,
+                                                        count=4500, dir=rng.normal(size=(4500, 3)).astype(np.float32))],
+                              bbox=(0, 0, 0, 20, 20, 20), res=(22, 20, 21), cyclic=(1, 1, 1), normalize=False,
+                              sigma=1.0)
+    rec2 = np.zeros((3500, 4), np.float32)
+    rec2[:, :3] = rng.uniform(0, 20, size=(3500, 3))
+    rec2[:, 3] = rng.uniform(0.5, 1.3, size=3500)
+    out["ivec_mixed_norm"] = dict(aggregator=2, lists=[dict(type=VERT_FLOAT_XYZR, data=rec2, stride=0, radius=0.0,
+                                                            count=3500,
+                                                            dir=rng.uniform(-2, 2, (3500, 3)).astype(np.float32))],
+                                  bbox=(0, 0, 0, 20, 20, 20), res=(20, 22, 24), cyclic=(1, 0, 1), normalize=True,
+                                  sigma=1.0)
+    return out
+
+
 def main():
     oracle.build(with_reference=True)
+    for name, c in agg_cases().items():
+        vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"],
+                                             aggregator=c["aggregator"])
+        d = dict(aggregator=np.int32(c["aggregator"]), bbox=np.array(c["bbox"], np.float32),
+                 res=np.array(c["res"], np.int32), cyclic=np.array(c["cyclic"], np.int32),
+                 normalize=np.int32(c["normalize"]), sigma=np.float32(c["sigma"]), nlists=np.int32(len(c["lists"])),
+                 volume=vol, components=np.int32(meta["components"]), min_value=np.float64(meta["min_value"]),
+                 max_value=np.float64(meta["max_value"]))
+        for i, L in enumerate(c["lists"]):
+            d[f"l{i}_type"] = np.int32(L["type"])
+            d[f"l{i}_data"] = np.ascontiguousarray(L["data"])
+            d[f"l{i}_stride"] = np.int32(L["stride"])
+            d[f"l{i}_radius"] = np.float32(L["radius"])
+            d[f"l{i}_count"] = np.int64(L["count"])
+            if "icol" in L:
+                d[f"l{i}_icol"] = L["icol"]
+            if "dir" in L:
+                d[f"l{i}_dir"] = L["dir"]
+        path = os.path.join(HERE, f"agg_{name}.npz")
+        np.savez_compressed(path, **d)
+        print(f"{path}: volume {vol.shape} range [{vol.min():.6g}, {vol.max():.6g}]")
     for name, c in cases().items():
         vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"])
         d = dict(bbox=np.array(c["bbox"], np.float32), res=np.array(c["res"], np.int32),

@@ -1,0 +1,65 @@
+"""The intensity and vector aggregators of the CPU restatement against MegaMol's own ParticlesToDensity
+(compiled from the reference tree where it exists): bit-exact with one thread."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+# the reference's OpenMP team size; the restatement reproduces its static partition and thread-grid sum
+T = int(os.environ.get("OMP_NUM_THREADS", "0")) or os.cpu_count()
+
+
+def frame(rng, n=3000):
+    xyz = rng.uniform(0, 20, (n, 3)).astype(np.float32)
+    xyzr = np.column_stack([xyz, np.full(n, 0.9, np.float32)])
+    inten = rng.uniform(-1.0, 3.0, n).astype(np.float32)
+    dirs = rng.normal(size=(n, 3)).astype(np.float32)
+    return xyz, xyzr, inten, dirs
+
+
+needs_ref = pytest.mark.skipif(not oracle.reference_available(), reason="reference tree not compiled here")
+
+
+@needs_ref
+@pytest.mark.parametrize("normalize", [False, True])
+def test_intensity_aggregator_bit_exact(normalize):
+    rng = np.random.default_rng(7)
+    xyz, xyzr, inten, _ = frame(rng)
+    res, bbox = (22, 20, 24), (0, 0, 0, 20, 20, 20)
+    ref, meta = oracle.reference_density([dict(type=1, data=xyz, stride=0, radius=0.9, count=len(xyz), icol=inten)],
+                                         bbox, res, (1, 1, 1), normalize, 1.0, aggregator=1)
+    mine = oracle.density_weighted(xyzr, inten, bbox, res, nthreads=T)
+    mine, mn, mx = oracle.normalize_minmax_f32(mine, normalize)
+    assert np.array_equal(ref.reshape(-1), mine.reshape(-1))
+    assert meta["min_value"] == (0.0 if normalize else mn) and meta["max_value"] == (1.0 if normalize else mx)
+
+
+@needs_ref
+@pytest.mark.parametrize("normalize", [False, True])
+def test_vector_aggregator_bit_exact(normalize):
+    rng = np.random.default_rng(8)
+    xyz, xyzr, _, dirs = frame(rng)
+    res, bbox = (18, 21, 19), (0, 0, 0, 20, 20, 20)
+    ref, meta = oracle.reference_density([dict(type=1, data=xyz, stride=0, radius=0.9, count=len(xyz), dir=dirs)],
+                                         bbox, res, (1, 0, 1), normalize, 1.0, aggregator=2)
+    v3 = oracle.density_weighted(xyzr, dirs, bbox, res, cyclic=(1, 0, 1), nthreads=T)
+    w = oracle.density_f32(xyzr, bbox, res, cyclic=(1, 0, 1), nthreads=T)
+    mine, mn, mx = oracle.vector_finish_f32(v3, w, normalize)
+    assert np.array_equal(ref.reshape(-1), mine.reshape(-1))
+    if normalize:
+        assert (meta["min_value"], meta["max_value"]) == (0.0, 1.0)
+    else:
+        assert (meta["min_value"], meta["max_value"]) == (mn, mx)
+
+
+def test_weighted_fp64_is_linear():
+    rng = np.random.default_rng(9)
+    _, xyzr, inten, dirs = frame(rng, 800)
+    res, bbox = (12, 12, 12), (0, 0, 0, 20, 20, 20)
+    a = oracle.density_weighted(xyzr, inten, bbox, res, fp64=True)
+    b = oracle.density_weighted(xyzr, 4.0 * inten, bbox, res, fp64=True)  # exact scaling in float32
+    assert np.allclose(b, 4.0 * a, rtol=1e-12, atol=1e-12)
+    ones = oracle.density_weighted(xyzr, np.ones(len(xyzr), np.float32), bbox, res, fp64=True)
+    assert np.allclose(ones, oracle.density_f64(xyzr, bbox, res), rtol=1e-12, atol=1e-14)
