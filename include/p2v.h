@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 3
+#define P2V_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -143,7 +143,8 @@ typedef struct p2v_volume {
 typedef struct p2v_params {
     uint32_t struct_size; /* sizeof(p2v_params); set by p2v_params_default */
     /* --- ParticlesToDensity slots (ParticlesToDensity.cpp:59-152) --- */
-    int32_t aggregator;   /* 0 = PosToSingleCell_Volume (only 0 is implemented) */
+    int32_t aggregator;   /* 0 = PosToSingleCell_Volume (density), 1 = IColToSingleCell_Volume (first colour
+                             channel), 2 = IVecToSingleCell_Volume (normals as DIRDATA_FLOAT_XYZ; 3 components) */
     int32_t sizex, sizey, sizez;
     int32_t cyclX, cyclY, cyclZ;
     int32_t normalize;    /* min-max to [0,1] after accumulation (ParticlesToDensity.cpp:676-682) */
@@ -178,6 +179,8 @@ typedef struct p2v_params {
     int32_t batch_lanes;    /* p2v_run_batch: concurrent frame pipelines; 0 = the autotuned count or 4 */
     int32_t batch_graph;    /* p2v_run_batch: capture the batch as a CUDA graph and replay it while the batch's
                                shape (frames, sizes, pointers, parameters) repeats (1) */
+    /* --- outputs --- */
+    int32_t vector_grid;    /* aggregator 2: also build the outParticles / outInfo grid of p2v_get_vector_grid (0) */
 } p2v_params;
 
 typedef struct p2v_stats {
@@ -257,6 +260,24 @@ P2V_API p2v_status p2v_get_ao_volume(p2v_ctx* ctx, int32_t level, float* out, ui
  * count and nbins (nullable) receive the sizes. Synchronises the device. */
 P2V_API p2v_status p2v_get_binning(p2v_ctx* ctx, uint32_t* keys, uint32_t* order, uint64_t capacity,
                                    uint32_t* cell_start, uint64_t start_capacity, uint32_t* count, uint32_t* nbins);
+
+/* The vector aggregator's two extra outputs (ParticlesToDensity.cpp:306-380, 436-456, 628-727) of the last
+ * p2v_run_frame with aggregator 2 and vector_grid set: the grid nodes whose average direction is non-zero,
+ * sorted by its length (the "density") descending, equal densities in node order. Per entry: the node
+ * position (3 floats, min + slice distance * index), the unit direction (3), the colour
+ * (density - min) / (max - min) (the outParticles list: VERTDATA_FLOAT_XYZ, DIRDATA_FLOAT_XYZ,
+ * COLDATA_FLOAT_I), and the outInfo row of 7 floats (PositionX/Y/Z, VelocityX/Y/Z, VelocityMag = the colour
+ * when normalising, else the density). meta receives the entry count, outParticles' global radius (bbox
+ * width / sizex / 5) and the 7 columns' minimum / maximum values. Each output pointer may be NULL; the
+ * others need capacity >= count entries, in host or device memory per mem. Synchronises the device. */
+typedef struct p2v_vector_grid_info {
+    uint64_t count;
+    float global_radius;
+    float col_min[7], col_max[7];
+} p2v_vector_grid_info;
+
+P2V_API p2v_status p2v_get_vector_grid(p2v_ctx* ctx, float* positions, float* directions, float* colours,
+                                       float* info, uint64_t capacity, int32_t mem, p2v_vector_grid_info* meta);
 
 P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
 /* Last error message of this context ("" if none); returns the message length. */

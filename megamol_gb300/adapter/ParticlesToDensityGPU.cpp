@@ -43,10 +43,14 @@ ParticlesToDensityGPU::ParticlesToDensityGPU()
         , aoStrengthSlot("ao::strength", "Strength")
         , aoConeLengthSlot("ao::coneLength", "Cone length")
         , outDataSlot("outData", "Provides a density volume for the particles")
+        , outParticlesSlot("outParticles", "Provides particles forming a regular grid with the sampled values")
+        , outInfoSlot("outInfo", "Provides information which can be used for visualization and filtering")
         , outAOSlot("outAO", "Provides the particles with their ambient occlusion as intensity colour")
         , inDataSlot("inData", "Takes the particle data") {
     auto* ep = new EnumParam(0);
     ep->SetTypePair(0, "PosToSingleCell_Volume");
+    ep->SetTypePair(1, "IColToSingleCell_Volume");
+    ep->SetTypePair(2, "IVecToSingleCell_Volume");
     aggregatorSlot << ep;
     MakeSlotAvailable(&aggregatorSlot);
     xResSlot << new IntParam(16);
@@ -114,6 +118,16 @@ ParticlesToDensityGPU::ParticlesToDensityGPU()
     MakeSlotAvailable(&outDataSlot);
 
     using MPDC = geocalls::MultiParticleDataCall;
+    using TDC = datatools::table::TableDataCall;
+    // as the reference, one data and one extent callback serve the volume, the grid and the table
+    // (ParticlesToDensity.cpp:114-124)
+    outParticlesSlot.SetCallback(MPDC::ClassName(), MPDC::FunctionName(0), &ParticlesToDensityGPU::getDataCallback);
+    outParticlesSlot.SetCallback(MPDC::ClassName(), MPDC::FunctionName(1), &ParticlesToDensityGPU::getExtentCallback);
+    MakeSlotAvailable(&outParticlesSlot);
+    outInfoSlot.SetCallback(TDC::ClassName(), TDC::FunctionName(0), &ParticlesToDensityGPU::getDataCallback);
+    outInfoSlot.SetCallback(TDC::ClassName(), TDC::FunctionName(1), &ParticlesToDensityGPU::getExtentCallback);
+    MakeSlotAvailable(&outInfoSlot);
+
     outAOSlot.SetCallback(MPDC::ClassName(), MPDC::FunctionName(0), &ParticlesToDensityGPU::getAODataCallback);
     outAOSlot.SetCallback(MPDC::ClassName(), MPDC::FunctionName(1), &ParticlesToDensityGPU::getAOExtentCallback);
     MakeSlotAvailable(&outAOSlot);
@@ -158,16 +172,31 @@ void ParticlesToDensityGPU::resetDirty() {
 
 bool ParticlesToDensityGPU::getExtentCallback(core::Call& c) {
     auto* out = dynamic_cast<geocalls::VolumetricDataCall*>(&c);
+    auto* outGrid = dynamic_cast<geocalls::MultiParticleDataCall*>(&c);
+    auto* outInfo = dynamic_cast<datatools::table::TableDataCall*>(&c);
     auto* in = inDataSlot.CallAs<geocalls::MultiParticleDataCall>();
-    if (out == nullptr || in == nullptr)
+    if (in == nullptr)
         return false;
-    in->SetFrameID(out->FrameID(), true);
+    in->SetFrameID(out != nullptr ? out->FrameID() : (outGrid != nullptr ? outGrid->FrameID() : 0), true);
     if (!(*in)(1))
         return false;
-    out->AccessBoundingBoxes().SetObjectSpaceBBox(in->GetBoundingBoxes().ObjectSpaceBBox());
-    out->AccessBoundingBoxes().SetObjectSpaceClipBox(in->GetBoundingBoxes().ObjectSpaceClipBox());
-    out->AccessBoundingBoxes().MakeScaledWorld(1.0f);
-    out->SetFrameCount(in->FrameCount());
+    if (out != nullptr) {
+        out->AccessBoundingBoxes().SetObjectSpaceBBox(in->GetBoundingBoxes().ObjectSpaceBBox());
+        out->AccessBoundingBoxes().SetObjectSpaceClipBox(in->GetBoundingBoxes().ObjectSpaceClipBox());
+        out->AccessBoundingBoxes().MakeScaledWorld(1.0f);
+        out->SetFrameCount(in->FrameCount());
+    }
+    if (outGrid != nullptr) {
+        outGrid->AccessBoundingBoxes().SetObjectSpaceBBox(in->GetBoundingBoxes().ObjectSpaceBBox());
+        outGrid->AccessBoundingBoxes().SetObjectSpaceClipBox(in->GetBoundingBoxes().ObjectSpaceClipBox());
+        outGrid->AccessBoundingBoxes().MakeScaledWorld(1.0f);
+        outGrid->SetFrameCount(in->FrameCount());
+    }
+    if (outInfo != nullptr) {
+        outInfo->SetDataHash(dataHash);
+        outInfo->SetUnlocker(nullptr);
+        outInfo->SetFrameCount(in->FrameCount());
+    }
     return true;
 }
 
@@ -217,6 +246,7 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
     prm.ao_offset = aoOffsetSlot.Param<FloatParam>()->Value();
     prm.ao_strength = aoStrengthSlot.Param<FloatParam>()->Value();
     prm.ao_cone_length = aoConeLengthSlot.Param<FloatParam>()->Value();
+    prm.vector_grid = prm.aggregator == 2;
     if (p2v_set_params(ctx, &prm) != P2V_OK)
         return false;
 
@@ -233,6 +263,16 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
         L.count = p.GetCount();
         L.global_radius = p.GetGlobalRadius();
         L.mem = P2V_MEM_HOST;
+        // the intensity aggregator reads the first colour channel, or the global colour's red
+        L.colour_type = static_cast<int32_t>(p.GetColourDataType());
+        L.colour_data = p.GetColourData();
+        L.colour_stride = p.GetColourDataStride();
+        std::copy(p.GetGlobalColour(), p.GetGlobalColour() + 4, L.global_colour);
+        // the vector aggregator's directions: DIRDATA_FLOAT_XYZ
+        if (prm.aggregator == 2 && p.GetDirDataType() == geocalls::SimpleSphericalParticles::DIRDATA_FLOAT_XYZ) {
+            L.normals = static_cast<const float*>(p.GetDirData());
+            L.normal_stride = p.GetDirDataStride();
+        }
         if (prm.ao_mode != P2V_AO_NONE) {
             L.normals = static_cast<const float*>(p.GetDirData());
             L.normal_stride = p.GetDirDataStride();
@@ -261,7 +301,8 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
         v.resolution[1] = prm.sizey;
         v.resolution[2] = prm.sizez;
     }
-    volume.resize(v.resolution[0] * v.resolution[1] * v.resolution[2]);
+    const int comps = prm.aggregator == 2 ? 3 : 1;
+    volume.resize(v.resolution[0] * v.resolution[1] * v.resolution[2] * comps);
     v.data = volume.data();
     v.mem = P2V_MEM_HOST;
     v.capacity = volume.size();
@@ -276,7 +317,7 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
         xResSlot.Param<IntParam>()->SetValue(static_cast<int>(v.resolution[0]), false);
         yResSlot.Param<IntParam>()->SetValue(static_cast<int>(v.resolution[1]), false);
     }
-    metadata.Components = 1;
+    metadata.Components = comps;
     metadata.GridType = geocalls::CARTESIAN;
     metadata.ScalarType = geocalls::FLOATING_POINT;
     metadata.ScalarLength = sizeof(float);
@@ -289,24 +330,80 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
         metadata.SliceDists[a] = &sliceDists[a];
         metadata.IsUniform[a] = true;
     }
-    minValue = v.min_value;
-    maxValue = v.max_value;
-    metadata.MinValues = &minValue;
-    metadata.MaxValues = &maxValue;
+    // every component carries the published range (ParticlesToDensity.cpp:259-270)
+    for (int k = 0; k < 3; ++k) {
+        minValues[k] = v.min_value;
+        maxValues[k] = v.max_value;
+    }
+    metadata.MinValues = minValues;
+    metadata.MaxValues = maxValues;
+    hasData = true;
+    return prm.aggregator != 2 || fetchVectorGrid();
+}
+
+bool ParticlesToDensityGPU::fetchVectorGrid() {
+    p2v_vector_grid_info vg{};
+    if (p2v_get_vector_grid(ctx, nullptr, nullptr, nullptr, nullptr, 0, P2V_MEM_HOST, &vg) != P2V_OK)
+        return false;
+    grid.resize(3 * vg.count);
+    directions.resize(3 * vg.count);
+    colors.resize(vg.count);
+    infoData.resize(7 * vg.count);
+    if (p2v_get_vector_grid(ctx, grid.data(), directions.data(), colors.data(), infoData.data(), vg.count,
+            P2V_MEM_HOST, &vg) != P2V_OK)
+        return false;
+    gridRadius = vg.global_radius;
+    static const char* names[7] = {
+        "PositionX", "PositionY", "PositionZ", "VelocityX", "VelocityY", "VelocityZ", "VelocityMag"};
+    for (int k = 0; k < 7; ++k) {  // ParticlesToDensity.cpp:327-377
+        info[k].SetName(names[k]);
+        info[k].SetType(datatools::table::TableDataCall::ColumnType::QUANTITATIVE);
+        info[k].SetMinimumValue(vg.col_min[k]);
+        info[k].SetMaximumValue(vg.col_max[k]);
+    }
     return true;
 }
 
 bool ParticlesToDensityGPU::getDataCallback(core::Call& c) {
     auto* in = inDataSlot.CallAs<geocalls::MultiParticleDataCall>();
     auto* out = dynamic_cast<geocalls::VolumetricDataCall*>(&c);
-    if (in == nullptr || out == nullptr)
+    auto* outGrid = dynamic_cast<geocalls::MultiParticleDataCall*>(&c);
+    auto* outInfo = dynamic_cast<datatools::table::TableDataCall*>(&c);
+    if (in == nullptr)
         return false;
-    if (!pullFrame(in, out->FrameID()))
-        return false;
-    out->SetFrameID(time);
-    out->SetData(volume.data());
-    out->SetMetadata(&metadata);
-    out->SetDataHash(dataHash);
+    // the volume and the grid pull the frame; the table serves the last result (ParticlesToDensity.cpp:220-245)
+    if (out != nullptr || outGrid != nullptr)
+        if (!pullFrame(in, out != nullptr ? out->FrameID() : outGrid->FrameID()))
+            return false;
+    const bool isVector = aggregatorSlot.Param<EnumParam>()->Value() == 2;
+    if (out != nullptr) {
+        out->SetFrameID(time);
+        out->SetData(volume.data());
+        out->SetMetadata(&metadata);
+        out->SetDataHash(dataHash);
+    }
+    if (outGrid != nullptr && isVector) {  // ParticlesToDensity.cpp:306-323
+        outGrid->SetFrameID(time);
+        outGrid->SetDataHash(dataHash);
+        outGrid->SetParticleListCount(1);
+        auto& p = outGrid->AccessParticles(0);
+        p.SetCount(colors.size());
+        if (p.GetCount() > 0) {
+            p.SetVertexData(geocalls::SimpleSphericalParticles::VERTDATA_FLOAT_XYZ, grid.data());
+            p.SetDirData(geocalls::SimpleSphericalParticles::DIRDATA_FLOAT_XYZ, directions.data());
+            p.SetColourData(geocalls::SimpleSphericalParticles::COLDATA_FLOAT_I, colors.data());
+            p.SetGlobalRadius(gridRadius);
+        }
+    }
+    if (outInfo != nullptr && isVector) {  // ParticlesToDensity.cpp:325-380
+        if (!hasData) {
+            infoData.clear();
+            outInfo->SetDataHash(0);
+        } else {
+            outInfo->SetDataHash(dataHash);
+        }
+        outInfo->Set(info.size(), infoData.size() / info.size(), info.data(), infoData.data());
+    }
     return true;
 }
 

@@ -4,7 +4,9 @@
  *
  * Slots and parameters keep the reference module's names and defaults ("aggregator", "sizex/y/z",
  * "cyclX/Y/Z", "normalize", "sigma", "forSurfaceReconstruction"; callee "outData" answering all six
- * VolumetricDataCall functions; caller "inData" for a MultiParticleDataCall). Added: "outAO", a
+ * VolumetricDataCall functions; callees "outParticles" (MultiParticleDataCall) and "outInfo"
+ * (TableDataCall) carrying the vector aggregator's grid; caller "inData" for a MultiParticleDataCall).
+ * Added: "outAO", a
  * MultiParticleDataCall whose lists carry the input particles with COLDATA_FLOAT_I = ambient occlusion,
  * and the AO / kernel parameters of p2v_params.
  */
@@ -13,6 +15,7 @@
 #include <array>
 #include <vector>
 
+#include "datatools/table/TableDataCall.h"
 #include "geometry_calls/MultiParticleDataCall.h"
 #include "geometry_calls/VolumetricDataCall.h"
 #include "mmcore/CalleeSlot.h"
@@ -51,6 +54,7 @@ private:
     bool getAOExtentCallback(core::Call& c);
 
     bool pullFrame(geocalls::MultiParticleDataCall* in, unsigned int frame);
+    bool fetchVectorGrid();
     bool recompute(geocalls::MultiParticleDataCall* in);
     bool anythingDirty() const;
     void resetDirty();
@@ -63,6 +67,8 @@ private:
         aoOffsetSlot, aoStrengthSlot, aoConeLengthSlot;
 
     core::CalleeSlot outDataSlot;
+    core::CalleeSlot outParticlesSlot;
+    core::CalleeSlot outInfoSlot;
     core::CalleeSlot outAOSlot;
     core::CallerSlot inDataSlot;
 
@@ -71,7 +77,12 @@ private:
     std::vector<std::vector<float>> ao;
     geocalls::VolumetricDataCall::Metadata metadata;
     std::array<float, 3> sliceDists{};
-    double minValue = 0.0, maxValue = 0.0;
+    double minValues[3] = {0.0, 0.0, 0.0}, maxValues[3] = {0.0, 0.0, 0.0};
+    // the vector aggregator's grid (ParticlesToDensity.h:115-126): positions, directions, colours, info rows
+    std::vector<float> grid, directions, colors, infoData;
+    float gridRadius = 0.0f;
+    std::array<datatools::table::TableDataCall::ColumnInfo, 7> info;
+    bool hasData = false;
     unsigned int time = static_cast<unsigned int>(-1);
     size_t inDataHash = static_cast<size_t>(-1);
     size_t dataHash = 0;

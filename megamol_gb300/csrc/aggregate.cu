@@ -91,11 +91,13 @@ __global__ void __launch_bounds__(256) permute_weights_kernel(const uint32_t* __
 
 // ParticlesToDensity.cpp:628-652 per voxel: v /= (w == 0 ? 1 : w); density = sqrt(x*x + y*y + z*z), in
 // float without contraction; the density range (max starting at 0, min at FLT_MAX) by atomics on the bits
-// of the non-negative densities.
+// of the non-negative densities. With the grid buffers also the density, the unit direction v / density
+// (0 where the density is 0), the descending sort key and the count of non-zero densities.
 __global__ void __launch_bounds__(256) vector_finish_kernel(float* __restrict__ vol3, const float* __restrict__ wsum,
-                                                            int64_t V, FrameScalars* __restrict__ fs) {
-    __shared__ uint32_t s_lo[8], s_hi[8];
-    uint32_t lo = 0x7f7fffffu, hi = 0u;
+                                                            int64_t V, FrameScalars* __restrict__ fs,
+                                                            VectorGridBufs vg) {
+    __shared__ uint32_t s_lo[8], s_hi[8], s_nz[8];
+    uint32_t lo = 0x7f7fffffu, hi = 0u, nz = 0u;
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < V; i += (int64_t) gridDim.x * blockDim.x) {
         const float wv = wsum[i] == 0.0f ? 1.0f : wsum[i];
         float v[3];
@@ -110,24 +112,84 @@ __global__ void __launch_bounds__(256) vector_finish_kernel(float* __restrict__ 
             lo = min(lo, __float_as_uint(d));
             hi = max(hi, __float_as_uint(d));
         }
+        if (vg.dens) {
+            vg.dens[i] = d;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                vg.dirs[i * 3 + c] = d == 0.0f ? 0.0f : __fdiv_rn(v[c], d);
+            vg.keys[i] = ~__float_as_uint(d);
+            vg.vals[i] = (uint32_t) i;
+            nz += d != 0.0f ? 1u : 0u;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        nz += __shfl_xor_sync(0xffffffffu, nz, o);
     }
     if ((threadIdx.x & 31) == 0) {
         s_lo[threadIdx.x >> 5] = lo;
         s_hi[threadIdx.x >> 5] = hi;
+        s_nz[threadIdx.x >> 5] = nz;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int k = 1; k < (int) (blockDim.x >> 5); ++k) {
             lo = min(lo, s_lo[k]);
             hi = max(hi, s_hi[k]);
+            nz += s_nz[k];
         }
         atomicMin(&fs->dmin_bits, lo);
         atomicMax(&fs->dmax_bits, hi);
+        if (nz)
+            atomicAdd(&fs->vcount, nz);
+    }
+}
+
+// ParticlesToDensity.cpp:436-456, 653-668, 685-727: entry j of the sorted, compacted grid. The node position
+// is min + h * index, the colour (density - min) / (max - min) with the densities' range, the info row the
+// position, the direction and the colour when normalising, else the density.
+__global__ void __launch_bounds__(256) vector_grid_kernel(const uint32_t* __restrict__ order,
+                                                          const float* __restrict__ dens,
+                                                          const float* __restrict__ dirs,
+                                                          const FrameScalars* __restrict__ fs, VectorGridGeo geo,
+                                                          uint32_t count, float* __restrict__ pos,
+                                                          float* __restrict__ dir, float* __restrict__ col,
+                                                          float* __restrict__ info) {
+    const float mn = __uint_as_float(fs->dmin_bits), mx = __uint_as_float(fs->dmax_bits);
+    const float range = __fsub_rn(mx, mn);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+        const uint32_t idx = order[j];
+        const uint32_t sx = (uint32_t) geo.res[0], sy = (uint32_t) geo.res[1];
+        const uint32_t xyz[3] = {idx % sx, (idx / sx) % sy, idx / (sx * sy)};
+        float p[3], u[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            p[a] = __fadd_rn(geo.minf[a], __fmul_rn(geo.hf[a], static_cast<float>(xyz[a])));
+            u[a] = dirs[(size_t) idx * 3 + a];
+        }
+        const float d = dens[idx];
+        const float c = __fdiv_rn(__fsub_rn(d, mn), range);
+        if (pos)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                pos[(size_t) j * 3 + a] = p[a];
+        if (dir)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                dir[(size_t) j * 3 + a] = u[a];
+        if (col)
+            col[j] = c;
+        if (info) {
+            float* r = info + (size_t) j * 7;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                r[a] = p[a];
+                r[3 + a] = u[a];
+            }
+            r[6] = geo.normalize ? c : d;
+        }
     }
 }
 
@@ -174,10 +236,20 @@ cudaError_t launch_permute_weights(const uint32_t* order, const float* win, floa
 }
 
 cudaError_t launch_vector_finish(float* vol3, const float* wsum, int64_t V, FrameScalars* fs, int minmax_normalize,
-                                 int sms, cudaStream_t st) {
+                                 int sms, cudaStream_t st, const VectorGridBufs* vg) {
     const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((V + 255) / 256, (int64_t) sms * 16));
-    vector_finish_kernel<<<grd, 256, 0, st>>>(vol3, wsum, V, fs);
+    vector_finish_kernel<<<grd, 256, 0, st>>>(vol3, wsum, V, fs, vg ? *vg : VectorGridBufs{});
     vector_range_kernel<<<1, 1, 0, st>>>(fs, minmax_normalize);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vector_grid(const uint32_t* order, const float* dens, const float* dirs, const FrameScalars* fs,
+                               const VectorGridGeo& geo, uint32_t count, float* pos, float* dir, float* col, float* info,
+                               int sms, cudaStream_t st) {
+    if (count == 0)
+        return cudaSuccess;
+    const unsigned grd = (unsigned) std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(count, 256), (uint32_t) sms * 16));
+    vector_grid_kernel<<<grd, 256, 0, st>>>(order, dens, dirs, fs, geo, count, pos, dir, col, info);
     return cudaGetLastError();
 }
 

@@ -65,6 +65,7 @@ enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_C
 struct Pipe {
     DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
     DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list, wts, wsorted, wsum;
+    DevBuf vdens, vdirs, vkeys0, vkeys1, vvals0, vvals1, vout;  // the vector aggregator's grid outputs
     StencilTex stex[2];                    // the learned AO's two stencil levels as textures
     cudaEvent_t ev[EV_COUNT] = {};
     FrameScalars* h_scal = nullptr;        // pinned mirror of the last frame's scalars
@@ -75,6 +76,11 @@ struct Pipe {
     const uint32_t* last_keys = nullptr;   // sorted bin keys of the last frame
     uint32_t last_n = 0, last_nbins = 0;
     uint64_t last_res[3] = {0, 0, 0};
+    // the vector grid of the last frame (aggregator 2 with vector_grid)
+    const uint32_t* vg_order = nullptr;
+    VectorGridGeo vg_geo{};
+    uint32_t vg_count = 0;
+    float vg_radius = 0.0f, vg_bbox[6] = {}, vg_range[2] = {0.0f, 0.0f};
 
     cudaError_t init(bool with_stream) {
         for (auto& e : ev) {
@@ -94,7 +100,7 @@ struct Pipe {
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &rec_b, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout})
             b->release();
         stex[0].release();
         stex[1].release();
@@ -109,6 +115,7 @@ struct Pipe {
         stream = nullptr;
         last_grid = nullptr;
         last_order = nullptr;
+        vg_order = nullptr;
     }
 };
 
@@ -122,6 +129,8 @@ struct FrameJob {
     const uint32_t* keys = nullptr;
     uint32_t nbins = 0;
     int components = 1;
+    const uint32_t* vg_order = nullptr;  // sorted vector grid (aggregator 2 with vector_grid), else null
+    VectorGridGeo vg_geo{};
     FrameScalars* h_out = nullptr;  // pinned slot that receives the frame's scalars
     bool timed = false;             // stage events were recorded
 };
@@ -442,6 +451,18 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         if (agg == 2)
             P2V_CUDA_TRY(pp.wsum.ensure(sizeof(float) * V));
     }
+    const bool vgrid = agg == 2 && P.vector_grid;
+    if (vgrid) {
+        if (V >= (1ull << 31))
+            return fail(P2V_EINVAL, "the vector grid holds at most 2^31 - 1 nodes");
+        P2V_CUDA_TRY(pp.vdens.ensure(sizeof(float) * V));
+        P2V_CUDA_TRY(pp.vdirs.ensure(sizeof(float) * 3 * V));
+        P2V_CUDA_TRY(pp.vkeys0.ensure(sizeof(uint32_t) * V));
+        P2V_CUDA_TRY(pp.vkeys1.ensure(sizeof(uint32_t) * V));
+        P2V_CUDA_TRY(pp.vvals0.ensure(sizeof(uint32_t) * V));
+        P2V_CUDA_TRY(pp.vvals1.ensure(sizeof(uint32_t) * V));
+        P2V_CUDA_TRY(status.ensure(4 * (sort_status_words((uint32_t) V) + 256)));
+    }
 
     FrameScalars* fs = scal.as<FrameScalars>();
     if (timed)
@@ -627,9 +648,26 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_DENSITY], st));
     const double voxel_volume = (double) g.hhi[0] * g.hhi[1] * g.hhi[2];
+    const uint32_t* vg_order = nullptr;
     if (agg == 2) {
-        P2V_CUDA_TRY(launch_vector_finish(dgrid, pp.wsum.as<float>(), (int64_t) V, fs, P.normalize, sms, st));
+        VectorGridBufs vb{pp.vdens.as<float>(), pp.vdirs.as<float>(), pp.vkeys0.as<uint32_t>(),
+                          pp.vvals0.as<uint32_t>()};
+        P2V_CUDA_TRY(launch_vector_finish(dgrid, pp.wsum.as<float>(), (int64_t) V, fs, P.normalize, sms, st,
+                                          vgrid ? &vb : nullptr));
         P2V_CUDA_TRY(launch_normalize_modes(dgrid, VC, fs, 0, P.normalize, sms, st));
+        if (vgrid) {
+            // densities descending, equal densities in node order: a stable sort of ~bits(density)
+            SortBuffers vs{};
+            vs.keys[0] = pp.vkeys0.as<uint32_t>();
+            vs.keys[1] = pp.vkeys1.as<uint32_t>();
+            vs.vals[0] = pp.vvals0.as<uint32_t>();
+            vs.vals[1] = pp.vvals1.as<uint32_t>();
+            vs.hist = hist.as<uint32_t>();
+            vs.status = status.as<uint32_t>();
+            vs.err = &fs->error;
+            P2V_CUDA_TRY(launch_sort(vs, (uint32_t) V, 0xFFFFFFFFu, sms, st));
+            vg_order = vs.vals[vs.result];
+        }
     } else {
         P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume,
                                      st));
@@ -674,6 +712,13 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     job.keys = skeys;
     job.nbins = g.nbins;
     job.components = comps;
+    job.vg_order = vg_order;
+    for (int a = 0; a < 3; ++a) {
+        job.vg_geo.minf[a] = g.minf[a];
+        job.vg_geo.hf[a] = g.hf[a];
+        job.vg_geo.res[a] = res[a];
+    }
+    job.vg_geo.normalize = P.normalize ? 1 : 0;
     job.h_out = h_out;
     job.timed = timed;
     return P2V_OK;
@@ -692,6 +737,18 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
     const FrameScalars& hs = *job.h_out;
     last_grid = dgrid;
     last_order = job.order;
+    // the vector grid: ParticlesToDensity.cpp:306-323 (global radius = bbox width / sizex / 5) and :358-377
+    // (column ranges: the bbox, [-1, 1] for the directions, the published density range)
+    pp.vg_order = job.vg_order;
+    pp.vg_geo = job.vg_geo;
+    pp.vg_count = job.vg_order ? job.h_out->vcount : 0u;
+    std::memcpy(pp.vg_bbox, bb, sizeof(pp.vg_bbox));
+    {
+        const float w = bb[3] > bb[0] ? bb[3] - bb[0] : bb[0] - bb[3];
+        pp.vg_radius = w / static_cast<float>(res[0]) / 5.0f;
+    }
+    pp.vg_range[0] = job.h_out->out_min;
+    pp.vg_range[1] = job.h_out->out_max;
     pp.last_keys = job.keys;
     pp.last_n = (uint32_t) job.N;
     pp.last_nbins = job.nbins;
@@ -1287,6 +1344,7 @@ void p2v_params_default(p2v_params* p) {
     p->aos_eval_fac = 1.0f;
     p->batch_lanes = 0;
     p->batch_graph = 1;
+    p->vector_grid = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {
@@ -1506,6 +1564,68 @@ p2v_status p2v_get_binning(p2v_ctx* c, uint32_t* keys, uint32_t* order, uint64_t
                        cudaMemcpyDeviceToHost);
     if (e != cudaSuccess)
         return c->fail(P2V_ECUDA, "binning copy failed: %s", cudaGetErrorString(e));
+    return P2V_OK;
+}
+
+p2v_status p2v_get_vector_grid(p2v_ctx* c, float* positions, float* directions, float* colours, float* info,
+                               uint64_t capacity, int32_t mem, p2v_vector_grid_info* meta) {
+    if (!c)
+        return P2V_EINVAL;
+    Pipe& pp = c->main;
+    if (!pp.vg_order)
+        return c->fail(P2V_EINVAL, "no vector grid: run a frame with aggregator 2 and vector_grid set");
+    const uint32_t n = pp.vg_count;
+    if (meta) {
+        meta->count = n;
+        meta->global_radius = pp.vg_radius;
+        for (int a = 0; a < 3; ++a) {  // vislib Cuboid Left/Right, Bottom/Top, Back/Front
+            meta->col_min[a] = pp.vg_bbox[a];
+            meta->col_max[a] = pp.vg_bbox[a + 3];
+            meta->col_min[3 + a] = -1.0f;
+            meta->col_max[3 + a] = 1.0f;
+        }
+        meta->col_min[6] = pp.vg_range[0];
+        meta->col_max[6] = pp.vg_range[1];
+    }
+    if (!positions && !directions && !colours && !info)
+        return P2V_OK;
+    if (capacity < n)
+        return c->fail(P2V_EINVAL, "capacity %llu < %u grid entries", (unsigned long long) capacity, n);
+    if (mem != P2V_MEM_HOST && mem != P2V_MEM_DEVICE)
+        return c->fail(P2V_EINVAL, "mem must be P2V_MEM_HOST or P2V_MEM_DEVICE");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "vector grid: %s", cudaGetErrorString(e));
+    if (n == 0)
+        return P2V_OK;
+    float* d_out[4] = {positions, directions, colours, info};
+    const int width[4] = {3, 3, 1, 7};
+    if (mem == P2V_MEM_HOST) {  // staged in device memory, then copied
+        uint64_t off = 0;
+        uint64_t offs[4];
+        for (int k = 0; k < 4; ++k) {
+            offs[k] = off;
+            if (d_out[k])
+                off += (uint64_t) width[k] * n;
+        }
+        e = pp.vout.ensure(sizeof(float) * off);
+        if (e != cudaSuccess)
+            return c->fail(P2V_ENOMEM, "vector grid staging: %s", cudaGetErrorString(e));
+        for (int k = 0; k < 4; ++k)
+            d_out[k] = d_out[k] ? pp.vout.as<float>() + offs[k] : nullptr;
+    }
+    e = launch_vector_grid(pp.vg_order, pp.vdens.as<float>(), pp.vdirs.as<float>(), pp.scal.as<FrameScalars>(),
+                           pp.vg_geo, n, d_out[0], d_out[1], d_out[2], d_out[3], c->sms, 0);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    float* h_out[4] = {positions, directions, colours, info};
+    for (int k = 0; k < 4 && e == cudaSuccess && mem == P2V_MEM_HOST; ++k)
+        if (h_out[k])
+            e = cudaMemcpy(h_out[k], d_out[k], sizeof(float) * width[k] * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "vector grid: %s", cudaGetErrorString(e));
     return P2V_OK;
 }
 

@@ -42,6 +42,7 @@ struct FrameScalars {
     uint32_t ao_fallback;   // learned AO: particles handed to the cone march
     uint32_t wmax_bits;     // float bits of the largest |weight| (intensity / vector aggregators)
     uint32_t dmin_bits, dmax_bits;  // vector aggregator: density range (float bits, densities >= 0)
+    uint32_t vcount;        // vector aggregator: nodes with a non-zero density
     double mass;            // FP64 sum of the raw grid
     float vmin, vmax;       // raw grid min / max
     float out_min, out_max; // after normalisation

@@ -77,8 +77,28 @@ cudaError_t launch_pack_weights(const WeightSource& src, int nc, float* w, Frame
 cudaError_t launch_permute_weights(const uint32_t* order, const float* win, float* wout, uint32_t n, int nc, int sms,
                                    cudaStream_t st);
 // vol3 /= weight sums, density range into fs, normalisation constants (ParticlesToDensity.cpp:628-682)
+// The vector aggregator's outParticles / outInfo grid: per node the density, the unit direction and the sort
+// key ~bits(density) (descending densities in a stable ascending sort) with the node index as value.
+struct VectorGridBufs {
+    float* dens;       // V
+    float* dirs;       // 3 V
+    uint32_t* keys;    // V
+    uint32_t* vals;    // V
+};
+// Node positions of the grid: min + h * index in float (ParticlesToDensity.cpp:436-456).
+struct VectorGridGeo {
+    float minf[3], hf[3];
+    int32_t res[3];
+    int normalize;
+};
+// vg == nullptr: the volume only; otherwise also the grid buffers and fs->vcount (non-zero densities).
 cudaError_t launch_vector_finish(float* vol3, const float* wsum, int64_t V, FrameScalars* fs, int minmax_normalize,
-                                 int sms, cudaStream_t st);
+                                 int sms, cudaStream_t st, const VectorGridBufs* vg = nullptr);
+// The first `count` entries of the sorted grid into positions (3), directions (3), colours (1) and info rows
+// (7); any output may be null.
+cudaError_t launch_vector_grid(const uint32_t* order, const float* dens, const float* dirs, const FrameScalars* fs,
+                               const VectorGridGeo& geo, uint32_t count, float* pos, float* dir, float* col, float* info,
+                               int sms, cudaStream_t st);
 
 size_t gather_smem_bytes(const GatherConfig& c);
 cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4* rec_a, const int4* rec_b,

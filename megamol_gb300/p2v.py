@@ -54,7 +54,7 @@ class Params(C.Structure):
         ("aos_sizex", C.c_int32), ("aos_sizey", C.c_int32), ("aos_sizez", C.c_int32),
         ("aos_step_len", C.c_float), ("aos_gen_fac", C.c_float), ("aos_eval_fac", C.c_float),
         ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("tile_z", C.c_int32),
-        ("batch_lanes", C.c_int32), ("batch_graph", C.c_int32),
+        ("batch_lanes", C.c_int32), ("batch_graph", C.c_int32), ("vector_grid", C.c_int32),
     ]
 
 
@@ -78,6 +78,11 @@ class MmpldListInfoC(C.Structure):
 class FrameC(C.Structure):
     _fields_ = [("bbox", C.c_float * 6), ("clipbox", C.c_float * 6), ("frame_id", C.c_uint32),
                 ("list_count", C.c_uint32), ("lists", C.POINTER(ParticleListC))]
+
+
+class VectorGridInfoC(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("global_radius", C.c_float), ("col_min", C.c_float * 7),
+                ("col_max", C.c_float * 7)]
 
 
 class BatchItemC(C.Structure):
@@ -143,6 +148,8 @@ _SIGNATURES = {
     "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
                           C.c_int),
+    "p2v_get_vector_grid": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32,
+                             C.c_void_p], C.c_int),
     "p2v_get_binning": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
                          C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)], C.c_int),
     "p2v_get_stats": ([C.c_void_p, C.POINTER(StatsC)], C.c_int),
@@ -481,6 +488,21 @@ class Context:
                                              start.ctypes.data, start.size, None, None))
         return keys, order, start
 
+    def vector_grid(self) -> dict:
+        """The vector aggregator's outParticles / outInfo grid of the last frame (aggregator 2 with
+        vector_grid): positions (n, 3), directions (n, 3), colours (n,), info (n, 7), global_radius and the
+        7 columns' col_min / col_max."""
+        meta = VectorGridInfoC()
+        self._check(self.lib.p2v_get_vector_grid(self.h, None, None, None, None, 0, MEM_HOST, C.byref(meta)))
+        n = int(meta.count)
+        pos, dr = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)
+        col, info = np.empty(n, np.float32), np.empty((n, 7), np.float32)
+        self._check(self.lib.p2v_get_vector_grid(self.h, pos.ctypes.data, dr.ctypes.data, col.ctypes.data,
+                                                 info.ctypes.data, n, MEM_HOST, C.byref(meta)))
+        return dict(count=n, positions=pos, directions=dr, colours=col, info=info,
+                    global_radius=float(meta.global_radius), col_min=np.array(meta.col_min[:], np.float32),
+                    col_max=np.array(meta.col_max[:], np.float32))
+
     def ao_volume(self, level: int = 0) -> np.ndarray:
         """Level `level` of the last cone-march pyramid as a (z, y, x) float32 host array."""
         dims = (C.c_int32 * 3)()
@@ -509,9 +531,12 @@ class ParticlesToDensity:
         return getattr(self.ctx.get_params(), name)
 
     def get_data(self, lists: Sequence[ParticleList], bbox, clipbox=None, out=None):
-        """VolumetricDataCall GET_DATA: returns (volume, metadata). The volume is a (z, y, x) float32 array
-        (or the given `out`)."""
+        """VolumetricDataCall GET_DATA: returns (volume, metadata). The volume is a (z, y, x) float32 array,
+        (z, y, x, 3) for the vector aggregator (or the given `out`)."""
         p = self.ctx.get_params()
+        comps = 3 if p.aggregator == 2 else 1
+        if p.aggregator == 2 and not p.vector_grid:
+            self.ctx.set_params(vector_grid=1)  # the outParticles / outInfo grid, as the reference always builds
         res = [p.sizex, p.sizey, p.sizez]
         host_out = out
         if out is None:
@@ -519,14 +544,34 @@ class ParticlesToDensity:
                 # the resolution is only known after the box adjustment: compute into the device buffer
                 meta = self.ctx.run_frame(lists, bbox, None, clipbox)
                 res = meta["resolution"]
-                host_out = np.empty(res[2] * res[1] * res[0], np.float32)
+                host_out = np.empty(res[2] * res[1] * res[0] * comps, np.float32)
                 meta = self.ctx.run_frame(lists, bbox, host_out, clipbox)
                 self.metadata = meta
-                return host_out.reshape(res[2], res[1], res[0]), meta
-            host_out = np.empty(res[2] * res[1] * res[0], np.float32)
+                return self._shape(host_out, res, comps), meta
+            host_out = np.empty(res[2] * res[1] * res[0] * comps, np.float32)
         meta = self.ctx.run_frame(lists, bbox, host_out, clipbox)
         self.metadata = meta
         if isinstance(host_out, np.ndarray):
-            r = meta["resolution"]
-            return host_out.reshape(r[2], r[1], r[0]), meta
+            return self._shape(host_out, meta["resolution"], comps), meta
         return host_out, meta
+
+    @staticmethod
+    def _shape(a, r, comps):
+        return a.reshape(r[2], r[1], r[0]) if comps == 1 else a.reshape(r[2], r[1], r[0], comps)
+
+    def get_particles(self) -> dict:
+        """The "outParticles" MultiParticleDataCall of the vector aggregator after get_data
+        (ParticlesToDensity.cpp:306-323): one list of grid nodes with VERTDATA_FLOAT_XYZ positions,
+        DIRDATA_FLOAT_XYZ directions, COLDATA_FLOAT_I colours and the global radius."""
+        g = self.ctx.vector_grid()
+        return dict(count=g["count"], vertex=g["positions"], directions=g["directions"], colours=g["colours"],
+                    global_radius=g["global_radius"])
+
+    COLUMNS = ("PositionX", "PositionY", "PositionZ", "VelocityX", "VelocityY", "VelocityZ", "VelocityMag")
+
+    def get_info(self):
+        """The "outInfo" TableDataCall of the vector aggregator after get_data (ParticlesToDensity.cpp:
+        325-380): (columns as (name, minimum, maximum), rows (n, 7))."""
+        g = self.ctx.vector_grid()
+        cols = [(nm, float(g["col_min"][k]), float(g["col_max"][k])) for k, nm in enumerate(self.COLUMNS)]
+        return cols, g["info"]

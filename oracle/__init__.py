@@ -208,6 +208,11 @@ class _RefResult(C.Structure):
                 ("max_value", C.c_double), ("millis", C.c_double), ("needed_floats", C.c_uint64)]
 
 
+class _RefVGrid(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("info_cols", C.c_uint64), ("global_radius", C.c_float),
+                ("col_min", C.c_float * 7), ("col_max", C.c_float * 7)]
+
+
 def reference_available() -> bool:
     return os.path.exists(REF_SO)
 
@@ -221,17 +226,15 @@ def ref():
         _ref.ref_p2d_run.argtypes = [C.POINTER(_RefList), C.c_int, C.POINTER(C.c_float), C.POINTER(_RefParams),
                                      C.c_void_p, C.c_uint64, C.POINTER(_RefResult)]
         _ref.ref_p2d_run.restype = C.c_int
+        _ref.ref_p2d_run_vector.argtypes = [C.POINTER(_RefList), C.c_int, C.POINTER(C.c_float),
+                                            C.POINTER(_RefParams), C.c_void_p, C.c_uint64, C.POINTER(_RefResult),
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                            C.POINTER(_RefVGrid)]
+        _ref.ref_p2d_run_vector.restype = C.c_int
     return _ref
 
 
-def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0, aggregator=0,
-                      surface=False):
-    """Run MegaMol's ParticlesToDensity once.
-
-    ``lists`` is a sequence of dicts with keys ``type`` (VertexDataType), ``data`` (numpy array whose
-    bytes are the vertex records), ``stride`` (bytes, 0 = packed), ``radius`` (global radius), ``count``
-    and optionally ``icol`` / ``dir``. Returns (volume (z,y,x) float32, metadata dict).
-    """
+def _ref_lists(lists):
     keep = []
     arr = (_RefList * max(1, len(lists)))()
     for i, L in enumerate(lists):
@@ -248,6 +251,18 @@ def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma
         arr[i] = _RefList(int(L["type"]), data.ctypes.data, int(L.get("stride", 0)), float(L.get("radius", 0.5)),
                           int(L["count"]), icol.ctypes.data if icol is not None else None,
                           dr.ctypes.data if dr is not None else None)
+    return arr, keep
+
+
+def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0, aggregator=0,
+                      surface=False):
+    """Run MegaMol's ParticlesToDensity once.
+
+    ``lists`` is a sequence of dicts with keys ``type`` (VertexDataType), ``data`` (numpy array whose
+    bytes are the vertex records), ``stride`` (bytes, 0 = packed), ``radius`` (global radius), ``count``
+    and optionally ``icol`` / ``dir``. Returns (volume (z,y,x) float32, metadata dict).
+    """
+    arr, keep = _ref_lists(lists)
     prm = _RefParams(int(aggregator), int(res[0]), int(res[1]), int(res[2]), int(bool(cyclic[0])),
                      int(bool(cyclic[1])), int(bool(cyclic[2])), int(bool(normalize)), int(bool(surface)),
                      float(sigma))
@@ -271,6 +286,61 @@ def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma
                 extents=list(res_out.extents), min_value=res_out.min_value, max_value=res_out.max_value,
                 millis=res_out.millis)
     return vol, meta
+
+
+def reference_vector_grid(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0):
+    """The vector aggregator's outParticles and outInfo outputs of MegaMol's ParticlesToDensity
+    (ParticlesToDensity.cpp:306-380, 628-727): dict with positions (n, 3), directions (n, 3), colours (n,),
+    info (n, 7), global_radius, col_min / col_max (7 each), and the volume."""
+    arr, keep = _ref_lists(lists)
+    prm = _RefParams(2, int(res[0]), int(res[1]), int(res[2]), int(bool(cyclic[0])), int(bool(cyclic[1])),
+                     int(bool(cyclic[2])), int(bool(normalize)), 0, float(sigma))
+    bb = (C.c_float * 6)(*[float(v) for v in bbox])
+    res_out, vg = _RefResult(), _RefVGrid()
+    V = int(res[0]) * int(res[1]) * int(res[2])
+    vol = np.zeros(3 * V, np.float32)
+    pos, dr, col, info = (np.zeros(3 * V, np.float32), np.zeros(3 * V, np.float32), np.zeros(V, np.float32),
+                          np.zeros(7 * V, np.float32))
+    rc = ref().ref_p2d_run_vector(arr, len(lists), bb, C.byref(prm), vol.ctypes.data, vol.size, C.byref(res_out),
+                                  pos.ctypes.data, dr.ctypes.data, col.ctypes.data, info.ctypes.data, V,
+                                  C.byref(vg))
+    if rc != 0:
+        raise RuntimeError(f"reference ParticlesToDensity failed (rc={rc})")
+    n = int(vg.count)
+    return dict(volume=vol.reshape(int(res[2]), int(res[1]), int(res[0]), 3), count=n,
+                positions=pos[:3 * n].reshape(n, 3), directions=dr[:3 * n].reshape(n, 3), colours=col[:n],
+                info=info[:7 * n].reshape(n, 7), global_radius=float(vg.global_radius),
+                col_min=np.array(vg.col_min[:], np.float32), col_max=np.array(vg.col_max[:], np.float32),
+                min_value=res_out.min_value, max_value=res_out.max_value)
+
+
+def vector_grid_f32(v3, bbox, res, normalize):
+    """The vector aggregator's compacted grid (ParticlesToDensity.cpp:436-456, 628-668, 685-727) from the
+    finished, not normalised direction volume v3 (z, y, x, 3) in float32: per node the position
+    min + h * x, the density |v|, the unit direction v / |v| (0 where |v| = 0) and the colour
+    (|v| - min) / (max - min); the nodes with |v| > 0 sorted by |v| descending, equal densities in node
+    order (a stable sort); info rows (position, direction, colour if normalize else |v|). numpy float32
+    arithmetic rounds every operation as the reference's float code does."""
+    f = np.float32
+    v = np.ascontiguousarray(v3, f).reshape(-1, 3)
+    d = np.sqrt(v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2])
+    with np.errstate(invalid="ignore", divide="ignore"):
+        dirs = np.where(d[:, None] == 0, f(0), v / np.where(d == 0, f(1), d)[:, None]).astype(f)
+    mx = max(f(0), d.max()) if d.size else f(0)
+    mn = min(f(np.finfo(f).max), d.min()) if d.size else f(np.finfo(f).max)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        col = ((d - mn) / (mx - mn)).astype(f)
+    h = [f(abs(f(bbox[a + 3]) - f(bbox[a]))) / f(res[a] - 1) for a in range(3)]
+    z, y, x = np.meshgrid(np.arange(res[2]), np.arange(res[1]), np.arange(res[0]), indexing="ij")
+    pos = np.stack([f(bbox[0]) + h[0] * x.ravel().astype(f), f(bbox[1]) + h[1] * y.ravel().astype(f),
+                    f(bbox[2]) + h[2] * z.ravel().astype(f)], axis=1).astype(f)
+    order = np.argsort(-d, kind="stable")
+    n = int(np.count_nonzero(d != 0))
+    order = order[:n]
+    info = np.column_stack([pos[order], dirs[order], col[order] if normalize else d[order]]).astype(f)
+    return dict(count=n, positions=pos[order], directions=dirs[order], colours=col[order], info=info,
+                order=order, min=mn, max=mx,
+                global_radius=f(f(abs(f(bbox[3]) - f(bbox[0]))) / f(res[0])) / f(5))
 
 
 # ------------------------------------------------------------------------------------------------

@@ -11,6 +11,7 @@
 #include <memory>
 
 #include "ParticlesToDensity.h"
+#include "datatools/table/TableDataCall.h"
 #include "mmcore/param/BoolParam.h"
 #include "mmcore/param/EnumParam.h"
 #include "mmcore/param/FloatParam.h"
@@ -58,12 +59,30 @@ struct ref_p2d_result {
     uint64_t needed_floats;
 };
 
-// Runs the reference module once. `out` receives the volume when `out_cap` floats suffice; the
-// call returns 0 on success, 1 if the module reported failure, 2 if `out_cap` was too small (the
-// result then holds the required size in needed_floats).
-int ref_p2d_run(const ref_p2d_list* lists, int n_lists, const float bbox[6], const ref_p2d_params* prm,
-    float* out, uint64_t out_cap, ref_p2d_result* res) {
-    auto mod = std::make_unique<datatools::ParticlesToDensity>();
+struct ref_p2d_vgrid {
+    uint64_t count;       // entries of the outParticles list / rows of the outInfo table
+    uint64_t info_cols;
+    float global_radius;  // outParticles' global radius
+    float col_min[7], col_max[7];
+};
+
+} // extern "C"
+
+namespace {
+
+// One configured module with its input call; both live until the session ends, as in a MegaMol graph.
+struct Session {
+    std::unique_ptr<datatools::ParticlesToDensity> mod;
+    geocalls::MultiParticleDataCall mpdc;
+    ~Session() {
+        if (mod)
+            mod->Release();
+    }
+};
+
+void setup(Session& S, const ref_p2d_list* lists, int n_lists, const float bbox[6], const ref_p2d_params* prm) {
+    S.mod = std::make_unique<datatools::ParticlesToDensity>();
+    auto& mod = S.mod;
     mod->Create();
     set_param<core::param::EnumParam>(*mod, "aggregator", prm->aggregator);
     set_param<core::param::IntParam>(*mod, "sizex", prm->sizex);
@@ -76,7 +95,7 @@ int ref_p2d_run(const ref_p2d_list* lists, int n_lists, const float bbox[6], con
     set_param<core::param::FloatParam>(*mod, "sigma", prm->sigma);
     set_param<core::param::BoolParam>(*mod, "forSurfaceReconstruction", prm->surface != 0);
 
-    geocalls::MultiParticleDataCall mpdc;
+    auto& mpdc = S.mpdc;
     mpdc.SetParticleListCount(static_cast<unsigned int>(n_lists));
     for (int i = 0; i < n_lists; ++i) {
         auto& p = mpdc.AccessParticles(static_cast<unsigned int>(i));
@@ -91,11 +110,14 @@ int ref_p2d_run(const ref_p2d_list* lists, int n_lists, const float bbox[6], con
     }
     mpdc.AccessBoundingBoxes().SetObjectSpaceBBox(bbox[0], bbox[1], bbox[2], bbox[3], bbox[4], bbox[5]);
     mpdc.AccessBoundingBoxes().SetObjectSpaceClipBox(bbox[0], bbox[1], bbox[2], bbox[3], bbox[4], bbox[5]);
-
     auto* in = dynamic_cast<core::CallerSlot*>(mod->FindSlot("inData"));
     in->ConnectCall(&mpdc);
-    auto* outSlot = dynamic_cast<core::CalleeSlot*>(mod->FindSlot("outData"));
+}
 
+// GET_DATA on "outData" (ParticlesToDensity.cpp:94-112,210-304); returns 0, 1 (module failure) or 2 (out_cap
+// too small).
+int get_volume(Session& S, float* out, uint64_t out_cap, ref_p2d_result* res) {
+    auto* outSlot = dynamic_cast<core::CalleeSlot*>(S.mod->FindSlot("outData"));
     geocalls::VolumetricDataCall vdc;
     vdc.SetFrameID(0);
     auto t0 = std::chrono::steady_clock::now();
@@ -104,7 +126,6 @@ int ref_p2d_run(const ref_p2d_list* lists, int n_lists, const float bbox[6], con
     auto t1 = std::chrono::steady_clock::now();
     if (!ok)
         return 1;
-
     const auto* md = vdc.GetMetadata();
     std::memset(res, 0, sizeof(*res));
     for (int a = 0; a < 3; ++a) {
@@ -121,7 +142,65 @@ int ref_p2d_run(const ref_p2d_list* lists, int n_lists, const float bbox[6], con
     if (res->needed_floats > out_cap)
         return 2;
     std::memcpy(out, vdc.GetData(), res->needed_floats * sizeof(float));
-    mod->Release();
+    return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+// Runs the reference module once. `out` receives the volume when `out_cap` floats suffice; the
+// call returns 0 on success, 1 if the module reported failure, 2 if `out_cap` was too small (the
+// result then holds the required size in needed_floats).
+int ref_p2d_run(const ref_p2d_list* lists, int n_lists, const float bbox[6], const ref_p2d_params* prm,
+    float* out, uint64_t out_cap, ref_p2d_result* res) {
+    Session S;
+    setup(S, lists, n_lists, bbox, prm);
+    return get_volume(S, out, out_cap, res);
+}
+
+// The vector aggregator's two extra outputs after the volume: GET_DATA on "outParticles" (the compacted
+// grid as a particle list: positions, directions, colours; ParticlesToDensity.cpp:306-323) and on "outInfo"
+// (the 7-column table; :325-380). Entries are copied when `cap` suffices (return 3 otherwise, with the
+// count in vg).
+int ref_p2d_run_vector(const ref_p2d_list* lists, int n_lists, const float bbox[6], const ref_p2d_params* prm,
+    float* out, uint64_t out_cap, ref_p2d_result* res, float* pos, float* dir, float* col, float* info,
+    uint64_t cap, ref_p2d_vgrid* vg) {
+    Session S;
+    setup(S, lists, n_lists, bbox, prm);
+    const int rc = get_volume(S, out, out_cap, res);
+    if (rc != 0)
+        return rc;
+    std::memset(vg, 0, sizeof(*vg));
+    geocalls::MultiParticleDataCall grid;
+    grid.SetFrameID(0);
+    auto* ps = dynamic_cast<core::CalleeSlot*>(S.mod->FindSlot("outParticles"));
+    if (!ps->InCall(geocalls::MultiParticleDataCall::ClassName(), geocalls::MultiParticleDataCall::FunctionName(0),
+            grid))
+        return 1;
+    datatools::table::TableDataCall table;
+    auto* ts = dynamic_cast<core::CalleeSlot*>(S.mod->FindSlot("outInfo"));
+    if (!ts->InCall(datatools::table::TableDataCall::ClassName(), datatools::table::TableDataCall::FunctionName(0),
+            table))
+        return 1;
+    const auto& p = grid.AccessParticles(0);
+    vg->count = p.GetCount();
+    vg->global_radius = p.GetGlobalRadius();
+    vg->info_cols = table.GetColumnsCount();
+    for (size_t c = 0; c < 7 && c < table.GetColumnsCount(); ++c) {
+        vg->col_min[c] = table.GetColumnsInfos()[c].MinimumValue();
+        vg->col_max[c] = table.GetColumnsInfos()[c].MaximumValue();
+    }
+    if (table.GetRowsCount() != vg->count)
+        return 1;
+    if (vg->count > cap)
+        return 3;
+    if (vg->count > 0) {
+        std::memcpy(pos, p.GetVertexData(), vg->count * 3 * sizeof(float));
+        std::memcpy(dir, p.GetDirData(), vg->count * 3 * sizeof(float));
+        std::memcpy(col, p.GetColourData(), vg->count * sizeof(float));
+        std::memcpy(info, table.GetData(), vg->count * table.GetColumnsCount() * sizeof(float));
+    }
     return 0;
 }
 

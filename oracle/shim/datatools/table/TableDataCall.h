@@ -30,6 +30,15 @@ public:
             max_ = v;
             return *this;
         }
+        const std::string& Name() const {
+            return name_;
+        }
+        float MinimumValue() const {
+            return min_;
+        }
+        float MaximumValue() const {
+            return max_;
+        }
 
     private:
         std::string name_;
@@ -52,6 +61,18 @@ public:
     }
     void SetDataHash(size_t h) {
         hash_ = h;
+    }
+    size_t GetColumnsCount() const {
+        return cols_;
+    }
+    size_t GetRowsCount() const {
+        return rows_;
+    }
+    const ColumnInfo* GetColumnsInfos() const {
+        return infos_;
+    }
+    const float* GetData() const {
+        return data_;
     }
     void SetUnlocker(void*, bool = true) {}
     void SetFrameCount(unsigned int n) {

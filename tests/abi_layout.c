@@ -11,11 +11,12 @@
 int main(void) {
     printf("{");
     S(p2v_params); S(p2v_particle_list); S(p2v_frame); S(p2v_volume); S(p2v_stats);
-    S(p2v_batch_item); S(p2v_tune_report); S(p2v_mmpld_info); S(p2v_mmpld_list_info);
+    S(p2v_batch_item); S(p2v_tune_report); S(p2v_mmpld_info); S(p2v_mmpld_list_info); S(p2v_vector_grid_info);
+    F(p2v_vector_grid_info, global_radius); F(p2v_vector_grid_info, col_max);
     F(p2v_particle_list, colour_type); F(p2v_particle_list, colour_data); F(p2v_particle_list, global_colour);
     F(p2v_mmpld_info, clipbox); F(p2v_mmpld_list_info, bbox); F(p2v_mmpld_list_info, clusters);
     F(p2v_params, sigma); F(p2v_params, kernel); F(p2v_params, ao_mode); F(p2v_params, aos_eval_fac);
-    F(p2v_params, tile_z); F(p2v_params, batch_graph);
+    F(p2v_params, tile_z); F(p2v_params, batch_graph); F(p2v_params, vector_grid);
     F(p2v_batch_item, volume); F(p2v_batch_item, size);
     F(p2v_tune_report, ms_best); F(p2v_tune_report, cand_lanes); F(p2v_tune_report, cand_ms);
     F(p2v_particle_list, count); F(p2v_particle_list, mem); F(p2v_particle_list, ao_out);

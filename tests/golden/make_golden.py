@@ -5,7 +5,8 @@ Runs the reference's unmodified plugins/datatools/src/ParticlesToDensity.cpp (co
 parameters and the reference output as ``tests/golden/p2d_<case>.npz``. The reference tree exists only
 on the development machine, so the fixtures are committed and the GPU tests read them from here.
 
-Usage:  python tests/golden/make_golden.py        (OMP_NUM_THREADS is forced to 1: the reference's
+Usage:  python tests/golden/make_golden.py [prefix]   (only the fixtures whose name starts with prefix;
+        OMP_NUM_THREADS is forced to 1: the reference's
         float sums then run in particle order, the order the CPU restatement reproduces bit-exactly)
 """
 from __future__ import annotations
@@ -108,9 +109,11 @@ def agg_cases():
     return out
 
 
-def main():
+def main(only=None):
     oracle.build(with_reference=True)
     for name, c in agg_cases().items():
+        if only and not f"agg_{name}".startswith(only):
+            continue
         vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"],
                                              aggregator=c["aggregator"])
         d = dict(aggregator=np.int32(c["aggregator"]), bbox=np.array(c["bbox"], np.float32),
@@ -118,6 +121,15 @@ def main():
                  normalize=np.int32(c["normalize"]), sigma=np.float32(c["sigma"]), nlists=np.int32(len(c["lists"])),
                  volume=vol, components=np.int32(meta["components"]), min_value=np.float64(meta["min_value"]),
                  max_value=np.float64(meta["max_value"]))
+        if c["aggregator"] == 2:
+            # the outParticles / outInfo outputs of the vector aggregator (ParticlesToDensity.cpp:306-380)
+            vg = oracle.reference_vector_grid(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"],
+                                              c["sigma"])
+            assert np.array_equal(vg["volume"], vol)
+            for k in ("positions", "directions", "colours", "info", "col_min", "col_max"):
+                d[f"vg_{k}"] = vg[k]
+            d["vg_count"] = np.int64(vg["count"])
+            d["vg_radius"] = np.float32(vg["global_radius"])
         for i, L in enumerate(c["lists"]):
             d[f"l{i}_type"] = np.int32(L["type"])
             d[f"l{i}_data"] = np.ascontiguousarray(L["data"])
@@ -132,6 +144,8 @@ def main():
         np.savez_compressed(path, **d)
         print(f"{path}: volume {vol.shape} range [{vol.min():.6g}, {vol.max():.6g}]")
     for name, c in cases().items():
+        if only and not f"p2d_{name}".startswith(only):
+            continue
         vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"])
         d = dict(bbox=np.array(c["bbox"], np.float32), res=np.array(c["res"], np.int32),
                  cyclic=np.array(c["cyclic"], np.int32), normalize=np.int32(c["normalize"]),
@@ -150,4 +164,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

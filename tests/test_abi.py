@@ -52,7 +52,7 @@ def test_struct_layout_matches_header(tmp_path):
     types = {"p2v_params": p2v.Params, "p2v_particle_list": p2v.ParticleListC, "p2v_frame": p2v.FrameC,
              "p2v_volume": p2v.VolumeC, "p2v_stats": p2v.StatsC, "p2v_batch_item": p2v.BatchItemC,
              "p2v_tune_report": p2v.TuneReportC, "p2v_mmpld_info": p2v.MmpldInfoC,
-             "p2v_mmpld_list_info": p2v.MmpldListInfoC}
+             "p2v_mmpld_list_info": p2v.MmpldListInfoC, "p2v_vector_grid_info": p2v.VectorGridInfoC}
     for k, v in lay.items():
         if k == "end":
             continue
@@ -73,8 +73,8 @@ def test_params_default_mirror_reference_slots(lib):
     # SphereRenderer.cpp:199-212 MDAO defaults
     assert p.ao_cones == 3 and abs(p.ao_apex_deg - 50) < 1e-6 and abs(p.ao_offset - 0.01) < 1e-7
     assert abs(p.ao_cone_length - 0.8) < 1e-7 and p.mdao_volume_size == 128
-    assert p.batch_lanes == 0 and p.batch_graph == 1
-    assert lib.p2v_abi_version() == 3
+    assert p.batch_lanes == 0 and p.batch_graph == 1 and p.vector_grid == 0
+    assert lib.p2v_abi_version() == 4
 
 
 def test_create_without_device_fails_cleanly(lib):

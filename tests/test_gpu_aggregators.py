@@ -168,3 +168,49 @@ def test_aggregators_are_deterministic_and_reject_bad_settings(ctx):
     with pytest.raises(p2v.P2VError):
         ctx.run_frame(p2v_lists(c), [float(v) for v in c["bbox"]], None)
     ctx.set_params(aggregator=0, accumulate=p2v.ACCUM_EXACT)
+
+
+@pytest.mark.parametrize("name", ["ivec_cyclic", "ivec_mixed_norm"])
+def test_vector_grid_outputs(ctx, name):
+    """The vector aggregator's outParticles / outInfo grid (p2v_get_vector_grid). Bit for bit against the
+    float32 restatement applied to the GPU's own direction volume (the finish, the stable descending sort
+    by density and the compaction); against the reference's grid: the same node set up to nodes reached only
+    by tails whose float sums are subnormal, and directions within 2e-3 on nodes of normal weight."""
+    c = load_agg(name)
+    norm = int(c["normalize"])
+    res = [int(v) for v in c["res"]]
+    bbox = [float(v) for v in c["bbox"]]
+    raw = dict(c)
+    raw["normalize"] = np.int32(0)
+    ctx.set_params(vector_grid=1)
+    v3, _ = run(ctx, raw, p2v_lists(c), 2)           # the finished, not normalised volume
+    ctx.set_params(vector_grid=1)
+    run(ctx, c, p2v_lists(c), 2)
+    g = ctx.vector_grid()
+    mine = oracle.vector_grid_f32(v3, bbox, res, norm)
+    assert g["count"] == mine["count"]
+    for k in ("positions", "directions", "colours", "info"):
+        assert np.array_equal(g[k], mine[k]), k
+    assert g["global_radius"] == float(c["vg_radius"])
+    assert np.array_equal(g["col_min"][:6], c["vg_col_min"][:6]) and np.array_equal(g["col_max"][:6],
+                                                                                  c["vg_col_max"][:6])
+    # against the reference module's grid
+    _, w64 = fp64_reference(c, 2)
+    ref_pos = c["vg_positions"]
+    key = lambda p: {tuple(r): i for i, r in enumerate(p.tolist())}
+    gi, ri = key(g["positions"]), key(ref_pos)
+    sub = w64 < np.finfo(np.float32).tiny
+    flat_sub = set(np.flatnonzero(sub.ravel()).tolist())
+    h = [np.float32(abs(np.float32(bbox[a + 3]) - np.float32(bbox[a]))) / np.float32(res[a] - 1) for a in range(3)]
+
+    def node(p):
+        ix = [int(round((p[a] - bbox[a]) / float(h[a]))) for a in range(3)]
+        return ix[0] + (ix[1] + ix[2] * res[1]) * res[0]
+
+    for p in set(gi) ^ set(ri):          # nodes in one grid only: subnormal tails
+        assert node(p) in flat_sub
+    both = [p for p in set(gi) & set(ri) if node(p) not in flat_sub]
+    assert len(both) > 0.5 * len(ri)
+    a = np.array([g["directions"][gi[p]] for p in both])
+    b = np.array([c["vg_directions"][ri[p]] for p in both])
+    assert np.abs(a - b).max() <= 2e-3

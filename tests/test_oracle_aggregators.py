@@ -63,3 +63,34 @@ def test_weighted_fp64_is_linear():
     assert np.allclose(b, 4.0 * a, rtol=1e-12, atol=1e-12)
     ones = oracle.density_weighted(xyzr, np.ones(len(xyzr), np.float32), bbox, res, fp64=True)
     assert np.allclose(ones, oracle.density_f64(xyzr, bbox, res), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["ivec_cyclic", "ivec_mixed_norm"])
+def test_vector_grid_restatement_matches_reference_fixture(name):
+    """The outParticles / outInfo grid of the vector aggregator (ParticlesToDensity.cpp:306-380, 628-727)
+    restated in numpy float32 from the restatement's volume equals, bit for bit, what MegaMol's module
+    produced for the fixture (one OpenMP thread)."""
+    from tests import golden_io as G
+    from tests.test_gpu_aggregators import load_agg
+
+    c = load_agg(name)
+    xyzr = np.concatenate([G.list_to_xyzr(L) for L in c["lists"]])
+    d = np.concatenate([L["dir"] for L in c["lists"]])
+    res = [int(v) for v in c["res"]]
+    bbox = [float(v) for v in c["bbox"]]
+    cyc = [int(v) for v in c["cyclic"]]
+    v3 = oracle.density_weighted(xyzr, d, bbox, res, cyc, float(c["sigma"]))
+    w = oracle.density_f32(xyzr, bbox, res, cyc, float(c["sigma"]))
+    fin, mn, mx = oracle.vector_finish_f32(v3, w, False)
+    g = oracle.vector_grid_f32(fin, bbox, res, int(c["normalize"]))
+    assert g["count"] == int(c["vg_count"])
+    for k in ("positions", "directions", "colours", "info"):
+        assert np.array_equal(g[k], c[f"vg_{k}"]), k
+    assert g["global_radius"] == c["vg_radius"]
+    # the table's column ranges: the box, [-1, 1] for the directions, the published density range
+    assert np.array_equal(c["vg_col_min"][:3], np.float32(bbox[:3])) and np.all(c["vg_col_min"][3:6] == -1)
+    assert np.array_equal(c["vg_col_max"][:3], np.float32(bbox[3:])) and np.all(c["vg_col_max"][3:6] == 1)
+    if int(c["normalize"]):
+        assert (c["vg_col_min"][6], c["vg_col_max"][6]) == (0.0, 1.0)
+    else:
+        assert (c["vg_col_min"][6], c["vg_col_max"][6]) == (np.float32(mn), np.float32(mx))
