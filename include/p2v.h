@@ -283,6 +283,19 @@ P2V_API p2v_status p2v_get_stats(const p2v_ctx* ctx, p2v_stats* st);
 /* Last error message of this context ("" if none); returns the message length. */
 P2V_API size_t p2v_get_last_error(const p2v_ctx* ctx, char* buf, size_t len);
 
+/* ---- dat/raw output ----
+ * Writes a volume as MegaMol's volume::DatRawWriter does (plugins/volume/src/DatRawWriter.cpp:58-186):
+ * <prefix><frame, 4 digits zero-filled>.dat, a text header (ObjectFileName = the raw file's name, Format
+ * FLOAT, GridType EQUIDISTANT, Components, Dimensions 3, TimeSteps 1, ByteOrder LITTLE_ENDIAN, Resolution,
+ * SliceThickness - x, y and y again, as the reference writes it -, Origin, Time = frame), and
+ * <prefix><frame>.raw, the voxels x fastest with interleaved components. vol is a volume p2v_run_frame
+ * described (resolution, components, slice distances, origin); its data in host or device memory per
+ * vol->mem, or vol->data == NULL for the context's device grid of the last frame. A device volume streams
+ * through two pinned buffers, copy and file write overlapped. ctx may be NULL for host data. frame_count > 0
+ * rejects frame >= frame_count as the reference does; the prefix may not be empty or end in '/'. */
+P2V_API p2v_status p2v_write_datraw(p2v_ctx* ctx, const char* prefix, uint32_t frame, uint32_t frame_count,
+                                    const p2v_volume* vol);
+
 /* ---- batched frames ----
  * No counterpart in the reference, whose ParticlesToDensity computes one frame per GET_DATA call. A batch
  * runs many frames (a trajectory's, of uneven particle counts and grid sizes) with the current parameters:

@@ -148,6 +148,7 @@ _SIGNATURES = {
     "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
                           C.c_int),
+    "p2v_write_datraw": ([C.c_void_p, C.c_char_p, C.c_uint32, C.c_uint32, C.c_void_p], C.c_int),
     "p2v_get_vector_grid": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32,
                              C.c_void_p], C.c_int),
     "p2v_get_binning": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
@@ -205,6 +206,26 @@ def _ptr(x) -> tuple[int, int]:
     if hasattr(x, "data_ptr"):
         return x.data_ptr(), (MEM_DEVICE if getattr(x, "is_cuda", False) else MEM_HOST)
     raise TypeError(f"unsupported buffer type {type(x)}")
+
+
+def write_datraw(prefix: str, frame: int, volume, meta: dict, frame_count: int = 0, ctx: "Context" = None) -> None:
+    """Write a volume as MegaMol's DatRawWriter does (plugins/volume/src/DatRawWriter.cpp:58-186):
+    <prefix><frame:04>.dat and .raw. `volume` is a host array, a CUDA tensor, or None for the context's
+    device grid of the last frame; `meta` the metadata dict run_frame returned (resolution, components,
+    slice_dists, origin). frame_count > 0 rejects frames past it, as the reference does."""
+    v = VolumeC()
+    p, mem = _ptr(volume)
+    v.data = p or None
+    v.mem = mem
+    v.capacity = int(volume.size if isinstance(volume, np.ndarray) else (volume.numel() if volume is not None else 0))
+    v.resolution[:] = [int(x) for x in meta["resolution"]]
+    v.components = int(meta.get("components", 1))
+    v.slice_dists[:] = [float(x) for x in meta["slice_dists"]]
+    v.origin[:] = [float(x) for x in meta["origin"]]
+    st = library().p2v_write_datraw(ctx.h if ctx is not None else None, prefix.encode(), int(frame),
+                                    int(frame_count), C.byref(v))
+    if st != OK:
+        raise P2VError(st, f"dat/raw write of {prefix}{int(frame):04d} failed")
 
 
 @dataclass

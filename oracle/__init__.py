@@ -288,6 +288,25 @@ def reference_density(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma
     return vol, meta
 
 
+REF_DATRAW_SO = os.path.join(os.path.dirname(REF_SO), "libref_datraw.so")
+
+
+def reference_write_datraw(prefix, frame, volume, resolution, components, slice_dists, origin, frame_count=1):
+    """Run MegaMol's own volume::DatRawWriter (oracle/_ref/libref_datraw.so) on a float volume; returns
+    True when the module reported success."""
+    lib_ = C.CDLL(REF_DATRAW_SO)
+    lib_.ref_datraw_write.argtypes = [C.c_char_p, C.c_uint, C.c_uint, C.POINTER(C.c_uint64), C.c_uint64, C.c_int,
+                                      C.c_uint64, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p]
+    lib_.ref_datraw_write.restype = C.c_int
+    v = np.ascontiguousarray(volume, np.float32)
+    res = (C.c_uint64 * 3)(*[int(x) for x in resolution])
+    sd = (C.c_float * 3)(*[float(x) for x in slice_dists])
+    org = (C.c_float * 3)(*[float(x) for x in origin])
+    # ScalarType_t FLOATING_POINT = 3, GridType_t CARTESIAN = 1 (VolumetricDataCallTypes.h:16-19)
+    return lib_.ref_datraw_write(prefix.encode(), int(frame), int(frame_count), res, int(components), 3, 4, 1, sd,
+                                 org, v.ctypes.data) == 0
+
+
 def reference_vector_grid(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0):
     """The vector aggregator's outParticles and outInfo outputs of MegaMol's ParticlesToDensity
     (ParticlesToDensity.cpp:306-380, 628-727): dict with positions (n, 3), directions (n, 3), colours (n,),

@@ -12,6 +12,8 @@ namespace megamol::geocalls {
 class VolumetricDataCall : public core::AbstractGetData3DCall {
 public:
     typedef VolumetricMetadata_t Metadata;
+    typedef ScalarType_t ScalarType;
+    typedef GridType_t GridType;
 
     static const unsigned int IDX_GET_EXTENTS = 0;
     static const unsigned int IDX_GET_DATA = 1;
@@ -40,6 +42,13 @@ public:
     }
     const Metadata* GetMetadata() const {
         return meta_;
+    }
+    // VolumetricDataCall.h:245-247 and VolumetricDataCall.cpp:201-211
+    size_t GetVoxelSize() const {
+        return meta_ ? meta_->ScalarLength * meta_->Components : 0;
+    }
+    size_t GetVoxelsPerFrame() const {
+        return meta_ ? meta_->Resolution[0] * meta_->Resolution[1] * meta_->Resolution[2] : 0;
     }
 
 private:

@@ -109,8 +109,37 @@ def agg_cases():
     return out
 
 
+def datraw_cases():
+    """Volumes for MegaMol's DatRawWriter: a scalar grid and a 3-component grid with a five-digit frame."""
+    rng = np.random.default_rng(20241203)
+    return {
+        "scalar": dict(volume=rng.uniform(-1, 5, 5 * 4 * 3).astype(np.float32), resolution=(5, 4, 3), components=1,
+                       slice_dists=(0.787402, 1.2345678, 2.5), origin=(-1.25, 0.0, 3e-7), frame=7, frame_count=10),
+        "vector": dict(volume=rng.normal(size=3 * 2 * 2 * 3).astype(np.float32), resolution=(3, 2, 2), components=3,
+                       slice_dists=(1.0 / 3.0, 1e10, 0.125), origin=(-0.0, 123456.789, -2.5e-12), frame=12345,
+                       frame_count=20000),
+    }
+
+
 def main(only=None):
     oracle.build(with_reference=True)
+    import tempfile
+    for name, c in datraw_cases().items():
+        if only and not f"datraw_{name}".startswith(only):
+            continue
+        with tempfile.TemporaryDirectory() as d:
+            assert oracle.reference_write_datraw(os.path.join(d, "vol_"), c["frame"], c["volume"], c["resolution"],
+                                                 c["components"], c["slice_dists"], c["origin"], c["frame_count"])
+            stem = os.path.join(d, f"vol_{c['frame']:04d}")
+            dat = open(stem + ".dat", "rb").read()
+            raw = open(stem + ".raw", "rb").read()
+        path = os.path.join(HERE, f"datraw_{name}.npz")
+        np.savez_compressed(path, dat=np.frombuffer(dat, np.uint8), raw=np.frombuffer(raw, np.uint8),
+                            volume=c["volume"], resolution=np.array(c["resolution"], np.uint64),
+                            components=np.int64(c["components"]), slice_dists=np.array(c["slice_dists"], np.float32),
+                            origin=np.array(c["origin"], np.float32), frame=np.int64(c["frame"]),
+                            frame_count=np.int64(c["frame_count"]))
+        print(f"{path}: {len(dat)} B header, {len(raw)} B raw")
     for name, c in agg_cases().items():
         if only and not f"agg_{name}".startswith(only):
             continue
