@@ -58,6 +58,9 @@ struct DevBuf {
 };
 
 enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_COUNT };
+// fork/join events of a pipe's side stream: the normals upload runs under binning and density, the grid
+// download under AO
+enum SideEv { SEV_FORK, SEV_NRM, SEV_GRID, SEV_JOIN, SEV_COUNT };
 
 // Scratch of one frame pipeline: every device buffer a frame touches, the stage timing events and the
 // pinned mirror of the frame scalars. A context owns one pipe for p2v_run_frame and one per lane of
@@ -68,8 +71,10 @@ struct Pipe {
     DevBuf vdens, vdirs, vkeys0, vkeys1, vvals0, vvals1, vout;  // the vector aggregator's grid outputs
     StencilTex stex[2];                    // the learned AO's two stencil levels as textures
     cudaEvent_t ev[EV_COUNT] = {};
+    cudaEvent_t sev[SEV_COUNT] = {};
     FrameScalars* h_scal = nullptr;        // pinned mirror of the last frame's scalars
     cudaStream_t stream = nullptr;         // the stream of a batch lane
+    cudaStream_t side = nullptr;           // copies that overlap the frame's kernels
     ConeParams last_cp{};
     const float* last_grid = nullptr;
     const uint32_t* last_order = nullptr;  // sorted position -> particle index of the last frame
@@ -85,6 +90,16 @@ struct Pipe {
     cudaError_t init(bool with_stream) {
         for (auto& e : ev) {
             const cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess)
+                return r;
+        }
+        for (auto& e : sev) {
+            const cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            if (r != cudaSuccess)
+                return r;
+        }
+        {
+            const cudaError_t r = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
             if (r != cudaSuccess)
                 return r;
         }
@@ -104,13 +119,21 @@ struct Pipe {
             b->release();
         stex[0].release();
         stex[1].release();
+        if (side)
+            cudaStreamSynchronize(side);
         for (auto& e : ev)
+            if (e)
+                cudaEventDestroy(e);
+        for (auto& e : sev)
             if (e)
                 cudaEventDestroy(e);
         if (h_scal)
             cudaFreeHost(h_scal);
         if (stream)
             cudaStreamDestroy(stream);
+        if (side)
+            cudaStreamDestroy(side);
+        side = nullptr;
         h_scal = nullptr;
         stream = nullptr;
         last_grid = nullptr;
@@ -514,46 +537,56 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
                 raw_off += (bytes + 15) & ~uint64_t(15);
             }
         }
-        if (timed)
-            if (timed)
-        P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
         P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), vals0.as<uint32_t>(), fs, st));
         off += L.count;
     }
-    if (N == 0)
-        if (timed)
-            if (timed)
+    if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
-    // ---- normals for AO ----
+    // ---- normals for AO, on the side stream: needed only by the AO stage ----
     const bool want_ao = P.ao_mode != P2V_AO_NONE;
+    cudaStream_t side = pp.side;
     if (want_ao) {
         P2V_CUDA_TRY(nrm.ensure(sizeof(float4) * (N + 1)));
         P2V_CUDA_TRY(ao.ensure(sizeof(float) * (N + 1)));
+        // every check before the fork: an error return must not leave work on the side stream
+        uint64_t nbytes = 0;
+        for (uint32_t l = 0; l < fr->list_count; ++l) {
+            const p2v_particle_list& L = fr->lists[l];
+            if (L.vertex_type == P2V_VERTDATA_NONE || L.count == 0)
+                continue;
+            if (L.normals == nullptr)
+                return fail(P2V_EINVAL, "list %u: AO needs per-particle normals", l);
+            const uint32_t ns = L.normal_stride ? L.normal_stride : 12u;
+            if (ns < 12u)
+                return fail(P2V_EINVAL, "list %u: normal stride %u < 12", l, ns);
+            if (L.mem != P2V_MEM_DEVICE)
+                nbytes += (((L.count - 1) * (uint64_t) ns + 12) + 15) & ~uint64_t(15);
+        }
+        if (raw_off + nbytes > raw.bytes)
+            return fail(P2V_EINVAL, "normals larger than the staging buffer");
+        // ordered after everything queued on st so far (the previous frame's AO still reads nrm and raw)
+        P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_FORK], st));
+        P2V_CUDA_TRY(cudaStreamWaitEvent(side, pp.sev[SEV_FORK], 0));
         uint64_t noff = 0;
         for (uint32_t l = 0; l < fr->list_count; ++l) {
             const p2v_particle_list& L = fr->lists[l];
             if (L.vertex_type == P2V_VERTDATA_NONE)
                 continue;
-            if (L.count > 0 && L.normals == nullptr)
-                return fail(P2V_EINVAL, "list %u: AO needs per-particle normals", l);
             if (L.count > 0) {
                 const uint32_t ns = L.normal_stride ? L.normal_stride : 12u;
-                if (ns < 12u)
-                    return fail(P2V_EINVAL, "list %u: normal stride %u < 12", l, ns);
                 const void* src = L.normals;
                 if (L.mem != P2V_MEM_DEVICE) {
                     const uint64_t bytes = (L.count - 1) * (uint64_t) ns + 12;
-                    P2V_CUDA_TRY(raw.ensure(raw_off + bytes + 16));
-                    // raw may have been reallocated: only grow it before any upload is queued
                     uint8_t* dst = raw.as<uint8_t>() + raw_off;
-                    P2V_CUDA_TRY(cudaMemcpyAsync(dst, L.normals, bytes, cudaMemcpyHostToDevice, st));
+                    P2V_CUDA_TRY(cudaMemcpyAsync(dst, L.normals, bytes, cudaMemcpyHostToDevice, side));
                     src = dst;
                     raw_off += (bytes + 15) & ~uint64_t(15);
                 }
-                P2V_CUDA_TRY(launch_pack_normals(src, ns, L.count, noff, nrm.as<float4>(), st));
+                P2V_CUDA_TRY(launch_pack_normals(src, ns, L.count, noff, nrm.as<float4>(), side));
             }
             noff += L.count;
         }
+        P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_NRM], side));
     }
 
     // ---- weights of the intensity / vector aggregators ----
@@ -675,18 +708,29 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     }
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_NORM], st));
+    // the grid is final here and AO only reads it: with AO its download runs on the side stream meanwhile
+    const bool grid_out = vol && vol->data && !direct;
+    const cudaMemcpyKind grid_kind = vol && vol->mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     if (want_ao) {
+        if (grid_out) {
+            P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_GRID], st));
+            P2V_CUDA_TRY(cudaStreamWaitEvent(side, pp.sev[SEV_GRID], 0));
+            P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * VC, grid_kind, side));
+        }
+        P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_JOIN], side));
+        P2V_CUDA_TRY(cudaStreamWaitEvent(st, pp.sev[SEV_NRM], 0));
         const p2v_status as = run_ao(pp, fr, g, dgrid, bb, n, sb.vals[sb.result], st);
-        if (as != P2V_OK)
+        if (as != P2V_OK) {
+            cudaStreamWaitEvent(st, pp.sev[SEV_JOIN], 0);  // no side work left outside st (graph capture)
             return as;
+        }
     }
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_AO], st));
 
     // ---- outputs ----
-    if (vol && vol->data && !direct)
-        P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * VC,
-                                     vol->mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (grid_out && !want_ao)
+        P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * VC, grid_kind, st));
     if (want_ao) {
         uint64_t aoff = 0;
         for (uint32_t l = 0; l < fr->list_count; ++l) {
@@ -700,6 +744,8 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
             aoff += L.count;
         }
     }
+    if (want_ao)
+        P2V_CUDA_TRY(cudaStreamWaitEvent(st, pp.sev[SEV_JOIN], 0));
     P2V_CUDA_TRY(cudaMemcpyAsync(h_out, fs, sizeof(FrameScalars), cudaMemcpyDeviceToHost, st));
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_DOWN], st));
