@@ -375,6 +375,12 @@ P2V_API void p2v_train_params_default(p2v_train_params* tp);
 P2V_API p2v_status p2v_mlp_collect(p2v_ctx* ctx, const p2v_frame* frame, uint32_t max_pairs, uint64_t seed,
                                    uint64_t* total);
 P2V_API p2v_status p2v_mlp_clear(p2v_ctx* ctx);
+/* The collected training pairs in collection order (P2V_MLP_INPUTS features and the cone-march AO per
+ * pair; a pair without features, from a particle with a zero normal, has target -1). *count receives the
+ * number of pairs; x (count x P2V_MLP_INPUTS) and t (count) are host arrays of capacity pairs, each
+ * nullable. With max_pairs >= the frame's binned particles, p2v_mlp_collect takes every particle in the
+ * sorted order of p2v_get_binning. */
+P2V_API p2v_status p2v_mlp_get_pairs(p2v_ctx* ctx, float* x, float* t, uint64_t capacity, uint64_t* count);
 /* Train the MLP on the collected pairs with FP32 forward/backward kernels and Adam. */
 P2V_API p2v_status p2v_mlp_train(p2v_ctx* ctx, const p2v_train_params* tp, p2v_train_report* rep);
 /* Flat binary file: header (magic, version, sizes, seed, Adam step), FP32 parameters, Adam moments,

@@ -1790,6 +1790,28 @@ p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, 
     return P2V_OK;
 }
 
+p2v_status p2v_mlp_get_pairs(p2v_ctx* c, float* x, float* t, uint64_t capacity, uint64_t* count) {
+    if (!c)
+        return P2V_EINVAL;
+    if (count)
+        *count = c->t_pairs;
+    if (!x && !t)
+        return P2V_OK;
+    if (capacity < c->t_pairs)
+        return c->fail(P2V_EINVAL, "capacity %llu < %llu pairs", (unsigned long long) capacity,
+                       (unsigned long long) c->t_pairs);
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && x && c->t_pairs)
+        e = cudaMemcpy(x, c->tX.as<float>(), sizeof(float) * MLP_IN * c->t_pairs, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && t && c->t_pairs)
+        e = cudaMemcpy(t, c->tT.as<float>(), sizeof(float) * c->t_pairs, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return c->fail(P2V_ECUDA, "pairs copy failed: %s", cudaGetErrorString(e));
+    return P2V_OK;
+}
+
 p2v_status p2v_mlp_train(p2v_ctx* c, const p2v_train_params* tp, p2v_train_report* rep) {
     if (!c || !tp)
         return P2V_EINVAL;

@@ -148,6 +148,7 @@ _SIGNATURES = {
     "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
                           C.c_int),
+    "p2v_mlp_get_pairs": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "p2v_write_datraw": ([C.c_void_p, C.c_char_p, C.c_uint32, C.c_uint32, C.c_void_p], C.c_int),
     "p2v_get_vector_grid": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32,
                              C.c_void_p], C.c_int),
@@ -508,6 +509,15 @@ class Context:
         self._check(self.lib.p2v_get_binning(self.h, keys.ctypes.data, order.ctypes.data, keys.size,
                                              start.ctypes.data, start.size, None, None))
         return keys, order, start
+
+    def mlp_pairs(self):
+        """(features (n, 131), targets (n,)) of the collected training pairs, in collection order."""
+        n = C.c_uint64()
+        self._check(self.lib.p2v_mlp_get_pairs(self.h, None, None, 0, C.byref(n)))
+        x = np.empty((n.value, MLP_INPUTS), np.float32)
+        t = np.empty(n.value, np.float32)
+        self._check(self.lib.p2v_mlp_get_pairs(self.h, x.ctypes.data, t.ctypes.data, n.value, None))
+        return x, t
 
     def vector_grid(self) -> dict:
         """The vector aggregator's outParticles / outInfo grid of the last frame (aggregator 2 with

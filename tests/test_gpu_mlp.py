@@ -147,3 +147,69 @@ def test_save_load_roundtrip(ctx, trained, tmp_path):
     x = np.random.default_rng(5).uniform(0, 1, (256, p2v.MLP_INPUTS)).astype(np.float32)
     assert np.array_equal(c2.mlp_infer(x), ctx.mlp_infer(x))
     c2.close()
+
+
+def _trilinear_border(T, x, y, z):
+    """GL LINEAR sampling with CLAMP_TO_BORDER (0) of texels T (z, y, x) at normalised (x, y, z), FP64."""
+    dz, dy, dx = T.shape
+    out = np.zeros(x.shape, np.float64)
+    xs, ys, zs = x * dx - 0.5, y * dy - 0.5, z * dz - 0.5
+    i0, j0, k0 = np.floor(xs).astype(np.int64), np.floor(ys).astype(np.int64), np.floor(zs).astype(np.int64)
+    fx, fy, fz = xs - i0, ys - j0, zs - k0
+    for a in (0, 1):
+        for b in (0, 1):
+            for c in (0, 1):
+                i, j, k = i0 + a, j0 + b, k0 + c
+                ok = (i >= 0) & (i < dx) & (j >= 0) & (j < dy) & (k >= 0) & (k < dz)
+                v = np.where(ok, T[np.clip(k, 0, dz - 1), np.clip(j, 0, dy - 1), np.clip(i, 0, dx - 1)], 0.0)
+                out += v * (fx if a else 1 - fx) * (fy if b else 1 - fy) * (fz if c else 1 - fz)
+    return out
+
+
+def test_stencil_features_vs_fp64():
+    """The learned AO's 131 features of every particle (collected through p2v_mlp_collect, in binning order)
+    against a CPU evaluation: two consecutive levels of the AO pyramid as the GPU built them, rounded to the
+    FP16 texels the stencils read, sampled trilinearly with a zero border at the 4x4x4 texel-spaced offsets
+    around the surface point p + r n, then the unit normal."""
+    c = p2v.Context(0)
+    try:
+        f = synth.uniform(n=30_000, edge=40.0, res=44, seed=9)
+        f.xyzr[:, 3] = np.random.default_rng(9).uniform(0.4, 0.8, f.n).astype(np.float32)
+        nrm = synth.random_normals(f.n, 10)
+        set_ao(c, f, p2v.AO_CONE)
+        c.mlp_clear()
+        c.mlp_collect([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm)], f.bbox, f.n, 0)
+        x, t = c.mlp_pairs()
+        _, order, _ = c.binning()
+        assert x.shape == (f.n, p2v.MLP_INPUTS) and np.all(t >= 0)
+        levels = [c.ao_volume(l).astype(np.float64) for l in range(3)]
+        levels[0] = np.clip(levels[0] * AO["ao_volume_scale"], 0.0, 1.0)
+        tex = [lv.astype(np.float16).astype(np.float64) for lv in levels]
+        h = oracle.spacing_f64(f.bbox, f.res)
+        bmin = [np.float64(np.float32(f.bbox[a] - 0.5 * h[a])) for a in range(3)]
+        ibs = [np.float64(np.float32(1.0 / (f.res[a] * h[a]))) for a in range(3)]
+        p = f.xyzr[order].astype(np.float64)
+        n = nrm[order].astype(np.float64)
+        n /= np.linalg.norm(n, axis=1, keepdims=True)
+        u = [(p[:, a] + p[:, 3] * n[:, a] - bmin[a]) * ibs[a] for a in range(3)]
+        k = np.arange(4) - 1.5
+
+        def stencil(T):
+            dz, dy, dx = T.shape
+            X = u[0][:, None, None, None] + k[None, None, None, :] / dx
+            Y = u[1][:, None, None, None] + k[None, None, :, None] / dy
+            Z = u[2][:, None, None, None] + k[None, :, None, None] / dz
+            X, Y, Z = np.broadcast_arrays(X, Y, Z)
+            return _trilinear_border(T, X, Y, Z).reshape(len(u[0]), 64)
+
+        errs = {}
+        for s in (0, 1):
+            ref = np.concatenate([stencil(tex[s]), stencil(tex[s + 1]), n], axis=1)
+            errs[s] = np.abs(x.astype(np.float64) - ref)
+        s = min(errs, key=lambda q: errs[q].max())
+        e = errs[s]
+        assert np.abs(x[:, 128:] - n).max() <= 1e-6
+        assert e[:, :128].max() <= 4e-3, e[:, :128].max()
+        assert np.sqrt(np.mean(e[:, :128] ** 2)) <= 5e-4, np.sqrt(np.mean(e[:, :128] ** 2))
+    finally:
+        c.close()
