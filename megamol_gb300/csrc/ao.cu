@@ -163,32 +163,11 @@ __device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const f
     return acc;
 }
 
-// G lanes per particle: G = 1 marches all cones in one thread (throughput: millions of particles); G > 1
-// spreads the cones over G lanes (latency: the short fallback list of the learned AO). The cone sum is
-// formed in cone order either way, so both give the same bits.
-template <int G>
-__global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
-    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, const uint32_t* __restrict__ n_dev,
-    float* __restrict__ ao) {
-    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = gt / G;
-    const int sub = (int) (gt % G);
-    if (n_dev != nullptr)
-        n = min(n, *n_dev);
-    // whole groups leave together (the group's lanes share i), so the shuffles below see full groups
-    if (i >= n)
-        return;
-    const uint32_t o = order ? order[i] : i;
-    const float4 p = xyzr[o];
-    const float4 nv = nrm[o];
-    float x[3], nn[3];
-    if (!surface_point(p, nv, x, nn)) {
-        if (sub == 0)
-            ao[o] = 1.0f;  // no normal: no occlusion
-        return;
-    }
-    // frame (mdao_deferred_fragment_ambocc.inc.glsl:18-21): new_y = n, new_x = cross(n, normalize(objPos)),
-    // new_z = cross(new_x, new_y)
+// Cone frame at surface point x with unit normal nn (mdao_deferred_fragment_ambocc.inc.glsl:18-21):
+// new_y = n, new_x = cross(n, normalize(objPos)), new_z = cross(new_x, new_y); and x in normalised volume
+// coordinates.
+__device__ __forceinline__ void cone_frame(const ConeParams& cp, const float x[3], const float nn[3], float u[3],
+                                           float ex[3], float ez[3]) {
     float xn[3] = {x[0], x[1], x[2]};
     const float xl2 = __fmaf_rn(xn[2], xn[2], __fmaf_rn(xn[1], xn[1], __fmul_rn(xn[0], xn[0])));
     if (xl2 > 0.0f) {
@@ -200,26 +179,67 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
         xn[0] = 1.0f;
         xn[1] = xn[2] = 0.0f;
     }
-    float ex[3], ez[3];
     cross_rn(nn, xn, ex);
     cross_rn(ex, nn, ez);
-    const float u[3] = {__fmul_rn(__fsub_rn(x[0], cp.bmin[0]), cp.ibsize[0]),
-                        __fmul_rn(__fsub_rn(x[1], cp.bmin[1]), cp.ibsize[1]),
-                        __fmul_rn(__fsub_rn(x[2], cp.bmin[2]), cp.ibsize[2])};
+    u[0] = __fmul_rn(__fsub_rn(x[0], cp.bmin[0]), cp.ibsize[0]);
+    u[1] = __fmul_rn(__fsub_rn(x[1], cp.bmin[1]), cp.ibsize[1]);
+    u[2] = __fmul_rn(__fsub_rn(x[2], cp.bmin[2]), cp.ibsize[2]);
+}
+
+// One thread per particle: marches all cones (throughput: millions of particles).
+__global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, float* __restrict__ ao) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint32_t o = order ? order[i] : i;
+    const float4 p = xyzr[o];
+    const float4 nv = nrm[o];
+    float x[3], nn[3];
+    if (!surface_point(p, nv, x, nn)) {
+        ao[o] = 1.0f;  // no normal: no occlusion
+        return;
+    }
+    float u[3], ex[3], ez[3];
+    cone_frame(cp, x, nn, u, ex, ez);
     float ambient = 0.0f;
-    if (G == 1) {
-        for (int c = 0; c < cp.ncones; ++c)
-            ambient += march_cone(cp, c, u, ex, nn, ez);
-    } else {
-        // lane `sub` marches cone sub (G >= ncones); the group's first lane adds them up in cone order
+    for (int c = 0; c < cp.ncones; ++c)
+        ambient += march_cone(cp, c, u, ex, nn, ez);
+    ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+}
+
+// G lanes per particle, lane c marching cone c (latency: the short fallback list of the learned AO, whose
+// length is a device-side count). A bounded grid strides over the list; the stride is a multiple of the
+// block and so of G, so a group's lanes always share the particle. The group's first lane adds the cones
+// up in cone order, so the result has the bits of cone_ao_kernel.
+template <int G>
+__global__ void __launch_bounds__(128) cone_ao_group_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, const uint32_t* __restrict__ n_dev,
+    float* __restrict__ ao) {
+    n = min(n, *n_dev);
+    for (uint64_t gt = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; gt / G < n;
+         gt += (uint64_t) gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t) (gt / G);
+        const int sub = (int) (gt % G);
+        const uint32_t o = order[i];
+        const float4 p = xyzr[o];
+        const float4 nv = nrm[o];
+        float x[3], nn[3];
+        if (!surface_point(p, nv, x, nn)) {  // the whole group takes this branch
+            if (sub == 0)
+                ao[o] = 1.0f;
+            continue;
+        }
+        float u[3], ex[3], ez[3];
+        cone_frame(cp, x, nn, u, ex, ez);
         const float a = sub < cp.ncones ? march_cone(cp, sub, u, ex, nn, ez) : 0.0f;
         const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << ((threadIdx.x & 31) / G * G);
+        float ambient = 0.0f;
         for (int c = 0; c < cp.ncones; ++c)
             ambient += __shfl_sync(gmask, a, c, G);
-        if (sub != 0)
-            return;
+        if (sub == 0)
+            ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
     }
-    ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -347,19 +367,19 @@ cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const fl
     if (n == 0)
         return cudaSuccess;
     if (n_dev == nullptr) {
-        cone_ao_kernel<1><<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+        cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, ao);
     } else {
         // a device-side count (the learned AO's fallback list) is usually tiny: spread the cones over lanes
-        // and size the grid for the list's capacity n, most of whose threads leave at once
+        // and let a bounded grid stride over the list (a grid for its capacity n would mostly idle)
         const int g = cp.ncones <= 4 ? 4 : (cp.ncones <= 8 ? 8 : 16);
         const uint64_t threads = (uint64_t) n * g;
-        const unsigned grd = (unsigned) ((threads + 127) / 128);
+        const unsigned grd = (unsigned) std::min<uint64_t>((threads + 127) / 128, 2048);
         if (g == 4)
-            cone_ao_kernel<4><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+            cone_ao_group_kernel<4><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
         else if (g == 8)
-            cone_ao_kernel<8><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+            cone_ao_group_kernel<8><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
         else
-            cone_ao_kernel<16><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+            cone_ao_group_kernel<16><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
     }
     return cudaGetLastError();
 }

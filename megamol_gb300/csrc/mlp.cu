@@ -39,12 +39,13 @@ __device__ __forceinline__ float sigmoidf_(float a) {
 }
 
 // 4x4x4 trilinear samples of one mip level at texel-spaced offsets (k - 1.5) around normalised point u.
-// The level is a layered 2D texture (one layer per z slice, FP16 texels, GL LINEAR in x and y with
-// CLAMP_TO_BORDER): the texture units filter the 16 (x, y) positions bilinearly on each of the five z
-// slices the stencil spans, and the z interpolation runs in FP32 (slices outside the level read 0, the
-// border). emit(kz, v) receives the 16 samples of z row kz, in the order ky*4 + kx. The features feed a
-// BF16 network, so the texture filter's 8-bit weight fractions sit below the features' own rounding;
-// training pairs are extracted by the same code.
+// The level is a layered 2D texture of FP16 pairs: layer L holds z slices L - 1 (red) and L (green), so one
+// bilinear fetch (GL LINEAR in x and y, CLAMP_TO_BORDER) filters two slices; slices outside the level are
+// 0, as the border. The five slices the stencil spans take three fetches per (x, y) position (48 per level
+// where one slice per fetch takes 80); the z interpolation runs in FP32. emit(kz, v) receives the 16
+// samples of z row kz, in the order ky*4 + kx. The features feed a BF16 network, so the texture filter's
+// 8-bit weight fractions sit below the features' own rounding; training pairs are extracted by the same
+// code.
 template<class Emit>
 __device__ __forceinline__ void stencil64(unsigned long long tex, const float inv[3], int nz, float ux, float uy,
                                           float uz, Emit&& emit) {
@@ -58,45 +59,65 @@ __device__ __forceinline__ void stencil64(unsigned long long tex, const float in
     const float fz0 = floorf(cz);
     const float fz = cz - fz0;
     const int z0 = (int) fz0;
-    float prev[16];
+    float prev[16];  // the last slice of the previous pair
 #pragma unroll 1
-    for (int s = 0; s < 5; ++s) {
-        const int layer = z0 + s;
-        float cur[16];
-        if (layer >= 0 && layer < nz) {
+    for (int q = 0; q < 3; ++q) {
+        // slices z0 + 2q and z0 + 2q + 1 live in layer z0 + 2q + 1
+        const int layer = z0 + 2 * q + 1;
+        float lo[16], hi[16];
+        if (layer >= 0 && layer <= nz) {
 #pragma unroll
             for (int ky = 0; ky < 4; ++ky)
 #pragma unroll
-                for (int kx = 0; kx < 4; ++kx)
-                    cur[ky * 4 + kx] = tex2DLayered<float>((cudaTextureObject_t) tex, px[kx], py[ky], layer);
+                for (int kx = 0; kx < 4; ++kx) {
+                    const float2 v = tex2DLayered<float2>((cudaTextureObject_t) tex, px[kx], py[ky], layer);
+                    lo[ky * 4 + kx] = v.x;
+                    hi[ky * 4 + kx] = v.y;
+                }
         } else {
 #pragma unroll
             for (int k = 0; k < 16; ++k)
-                cur[k] = 0.0f;
+                lo[k] = hi[k] = 0.0f;
         }
-        if (s > 0) {
-            float v[16];
+        float v[16];
+        if (q > 0) {  // z row 2q - 1: slices 2q - 1 and 2q
 #pragma unroll
             for (int k = 0; k < 16; ++k)
-                v[k] = prev[k] + fz * (cur[k] - prev[k]);
-            emit(s - 1, v);
+                v[k] = prev[k] + fz * (lo[k] - prev[k]);
+            emit(2 * q - 1, v);
+        }
+        if (q < 2) {  // z row 2q: slices 2q and 2q + 1
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+                v[k] = lo[k] + fz * (hi[k] - lo[k]);
+            emit(2 * q, v);
         }
 #pragma unroll
         for (int k = 0; k < 16; ++k)
-            prev[k] = cur[k];
+            prev[k] = hi[k];
     }
 }
 
+// Layer L of the paired texture = (slice L - 1, slice L) of level (dx, dy, dz), L in [0, dz].
 __global__ void __launch_bounds__(256) fill_stencil_tex_kernel(const float* __restrict__ src, int dx, int dy, int dz,
                                                                float sat, unsigned long long surf) {
-    const int64_t n = (int64_t) dx * dy * dz;
+    const int64_t n = (int64_t) dx * dy * (dz + 1);
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
-        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), z = (int) (i / ((int64_t) dx * dy));
-        float v = src[i];
-        if (sat > 0.0f)
-            v = fminf(fmaxf(v * sat, 0.0f), 1.0f);
-        surf2DLayeredwrite(__half_as_ushort(__float2half_rn(v)), (cudaSurfaceObject_t) surf, x * (int) sizeof(__half), y,
-                           z);
+        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), L = (int) (i / ((int64_t) dx * dy));
+        float v[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int z = L - 1 + c;
+            v[c] = 0.0f;
+            if (z >= 0 && z < dz) {
+                v[c] = src[((int64_t) z * dy + y) * dx + x];
+                if (sat > 0.0f)
+                    v[c] = fminf(fmaxf(v[c] * sat, 0.0f), 1.0f);
+            }
+        }
+        const __half2 h = __floats2half2_rn(v[0], v[1]);
+        surf2DLayeredwrite(*reinterpret_cast<const unsigned int*>(&h), (cudaSurfaceObject_t) surf,
+                           x * (int) sizeof(__half2), y, L);
     }
 }
 
@@ -723,9 +744,9 @@ cudaError_t StencilTex::ensure(const int dims[3]) {
     if (arr && d[0] == dims[0] && d[1] == dims[1] && d[2] == dims[2])
         return cudaSuccess;
     release();
-    cudaChannelFormatDesc fmt = cudaCreateChannelDescHalf();
-    // one layer per z slice
-    cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2]),
+    cudaChannelFormatDesc fmt = cudaCreateChannelDescHalf2();
+    // dims[2] + 1 layers of slice pairs (slice L - 1, slice L)
+    cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2] + 1),
                                       cudaArrayLayered | cudaArraySurfaceLoadStore);
     if (e != cudaSuccess) {
         arr = nullptr;
@@ -770,7 +791,7 @@ void StencilTex::release() {
 }
 
 cudaError_t launch_fill_stencil_tex(const ConeLevel& L, float sat, const StencilTex& t, cudaStream_t st) {
-    const int64_t n = (int64_t) L.d[0] * L.d[1] * L.d[2];
+    const int64_t n = (int64_t) L.d[0] * L.d[1] * (L.d[2] + 1);
     const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
     fill_stencil_tex_kernel<<<grd, 256, 0, st>>>(L.v, L.d[0], L.d[1], L.d[2], sat, t.surf);
     return cudaGetLastError();
