@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 4
+#define P2V_ABI_VERSION 5
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -193,6 +193,8 @@ typedef struct p2v_stats {
     double ms_upload, ms_binning, ms_density, ms_normalize, ms_ao, ms_download, ms_total; /* CUDA events */
     uint32_t device_error;       /* nonzero: a bounded device wait gave up (status P2V_ETIMEOUT) */
     uint32_t ao_fallback;        /* learned AO: particles that fell back to the cone march */
+    uint32_t cell_max_count;     /* binning: particles in the fullest cell when the counting sort by cell was
+                                    tried (it takes frames whose cells hold at most 32), 0 = radix sort only */
 } p2v_stats;
 
 /* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle:

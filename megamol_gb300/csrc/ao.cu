@@ -138,25 +138,37 @@ __device__ __forceinline__ void cross_rn(const float a[3], const float b[3], flo
     out[2] = __fsub_rn(__fmul_rn(a[0], b[1]), __fmul_rn(a[1], b[0]));
 }
 
-// One cone of the MDAO march (mdao_deferred_fragment_ambocc.inc.glsl:30-51) from normalised point u.
-__device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const float u[3], const float ex[3],
-                                            const float nn[3], const float ez[3]) {
+// Cone c's direction in the particle's frame.
+__device__ __forceinline__ void cone_dir(const ConeParams& cp, int c, const float ex[3], const float nn[3],
+                                         const float ez[3], float dir[3]) {
     const float4 cd = cp.dirs[c];
-    float dir[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         dir[a] = __fmaf_rn(ez[a], cd.z, __fmaf_rn(nn[a], cd.y, __fmul_rn(ex[a], cd.x)));
+}
+
+// Visibility sample k of a cone: trilinear in the two levels around its lod, blended linearly
+// (LINEAR_MIPMAP_LINEAR).
+__device__ __forceinline__ float cone_sample(const ConeParams& cp, const float dir[3], const float u[3], int k) {
+    const float t = cp.t[k];
+    const float lod = cp.lod[k];
+    const float qx = __fmaf_rn(t, dir[0], u[0]), qy = __fmaf_rn(t, dir[1], u[1]), qz = __fmaf_rn(t, dir[2], u[2]);
+    const int l0 = min((int) lod, cp.nlevels - 1);
+    const float fr = __fsub_rn(lod, (float) l0);
+    float vis = trilinear(cp.lv[l0], qx, qy, qz, cp.border, l0 == 0 ? cp.sat : 0.0f);
+    if (fr > 0.0f && l0 + 1 < cp.nlevels)
+        vis = __fmaf_rn(fr, trilinear(cp.lv[l0 + 1], qx, qy, qz, cp.border, 0.0f), __fmul_rn(1.0f - fr, vis));
+    return vis;
+}
+
+// One cone of the MDAO march (mdao_deferred_fragment_ambocc.inc.glsl:30-51) from normalised point u.
+__device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const float u[3], const float ex[3],
+                                            const float nn[3], const float ez[3]) {
+    float dir[3];
+    cone_dir(cp, c, ex, nn, ez, dir);
     float acc = 0.0f;
     for (int k = 0; k < cp.nsteps; ++k) {
-        const float t = cp.t[k];
-        const float lod = cp.lod[k];
-        const float qx = __fmaf_rn(t, dir[0], u[0]), qy = __fmaf_rn(t, dir[1], u[1]), qz = __fmaf_rn(t, dir[2], u[2]);
-        const int l0 = min((int) lod, cp.nlevels - 1);
-        const float fr = __fsub_rn(lod, (float) l0);
-        float vis = trilinear(cp.lv[l0], qx, qy, qz, cp.border, l0 == 0 ? cp.sat : 0.0f);
-        if (fr > 0.0f && l0 + 1 < cp.nlevels)
-            vis = __fmaf_rn(fr, trilinear(cp.lv[l0 + 1], qx, qy, qz, cp.border, 0.0f), __fmul_rn(1.0f - fr, vis));
-        acc = __fmaf_rn(1.0f - acc, vis, acc);
+        acc = __fmaf_rn(1.0f - acc, cone_sample(cp, dir, u, k), acc);
         if (cp.early_exit && acc > 0.99f)
             break;
     }
@@ -208,37 +220,54 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
     ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
 }
 
-// G lanes per particle, lane c marching cone c (latency: the short fallback list of the learned AO, whose
-// length is a device-side count). A bounded grid strides over the list; the stride is a multiple of the
-// block and so of G, so a group's lanes always share the particle. The group's first lane adds the cones
-// up in cone order, so the result has the bits of cone_ao_kernel.
-template <int G>
-__global__ void __launch_bounds__(128) cone_ao_group_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
-    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, const uint32_t* __restrict__ n_dev,
-    float* __restrict__ ao) {
+// The learned AO's fallback list (its length a device-side count, usually tiny): latency matters, so a
+// block takes one particle with one warp per cone, and the lanes of a warp take the cone's samples (32 at a
+// time: the step positions are tabulated, so all samples load at once). Every lane then runs the march's
+// recurrence over the shuffled samples in step order with the same early exit, the block's first thread
+// adds the cones in cone order: the result has the bits of cone_ao_kernel. A bounded grid strides over the
+// list.
+__global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const ConeParams cp,
+    const uint32_t* __restrict__ list, const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n,
+    const uint32_t* __restrict__ n_dev, float* __restrict__ ao) {
+    __shared__ float s_acc[MAX_CONES];
+    const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
     n = min(n, *n_dev);
-    for (uint64_t gt = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; gt / G < n;
-         gt += (uint64_t) gridDim.x * blockDim.x) {
-        const uint32_t i = (uint32_t) (gt / G);
-        const int sub = (int) (gt % G);
-        const uint32_t o = order[i];
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint32_t o = list[i];
         const float4 p = xyzr[o];
         const float4 nv = nrm[o];
         float x[3], nn[3];
-        if (!surface_point(p, nv, x, nn)) {  // the whole group takes this branch
-            if (sub == 0)
+        if (!surface_point(p, nv, x, nn)) {  // the whole block takes this branch
+            if (threadIdx.x == 0)
                 ao[o] = 1.0f;
             continue;
         }
-        float u[3], ex[3], ez[3];
+        float u[3], ex[3], ez[3], dir[3];
         cone_frame(cp, x, nn, u, ex, ez);
-        const float a = sub < cp.ncones ? march_cone(cp, sub, u, ex, nn, ez) : 0.0f;
-        const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << ((threadIdx.x & 31) / G * G);
-        float ambient = 0.0f;
-        for (int c = 0; c < cp.ncones; ++c)
-            ambient += __shfl_sync(gmask, a, c, G);
-        if (sub == 0)
+        cone_dir(cp, c, ex, nn, ez, dir);
+        float acc = 0.0f;
+        bool done = false;
+        for (int k0 = 0; k0 < cp.nsteps && !done; k0 += 32) {
+            const float vis = k0 + lane < cp.nsteps ? cone_sample(cp, dir, u, k0 + lane) : 0.0f;
+            const int m = min(32, cp.nsteps - k0);
+            for (int s = 0; s < m; ++s) {
+                acc = __fmaf_rn(1.0f - acc, __shfl_sync(0xffffffffu, vis, s), acc);
+                if (cp.early_exit && acc > 0.99f) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+        if (lane == 0)
+            s_acc[c] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float ambient = 0.0f;
+            for (int k = 0; k < cp.ncones; ++k)
+                ambient += s_acc[k];
             ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+        }
+        __syncthreads();
     }
 }
 
@@ -369,17 +398,9 @@ cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const fl
     if (n_dev == nullptr) {
         cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, ao);
     } else {
-        // a device-side count (the learned AO's fallback list) is usually tiny: spread the cones over lanes
-        // and let a bounded grid stride over the list (a grid for its capacity n would mostly idle)
-        const int g = cp.ncones <= 4 ? 4 : (cp.ncones <= 8 ? 8 : 16);
-        const uint64_t threads = (uint64_t) n * g;
-        const unsigned grd = (unsigned) std::min<uint64_t>((threads + 127) / 128, 2048);
-        if (g == 4)
-            cone_ao_group_kernel<4><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
-        else if (g == 8)
-            cone_ao_group_kernel<8><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
-        else
-            cone_ao_group_kernel<16><<<grd, 128, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+        // the learned AO's fallback list: one block of ncones warps per particle, a bounded grid
+        const unsigned grd = (unsigned) std::min<uint32_t>(n, 4096u);
+        cone_ao_list_kernel<<<grd, 32 * cp.ncones, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
     }
     return cudaGetLastError();
 }

@@ -151,8 +151,9 @@ constexpr int SORT_WARPS = SORT_THREADS / 32;
 constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 4096 keys per tile
 constexpr int MAX_RADIX = 512;
-constexpr int MAX_PASSES = 4;
+constexpr int MAX_PASSES = 5;
 constexpr int HIST_WORDS = MAX_PASSES * MAX_RADIX;    // digit histograms, pass p at p * MAX_RADIX
+// after the histograms: one tile counter per radix pass
 constexpr uint32_t FLAG_AGG = 1u << 30;
 constexpr uint32_t FLAG_PRE = 2u << 30;
 constexpr uint32_t FLAG_MASK = 3u << 30;
@@ -164,13 +165,16 @@ struct SortPlan {
     int bits[MAX_PASSES];
 };
 
-SortPlan sort_plan(uint32_t max_key) {
+// odd: an odd number of passes, so the sorted keys end in buffer 1 (8-bit digits where a pass is added)
+SortPlan sort_plan(uint32_t max_key, bool odd = false) {
     int nb = 0;
     while (nb < 32 && (max_key >> nb) != 0u)
         ++nb;
     nb = std::max(nb, 1);
     SortPlan pl{};
     pl.passes = (nb + 8) / 9;
+    if (odd && (pl.passes & 1) == 0)
+        ++pl.passes;
     // the first (nb - 8 * passes) passes take 9 bits, the others 8
     int nine = std::max(0, nb - 8 * pl.passes);
     int sh = 0;
@@ -182,8 +186,19 @@ SortPlan sort_plan(uint32_t max_key) {
     return pl;
 }
 
+constexpr uint32_t BIN_CELL_MAX = 32;  // the counting sort orders cells of up to this many particles
+
+// The radix path runs unless the counting sort (count_bins / scan_bins / scatter_bins / order_bins) took the
+// frame: with a gate, every radix kernel returns at once when the frame's fullest cell fits the counting
+// sort's per-cell ordering.
+__device__ __forceinline__ bool radix_skipped(const FrameScalars* gate) {
+    return gate != nullptr && gate->bin_maxcount <= BIN_CELL_MAX;
+}
+
 __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n, SortPlan pl,
-    uint32_t* __restrict__ hist) {
+    uint32_t* __restrict__ hist, const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate))
+        return;
     __shared__ uint32_t sh[HIST_WORDS];
     for (int i = threadIdx.x; i < HIST_WORDS; i += blockDim.x)
         sh[i] = 0;
@@ -200,7 +215,10 @@ __global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restr
 }
 
 // Exclusive scan of each pass' digit histogram (one block of MAX_RADIX threads).
-__global__ void __launch_bounds__(MAX_RADIX) radix_scan_kernel(uint32_t* hist, int passes) {
+__global__ void __launch_bounds__(MAX_RADIX) radix_scan_kernel(uint32_t* hist, int passes,
+                                                                const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate))
+        return;
     __shared__ uint32_t s[MAX_RADIX];
     for (int p = 0; p < passes; ++p) {
         const uint32_t v = hist[p * MAX_RADIX + threadIdx.x];
@@ -234,7 +252,9 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
     const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
     int shift, const uint32_t* __restrict__ digit_offsets, uint32_t* __restrict__ tile_counter,
     uint32_t* __restrict__ status, uint32_t* __restrict__ err, const float4* __restrict__ xyzr_in,
-    float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo) {
+    float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo, const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate))
+        return;
     constexpr int RADIX = 1 << BITS;
     constexpr uint32_t DMASK = RADIX - 1u;
     constexpr int DPT = RADIX / SORT_THREADS;  // digits per thread in the per-digit phases
@@ -379,8 +399,8 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
             float4 A;
             int4 B;
             make_record(xyzr_in[vv], geo, A, B);
-            rec_a[dst] = A;
-            rec_b[dst] = B;
+            rec_a[REC_STRIDE * (size_t) dst] = A;
+            rec_b[REC_STRIDE * (size_t) dst] = B;
         }
     }
 }
@@ -388,7 +408,10 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
 // start[c] = first sorted position whose key is >= c, for c in [0, nbins]. Short gaps are filled by
 // the thread that sees them; gaps of 64 cells or more are queued for a block-wide fill.
 __global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t nbins,
-    uint32_t* __restrict__ start, uint4* __restrict__ gaps, uint32_t gap_cap, FrameScalars* __restrict__ fs) {
+    uint32_t* __restrict__ start, uint4* __restrict__ gaps, uint32_t gap_cap, FrameScalars* __restrict__ fs,
+    const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate))
+        return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
         const uint32_t lo = i == 0 ? 0u : keys[i - 1] + 1u;
         uint32_t hi = i == n ? nbins : keys[i];
@@ -410,12 +433,248 @@ __global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restr
 }
 
 __global__ void __launch_bounds__(256) cell_gap_fill_kernel(const uint4* __restrict__ gaps, uint32_t gap_cap,
-    uint32_t* __restrict__ start, const FrameScalars* __restrict__ fs) {
+    uint32_t* __restrict__ start, const FrameScalars* __restrict__ fs, const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate))
+        return;
     const uint32_t ng = min(fs->ngaps, gap_cap);
     for (uint32_t g = blockIdx.x; g < ng; g += gridDim.x) {
         const uint4 e = gaps[g];
         for (uint32_t c = e.x + threadIdx.x; c <= e.y; c += blockDim.x)
             start[c] = e.z;
+    }
+}
+
+// ---- counting sort by cell ----
+// counts[key] = particles per key, keys in [0, nbins] (nbins: the invalid particles)
+__global__ void __launch_bounds__(256) count_bins_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                         uint32_t* __restrict__ counts) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(counts + keys[i], 1u);
+}
+
+constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 16, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// 16 consecutive counts of thread `tid` in tile `tile` (zeros past nb); true when all 16 exist
+__device__ __forceinline__ bool load_counts(const uint32_t* __restrict__ counts, uint32_t nb, uint64_t b0,
+                                            uint32_t v[SCAN_ITEMS]) {
+    const bool full = b0 + SCAN_ITEMS <= nb;
+    if (full) {
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
+            const uint4 u = reinterpret_cast<const uint4*>(counts + b0)[q];
+            v[4 * q] = u.x;
+            v[4 * q + 1] = u.y;
+            v[4 * q + 2] = u.z;
+            v[4 * q + 3] = u.w;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < SCAN_ITEMS; ++e)
+            v[e] = b0 + e < nb ? counts[b0 + e] : 0u;
+    }
+    return full;
+}
+
+// Scan of the cell counts in three steps (tile sums, their scan, tile scans): no cross-tile waiting.
+// Step 1: the sum of every tile of SCAN_TILE counts, and the largest count (fs->bin_maxcount).
+__global__ void __launch_bounds__(SCAN_THREADS) bin_tile_sums_kernel(const uint32_t* __restrict__ counts, uint32_t nb,
+    uint32_t* __restrict__ tsum, FrameScalars* __restrict__ fs) {
+    __shared__ uint32_t s_sum[SCAN_THREADS / 32], s_max[SCAN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    uint32_t v[SCAN_ITEMS];
+    load_counts(counts, nb, (uint64_t) blockIdx.x * SCAN_TILE + (uint64_t) tid * SCAN_ITEMS, v);
+    uint32_t sum = 0, vmax = 0;
+#pragma unroll
+    for (int e = 0; e < SCAN_ITEMS; ++e) {
+        sum += v[e];
+        vmax = max(vmax, v[e]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        vmax = max(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    }
+    if (lane == 0) {
+        s_sum[w] = sum;
+        s_max[w] = vmax;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int k = 1; k < SCAN_THREADS / 32; ++k) {
+            sum += s_sum[k];
+            vmax = max(vmax, s_max[k]);
+        }
+        tsum[blockIdx.x] = sum;
+        if (vmax > 0)
+            atomicMax(&fs->bin_maxcount, vmax);
+    }
+}
+
+// Step 2: exclusive scan of the tile sums in place (one block).
+__global__ void __launch_bounds__(1024) bin_tile_scan_kernel(uint32_t* __restrict__ tsum, uint32_t ntiles) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0)
+        s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < ntiles; base += 1024) {
+        const uint32_t i = base + tid;
+        const uint32_t x = i < ntiles ? tsum[i] : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        if (lane == 31)
+            s_warp[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t ws = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o)
+                    ws += t;
+            }
+            s_warp[lane] = ws;  // inclusive over warps
+        }
+        __syncthreads();
+        const uint32_t carry = s_carry;
+        const uint32_t excl = carry + (w > 0 ? s_warp[w - 1] : 0u) + incl - x;
+        if (i < ntiles)
+            tsum[i] = excl;
+        __syncthreads();
+        if (tid == 0)
+            s_carry = carry + s_warp[31];
+        __syncthreads();
+    }
+}
+
+// Step 3: start[c] = tile prefix + the scan inside the tile, for c in [0, nb); cells holding two or more
+// particles are appended to `multi` (their order inside the cell is fixed by order_bins_kernel).
+__global__ void __launch_bounds__(SCAN_THREADS) bin_starts_kernel(const uint32_t* __restrict__ counts, uint32_t nb,
+    const uint32_t* __restrict__ tsum, uint32_t* __restrict__ start, uint32_t* __restrict__ multi,
+    FrameScalars* __restrict__ fs) {
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint64_t b0 = (uint64_t) blockIdx.x * SCAN_TILE + (uint64_t) tid * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    const bool full = load_counts(counts, nb, b0, v);
+    uint32_t sum = 0, nm = 0;
+#pragma unroll
+    for (int e = 0; e < SCAN_ITEMS; ++e) {
+        sum += v[e];
+        nm += v[e] >= 2u ? 1u : 0u;
+    }
+    uint32_t incl = sum, mincl = nm;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        const uint32_t tm = __shfl_up_sync(0xffffffffu, mincl, o);
+        if (lane >= o) {
+            incl += t;
+            mincl += tm;
+        }
+    }
+    if (lane == 31)
+        s_warp[w] = incl;
+    // the warp's multi-particle cells take consecutive list entries
+    const uint32_t mtot = __shfl_sync(0xffffffffu, mincl, 31);
+    uint32_t mbase = 0;
+    if (lane == 31 && mtot)
+        mbase = atomicAdd(&fs->bin_nmulti, mtot);
+    mbase = __shfl_sync(0xffffffffu, mbase, 31) + mincl - nm;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int k = 0; k < w; ++k)
+        wpre += s_warp[k];
+    uint32_t run = tsum[blockIdx.x] + wpre + incl - sum;
+#pragma unroll
+    for (int e = 0; e < SCAN_ITEMS; ++e) {
+        if (v[e] >= 2u)
+            multi[mbase++] = (uint32_t) (b0 + e);
+        const uint32_t x = run;
+        run += v[e];
+        v[e] = x;
+    }
+    if (full) {
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS / 4; ++q)
+            reinterpret_cast<uint4*>(start + b0)[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < SCAN_ITEMS; ++e)
+            if (b0 + e < nb)
+                start[b0 + e] = v[e];
+    }
+}
+
+// Each particle takes a slot of its cell (arrival order within the cell, fixed by order_bins_kernel) and
+// writes its index and its 32-byte gather record there. The sorted keys are not written: the cell starts
+// hold them (keys_from_starts_kernel rebuilds them for the binning readback).
+__global__ void __launch_bounds__(256) scatter_bins_kernel(const uint32_t* __restrict__ keys_in,
+    const float4* __restrict__ xyzr, uint32_t n, const uint32_t* __restrict__ start, uint32_t* __restrict__ counts,
+    uint32_t* __restrict__ vals_out, float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo,
+    const FrameScalars* __restrict__ fs) {
+    if (fs->bin_maxcount > BIN_CELL_MAX)
+        return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys_in[i];
+        const uint32_t slot = start[k] + atomicSub(counts + k, 1u) - 1u;
+        vals_out[slot] = i;
+        float4 A;
+        int4 B;
+        make_record(xyzr[i], geo, A, B);
+        rec_a[REC_STRIDE * (size_t) slot] = A;
+        rec_b[REC_STRIDE * (size_t) slot] = B;
+    }
+}
+
+// Every cell with two or more particles (the list `multi`) puts them in index order (an insertion sort of
+// at most BIN_CELL_MAX entries) and rewrites their values and records: the result is the stable sort by key.
+__global__ void __launch_bounds__(256) order_bins_kernel(uint32_t n, uint32_t nbins, const uint32_t* __restrict__ multi,
+    uint32_t* __restrict__ vals, const uint32_t* __restrict__ start, const float4* __restrict__ xyzr,
+    float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo, const FrameScalars* __restrict__ fs) {
+    if (fs->bin_maxcount > BIN_CELL_MAX)
+        return;
+    const uint32_t nm = fs->bin_nmulti;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nm; q += gridDim.x * blockDim.x) {
+        const uint32_t k = multi[q];
+        const uint32_t j = start[k];
+        const uint32_t m = (k < nbins ? start[k + 1] : n) - j;
+        uint32_t v[BIN_CELL_MAX];
+        for (uint32_t a = 0; a < m; ++a) {
+            const uint32_t x = vals[j + a];
+            uint32_t b = a;
+            while (b > 0 && v[b - 1] > x) {
+                v[b] = v[b - 1];
+                --b;
+            }
+            v[b] = x;
+        }
+        for (uint32_t a = 0; a < m; ++a) {
+            if (vals[j + a] == v[a])
+                continue;
+            vals[j + a] = v[a];
+            float4 A;
+            int4 B;
+            make_record(xyzr[v[a]], geo, A, B);
+            rec_a[REC_STRIDE * (size_t) (j + a)] = A;
+            rec_b[REC_STRIDE * (size_t) (j + a)] = B;
+        }
+    }
+}
+
+// keys[j] = the cell whose start range holds sorted position j (the counting sort writes no keys)
+__global__ void __launch_bounds__(256) keys_from_starts_kernel(const uint32_t* __restrict__ start, uint32_t nbins,
+                                                               uint32_t n, uint32_t* __restrict__ keys) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= nbins; k += gridDim.x * blockDim.x) {
+        const uint32_t e = k < nbins ? start[k + 1] : n;
+        for (uint32_t j = start[k]; j < e; ++j)
+            keys[j] = k;
     }
 }
 
@@ -485,7 +744,7 @@ int sort_passes(uint32_t max_key) {
 
 template<bool GATHER, int BITS>
 cudaError_t launch_onesweep_bits(uint32_t tiles, SortBuffers& b, int cur, uint32_t n, int shift, const uint32_t* offs,
-                                 uint32_t* counter, cudaStream_t st) {
+                                 uint32_t* counter, cudaStream_t st, const FrameScalars* gate) {
     constexpr int RADIX = 1 << BITS;
     const int smem = (int) sizeof(uint32_t) * (2 * SORT_TILE + SORT_WARPS * RADIX + 2 * RADIX);
     const cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<GATHER, BITS>,
@@ -494,28 +753,30 @@ cudaError_t launch_onesweep_bits(uint32_t tiles, SortBuffers& b, int cur, uint32
         return e;
     onesweep_kernel<GATHER, BITS><<<tiles, SORT_THREADS, smem, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
         b.vals[cur ^ 1], n, shift, offs, counter, b.status, b.err, GATHER ? b.xyzr_in : nullptr,
-        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, b.geo);
+        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, b.geo, gate);
     return cudaSuccess;
 }
 
 template<bool GATHER>
 cudaError_t launch_onesweep(int bits, uint32_t tiles, SortBuffers& b, int cur, uint32_t n, int shift,
-                            const uint32_t* offs, uint32_t* counter, cudaStream_t st) {
-    return bits == 9 ? launch_onesweep_bits<GATHER, 9>(tiles, b, cur, n, shift, offs, counter, st)
-                     : launch_onesweep_bits<GATHER, 8>(tiles, b, cur, n, shift, offs, counter, st);
+                            const uint32_t* offs, uint32_t* counter, cudaStream_t st, const FrameScalars* gate) {
+    return bits == 9 ? launch_onesweep_bits<GATHER, 9>(tiles, b, cur, n, shift, offs, counter, st, gate)
+                     : launch_onesweep_bits<GATHER, 8>(tiles, b, cur, n, shift, offs, counter, st, gate);
 }
 
-cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st) {
-    const SortPlan pl = sort_plan(max_key);
+cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st, const FrameScalars* gate,
+                        bool odd) {
+    const SortPlan pl = sort_plan(max_key, odd);
     const uint32_t tiles = ceil_div(n, SORT_TILE);
-    cudaError_t e = cudaMemsetAsync(b.hist, 0, sizeof(uint32_t) * sort_hist_words(), st);
+    cudaError_t e = cudaMemsetAsync(b.hist, 0, sizeof(uint32_t) * HIST_WORDS + sizeof(uint32_t) * MAX_PASSES, st);
     if (e != cudaSuccess)
         return e;
+    b.result = pl.passes & 1;
     if (n == 0)
         return cudaSuccess;
     const unsigned hgrid = (unsigned) std::min<uint32_t>(ceil_div(n, 256 * 8), (uint32_t) sms * 4);
-    radix_hist_kernel<<<hgrid ? hgrid : 1, 256, 0, st>>>(b.keys[0], n, pl, b.hist);
-    radix_scan_kernel<<<1, MAX_RADIX, 0, st>>>(b.hist, pl.passes);
+    radix_hist_kernel<<<hgrid ? hgrid : 1, 256, 0, st>>>(b.keys[0], n, pl, b.hist, gate);
+    radix_scan_kernel<<<1, MAX_RADIX, 0, st>>>(b.hist, pl.passes, gate);
     int cur = 0;
     for (int p = 0; p < pl.passes; ++p) {
         e = cudaMemsetAsync(b.status, 0, sizeof(uint32_t) * (size_t) tiles * ((size_t) 1 << pl.bits[p]), st);
@@ -524,23 +785,60 @@ cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, c
         uint32_t* counter = b.hist + HIST_WORDS + p;
         const bool last = p == pl.passes - 1;
         if (last && b.xyzr_in != nullptr)
-            e = launch_onesweep<true>(pl.bits[p], tiles, b, cur, n, pl.shift[p], b.hist + p * MAX_RADIX, counter, st);
+            e = launch_onesweep<true>(pl.bits[p], tiles, b, cur, n, pl.shift[p], b.hist + p * MAX_RADIX, counter, st,
+                                      gate);
         else
-            e = launch_onesweep<false>(pl.bits[p], tiles, b, cur, n, pl.shift[p], b.hist + p * MAX_RADIX, counter, st);
+            e = launch_onesweep<false>(pl.bits[p], tiles, b, cur, n, pl.shift[p], b.hist + p * MAX_RADIX, counter, st,
+                                       gate);
         if (e != cudaSuccess)
             return e;
         cur ^= 1;
     }
-    b.result = cur;
     return cudaGetLastError();
 }
 
-cudaError_t launch_cell_start(const uint32_t* keys, uint32_t n, uint32_t nbins, uint32_t* start, uint4* gaps,
-    uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st) {
+cudaError_t launch_keys_from_starts(const uint32_t* start, uint32_t nbins, uint32_t n, uint32_t* keys, int sms,
+                                    cudaStream_t st) {
+    const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(nbins + 1, 256), (uint32_t) sms * 16));
+    keys_from_starts_kernel<<<grid, 256, 0, st>>>(start, nbins, n, keys);
+    return cudaGetLastError();
+}
+
+size_t bin_scan_words(uint32_t nbins) {
+    return (size_t) ceil_div(nbins + 1, SCAN_TILE);
+}
+
+cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32_t* counts, uint32_t* start,
+                            uint4* gaps, uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st) {
+    const uint32_t nb = g.nbins + 1;
+    cudaError_t e;
+    const bool counting = counts != nullptr && n > 0;
+    if (counting) {
+        // counting sort by cell: histogram, scan (= the cell starts), scatter, per-cell index order
+        const uint32_t ntiles = (uint32_t) bin_scan_words(g.nbins);
+        if ((e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * nb, st)) != cudaSuccess)
+            return e;
+        const unsigned pgrid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
+        count_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], n, counts);
+        // tile sums in the status buffer; the multi-particle cell list in keys[1] (the counting sort writes no
+        // sorted keys there)
+        bin_tile_sums_kernel<<<ntiles, SCAN_THREADS, 0, st>>>(counts, nb, b.status, fs);
+        bin_tile_scan_kernel<<<1, 1024, 0, st>>>(b.status, ntiles);
+        bin_starts_kernel<<<ntiles, SCAN_THREADS, 0, st>>>(counts, nb, b.status, start, b.keys[1], fs);
+        scatter_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], b.xyzr_in, n, start, counts, b.vals[1], b.rec_a, b.rec_b,
+                                                   b.geo, fs);
+        order_bins_kernel<<<pgrid, 256, 0, st>>>(n, g.nbins, b.keys[1], b.vals[1], start, b.xyzr_in, b.rec_a, b.rec_b,
+                                                 b.geo, fs);
+    }
+    // the radix path: alone, or as the fallback (gated) when a cell holds more than BIN_CELL_MAX particles;
+    // with the counting sort its pass count is odd so both leave the sorted keys in buffer 1
+    const FrameScalars* gate = counting ? fs : nullptr;
+    if ((e = launch_sort(b, n, g.nbins, sms, st, gate, counting)) != cudaSuccess)
+        return e;
     const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n + 1, 256), sms * 8));
-    cell_start_kernel<<<grid, 256, 0, st>>>(keys, n, nbins, start, gaps, gap_cap, fs);
-    cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs);
-    count_valid_kernel<<<1, 1, 0, st>>>(start, nbins, fs);
+    cell_start_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, start, gaps, gap_cap, fs, gate);
+    cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs, gate);
+    count_valid_kernel<<<1, 1, 0, st>>>(start, g.nbins, fs);
     return cudaGetLastError();
 }
 

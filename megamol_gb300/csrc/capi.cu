@@ -66,9 +66,10 @@ enum SideEv { SEV_FORK, SEV_NRM, SEV_GRID, SEV_JOIN, SEV_COUNT };
 // pinned mirror of the frame scalars. A context owns one pipe for p2v_run_frame and one per lane of
 // p2v_run_batch; frames on different pipes may run concurrently.
 struct Pipe {
-    DevBuf raw, xyzr, rec_a, rec_b, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
+    DevBuf raw, xyzr, rec_a, keys0, keys1, vals0, vals1, status, hist, cstart, gaps, grid, tiles, scal;
     DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list, wts, wsorted, wsum;
     DevBuf vdens, vdirs, vkeys0, vkeys1, vvals0, vvals1, vout;  // the vector aggregator's grid outputs
+    DevBuf bcount;                         // particles per cell (the counting sort)
     StencilTex stex[2];                    // the learned AO's two stencil levels as textures
     cudaEvent_t ev[EV_COUNT] = {};
     cudaEvent_t sev[SEV_COUNT] = {};
@@ -113,9 +114,9 @@ struct Pipe {
     void release() {
         if (stream)
             cudaStreamSynchronize(stream);
-        for (DevBuf* b : {&raw, &xyzr, &rec_a, &rec_b, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
+        for (DevBuf* b : {&raw, &xyzr, &rec_a, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount})
             b->release();
         stex[0].release();
         stex[1].release();
@@ -350,7 +351,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
 // copied to the pinned slot h_out at the end. Nothing here waits for the device.
 p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol, cudaStream_t st,
                                   FrameScalars* h_out, bool timed, FrameJob& job) {
-    DevBuf &raw = pp.raw, &xyzr = pp.xyzr, &rec_a = pp.rec_a, &rec_b = pp.rec_b, &keys0 = pp.keys0,
+    DevBuf &raw = pp.raw, &xyzr = pp.xyzr, &rec_a = pp.rec_a, &keys0 = pp.keys0,
            &keys1 = pp.keys1, &vals0 = pp.vals0, &vals1 = pp.vals1, &status = pp.status, &hist = pp.hist,
            &cstart = pp.cstart, &gaps = pp.gaps, &grid = pp.grid, &tiles = pp.tiles, &scal = pp.scal, &nrm = pp.nrm,
            &ao = pp.ao;
@@ -445,13 +446,17 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     const uint32_t ntiles = gather_tile_count(gc, g);
     const uint32_t gap_cap = g.nbins / 64 + 2;
     P2V_CUDA_TRY(xyzr.ensure(sizeof(float4) * (N + 1)));
-    P2V_CUDA_TRY(rec_a.ensure(sizeof(float4) * (N + 1)));
-    P2V_CUDA_TRY(rec_b.ensure(sizeof(int4) * (N + 1)));
+    P2V_CUDA_TRY(rec_a.ensure(2 * sizeof(float4) * (N + 1)));  // interleaved 32-byte records
     P2V_CUDA_TRY(keys0.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(keys1.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals0.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals1.ensure(4 * (N + 1)));
-    P2V_CUDA_TRY(status.ensure(4 * (sort_status_words(n) + 256)));
+    // the counting sort by cell when the cell table is not much larger than the particle count (it costs
+    // O(cells)); the radix sort otherwise
+    const bool counting = n > 0 && (uint64_t) g.nbins + 1 <= 16ull * n;
+    if (counting)
+        P2V_CUDA_TRY(pp.bcount.ensure(4 * ((size_t) g.nbins + 1)));
+    P2V_CUDA_TRY(status.ensure(4 * (std::max(sort_status_words(n), bin_scan_words(g.nbins)) + 256)));
     P2V_CUDA_TRY(hist.ensure(4 * sort_hist_words()));
     P2V_CUDA_TRY(cstart.ensure(4 * ((size_t) g.nbins + 1)));
     P2V_CUDA_TRY(gaps.ensure(sizeof(uint4) * gap_cap));
@@ -638,11 +643,11 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     sb.err = &fs->error;
     sb.xyzr_in = xyzr.as<float4>();
     sb.rec_a = rec_a.as<float4>();
-    sb.rec_b = rec_b.as<int4>();
+    sb.rec_b = reinterpret_cast<int4*>(rec_a.as<float4>() + 1);
     sb.geo = g;
-    P2V_CUDA_TRY(launch_sort(sb, n, g.nbins, sms, st));
+    P2V_CUDA_TRY(launch_bin_sort(sb, n, g, counting ? pp.bcount.as<uint32_t>() : nullptr, cstart.as<uint32_t>(),
+                                 gaps.as<uint4>(), gap_cap, fs, sms, st));
     const uint32_t* skeys = sb.keys[sb.result];
-    P2V_CUDA_TRY(launch_cell_start(skeys, n, g.nbins, cstart.as<uint32_t>(), gaps.as<uint4>(), gap_cap, fs, sms, st));
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
 
@@ -670,7 +675,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
                 gw.mode = GatherWeights::DOUBLE;  // the weights: plain kernel sums in FP64
                 out = pp.wsum.as<float>();
             }
-            const cudaError_t ge = launch_gather(gc, g, rec_a.as<float4>(), rec_b.as<int4>(), cstart.as<uint32_t>(),
+            const cudaError_t ge = launch_gather(gc, g, sb.rec_a, sb.rec_b, cstart.as<uint32_t>(),
                                                  out, tiles.as<TileStats>(), fs, st, gw);
             if (ge == cudaErrorInvalidValue)
                 return fail(P2V_EUNSUPPORTED, "density tile %dx%dx%d is not compiled for accumulate=%d", gc.tx, gc.ty,
@@ -829,6 +834,7 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
     }
     stats.device_error = hs.error;
     stats.ao_fallback = hs.ao_fallback;
+    stats.cell_max_count = hs.bin_maxcount;
 
     if (vol) {
         for (int a = 0; a < 3; ++a) {
@@ -1601,6 +1607,14 @@ p2v_status p2v_get_binning(p2v_ctx* c, uint32_t* keys, uint32_t* order, uint64_t
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess)
         e = cudaDeviceSynchronize();
+    // the counting sort by cell writes no sorted keys: rebuild them from the cell starts
+    const bool counted = c->stats.cell_max_count > 0 && c->stats.cell_max_count <= 32;
+    if (e == cudaSuccess && keys && pp.last_n && counted) {
+        e = launch_keys_from_starts(pp.cstart.as<uint32_t>(), pp.last_nbins, pp.last_n,
+                                    const_cast<uint32_t*>(pp.last_keys), c->sms, 0);
+        if (e == cudaSuccess)
+            e = cudaDeviceSynchronize();
+    }
     if (e == cudaSuccess && keys && pp.last_n)
         e = cudaMemcpy(keys, pp.last_keys, sizeof(uint32_t) * pp.last_n, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && order && pp.last_n)

@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
                                         hi = mid;
                                 }
                                 const uint32_t j = row_beg[lo] + (f - row_off[lo]);
-                                const float4 A = rec_a[j];
-                                const int4 B = rec_b[j];
+                                const float4 A = rec_a[REC_STRIDE * (size_t) j];
+                                const int4 B = rec_b[REC_STRIDE * (size_t) j];
                                 const float phi[3] = {A.x, A.y, A.z};
                                 const int cf[3] = {B.x, B.y, B.z};
                                 const uint32_t meta = (uint32_t) B.w;
@@ -549,8 +549,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                         hi = mid;
                                 }
                                 const uint32_t j = row_beg[lo] + (f - row_off[lo]);
-                                const float4 A = rec_a[j];
-                                const int4 B = rec_b[j];
+                                const float4 A = rec_a[REC_STRIDE * (size_t) j];
+                                const int4 B = rec_b[REC_STRIDE * (size_t) j];
                                 const float phi[3] = {A.x, A.y, A.z};
                                 const int cf[3] = {B.x, B.y, B.z};
                                 const uint32_t meta = (uint32_t) B.w;

@@ -43,6 +43,8 @@ struct FrameScalars {
     uint32_t wmax_bits;     // float bits of the largest |weight| (intensity / vector aggregators)
     uint32_t dmin_bits, dmax_bits;  // vector aggregator: density range (float bits, densities >= 0)
     uint32_t vcount;        // vector aggregator: nodes with a non-zero density
+    uint32_t bin_maxcount;  // counting sort: particles in the fullest cell (0 when the radix path ran alone)
+    uint32_t bin_nmulti;    // counting sort: cells holding two or more particles
     double mass;            // FP64 sum of the raw grid
     float vmin, vmax;       // raw grid min / max
     float out_min, out_max; // after normalisation

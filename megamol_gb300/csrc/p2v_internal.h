@@ -28,8 +28,8 @@ struct SortBuffers {
     uint32_t* status;      // look-back words, sort_status_words(n)
     uint32_t* err;
     const float4* xyzr_in; // when non-null the last pass writes every particle's gather record
-    float4* rec_a;         // (particle_record.cuh) in sorted order
-    int4* rec_b;
+    float4* rec_a;         // (particle_record.cuh) in sorted order, interleaved: rec_b = rec_a + 1, both
+    int4* rec_b;           // indexed with REC_STRIDE * position
     GridGeo geo;
     int result;            // index of the buffers holding the sorted output
 };
@@ -39,9 +39,21 @@ cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, 
 size_t sort_status_words(uint32_t n);
 size_t sort_hist_words();
 int sort_passes(uint32_t max_key);
-cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st);
-cudaError_t launch_cell_start(const uint32_t* keys, uint32_t n, uint32_t nbins, uint32_t* start, uint4* gaps,
-    uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st);
+// Stable LSD radix sort of keys[0] / vals[0]; b.result names the buffers holding the output. With a gate
+// every kernel returns at once unless the gate's counting sort overflowed; odd: an odd pass count.
+cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, cudaStream_t st,
+    const FrameScalars* gate = nullptr, bool odd = false);
+// keys[j] for sorted positions j from the cell start table (the counting sort writes no sorted keys).
+cudaError_t launch_keys_from_starts(const uint32_t* start, uint32_t nbins, uint32_t n, uint32_t* keys, int sms,
+    cudaStream_t st);
+// Words of the status buffer the counting sort's scan needs for nbins + 1 cells.
+size_t bin_scan_words(uint32_t nbins);
+// The particle binning: the stable sort of the bin keys (keys[0], vals[0] from launch_pack_keys) with the
+// gather records, and the cell start table (nbins + 1 entries). counts (nbins + 1 words) selects the
+// counting sort by cell, whose per-cell ordering handles cells of up to 32 particles; a fuller cell sends
+// the frame through the radix sort on the device. counts == nullptr: the radix sort alone.
+cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32_t* counts, uint32_t* start,
+    uint4* gaps, uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st);
 
 // Density gather configuration chosen on the host.
 enum GatherMode { GATHER_EXACT = 0, GATHER_KAHAN = 1 };

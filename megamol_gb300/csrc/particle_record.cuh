@@ -16,6 +16,11 @@
 
 namespace p2v {
 
+// The records live interleaved, 32 bytes per particle: A = {phi x, y, z, r} at float4 index 2 j and
+// B = {floor cell x, y, z, meta} at 2 j + 1, so one particle's record fills one 32-byte sector. A pointer
+// pair (rec_a, rec_b = rec_a + 1) indexed with REC_STRIDE * j addresses them.
+constexpr int REC_STRIDE = 2;
+
 struct PRecA {
     float phi[3];
     float r;

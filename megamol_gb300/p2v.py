@@ -111,7 +111,7 @@ class StatsC(C.Structure):
                 ("mass_sum", C.c_double), ("ms_upload", C.c_double), ("ms_binning", C.c_double),
                 ("ms_density", C.c_double), ("ms_normalize", C.c_double), ("ms_ao", C.c_double),
                 ("ms_download", C.c_double), ("ms_total", C.c_double), ("device_error", C.c_uint32),
-                ("ao_fallback", C.c_uint32)]
+                ("ao_fallback", C.c_uint32), ("cell_max_count", C.c_uint32)]
 
 
 class TrainParams(C.Structure):

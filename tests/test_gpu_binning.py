@@ -1,6 +1,8 @@
-"""GPU test of the cell binning: the radix sort of the bin keys must equal a CPU stable sort bit for bit
-(sorted keys, permutation and cell starts), for ordinary, ragged, out-of-box, invalid and crowded inputs
-and at the full LJ-liquid size (4,000,000 particles, 256^3 grid, 25-bit keys, three digit passes)."""
+"""GPU test of the cell binning: the sort of the bin keys must equal a CPU stable sort bit for bit (sorted
+keys, permutation and cell starts), for ordinary, ragged, out-of-box, invalid and crowded inputs and at the
+full LJ-liquid size (4,000,000 particles, 256^3 grid, 25-bit keys). Both sorting paths are covered: the
+counting sort by cell (cells of at most 32 particles, ordered by index within the cell) and the radix sort,
+alone (cell table much larger than the particle count) or as the fallback for a fuller cell."""
 import numpy as np
 import pytest
 
@@ -28,11 +30,36 @@ def check(ctx, xyzr, bbox, res, lists=None):
     assert np.array_equal(keys, rk)
     assert np.array_equal(order, ro)
     assert np.array_equal(start, rs)
+    return ctx.stats()["cell_max_count"]
+
+
+COUNTING = range(1, 33)   # cell_max_count of a frame the counting sort took
 
 
 def test_uniform_frame(ctx):
     f = synth.uniform(n=200_000, edge=50.0, res=64, seed=3)
-    check(ctx, f.xyzr, f.bbox, f.res)
+    assert check(ctx, f.xyzr, f.bbox, f.res) in COUNTING
+
+
+@pytest.mark.parametrize("fill,invalid", [(32, 0), (33, 0), (1, 32), (1, 33)])
+def test_cell_occupancy_limit(ctx, fill, invalid):
+    """One cell holding exactly `fill` particles, `invalid` particles with a NaN coordinate (they share
+    the invalid key): 32 stays with the counting sort, 33 sends the frame through the radix sort."""
+    rng = np.random.default_rng(fill + 100 * invalid)
+    n = 40_000
+    x = np.empty((n, 4), np.float32)
+    x[:, :3] = rng.uniform(0, 30, (n, 3))
+    x[:, 3] = 0.6
+    # move every particle of cell (10, 10, 10) out, then put `fill` particles into it at scattered indices
+    h = 30.0 / 29.0
+    cell = np.floor(x[:, :3] / np.float32(h)).astype(int)
+    hit = np.all(cell == 10, axis=1)
+    x[hit, :3] = np.float32(0.1)
+    idx = rng.choice(np.flatnonzero(~hit), fill + invalid, replace=False)
+    x[idx[:fill], :3] = rng.uniform(10.05 * h, 10.95 * h, (fill, 3)).astype(np.float32)
+    x[idx[fill:], 1] = np.nan
+    m = check(ctx, x, (0.0, 0.0, 0.0, 30.0, 30.0, 30.0), (30, 30, 30))
+    assert (m in COUNTING) == (max(fill, invalid) <= 32), m
 
 
 def test_out_of_box_invalid_and_crowded(ctx):
@@ -44,14 +71,15 @@ def test_out_of_box_invalid_and_crowded(ctx):
     x[::11, :3] = np.float32(17.25)                # one crowded cell (~14k particles)
     x[5::97, 3] = 0.0                              # invalid radius
     x[7::101, 1] = np.nan                          # invalid coordinate
-    check(ctx, x, (0.0, 0.0, 0.0, 40.0, 40.0, 40.0), (48, 40, 56))
+    assert check(ctx, x, (0.0, 0.0, 0.0, 40.0, 40.0, 40.0), (48, 40, 56)) > 32   # the radix fallback
 
 
 def test_ragged_sizes(ctx):
     rng = np.random.default_rng(5)
     for n in (1, 31, 4095, 4096, 4097, 70_001):
         x = np.concatenate([rng.uniform(0, 10, (n, 3)), np.full((n, 1), 0.5)], 1).astype(np.float32)
-        check(ctx, x, (0, 0, 0, 10, 10, 10), (20, 20, 20))
+        m = check(ctx, x, (0, 0, 0, 10, 10, 10), (20, 20, 20))
+        assert (m == 0) == (22 ** 3 > 16 * n), (n, m)   # a sparse frame: the radix sort alone
 
 
 def test_mixed_list_types(ctx):
@@ -69,4 +97,4 @@ def test_mixed_list_types(ctx):
 
 def test_lj_liquid_full_size(ctx):
     f = synth.lj_liquid(seed=2)
-    check(ctx, f.xyzr, f.bbox, f.res)
+    assert check(ctx, f.xyzr, f.bbox, f.res) in COUNTING
