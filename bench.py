@@ -437,7 +437,7 @@ def run_ours(args):
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP: bf16 x bf16 -> f32)", "data": "synthetic",
-                "config": dict(desc, ao=("learned AO (MLP 131-64-64-1, BF16 tensor cores) with cone-march fallback"
+                "config": dict(desc, ao=("learned AO (MLP 134-64-64-1, BF16 tensor cores) with cone-march fallback"
                                          if use_learned else "plain cone march") +
                                         ", 8 cones x 32 steps, 3-level mip, gradient normals",
                                l2="per-step working set ~0.6 GB > 126 MB L2 (no flush)"),
@@ -481,7 +481,7 @@ def run_batch_bench(args):
     frames_dev, frames_host, total = [], [], 0
     for f in traj:
         ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1,
-                       **(dparams or {}))
+                       kernel=p2v.KERNEL_BUMP, sigma=1.0)
         vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
         ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
         nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 5
+#define P2V_ABI_VERSION 6
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -198,12 +198,14 @@ typedef struct p2v_stats {
 } p2v_stats;
 
 /* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle:
- * mip levels 1 and 2 of the AO volume, each a 4x4x4 stencil of trilinear samples one texel apart centred
- * on the surface point, then the unit normal (P2V_MLP_INPUTS values); network 131 -> 64 -> 64 -> 1 with
- * SiLU, SiLU, sigmoid. Parameter vector: W1[64][131], b1[64], W2[64][64], b2[64], w3[64], b3. */
-#define P2V_MLP_INPUTS 131
+ * mip levels s and s + 1 of the AO volume, each a 4x4x4 stencil of trilinear samples one texel apart centred
+ * on the surface point, then the unit normal, then the surface point in normalised volume coordinates (the
+ * cones reach a large fraction of the volume, so AO also depends on where the point sits in it);
+ * P2V_MLP_INPUTS values. Network 134 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid. Parameter vector:
+ * W1[64][134], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define P2V_MLP_INPUTS 134
 #define P2V_MLP_HIDDEN 64
-#define P2V_MLP_PARAMS 12673
+#define P2V_MLP_PARAMS 12865
 
 typedef struct p2v_train_params {
     uint32_t struct_size;   /* sizeof(p2v_train_params); set by p2v_train_params_default */

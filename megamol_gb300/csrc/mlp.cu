@@ -1,9 +1,11 @@
 // Learned AO: a small MLP that stands in for the cone march.
 //
-// Input (131): two consecutive mip levels of the AO volume (the levels the cone's first samples read), each
+// Input (134): two consecutive mip levels of the AO volume (the levels the cone's first samples read), each
 // resampled as a 4x4x4 stencil of trilinear samples
 // centred on the particle's surface point (sample spacing = one texel of that level, so the stencil moves
-// continuously with the point), then the unit normal. Network 131 -> 64 -> 64 -> 1, SiLU, SiLU, sigmoid.
+// continuously with the point), then the unit normal and the surface point in normalised volume coordinates
+// (the cones reach far into the volume, so AO also depends on where in the volume the point lies).
+// Network 134 -> 64 -> 64 -> 1, SiLU, SiLU, sigmoid.
 // Training: FP32 forward/backward kernels per CTA with a fixed-order reduction of the per-CTA gradients,
 // then Adam; pairs come from the plain cone march. Inference: BF16 weights and features, FP32 accumulation
 // on the 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM), bias/activations in FP32. A
@@ -164,6 +166,9 @@ __global__ void __launch_bounds__(128) mlp_collect_kernel(const ConeParams cp, c
     x[128] = n[0];
     x[129] = n[1];
     x[130] = n[2];
+    x[131] = u[0];
+    x[132] = u[1];
+    x[133] = u[2];
     T[i] = ao[o];
     atomicAdd(kept, 1u);
 }
@@ -607,6 +612,19 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
                 valid = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f &&
                         mlp_point(cp, p, args.nrm[o], u, nn);
             }
+            // features 128..143 first (the normal and the position are then no longer needed): the normal,
+            // the position and zero padding (chunk 16 on half 0, chunk 17 on half 1)
+            if (half == 0) {
+                const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
+                const __nv_bfloat162 n2u0 = __floats2bfloat162_rn(nn[2], u[0]);
+                const __nv_bfloat162 u12 = __floats2bfloat162_rn(u[1], u[2]);
+                st_shared_v4(sA + canon_off(row, 128, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
+                             *reinterpret_cast<const uint32_t*>(&n2u0), *reinterpret_cast<const uint32_t*>(&u12), 0u);
+                if (valid && check)
+                    oor |= !(in_range(64, n01) && in_range(65, n2u0) && in_range(66, u12));
+            } else {
+                st_shared_v4(sA + canon_off(row, 136, tc::SBO1), 0u, 0u, 0u, 0u);
+            }
             uint8_t* arow = sA + canon_off(row, 64 * half, tc::SBO1);
             if (valid) {
                 // z row kz of the stencil = two 16-byte chunks of the A row
@@ -630,17 +648,6 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
                     st_shared_v4(arow + c * 128, 0u, 0u, 0u, 0u);
-            }
-            // features 128..143: the normal and zero padding (chunk 16 on half 0, chunk 17 on half 1)
-            if (half == 0) {
-                const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
-                const __nv_bfloat162 n2 = __floats2bfloat162_rn(nn[2], 0.0f);
-                st_shared_v4(sA + canon_off(row, 128, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
-                             *reinterpret_cast<const uint32_t*>(&n2), 0u, 0u);
-                if (valid && check)
-                    oor |= !(in_range(64, n01) && in_range(65, n2));
-            } else {
-                st_shared_v4(sA + canon_off(row, 136, tc::SBO1), 0u, 0u, 0u, 0u);
             }
             oor = oor && valid;
         }

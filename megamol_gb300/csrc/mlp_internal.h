@@ -10,7 +10,7 @@
 
 namespace p2v {
 
-constexpr int MLP_IN = 131;   // 2 levels x 64 stencil samples + 3 normal components
+constexpr int MLP_IN = 134;   // 2 levels x 64 stencil samples, 3 normal components, 3 position components
 constexpr int MLP_KP = 144;   // input padded to a multiple of the MMA K (16)
 constexpr int MLP_H = 64;
 // parameter vector: W1[H][IN], b1[H], W2[H][H], b2[H], w3[H], b3
