@@ -426,13 +426,18 @@ def run_ours(args):
                "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on "
                          f"{ao_sample(f)} particles scaled to the frame ({dt_ao:.2f} s)"}
 
-    # kernels per frame: scalar init, pack, digit histogram + scan, the radix passes (9/8-bit digits over the
-    # bin keys), cell starts (3), gather, finalize + normalise; AO: normals, mips, then the cone march or
-    # stencil textures (2) + tensor-core inference + fallback cone march
+    # kernels per frame: scalar init, pack, [the counting sort by cell: histogram, tile sums, tile scan, cell
+    # starts, scatter, in-cell order], digit histogram + scan, the radix passes (9/8-bit digits over the bin
+    # keys; an odd count and launched gated after a counting sort), cell starts (3), gather, finalize +
+    # normalise; AO: normals, mips, sorted copies, then the cone march or stencil textures (2) + tensor-core
+    # inference + fallback cone march, and the AO back to input order
     key_bits = int(nb).bit_length()
     passes = (key_bits + 8) // 9
-    launches_density = 1 + 1 + 2 + passes + 3 + 1 + 2
-    launches_ao = 1 + (AO_PARAMS["ao_levels"] - 1) + (4 if use_learned else 1)
+    counting = nb + 1 <= 16 * f.n
+    if counting and passes % 2 == 0:
+        passes += 1
+    launches_density = 1 + 1 + (6 if counting else 0) + 2 + passes + 3 + 1 + 2
+    launches_ao = 1 + (AO_PARAMS["ao_levels"] - 1) + 1 + (5 if use_learned else 2)
     if rank == 0:
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,

@@ -271,6 +271,25 @@ __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const Cone
     }
 }
 
+// Positions and normals in sorted (cell) order: the AO kernels then read them coalesced whatever the input
+// order was (a streaming kernel keeps many of these scattered reads in flight; inside the latency-bound AO
+// kernels they stalled every tile), and the AO returns to input order once at the end.
+__global__ void __launch_bounds__(256) sort_particles_kernel(const uint32_t* __restrict__ order, uint32_t n,
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, float4* __restrict__ xyzr_s,
+    float4* __restrict__ nrm_s) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t o = order[j];
+        xyzr_s[j] = xyzr[o];
+        nrm_s[j] = nrm[o];
+    }
+}
+
+__global__ void __launch_bounds__(256) unsort_ao_kernel(const uint32_t* __restrict__ order, uint32_t n,
+    const float* __restrict__ ao_s, float* __restrict__ ao) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        ao[order[j]] = ao_s[j];
+}
+
 // ---------------------------------------------------------------------------------------------
 // AOSphere volume: nearest inner voxel, (4/3 pi r^3 / voxel volume) * genFac, summed exactly in
 // 64-bit fixed point (2^-32) so the result does not depend on the particle order.
@@ -417,6 +436,23 @@ cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32
     fixed_to_float_kernel<<<grd, 256, 0, st>>>(acc, nv, tex);
     if (n > 0)
         aosphere_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(ap, tex, order, xyzr, nrm, n, mode, ao);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_particles(const uint32_t* order, uint32_t n, const float4* xyzr, const float4* nrm,
+                                  float4* xyzr_s, float4* nrm_s, int sms, cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
+    sort_particles_kernel<<<grd, 256, 0, st>>>(order, n, xyzr, nrm, xyzr_s, nrm_s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unsort_ao(const uint32_t* order, uint32_t n, const float* ao_s, float* ao, int sms, cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
+    unsort_ao_kernel<<<grd, 256, 0, st>>>(order, n, ao_s, ao);
     return cudaGetLastError();
 }
 

@@ -56,6 +56,10 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
 cudaError_t launch_mdao_volume(const MdaoParams& mp, const uint32_t* order, const float4* xyzr, uint32_t n,
     void* acc, float* vol, int sms, cudaStream_t st);
 // n_dev (nullable): device-side particle count, at most n (the cone march of the learned-AO fallback list)
+// xyzr_s[j] = xyzr[order[j]], nrm_s[j] = nrm[order[j]] (sorted order), and back for the AO values.
+cudaError_t launch_sort_particles(const uint32_t* order, uint32_t n, const float4* xyzr, const float4* nrm,
+    float4* xyzr_s, float4* nrm_s, int sms, cudaStream_t st);
+cudaError_t launch_unsort_ao(const uint32_t* order, uint32_t n, const float* ao_s, float* ao, int sms, cudaStream_t st);
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
     uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st);
 cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc,

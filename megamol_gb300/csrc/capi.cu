@@ -70,6 +70,7 @@ struct Pipe {
     DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list, wts, wsorted, wsum;
     DevBuf vdens, vdirs, vkeys0, vkeys1, vvals0, vvals1, vout;  // the vector aggregator's grid outputs
     DevBuf bcount;                         // particles per cell (the counting sort)
+    DevBuf xyzr_s, nrm_s, ao_s;            // positions, normals and AO in sorted order (the cone AO stages)
     StencilTex stex[2];                    // the learned AO's two stencil levels as textures
     cudaEvent_t ev[EV_COUNT] = {};
     cudaEvent_t sev[SEV_COUNT] = {};
@@ -116,7 +117,7 @@ struct Pipe {
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &xyzr_s, &nrm_s, &ao_s})
             b->release();
         stex[0].release();
         stex[1].release();
@@ -1019,12 +1020,28 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
     DevBuf &xyzr = pp.xyzr, &nrm = pp.nrm, &ao = pp.ao, &scal = pp.scal, &fb_list = pp.fb_list,
            &aos_acc = pp.aos_acc, &aos_tex = pp.aos_tex;
     const p2v_params& P = prm;
+    // the cone-march stages run on sorted copies of the positions and normals (coalesced whatever the input
+    // order) and scatter the AO back to input order at the end
+    auto to_sorted = [&]() -> cudaError_t {
+        cudaError_t e = pp.xyzr_s.ensure(sizeof(float4) * ((size_t) n + 1));
+        if (e == cudaSuccess)
+            e = pp.nrm_s.ensure(sizeof(float4) * ((size_t) n + 1));
+        if (e == cudaSuccess)
+            e = pp.ao_s.ensure(sizeof(float) * ((size_t) n + 1));
+        if (e == cudaSuccess)
+            e = launch_sort_particles(order, n, xyzr.as<float4>(), nrm.as<float4>(), pp.xyzr_s.as<float4>(),
+                                      pp.nrm_s.as<float4>(), sms, st);
+        return e;
+    };
     if (P.ao_mode == P2V_AO_CONE) {
         ConeParams cp{};
         const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st);
         if (bs != P2V_OK)
             return bs;
-        P2V_CUDA_TRY(launch_cone_ao(cp, order, xyzr.as<float4>(), nrm.as<float4>(), n, nullptr, ao.as<float>(), st));
+        P2V_CUDA_TRY(to_sorted());
+        P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr,
+                                    pp.ao_s.as<float>(), st));
+        P2V_CUDA_TRY(launch_unsort_ao(order, n, pp.ao_s.as<float>(), ao.as<float>(), sms, st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_LEARNED) {
@@ -1049,18 +1066,20 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         a.w2h = mlp_w2h.as<__nv_bfloat16>();
         a.lo = mlp_has_range ? mlp_lo.as<float>() : nullptr;
         a.hi = mlp_has_range ? mlp_hi.as<float>() : nullptr;
+        P2V_CUDA_TRY(to_sorted());
         a.n = n;
-        a.order = order;
-        a.xyzr = xyzr.as<float4>();
-        a.nrm = nrm.as<float4>();
-        a.y = ao.as<float>();
+        a.order = nullptr;  // sorted copies: position j is sorted position j
+        a.xyzr = pp.xyzr_s.as<float4>();
+        a.nrm = pp.nrm_s.as<float4>();
+        a.y = pp.ao_s.as<float>();
         a.fallback = fb_list.as<uint32_t>();
         a.nfallback = &fs->ao_fallback;
         a.err = &fs->error;
         P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
         // the plain cone march for every particle whose stencil left the training range
-        P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), xyzr.as<float4>(), nrm.as<float4>(), n,
-                                    &fs->ao_fallback, ao.as<float>(), st));
+        P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n,
+                                    &fs->ao_fallback, pp.ao_s.as<float>(), st));
+        P2V_CUDA_TRY(launch_unsort_ao(order, n, pp.ao_s.as<float>(), ao.as<float>(), sms, st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_AOSPHERE_AXES || P.ao_mode == P2V_AO_AOSPHERE_NORMAL) {

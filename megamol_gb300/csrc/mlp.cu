@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
         } else {
             float u[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
             if (valid) {
-                o = args.order[pi];
+                o = args.order ? args.order[pi] : pi;
                 const float4 p = args.xyzr[o];
                 valid = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f &&
                         mlp_point(cp, p, args.nrm[o], u, nn);
