@@ -433,7 +433,7 @@ def run_ours(args):
     # inference + fallback cone march, and the AO back to input order
     key_bits = int(nb).bit_length()
     passes = (key_bits + 8) // 9
-    counting = nb + 1 <= 16 * f.n
+    counting = nb + 1 <= 64 * f.n
     if counting and passes % 2 == 0:
         passes += 1
     launches_density = 1 + 1 + (6 if counting else 0) + 2 + passes + 3 + 1 + 2

@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
     for (int i = 0; i < SORT_ITEMS; ++i) {
         const uint32_t j = wbase + i * 32 + lane;
         k[i] = j < n ? keys_in[j] : 0u;
-        v[i] = j < n ? vals_in[j] : 0u;
+        v[i] = j < n ? (vals_in ? vals_in[j] : j) : 0u;  // no input values: the identity (particle indices)
     }
     const uint32_t lt_mask = (1u << lane) - 1u;
 #pragma unroll
@@ -445,11 +445,12 @@ __global__ void __launch_bounds__(256) cell_gap_fill_kernel(const uint4* __restr
 }
 
 // ---- counting sort by cell ----
-// counts[key] = particles per key, keys in [0, nbins] (nbins: the invalid particles)
+// counts[key] = particles per key, keys in [0, nbins] (nbins: the invalid particles); rank[i] = the
+// particle's arrival rank in its cell (its slot there until order_bins_kernel fixes the order)
 __global__ void __launch_bounds__(256) count_bins_kernel(const uint32_t* __restrict__ keys, uint32_t n,
-                                                         uint32_t* __restrict__ counts) {
+                                                         uint32_t* __restrict__ counts, uint32_t* __restrict__ rank) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        atomicAdd(counts + keys[i], 1u);
+        rank[i] = atomicAdd(counts + keys[i], 1u);
 }
 
 constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 16, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
@@ -612,18 +613,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) bin_starts_kernel(const uint32_t
     }
 }
 
-// Each particle takes a slot of its cell (arrival order within the cell, fixed by order_bins_kernel) and
-// writes its index and its 32-byte gather record there. The sorted keys are not written: the cell starts
-// hold them (keys_from_starts_kernel rebuilds them for the binning readback).
+// Each particle takes slot start[key] + rank of its cell (arrival order within the cell, fixed by
+// order_bins_kernel) and writes its index and its 32-byte gather record there. The sorted keys are not
+// written: the cell starts hold them (keys_from_starts_kernel rebuilds them for the binning readback).
 __global__ void __launch_bounds__(256) scatter_bins_kernel(const uint32_t* __restrict__ keys_in,
-    const float4* __restrict__ xyzr, uint32_t n, const uint32_t* __restrict__ start, uint32_t* __restrict__ counts,
-    uint32_t* __restrict__ vals_out, float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo,
-    const FrameScalars* __restrict__ fs) {
+    const uint32_t* __restrict__ rank, const float4* __restrict__ xyzr, uint32_t n,
+    const uint32_t* __restrict__ start, uint32_t* __restrict__ vals_out, float4* __restrict__ rec_a,
+    int4* __restrict__ rec_b, GridGeo geo, const FrameScalars* __restrict__ fs) {
     if (fs->bin_maxcount > BIN_CELL_MAX)
         return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t k = keys_in[i];
-        const uint32_t slot = start[k] + atomicSub(counts + k, 1u) - 1u;
+        const uint32_t slot = start[keys_in[i]] + rank[i];
         vals_out[slot] = i;
         float4 A;
         int4 B;
@@ -751,7 +751,8 @@ cudaError_t launch_onesweep_bits(uint32_t tiles, SortBuffers& b, int cur, uint32
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess)
         return e;
-    onesweep_kernel<GATHER, BITS><<<tiles, SORT_THREADS, smem, st>>>(b.keys[cur], b.vals[cur], b.keys[cur ^ 1],
+    onesweep_kernel<GATHER, BITS><<<tiles, SORT_THREADS, smem, st>>>(b.keys[cur],
+        (cur == 0 && b.implicit_vals0 && b.first_pass) ? nullptr : b.vals[cur], b.keys[cur ^ 1],
         b.vals[cur ^ 1], n, shift, offs, counter, b.status, b.err, GATHER ? b.xyzr_in : nullptr,
         GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, b.geo, gate);
     return cudaSuccess;
@@ -779,6 +780,7 @@ cudaError_t launch_sort(SortBuffers& b, uint32_t n, uint32_t max_key, int sms, c
     radix_scan_kernel<<<1, MAX_RADIX, 0, st>>>(b.hist, pl.passes, gate);
     int cur = 0;
     for (int p = 0; p < pl.passes; ++p) {
+        b.first_pass = p == 0;
         e = cudaMemsetAsync(b.status, 0, sizeof(uint32_t) * (size_t) tiles * ((size_t) 1 << pl.bits[p]), st);
         if (e != cudaSuccess)
             return e;
@@ -819,14 +821,16 @@ cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32
         if ((e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * nb, st)) != cudaSuccess)
             return e;
         const unsigned pgrid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
-        count_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], n, counts);
+        // ranks in vals[0]: the gated radix sort then takes the identity as its first pass' values
+        b.implicit_vals0 = true;
+        count_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], n, counts, b.vals[0]);
         // tile sums in the status buffer; the multi-particle cell list in keys[1] (the counting sort writes no
         // sorted keys there)
         bin_tile_sums_kernel<<<ntiles, SCAN_THREADS, 0, st>>>(counts, nb, b.status, fs);
         bin_tile_scan_kernel<<<1, 1024, 0, st>>>(b.status, ntiles);
         bin_starts_kernel<<<ntiles, SCAN_THREADS, 0, st>>>(counts, nb, b.status, start, b.keys[1], fs);
-        scatter_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], b.xyzr_in, n, start, counts, b.vals[1], b.rec_a, b.rec_b,
-                                                   b.geo, fs);
+        scatter_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], b.vals[0], b.xyzr_in, n, start, b.vals[1], b.rec_a,
+                                                   b.rec_b, b.geo, fs);
         order_bins_kernel<<<pgrid, 256, 0, st>>>(n, g.nbins, b.keys[1], b.vals[1], start, b.xyzr_in, b.rec_a, b.rec_b,
                                                  b.geo, fs);
     }

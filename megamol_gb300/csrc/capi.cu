@@ -452,9 +452,10 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     P2V_CUDA_TRY(keys1.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals0.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals1.ensure(4 * (N + 1)));
-    // the counting sort by cell when the cell table is not much larger than the particle count (it costs
-    // O(cells)); the radix sort otherwise
-    const bool counting = n > 0 && (uint64_t) g.nbins + 1 <= 16ull * n;
+    // the counting sort by cell unless the cell table dwarfs the particle count: it passes over the table
+    // about four times (16 bytes per cell), where the radix sort spends ~150 bytes and several latency-bound
+    // passes per particle
+    const bool counting = n > 0 && (uint64_t) g.nbins + 1 <= 64ull * n;
     if (counting)
         P2V_CUDA_TRY(pp.bcount.ensure(4 * ((size_t) g.nbins + 1)));
     P2V_CUDA_TRY(status.ensure(4 * (std::max(sort_status_words(n), bin_scan_words(g.nbins)) + 256)));

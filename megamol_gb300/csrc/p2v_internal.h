@@ -32,6 +32,8 @@ struct SortBuffers {
     int4* rec_b;           // indexed with REC_STRIDE * position
     GridGeo geo;
     int result;            // index of the buffers holding the sorted output
+    bool implicit_vals0;   // vals[0] holds no input values: the first pass takes the identity (indices)
+    bool first_pass;       // set by launch_sort for its own bookkeeping
 };
 
 cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,

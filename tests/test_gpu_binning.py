@@ -79,7 +79,7 @@ def test_ragged_sizes(ctx):
     for n in (1, 31, 4095, 4096, 4097, 70_001):
         x = np.concatenate([rng.uniform(0, 10, (n, 3)), np.full((n, 1), 0.5)], 1).astype(np.float32)
         m = check(ctx, x, (0, 0, 0, 10, 10, 10), (20, 20, 20))
-        assert (m == 0) == (22 ** 3 > 16 * n), (n, m)   # a sparse frame: the radix sort alone
+        assert (m == 0) == (22 ** 3 > 64 * n), (n, m)   # a sparse frame: the radix sort alone
 
 
 def test_mixed_list_types(ctx):
