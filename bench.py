@@ -360,6 +360,10 @@ def run_ours(args):
             return float(t.item())
         return x
 
+    # ---- the density tile for this frame: the autotuner times the compiled tiles on it (density only);
+    # both pipelines below use the winner ----
+    ctx.set_params(ao_mode=p2v.AO_NONE, tile_x=0, tile_y=0, tile_z=0)
+    tune = ctx.autotune_batch([dict(lists=dev_lists, bbox=f.bbox, out=d_out, size=f.res)])
     # ---- plain cone-march pipeline ----
     ctx.set_params(ao_mode=p2v.AO_CONE)
     ms_plain, st_plain = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier,
@@ -454,6 +458,8 @@ def run_ours(args):
                                      "plain_ao_ms": st_plain["ms_ao"], "learned_ao_ms": st_learn["ms_ao"],
                                      "training": {"pairs": pairs, "val_rmse": train_rep["val_rmse"],
                                                   "steps": train_rep["steps"], "ms": train_rep["ms"]}},
+                "density_tile": {"tile": tune["tile"], "candidates_ms": {"x".join(map(str, c["tile"])): c["ms"]
+                                                                         for c in tune["candidates"] if c["lanes"] == 1}},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": (launches_density + launches_ao) * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)

@@ -790,18 +790,58 @@ __global__ void __launch_bounds__(1024) finalize_kernel(const TileStats* __restr
     }
 }
 
+__device__ __forceinline__ float normalize_one(float v, float ms, float off, float sc, int mass_normalize,
+                                               int minmax_normalize) {
+    if (mass_normalize)
+        v = v * ms;
+    if (minmax_normalize)
+        v = (v - off) * sc;
+    return v;
+}
+
+__global__ void __launch_bounds__(256) normalize_scalar_kernel(float* __restrict__ grid, uint64_t n,
+    const FrameScalars* __restrict__ fs, int mass_normalize, int minmax_normalize) {
+    const float ms = (float) fs->mass_scale;
+    const float off = fs->offset, sc = fs->scale;
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+        grid[i] = normalize_one(grid[i], ms, off, sc, mass_normalize, minmax_normalize);
+}
+
+// Streams the grid in 16-byte vectors, four per thread per round (many loads in flight); the tail past
+// the last whole vector is done element-wise.
 __global__ void __launch_bounds__(256) normalize_kernel(float* __restrict__ grid, uint64_t n,
     const FrameScalars* __restrict__ fs, int mass_normalize, int minmax_normalize) {
     const float ms = (float) fs->mass_scale;
     const float off = fs->offset, sc = fs->scale;
-    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
-        float v = grid[i];
-        if (mass_normalize)
-            v = v * ms;
-        if (minmax_normalize)
-            v = (v - off) * sc;
-        grid[i] = v;
+    float4* g4 = reinterpret_cast<float4*>(grid);
+    const uint64_t n4 = n / 4;
+    const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+    uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            v[u] = g4[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u].x = normalize_one(v[u].x, ms, off, sc, mass_normalize, minmax_normalize);
+            v[u].y = normalize_one(v[u].y, ms, off, sc, mass_normalize, minmax_normalize);
+            v[u].z = normalize_one(v[u].z, ms, off, sc, mass_normalize, minmax_normalize);
+            v[u].w = normalize_one(v[u].w, ms, off, sc, mass_normalize, minmax_normalize);
+            g4[i + u * stride] = v[u];
+        }
     }
+    for (; i < n4; i += stride) {
+        float4 v = g4[i];
+        v.x = normalize_one(v.x, ms, off, sc, mass_normalize, minmax_normalize);
+        v.y = normalize_one(v.y, ms, off, sc, mass_normalize, minmax_normalize);
+        v.z = normalize_one(v.z, ms, off, sc, mass_normalize, minmax_normalize);
+        v.w = normalize_one(v.w, ms, off, sc, mass_normalize, minmax_normalize);
+        g4[i] = v;
+    }
+    const uint64_t t = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+    if (t < n - 4 * n4)
+        grid[4 * n4 + t] = normalize_one(grid[4 * n4 + t], ms, off, sc, mass_normalize, minmax_normalize);
 }
 
 }  // namespace
@@ -881,7 +921,13 @@ cudaError_t launch_normalize_modes(float* grid, uint64_t nvox, const FrameScalar
     int minmax_normalize, int sms, cudaStream_t st) {
     if (!mass_normalize && !minmax_normalize)
         return cudaSuccess;
-    const unsigned grd = (unsigned) std::max<uint64_t>(1, std::min<uint64_t>((nvox + 255) / 256, (uint64_t) sms * 16));
+    // the grid starts 16-byte aligned (cudaMalloc, or a caller's device buffer checked below)
+    if (reinterpret_cast<uintptr_t>(grid) % 16 != 0) {
+        const unsigned g1 = (unsigned) std::max<uint64_t>(1, std::min<uint64_t>((nvox + 255) / 256, (uint64_t) sms * 16));
+        normalize_scalar_kernel<<<g1, 256, 0, st>>>(grid, nvox, fs, mass_normalize, minmax_normalize);
+        return cudaGetLastError();
+    }
+    const unsigned grd = (unsigned) std::max<uint64_t>(1, std::min<uint64_t>((nvox / 4 + 255) / 256, (uint64_t) sms * 8));
     normalize_kernel<<<grd, 256, 0, st>>>(grid, nvox, fs, mass_normalize, minmax_normalize);
     return cudaGetLastError();
 }
