@@ -446,7 +446,7 @@ def run_ours(args):
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP: bf16 x bf16 -> f32)", "data": "synthetic",
-                "config": dict(desc, ao=("learned AO (MLP 134-64-64-1, BF16 tensor cores) with cone-march fallback"
+                "config": dict(desc, ao=("learned AO (MLP 60-64-64-1, BF16 tensor cores) with cone-march fallback"
                                          if use_learned else "plain cone march") +
                                         ", 8 cones x 32 steps, 3-level mip, gradient normals",
                                l2="per-step working set ~0.6 GB > 126 MB L2 (no flush)"),

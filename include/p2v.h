@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 6
+#define P2V_ABI_VERSION 7
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -198,14 +198,14 @@ typedef struct p2v_stats {
 } p2v_stats;
 
 /* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle:
- * mip levels s and s + 1 of the AO volume, each a 4x4x4 stencil of trilinear samples one texel apart centred
- * on the surface point, then the unit normal, then the surface point in normalised volume coordinates (the
- * cones reach a large fraction of the volume, so AO also depends on where the point sits in it);
- * P2V_MLP_INPUTS values. Network 134 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid. Parameter vector:
- * W1[64][134], b1[64], W2[64][64], b2[64], w3[64], b3. */
-#define P2V_MLP_INPUTS 134
+ * mip levels s and s + 1 of the AO volume, each a 3x3x3 stencil of trilinear samples 1.5 texels apart
+ * centred on the surface point (in the order kz*9 + ky*3 + kx), then the unit normal, then the surface point
+ * in normalised volume coordinates (the cones reach a large fraction of the volume, so AO also depends on
+ * where the point sits in it); P2V_MLP_INPUTS values. Network 60 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid.
+ * Parameter vector: W1[64][60], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define P2V_MLP_INPUTS 60
 #define P2V_MLP_HIDDEN 64
-#define P2V_MLP_PARAMS 12865
+#define P2V_MLP_PARAMS 8129
 
 typedef struct p2v_train_params {
     uint32_t struct_size;   /* sizeof(p2v_train_params); set by p2v_train_params_default */

@@ -1736,7 +1736,7 @@ void p2v_train_params_default(p2v_train_params* tp) {
     std::memset(tp, 0, sizeof(*tp));
     tp->struct_size = sizeof(p2v_train_params);
     tp->epochs = 16;
-    tp->batch = 4096;
+    tp->batch = 2048;
     tp->lr = 3e-3f;
     tp->beta1 = 0.9f;
     tp->beta2 = 0.999f;

@@ -1,11 +1,10 @@
 // Learned AO: a small MLP that stands in for the cone march.
 //
-// Input (134): two consecutive mip levels of the AO volume (the levels the cone's first samples read), each
-// resampled as a 4x4x4 stencil of trilinear samples
-// centred on the particle's surface point (sample spacing = one texel of that level, so the stencil moves
-// continuously with the point), then the unit normal and the surface point in normalised volume coordinates
-// (the cones reach far into the volume, so AO also depends on where in the volume the point lies).
-// Network 134 -> 64 -> 64 -> 1, SiLU, SiLU, sigmoid.
+// Input (60): two consecutive mip levels of the AO volume (the levels the cone's first samples read), each
+// resampled as a 3x3x3 stencil of trilinear samples 1.5 texels apart centred on the particle's surface
+// point (the stencil moves continuously with the point), then the unit normal and the surface point in
+// normalised volume coordinates (the cones reach far into the volume, so AO also depends on where in the
+// volume the point lies). Network 60 -> 64 -> 64 -> 1, SiLU, SiLU, sigmoid.
 // Training: FP32 forward/backward kernels per CTA with a fixed-order reduction of the per-CTA gradients,
 // then Adam; pairs come from the plain cone march. Inference: BF16 weights and features, FP32 accumulation
 // on the 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM), bias/activations in FP32. A
@@ -40,63 +39,39 @@ __device__ __forceinline__ float sigmoidf_(float a) {
     return 1.0f / (1.0f + __expf(-a));
 }
 
-// 4x4x4 trilinear samples of one mip level at texel-spaced offsets (k - 1.5) around normalised point u.
+// 3x3x3 trilinear samples of one mip level at offsets 1.5 (k - 1) texels around normalised point u (the
+// extent of a 4x4x4 stencil one texel apart, with 27 samples instead of 64), in the order kz*9 + ky*3 + kx.
 // The level is a layered 2D texture of FP16 pairs: layer L holds z slices L - 1 (red) and L (green), so one
-// bilinear fetch (GL LINEAR in x and y, CLAMP_TO_BORDER) filters two slices; slices outside the level are
-// 0, as the border. The five slices the stencil spans take three fetches per (x, y) position (48 per level
-// where one slice per fetch takes 80); the z interpolation runs in FP32. emit(kz, v) receives the 16
-// samples of z row kz, in the order ky*4 + kx. The features feed a BF16 network, so the texture filter's
+// bilinear fetch (GL LINEAR in x and y, CLAMP_TO_BORDER) returns both slices around a sample's z; the z
+// interpolation runs in FP32 with the sample's own fraction; slices outside the level are 0, as the border.
+// The 27 fetches do not depend on each other. The features feed a BF16 network, so the texture filter's
 // 8-bit weight fractions sit below the features' own rounding; training pairs are extracted by the same
 // code.
-template<class Emit>
-__device__ __forceinline__ void stencil64(unsigned long long tex, const float inv[3], int nz, float ux, float uy,
-                                          float uz, Emit&& emit) {
-    float px[4], py[4];
+__device__ __forceinline__ void stencil27(unsigned long long tex, const float inv[3], int nz, float ux, float uy,
+                                          float uz, float v[MLP_STENCIL]) {
+    float px[3], py[3];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        px[k] = fmaf((float) k - 1.5f, inv[0], ux);
-        py[k] = fmaf((float) k - 1.5f, inv[1], uy);
+    for (int k = 0; k < 3; ++k) {
+        px[k] = fmaf(1.5f * (float) (k - 1), inv[0], ux);
+        py[k] = fmaf(1.5f * (float) (k - 1), inv[1], uy);
     }
-    const float cz = uz * (float) nz - 2.0f;
-    const float fz0 = floorf(cz);
-    const float fz = cz - fz0;
-    const int z0 = (int) fz0;
-    float prev[16];  // the last slice of the previous pair
-#pragma unroll 1
-    for (int q = 0; q < 3; ++q) {
-        // slices z0 + 2q and z0 + 2q + 1 live in layer z0 + 2q + 1
-        const int layer = z0 + 2 * q + 1;
-        float lo[16], hi[16];
-        if (layer >= 0 && layer <= nz) {
 #pragma unroll
-            for (int ky = 0; ky < 4; ++ky)
+    for (int kz = 0; kz < 3; ++kz) {
+        // texel-space z of the sample minus the half texel: slices z0 and z0 + 1 live in layer z0 + 1
+        const float zs = fmaf(uz, (float) nz, 1.5f * (float) (kz - 1) - 0.5f);
+        const float z0f = floorf(zs);
+        const float fz = zs - z0f;
+        const int layer = (int) z0f + 1;
+        const bool in = layer >= 0 && layer <= nz;
 #pragma unroll
-                for (int kx = 0; kx < 4; ++kx) {
-                    const float2 v = tex2DLayered<float2>((cudaTextureObject_t) tex, px[kx], py[ky], layer);
-                    lo[ky * 4 + kx] = v.x;
-                    hi[ky * 4 + kx] = v.y;
-                }
-        } else {
+        for (int ky = 0; ky < 3; ++ky)
 #pragma unroll
-            for (int k = 0; k < 16; ++k)
-                lo[k] = hi[k] = 0.0f;
-        }
-        float v[16];
-        if (q > 0) {  // z row 2q - 1: slices 2q - 1 and 2q
-#pragma unroll
-            for (int k = 0; k < 16; ++k)
-                v[k] = prev[k] + fz * (lo[k] - prev[k]);
-            emit(2 * q - 1, v);
-        }
-        if (q < 2) {  // z row 2q: slices 2q and 2q + 1
-#pragma unroll
-            for (int k = 0; k < 16; ++k)
-                v[k] = lo[k] + fz * (hi[k] - lo[k]);
-            emit(2 * q, v);
-        }
-#pragma unroll
-        for (int k = 0; k < 16; ++k)
-            prev[k] = hi[k];
+            for (int kx = 0; kx < 3; ++kx) {
+                float2 t = make_float2(0.0f, 0.0f);
+                if (in)
+                    t = tex2DLayered<float2>((cudaTextureObject_t) tex, px[kx], py[ky], layer);
+                v[kz * 9 + ky * 3 + kx] = t.x + fz * (t.y - t.x);
+            }
     }
 }
 
@@ -156,19 +131,19 @@ __global__ void __launch_bounds__(128) mlp_collect_kernel(const ConeParams cp, c
         return;
     }
     float* x = X + (size_t) i * MLP_IN;
+    float v[MLP_STENCIL];
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
-        stencil64(cp.stex[h], cp.sinv[h], cp.lv[cp.stencil_level + h].d[2], u[0], u[1], u[2],
-                  [&](int kz, const float* v) {
-                      for (int k = 0; k < 16; ++k)
-                          x[64 * h + 16 * kz + k] = v[k];
-                  });
-    x[128] = n[0];
-    x[129] = n[1];
-    x[130] = n[2];
-    x[131] = u[0];
-    x[132] = u[1];
-    x[133] = u[2];
+    for (int h = 0; h < 2; ++h) {
+        stencil27(cp.stex[h], cp.sinv[h], cp.lv[cp.stencil_level + h].d[2], u[0], u[1], u[2], v);
+        for (int k = 0; k < MLP_STENCIL; ++k)
+            x[MLP_STENCIL * h + k] = v[k];
+    }
+    x[54] = n[0];
+    x[55] = n[1];
+    x[56] = n[2];
+    x[57] = u[0];
+    x[58] = u[1];
+    x[59] = u[2];
     T[i] = ao[o];
     atomicAdd(kept, 1u);
 }
@@ -392,7 +367,8 @@ __global__ void mlp_pack_kernel(const float* __restrict__ P, __nv_bfloat16* __re
     __nv_bfloat16* __restrict__ w2h) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < MLP_H * MLP_KP; k += gridDim.x * blockDim.x) {
         const int j = k / MLP_KP, i = k % MLP_KP;
-        w1h[k] = __float2bfloat16_rn(i < MLP_IN ? P[OFF_W1 + j * MLP_IN + i] : 0.0f);
+        const int f = mlp_feature_at(i);
+        w1h[k] = __float2bfloat16_rn(f >= 0 ? P[OFF_W1 + j * MLP_IN + f] : 0.0f);
     }
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < MLP_H * MLP_H; k += gridDim.x * blockDim.x)
         w2h[k] = __float2bfloat16_rn(P[OFF_W2 + k]);
@@ -406,8 +382,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // ---------------------------------------------------------------------------------------------
 // Inference on the 5th-generation tensor cores (tcgen05). One CTA of 256 threads takes 128 particles per
 // tile. Threads t and t + 128 extract the two stencil levels of particle t straight into the A tile (BF16,
-// canonical no-swizzle K-major layout in shared memory); one thread issues the layer-1 MMAs (M = 128,
-// N = 64, K = 144) into 64 TMEM columns and commits them to an mbarrier. The epilogue reads TMEM
+// canonical no-swizzle K-major layout in shared memory; each thread's features fill whole 16-byte chunks, see
+// mlp_kpos); one thread issues the layer-1 MMAs (M = 128, N = 64, K = 80) into 64 TMEM columns and commits
+// them to an mbarrier. The epilogue reads TMEM
 // (warp w: lanes 32 (w % 4).., columns 32 (w / 4)..), adds the bias, applies SiLU and writes the hidden
 // layer back into the A tile as layer 2's A operand; layer 2 (K = 64) reuses the TMEM columns, and its
 // epilogue finishes layer 3 (64 -> 1) in FP32 with the sigmoid. The accumulators never occupy registers,
@@ -417,12 +394,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 namespace tc {
 constexpr int THREADS = 256;
 constexpr int M = 128;                         // particles per tile (MMA M, TMEM lanes)
-constexpr int KCH1 = MLP_KP / 8;               // 16-byte core-matrix columns of layer 1's K (18)
+constexpr int KCH1 = MLP_KP / 8;               // 16-byte core-matrix columns of layer 1's K (10)
 constexpr int KCH2 = MLP_H / 8;                // of layer 2's K (8)
 constexpr int SBO1 = KCH1 * 128;               // bytes between 8-row core-matrix groups, layer 1
 constexpr int SBO2 = KCH2 * 128;               // layer 2
-constexpr int A_BYTES = (M / 8) * SBO1;        // 36864: features; later the hidden layer (16384 B)
-constexpr int W1_BYTES = (MLP_H / 8) * SBO1;   // 18432
+constexpr int A_BYTES = (M / 8) * SBO1;        // 20480: features; later the hidden layer (16384 B)
+constexpr int W1_BYTES = (MLP_H / 8) * SBO1;   // 10240
 constexpr int W2_BYTES = (MLP_H / 8) * SBO2;   // 8192
 constexpr int DYN_SMEM = A_BYTES + W1_BYTES + W2_BYTES;
 constexpr uint32_t TMEM_COLS = 64;
@@ -549,9 +526,9 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
     for (int w = t; w < MLP_KP / 2; w += tc::THREADS) {
         float lo[2], hi[2];
         for (int e = 0; e < 2; ++e) {
-            const int k = 2 * w + e;
-            lo[e] = (args.lo && k < MLP_IN) ? args.lo[k] : -INFINITY;
-            hi[e] = (args.hi && k < MLP_IN) ? args.hi[k] : INFINITY;
+            const int f = mlp_feature_at(2 * w + e);
+            lo[e] = (args.lo && f >= 0) ? args.lo[f] : -INFINITY;
+            hi[e] = (args.hi && f >= 0) ? args.hi[f] : INFINITY;
         }
         sLo2[w] = __halves2bfloat162(__float2bfloat16_rd(lo[0]), __float2bfloat16_rd(lo[1]));
         sHi2[w] = __halves2bfloat162(__float2bfloat16_ru(hi[0]), __float2bfloat16_ru(hi[1]));
@@ -587,7 +564,7 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
         // ---- features: this thread's half of row `row` ----
         auto in_range = [&](int w, __nv_bfloat162 v2) { return __hble2(sLo2[w], v2) && __hble2(v2, sHi2[w]); };
         if (FEATURES_IN) {
-            // half h writes k in [72 h, 72 h + 72)
+            // half h writes the K chunks [5 h, 5 h + 5)
 #pragma unroll 1
             for (int c = 0; c < tc::KCH1 / 2; ++c) {
                 const int k0 = 8 * (c + half * (tc::KCH1 / 2));
@@ -595,8 +572,9 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int k = k0 + 2 * e;
-                    const float a = (valid && k < MLP_IN) ? args.X[(size_t) pi * MLP_IN + k] : 0.0f;
-                    const float b = (valid && k + 1 < MLP_IN) ? args.X[(size_t) pi * MLP_IN + k + 1] : 0.0f;
+                    const int fa = mlp_feature_at(k), fb = mlp_feature_at(k + 1);
+                    const float a = (valid && fa >= 0) ? args.X[(size_t) pi * MLP_IN + fa] : 0.0f;
+                    const float b = (valid && fb >= 0) ? args.X[(size_t) pi * MLP_IN + fb] : 0.0f;
                     const __nv_bfloat162 v2 = __floats2bfloat162_rn(a, b);
                     if (check && valid)
                         oor |= !in_range(k >> 1, v2);
@@ -612,42 +590,37 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
                 valid = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f &&
                         mlp_point(cp, p, args.nrm[o], u, nn);
             }
-            // features 128..143 first (the normal and the position are then no longer needed): the normal,
-            // the position and zero padding (chunk 16 on half 0, chunk 17 on half 1)
+            // K 64..79 first (the normal and the position are then no longer needed): the normal, the
+            // position and zero padding (chunk 8 on half 0, chunk 9 on half 1)
             if (half == 0) {
                 const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
                 const __nv_bfloat162 n2u0 = __floats2bfloat162_rn(nn[2], u[0]);
                 const __nv_bfloat162 u12 = __floats2bfloat162_rn(u[1], u[2]);
-                st_shared_v4(sA + canon_off(row, 128, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
+                st_shared_v4(sA + canon_off(row, 64, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
                              *reinterpret_cast<const uint32_t*>(&n2u0), *reinterpret_cast<const uint32_t*>(&u12), 0u);
                 if (valid && check)
-                    oor |= !(in_range(64, n01) && in_range(65, n2u0) && in_range(66, u12));
+                    oor |= !(in_range(32, n01) && in_range(33, n2u0) && in_range(34, u12));
             } else {
-                st_shared_v4(sA + canon_off(row, 136, tc::SBO1), 0u, 0u, 0u, 0u);
+                st_shared_v4(sA + canon_off(row, 72, tc::SBO1), 0u, 0u, 0u, 0u);
             }
-            uint8_t* arow = sA + canon_off(row, 64 * half, tc::SBO1);
-            if (valid) {
-                // z row kz of the stencil = two 16-byte chunks of the A row
-                stencil64(cp.stex[half], cp.sinv[half], cp.lv[cp.stencil_level + half].d[2], u[0], u[1], u[2],
-                          [&](int kz, const float* v) {
+            // this half's stencil level: K 32 h .. 32 h + 26, padded with zeros to 32 h + 31 (chunks 4 h .. 4 h + 3)
+            float sv[MLP_STENCIL];
+            if (valid)
+                stencil27(cp.stex[half], cp.sinv[half], cp.lv[cp.stencil_level + half].d[2], u[0], u[1], u[2], sv);
 #pragma unroll
-                              for (int c = 0; c < 2; ++c) {
-                                  uint32_t pk[4];
+            for (int c = 0; c < 4; ++c) {
+                uint32_t pk[4];
 #pragma unroll
-                                  for (int e = 0; e < 4; ++e) {
-                                      const __nv_bfloat162 v2 =
-                                          __floats2bfloat162_rn(v[8 * c + 2 * e], v[8 * c + 2 * e + 1]);
-                                      if (check)
-                                          oor |= !in_range(32 * half + 8 * kz + 4 * c + e, v2);
-                                      pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
-                                  }
-                                  st_shared_v4(arow + (2 * kz + c) * 128, pk[0], pk[1], pk[2], pk[3]);
-                              }
-                          });
-            } else {
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    st_shared_v4(arow + c * 128, 0u, 0u, 0u, 0u);
+                for (int e = 0; e < 4; ++e) {
+                    const int j = 8 * c + 2 * e;
+                    const float a = (valid && j < MLP_STENCIL) ? sv[j] : 0.0f;
+                    const float b = (valid && j + 1 < MLP_STENCIL) ? sv[j + 1] : 0.0f;
+                    const __nv_bfloat162 v2 = __floats2bfloat162_rn(a, b);
+                    if (check && valid)
+                        oor |= !in_range(16 * half + 4 * c + e, v2);
+                    pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
+                }
+                st_shared_v4(sA + canon_off(row, 32 * half + 8 * c, tc::SBO1), pk[0], pk[1], pk[2], pk[3]);
             }
             oor = oor && valid;
         }

@@ -10,8 +10,18 @@
 
 namespace p2v {
 
-constexpr int MLP_IN = 134;   // 2 levels x 64 stencil samples, 3 normal components, 3 position components
-constexpr int MLP_KP = 144;   // input padded to a multiple of the MMA K (16)
+constexpr int MLP_STENCIL = 27;                // 3x3x3 samples per stencil level
+constexpr int MLP_IN = 2 * MLP_STENCIL + 6;    // 60: two stencil levels, 3 normal and 3 position components
+// The tensor-core tile keeps each group of features in whole 16-byte chunks: level s at K 0..26, level s + 1
+// at K 32..58, normal and position at K 64..69, zeros elsewhere (MLP_KP = 80, five MMAs of K = 16).
+constexpr int MLP_KP = 80;
+// K position of logical feature i, and the logical feature at K position k (-1: padding)
+__host__ __device__ constexpr int mlp_kpos(int i) {
+    return i < 27 ? i : (i < 54 ? i + 5 : i + 10);
+}
+__host__ __device__ constexpr int mlp_feature_at(int k) {
+    return k < 27 ? k : (k < 32 ? -1 : (k < 59 ? k - 5 : (k < 64 ? -1 : (k < 70 ? k - 10 : -1))));
+}
 constexpr int MLP_H = 64;
 // parameter vector: W1[H][IN], b1[H], W2[H][H], b2[H], w3[H], b3
 constexpr int OFF_W1 = 0;

@@ -440,7 +440,7 @@ def aosphere_ao_f64(tex, clip, xyzr, normals, mode=0, step_len=0.5, eval_fac=1.0
     return out
 
 
-MLP_IN, MLP_HIDDEN = 134, 64
+MLP_IN, MLP_HIDDEN = 60, 64
 MLP_NPARAM = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
 
 

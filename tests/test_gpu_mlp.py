@@ -35,7 +35,7 @@ def test_gradients_match_fp64(ctx):
     w = random_params(1)
     ctx.mlp_set_weights(w)
     x = rng.uniform(0, 1, (96, p2v.MLP_INPUTS)).astype(np.float32)
-    x[:, 128:131] = synth.random_normals(96, 2)
+    x[:, 54:57] = synth.random_normals(96, 2)
     t = rng.uniform(0, 1, 96).astype(np.float32)
     g, loss = ctx.mlp_gradients(x, t)
     l64, _, g64 = oracle.mlp_f64(w.astype(np.float64), x, t)
@@ -49,7 +49,7 @@ def test_tensor_core_inference_matches_fp64(ctx):
     w = random_params(3, 0.15)
     ctx.mlp_set_weights(w)
     x = rng.uniform(0, 1, (1000, p2v.MLP_INPUTS)).astype(np.float32)
-    x[:, 128:131] = synth.random_normals(1000, 4)
+    x[:, 54:57] = synth.random_normals(1000, 4)
     y = ctx.mlp_infer(x)
     _, y64, _ = oracle.mlp_f64(w.astype(np.float64), x, None, grads=False)
     # BF16 weights and features (8 mantissa bits), FP32 accumulation
@@ -167,10 +167,10 @@ def _trilinear_border(T, x, y, z):
 
 
 def test_stencil_features_vs_fp64():
-    """The learned AO's 134 features of every particle (collected through p2v_mlp_collect, in binning order)
+    """The learned AO's 60 features of every particle (collected through p2v_mlp_collect, in binning order)
     against a CPU evaluation: two consecutive levels of the AO pyramid as the GPU built them, rounded to the
-    FP16 texels the stencils read, sampled trilinearly with a zero border at the 4x4x4 texel-spaced offsets
-    around the surface point p + r n, then the unit normal and the surface point in volume coordinates."""
+    FP16 texels the stencils read, sampled trilinearly with a zero border at the 3x3x3 offsets 1.5 texels
+    apart around the surface point p + r n, then the unit normal and the surface point in volume coordinates."""
     c = p2v.Context(0)
     try:
         f = synth.uniform(n=30_000, edge=40.0, res=44, seed=9)
@@ -192,7 +192,7 @@ def test_stencil_features_vs_fp64():
         n = nrm[order].astype(np.float64)
         n /= np.linalg.norm(n, axis=1, keepdims=True)
         u = [(p[:, a] + p[:, 3] * n[:, a] - bmin[a]) * ibs[a] for a in range(3)]
-        k = np.arange(4) - 1.5
+        k = 1.5 * (np.arange(3) - 1.0)
 
         def stencil(T):
             dz, dy, dx = T.shape
@@ -200,7 +200,7 @@ def test_stencil_features_vs_fp64():
             Y = u[1][:, None, None, None] + k[None, None, :, None] / dy
             Z = u[2][:, None, None, None] + k[None, :, None, None] / dz
             X, Y, Z = np.broadcast_arrays(X, Y, Z)
-            return _trilinear_border(T, X, Y, Z).reshape(len(u[0]), 64)
+            return _trilinear_border(T, X, Y, Z).reshape(len(u[0]), 27)
 
         errs = {}
         pos = np.stack(u, axis=1)
@@ -209,9 +209,9 @@ def test_stencil_features_vs_fp64():
             errs[s] = np.abs(x.astype(np.float64) - ref)
         s = min(errs, key=lambda q: errs[q].max())
         e = errs[s]
-        assert np.abs(x[:, 128:131] - n).max() <= 1e-6
-        assert np.abs(x[:, 131:134] - pos).max() <= 1e-5
-        assert e[:, :128].max() <= 4e-3, e[:, :128].max()
-        assert np.sqrt(np.mean(e[:, :128] ** 2)) <= 5e-4, np.sqrt(np.mean(e[:, :128] ** 2))
+        assert np.abs(x[:, 54:57] - n).max() <= 1e-6
+        assert np.abs(x[:, 57:60] - pos).max() <= 1e-5
+        assert e[:, :54].max() <= 4e-3, e[:, :54].max()
+        assert np.sqrt(np.mean(e[:, :54] ** 2)) <= 5e-4, np.sqrt(np.mean(e[:, :54] ** 2))
     finally:
         c.close()
