@@ -30,9 +30,17 @@ __device__ __forceinline__ float silu(float a) {
     return a / (1.0f + __expf(-a));
 }
 
-// inference: fast division (2 ulp) instead of the IEEE quotient
+// inference: silu(a) = a * sigmoid(a) with sigmoid(a) = 0.5 tanh(a / 2) + 0.5 from the hardware tanh
+// approximation (one special-function operation instead of an exponential and a division; its ~2^-11
+// relative error lies below the BF16 rounding the activations receive next)
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float silu_fast(float a) {
-    return __fdividef(a, 1.0f + __expf(-a));
+    const float h = 0.5f * a;
+    return fmaf(h, tanh_approx(h), h);
 }
 
 __device__ __forceinline__ float sigmoidf_(float a) {
