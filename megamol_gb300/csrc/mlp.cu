@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) mlp_range_kernel(const float* __restrict_
 }
 
 // ---------------------------------------------------------------------------------------------
-// inference weights: BF16 copies of W1 (K padded to 144 with zeros) and W2
+// inference weights: BF16 copies of W1 (its columns at the K positions of mlp_kpos, zeros between) and W2
 // ---------------------------------------------------------------------------------------------
 __global__ void mlp_pack_kernel(const float* __restrict__ P, __nv_bfloat16* __restrict__ w1h,
     __nv_bfloat16* __restrict__ w2h) {
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpI
         __syncthreads();
         if (half == 0)
             oor = oor || s_flag[row] != 0u;
-        // ---- layer 1: D[128 x 64] = A[128 x 144] W1^T ----
+        // ---- layer 1: D[128 x 64] = A[128 x 80] W1^T ----
         if (t == 0) {
             tc_fence_after();
 #pragma unroll
