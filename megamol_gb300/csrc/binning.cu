@@ -1,6 +1,10 @@
-// Cell binning: typed particle lists -> float4 xyzr records + cell keys, a stable LSD radix sort
-// (onesweep: one read and one write of the keys per 8-bit digit, decoupled look-back across tiles),
-// and the per-cell start table of the sorted order.
+// Cell binning: typed particle lists -> float4 xyzr records + cell keys, their stable sort by cell with
+// every particle's gather record in sorted order, and the per-cell start table of the sorted order.
+// Two sorts give the same permutation bit for bit: a counting sort by cell (histogram, scan of the cell
+// counts = the start table, scatter, and an index-order pass over the cells holding two or more particles;
+// taken while no cell holds more than 32 particles) and a stable LSD radix sort (onesweep: one read and
+// one write of the keys per 8- or 9-bit digit, decoupled look-back across tiles), which runs alone for
+// sparse frames and as the device-side fallback of the counting sort.
 //
 // Reference semantics (plugins/datatools/src/ParticlesToDensity.cpp):
 //   - particle components are read through SimpleSphericalParticles' accessors, i.e. converted to
