@@ -396,7 +396,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // (warp w: lanes 32 (w % 4).., columns 32 (w / 4)..), adds the bias, applies SiLU and writes the hidden
 // layer back into the A tile as layer 2's A operand; layer 2 (K = 64) reuses the TMEM columns, and its
 // epilogue finishes layer 3 (64 -> 1) in FP32 with the sigmoid. The accumulators never occupy registers,
-// so three CTAs (24 warps) stay resident per SM to hide the stencil loads' latency. Every mbarrier wait
+// so four CTAs (32 warps, 64 registers each: more warps hide the texture latency better than the few
+// spilled registers cost) stay resident per SM. Every mbarrier wait
 // is bounded: on timeout the CTA records ERR_MMA_TIMEOUT, drains its MMAs (bounded) and frees TMEM.
 // ---------------------------------------------------------------------------------------------
 namespace tc {
@@ -498,7 +499,7 @@ __device__ __forceinline__ void st_shared_v4(uint8_t* p, uint32_t a, uint32_t b,
 }
 
 template<bool FEATURES_IN>
-__global__ void __launch_bounds__(tc::THREADS, 3) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
+__global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     uint8_t* sA = tc_smem;
     uint8_t* sW1 = tc_smem + tc::A_BYTES;
@@ -837,8 +838,9 @@ cudaError_t launch_mlp_infer(const MlpInferArgs& a, const ConeParams& cp, bool f
         return cudaSuccess;
     static_assert(tc::DYN_SMEM <= 227 * 1024, "tensor-core tile does not fit in shared memory");
     const uint32_t ntiles = (a.n + tc::M - 1) / tc::M;
-    // three resident CTAs per SM (shared memory allows three; 3 x 64 TMEM columns of 512): one wave
-    const unsigned grid = (unsigned) std::min<uint32_t>(ntiles, (uint32_t) sms * 3);
+    // four resident CTAs per SM (41 KB of shared memory and 64 registers per thread each; 4 x 64 TMEM
+    // columns of 512): one wave
+    const unsigned grid = (unsigned) std::min<uint32_t>(ntiles, (uint32_t) sms * 4);
     cudaError_t e;
     if (features_in) {
         e = cudaFuncSetAttribute(mlp_infer_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::DYN_SMEM);
