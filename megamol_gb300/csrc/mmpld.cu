@@ -191,7 +191,7 @@ p2v_status p2v_mmpld_read_frame(p2v_mmpld* f, uint32_t frame, void* buffer, uint
         if (vb != 0)
             colour_of(ct, cb, ctype);
         const uint32_t stride = vb + cb;
-        L.vertex_type = vb ? vt : P2V_VERTDATA_NONE;
+        L.vertex_type = vb ? static_cast<int32_t>(vt) : static_cast<int32_t>(P2V_VERTDATA_NONE);
         L.global_radius = (vt == 1 || vt == 3 || vt == 4) ? c.get<float>() : 0.05f;
         // the raw colour byte decides what follows (:164-177), whatever the vertex type
         L.global_colour[0] = L.global_colour[1] = L.global_colour[2] = 192;
