@@ -19,8 +19,11 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libp2v.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off: the host-side float expressions restated from the reference (the surface box
+# adjustment, cone directions and step tables) stay unfused, so the x86 and Arm builds give the same bits
+# (gcc fuses a*b+c into FMA by default on Arm). Device code is unaffected by this host-compiler flag.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-              "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

@@ -173,6 +173,36 @@ def normalize_f64(vol: np.ndarray, mode: str, n_particles: int = 0, spacing=(1.0
     return v.copy(), v.min(), v.max()
 
 
+def modify_bbox_f32(bbox, res):
+    """ParticlesToDensity::modifyBBox (ParticlesToDensity.cpp:749-799) in FP32 numpy scalars, one rounding
+    per C++ operation: grow the box by 1.1 plus two voxels in z, make voxels cubic by rewriting sizex and
+    sizey, centre the grown box on the old one. Returns (bbox (6 floats), resolution (3 ints))."""
+    f = np.float32
+    sz = int(res[2])
+    lo = [f(bbox[a]) for a in range(3)]
+    hi = [f(bbox[a + 3]) for a in range(3)]
+    rng = [abs(hi[a] - lo[a]) for a in range(3)]  # vislib Cuboid::Width/Height/Depth
+    scale = f(1.1)
+    spacing = (rng[2] * scale) / f(sz)
+    depth = (rng[2] * scale) + f(2) * spacing
+    spacing = depth / f(sz)
+
+    def cubic(r):
+        size = (r * scale) + f(2) * spacing
+        q = size / spacing
+        n = int(q)  # float -> int truncation
+        rest = q - f(n)
+        size = size + (f(1) - rest) * spacing
+        return size, n + 1
+
+    width, sx = cubic(rng[0])
+    height, sy = cubic(rng[1])
+    grown = (width, height, depth)
+    out = [lo[a] - (grown[a] - rng[a]) / f(2) for a in range(3)] + \
+          [hi[a] + (grown[a] - rng[a]) / f(2) for a in range(3)]
+    return tuple(float(v) for v in out), (sx, sy, sz)
+
+
 def spacing_f64(bbox, res):
     """Exact grid spacing of the reference grid, (right-left)/(res-1) per axis."""
     return tuple(abs(float(bbox[a + 3]) - float(bbox[a])) / (res[a] - 1) for a in range(3))

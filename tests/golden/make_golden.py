@@ -73,6 +73,16 @@ def cases():
     out["zero_radius"] = dict(lists=[dict(type=VERT_FLOAT_XYZR, data=rec0, stride=0, radius=0.0, count=500)],
                               bbox=(0, 0, 0, 10, 10, 10), res=(16, 16, 16), cyclic=(0, 0, 0), normalize=False,
                               sigma=1.0)
+    # 8. forSurfaceReconstruction: the module grows the box and rewrites sizex / sizey for cubic voxels
+    #    (ParticlesToDensity.cpp:234-235, 749-799); a flat, off-origin box with per-particle radii
+    rec1 = np.zeros((3000, 4), np.float32)
+    rec1[:, 0] = rng.uniform(-3.0, 17.0, 3000)
+    rec1[:, 1] = rng.uniform(0.5, 12.5, 3000)
+    rec1[:, 2] = rng.uniform(1.0, 25.0, 3000)
+    rec1[:, 3] = rng.uniform(0.4, 1.1, 3000)
+    out["surface_box"] = dict(lists=[dict(type=VERT_FLOAT_XYZR, data=rec1, stride=0, radius=0.0, count=3000)],
+                              bbox=(-3.0, 0.5, 1.0, 17.0, 12.5, 25.0), res=(16, 16, 20), cyclic=(0, 0, 0),
+                              normalize=False, sigma=1.0, surface=True)
     return out
 
 
@@ -175,12 +185,18 @@ def main(only=None):
     for name, c in cases().items():
         if only and not f"p2d_{name}".startswith(only):
             continue
-        vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"])
+        surface = bool(c.get("surface", False))
+        vol, meta = oracle.reference_density(c["lists"], c["bbox"], c["res"], c["cyclic"], c["normalize"], c["sigma"],
+                                             surface=surface)
         d = dict(bbox=np.array(c["bbox"], np.float32), res=np.array(c["res"], np.int32),
                  cyclic=np.array(c["cyclic"], np.int32), normalize=np.int32(c["normalize"]),
                  sigma=np.float32(c["sigma"]), nlists=np.int32(len(c["lists"])), volume=vol,
                  min_value=np.float64(meta["min_value"]), max_value=np.float64(meta["max_value"]),
                  slice_dists=np.array(meta["slice_dists"], np.float32))
+        if surface:
+            # the module's published grid after the box adjustment
+            d.update(surface=np.int32(1), out_res=np.array(meta["resolution"], np.int32),
+                     origin=np.array(meta["origin"], np.float32), extents=np.array(meta["extents"], np.float32))
         for i, L in enumerate(c["lists"]):
             d[f"l{i}_type"] = np.int32(L["type"])
             d[f"l{i}_data"] = np.ascontiguousarray(L["data"])

@@ -24,7 +24,17 @@ def load(name):
         lists.append(dict(type=int(case[f"l{i}_type"]), data=case[f"l{i}_data"], stride=int(case[f"l{i}_stride"]),
                           radius=float(case[f"l{i}_radius"]), count=int(case[f"l{i}_count"])))
     case["lists"] = lists
+    case.setdefault("surface", np.int32(0))
     return case
+
+
+def grid(case):
+    """(bbox, resolution) of the grid the module computes on: the stored box and slot resolution, or for a
+    forSurfaceReconstruction case the box adjustment restated by the oracle (ParticlesToDensity.cpp:749-799)."""
+    if int(case["surface"]):
+        import oracle
+        return oracle.modify_bbox_f32(case["bbox"], case["res"])
+    return tuple(float(v) for v in case["bbox"]), tuple(int(v) for v in case["res"])
 
 
 def list_to_xyzr(L):

@@ -27,15 +27,19 @@ def ctx():
 
 
 def run(ctx, lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0, kernel=p2v.KERNEL_BUMP, mass=False,
-        out=None, accumulate=p2v.ACCUM_EXACT):
+        out=None, accumulate=p2v.ACCUM_EXACT, surface=False, out_res=None):
+    """One frame; `out_res` sizes the host output when the module rewrites the resolution (surface)."""
     ctx.set_params(sizex=int(res[0]), sizey=int(res[1]), sizez=int(res[2]), cyclX=int(cyclic[0]),
                    cyclY=int(cyclic[1]), cyclZ=int(cyclic[2]), normalize=int(bool(normalize)), sigma=float(sigma),
-                   kernel=kernel, mass_normalize=int(mass), forSurfaceReconstruction=0, accumulate=accumulate)
+                   kernel=kernel, mass_normalize=int(mass), forSurfaceReconstruction=int(bool(surface)),
+                   accumulate=accumulate)
+    r = out_res if out_res is not None else res
     if out is None:
-        out = np.full(int(res[0]) * int(res[1]) * int(res[2]), np.nan, np.float32)
+        out = np.full(int(r[0]) * int(r[1]) * int(r[2]), np.nan, np.float32)
     meta = ctx.run_frame(lists, bbox, out)
     if isinstance(out, np.ndarray):
-        out = out.reshape(int(res[2]), int(res[1]), int(res[0]))
+        r = meta["resolution"]
+        out = out.reshape(int(r[2]), int(r[1]), int(r[0]))
     return out, meta
 
 
@@ -56,17 +60,21 @@ ACCUM = [p2v.ACCUM_EXACT, p2v.ACCUM_KAHAN]
 @pytest.mark.parametrize("name", G.golden_names())
 def test_golden_vs_reference_and_fp64(ctx, name, accumulate):
     c = G.load(name)
+    bbox, res = G.grid(c)  # the surface case's adjusted box, restated bit-exactly against the reference
     vol, meta = run(ctx, golden_lists(c), c["bbox"], c["res"], c["cyclic"], bool(c["normalize"]), float(c["sigma"]),
-                    accumulate=accumulate)
+                    accumulate=accumulate, surface=bool(c["surface"]), out_res=res)
     ref = c["volume"]
+    assert meta["resolution"] == [int(x) for x in res] and vol.shape == ref.shape
     xyzr = G.case_xyzr(c)
-    v64 = oracle.density_f64(xyzr, c["bbox"], c["res"], c["cyclic"], float(c["sigma"]), oracle.BUMP, NT)
+    v64 = oracle.density_f64(xyzr, bbox, res, c["cyclic"], float(c["sigma"]), oracle.BUMP, NT)
     if bool(c["normalize"]):
         v64, _, _ = oracle.normalize_f64(v64, "minmax")
     assert maxrel(vol, v64) <= 1e-6, f"{name}: vs FP64 {maxrel(vol, v64):.3e}"
     assert maxrel(vol, ref) <= 2e-5, f"{name}: vs reference {maxrel(vol, ref):.3e}"
     assert meta["slice_dists"] == [float(x) for x in c["slice_dists"]]
-    assert meta["resolution"] == [int(x) for x in c["res"]]
+    if int(c["surface"]):
+        assert meta["origin"] == [float(x) for x in c["origin"]]
+        assert meta["extents"] == [float(x) for x in c["extents"]]
     if bool(c["normalize"]):
         assert meta["min_value"] == 0.0 and meta["max_value"] == 1.0
     else:
@@ -161,6 +169,7 @@ def test_surface_reconstruction_box(ctx):
     sd = meta["slice_dists"]
     assert vol.shape == tuple(meta["resolution"][::-1])
     bb = meta["bbox"]
+    assert (tuple(bb), tuple(meta["resolution"])) == oracle.modify_bbox_f32(f.bbox, (16, 16, 20))
     v64 = oracle.density_f64(f.xyzr, bb, meta["resolution"], (1, 1, 1), 1.0, oracle.BUMP, NT)
     assert maxrel(vol, v64) <= 1e-6
     assert m.param("sizex") == meta["resolution"][0]

@@ -17,7 +17,8 @@ def test_golden_fixtures_present():
 def test_restatement_f32_bitexact_vs_reference_golden(name):
     c = G.load(name)
     xyzr = G.case_xyzr(c)
-    v = oracle.density_f32(xyzr, c["bbox"], c["res"], c["cyclic"], float(c["sigma"]), oracle.BUMP, nthreads=1)
+    bbox, res = G.grid(c)
+    v = oracle.density_f32(xyzr, bbox, res, c["cyclic"], float(c["sigma"]), oracle.BUMP, nthreads=1)
     v, mn, mx = oracle.normalize_minmax_f32(v, apply=bool(c["normalize"]))
     assert np.array_equal(v, c["volume"]), f"max diff {np.abs(v - c['volume']).max()}"
     assert float(np.float32(c["min_value"])) == mn or bool(c["normalize"])
@@ -27,13 +28,28 @@ def test_restatement_f32_bitexact_vs_reference_golden(name):
 def test_fp64_judge_close_to_reference_golden(name):
     c = G.load(name)
     xyzr = G.case_xyzr(c)
-    v64 = oracle.density_f64(xyzr, c["bbox"], c["res"], c["cyclic"], float(c["sigma"]), oracle.BUMP)
+    bbox, res = G.grid(c)
+    v64 = oracle.density_f64(xyzr, bbox, res, c["cyclic"], float(c["sigma"]), oracle.BUMP)
     if bool(c["normalize"]):
         v64, _, _ = oracle.normalize_f64(v64, "minmax")
     ref = c["volume"].astype(np.float64)
     err = np.abs(v64 - ref).max() / max(np.abs(v64).max(), 1e-30)
     # the reference rounds node positions and distances in float; that costs it up to ~1e-5 of the max
     assert err < 2e-5, err
+
+
+def test_surface_box_adjustment_vs_reference_golden():
+    """The restated box adjustment publishes the reference module's grid bit for bit: rewritten sizex /
+    sizey, origin, extents and slice distances (ParticlesToDensity.cpp:249-288, 749-799)."""
+    c = G.load("surface_box")
+    bbox, res = G.grid(c)
+    f = np.float32
+    assert list(res) == [int(v) for v in c["out_res"]] and list(res) != [int(v) for v in c["res"]]
+    for a in range(3):
+        ext = abs(f(bbox[a + 3]) - f(bbox[a]))
+        assert f(bbox[a]) == c["origin"][a] and ext == c["extents"][a]
+        assert ext / f(res[a] - 1) == c["slice_dists"][a]
+    assert c["volume"].shape == tuple(res[::-1])
 
 
 def test_kat_single_particle_on_node():
