@@ -337,6 +337,64 @@ def reference_write_datraw(prefix, frame, volume, resolution, components, slice_
                                  org, v.ctypes.data) == 0
 
 
+REF_MMPLD_SO = os.path.join(os.path.dirname(REF_SO), "libref_mmpld.so")
+# record bytes of SimpleSphericalParticles' vertex and colour types (SimpleSphericalParticles.h:28-50)
+VERTEX_RECORD_BYTES = {0: 0, 1: 12, 2: 16, 3: 6, 4: 24}
+COLOUR_RECORD_BYTES = {0: 0, 1: 3, 2: 4, 3: 12, 4: 16, 5: 4, 6: 8, 7: 8}
+
+
+class _RefMmpldList(C.Structure):
+    _fields_ = [("vert_type", C.c_int32), ("col_type", C.c_int32), ("count", C.c_uint64),
+                ("global_radius", C.c_float), ("global_colour", C.c_uint8 * 4), ("col_min", C.c_float),
+                ("col_max", C.c_float), ("vert_stride", C.c_uint32), ("col_stride", C.c_uint32),
+                ("bbox", C.c_float * 6), ("clusters", C.c_uint32), ("cluster_bytes", C.c_uint64)]
+
+
+class _RefMmpldExtent(C.Structure):
+    _fields_ = [("frames", C.c_uint32), ("bbox", C.c_float * 6), ("clipbox", C.c_float * 6)]
+
+
+def reference_mmpld(path, max_lists: int = 256) -> dict:
+    """Read an MMPLD file with MegaMol's own MMPLDDataSource (oracle/_ref/libref_mmpld.so): the extent it
+    publishes (frames, bbox, clipbox) and, for every frame, the lists of the MultiParticleDataCall as dicts
+    (types, count, global radius / colour, colour map range, strides, list box, cluster infos, and the packed
+    vertex and colour records as uint8 arrays)."""
+    lib_ = C.CDLL(REF_MMPLD_SO)
+    lib_.ref_mmpld_open.argtypes = [C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(_RefMmpldExtent)]
+    lib_.ref_mmpld_frame.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(_RefMmpldList), C.c_uint32,
+                                     C.POINTER(C.c_uint32)]
+    lib_.ref_mmpld_list_data.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]
+    lib_.ref_mmpld_close.argtypes = [C.c_void_p]
+    h, ext = C.c_void_p(), _RefMmpldExtent()
+    if lib_.ref_mmpld_open(os.fsencode(str(path)), C.byref(h), C.byref(ext)) != 0:
+        lib_.ref_mmpld_close(h)
+        raise RuntimeError("reference MMPLDDataSource: GetExtent failed")
+    out = dict(frames=int(ext.frames), bbox=list(ext.bbox), clipbox=list(ext.clipbox), frame_lists=[])
+    try:
+        arr = (_RefMmpldList * max_lists)()
+        for fi in range(out["frames"]):
+            n = C.c_uint32()
+            if lib_.ref_mmpld_frame(h, fi, arr, max_lists, C.byref(n)) != 0:
+                raise RuntimeError(f"reference MMPLDDataSource: GetData failed on frame {fi}")
+            lists = []
+            for i in range(min(n.value, max_lists)):
+                L = arr[i]
+                vb, cb = VERTEX_RECORD_BYTES.get(L.vert_type, 0), COLOUR_RECORD_BYTES.get(L.col_type, 0)
+                vert = np.zeros(vb * L.count, np.uint8)
+                col = np.zeros(cb * L.count, np.uint8)
+                lib_.ref_mmpld_list_data(h, i, vb, vert.ctypes.data if vb else None, cb,
+                                         col.ctypes.data if cb else None)
+                lists.append(dict(vert_type=L.vert_type, col_type=L.col_type, count=int(L.count),
+                                  global_radius=float(L.global_radius), global_colour=tuple(L.global_colour),
+                                  col_min=float(L.col_min), col_max=float(L.col_max), vert_stride=int(L.vert_stride),
+                                  col_stride=int(L.col_stride), bbox=list(L.bbox), clusters=int(L.clusters),
+                                  cluster_bytes=int(L.cluster_bytes), vertex=vert, colour=col))
+            out["frame_lists"].append(lists)
+    finally:
+        lib_.ref_mmpld_close(h)
+    return out
+
+
 def reference_vector_grid(lists, bbox, res, cyclic=(1, 1, 1), normalize=False, sigma=1.0):
     """The vector aggregator's outParticles and outInfo outputs of MegaMol's ParticlesToDensity
     (ParticlesToDensity.cpp:306-380, 628-727): dict with positions (n, 3), directions (n, 3), colours (n,),

@@ -4,6 +4,7 @@
 
 #include <filesystem>
 #include <string>
+#include <vector>
 
 #include "mmcore/param/ParamSlot.h"
 
@@ -17,8 +18,9 @@ public:
         Flag_NoExistenceCheck = 1 << 2,
         Flag_RestrictExtension = 1 << 3,
         Flag_File_ToBeCreated = Flag_File | Flag_NoExistenceCheck,
+        Flag_File_RestrictExtension = Flag_File | Flag_RestrictExtension,
     };
-    explicit FilePathParam(const std::string& v, int = 0) : value_(v) {}
+    explicit FilePathParam(const std::string& v, int = 0, const std::vector<std::string>& = {}) : value_(v) {}
     const std::filesystem::path& Value() const {
         return value_;
     }

@@ -1,8 +1,11 @@
 // Minimal stand-ins for MegaMol's parameter slots and parameter types
 // (core/include/mmcore/param/ParamSlot.h:28, AbstractParamSlot.h:33,80), oracle build only.
 // A parameter is dirty after construction and after every SetValue(), until ResetDirty().
+// SetUpdateCallback() stores the module's update callback (ParamSlot.h SetUpdateCallback); the harness
+// runs it with Update() after it changed the value, as the core does when a parameter changes.
 #pragma once
 
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -45,8 +48,18 @@ public:
             param_->dirty = false;
     }
 
+    template<class C>
+    void SetUpdateCallback(bool (C::*func)(ParamSlot&)) {
+        update_ = [func](Module* m, ParamSlot& s) { return (static_cast<C*>(m)->*func)(s); };
+    }
+
+    bool Update() {
+        return update_ && Owner() ? update_(Owner(), *this) : true;
+    }
+
 private:
     std::unique_ptr<AbstractParam> param_;
+    std::function<bool(Module*, ParamSlot&)> update_;
 };
 
 template<class T>

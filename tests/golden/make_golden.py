@@ -1,9 +1,10 @@
-"""Generate golden density vectors from MegaMol's own ParticlesToDensity module.
+"""Generate golden vectors from MegaMol's own modules: ParticlesToDensity (density, aggregators, surface box),
+DatRawWriter (dat/raw files) and MMPLDDataSource (MMPLD frames as the module publishes them).
 
-Runs the reference's unmodified plugins/datatools/src/ParticlesToDensity.cpp (compiled by
-``oracle/Makefile`` target ``ref`` into ``oracle/_ref``) on small seeded inputs and stores inputs,
-parameters and the reference output as ``tests/golden/p2d_<case>.npz``. The reference tree exists only
-on the development machine, so the fixtures are committed and the GPU tests read them from here.
+Runs the reference's unmodified modules (compiled by ``oracle/Makefile`` target ``ref`` into
+``oracle/_ref``) on small seeded inputs and stores inputs, parameters and the reference output as
+``tests/golden/{p2d,agg,datraw,mmpld}_<case>.npz``. The reference tree exists only on the development
+machine, so the fixtures are committed and the tests read them from here.
 
 Usage:  python tests/golden/make_golden.py [prefix]   (only the fixtures whose name starts with prefix;
         OMP_NUM_THREADS is forced to 1: the reference's
@@ -131,9 +132,47 @@ def datraw_cases():
     }
 
 
+def mmpld_cases():
+    from tests import mmpld_io
+    rng = np.random.default_rng(20241204)
+    out = {}
+    for version in (100, 101, 102, 103):
+        lists = mmpld_io.mixed_lists(rng)
+        out[f"v{version}"] = dict(version=version, frames=[(0.25, lists), (1.5, lists[3:7]), (2.75, [])],
+                                  bbox=(-5, -5, -5, 15, 15, 15), clipbox=(-6, -6, -6, 16, 16, 16.5))
+    return out
+
+
 def main(only=None):
     oracle.build(with_reference=True)
     import tempfile
+    for name, c in mmpld_cases().items():
+        if only and not f"mmpld_{name}".startswith(only):
+            continue
+        from tests import mmpld_io
+        with tempfile.TemporaryDirectory() as d:
+            fpath = os.path.join(d, f"{name}.mmpld")
+            mmpld_io.write(fpath, c["frames"], version=c["version"], bbox=c["bbox"], clipbox=c["clipbox"])
+            raw = open(fpath, "rb").read()
+            r = oracle.reference_mmpld(fpath)
+        d = dict(mmpld=np.frombuffer(raw, np.uint8), frames=np.int64(r["frames"]),
+                 bbox=np.array(r["bbox"], np.float32), clipbox=np.array(r["clipbox"], np.float32))
+        for fi, lists in enumerate(r["frame_lists"]):
+            d[f"f{fi}_nlists"] = np.int64(len(lists))
+            for li, L in enumerate(lists):
+                vb = oracle.VERTEX_RECORD_BYTES.get(L["vert_type"], 0)
+                cb = oracle.COLOUR_RECORD_BYTES.get(L["col_type"], 0)
+                # strides as the records lie in the frame (the getters report 0 for packed records)
+                vs = L["vert_stride"] or vb
+                cs = L["col_stride"] or cb
+                d[f"f{fi}_l{li}_meta"] = np.array(
+                    [L["vert_type"], L["col_type"], L["count"], L["global_radius"], *L["global_colour"], L["col_min"],
+                     L["col_max"], vs, cs, *L["bbox"], L["clusters"], L["cluster_bytes"]], np.float64)
+                d[f"f{fi}_l{li}_vertex"] = L["vertex"]
+                d[f"f{fi}_l{li}_colour"] = L["colour"]
+        path = os.path.join(HERE, f"mmpld_{name}.npz")
+        np.savez_compressed(path, **d)
+        print(f"{path}: {len(raw)} B file, {r['frames']} frames")
     for name, c in datraw_cases().items():
         if only and not f"datraw_{name}".startswith(only):
             continue

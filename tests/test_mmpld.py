@@ -104,3 +104,102 @@ def test_corrupt_list_count_is_an_error(tmp_path):
     f = p2v.Mmpld(p)
     with pytest.raises(p2v.P2VError):
         f.read(0)
+
+
+# ---- parity with MegaMol's own reader -------------------------------------------------------------------
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MMPLD_GOLDEN = sorted(n[6:-4] for n in os.listdir(GOLDEN) if n.startswith("mmpld_") and n.endswith(".npz"))
+RECORD_BYTES = ({0: 0, 1: 12, 2: 16, 3: 6, 4: 24}, {0: 0, 1: 3, 2: 4, 3: 12, 4: 16, 5: 4, 6: 8, 7: 8})
+
+
+def packed_records(ptr, stride, count, nbytes):
+    """The `nbytes` leading bytes of each of `count` records `stride` apart, packed."""
+    import ctypes as C
+
+    if count == 0 or nbytes == 0:
+        return np.zeros(0, np.uint8)
+    buf = (C.c_uint8 * (stride * (count - 1) + nbytes)).from_address(ptr)
+    raw = np.frombuffer(buf, np.uint8)
+    idx = (np.arange(count)[:, None] * stride + np.arange(nbytes)[None, :]).ravel()
+    return raw[idx].copy()
+
+
+def compare_with_reference(f, ref_frames, ref_bbox, ref_clipbox, frame_lists):
+    """Our reader `f` against what MMPLDDataSource published: the extent (GetExtent, :469-481) and per frame
+    every list's types, count, global radius and colour, colour map range, record strides, the version 1.3
+    list box, the version 1.1 cluster count, and the vertex and colour bytes."""
+    assert f.frames == ref_frames
+    assert f.bbox == list(ref_bbox) and f.clipbox == list(ref_clipbox)
+    for fi, ref_lists in enumerate(frame_lists):
+        lists, info, _, buf = f.read(fi, max_lists=256)
+        assert len(lists) == len(ref_lists), fi
+        for L, li, R in zip(lists, info, ref_lists):
+            meta = R["meta"]
+            vt, ct, count = int(meta[0]), int(meta[1]), int(meta[2])
+            assert (L.vertex_type, L.colour_type, L.count) == (vt, ct, count)
+            assert np.float32(L.global_radius) == np.float32(meta[3])
+            assert tuple(L.global_colour) == tuple(int(x) for x in meta[4:8])
+            assert [np.float32(x) for x in li["intensity_range"]] == [np.float32(meta[8]), np.float32(meta[9])]
+            vb, cb = RECORD_BYTES[0][vt], RECORD_BYTES[1][ct]
+            if vb:
+                assert L.stride == int(meta[10])
+                assert np.array_equal(packed_records(L.data, L.stride, count, vb), R["vertex"])
+            if cb:
+                assert L.colour_stride == int(meta[11])
+                assert np.array_equal(packed_records(L.colour, L.colour_stride, count, cb), R["colour"])
+            if f.version >= 103:
+                assert [np.float32(x) for x in li["bbox"]] == [np.float32(x) for x in meta[12:18]]
+            assert li["clusters"] == int(meta[18])
+        del buf
+
+
+@pytest.mark.parametrize("name", MMPLD_GOLDEN)
+def test_reader_matches_reference_reader_golden(tmp_path, name):
+    """Golden frames published by MegaMol's own MMPLDDataSource (tests/golden/make_golden.py): every vertex
+    and colour type, lists without vertex data, unknown colour types, empty lists and frames."""
+    z = np.load(os.path.join(GOLDEN, f"mmpld_{name}.npz"))
+    path = tmp_path / f"{name}.mmpld"
+    path.write_bytes(z["mmpld"].tobytes())
+    frame_lists = []
+    for fi in range(int(z["frames"])):
+        frame_lists.append([dict(meta=z[f"f{fi}_l{li}_meta"], vertex=z[f"f{fi}_l{li}_vertex"],
+                                 colour=z[f"f{fi}_l{li}_colour"]) for li in range(int(z[f"f{fi}_nlists"]))])
+    f = p2v.Mmpld(path)
+    compare_with_reference(f, int(z["frames"]), z["bbox"], z["clipbox"], frame_lists)
+    f.close()
+
+
+def _reference_reader_built():
+    import oracle
+    return os.path.exists(oracle.REF_MMPLD_SO)
+
+
+@pytest.mark.skipif(not _reference_reader_built(), reason="reference MMPLDDataSource build not present")
+@pytest.mark.parametrize("seed", range(6))
+def test_reader_matches_live_reference_reader(tmp_path, seed):
+    """Random files (versions, list mixes, several frames) read by both readers."""
+    import oracle
+    rng = np.random.default_rng(1000 + seed)
+    version = [100, 101, 102, 103][seed % 4]
+    frames = []
+    for _ in range(int(rng.integers(1, 4))):
+        lists = mmpld_io.mixed_lists(rng)
+        keep = rng.permutation(len(lists))[:int(rng.integers(0, len(lists) + 1))]
+        frames.append((float(rng.uniform(0, 10)), [lists[k] for k in keep]))
+    path = tmp_path / f"r{seed}.mmpld"
+    mmpld_io.write(path, frames, version=version, bbox=tuple(rng.uniform(-9, 0, 3)) + tuple(rng.uniform(1, 9, 3)))
+    r = oracle.reference_mmpld(path)
+    frame_lists = []
+    for lists in r["frame_lists"]:
+        out = []
+        for L in lists:
+            vb = oracle.VERTEX_RECORD_BYTES.get(L["vert_type"], 0)
+            cb = oracle.COLOUR_RECORD_BYTES.get(L["col_type"], 0)
+            meta = np.array([L["vert_type"], L["col_type"], L["count"], L["global_radius"], *L["global_colour"],
+                             L["col_min"], L["col_max"], L["vert_stride"] or vb, L["col_stride"] or cb, *L["bbox"],
+                             L["clusters"], L["cluster_bytes"]], np.float64)
+            out.append(dict(meta=meta, vertex=L["vertex"], colour=L["colour"]))
+        frame_lists.append(out)
+    f = p2v.Mmpld(path)
+    compare_with_reference(f, r["frames"], r["bbox"], r["clipbox"], frame_lists)
+    f.close()
