@@ -3,13 +3,15 @@
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this package,
 and only as the checker / the timed CPU baseline. The shipped GPU library never calls it.
 
-Two native libraries back it (both built by ``oracle/Makefile``):
+Native libraries back it (all built by ``oracle/Makefile``):
 
 * ``_build/libp2v_oracle.so`` — our restatement of the reference algorithms (``p2v_oracle.cpp``), FP32
   with the reference's operation order and FP64 for error judging.
 * ``_ref/libref_p2d.so`` — MegaMol's own ``plugins/datatools/src/ParticlesToDensity.cpp``, compiled
-  unmodified against ``oracle/shim`` and driven through its slots by ``ref_harness.cpp``. It exists only
-  where the reference tree was available at build time.
+  unmodified against ``oracle/shim`` and driven through its slots by ``ref_harness.cpp``;
+  ``_ref/libref_datraw.so`` (``volume::DatRawWriter``, ``ref_datraw.cpp``) and ``_ref/libref_mmpld.so``
+  (``moldyn::io::MMPLDDataSource`` with the vislib classes it reads through, ``ref_mmpld.cpp``) likewise.
+  They exist only where the reference tree was available at build time.
 """
 from __future__ import annotations
 
@@ -223,7 +225,9 @@ def mip_step_f64(src: np.ndarray) -> np.ndarray:
 # ------------------------------------------------------------------------------------------------
 class _RefList(C.Structure):
     _fields_ = [("vert_type", C.c_int), ("vert", C.c_void_p), ("vert_stride", C.c_uint32),
-                ("global_radius", C.c_float), ("count", C.c_uint64), ("icol", C.c_void_p), ("dir", C.c_void_p)]
+                ("global_radius", C.c_float), ("count", C.c_uint64), ("icol", C.c_void_p), ("dir", C.c_void_p),
+                ("has_col", C.c_int), ("col_type", C.c_int), ("col", C.c_void_p), ("col_stride", C.c_uint32),
+                ("global_colour", C.c_uint8 * 4)]
 
 
 class _RefParams(C.Structure):
@@ -278,9 +282,20 @@ def _ref_lists(lists):
         if dr is not None:
             dr = np.ascontiguousarray(dr, np.float32)
             keep.append(dr)
+        # other colour types: "col_type", "col_offset" (bytes into each vertex record, the colour interleaved
+        # with the vertex data) or a separate "col" array with "col_stride", and "global_colour"
+        col_ptr, has_col = None, int("col_type" in L)
+        if "col_offset" in L:
+            col_ptr = data.ctypes.data + int(L["col_offset"])
+        elif L.get("col") is not None:
+            col = np.ascontiguousarray(L["col"])
+            keep.append(col)
+            col_ptr = col.ctypes.data
+        gcol = (C.c_uint8 * 4)(*L.get("global_colour", (255, 255, 255, 255)))
         arr[i] = _RefList(int(L["type"]), data.ctypes.data, int(L.get("stride", 0)), float(L.get("radius", 0.5)),
                           int(L["count"]), icol.ctypes.data if icol is not None else None,
-                          dr.ctypes.data if dr is not None else None)
+                          dr.ctypes.data if dr is not None else None, has_col, int(L.get("col_type", 0)), col_ptr,
+                          int(L.get("col_stride", 0)), gcol)
     return arr, keep
 
 

@@ -41,6 +41,13 @@ struct ref_p2d_list {
     uint64_t count;
     const float* icol;    // COLDATA_FLOAT_I (aggregator 1) or nullptr
     const float* dir;     // DIRDATA_FLOAT_XYZ (aggregator 2) or nullptr
+    // any other colour data (used when icol is null and has_col is set): type, data, stride (0 = packed) and
+    // the global colour, set before the colour data as MMPLDDataSource does (MMPLDDataSource.cpp:164-196)
+    int has_col;
+    int col_type;         // SimpleSphericalParticles::ColourDataType
+    const void* col;
+    uint32_t col_stride;
+    uint8_t global_colour[4];
 };
 
 struct ref_p2d_params {
@@ -103,8 +110,14 @@ void setup(Session& S, const ref_p2d_list* lists, int n_lists, const float bbox[
         p.SetGlobalRadius(lists[i].global_radius);
         p.SetVertexData(static_cast<geocalls::SimpleSphericalParticles::VertexDataType>(lists[i].vert_type),
             lists[i].vert, lists[i].vert_stride);
-        if (lists[i].icol != nullptr)
+        if (lists[i].icol != nullptr) {
             p.SetColourData(geocalls::SimpleSphericalParticles::COLDATA_FLOAT_I, lists[i].icol);
+        } else if (lists[i].has_col) {
+            const uint8_t* g = lists[i].global_colour;
+            p.SetGlobalColour(g[0], g[1], g[2], g[3]);
+            p.SetColourData(static_cast<geocalls::SimpleSphericalParticles::ColourDataType>(lists[i].col_type),
+                lists[i].col, lists[i].col_stride);
+        }
         if (lists[i].dir != nullptr)
             p.SetDirData(geocalls::SimpleSphericalParticles::DIRDATA_FLOAT_XYZ, lists[i].dir);
     }

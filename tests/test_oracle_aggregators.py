@@ -54,6 +54,58 @@ def test_vector_aggregator_bit_exact(normalize):
         assert (meta["min_value"], meta["max_value"]) == (mn, mx)
 
 
+def _colour_list(kind, rng, n=900):
+    """One particle list with colour data of `kind`, the colour interleaved after the vertex record (the MMPLD
+    layout), and the weights the intensity aggregator reads from it."""
+    def interleaved(vt, v, ct, c):
+        rec = np.concatenate([np.ascontiguousarray(v).view(np.uint8).reshape(len(v), -1),
+                              np.ascontiguousarray(c).view(np.uint8).reshape(len(c), -1)], 1)
+        return dict(type=vt, data=rec.copy(), stride=rec.shape[1], count=len(v), col_type=ct,
+                    col_offset=v.itemsize * v.shape[1], col_stride=rec.shape[1], radius=0.8)
+
+    xyz = rng.uniform(0, 20, (n, 3)).astype(np.float32)
+    if kind == "uint8_rgba":
+        c = rng.integers(0, 256, (n, 4)).astype(np.uint8)
+        return interleaved(1, xyz, 2, c), c[:, 0].astype(np.float32)
+    if kind == "uint8_rgb":
+        c = rng.integers(0, 256, (n, 3)).astype(np.uint8)
+        return interleaved(1, xyz, 1, c), c[:, 0].astype(np.float32)
+    if kind == "float_rgb":
+        xyzr = np.column_stack([xyz, rng.uniform(0.4, 1.2, n)]).astype(np.float32)
+        c = rng.uniform(-2, 3, (n, 3)).astype(np.float32)
+        return dict(interleaved(2, xyzr, 3, c), radius=0.0), c[:, 0]
+    if kind == "float_rgba":
+        c = rng.uniform(-1, 1, (n, 4)).astype(np.float32)
+        return interleaved(1, xyz, 4, c), c[:, 0]
+    if kind == "ushort_rgba":
+        c = rng.integers(0, 65536, (n, 4)).astype(np.uint16)
+        return interleaved(4, xyz.astype(np.float64), 6, c), c[:, 0].astype(np.float32)
+    if kind == "double_i":
+        c = rng.uniform(-5, 5, (n, 1))
+        return interleaved(3, rng.integers(0, 20, (n, 3)).astype(np.uint16), 7, c), c[:, 0].astype(np.float32)
+    # COLDATA_NONE: the global colour's red channel
+    return (dict(type=1, data=xyz, stride=0, count=n, radius=0.85, col_type=0, global_colour=(77, 5, 6, 255)),
+            np.full(n, np.float32(77) / np.float32(255), np.float32))
+
+
+@needs_ref
+@pytest.mark.parametrize("kind", ["uint8_rgba", "uint8_rgb", "float_rgb", "float_rgba", "ushort_rgba", "double_i",
+                                  "global"])
+def test_intensity_from_every_colour_type_bit_exact(kind):
+    """The intensity aggregator reads the first colour channel through SimpleSphericalParticles' accessor
+    (ParticlesToDensity.cpp:483,508-516; SimpleSphericalParticles.h:123-177, Accessor.h:88-90,136-147): the raw
+    value as float for UINT8 / USHORT / FLOAT / DOUBLE data (with every vertex type), and the global colour's
+    red channel / 255 for COLDATA_NONE. The weights restated that way give the module's volume bit for bit
+    (one list per frame: the module's OpenMP partition is per list)."""
+    from tests import golden_io as G
+
+    L, w = _colour_list(kind, np.random.default_rng(12))
+    res, bbox = (21, 19, 23), (0, 0, 0, 20, 20, 20)
+    ref, _ = oracle.reference_density([L], bbox, res, (1, 0, 1), False, 1.0, aggregator=1)
+    mine = oracle.density_weighted(G.list_to_xyzr(L), w, bbox, res, cyclic=(1, 0, 1), nthreads=T)
+    assert np.array_equal(ref.reshape(-1), mine.reshape(-1))
+
+
 def test_weighted_fp64_is_linear():
     rng = np.random.default_rng(9)
     _, xyzr, inten, dirs = frame(rng, 800)
