@@ -52,6 +52,28 @@ def test_surface_box_adjustment_vs_reference_golden():
     assert c["volume"].shape == tuple(res[::-1])
 
 
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference module build not present")
+@pytest.mark.parametrize("seed", range(8))
+def test_surface_box_adjustment_vs_live_reference(seed):
+    """Random boxes (offsets, flat and tall aspect ratios) and slot resolutions: the restated box adjustment
+    publishes the module's resolution, origin, extents and slice distances bit for bit."""
+    rng = np.random.default_rng(300 + seed)
+    lo = rng.uniform(-50, 50, 3)
+    hi = lo + rng.uniform(0.5, 40, 3) * rng.choice([0.2, 1.0, 3.0], 3)
+    bbox = tuple(float(v) for v in np.concatenate([lo, hi]).astype(np.float32))
+    res = tuple(int(v) for v in rng.integers(6, 40, 3))
+    xyz = rng.uniform(lo, hi, (200, 3)).astype(np.float32)
+    _, meta = oracle.reference_density([dict(type=1, data=xyz, stride=0, radius=0.3, count=200)], bbox, res,
+                                       (0, 0, 0), False, 1.0, surface=True)
+    bb, rr = oracle.modify_bbox_f32(bbox, res)
+    f = np.float32
+    assert list(rr) == meta["resolution"]
+    for a in range(3):
+        ext = abs(f(bb[a + 3]) - f(bb[a]))
+        assert f(bb[a]) == f(meta["origin"][a]) and ext == f(meta["extents"][a])
+        assert ext / f(rr[a] - 1) == f(meta["slice_dists"][a])
+
+
 def test_kat_single_particle_on_node():
     """A particle on node (5,5,5) of a unit grid, r = 1: the bump at d=0 is exp(-1); nodes at distance
     1 lie on the support boundary and get exactly 0 (ParticlesToDensity.cpp:472-476)."""
