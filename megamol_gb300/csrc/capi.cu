@@ -241,22 +241,35 @@ struct p2v_ctx {
 namespace {
 
 // ParticlesToDensity::modifyBBox (ParticlesToDensity.cpp:749-799), in the same float arithmetic:
-// grow the box by 10% plus two voxels in z, make voxels cubic and rewrite sizex / sizey.
-void modify_bbox(float bb[6], int32_t& sx, int32_t& sy, int32_t sz) {
+// grow the box by 10% plus two voxels in z, make voxels cubic and rewrite sizex / sizey. Returns false
+// where the reference's float-to-int conversions would be undefined (a non-finite box, a box without
+// depth, sizez < 1, or a width or height of 2^30 voxels or more); the caller reports the error.
+bool modify_bbox(float bb[6], int32_t& sx, int32_t& sy, int32_t sz) {
+    for (int a = 0; a < 6; ++a)
+        if (!std::isfinite(bb[a]))
+            return false;
     float rangeOSx = std::fabs(bb[3] - bb[0]), rangeOSy = std::fabs(bb[4] - bb[1]), rangeOSz = std::fabs(bb[5] - bb[2]);
+    if (sz < 1 || !(rangeOSz > 0.0f))
+        return false;
     float general_box_scaling = 1.1f;
     float spacing = (rangeOSz * general_box_scaling) / sz;
     float newDepth = (rangeOSz * general_box_scaling) + 2 * spacing;
     spacing = newDepth / sz;
     float newWidth = (rangeOSx * general_box_scaling) + 2 * spacing;
-    int resolutionX = static_cast<int>(newWidth / spacing);
-    float rest = newWidth / spacing - static_cast<float>(resolutionX);
+    const float qx = newWidth / spacing;  // the reference evaluates this quotient twice, with the same result
+    if (!(qx < 1073741824.0f))
+        return false;
+    int resolutionX = static_cast<int>(qx);
+    float rest = qx - static_cast<float>(resolutionX);
     newWidth += (1 - rest) * spacing;
     resolutionX += 1;
     sx = resolutionX;
     float newHeight = (rangeOSy * general_box_scaling) + 2 * spacing;
-    int resolutionY = static_cast<int>(newHeight / spacing);
-    rest = newHeight / spacing - static_cast<float>(resolutionY);
+    const float qy = newHeight / spacing;
+    if (!(qy < 1073741824.0f))
+        return false;
+    int resolutionY = static_cast<int>(qy);
+    rest = qy - static_cast<float>(resolutionY);
     newHeight += (1 - rest) * spacing;
     resolutionY += 1;
     sy = resolutionY;
@@ -267,6 +280,7 @@ void modify_bbox(float bb[6], int32_t& sx, int32_t& sy, int32_t sz) {
     bb[3] = maxOSx + (newWidth - rangeOSx) / 2;
     bb[4] = maxOSy + (newHeight - rangeOSy) / 2;
     bb[5] = maxOSz + (newDepth - rangeOSz) / 2;
+    return true;
 }
 
 // SphereRenderer::generate3ConeDirections (SphereRenderer.cpp:2572-2587) for K = 3; other K use the
@@ -382,7 +396,9 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     std::memcpy(bb, fr->bbox, sizeof(bb));
     int32_t res[3] = {P.sizex, P.sizey, P.sizez};
     if (P.forSurfaceReconstruction) {
-        modify_bbox(bb, res[0], res[1], res[2]);
+        if (!modify_bbox(bb, res[0], res[1], res[2]))
+            return fail(P2V_EINVAL, "forSurfaceReconstruction needs a finite box with depth and sizez >= 1, and at "
+                                    "most 2^30 voxels along x and y");
         prm.sizex = res[0];
         prm.sizey = res[1];
     }

@@ -176,6 +176,19 @@ def test_surface_reconstruction_box(ctx):
     assert abs(sd[0] - sd[2]) < 0.2 * sd[2]
 
 
+def test_surface_reconstruction_rejects_flat_box(ctx):
+    """A box without depth would divide by a zero voxel spacing in the box adjustment (the reference's
+    float-to-int conversions are then undefined): the frame is rejected and the context stays usable."""
+    x = np.zeros((10, 4), np.float32)
+    x[:, :2] = np.random.default_rng(1).uniform(0, 1, (10, 2))
+    x[:, 3] = 0.5
+    ctx.set_params(sizex=8, sizey=8, sizez=8, forSurfaceReconstruction=1, normalize=0, cyclX=0, cyclY=0, cyclZ=0)
+    with pytest.raises(p2v.P2VError):
+        ctx.run_frame([p2v.ParticleList(x, p2v.VERTDATA_FLOAT_XYZR)], (0, 0, 0, 1, 1, 0), None)
+    vol, meta = run(ctx, [p2v.ParticleList(x, p2v.VERTDATA_FLOAT_XYZR)], (0, 0, 0, 1, 1, 1), (8, 8, 8))
+    assert meta["resolution"] == [8, 8, 8] and np.isfinite(vol).all()
+
+
 @pytest.mark.parametrize("seed,accumulate", [(0, p2v.ACCUM_EXACT), (1, p2v.ACCUM_KAHAN)])
 def test_lj_liquid_full_size(ctx, seed, accumulate):
     """The headline workload at full size (4M particles, 256^3), against the FP64 oracle."""
