@@ -65,7 +65,7 @@ typedef enum p2v_mem { P2V_MEM_HOST = 0, P2V_MEM_DEVICE = 1 } p2v_mem;
  * deviation sigma*r cut at 3 sigma, shifted by its value at the cut so it ends continuously at zero. */
 typedef enum p2v_kernel { P2V_KERNEL_BUMP = 0, P2V_KERNEL_GAUSS3 = 1 } p2v_kernel;
 
-/* Voxel accumulation. EXACT: every FP32 contribution is rounded to a multiple of 2^-40 and summed in
+/* Voxel accumulation. EXACT: every FP32 contribution is rounded to a multiple of 2^-32 and summed in
  * 64-bit integers, i.e. the exact, order-independent sum, rounded once to FP32 (particle-major scatter
  * into shared-memory tiles; the fast path). KAHAN: each voxel gathers its contributions in cell order
  * with a Kahan-compensated FP32 sum (node-major). Both are deterministic run to run. */

