@@ -102,3 +102,17 @@ def test_megamol_adapter_compiles_against_reference_headers():
                         os.path.join(ROOT, "include"), "-I", os.path.join(ref, "plugins", "geometry_calls", "include"),
                         "-I", os.path.join(ref, "vislib", "include"), src], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_header_constants_match_binding():
+    """Every #define and enum value of include/p2v.h that the ctypes binding mirrors (P2V_X -> p2v.X) has
+    the same value there."""
+    consts = {}
+    for h in HEADERS:
+        txt = open(h).read()
+        consts.update({m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+P2V_(\w+)\s+(-?\d+)\b", txt)})
+        consts.update({m.group(1): int(m.group(2)) for m in re.finditer(r"\bP2V_(\w+)\s*=\s*(-?\d+)", txt)})
+    matched = {k: v for k, v in consts.items() if hasattr(p2v, k) and isinstance(getattr(p2v, k), int)}
+    assert len(matched) >= 20, sorted(matched)
+    wrong = {k: (v, getattr(p2v, k)) for k, v in matched.items() if getattr(p2v, k) != v}
+    assert not wrong, wrong
