@@ -412,7 +412,7 @@ P2V_API p2v_status p2v_mlp_infer(p2v_ctx* ctx, const float* x, uint32_t n, float
  * loads the library); larger volumes are rejected with P2V_EINVAL. The first call on a device looks up
  * that array's address (make it before any stream capture). Calls share the array: calls that overlap on
  * the GPU race. Asynchronous on `stream` (a cudaStream_t, NULL = the legacy default stream). */
-#define P2V_NOALLOC_MAX_VOXELS (64 * 64 * 64)
+#define P2V_NOALLOC_MAX_VOXELS 262144 /* 64^3 */
 P2V_API p2v_status p2v_aosphere_ao_noalloc(const float* xyzr, const float* normals, uint64_t count,
                                            const float clipbox[6], const int32_t vol_size[3], float step_len,
                                            float gen_fac, float eval_fac, int32_t mode, float* ao_out, void* stream);

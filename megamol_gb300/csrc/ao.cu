@@ -80,8 +80,8 @@ __device__ __forceinline__ float saturate_if(float v, float sat) {
 }
 
 // One GL LINEAR sample. When the 2x2x2 block lies inside the level (the common case) the eight texels are
-// read from one base pointer without per-texel checks; the host keeps every level below 2^31 texels so the
-// offsets fit in 32 bits.
+// read from one base pointer without per-texel checks. The base offset and the z stride are 64-bit: a level
+// may hold more than 2^31 texels (an AOSphere volume of 2048^3, a density grid above 1290^3).
 __device__ __forceinline__ float trilinear(const Level& L, float ux, float uy, float uz, int border, float sat) {
     // explicitly rounded operations: every kernel that inlines this gets the same bits
     const float cx = __fmaf_rn(ux, L.fd[0], -0.5f), cy = __fmaf_rn(uy, L.fd[1], -0.5f);
@@ -91,8 +91,9 @@ __device__ __forceinline__ float trilinear(const Level& L, float ux, float uy, f
     const float fx = __fsub_rn(cx, fx0), fy = __fsub_rn(cy, fy0), fz = __fsub_rn(cz, fz0);
     float c000, c100, c010, c110, c001, c101, c011, c111;
     if (x0 >= 0 && y0 >= 0 && z0 >= 0 && x0 + 1 < L.d[0] && y0 + 1 < L.d[1] && z0 + 1 < L.d[2]) {
-        const int sy = L.d[0], sz = L.d[0] * L.d[1];
-        const float* b = L.v + ((z0 * L.d[1] + y0) * L.d[0] + x0);
+        const int sy = L.d[0];
+        const int64_t sz = (int64_t) L.d[0] * L.d[1];
+        const float* b = L.v + (((int64_t) z0 * L.d[1] + y0) * L.d[0] + x0);
         c000 = saturate_if(__ldg(b), sat);
         c100 = saturate_if(__ldg(b + 1), sat);
         c010 = saturate_if(__ldg(b + sy), sat);

@@ -75,14 +75,16 @@ extern "C" p2v_status p2v_aosphere_ao_noalloc(const float* xyzr, const float* no
         return P2V_EINVAL;
     if (count >= (1ull << 31))
         return P2V_EINVAL;
+    // Checked after every factor, so the product cannot wrap: each axis is at most the maximum, and a
+    // running product above it is rejected before the next multiplication.
     uint64_t voxels = 1;
     for (int a = 0; a < 3; ++a) {
-        if (vol_size[a] < 3)
+        if (vol_size[a] < 3 || vol_size[a] > P2V_NOALLOC_MAX_VOXELS)
             return P2V_EINVAL;
         voxels *= (uint64_t) vol_size[a];
+        if (voxels > (uint64_t) P2V_NOALLOC_MAX_VOXELS)
+            return P2V_EINVAL;  // beyond the static scratch; use p2v_run_frame, which allocates what it needs
     }
-    if (voxels > (uint64_t) P2V_NOALLOC_MAX_VOXELS)
-        return P2V_EINVAL;  // beyond the static scratch; use p2v_run_frame, which allocates what it needs
     p2v::AOSphereParams ap{};
     for (int a = 0; a < 3; ++a) {
         ap.s[a] = vol_size[a];

@@ -90,6 +90,7 @@ class BatchItemC(C.Structure):
 
 
 TUNE_MAX = 32
+NOALLOC_MAX_VOXELS = 262144  # P2V_NOALLOC_MAX_VOXELS: voxels of p2v_aosphere_ao_noalloc's static scratch
 
 
 class TuneReportC(C.Structure):

@@ -114,5 +114,6 @@ def test_header_constants_match_binding():
         consts.update({m.group(1): int(m.group(2)) for m in re.finditer(r"\bP2V_(\w+)\s*=\s*(-?\d+)", txt)})
     matched = {k: v for k, v in consts.items() if hasattr(p2v, k) and isinstance(getattr(p2v, k), int)}
     assert len(matched) >= 20, sorted(matched)
+    assert {"NOALLOC_MAX_VOXELS", "MLP_INPUTS", "MLP_PARAMS", "TUNE_MAX"} <= set(matched), sorted(matched)
     wrong = {k: (v, getattr(p2v, k)) for k, v in matched.items() if getattr(p2v, k) != v}
     assert not wrong, wrong

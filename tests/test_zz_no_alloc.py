@@ -55,7 +55,23 @@ def test_noalloc_rejects_volumes_beyond_its_scratch():
     d = torch.zeros((4, 4), dtype=torch.float32, device="cuda")
     ao = torch.zeros(4, dtype=torch.float32, device="cuda")
     clip = (C.c_float * 6)(0, 0, 0, 1, 1, 1)
-    too_big = (C.c_int32 * 3)(65, 64, 64)
+    edge = round(p2v.NOALLOC_MAX_VOXELS ** (1 / 3))
+    assert edge ** 3 == p2v.NOALLOC_MAX_VOXELS
+    too_big = (C.c_int32 * 3)(edge + 1, edge, edge)
     st = lib.p2v_aosphere_ao_noalloc(d.data_ptr(), d.data_ptr(), 4, clip, too_big, 0.5, 1.0, 1.0,
                                      p2v.AO_AOSPHERE_AXES, ao.data_ptr(), None)
     assert st == p2v.EINVAL
+
+
+def test_noalloc_rejects_sizes_whose_product_wraps():
+    """(2^21, 2^21, 2^22) voxels multiply to 2^64, which wraps to 0 in 64 bits; the size check must still
+    reject it. With count 0 no kernel would run even if the check let it through."""
+    torch = pytest.importorskip("torch")
+    lib = p2v.library()
+    ao = torch.zeros(4, dtype=torch.float32, device="cuda")
+    clip = (C.c_float * 6)(0, 0, 0, 1, 1, 1)
+    for size in [(1 << 21, 1 << 21, 1 << 22), (1 << 30, 1 << 30, 1 << 4), (3, 3, p2v.NOALLOC_MAX_VOXELS + 1)]:
+        vs = (C.c_int32 * 3)(*size)
+        st = lib.p2v_aosphere_ao_noalloc(ao.data_ptr(), ao.data_ptr(), 0, clip, vs, 0.5, 1.0, 1.0,
+                                         p2v.AO_AOSPHERE_AXES, ao.data_ptr(), None)
+        assert st == p2v.EINVAL, size
