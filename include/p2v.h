@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 7
+#define P2V_ABI_VERSION 8
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -197,15 +197,19 @@ typedef struct p2v_stats {
                                     tried (it takes frames whose cells hold at most 32), 0 = radix sort only */
 } p2v_stats;
 
-/* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle:
- * mip levels s and s + 1 of the AO volume, each a 3x3x3 stencil of trilinear samples 1.5 texels apart
- * centred on the surface point (in the order kz*9 + ky*3 + kx), then the unit normal, then the surface point
- * in normalised volume coordinates (the cones reach a large fraction of the volume, so AO also depends on
- * where the point sits in it); P2V_MLP_INPUTS values. Network 60 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid.
- * Parameter vector: W1[64][60], b1[64], W2[64][64], b2[64], w3[64], b3. */
-#define P2V_MLP_INPUTS 60
+/* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle: the
+ * cone march's own visibility samples (mdao_deferred_fragment_ambocc.inc.glsl:30-51), filtered by the texture
+ * units: for each of P2V_MLP_CONES cones, in the particle's cone frame, the AO volume at P2V_MLP_FSTEPS of the
+ * march's steps (step round(j (steps - 1) / (P2V_MLP_FSTEPS - 1)) for feature j), each at the step's own mip
+ * level (linear between the two levels around its lod); cone-major (feature c * P2V_MLP_FSTEPS + j). Then the
+ * unit normal and the surface point in normalised volume coordinates; P2V_MLP_INPUTS values. The learned AO
+ * therefore needs ao_cones = P2V_MLP_CONES. Network 78 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid. Parameter
+ * vector: W1[64][78], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define P2V_MLP_CONES 8
+#define P2V_MLP_FSTEPS 9
+#define P2V_MLP_INPUTS 78
 #define P2V_MLP_HIDDEN 64
-#define P2V_MLP_PARAMS 8129
+#define P2V_MLP_PARAMS 9281
 
 typedef struct p2v_train_params {
     uint32_t struct_size;   /* sizeof(p2v_train_params); set by p2v_train_params_default */

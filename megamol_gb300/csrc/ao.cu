@@ -14,6 +14,7 @@
 #include <cstdint>
 
 #include "ao_internal.h"
+#include "cone_device.cuh"
 #include "p2v_common.cuh"
 
 namespace p2v {
@@ -118,36 +119,6 @@ __device__ __forceinline__ float trilinear(const Level& L, float ux, float uy, f
     return lerp_rn(c0, c1, fz);
 }
 
-// Surface point and unit normal of particle `o`.
-__device__ __forceinline__ bool surface_point(const float4 p, const float4 nrm, float x[3], float n[3]) {
-    const float l2 = __fmaf_rn(nrm.z, nrm.z, __fmaf_rn(nrm.y, nrm.y, __fmul_rn(nrm.x, nrm.x)));
-    if (!(l2 > 0.0f))
-        return false;
-    const float il = rsqrtf(l2);
-    n[0] = __fmul_rn(nrm.x, il);
-    n[1] = __fmul_rn(nrm.y, il);
-    n[2] = __fmul_rn(nrm.z, il);
-    x[0] = __fmaf_rn(p.w, n[0], p.x);
-    x[1] = __fmaf_rn(p.w, n[1], p.y);
-    x[2] = __fmaf_rn(p.w, n[2], p.z);
-    return true;
-}
-
-__device__ __forceinline__ void cross_rn(const float a[3], const float b[3], float out[3]) {
-    out[0] = __fsub_rn(__fmul_rn(a[1], b[2]), __fmul_rn(a[2], b[1]));
-    out[1] = __fsub_rn(__fmul_rn(a[2], b[0]), __fmul_rn(a[0], b[2]));
-    out[2] = __fsub_rn(__fmul_rn(a[0], b[1]), __fmul_rn(a[1], b[0]));
-}
-
-// Cone c's direction in the particle's frame.
-__device__ __forceinline__ void cone_dir(const ConeParams& cp, int c, const float ex[3], const float nn[3],
-                                         const float ez[3], float dir[3]) {
-    const float4 cd = cp.dirs[c];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        dir[a] = __fmaf_rn(ez[a], cd.z, __fmaf_rn(nn[a], cd.y, __fmul_rn(ex[a], cd.x)));
-}
-
 // Visibility sample k of a cone: trilinear in the two levels around its lod, blended linearly
 // (LINEAR_MIPMAP_LINEAR).
 __device__ __forceinline__ float cone_sample(const ConeParams& cp, const float dir[3], const float u[3], int k) {
@@ -176,41 +147,22 @@ __device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const f
     return acc;
 }
 
-// Cone frame at surface point x with unit normal nn (mdao_deferred_fragment_ambocc.inc.glsl:18-21):
-// new_y = n, new_x = cross(n, normalize(objPos)), new_z = cross(new_x, new_y); and x in normalised volume
-// coordinates.
-__device__ __forceinline__ void cone_frame(const ConeParams& cp, const float x[3], const float nn[3], float u[3],
-                                           float ex[3], float ez[3]) {
-    float xn[3] = {x[0], x[1], x[2]};
-    const float xl2 = __fmaf_rn(xn[2], xn[2], __fmaf_rn(xn[1], xn[1], __fmul_rn(xn[0], xn[0])));
-    if (xl2 > 0.0f) {
-        const float il = rsqrtf(xl2);
-        xn[0] = __fmul_rn(xn[0], il);
-        xn[1] = __fmul_rn(xn[1], il);
-        xn[2] = __fmul_rn(xn[2], il);
-    } else {
-        xn[0] = 1.0f;
-        xn[1] = xn[2] = 0.0f;
-    }
-    cross_rn(nn, xn, ex);
-    cross_rn(ex, nn, ez);
-    u[0] = __fmul_rn(__fsub_rn(x[0], cp.bmin[0]), cp.ibsize[0]);
-    u[1] = __fmul_rn(__fsub_rn(x[1], cp.bmin[1]), cp.ibsize[1]);
-    u[2] = __fmul_rn(__fsub_rn(x[2], cp.bmin[2]), cp.ibsize[2]);
-}
-
-// One thread per particle: marches all cones (throughput: millions of particles).
+// One thread per particle: marches all cones (throughput: millions of particles). Particle i's data are
+// read at order[i] (or i) and its AO is written at out_order[i] (or there): the frame's kernels read sorted
+// copies and scatter the AO straight to input order.
 __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
-    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, float* __restrict__ ao) {
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n, const uint32_t* __restrict__ out_order,
+    float* __restrict__ ao) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     const uint32_t o = order ? order[i] : i;
+    const uint32_t w = out_order ? out_order[i] : o;
     const float4 p = xyzr[o];
     const float4 nv = nrm[o];
     float x[3], nn[3];
     if (!surface_point(p, nv, x, nn)) {
-        ao[o] = 1.0f;  // no normal: no occlusion
+        ao[w] = 1.0f;  // no normal: no occlusion
         return;
     }
     float u[3], ex[3], ez[3];
@@ -218,7 +170,7 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
     float ambient = 0.0f;
     for (int c = 0; c < cp.ncones; ++c)
         ambient += march_cone(cp, c, u, ex, nn, ez);
-    ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+    ao[w] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
 }
 
 // The learned AO's fallback list (its length a device-side count, usually tiny): latency matters, so a
@@ -229,7 +181,7 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
 // list.
 __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const ConeParams cp,
     const uint32_t* __restrict__ list, const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n,
-    const uint32_t* __restrict__ n_dev, float* __restrict__ ao) {
+    const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ out_order, float* __restrict__ ao) {
     __shared__ float s_acc[MAX_CONES];
     const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
     n = min(n, *n_dev);
@@ -238,9 +190,10 @@ __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const Cone
         const float4 p = xyzr[o];
         const float4 nv = nrm[o];
         float x[3], nn[3];
+        const uint32_t w = out_order ? out_order[o] : o;
         if (!surface_point(p, nv, x, nn)) {  // the whole block takes this branch
             if (threadIdx.x == 0)
-                ao[o] = 1.0f;
+                ao[w] = 1.0f;
             continue;
         }
         float u[3], ex[3], ez[3], dir[3];
@@ -266,7 +219,7 @@ __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const Cone
             float ambient = 0.0f;
             for (int k = 0; k < cp.ncones; ++k)
                 ambient += s_acc[k];
-            ao[o] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+            ao[w] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
         }
         __syncthreads();
     }
@@ -274,21 +227,16 @@ __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const Cone
 
 // Positions and normals in sorted (cell) order: the AO kernels then read them coalesced whatever the input
 // order was (a streaming kernel keeps many of these scattered reads in flight; inside the latency-bound AO
-// kernels they stalled every tile), and the AO returns to input order once at the end.
+// kernels they stalled every tile). The AO kernels store each result straight at its input-order index.
 __global__ void __launch_bounds__(256) sort_particles_kernel(const uint32_t* __restrict__ order, uint32_t n,
     const float4* __restrict__ xyzr, const float4* __restrict__ nrm, float4* __restrict__ xyzr_s,
     float4* __restrict__ nrm_s) {
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t o = order[j];
-        xyzr_s[j] = xyzr[o];
+        if (xyzr)  // null: the binning's last pass wrote the sorted positions already
+            xyzr_s[j] = xyzr[o];
         nrm_s[j] = nrm[o];
     }
-}
-
-__global__ void __launch_bounds__(256) unsort_ao_kernel(const uint32_t* __restrict__ order, uint32_t n,
-    const float* __restrict__ ao_s, float* __restrict__ ao) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        ao[order[j]] = ao_s[j];
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -412,15 +360,15 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
 }
 
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
-    uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st) {
+    uint32_t n, const uint32_t* n_dev, const uint32_t* out_order, float* ao, cudaStream_t st) {
     if (n == 0)
         return cudaSuccess;
     if (n_dev == nullptr) {
-        cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, ao);
+        cone_ao_kernel<<<ceil_div(n, 128), 128, 0, st>>>(cp, order, xyzr, nrm, n, out_order, ao);
     } else {
         // the learned AO's fallback list: one block of ncones warps per particle, a bounded grid
         const unsigned grd = (unsigned) std::min<uint32_t>(n, 4096u);
-        cone_ao_list_kernel<<<grd, 32 * cp.ncones, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, ao);
+        cone_ao_list_kernel<<<grd, 32 * cp.ncones, 0, st>>>(cp, order, xyzr, nrm, n, n_dev, out_order, ao);
     }
     return cudaGetLastError();
 }
@@ -446,14 +394,6 @@ cudaError_t launch_sort_particles(const uint32_t* order, uint32_t n, const float
         return cudaSuccess;
     const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
     sort_particles_kernel<<<grd, 256, 0, st>>>(order, n, xyzr, nrm, xyzr_s, nrm_s);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_unsort_ao(const uint32_t* order, uint32_t n, const float* ao_s, float* ao, int sms, cudaStream_t st) {
-    if (n == 0)
-        return cudaSuccess;
-    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
-    unsort_ao_kernel<<<grd, 256, 0, st>>>(order, n, ao_s, ao);
     return cudaGetLastError();
 }
 

@@ -10,6 +10,7 @@ namespace p2v {
 constexpr int MAX_CONES = 16;
 constexpr int MAX_STEPS = 256;
 constexpr int MAX_LEVELS = 12;
+constexpr int MAX_FSTEPS = 16;
 
 struct ConeLevel {
     const float* v;
@@ -28,9 +29,11 @@ struct ConeParams {
     float4 dirs[MAX_CONES];        // xyz around +Y, w = cone width
     float t[MAX_STEPS], lod[MAX_STEPS];
     ConeLevel lv[MAX_LEVELS];
-    int stencil_level;             // learned AO: first of the two mip levels its stencil reads
-    unsigned long long stex[2];    // learned AO: FP16 layered textures of those two levels (bilinear per slice)
-    float sinv[2][3];              // their inverse sizes (texel spacing in normalised coordinates)
+    // learned AO: the march steps its features sample (per cone), and 8-bit paired-slice layered textures of
+    // the mip levels those samples read (0 = level not needed)
+    int nfsteps;
+    int fstep[MAX_FSTEPS];
+    unsigned long long ftex[MAX_LEVELS];
 };
 
 struct AOSphereParams {
@@ -56,12 +59,13 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
 cudaError_t launch_mdao_volume(const MdaoParams& mp, const uint32_t* order, const float4* xyzr, uint32_t n,
     void* acc, float* vol, int sms, cudaStream_t st);
 // n_dev (nullable): device-side particle count, at most n (the cone march of the learned-AO fallback list)
-// xyzr_s[j] = xyzr[order[j]], nrm_s[j] = nrm[order[j]] (sorted order), and back for the AO values.
+// xyzr_s[j] = xyzr[order[j]] (skipped when xyzr is null), nrm_s[j] = nrm[order[j]] (sorted order).
 cudaError_t launch_sort_particles(const uint32_t* order, uint32_t n, const float4* xyzr, const float4* nrm,
     float4* xyzr_s, float4* nrm_s, int sms, cudaStream_t st);
-cudaError_t launch_unsort_ao(const uint32_t* order, uint32_t n, const float* ao_s, float* ao, int sms, cudaStream_t st);
+// particle i (or list entry i) reads xyzr / nrm at order[i] (or i); its AO goes to ao[out_order[that index]]
+// when out_order is given (sorted copies in, input order out), else to ao[that index]
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
-    uint32_t n, const uint32_t* n_dev, float* ao, cudaStream_t st);
+    uint32_t n, const uint32_t* n_dev, const uint32_t* out_order, float* ao, cudaStream_t st);
 cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc,
     float* tex, const uint32_t* order, const float4* nrm, int mode, float* ao, int sms, cudaStream_t st);
 cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,

@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
     const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
     int shift, const uint32_t* __restrict__ digit_offsets, uint32_t* __restrict__ tile_counter,
     uint32_t* __restrict__ status, uint32_t* __restrict__ err, const float4* __restrict__ xyzr_in,
-    float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo, const FrameScalars* __restrict__ gate) {
+    float4* __restrict__ rec_a, int4* __restrict__ rec_b, float4* __restrict__ xyzr_out, GridGeo geo,
+    const FrameScalars* __restrict__ gate) {
     if (radix_skipped(gate))
         return;
     constexpr int RADIX = 1 << BITS;
@@ -399,12 +400,15 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
         const uint32_t vv = s_vals[j];
         vals_out[dst] = vv;
         if (GATHER) {
-            // last pass: emit the particle's gather record in sorted order
+            // last pass: emit the particle's gather record (and its xyzr) in sorted order
+            const float4 p = xyzr_in[vv];
             float4 A;
             int4 B;
-            make_record(xyzr_in[vv], geo, A, B);
+            make_record(p, geo, A, B);
             rec_a[REC_STRIDE * (size_t) dst] = A;
             rec_b[REC_STRIDE * (size_t) dst] = B;
+            if (xyzr_out)
+                xyzr_out[dst] = p;
         }
     }
 }
@@ -623,17 +627,20 @@ __global__ void __launch_bounds__(SCAN_THREADS) bin_starts_kernel(const uint32_t
 __global__ void __launch_bounds__(256) scatter_bins_kernel(const uint32_t* __restrict__ keys_in,
     const uint32_t* __restrict__ rank, const float4* __restrict__ xyzr, uint32_t n,
     const uint32_t* __restrict__ start, uint32_t* __restrict__ vals_out, float4* __restrict__ rec_a,
-    int4* __restrict__ rec_b, GridGeo geo, const FrameScalars* __restrict__ fs) {
+    int4* __restrict__ rec_b, float4* __restrict__ xyzr_out, GridGeo geo, const FrameScalars* __restrict__ fs) {
     if (fs->bin_maxcount > BIN_CELL_MAX)
         return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t slot = start[keys_in[i]] + rank[i];
         vals_out[slot] = i;
+        const float4 p = xyzr[i];
         float4 A;
         int4 B;
-        make_record(xyzr[i], geo, A, B);
+        make_record(p, geo, A, B);
         rec_a[REC_STRIDE * (size_t) slot] = A;
         rec_b[REC_STRIDE * (size_t) slot] = B;
+        if (xyzr_out)
+            xyzr_out[slot] = p;
     }
 }
 
@@ -641,7 +648,8 @@ __global__ void __launch_bounds__(256) scatter_bins_kernel(const uint32_t* __res
 // at most BIN_CELL_MAX entries) and rewrites their values and records: the result is the stable sort by key.
 __global__ void __launch_bounds__(256) order_bins_kernel(uint32_t n, uint32_t nbins, const uint32_t* __restrict__ multi,
     uint32_t* __restrict__ vals, const uint32_t* __restrict__ start, const float4* __restrict__ xyzr,
-    float4* __restrict__ rec_a, int4* __restrict__ rec_b, GridGeo geo, const FrameScalars* __restrict__ fs) {
+    float4* __restrict__ rec_a, int4* __restrict__ rec_b, float4* __restrict__ xyzr_out, GridGeo geo,
+    const FrameScalars* __restrict__ fs) {
     if (fs->bin_maxcount > BIN_CELL_MAX)
         return;
     const uint32_t nm = fs->bin_nmulti;
@@ -663,11 +671,14 @@ __global__ void __launch_bounds__(256) order_bins_kernel(uint32_t n, uint32_t nb
             if (vals[j + a] == v[a])
                 continue;
             vals[j + a] = v[a];
+            const float4 p = xyzr[v[a]];
             float4 A;
             int4 B;
-            make_record(xyzr[v[a]], geo, A, B);
+            make_record(p, geo, A, B);
             rec_a[REC_STRIDE * (size_t) (j + a)] = A;
             rec_b[REC_STRIDE * (size_t) (j + a)] = B;
+            if (xyzr_out)
+                xyzr_out[j + a] = p;
         }
     }
 }
@@ -758,7 +769,7 @@ cudaError_t launch_onesweep_bits(uint32_t tiles, SortBuffers& b, int cur, uint32
     onesweep_kernel<GATHER, BITS><<<tiles, SORT_THREADS, smem, st>>>(b.keys[cur],
         (cur == 0 && b.implicit_vals0 && b.first_pass) ? nullptr : b.vals[cur], b.keys[cur ^ 1],
         b.vals[cur ^ 1], n, shift, offs, counter, b.status, b.err, GATHER ? b.xyzr_in : nullptr,
-        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, b.geo, gate);
+        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, GATHER ? b.xyzr_out : nullptr, b.geo, gate);
     return cudaSuccess;
 }
 
@@ -834,9 +845,9 @@ cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32
         bin_tile_scan_kernel<<<1, 1024, 0, st>>>(b.status, ntiles);
         bin_starts_kernel<<<ntiles, SCAN_THREADS, 0, st>>>(counts, nb, b.status, start, b.keys[1], fs);
         scatter_bins_kernel<<<pgrid, 256, 0, st>>>(b.keys[0], b.vals[0], b.xyzr_in, n, start, b.vals[1], b.rec_a,
-                                                   b.rec_b, b.geo, fs);
+                                                   b.rec_b, b.xyzr_out, b.geo, fs);
         order_bins_kernel<<<pgrid, 256, 0, st>>>(n, g.nbins, b.keys[1], b.vals[1], start, b.xyzr_in, b.rec_a, b.rec_b,
-                                                 b.geo, fs);
+                                                 b.xyzr_out, b.geo, fs);
     }
     // the radix path: alone, or as the fallback (gated) when a cell holds more than BIN_CELL_MAX particles;
     // with the counting sort its pass count is odd so both leave the sorted keys in buffer 1

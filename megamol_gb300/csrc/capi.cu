@@ -70,8 +70,9 @@ struct Pipe {
     DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list, wts, wsorted, wsum;
     DevBuf vdens, vdirs, vkeys0, vkeys1, vvals0, vvals1, vout;  // the vector aggregator's grid outputs
     DevBuf bcount;                         // particles per cell (the counting sort)
-    DevBuf xyzr_s, nrm_s, ao_s;            // positions, normals and AO in sorted order (the cone AO stages)
-    StencilTex stex[2];                    // the learned AO's two stencil levels as textures
+    DevBuf xyzr_s, nrm_s;                  // positions and normals in sorted order (the cone AO stages)
+    bool xyzr_sorted = false;              // the binning of this frame wrote xyzr_s
+    FeatureTex ftex[MAX_LEVELS];           // the learned AO's feature levels as paired-slice textures
     cudaEvent_t ev[EV_COUNT] = {};
     cudaEvent_t sev[SEV_COUNT] = {};
     FrameScalars* h_scal = nullptr;        // pinned mirror of the last frame's scalars
@@ -117,10 +118,10 @@ struct Pipe {
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &xyzr_s, &nrm_s, &ao_s})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &xyzr_s, &nrm_s})
             b->release();
-        stex[0].release();
-        stex[1].release();
+        for (FeatureTex& t : ftex)
+            t.release();
         if (side)
             cudaStreamSynchronize(side);
         for (auto& e : ev)
@@ -203,7 +204,6 @@ struct p2v_ctx {
     std::vector<uint32_t> t_valid;       // indices of pairs with features
     std::vector<float> t_host_T;         // targets on the host (validation error)
     bool mlp_ready = false, mlp_has_range = false;
-    int mlp_level = -1;                  // stencil base level the network was trained on
     int mlp_step = 0;
     uint64_t mlp_seed = 0;
 
@@ -226,7 +226,7 @@ struct p2v_ctx {
     p2v_status build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
                           uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st);
     p2v_status mlp_alloc();
-    p2v_status prepare_stencil(Pipe& pp, ConeParams& cp, cudaStream_t st);
+    p2v_status prepare_features(Pipe& pp, ConeParams& cp, cudaStream_t st);
     p2v_status run_batch(const p2v_batch_item* items, uint32_t count, p2v_stats* out, cudaStream_t st,
                          bool allow_graph, float* ms_out);
     void drop_graph() {
@@ -468,10 +468,12 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     P2V_CUDA_TRY(keys1.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals0.ensure(4 * (N + 1)));
     P2V_CUDA_TRY(vals1.ensure(4 * (N + 1)));
-    // the counting sort by cell unless the cell table dwarfs the particle count: it passes over the table
-    // about four times (16 bytes per cell), where the radix sort spends ~150 bytes and several latency-bound
-    // passes per particle
-    const bool counting = n > 0 && (uint64_t) g.nbins + 1 <= 64ull * n;
+    // the counting sort by cell while its cell table stays near L2-resident: it passes over the table about
+    // four times (16 bytes per cell) and scatters every particle by a table lookup and an atomic, cheap while
+    // the table sits in L2; a table of hundreds of MB turns every lookup into a DRAM sector, where the radix
+    // sort's streaming passes (~150 bytes per particle) win
+    const bool counting = n > 0 && (uint64_t) g.nbins + 1 <= 64ull * n &&
+                          4ull * ((uint64_t) g.nbins + 1) <= COUNTING_TABLE_MAX_BYTES;
     if (counting)
         P2V_CUDA_TRY(pp.bcount.ensure(4 * ((size_t) g.nbins + 1)));
     P2V_CUDA_TRY(status.ensure(4 * (std::max(sort_status_words(n), bin_scan_words(g.nbins)) + 256)));
@@ -662,6 +664,12 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     sb.xyzr_in = xyzr.as<float4>();
     sb.rec_a = rec_a.as<float4>();
     sb.rec_b = reinterpret_cast<int4*>(rec_a.as<float4>() + 1);
+    // the cone-march stages read the positions in sorted order: the binning's last pass writes them
+    pp.xyzr_sorted = P.ao_mode == P2V_AO_CONE || P.ao_mode == P2V_AO_LEARNED;
+    if (pp.xyzr_sorted) {
+        P2V_CUDA_TRY(pp.xyzr_s.ensure(sizeof(float4) * ((size_t) n + 1)));
+        sb.xyzr_out = pp.xyzr_s.as<float4>();
+    }
     sb.geo = g;
     P2V_CUDA_TRY(launch_bin_sort(sb, n, g, counting ? pp.bcount.as<uint32_t>() : nullptr, cstart.as<uint32_t>(),
                                  gaps.as<uint4>(), gap_cap, fs, sms, st));
@@ -980,8 +988,6 @@ p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, 
     if (P.ao_steps > MAX_STEPS || (P.ao_steps <= 0 && cp.nsteps >= MAX_STEPS))
         return fail(P2V_EUNSUPPORTED, "more than %d samples per cone", MAX_STEPS);
     cp.nlevels = L;
-    // the learned AO's stencil reads the two levels the cone's first sample blends
-    cp.stencil_level = std::max(0, std::min((int) std::floor(cp.lod[0]), L - 2));
     // the samplers address texels with 32-bit offsets
     if ((uint64_t) d0[0] * d0[1] * d0[2] >= (1ull << 31))
         return fail(P2V_EUNSUPPORTED, "AO volume %dx%dx%d exceeds 2^31 texels", d0[0], d0[1], d0[2]);
@@ -1016,18 +1022,33 @@ p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, 
     return P2V_OK;
 }
 
-// Copy the learned AO's two stencil levels into their textures (level 0 of a density volume saturated as
-// the cone march sees it) and hand the texture objects to the kernels.
-p2v_status p2v_ctx::prepare_stencil(Pipe& pp, ConeParams& cp, cudaStream_t st) {
-    StencilTex* stex = pp.stex;
-    for (int h = 0; h < 2; ++h) {
-        const int l = cp.stencil_level + h;
+// The learned AO's feature samples: MLP_FSTEPS steps spread evenly over the cone's step table (step
+// round(j (nsteps - 1) / (MLP_FSTEPS - 1)) for feature j), each at its own lod. Copy every mip level those
+// samples read (level 0 of a density volume saturated as the cone march sees it) into its paired-slice
+// texture and hand the texture objects to the kernels.
+p2v_status p2v_ctx::prepare_features(Pipe& pp, ConeParams& cp, cudaStream_t st) {
+    if (cp.ncones != MLP_CONES)
+        return fail(P2V_EINVAL, "learned AO: its features read %d cones (ao_cones is %d)", MLP_CONES, cp.ncones);
+    if (cp.nsteps < 1)
+        return fail(P2V_EINVAL, "learned AO: empty cone step table");
+    cp.nfsteps = MLP_FSTEPS;
+    bool need[MAX_LEVELS] = {};
+    for (int j = 0; j < MLP_FSTEPS; ++j) {
+        const int k = (int) std::lround((double) j * (cp.nsteps - 1) / (double) (MLP_FSTEPS - 1));
+        cp.fstep[j] = k;
+        const int l0 = std::min((int) cp.lod[k], cp.nlevels - 1);
+        need[l0] = true;
+        if (cp.lod[k] - (float) l0 > 0.0f && l0 + 1 < cp.nlevels)
+            need[l0 + 1] = true;
+    }
+    for (int l = 0; l < MAX_LEVELS; ++l) {
+        cp.ftex[l] = 0;
+        if (l >= cp.nlevels || !need[l])
+            continue;
         const ConeLevel& L = cp.lv[l];
-        P2V_CUDA_TRY(stex[h].ensure(L.d));
-        P2V_CUDA_TRY(launch_fill_stencil_tex(L, l == 0 ? cp.sat : 0.0f, stex[h], st));
-        cp.stex[h] = stex[h].tex;
-        for (int a = 0; a < 3; ++a)
-            cp.sinv[h][a] = 1.0f / L.fd[a];
+        P2V_CUDA_TRY(pp.ftex[l].ensure(L.d));
+        P2V_CUDA_TRY(launch_fill_feature_tex(L, l == 0 ? cp.sat : 0.0f, pp.ftex[l], st));
+        cp.ftex[l] = pp.ftex[l].tex;
     }
     return P2V_OK;
 }
@@ -1039,15 +1060,14 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
     const p2v_params& P = prm;
     // the cone-march stages run on sorted copies of the positions and normals (coalesced whatever the input
     // order) and scatter the AO back to input order at the end
+    // (the binning's last pass wrote the sorted positions when it knew the frame would march cones)
     auto to_sorted = [&]() -> cudaError_t {
         cudaError_t e = pp.xyzr_s.ensure(sizeof(float4) * ((size_t) n + 1));
         if (e == cudaSuccess)
             e = pp.nrm_s.ensure(sizeof(float4) * ((size_t) n + 1));
         if (e == cudaSuccess)
-            e = pp.ao_s.ensure(sizeof(float) * ((size_t) n + 1));
-        if (e == cudaSuccess)
-            e = launch_sort_particles(order, n, xyzr.as<float4>(), nrm.as<float4>(), pp.xyzr_s.as<float4>(),
-                                      pp.nrm_s.as<float4>(), sms, st);
+            e = launch_sort_particles(order, n, pp.xyzr_sorted ? nullptr : xyzr.as<float4>(), nrm.as<float4>(),
+                                      pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), sms, st);
         return e;
     };
     if (P.ao_mode == P2V_AO_CONE) {
@@ -1056,9 +1076,8 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         if (bs != P2V_OK)
             return bs;
         P2V_CUDA_TRY(to_sorted());
-        P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr,
-                                    pp.ao_s.as<float>(), st));
-        P2V_CUDA_TRY(launch_unsort_ao(order, n, pp.ao_s.as<float>(), ao.as<float>(), sms, st));
+        P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr, order,
+                                    ao.as<float>(), st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_LEARNED) {
@@ -1068,11 +1087,7 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st);
         if (bs != P2V_OK)
             return bs;
-        if (cp.nlevels < 2)
-            return fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
-        if (mlp_level >= 0)
-            cp.stencil_level = std::min(mlp_level, cp.nlevels - 2);
-        const p2v_status ps = prepare_stencil(pp, cp, st);
+        const p2v_status ps = prepare_features(pp, cp, st);
         if (ps != P2V_OK)
             return ps;
         P2V_CUDA_TRY(fb_list.ensure(sizeof(uint32_t) * ((size_t) n + 1)));
@@ -1088,15 +1103,15 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         a.order = nullptr;  // sorted copies: position j is sorted position j
         a.xyzr = pp.xyzr_s.as<float4>();
         a.nrm = pp.nrm_s.as<float4>();
-        a.y = pp.ao_s.as<float>();
+        a.y = ao.as<float>();
+        a.out_order = order;
         a.fallback = fb_list.as<uint32_t>();
         a.nfallback = &fs->ao_fallback;
         a.err = &fs->error;
         P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
-        // the plain cone march for every particle whose stencil left the training range
+        // the plain cone march for every particle whose features left the training range
         P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n,
-                                    &fs->ao_fallback, pp.ao_s.as<float>(), st));
-        P2V_CUDA_TRY(launch_unsort_ao(order, n, pp.ao_s.as<float>(), ao.as<float>(), sms, st));
+                                    &fs->ao_fallback, order, ao.as<float>(), st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_AOSPHERE_AXES || P.ao_mode == P2V_AO_AOSPHERE_NORMAL) {
@@ -1390,7 +1405,10 @@ cudaError_t grow_keep(DevBuf& b, size_t need, size_t used) {
     return e;
 }
 
-constexpr char MLP_MAGIC[8] = {'P', '2', 'V', 'M', 'L', 'P', '0', '1'};
+constexpr char MLP_MAGIC[8] = {'P', '2', 'V', 'M', 'L', 'P', '0', '2'};
+static_assert(P2V_MLP_INPUTS == MLP_IN && P2V_MLP_HIDDEN == MLP_H && P2V_MLP_PARAMS == MLP_NPARAM &&
+                  P2V_MLP_CONES == MLP_CONES && P2V_MLP_FSTEPS == MLP_FSTEPS,
+              "the header's MLP sizes differ from the kernels'");
 }  // namespace
 
 extern "C" {
@@ -1767,7 +1785,6 @@ p2v_status p2v_mlp_clear(p2v_ctx* c) {
     if (!c)
         return P2V_EINVAL;
     c->t_pairs = 0;
-    c->mlp_level = -1;
     c->t_valid.clear();
     c->t_host_T.clear();
     return P2V_OK;
@@ -1784,14 +1801,8 @@ p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, 
         return st;
     const uint32_t nvalid = (uint32_t) c->stats.particles_binned;
     const uint32_t nsel = std::min(max_pairs, nvalid);
-    if (c->main.last_cp.nlevels < 2)
-        return c->fail(P2V_EINVAL, "learned AO needs ao_levels >= 2 (its stencil reads two mip levels)");
-    // the first frame fixes the stencil levels of the training set; later frames use the same levels
-    if (c->t_pairs == 0 || c->mlp_level < 0)
-        c->mlp_level = c->main.last_cp.stencil_level;
-    c->main.last_cp.stencil_level = std::min(c->mlp_level, c->main.last_cp.nlevels - 2);
     if (nsel > 0) {
-        const p2v_status ps = c->prepare_stencil(c->main, c->main.last_cp, c->own_stream);
+        const p2v_status ps = c->prepare_features(c->main, c->main.last_cp, c->own_stream);
         if (ps != P2V_OK)
             return ps;
         std::vector<uint32_t> sel(nvalid);
@@ -1816,8 +1827,8 @@ p2v_status p2v_mlp_collect(p2v_ctx* c, const p2v_frame* fr, uint32_t max_pairs, 
         uint32_t* d_kept = d_sel + nsel;
         cudaMemcpyAsync(d_sel, sel.data(), sizeof(uint32_t) * nsel, cudaMemcpyHostToDevice, c->own_stream);
         cudaMemsetAsync(d_kept, 0, sizeof(uint32_t), c->own_stream);
-        cudaError_t e = launch_mlp_collect(c->main.last_cp, c->main.last_order, d_sel, nsel, c->main.xyzr.as<float4>(),
-                                           c->main.nrm.as<float4>(), c->main.ao.as<float>(),
+        cudaError_t e = launch_mlp_collect(c->main.last_cp, c->main.last_order, d_sel, nsel, c->main.xyzr_s.as<float4>(),
+                                           c->main.nrm_s.as<float4>(), c->main.ao.as<float>(),
                                            c->tX.as<float>() + c->t_pairs * MLP_IN, c->tT.as<float>() + c->t_pairs,
                                            d_kept, c->own_stream);
         if (e != cudaSuccess)
@@ -2091,7 +2102,7 @@ p2v_status p2v_mlp_save(p2v_ctx* c, const char* path) {
     FILE* f = std::fopen(path, "wb");
     if (!f)
         return c->fail(P2V_EINVAL, "cannot open %s", path);
-    const int32_t hdr[7] = {1, MLP_IN, MLP_H, MLP_NPARAM, c->mlp_step, c->mlp_has_range ? 1 : 0, c->mlp_level};
+    const int32_t hdr[7] = {2, MLP_IN, MLP_H, MLP_NPARAM, c->mlp_step, c->mlp_has_range ? 1 : 0, MLP_FSTEPS};
     bool ok = std::fwrite(MLP_MAGIC, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(hdr), 1, f) == 1 &&
               std::fwrite(&c->mlp_seed, sizeof(uint64_t), 1, f) == 1 &&
               std::fwrite(P.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
@@ -2114,8 +2125,8 @@ p2v_status p2v_mlp_load(p2v_ctx* c, const char* path) {
     uint64_t seed = 0;
     std::vector<float> P(MLP_NPARAM), m(MLP_NPARAM), v(MLP_NPARAM), lo(MLP_IN), hi(MLP_IN);
     bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, MLP_MAGIC, 8) == 0 &&
-              std::fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == 1 && hdr[1] == MLP_IN && hdr[2] == MLP_H &&
-              hdr[3] == MLP_NPARAM && std::fread(&seed, sizeof(uint64_t), 1, f) == 1 &&
+              std::fread(hdr, sizeof(hdr), 1, f) == 1 && hdr[0] == 2 && hdr[1] == MLP_IN && hdr[2] == MLP_H &&
+              hdr[3] == MLP_NPARAM && hdr[6] == MLP_FSTEPS && std::fread(&seed, sizeof(uint64_t), 1, f) == 1 &&
               std::fread(P.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
               std::fread(m.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
               std::fread(v.data(), sizeof(float), MLP_NPARAM, f) == (size_t) MLP_NPARAM &&
@@ -2132,7 +2143,6 @@ p2v_status p2v_mlp_load(p2v_ctx* c, const char* path) {
     c->mlp_step = hdr[4];
     c->mlp_seed = seed;
     c->mlp_has_range = hdr[5] != 0;
-    c->mlp_level = hdr[6];
     if (c->mlp_has_range) {
         cudaMemcpy(c->mlp_lo.ptr, lo.data(), sizeof(float) * MLP_IN, cudaMemcpyHostToDevice);
         cudaMemcpy(c->mlp_hi.ptr, hi.data(), sizeof(float) * MLP_IN, cudaMemcpyHostToDevice);

@@ -1,16 +1,18 @@
 // Learned AO: a small MLP that stands in for the cone march.
 //
-// Input (60): two consecutive mip levels of the AO volume (the levels the cone's first samples read), each
-// resampled as a 3x3x3 stencil of trilinear samples 1.5 texels apart centred on the particle's surface
-// point (the stencil moves continuously with the point), then the unit normal and the surface point in
-// normalised volume coordinates (the cones reach far into the volume, so AO also depends on where in the
-// volume the point lies). Network 60 -> 64 -> 64 -> 1, SiLU, SiLU, sigmoid.
+// Input (78): the cone march's own visibility samples, read by the texture units: for each of the 8 cones, in
+// the particle's MDAO cone frame, the volume at 9 of the march's steps (spread evenly over the step table),
+// each at the step's own mip level (LINEAR_MIPMAP_LINEAR between the two levels around its lod); then the
+// unit normal and the surface point in normalised volume coordinates. Network 78 -> 64 -> 64 -> 1, SiLU,
+// SiLU, sigmoid: it learns how the march's 32 steps, early exit and cone average turn these samples into AO.
 // Training: FP32 forward/backward kernels per CTA with a fixed-order reduction of the per-CTA gradients,
 // then Adam; pairs come from the plain cone march. Inference: BF16 weights and features, FP32 accumulation
 // on the 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM), bias/activations in FP32. A
 // particle whose features leave the training range (per feature, with a margin) falls back to the cone
 // march.
-// No reference counterpart: the reference evaluates AO only by the GLSL cone march / AOSphere taps.
+// No reference counterpart: the reference evaluates AO only by the GLSL cone march / AOSphere taps
+// (plugins/moldyn_gl/shaders/moldyn_gl/sphere_renderer/inc/mdao_deferred_fragment_ambocc.inc.glsl:30-51 is the
+// march whose samples the features are).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -19,6 +21,7 @@
 #include <cstdint>
 
 #include "ao_internal.h"
+#include "cone_device.cuh"
 #include "mlp_internal.h"
 #include "p2v_common.cuh"
 
@@ -47,83 +50,87 @@ __device__ __forceinline__ float sigmoidf_(float a) {
     return 1.0f / (1.0f + __expf(-a));
 }
 
-// 3x3x3 trilinear samples of one mip level at offsets 1.5 (k - 1) texels around normalised point u (the
-// extent of a 4x4x4 stencil one texel apart, with 27 samples instead of 64), in the order kz*9 + ky*3 + kx.
-// The level is a layered 2D texture of FP16 pairs: layer L holds z slices L - 1 (red) and L (green), so one
-// bilinear fetch (GL LINEAR in x and y, CLAMP_TO_BORDER) returns both slices around a sample's z; the z
-// interpolation runs in FP32 with the sample's own fraction; slices outside the level are 0, as the border.
-// The 27 fetches do not depend on each other. The features feed a BF16 network, so the texture filter's
-// 8-bit weight fractions sit below the features' own rounding; training pairs are extracted by the same
-// code.
-__device__ __forceinline__ void stencil27(unsigned long long tex, const float inv[3], int nz, float ux, float uy,
-                                          float uz, float v[MLP_STENCIL]) {
-    float px[3], py[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        px[k] = fmaf(1.5f * (float) (k - 1), inv[0], ux);
-        py[k] = fmaf(1.5f * (float) (k - 1), inv[1], uy);
-    }
-#pragma unroll
-    for (int kz = 0; kz < 3; ++kz) {
-        // texel-space z of the sample minus the half texel: slices z0 and z0 + 1 live in layer z0 + 1
-        const float zs = fmaf(uz, (float) nz, 1.5f * (float) (kz - 1) - 0.5f);
-        const float z0f = floorf(zs);
-        const float fz = zs - z0f;
-        const int layer = (int) z0f + 1;
-        const bool in = layer >= 0 && layer <= nz;
-#pragma unroll
-        for (int ky = 0; ky < 3; ++ky)
-#pragma unroll
-            for (int kx = 0; kx < 3; ++kx) {
-                float2 t = make_float2(0.0f, 0.0f);
-                if (in)
-                    t = tex2DLayered<float2>((cudaTextureObject_t) tex, px[kx], py[ky], layer);
-                v[kz * 9 + ky * 3 + kx] = t.x + fz * (t.y - t.x);
-            }
-    }
+// GL LINEAR sample of one mip level at normalised point q through its paired-slice texture: one bilinear
+// fetch (CLAMP_TO_BORDER in x and y) returns slices z0 and z0 + 1 around the sample's z (layer z0 + 1), and
+// the z interpolation runs in FP32 with the sample's own fraction; layers outside the level are 0, as the
+// border. The texels are 8-bit UNORM (the MDAO volume's own R8 format) and the texture units weight x and y
+// with 8-bit fractions: the features feed a BF16 network and training pairs are extracted by the same code
+// (measured on the CPU: the same test RMSE as FP32 texels on the LJ, uniform and mixed-phase frames).
+__device__ __forceinline__ float feature_tex_sample(unsigned long long tex, int nz, float qx, float qy, float qz) {
+    const float zs = fmaf(qz, (float) nz, -0.5f);
+    const float z0f = floorf(zs);
+    const float fz = zs - z0f;
+    const int layer = (int) z0f + 1;
+    if (layer < 0 || layer > nz)
+        return 0.0f;
+    const float2 t = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, layer);
+    return fmaf(fz, t.y - t.x, t.x);
 }
 
-// Layer L of the paired texture = (slice L - 1, slice L) of level (dx, dy, dz), L in [0, dz].
-__global__ void __launch_bounds__(256) fill_stencil_tex_kernel(const float* __restrict__ src, int dx, int dy, int dz,
+// Feature sample j of a cone with direction dir from normalised point u: the march's step fstep[j] at its
+// own lod, blended linearly between the two levels around it (the branch depends on j only, so it is uniform
+// across the warp).
+__device__ __forceinline__ float feature_sample(const ConeParams& cp, const float dir[3], const float u[3], int j) {
+    const int k = cp.fstep[j];
+    const float t = cp.t[k], lod = cp.lod[k];
+    const float qx = fmaf(t, dir[0], u[0]), qy = fmaf(t, dir[1], u[1]), qz = fmaf(t, dir[2], u[2]);
+    const int l0 = min((int) lod, cp.nlevels - 1);
+    const float fr = lod - (float) l0;
+    float v = feature_tex_sample(cp.ftex[l0], cp.lv[l0].d[2], qx, qy, qz);
+    if (fr > 0.0f && l0 + 1 < cp.nlevels)
+        v = fmaf(fr, feature_tex_sample(cp.ftex[l0 + 1], cp.lv[l0 + 1].d[2], qx, qy, qz) - v, v);
+    return v;
+}
+
+// The MLP_FSTEPS features of cone c, written to v[0 .. MLP_FSTEPS).
+__device__ __forceinline__ void cone_features(const ConeParams& cp, int c, const float u[3], const float nn[3],
+                                              const float ex[3], const float ez[3], float* v) {
+    float dir[3];
+    cone_dir(cp, c, ex, nn, ez, dir);
+#pragma unroll
+    for (int j = 0; j < MLP_FSTEPS; ++j)
+        v[j] = feature_sample(cp, dir, u, j);
+}
+
+// Surface point in normalised volume coordinates, unit normal and cone frame of a particle (the plain march's
+// own, cone_device.cuh); false for an invalid particle (non-finite position, radius <= 0) or a zero normal.
+__device__ __forceinline__ bool particle_frame(const ConeParams& cp, const float4 p, const float4 nv, float u[3],
+                                               float nn[3], float ex[3], float ez[3]) {
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f))
+        return false;
+    float x[3];
+    if (!surface_point(p, nv, x, nn))
+        return false;
+    cone_frame(cp, x, nn, u, ex, ez);
+    return true;
+}
+
+// Layer L of the paired texture = (slice L - 1, slice L) of level (dx, dy, dz), L in [0, dz], as 8-bit UNORM of
+// the texel clamped to [0, 1] (level-0 saturation clamp(v * sat, 0, 1) applied first when sat > 0).
+__global__ void __launch_bounds__(256) fill_feature_tex_kernel(const float* __restrict__ src, int dx, int dy, int dz,
                                                                float sat, unsigned long long surf) {
     const int64_t n = (int64_t) dx * dy * (dz + 1);
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
         const int x = (int) (i % dx), y = (int) ((i / dx) % dy), L = (int) (i / ((int64_t) dx * dy));
-        float v[2];
+        unsigned char q[2];
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
             const int z = L - 1 + c;
-            v[c] = 0.0f;
+            float v = 0.0f;
             if (z >= 0 && z < dz) {
-                v[c] = src[((int64_t) z * dy + y) * dx + x];
+                v = src[((int64_t) z * dy + y) * dx + x];
                 if (sat > 0.0f)
-                    v[c] = fminf(fmaxf(v[c] * sat, 0.0f), 1.0f);
+                    v = v * sat;
             }
+            q[c] = (unsigned char) __float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f);
         }
-        const __half2 h = __floats2half2_rn(v[0], v[1]);
-        surf2DLayeredwrite(*reinterpret_cast<const unsigned int*>(&h), (cudaSurfaceObject_t) surf,
-                           x * (int) sizeof(__half2), y, L);
+        surf2DLayeredwrite(make_uchar2(q[0], q[1]), (cudaSurfaceObject_t) surf, x * (int) sizeof(uchar2), y, L);
     }
 }
 
-// Surface point (normalised volume coordinates) and unit normal; false for a zero normal.
-__device__ __forceinline__ bool mlp_point(const ConeParams& cp, const float4 p, const float4 nv, float u[3], float n[3]) {
-    const float l2 = nv.x * nv.x + nv.y * nv.y + nv.z * nv.z;
-    if (!(l2 > 0.0f))
-        return false;
-    const float il = rsqrtf(l2);
-    n[0] = nv.x * il;
-    n[1] = nv.y * il;
-    n[2] = nv.z * il;
-    const float pc[3] = {p.x, p.y, p.z};
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        u[a] = (pc[a] + p.w * n[a] - cp.bmin[a]) * cp.ibsize[a];
-    return true;
-}
-
 // ---------------------------------------------------------------------------------------------
-// training pairs: features of selected particles (sorted positions `sel`) and their cone-march AO
+// training pairs: features of selected particles (sorted positions `sel`, read from the sorted copies of the
+// positions and normals) and their cone-march AO (input order)
 // ---------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) mlp_collect_kernel(const ConeParams cp, const uint32_t* __restrict__ order,
     const uint32_t* __restrict__ sel, uint32_t nsel, const float4* __restrict__ xyzr, const float4* __restrict__ nrm,
@@ -131,28 +138,26 @@ __global__ void __launch_bounds__(128) mlp_collect_kernel(const ConeParams cp, c
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsel)
         return;
-    const uint32_t o = order[sel[i]];
-    float u[3], n[3];
-    const float4 p = xyzr[o];
-    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f) || !mlp_point(cp, p, nrm[o], u, n)) {
+    const uint32_t js = sel[i];  // sorted position: positions and normals are read in sorted order
+    float u[3], nn[3], ex[3], ez[3];
+    if (!particle_frame(cp, xyzr[js], nrm[js], u, nn, ex, ez)) {
         T[i] = -1.0f;  // marks a pair without features; compacted away on the host side
         return;
     }
     float* x = X + (size_t) i * MLP_IN;
-    float v[MLP_STENCIL];
+    for (int c = 0; c < MLP_CONES; ++c) {
+        float v[MLP_FSTEPS];
+        cone_features(cp, c, u, nn, ex, ez, v);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        stencil27(cp.stex[h], cp.sinv[h], cp.lv[cp.stencil_level + h].d[2], u[0], u[1], u[2], v);
-        for (int k = 0; k < MLP_STENCIL; ++k)
-            x[MLP_STENCIL * h + k] = v[k];
+        for (int j = 0; j < MLP_FSTEPS; ++j)
+            x[c * MLP_FSTEPS + j] = v[j];
     }
-    x[54] = n[0];
-    x[55] = n[1];
-    x[56] = n[2];
-    x[57] = u[0];
-    x[58] = u[1];
-    x[59] = u[2];
-    T[i] = ao[o];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        x[MLP_SAMPLES + a] = nn[a];
+        x[MLP_SAMPLES + 3 + a] = u[a];
+    }
+    T[i] = ao[order[js]];
     atomicAdd(kept, 1u);
 }
 
@@ -369,7 +374,7 @@ __global__ void __launch_bounds__(256) mlp_range_kernel(const float* __restrict_
 }
 
 // ---------------------------------------------------------------------------------------------
-// inference weights: BF16 copies of W1 (its columns at the K positions of mlp_kpos, zeros between) and W2
+// inference weights: BF16 copies of W1 (feature i at K position i, zeros in the padding) and W2
 // ---------------------------------------------------------------------------------------------
 __global__ void mlp_pack_kernel(const float* __restrict__ P, __nv_bfloat16* __restrict__ w1h,
     __nv_bfloat16* __restrict__ w2h) {
@@ -389,9 +394,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 
 // ---------------------------------------------------------------------------------------------
 // Inference on the 5th-generation tensor cores (tcgen05). One CTA of 256 threads takes 128 particles per
-// tile. Threads t and t + 128 extract the two stencil levels of particle t straight into the A tile (BF16,
-// canonical no-swizzle K-major layout in shared memory; each thread's features fill whole 16-byte chunks, see
-// mlp_kpos); one thread issues the layer-1 MMAs (M = 128, N = 64, K = 80) into 64 TMEM columns and commits
+// tile. Threads t and t + 128 extract the cone samples of particle t (cones 0-3 and 4-7) straight into the A
+// tile (BF16, canonical no-swizzle K-major layout in shared memory, feature i at K position i); one thread
+// issues the layer-1 MMAs (M = 128, N = 64, K = 80) into 64 TMEM columns and commits
 // them to an mbarrier. The epilogue reads TMEM
 // (warp w: lanes 32 (w % 4).., columns 32 (w / 4)..), adds the bias, applies SiLU and writes the hidden
 // layer back into the A tile as layer 2's A operand; layer 2 (K = 64) reuses the TMEM columns, and its
@@ -498,6 +503,10 @@ __device__ __forceinline__ void st_shared_v4(uint8_t* p, uint32_t a, uint32_t b,
     *reinterpret_cast<uint4*>(p) = make_uint4(a, b, c, d);
 }
 
+__device__ __forceinline__ void st_shared_v2(uint8_t* p, uint32_t a, uint32_t b) {
+    *reinterpret_cast<uint2*>(p) = make_uint2(a, b);
+}
+
 template<bool FEATURES_IN>
 __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
@@ -592,44 +601,54 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
                 st_shared_v4(sA + canon_off(row, k0, tc::SBO1), pk[0], pk[1], pk[2], pk[3]);
             }
         } else {
-            float u[3] = {0, 0, 0}, nn[3] = {0, 0, 0};
+            float u[3] = {0, 0, 0}, nn[3] = {0, 0, 0}, ex[3], ez[3];
             if (valid) {
                 o = args.order ? args.order[pi] : pi;
-                const float4 p = args.xyzr[o];
-                valid = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w > 0.0f &&
-                        mlp_point(cp, p, args.nrm[o], u, nn);
+                valid = particle_frame(cp, args.xyzr[o], args.nrm[o], u, nn, ex, ez);
             }
-            // K 64..79 first (the normal and the position are then no longer needed): the normal, the
-            // position and zero padding (chunk 8 on half 0, chunk 9 on half 1)
+            // this half's cones 4 h .. 4 h + 3 = features 36 h .. 36 h + 35 (K positions equal feature indices)
+            constexpr int HALF_F = MLP_SAMPLES / 2;  // 36
+            float fv[HALF_F];
+#pragma unroll
+            for (int cc = 0; cc < MLP_CONES / 2; ++cc) {
+                if (valid)
+                    cone_features(cp, (MLP_CONES / 2) * half + cc, u, nn, ex, ez, fv + cc * MLP_FSTEPS);
+                else
+#pragma unroll
+                    for (int j = 0; j < MLP_FSTEPS; ++j)
+                        fv[cc * MLP_FSTEPS + j] = 0.0f;
+            }
+            uint32_t pk[HALF_F / 2];
+#pragma unroll
+            for (int e = 0; e < HALF_F / 2; ++e) {
+                const __nv_bfloat162 v2 = __floats2bfloat162_rn(fv[2 * e], fv[2 * e + 1]);
+                if (check && valid)
+                    oor |= !in_range((HALF_F / 2) * half + e, v2);
+                pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
+            }
             if (half == 0) {
+                // K 0..31 (chunks 0..3) and K 32..35 (the first half of chunk 4)
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    st_shared_v4(sA + canon_off(row, 8 * c, tc::SBO1), pk[4 * c], pk[4 * c + 1], pk[4 * c + 2],
+                                 pk[4 * c + 3]);
+                st_shared_v2(sA + canon_off(row, 32, tc::SBO1), pk[16], pk[17]);
+            } else {
+                // K 36..39 (the second half of chunk 4), K 40..71 (chunks 5..8), then chunk 9: the normal, the
+                // surface point and two zeros (K 72..79)
+                st_shared_v2(sA + canon_off(row, 36, tc::SBO1), pk[0], pk[1]);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    st_shared_v4(sA + canon_off(row, 40 + 8 * c, tc::SBO1), pk[2 + 4 * c], pk[3 + 4 * c],
+                                 pk[4 + 4 * c], pk[5 + 4 * c]);
                 const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
                 const __nv_bfloat162 n2u0 = __floats2bfloat162_rn(nn[2], u[0]);
                 const __nv_bfloat162 u12 = __floats2bfloat162_rn(u[1], u[2]);
-                st_shared_v4(sA + canon_off(row, 64, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
+                st_shared_v4(sA + canon_off(row, MLP_SAMPLES, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
                              *reinterpret_cast<const uint32_t*>(&n2u0), *reinterpret_cast<const uint32_t*>(&u12), 0u);
                 if (valid && check)
-                    oor |= !(in_range(32, n01) && in_range(33, n2u0) && in_range(34, u12));
-            } else {
-                st_shared_v4(sA + canon_off(row, 72, tc::SBO1), 0u, 0u, 0u, 0u);
-            }
-            // this half's stencil level: K 32 h .. 32 h + 26, padded with zeros to 32 h + 31 (chunks 4 h .. 4 h + 3)
-            float sv[MLP_STENCIL];
-            if (valid)
-                stencil27(cp.stex[half], cp.sinv[half], cp.lv[cp.stencil_level + half].d[2], u[0], u[1], u[2], sv);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                uint32_t pk[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int j = 8 * c + 2 * e;
-                    const float a = (valid && j < MLP_STENCIL) ? sv[j] : 0.0f;
-                    const float b = (valid && j + 1 < MLP_STENCIL) ? sv[j + 1] : 0.0f;
-                    const __nv_bfloat162 v2 = __floats2bfloat162_rn(a, b);
-                    if (check && valid)
-                        oor |= !in_range(16 * half + 4 * c + e, v2);
-                    pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
-                }
-                st_shared_v4(sA + canon_off(row, 32 * half + 8 * c, tc::SBO1), pk[0], pk[1], pk[2], pk[3]);
+                    oor |= !(in_range(MLP_SAMPLES / 2, n01) && in_range(MLP_SAMPLES / 2 + 1, n2u0) &&
+                             in_range(MLP_SAMPLES / 2 + 2, u12));
             }
             oor = oor && valid;
         }
@@ -697,14 +716,15 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
         if (half == 0 && pi < args.n) {
             const float y = sigmoidf_(z + s_part[row] + b3);
             const uint32_t oo = FEATURES_IN ? pi : o;
+            const uint32_t wo = (!FEATURES_IN && args.out_order) ? args.out_order[oo] : oo;
             if (!FEATURES_IN && !valid) {
-                args.y[oo] = 1.0f;  // no normal / invalid particle: unoccluded, as the cone march
+                args.y[wo] = 1.0f;  // no normal / invalid particle: unoccluded, as the cone march
             } else if (oor && args.fallback) {
                 args.fallback[atomicAdd(args.nfallback, 1u)] = oo;
                 if (FEATURES_IN)
-                    args.y[oo] = y;
+                    args.y[wo] = y;
             } else {
-                args.y[oo] = y;
+                args.y[wo] = y;
             }
         }
     }
@@ -729,11 +749,11 @@ size_t mlp_train_smem_bytes() {
     return sizeof(float) * (MLP_H * MLP_IN + MLP_H * MLP_H + TS * MLP_IN + 6 * TS * MLP_H + TS);
 }
 
-cudaError_t StencilTex::ensure(const int dims[3]) {
+cudaError_t FeatureTex::ensure(const int dims[3]) {
     if (arr && d[0] == dims[0] && d[1] == dims[1] && d[2] == dims[2])
         return cudaSuccess;
     release();
-    cudaChannelFormatDesc fmt = cudaCreateChannelDescHalf2();
+    cudaChannelFormatDesc fmt = cudaCreateChannelDesc<uchar2>();
     // dims[2] + 1 layers of slice pairs (slice L - 1, slice L)
     cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2] + 1),
                                       cudaArrayLayered | cudaArraySurfaceLoadStore);
@@ -748,7 +768,7 @@ cudaError_t StencilTex::ensure(const int dims[3]) {
     for (int a = 0; a < 3; ++a)
         td.addressMode[a] = cudaAddressModeBorder;  // CLAMP_TO_BORDER with border colour 0
     td.filterMode = cudaFilterModeLinear;
-    td.readMode = cudaReadModeElementType;
+    td.readMode = cudaReadModeNormalizedFloat;  // 8-bit UNORM texels read as floats in [0, 1]
     td.normalizedCoords = 1;
     cudaTextureObject_t to = 0;
     cudaSurfaceObject_t so = 0;
@@ -767,7 +787,7 @@ cudaError_t StencilTex::ensure(const int dims[3]) {
     return cudaSuccess;
 }
 
-void StencilTex::release() {
+void FeatureTex::release() {
     if (tex)
         cudaDestroyTextureObject((cudaTextureObject_t) tex);
     if (surf)
@@ -779,10 +799,10 @@ void StencilTex::release() {
     d[0] = d[1] = d[2] = 0;
 }
 
-cudaError_t launch_fill_stencil_tex(const ConeLevel& L, float sat, const StencilTex& t, cudaStream_t st) {
+cudaError_t launch_fill_feature_tex(const ConeLevel& L, float sat, const FeatureTex& t, cudaStream_t st) {
     const int64_t n = (int64_t) L.d[0] * L.d[1] * (L.d[2] + 1);
     const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
-    fill_stencil_tex_kernel<<<grd, 256, 0, st>>>(L.v, L.d[0], L.d[1], L.d[2], sat, t.surf);
+    fill_feature_tex_kernel<<<grd, 256, 0, st>>>(L.v, L.d[0], L.d[1], L.d[2], sat, t.surf);
     return cudaGetLastError();
 }
 

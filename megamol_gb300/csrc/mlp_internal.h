@@ -10,17 +10,17 @@
 
 namespace p2v {
 
-constexpr int MLP_STENCIL = 27;                // 3x3x3 samples per stencil level
-constexpr int MLP_IN = 2 * MLP_STENCIL + 6;    // 60: two stencil levels, 3 normal and 3 position components
-// The tensor-core tile keeps each group of features in whole 16-byte chunks: level s at K 0..26, level s + 1
-// at K 32..58, normal and position at K 64..69, zeros elsewhere (MLP_KP = 80, five MMAs of K = 16).
+// Features: the cone march's own samples, for each of MLP_CONES cones at MLP_FSTEPS of its steps (cone-major:
+// feature c * MLP_FSTEPS + j), then the unit normal and the surface point in normalised volume coordinates.
+constexpr int MLP_CONES = 8;
+constexpr int MLP_FSTEPS = 9;
+constexpr int MLP_SAMPLES = MLP_CONES * MLP_FSTEPS;   // 72
+constexpr int MLP_IN = MLP_SAMPLES + 6;               // 78
+static_assert(MLP_FSTEPS <= MAX_FSTEPS, "feature step table too small");
+// The tensor-core tile holds feature i at K position i; K 78, 79 are zero (MLP_KP = 80, five MMAs of K = 16).
 constexpr int MLP_KP = 80;
-// K position of logical feature i, and the logical feature at K position k (-1: padding)
-__host__ __device__ constexpr int mlp_kpos(int i) {
-    return i < 27 ? i : (i < 54 ? i + 5 : i + 10);
-}
 __host__ __device__ constexpr int mlp_feature_at(int k) {
-    return k < 27 ? k : (k < 32 ? -1 : (k < 59 ? k - 5 : (k < 64 ? -1 : (k < 70 ? k - 10 : -1))));
+    return k < MLP_IN ? k : -1;
 }
 constexpr int MLP_H = 64;
 // parameter vector: W1[H][IN], b1[H], W2[H][H], b2[H], w3[H], b3
@@ -46,15 +46,17 @@ struct MlpInferArgs {
     // given features (tests)
     const float* X;
     float* y;                       // output, indexed by particle (or by row for given features)
+    const uint32_t* out_order;      // nullable: particle j's output goes to y[out_order[j]] (sorted in, input order out)
     uint32_t* fallback;             // particle indices whose features left the training range (nullable)
     uint32_t* nfallback;
     uint32_t* err;                  // ERR_* bits (the tensor-core kernel's bounded waits)
 };
 
-// One mip level of the AO volume as an FP16 layered 2D texture, one layer per z slice (CLAMP_TO_BORDER,
-// linear filtering in x and y, normalised coordinates), written through a surface. The learned AO's
-// stencil samples it with the texture units.
-struct StencilTex {
+// One mip level of the AO volume as an 8-bit UNORM layered 2D texture of slice pairs: layer L holds z slices
+// L - 1 (red) and L (green), so one bilinear fetch (GL LINEAR in x and y, CLAMP_TO_BORDER, normalised
+// coordinates) returns both slices around a sample's z. Written through a surface; the learned AO's features
+// sample it with the texture units.
+struct FeatureTex {
     cudaArray_t arr = nullptr;
     unsigned long long tex = 0;   // cudaTextureObject_t
     unsigned long long surf = 0;  // cudaSurfaceObject_t
@@ -63,9 +65,10 @@ struct StencilTex {
     void release();
 };
 // copy level L (level-0 saturation `sat` applied when > 0) into the texture
-cudaError_t launch_fill_stencil_tex(const ConeLevel& L, float sat, const StencilTex& t, cudaStream_t st);
+cudaError_t launch_fill_feature_tex(const ConeLevel& L, float sat, const FeatureTex& t, cudaStream_t st);
 
 size_t mlp_train_smem_bytes();
+// xyzr, nrm in sorted order (sel holds sorted positions), ao in input order (order: sorted position -> index)
 cudaError_t launch_mlp_collect(const ConeParams& cp, const uint32_t* order, const uint32_t* sel, uint32_t nsel,
     const float4* xyzr, const float4* nrm, const float* ao, float* X, float* T, uint32_t* kept, cudaStream_t st);
 cudaError_t launch_mlp_train_step(const float* P, const float* X, const float* T, const uint32_t* idx, int nbatch,

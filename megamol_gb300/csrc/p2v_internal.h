@@ -21,6 +21,9 @@ struct ListDesc {
     uint64_t offset;       // index of the list's first record in the frame arrays
 };
 
+// The counting sort by cell is taken while its count table stays at most this large (near L2-resident).
+constexpr uint64_t COUNTING_TABLE_MAX_BYTES = 128ull << 20;
+
 struct SortBuffers {
     uint32_t* keys[2];
     uint32_t* vals[2];
@@ -30,6 +33,7 @@ struct SortBuffers {
     const float4* xyzr_in; // when non-null the last pass writes every particle's gather record
     float4* rec_a;         // (particle_record.cuh) in sorted order, interleaved: rec_b = rec_a + 1, both
     int4* rec_b;           // indexed with REC_STRIDE * position
+    float4* xyzr_out;      // nullable: with xyzr_in, the particles' xyzr in sorted order as well (the AO stages)
     GridGeo geo;
     int result;            // index of the buffers holding the sorted output
     bool implicit_vals0;   // vals[0] holds no input values: the first pass takes the identity (indices)

@@ -126,7 +126,7 @@ class TrainReport(C.Structure):
                 ("final_loss", C.c_float), ("val_rmse", C.c_float), ("val_max_err", C.c_float), ("ms", C.c_double)]
 
 
-MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 60, 64, 8129
+MLP_CONES, MLP_FSTEPS, MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 8, 9, 78, 64, 9281
 
 # Every entry point include/p2v.h declares, with its ctypes signature.
 _SIGNATURES = {
@@ -512,7 +512,7 @@ class Context:
         return keys, order, start
 
     def mlp_pairs(self):
-        """(features (n, 60), targets (n,)) of the collected training pairs, in collection order."""
+        """(features (n, MLP_INPUTS), targets (n,)) of the collected training pairs, in collection order."""
         n = C.c_uint64()
         self._check(self.lib.p2v_mlp_get_pairs(self.h, None, None, 0, C.byref(n)))
         x = np.empty((n.value, MLP_INPUTS), np.float32)

@@ -72,6 +72,12 @@ def lib() -> C.CDLL:
         f.p2vo_cone_steps.restype = C.c_int
         f.p2vo_cone_ao_f64.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_int32), C.c_int, C.c_void_p, C.c_int,
                                        C.POINTER(_ConeParams), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        f.p2vo_mip_levels_f32.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_float, C.c_int,
+                                          C.POINTER(C.c_void_p), C.c_int]
+        f.p2vo_cone_ao_f32.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_int32), C.c_int, C.c_void_p, C.c_int,
+                                       C.POINTER(_ConeParams), C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
+        f.p2vo_aosphere_volume_ex_f64.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
+                                                  C.c_float, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_void_p]
         f.p2vo_aosphere_volume_f64.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
                                                C.c_float, C.c_void_p]
         f.p2vo_aosphere_ao_f64.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_float,
@@ -522,12 +528,48 @@ def cone_ao_f64(levels, dirs, xyzr, normals, bounds_min, bounds_size, **kw) -> n
     return out
 
 
-def aosphere_volume_f64(xyzr, clip, s, gen_fac=1.0) -> np.ndarray:
+def mip_levels_f32(l0: np.ndarray, nlevels: int, sat_scale: float = 0.0, nthreads: int = 1):
+    """Levels 0..nlevels-1 of the MDAO pyramid in FP32 with OpenMP (level 0 returned as given; level 1 built
+    from clamp(v * sat_scale, 0, 1) when sat_scale > 0). Arrays (z, y, x) float32."""
+    src = np.ascontiguousarray(l0, np.float32)
+    d = list(src.shape[::-1])
+    outs = []
+    for _ in range(1, nlevels):
+        d = [max(1, v // 2) for v in d]
+        outs.append(np.empty(d[::-1], np.float32))
+    ptrs = (C.c_void_p * max(1, len(outs)))(*[o.ctypes.data for o in outs])
+    d0 = (C.c_int32 * 3)(*src.shape[::-1])
+    lib().p2vo_mip_levels_f32(src.ctypes.data, d0, float(sat_scale), int(nlevels), ptrs, int(nthreads))
+    return [src] + outs
+
+
+def cone_ao_f32(levels, dirs, xyzr, normals, bounds_min, bounds_size, nthreads: int = 1, **kw) -> np.ndarray:
+    """Cone-marched AO per particle in FP32 with OpenMP, the GPU kernel's operation order (the CPU baseline's
+    timing stand-in; the error judge is cone_ao_f64). `levels` as mip_levels_f32 returns them."""
+    lv = [np.ascontiguousarray(L, np.float32) for L in levels]
+    ptrs = (C.c_void_p * len(lv))(*[L.ctypes.data for L in lv])
+    dims = (C.c_int32 * (3 * len(lv)))(*[d for L in lv for d in (L.shape[2], L.shape[1], L.shape[0])])
+    d = np.ascontiguousarray(dirs, np.float32)
+    x = _xyzr(xyzr)
+    nrm = np.ascontiguousarray(normals, np.float32)
+    out = np.zeros(x.shape[0], np.float32)
+    cp = _cone_params(bounds_min, bounds_size, **kw)
+    lib().p2vo_cone_ao_f32(ptrs, dims, len(lv), d.ctypes.data, d.shape[0], C.byref(cp), x.ctypes.data,
+                           nrm.ctypes.data, x.shape[0], int(nthreads), out.ctypes.data)
+    return out
+
+
+def aosphere_volume_f64(xyzr, clip, s, gen_fac=1.0, glsl_rule=0, clip_plane=None) -> np.ndarray:
+    """AOSphere volume (FP64 sums; voxel decisions in float as the reference): the CPU rule of createVolumeCPU
+    (with the clip-plane discard when clip_plane = (nx, ny, nz, d) is given) or the GLSL rule of
+    createVolumeGLSL (glsl_rule=1)."""
     x = _xyzr(xyzr)
     tex = np.zeros((s[2], s[1], s[0]), np.float64)
     cl = (C.c_float * 6)(*[float(v) for v in clip])
     ss = (C.c_int32 * 3)(*[int(v) for v in s])
-    lib().p2vo_aosphere_volume_f64(x.ctypes.data, x.shape[0], cl, ss, float(gen_fac), tex.ctypes.data)
+    pl = (C.c_float * 4)(*([float(v) for v in clip_plane] if clip_plane is not None else [0.0] * 4))
+    lib().p2vo_aosphere_volume_ex_f64(x.ctypes.data, x.shape[0], cl, ss, float(gen_fac), int(glsl_rule),
+                                      int(clip_plane is not None), pl, tex.ctypes.data)
     return tex
 
 
@@ -543,7 +585,61 @@ def aosphere_ao_f64(tex, clip, xyzr, normals, mode=0, step_len=0.5, eval_fac=1.0
     return out
 
 
-MLP_IN, MLP_HIDDEN = 60, 64
+MLP_IN, MLP_HIDDEN = 78, 64
+MLP_CONES, MLP_FSTEPS = 8, 9
+
+
+def mlp_feature_steps(nsteps: int, fsteps: int = MLP_FSTEPS) -> list[int]:
+    """March steps the learned AO's features sample: step round(j (nsteps - 1) / (fsteps - 1)) for feature j."""
+    return [int(np.floor(j * (nsteps - 1) / (fsteps - 1) + 0.5)) for j in range(fsteps)]
+
+
+def _linear_border(T, q):
+    """GL LINEAR sample (texel centres (i + 0.5) / N, CLAMP_TO_BORDER with 0) of texels T (z, y, x) at
+    normalised points q (n, 3), FP64."""
+    dz, dy, dx = T.shape
+    c = q * np.array([dx, dy, dz], np.float64) - 0.5
+    i0 = np.floor(c).astype(np.int64)
+    f = c - i0
+    out = np.zeros(q.shape[0], np.float64)
+    for oz in (0, 1):
+        for oy in (0, 1):
+            for ox in (0, 1):
+                ix, iy, iz = i0[:, 0] + ox, i0[:, 1] + oy, i0[:, 2] + oz
+                ok = (ix >= 0) & (ix < dx) & (iy >= 0) & (iy < dy) & (iz >= 0) & (iz < dz)
+                v = np.where(ok, T[np.clip(iz, 0, dz - 1), np.clip(iy, 0, dy - 1), np.clip(ix, 0, dx - 1)], 0.0)
+                out += v * (f[:, 0] if ox else 1 - f[:, 0]) * (f[:, 1] if oy else 1 - f[:, 1]) * \
+                    (f[:, 2] if oz else 1 - f[:, 2])
+    return out
+
+
+def cone_features_f64(levels, dirs, t, lod, xyzr, normals, bounds_min, inv_size) -> np.ndarray:
+    """The learned AO's input features, FP64: for each cone (dirs, around +Y), in the MDAO cone frame of the
+    surface point x = p + r n (mdao_deferred_fragment_ambocc.inc.glsl:18-21: y = n, x = cross(n, normalize(x)),
+    z = cross(x, y)), the texels `levels` (z, y, x; as the sampler sees them, level 0 already saturated) at the
+    feature steps of the step table (t, lod), LINEAR within and between the two levels around each lod; then
+    the unit normal and x in normalised volume coordinates. Returns (n, cones * MLP_FSTEPS + 6)."""
+    p = np.asarray(xyzr, np.float64).reshape(-1, 4)
+    n = np.asarray(normals, np.float64).reshape(-1, 3)
+    n = n / np.linalg.norm(n, axis=1, keepdims=True)
+    x = p[:, :3] + p[:, 3:4] * n
+    u = (x - np.asarray(bounds_min, np.float64)) * np.asarray(inv_size, np.float64)
+    xn = x / np.linalg.norm(x, axis=1, keepdims=True)
+    ex = np.cross(n, xn)
+    ez = np.cross(ex, n)
+    L = len(levels)
+    cols = []
+    for d in np.asarray(dirs, np.float64):
+        dv = ex * d[0] + n * d[1] + ez * d[2]
+        for k in mlp_feature_steps(len(t)):
+            q = u + float(t[k]) * dv
+            l0 = min(int(lod[k]), L - 1)
+            fr = float(lod[k]) - l0
+            v = _linear_border(levels[l0], q)
+            if fr > 0 and l0 + 1 < L:
+                v = (1 - fr) * v + fr * _linear_border(levels[l0 + 1], q)
+            cols.append(v)
+    return np.column_stack(cols + [n, u])
 MLP_NPARAM = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
 
 

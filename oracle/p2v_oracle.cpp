@@ -492,9 +492,154 @@ extern "C" void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldi
     }
 }
 
-extern "C" void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3],
-    float gen_fac, double* tex) {
-    // AOSphereRenderer.cpp:918-1021: inner grid s-2, cell decisions in float as the reference
+/* ------------------------------------------------------------------------------------------------
+ * FP32 cone pipeline (the CPU baseline's timing stand-in for the GLSL march, OpenMP): the MDAO pyramid
+ * of a float volume (level 1 built from the saturated texels clamp(v * scale, 0, 1)) and the march in
+ * FP32 with the GPU kernel's operation order (fused multiply-adds where it fuses, level 0 saturated on
+ * the fly). The error judge stays the FP64 march above.
+ * ---------------------------------------------------------------------------------------------- */
+extern "C" void p2vo_mip_levels_f32(const float* l0, const int32_t d0[3], float sat_scale, int nlevels,
+                                    float* const* out, int nthreads) {
+    int sd[3] = {d0[0], d0[1], d0[2]};
+    const float* src = l0;
+    for (int l = 1; l < nlevels; ++l) {
+        const int dd[3] = {std::max(1, sd[0] / 2), std::max(1, sd[1] / 2), std::max(1, sd[2] / 2)};
+        float* dst = out[l - 1];
+        const bool sat = l == 1 && sat_scale > 0.0f;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+        for (int z = 0; z < dd[2]; ++z)
+            for (int y = 0; y < dd[1]; ++y)
+                for (int x = 0; x < dd[0]; ++x) {
+                    float acc = 0.0f;
+                    const int x1 = std::min(2 * x + 1, sd[0] - 1), y1 = std::min(2 * y + 1, sd[1] - 1),
+                              z1 = std::min(2 * z + 1, sd[2] - 1);
+                    for (int zz = 2 * z; zz <= z1; ++zz)
+                        for (int yy = 2 * y; yy <= y1; ++yy)
+                            for (int xx = 2 * x; xx <= x1; ++xx) {
+                                float v = src[xx + (yy + int64_t(zz) * sd[1]) * sd[0]];
+                                if (sat)
+                                    v = std::min(std::max(v * sat_scale, 0.0f), 1.0f);
+                                acc += v;
+                            }
+                    dst[x + (y + int64_t(z) * dd[1]) * dd[0]] = acc * 0.125f;
+                }
+        src = dst;
+        for (int a = 0; a < 3; ++a)
+            sd[a] = dd[a];
+    }
+}
+
+namespace {
+
+struct VolF {
+    const float* v;
+    int d[3];
+    float fd[3];
+};
+
+inline float fetch_f32(const VolF& L, int x, int y, int z, float sat) {
+    if (x < 0 || y < 0 || z < 0 || x >= L.d[0] || y >= L.d[1] || z >= L.d[2])
+        return 0.0f;  // CLAMP_TO_BORDER
+    const float v = L.v[x + (y + int64_t(z) * L.d[1]) * L.d[0]];
+    return sat > 0.0f ? std::min(std::max(v * sat, 0.0f), 1.0f) : v;
+}
+
+inline float lerp_f32(float a, float b, float w) {
+    return std::fma(w, b - a, a);
+}
+
+inline float trilinear_f32(const VolF& L, float ux, float uy, float uz, float sat) {
+    const float cx = std::fma(ux, L.fd[0], -0.5f), cy = std::fma(uy, L.fd[1], -0.5f), cz = std::fma(uz, L.fd[2], -0.5f);
+    const float fx0 = std::floor(cx), fy0 = std::floor(cy), fz0 = std::floor(cz);
+    const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
+    const float fx = cx - fx0, fy = cy - fy0, fz = cz - fz0;
+    const float c00 = lerp_f32(fetch_f32(L, x0, y0, z0, sat), fetch_f32(L, x0 + 1, y0, z0, sat), fx);
+    const float c10 = lerp_f32(fetch_f32(L, x0, y0 + 1, z0, sat), fetch_f32(L, x0 + 1, y0 + 1, z0, sat), fx);
+    const float c01 = lerp_f32(fetch_f32(L, x0, y0, z0 + 1, sat), fetch_f32(L, x0 + 1, y0, z0 + 1, sat), fx);
+    const float c11 = lerp_f32(fetch_f32(L, x0, y0 + 1, z0 + 1, sat), fetch_f32(L, x0 + 1, y0 + 1, z0 + 1, sat), fx);
+    return lerp_f32(lerp_f32(c00, c10, fy), lerp_f32(c01, c11, fy), fz);
+}
+
+inline void cross_f32(const float a[3], const float b[3], float o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+}  // namespace
+
+extern "C" void p2vo_cone_ao_f32(const float* const* levels, const int32_t* ldims, int nlevels, const float* dirs,
+    int ncones, const p2vo_cone_params* cp, const float* xyzr, const float* nrm, int64_t n, int nthreads, float* ao) {
+    std::vector<VolF> L(nlevels);
+    for (int l = 0; l < nlevels; ++l) {
+        L[l].v = levels[l];
+        for (int a = 0; a < 3; ++a) {
+            L[l].d[a] = ldims[3 * l + a];
+            L[l].fd[a] = (float) ldims[3 * l + a];
+        }
+    }
+    std::vector<float> ts(256), lods(256);
+    const int ns = p2vo_cone_steps(cp, dirs[3], ts.data(), lods.data(), 256);
+    float bmin[3], ibs[3];
+    for (int a = 0; a < 3; ++a) {
+        bmin[a] = cp->bounds_min[a];
+        ibs[a] = (float) (1.0 / (double) cp->bounds_size[a]);
+    }
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) {
+        const float* p = xyzr + 4 * i;
+        const float* nv = nrm + 3 * i;
+        const float l2 = std::fma(nv[2], nv[2], std::fma(nv[1], nv[1], nv[0] * nv[0]));
+        if (!(l2 > 0.0f)) {
+            ao[i] = 1.0f;  // no normal: no occlusion
+            continue;
+        }
+        const float il = 1.0f / std::sqrt(l2);
+        const float nn[3] = {nv[0] * il, nv[1] * il, nv[2] * il};
+        const float x[3] = {std::fma(p[3], nn[0], p[0]), std::fma(p[3], nn[1], p[1]), std::fma(p[3], nn[2], p[2])};
+        float xn[3] = {x[0], x[1], x[2]};
+        const float xl2 = std::fma(xn[2], xn[2], std::fma(xn[1], xn[1], xn[0] * xn[0]));
+        if (xl2 > 0.0f) {
+            const float ixl = 1.0f / std::sqrt(xl2);
+            for (float& c : xn)
+                c *= ixl;
+        } else {
+            xn[0] = 1.0f;
+            xn[1] = xn[2] = 0.0f;
+        }
+        float ex[3], ez[3];
+        cross_f32(nn, xn, ex);
+        cross_f32(ex, nn, ez);
+        const float u[3] = {(x[0] - bmin[0]) * ibs[0], (x[1] - bmin[1]) * ibs[1], (x[2] - bmin[2]) * ibs[2]};
+        float ambient = 0.0f;
+        for (int c = 0; c < ncones; ++c) {
+            const float* cd = dirs + 4 * c;
+            float dir[3];
+            for (int a = 0; a < 3; ++a)
+                dir[a] = std::fma(ez[a], cd[2], std::fma(nn[a], cd[1], ex[a] * cd[0]));
+            float acc = 0.0f;
+            for (int k = 0; k < ns; ++k) {
+                const float t = ts[k], lod = lods[k];
+                const float qx = std::fma(t, dir[0], u[0]), qy = std::fma(t, dir[1], u[1]), qz = std::fma(t, dir[2], u[2]);
+                const int l0 = std::min((int) lod, nlevels - 1);
+                const float fr = lod - (float) l0;
+                float vis = trilinear_f32(L[l0], qx, qy, qz, l0 == 0 ? cp->sat_scale : 0.0f);
+                if (fr > 0.0f && l0 + 1 < nlevels)
+                    vis = std::fma(fr, trilinear_f32(L[l0 + 1], qx, qy, qz, 0.0f), (1.0f - fr) * vis);
+                acc = std::fma(1.0f - acc, vis, acc);
+                if (cp->early_exit && acc > 0.99f)
+                    break;
+            }
+            ambient += acc;
+        }
+        ao[i] = 1.0f - std::min(std::max(cp->strength * ambient / (float) ncones, 0.0f), 1.0f);
+    }
+}
+
+extern "C" void p2vo_aosphere_volume_ex_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3],
+    float gen_fac, int glsl_rule, int use_clip, const float plane[4], double* tex) {
+    // AOSphereRenderer.cpp:918-1021 (CPU rule) and :1026-1221 with volume_updateVolume.vert.glsl:22-46 (GLSL
+    // rule): inner grid s-2, every voxel decision in float as the reference makes it
     const int sx = s[0] - 2, sy = s[1] - 2, sz = s[2] - 2;
     const float minOS[3] = {clip[0], clip[1], clip[2]};
     const float rangeOS[3] = {std::fabs(clip[3] - clip[0]), std::fabs(clip[4] - clip[1]), std::fabs(clip[5] - clip[2])};
@@ -504,14 +649,35 @@ extern "C" void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const flo
     for (int64_t i = 0; i < n; ++i) {
         const float* p = xyzr + 4 * i;
         int c[3];
-        for (int a = 0; a < 3; ++a) {
-            int v = static_cast<int>(((p[a] - minOS[a]) / rangeOS[a]) * static_cast<float>(si[a]));
-            c[a] = v < 0 ? 0 : (v >= si[a] ? si[a] - 1 : v);
+        if (!glsl_rule) {
+            for (int a = 0; a < 3; ++a) {
+                int v = static_cast<int>(((p[a] - minOS[a]) / rangeOS[a]) * static_cast<float>(si[a]));
+                c[a] = (v < 0 ? 0 : (v >= si[a] ? si[a] - 1 : v)) + 1;
+            }
+            if (use_clip) {  // :982-991, vislib's Dot as a running float sum
+                float od = 0.0f;
+                for (int a = 0; a < 3; ++a)
+                    od += p[a] * plane[a];
+                if (od - plane[3] >= 0.0f)
+                    continue;
+            }
+        } else {
+            for (int a = 0; a < 2; ++a) {
+                const float q = std::floor(((p[a] - minOS[a]) / rangeOS[a]) * static_cast<float>(si[a]));
+                c[a] = (int) std::min(std::max(q, 0.0f), (float) si[a]);
+            }
+            int vz = static_cast<int>(((p[2] - minOS[2]) / rangeOS[2]) * static_cast<float>(sz));
+            c[2] = std::max(0, std::min(vz, sz - 1)) + 1;
         }
         const double r = p[3];
         const double spVol = 4.0 / 3.0 * 3.14159265358979323846 * r * r * r;
-        tex[(c[0] + 1) + ((c[1] + 1) + int64_t(c[2] + 1) * s[1]) * s[0]] += spVol / voxelVol * gen_fac;
+        tex[c[0] + (c[1] + int64_t(c[2]) * s[1]) * s[0]] += spVol / voxelVol * gen_fac;
     }
+}
+
+extern "C" void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3],
+    float gen_fac, double* tex) {
+    p2vo_aosphere_volume_ex_f64(xyzr, n, clip, s, gen_fac, 0, 0, nullptr, tex);
 }
 
 extern "C" void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], const float clip[6], float step_len,
@@ -566,7 +732,7 @@ extern "C" void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], cons
  * ---------------------------------------------------------------------------------------------- */
 extern "C" void p2vo_mlp_f64(const double* P, const float* x, const float* t, int64_t n, double* grads, double* loss,
     double* y) {
-    const int IN = 60, H = 64;
+    const int IN = 78, H = 64;
     const double* W1 = P;
     const double* b1 = W1 + H * IN;
     const double* W2 = b1 + H;

@@ -84,11 +84,23 @@ void p2vo_cone_dirs(int K, float apex_rad, float* out4);
 /* Step table (t, lod) of one cone of width w; returns the number of samples (<= cap). */
 int p2vo_cone_steps(const p2vo_cone_params* cp, float w, float* t, float* lod, int cap);
 
+/* FP32 cone pipeline with OpenMP (nthreads): the MDAO pyramid of a float volume (out[l - 1] receives level l,
+ * l = 1 .. nlevels - 1; level 1 from the texels clamp(v * sat_scale, 0, 1) when sat_scale > 0) and the march in
+ * FP32 in the GPU kernel's operation order, level 0 saturated on the fly. The CPU baseline's timing stand-in. */
+void p2vo_mip_levels_f32(const float* l0, const int32_t d0[3], float sat_scale, int nlevels, float* const* out,
+    int nthreads);
+void p2vo_cone_ao_f32(const float* const* levels, const int32_t* ldims, int nlevels, const float* dirs, int ncones,
+    const p2vo_cone_params* cp, const float* xyzr, const float* nrm, int64_t n, int nthreads, float* ao);
 void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldims, int nlevels, const float* dirs, int ncones,
     const p2vo_cone_params* cp, const float* xyzr, const float* nrm, int64_t n, double* ao);
 
 /* AOSphereRenderer volume deposit (AOSphereRenderer.cpp:918-1021): s = "vol::size" including the
  * 1-voxel zero border; tex gets (4/3 pi r^3 / voxel volume) * genFac in the inner voxel of each particle. */
+/* AOSphere volume deposit with the renderer's two rules: glsl_rule 0 = createVolumeCPU (inner voxel +1, optional
+ * clip-plane discard of particles with dot(p, n) - d >= 0), 1 = createVolumeGLSL (x, y: floor clamped to
+ * [0, s_inner] without the border offset; z: slice trunc clamped to [0, s_inner - 1], + 1; no clip). */
+void p2vo_aosphere_volume_ex_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3], float gen_fac,
+    int glsl_rule, int use_clip, const float plane[4], double* tex);
 void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3], float gen_fac,
     double* tex);
 /* AOSphere sampling: mode 0 = main axes (mainaxes_vertex_2.glsl + mainaxes_fragLightAO_evalAO.glsl),
@@ -96,8 +108,8 @@ void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6],
 void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], const float clip[6], float step_len, float eval_fac,
     const float* xyzr, const float* nrm, int64_t n, int mode, double* ao);
 
-/* Learned-AO MLP 60 -> 64 -> 64 -> 1 (SiLU, SiLU, sigmoid), FP64 reference for gradient checks.
- * params: W1[64][60], b1[64], W2[64][64], b2[64], w3[64], b3 (8129 values). Loss = mean((y - t)^2).
+/* Learned-AO MLP 78 -> 64 -> 64 -> 1 (SiLU, SiLU, sigmoid), FP64 reference for gradient checks.
+ * params: W1[64][78], b1[64], W2[64][64], b2[64], w3[64], b3 (9281 values). Loss = mean((y - t)^2).
  * grads (may be NULL) receives dLoss/dparams; y (may be NULL) the predictions. */
 void p2vo_mlp_f64(const double* params, const float* x, const float* t, int64_t n, double* grads, double* loss,
     double* y);

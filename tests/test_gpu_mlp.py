@@ -35,7 +35,7 @@ def test_gradients_match_fp64(ctx):
     w = random_params(1)
     ctx.mlp_set_weights(w)
     x = rng.uniform(0, 1, (96, p2v.MLP_INPUTS)).astype(np.float32)
-    x[:, 54:57] = synth.random_normals(96, 2)
+    x[:, p2v.MLP_INPUTS - 6:p2v.MLP_INPUTS - 3] = synth.random_normals(96, 2)
     t = rng.uniform(0, 1, 96).astype(np.float32)
     g, loss = ctx.mlp_gradients(x, t)
     l64, _, g64 = oracle.mlp_f64(w.astype(np.float64), x, t)
@@ -49,7 +49,7 @@ def test_tensor_core_inference_matches_fp64(ctx):
     w = random_params(3, 0.15)
     ctx.mlp_set_weights(w)
     x = rng.uniform(0, 1, (1000, p2v.MLP_INPUTS)).astype(np.float32)
-    x[:, 54:57] = synth.random_normals(1000, 4)
+    x[:, p2v.MLP_INPUTS - 6:p2v.MLP_INPUTS - 3] = synth.random_normals(1000, 4)
     y = ctx.mlp_infer(x)
     _, y64, _ = oracle.mlp_f64(w.astype(np.float64), x, None, grads=False)
     # BF16 weights and features (8 mantissa bits), FP32 accumulation
@@ -57,14 +57,14 @@ def test_tensor_core_inference_matches_fp64(ctx):
     assert np.sqrt(np.mean((y - y64) ** 2)) <= 3e-3
 
 
-def set_ao(ctx, f, mode, normalize=1, **over):
+def set_ao(ctx, f, mode, normalize=1, kernel=p2v.KERNEL_BUMP, **over):
     ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], normalize=normalize, sigma=1.0, cyclX=1, cyclY=1,
                    cyclZ=1, accumulate=p2v.ACCUM_EXACT, forSurfaceReconstruction=0, mass_normalize=0,
-                   kernel=p2v.KERNEL_BUMP, ao_mode=mode, **dict(AO, **over))
+                   kernel=kernel, ao_mode=mode, **dict(AO, **over))
 
 
-def with_normals(ctx, f):
-    set_ao(ctx, f, p2v.AO_NONE)
+def with_normals(ctx, f, kernel=p2v.KERNEL_BUMP):
+    set_ao(ctx, f, p2v.AO_NONE, kernel=kernel)
     vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
     ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
     return synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
@@ -79,7 +79,7 @@ def ao_of(ctx, f, nrm, mode, **over):
 
 @pytest.fixture(scope="module")
 def trained(ctx):
-    """Train on two small LJ-liquid frames (cone-march pairs), like the headline model at smaller size."""
+    """Train on two small LJ-liquid frames (cone-march pairs); the tests infer on frames of other seeds."""
     ctx.mlp_clear()
     total = 0
     for seed in (41, 42):
@@ -96,10 +96,12 @@ def test_training_converges(trained):
     total, rep = trained
     assert total >= 200_000
     assert rep["pairs_val"] > 0 and rep["steps"] > 0
-    assert rep["val_rmse"] <= 0.03, rep
+    assert rep["val_rmse"] <= 0.02, rep
 
 
 def test_learned_ao_matches_cone_march_and_is_faster(ctx, trained):
+    """On a frame the network never saw: AO RMSE <= 0.02 against the plain cone march (the benchmark spec's bar),
+    well below the constant predictor's, and an AO stage faster than the march it replaces."""
     f = synth.lj_liquid(cells=32, res=80, seed=43)
     nrm = with_normals(ctx, f)
     plain = ao_of(ctx, f, nrm, p2v.AO_CONE)
@@ -108,7 +110,7 @@ def test_learned_ao_matches_cone_march_and_is_faster(ctx, trained):
     rmse = float(np.sqrt(np.mean((learned - plain) ** 2)))
     base = float(np.sqrt(np.mean((plain.mean() - plain) ** 2)))  # the constant predictor
     assert np.isfinite(learned).all()
-    assert rmse <= 0.03, (rmse, st["ao_fallback"])
+    assert rmse <= 0.02, (rmse, st["ao_fallback"])
     assert rmse < 0.5 * base, (rmse, base)
     # AO stage time: the network against the cone march it replaces
     t_plain = min(_ao_ms(ctx, f, nrm, p2v.AO_CONE) for _ in range(3))
@@ -124,7 +126,7 @@ def _ao_ms(ctx, f, nrm, mode):
 
 
 def test_fallback_outside_training_range_is_the_cone_march(ctx, trained):
-    """With a 10x density-to-occlusion scale the liquid's texels saturate, so its stencils lie above the
+    """With a 10x density-to-occlusion scale the liquid's texels saturate, so its cone samples lie above the
     training range (scale 1): those particles take the cone march, and their AO equals the plain cone march
     bit for bit."""
     f = synth.lj_liquid(cells=32, res=80, seed=44)
@@ -149,28 +151,13 @@ def test_save_load_roundtrip(ctx, trained, tmp_path):
     c2.close()
 
 
-def _trilinear_border(T, x, y, z):
-    """GL LINEAR sampling with CLAMP_TO_BORDER (0) of texels T (z, y, x) at normalised (x, y, z), FP64."""
-    dz, dy, dx = T.shape
-    out = np.zeros(x.shape, np.float64)
-    xs, ys, zs = x * dx - 0.5, y * dy - 0.5, z * dz - 0.5
-    i0, j0, k0 = np.floor(xs).astype(np.int64), np.floor(ys).astype(np.int64), np.floor(zs).astype(np.int64)
-    fx, fy, fz = xs - i0, ys - j0, zs - k0
-    for a in (0, 1):
-        for b in (0, 1):
-            for c in (0, 1):
-                i, j, k = i0 + a, j0 + b, k0 + c
-                ok = (i >= 0) & (i < dx) & (j >= 0) & (j < dy) & (k >= 0) & (k < dz)
-                v = np.where(ok, T[np.clip(k, 0, dz - 1), np.clip(j, 0, dy - 1), np.clip(i, 0, dx - 1)], 0.0)
-                out += v * (fx if a else 1 - fx) * (fy if b else 1 - fy) * (fz if c else 1 - fz)
-    return out
-
-
-def test_stencil_features_vs_fp64():
-    """The learned AO's 60 features of every particle (collected through p2v_mlp_collect, in binning order)
-    against a CPU evaluation: two consecutive levels of the AO pyramid as the GPU built them, rounded to the
-    FP16 texels the stencils read, sampled trilinearly with a zero border at the 3x3x3 offsets 1.5 texels
-    apart around the surface point p + r n, then the unit normal and the surface point in volume coordinates."""
+def test_cone_features_vs_fp64():
+    """The learned AO's features of every particle (collected through p2v_mlp_collect, in binning order) against
+    the FP64 restatement (oracle.cone_features_f64): the AO pyramid as the GPU built it, rounded to the 8-bit
+    UNORM texels the texture units read, sampled along each cone of the MDAO frame at the feature steps,
+    linear within and between levels; then the unit normal and the surface point in volume coordinates. The
+    texture units weight x and y with 8-bit fractions, hence the tolerance. The 44^3 grid puts the steps on
+    all three levels, with level blends."""
     c = p2v.Context(0)
     try:
         f = synth.uniform(n=30_000, edge=40.0, res=44, seed=9)
@@ -182,36 +169,48 @@ def test_stencil_features_vs_fp64():
         x, t = c.mlp_pairs()
         _, order, _ = c.binning()
         assert x.shape == (f.n, p2v.MLP_INPUTS) and np.all(t >= 0)
-        levels = [c.ao_volume(l).astype(np.float64) for l in range(3)]
+        L = AO["ao_levels"]
+        levels = [c.ao_volume(l).astype(np.float64) for l in range(L)]
         levels[0] = np.clip(levels[0] * AO["ao_volume_scale"], 0.0, 1.0)
-        tex = [lv.astype(np.float16).astype(np.float64) for lv in levels]
+        tex = [np.round(np.clip(lv, 0.0, 1.0) * 255.0) / 255.0 for lv in levels]  # 8-bit UNORM texels
         h = oracle.spacing_f64(f.bbox, f.res)
         bmin = [np.float64(np.float32(f.bbox[a] - 0.5 * h[a])) for a in range(3)]
         ibs = [np.float64(np.float32(1.0 / (f.res[a] * h[a]))) for a in range(3)]
-        p = f.xyzr[order].astype(np.float64)
-        n = nrm[order].astype(np.float64)
-        n /= np.linalg.norm(n, axis=1, keepdims=True)
-        u = [(p[:, a] + p[:, 3] * n[:, a] - bmin[a]) * ibs[a] for a in range(3)]
-        k = 1.5 * (np.arange(3) - 1.0)
+        dirs = oracle.cone_dirs(AO["ao_cones"], np.deg2rad(np.float32(AO["ao_apex_deg"])))
+        ts, lods = oracle.cone_steps(float(dirs[0, 3]), offset=AO["ao_offset"], cone_length=AO["ao_cone_length"],
+                                     shortest_edge=float(min(f.res)), max_lod=float(L - 1), steps=AO["ao_steps"])
+        fl = lods[oracle.mlp_feature_steps(len(ts))]
+        assert fl.min() < 1.0 and fl.max() == L - 1 and np.any(fl != np.floor(fl)), fl  # all levels, blends
+        ref = oracle.cone_features_f64(tex, dirs, ts, lods, f.xyzr[order], nrm[order], bmin, ibs)
+        ns = p2v.MLP_INPUTS - 6
+        e = np.abs(x[:, :ns].astype(np.float64) - ref[:, :ns])
+        assert np.abs(x[:, ns:ns + 3] - ref[:, ns:ns + 3]).max() <= 1e-6
+        assert np.abs(x[:, ns + 3:] - ref[:, ns + 3:]).max() <= 1e-5
+        assert e.max() <= 4e-3, e.max()
+        assert np.sqrt(np.mean(e ** 2)) <= 5e-4, np.sqrt(np.mean(e ** 2))
+    finally:
+        c.close()
 
-        def stencil(T):
-            dz, dy, dx = T.shape
-            X = u[0][:, None, None, None] + k[None, None, None, :] / dx
-            Y = u[1][:, None, None, None] + k[None, None, :, None] / dy
-            Z = u[2][:, None, None, None] + k[None, :, None, None] / dz
-            X, Y, Z = np.broadcast_arrays(X, Y, Z)
-            return _trilinear_border(T, X, Y, Z).reshape(len(u[0]), 27)
 
-        errs = {}
-        pos = np.stack(u, axis=1)
-        for s in (0, 1):
-            ref = np.concatenate([stencil(tex[s]), stencil(tex[s + 1]), n, pos], axis=1)
-            errs[s] = np.abs(x.astype(np.float64) - ref)
-        s = min(errs, key=lambda q: errs[q].max())
-        e = errs[s]
-        assert np.abs(x[:, 54:57] - n).max() <= 1e-6
-        assert np.abs(x[:, 57:60] - pos).max() <= 1e-5
-        assert e[:, :54].max() <= 4e-3, e[:, :54].max()
-        assert np.sqrt(np.mean(e[:, :54] ** 2)) <= 5e-4, np.sqrt(np.mean(e[:, :54] ** 2))
+def test_learned_ao_uniform_100k_gauss3():
+    """The small plain-method workload (100k particles, 128^3, Gaussian 3-sigma kernel): a network trained on
+    eight frames of other seeds reaches AO RMSE <= 0.02 against the plain cone march on the seed-1 frame."""
+    c = p2v.Context(0)
+    try:
+        c.mlp_clear()
+        for k in range(8):
+            f = synth.uniform(n=100_000, seed=101 + k)
+            nrm = with_normals(c, f, kernel=p2v.KERNEL_GAUSS3)
+            set_ao(c, f, p2v.AO_CONE, kernel=p2v.KERNEL_GAUSS3)
+            c.mlp_collect([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm)], f.bbox, 100_000,
+                          seed=k)
+        rep = c.mlp_train(epochs=16, batch=2048, lr=3e-3, lr_decay=0.85, seed=7)
+        f = synth.uniform(n=100_000, seed=1)
+        nrm = with_normals(c, f, kernel=p2v.KERNEL_GAUSS3)
+        plain = ao_of(c, f, nrm, p2v.AO_CONE, kernel=p2v.KERNEL_GAUSS3)
+        learned = ao_of(c, f, nrm, p2v.AO_LEARNED, kernel=p2v.KERNEL_GAUSS3)
+        rmse = float(np.sqrt(np.mean((learned.astype(np.float64) - plain) ** 2)))
+        assert np.isfinite(learned).all()
+        assert rmse <= 0.02, (rmse, rep, c.stats()["ao_fallback"])
     finally:
         c.close()
