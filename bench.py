@@ -1,8 +1,9 @@
 """Benchmark of the particle-to-volume path (density + AO) on GB300.
 
-Default workload: the LJ-liquid frame (4,000,000 particles on a jittered FCC lattice, radii U[0.4,0.6],
-256^3 grid), seeded synthetic data. One step = one full frame through the pipeline (binning + sort +
-density gather + statistics/normalisation [+ mip + AO]).
+Default workload: the large mixed-phase frame (64,000,000 particles: half a jittered FCC slab, half a uniform
+gas at 1/20 of its density, radii 0.5/0.8/1.2 in ratio 6:3:1, 512^3 grid), seeded synthetic data: the largest
+single-GPU configuration. One step = one full frame through the pipeline (binning + sort + density gather +
+statistics/normalisation + mip pyramid + AO).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
@@ -35,7 +36,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lj_liquid_4M")
+    ap.add_argument("--workload", default="mixed_phase_64M")
+    ap.add_argument("--model", default=None,
+                    help="learned-AO network file: loaded when it exists (no training), else written after training")
     return ap.parse_args()
 
 
@@ -67,7 +70,7 @@ def make_workload(name: str, rank: int = 0):
         scale = (n / 100_000) ** (1.0 / 3.0)
         f = synth.uniform(n=n, edge=100.0 * scale, res=int(round(128 * scale)), seed=1 + rank)
         desc = dict(workload="uniform_16M", particles=f.n, grid=list(f.res), radius=0.5,
-                    kernel="bump sigma=1 (reference rbf)", cyclic=True)
+                    kernel="gauss3 sigma=r (cut at 3 sigma)", cyclic=True)
         return f, desc
     if name == "mixed_phase_64M":
         f = synth.mixed_phase(seed=5 + rank)
@@ -154,7 +157,6 @@ def profile_traffic(name: str):
 
 AO_PARAMS = dict(ao_mode=1, ao_volume=0, ao_volume_scale=1.0, ao_cones=8, ao_steps=32, ao_levels=3, ao_apex_deg=50.0,
                  ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1)
-AO_SAMPLE = 50_000  # particles in the CPU AO sample
 
 
 def setup_frame(ctx, f, dparams=None):
@@ -191,41 +193,61 @@ def cpu_reference_density(f, nthreads: int, kernel: int = 0):
     return time.perf_counter() - t0, "port", vol
 
 
-def ao_sample(f) -> int:
-    return AO_SAMPLE if f.res[0] * f.res[1] * f.res[2] <= 256 ** 3 else AO_SAMPLE // 10
+AO_SAMPLE = 1_000_000  # particles in the CPU baseline's AO sample (the whole frame when smaller)
 
 
-def cpu_cone_ao(f, grid, nrm, sample: int):
-    """Time the CPU cone march (restatement of the MDAO shader, OpenMP) on `sample` particles; returns
-    seconds for the sample."""
+def ao_sample_index(f) -> np.ndarray:
+    """Particles of the CPU AO sample: evenly spaced over the frame (every phase and region of it)."""
+    if f.n <= AO_SAMPLE:
+        return np.arange(f.n)
+    return np.linspace(0, f.n - 1, AO_SAMPLE).astype(np.int64)
+
+
+def cone_geometry(f):
+    """Bounds of the density grid as the cone march's texture (node-centred, [min - h/2, max + h/2])."""
     import oracle
 
     h = oracle.spacing_f64(f.bbox, f.res)
-    bmin = [f.bbox[a] - 0.5 * h[a] for a in range(3)]
-    bsize = [f.res[a] * h[a] for a in range(3)]
-    lv = oracle.mip_chain_f64(grid, AO_PARAMS["ao_levels"], AO_PARAMS["ao_volume_scale"])
-    dirs = oracle.cone_dirs(AO_PARAMS["ao_cones"], np.deg2rad(np.float32(AO_PARAMS["ao_apex_deg"])))
-    idx = np.linspace(0, f.n - 1, sample).astype(np.int64)
-    t0 = time.perf_counter()
-    oracle.cone_ao_f64(lv, dirs, f.xyzr[idx], nrm[idx], bmin, bsize, offset=AO_PARAMS["ao_offset"],
-                       strength=AO_PARAMS["ao_strength"], cone_length=AO_PARAMS["ao_cone_length"],
-                       shortest_edge=float(min(f.res)), max_lod=float(AO_PARAMS["ao_levels"] - 1),
-                       steps=AO_PARAMS["ao_steps"], early_exit=1, border=0, sat_scale=AO_PARAMS["ao_volume_scale"])
-    return time.perf_counter() - t0
+    return [f.bbox[a] - 0.5 * h[a] for a in range(3)], [f.res[a] * h[a] for a in range(3)]
 
 
-def cpu_pipeline(f, nthreads, grid=None, nrm=None, kernel: int = 0):
-    """CPU particles/s of density + plain cone AO: the density stage on the full frame, the AO stage on a
-    sample of particles scaled to the frame (AO_SAMPLE, a tenth of that above 256^3 voxels, so the CPU leg
-    stays within about half a minute)."""
-    from megamol_gb300 import synth
+def cone_kw(f) -> dict:
+    return dict(offset=AO_PARAMS["ao_offset"], strength=AO_PARAMS["ao_strength"],
+                cone_length=AO_PARAMS["ao_cone_length"], shortest_edge=float(min(f.res)),
+                max_lod=float(AO_PARAMS["ao_levels"] - 1), steps=AO_PARAMS["ao_steps"],
+                early_exit=AO_PARAMS["ao_early_exit"], border=0, sat_scale=AO_PARAMS["ao_volume_scale"])
+
+
+def cpu_pipeline(f, nthreads, nrm, kernel: int = 0):
+    """One step of the CPU pipeline, every stage timed as it ran: the density on the full frame (the compiled
+    reference module where present, else its bit-exact FP32 port), the mip pyramid of the normalised grid
+    (FP32, OpenMP) and the plain cone march (FP32 restatement of the shader in the GPU kernel's operation
+    order, OpenMP) on the AO sample. Returns a dict of measured seconds and particle counts; the step's
+    particles/s combines the measured stage rates: 1 / (t_density / N + t_mip / N + t_ao / S)."""
+    import oracle
 
     dt_d, kind, vol = cpu_reference_density(f, nthreads, kernel)
-    if nrm is None:
-        nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
-    sample = ao_sample(f)
-    dt_ao = cpu_cone_ao(f, vol, nrm, sample) * (f.n / sample)
-    return f.n / (dt_d + dt_ao), kind, dt_d, dt_ao
+    grid = np.ascontiguousarray(vol, np.float32).reshape(f.res[2], f.res[1], f.res[0])
+    t0 = time.perf_counter()
+    lv = oracle.mip_levels_f32(grid, AO_PARAMS["ao_levels"], AO_PARAMS["ao_volume_scale"], nthreads)
+    dt_mip = time.perf_counter() - t0
+    idx = ao_sample_index(f)
+    xs, ns = np.ascontiguousarray(f.xyzr[idx]), np.ascontiguousarray(nrm[idx])
+    bmin, bsize = cone_geometry(f)
+    dirs = oracle.cone_dirs(AO_PARAMS["ao_cones"], np.deg2rad(np.float32(AO_PARAMS["ao_apex_deg"])))
+    t0 = time.perf_counter()
+    oracle.cone_ao_f32(lv, dirs, xs, ns, bmin, bsize, nthreads=nthreads, **cone_kw(f))
+    dt_ao = time.perf_counter() - t0
+    rate = 1.0 / (dt_d / f.n + dt_mip / f.n + dt_ao / idx.size)
+    return dict(value=rate, kind=kind, s_density=dt_d, s_mip=dt_mip, s_ao=dt_ao, particles=f.n,
+                ao_particles=int(idx.size), s_step=dt_d + dt_mip + dt_ao)
+
+
+def cpu_sample_text(r: dict) -> str:
+    return (f"measured stages per step: density on the full frame ({r['particles']} particles, "
+            f"{r['s_density']:.2f} s, {r['kind']}), mip pyramid of the full grid ({r['s_mip']:.2f} s), plain "
+            f"cone march (FP32 restatement, OpenMP) on {r['ao_particles']} evenly spaced particles "
+            f"({r['s_ao']:.2f} s); particles/s = 1 / (t_density/N + t_mip/N + t_ao/N_ao), measured rates only")
 
 
 def run_reference(args):
@@ -242,47 +264,51 @@ def run_reference(args):
     from megamol_gb300 import synth
 
     _, _, vol = cpu_reference_density(f, nthreads, kern)
-    nrm = synth.gradient_normals(f.xyzr, vol, f.bbox)
+    nrm = synth.gradient_normals(f.xyzr, np.asarray(vol).reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
     for _ in range(max(0, args.warmup)):
-        cpu_pipeline(f, nthreads, nrm=nrm, kernel=kern)
-    vals, kind = [], "port"
-    tot = 0.0
-    for _ in range(args.steps):
-        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm, kernel=kern)
-        vals.append(v)
-        tot += dt_d + dt_ao
-    value = f.n * args.steps / tot
+        cpu_pipeline(f, nthreads, nrm, kern)
+    runs = [cpu_pipeline(f, nthreads, nrm, kern) for _ in range(args.steps)]
+    tot = {k: sum(r[k] for r in runs) for k in ("s_density", "s_mip", "s_ao", "s_step")}
+    value = 1.0 / (tot["s_density"] / f.n + tot["s_mip"] / f.n + tot["s_ao"] / runs[0]["ao_particles"])
+    cpu = dict(runs[0], **{k: v / args.steps for k, v in tot.items()})
     line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot["s_step"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference", "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip"),
-            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": kind,
-                             "sample": f"density on the full frame ({f.n} particles) + cone AO on {ao_sample(f)} "
-                                       "particles scaled to the frame, per step"},
+            "impl": "reference",
+            "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip, gradient normals"),
+            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": runs[0]["kind"],
+                             "sample": cpu_sample_text(cpu)},
+            "stages_s_per_step": {k: tot[k] / args.steps for k in ("s_density", "s_mip", "s_ao")},
             "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def train_learned_ao(ctx, f_main, dparams=None, workload: str = "lj_liquid_4M"):
-    """Train the learned AO on cone-march pairs of other frames. LJ liquid: two other LJ frames (seeds 3
-    and 4, 500,000 pairs each) and ten uniform 100k-particle frames of the small plain-method workload.
-    Other workloads: other seeds of the same workload (the cone length is a fraction of the volume, so the
-    network must see the box geometry it infers on): two frames of 1,000,000 pairs, one for the 64M frame."""
+def train_learned_ao(ctx, f_main, dparams=None, workload: str = "mixed_phase_64M"):
+    """Train the learned AO on cone-march pairs of frames other than the timed one (other seeds):
+    * LJ liquid: two other LJ frames (500,000 pairs each) and ten uniform 100k-particle frames;
+    * uniform 100k (3-sigma Gaussian): twelve frames of 100,000 pairs;
+    * uniform 16M (the 16M inference set, 3-sigma Gaussian): pairs of the two smaller configurations, ten
+      uniform 100k Gaussian frames (100,000 pairs each) and two LJ frames (500,000 pairs each);
+    * mixed phase 64M: two other 64M frames (1,000,000 pairs each): the cone length is a fraction of the
+      volume, so the network sees the box geometry it infers on."""
     from megamol_gb300 import p2v, synth
 
+    bump = dict(kernel=p2v.KERNEL_BUMP, sigma=1.0)
+    gauss = dict(kernel=p2v.KERNEL_GAUSS3, sigma=1.0)
     ctx.mlp_clear()
     total = 0
     if workload == "lj_liquid_4M":
-        frames = [(synth.lj_liquid(seed=s), 500_000) for s in (3, 4)]
-        frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000) for k in range(10)]
+        frames = [(synth.lj_liquid(seed=s), 500_000, bump) for s in (3, 4)]
+        frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000, bump) for k in range(10)]
     elif workload == "uniform_100k":
-        frames = [(make_workload(workload, rank=100 + k)[0], 100_000) for k in range(12)]
+        frames = [(make_workload(workload, rank=100 + k)[0], 100_000, gauss) for k in range(12)]
+    elif workload == "uniform_16M":
+        frames = [(synth.uniform(n=100_000, seed=10 + k), 100_000, gauss) for k in range(10)]
+        frames += [(synth.lj_liquid(seed=s), 500_000, bump) for s in (3, 4)]
     else:
-        kk = (100,) if workload == "mixed_phase_64M" else (100, 101)
-        frames = [(make_workload(workload, rank=k)[0], 1_000_000) for k in kk]
-    for k, (f, npairs) in enumerate(frames):
-        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1,
-                       **(dparams or {}))
+        frames = [(make_workload(workload, rank=k)[0], 1_000_000, dparams or bump) for k in (100, 101)]
+    for k, (f, npairs, dp) in enumerate(frames):
+        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1, **dp)
         vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
         ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
         nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
@@ -290,8 +316,53 @@ def train_learned_ao(ctx, f_main, dparams=None, workload: str = "lj_liquid_4M"):
         total = ctx.mlp_collect([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm)], f.bbox, npairs,
                                 seed=100 + k)
     rep = ctx.mlp_train(seed=7)
-    ctx.set_params(sizex=f_main.res[0], sizey=f_main.res[1], sizez=f_main.res[2], normalize=1, **AO_PARAMS)
+    ctx.set_params(sizex=f_main.res[0], sizey=f_main.res[1], sizez=f_main.res[2], normalize=1, **(dparams or bump),
+                   **AO_PARAMS)
     return total, rep
+
+
+def error_figures(ctx, f, dparams, nrm, ao_plain, ao_learned):
+    """Errors of the timed frame against the FP64 oracle (untimed): the density of a z-slab (computed from the
+    particles that reach it, un-normalised: max|a - b| / max|b| and RMS / max|b|), and the plain and learned
+    AO on 2,000 evenly spaced particles against the FP64 cone march over the FP64 pyramid of the GPU's
+    normalised grid (max and RMS)."""
+    import oracle
+    from megamol_gb300 import p2v, sharding
+
+    nthreads = os.cpu_count() or 1
+    ctx.set_params(normalize=0, ao_mode=p2v.AO_NONE)
+    raw = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
+    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, raw)
+    raw = raw.reshape(f.res[2], f.res[1], f.res[0])
+    gauss = dparams["kernel"] == p2v.KERNEL_GAUSS3
+    z0 = f.res[2] // 2 - 4
+    z1 = z0 + 8
+    keep = sharding.slab_particle_mask(f.xyzr, f.bbox, f.res, True, z0, z1, 3.0 if gauss else 1.0)
+    # four threads: the FP64 oracle keeps one full grid per thread
+    ref = oracle.density_f64(f.xyzr[keep], f.bbox, f.res, (1, 1, 1), 1.0, oracle.GAUSS3 if gauss else oracle.BUMP,
+                             min(4, nthreads))[z0:z1]
+    d = raw[z0:z1].astype(np.float64) - ref
+    den = {"slab_z": [int(z0), int(z1)], "max_rel": float(np.abs(d).max() / np.abs(ref).max()),
+           "rms_rel": float(np.sqrt(np.mean(d ** 2)) / np.abs(ref).max()), "bar": 1e-5}
+    del ref, d
+    ctx.set_params(normalize=1)
+    grid = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
+    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, grid)
+    grid = grid.reshape(f.res[2], f.res[1], f.res[0])
+    ctx.set_params(**AO_PARAMS)
+    idx = np.linspace(0, f.n - 1, 2000).astype(np.int64)
+    bmin, bsize = cone_geometry(f)
+    lv = oracle.mip_chain_f64(grid, AO_PARAMS["ao_levels"], AO_PARAMS["ao_volume_scale"])
+    dirs = oracle.cone_dirs(AO_PARAMS["ao_cones"], np.deg2rad(np.float32(AO_PARAMS["ao_apex_deg"])))
+    ref_ao = oracle.cone_ao_f64(lv, dirs, f.xyzr[idx], nrm[idx], bmin, bsize, **cone_kw(f))
+    out = {"density_vs_fp64": den}
+    for name, ao in (("plain_ao_vs_fp64", ao_plain), ("learned_ao_vs_fp64", ao_learned)):
+        e = np.abs(ao[idx].astype(np.float64) - ref_ao)
+        out[name] = {"particles": int(idx.size), "max": float(e.max()), "rms": float(np.sqrt(np.mean(e ** 2)))}
+    out["learned_ao_vs_plain"] = {"particles": int(f.n),
+                                  "rms": float(np.sqrt(np.mean((ao_learned.astype(np.float64) - ao_plain) ** 2))),
+                                  "max": float(np.abs(ao_learned - ao_plain).max()), "bar": 0.02}
+    return out
 
 
 def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, sampler=None, tag="timed"):
@@ -322,6 +393,27 @@ def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, 
     return ev0.elapsed_time(ev1) / steps, {k: v / steps for k, v in stage.items()}
 
 
+def feature_levels(f) -> int:
+    """Mip levels the learned AO's feature samples read (one texture each): the step table of the cone march
+    (geometric steps from offset + 1e-4 to the cone length, lod = log2(t * w * shortest edge) clamped to
+    [0, levels - 1], w = 2 tan(apex / 2)) at the 9 feature steps, two levels where a lod is fractional."""
+    import math
+
+    t0 = AO_PARAMS["ao_offset"] + 1e-4
+    n = AO_PARAMS["ao_steps"]
+    g = (AO_PARAMS["ao_cone_length"] / t0) ** (1.0 / n)
+    w = 2.0 * math.tan(math.radians(AO_PARAMS["ao_apex_deg"]) / 2)
+    top = AO_PARAMS["ao_levels"] - 1
+    need = set()
+    for j in range(9):
+        k = int(math.floor(j * (n - 1) / 8 + 0.5))
+        lod = min(max(math.log2(t0 * g ** k * w * min(f.res)), 0.0), top)
+        need.add(int(lod))
+        if lod > int(lod) and int(lod) < top:
+            need.add(int(lod) + 1)
+    return len(need)
+
+
 def run_ours(args):
     import torch
 
@@ -337,7 +429,13 @@ def run_ours(args):
     f, desc = make_workload(args.workload, rank)
     ctx = p2v.Context(dev)
     dparams = density_params(desc)
-    pairs, train_rep = train_learned_ao(ctx, f, dparams, args.workload)
+    if args.model and os.path.exists(args.model):
+        ctx.mlp_load(args.model)
+        pairs, train_rep = 0, {"val_rmse": None, "steps": 0, "ms": 0.0, "loaded": args.model}
+    else:
+        pairs, train_rep = train_learned_ao(ctx, f, dparams, args.workload)
+        if args.model:
+            ctx.mlp_save(args.model)
     grid0, nrm = setup_frame(ctx, f, dparams)
     V = f.res[0] * f.res[1] * f.res[2]
     stream = torch.cuda.Stream()
@@ -397,59 +495,74 @@ def run_ours(args):
     e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * (16 + 12)),
            "d2h_bytes_per_step": int(V * 4 + f.n * 4), "ms_per_step": e2e_ms}
 
-    # ---- roofline of the dominant kernel of the measured pipeline ----
+    # ---- errors of the timed frame against the FP64 oracle (untimed) ----
+    errors = error_figures(ctx, f, dparams, nrm, ao_plain, ao_learn) if rank == 0 else None
+
+    # ---- roofline: algorithmic bytes per stage / its device time; the dominant stage's kernel ----
     peak, peak_kind = peaks()
     nb = (f.res[0] + 2) * (f.res[1] + 2) * (f.res[2] + 2)
-    gather_bytes = f.n * 16 + V * 4 + nb * 4
-    lv_bytes, d = 0, list(f.res)
-    for _ in range(AO_PARAMS["ao_levels"]):
-        lv_bytes += d[0] * d[1] * d[2] * 4
-        d = [max(1, x // 2) for x in d]
-    ao_bytes = f.n * (16 + 12 + 4) + lv_bytes
-    ao_name = "p2v::mlp_infer_tc_kernel (+ mip levels, stencil textures, fallback cone march)" if use_learned else \
-        "p2v::cone_ao_kernel (+ mip levels)"
-    if st["ms_ao"] >= st["ms_density"]:
-        dom = (ao_name, ao_bytes, st["ms_ao"], "learned_ao_lj_liquid_4M.md" if use_learned else "cone_ao_lj_liquid_4M.md")
-    else:
-        dom = ("p2v::gather_fixed_kernel", gather_bytes, st["ms_density"], "density_gather_lj_liquid_4M.md")
-    achieved = dom[1] / (dom[2] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind,
-                "traffic": profile_traffic(dom[3]) if args.workload == "lj_liquid_4M" else None,
-                "algorithmic_bytes": dom[1], "ms_per_launch": dom[2],
-                "stages_ms": {k: st[k] for k in ("ms_binning", "ms_density", "ms_normalize", "ms_ao")},
-                "density_gather": {"algorithmic_bytes": gather_bytes, "ms": st["ms_density"],
-                                   "frac": gather_bytes / (st["ms_density"] * 1e-3) / 1e9 / peak}}
+    dims = [list(f.res)]
+    for _ in range(1, AO_PARAMS["ao_levels"]):
+        dims.append([max(1, x // 2) for x in dims[-1]])
+    vox = [d[0] * d[1] * d[2] for d in dims]
+    key_bits = int(nb).bit_length()
+    counting = nb + 1 <= 64 * f.n and 4 * (nb + 1) <= 128 * 2 ** 20  # the library's counting-sort rule
+    radix_passes = 0 if counting else (key_bits + 8) // 9
+    stage_bytes = {
+        # read xyzr, write key + index, the radix passes (8 B in, 8 B out each), the sorted records, cell starts
+        "ms_binning": f.n * (16 + 8 + 16 * radix_passes + 32) + nb * 8,
+        "ms_density": f.n * 16 + V * 4 + nb * 4,   # sorted records once, the grid written, cell starts
+        "ms_normalize": V * 8,                      # statistics read + normalised write
+        # mip levels read and written, positions + normals in, AO out, the levels read once
+        "ms_ao": sum(4 * (vox[l] + vox[l + 1]) for l in range(len(vox) - 1)) + f.n * (16 + 12 + 4) + 4 * sum(vox),
+    }
+    names = {"ms_binning": "p2v::pack_keys_kernel + " + ("counting sort by cell (scatter_bins_kernel, order_bins_kernel)"
+                                                         if counting else "onesweep radix sort (onesweep_kernel)"),
+             "ms_density": "p2v::gather_fixed_kernel",
+             "ms_normalize": "p2v::finalize_kernel + normalize_kernel",
+             "ms_ao": ("p2v::mlp_infer_tc_kernel (+ mip levels, feature textures, fallback cone march)"
+                       if use_learned else "p2v::cone_ao_kernel (+ mip levels)")}
+    stages = {k: {"kernel": names[k], "ms": st[k], "algorithmic_bytes": int(b),
+                  "achieved_gbs": b / (st[k] * 1e-3) / 1e9 if st[k] > 0 else None,
+                  "frac": b / (st[k] * 1e-3) / 1e9 / peak if st[k] > 0 else None}
+              for k, b in stage_bytes.items()}
+    dom = max(stages, key=lambda k: stages[k]["ms"])
+    prof = {"ms_binning": "binning", "ms_density": "density_gather", "ms_normalize": "normalize",
+            "ms_ao": "learned_ao" if use_learned else "cone_ao"}[dom]
+    roofline = {"bound": "hbm", "kernel": stages[dom]["kernel"], "achieved": stages[dom]["achieved_gbs"],
+                "peak": peak, "unit": "GB/s", "frac": stages[dom]["frac"], "peak_kind": peak_kind,
+                "traffic": profile_traffic(f"{prof}_{args.workload}.md"),
+                "algorithmic_bytes": stages[dom]["algorithmic_bytes"], "ms_per_launch": stages[dom]["ms"],
+                "stages": stages}
 
-    # ---- CPU baseline (rank 0, N=1 only) ----
+    # ---- CPU baseline (rank 0, N=1 only): one measured step of the CPU pipeline ----
     cpu = None
     if rank == 0 and ws == 1:
         nthreads = os.cpu_count() or 1
-        v, kind, dt_d, dt_ao = cpu_pipeline(f, nthreads, nrm=nrm, kernel=dparams["kernel"])
-        cpu = {"value": v, "unit": "particles/s", "cores": nthreads, "kind": kind,
-               "sample": f"density on the full frame ({f.n} particles, {dt_d:.2f} s) + plain cone AO on "
-                         f"{ao_sample(f)} particles scaled to the frame ({dt_ao:.2f} s)"}
+        r = cpu_pipeline(f, nthreads, nrm, dparams["kernel"])
+        cpu = {"value": r["value"], "unit": "particles/s", "cores": nthreads, "kind": r["kind"],
+               "sample": cpu_sample_text(r)}
 
     # kernels per frame: scalar init, pack, [the counting sort by cell: histogram, tile sums, tile scan, cell
     # starts, scatter, in-cell order], digit histogram + scan, the radix passes (9/8-bit digits over the bin
     # keys; an odd count and launched gated after a counting sort), cell starts (3), gather, finalize +
-    # normalise; AO: normals, mips, sorted copies, then the cone march or stencil textures (2) + tensor-core
-    # inference + fallback cone march, and the AO back to input order
-    key_bits = int(nb).bit_length()
+    # normalise; AO: normals, mips, sorted normals, then the cone march, or the feature textures (one per mip
+    # level the feature samples read) + tensor-core inference + fallback cone march (each writes the AO in
+    # input order)
     passes = (key_bits + 8) // 9
-    counting = nb + 1 <= 64 * f.n
     if counting and passes % 2 == 0:
         passes += 1
     launches_density = 1 + 1 + (6 if counting else 0) + 2 + passes + 3 + 1 + 2
-    launches_ao = 1 + (AO_PARAMS["ao_levels"] - 1) + 1 + (5 if use_learned else 2)
+    launches_ao = 1 + (AO_PARAMS["ao_levels"] - 1) + 1 + (feature_levels(f) + 2 if use_learned else 1)
     if rank == 0:
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP: bf16 x bf16 -> f32)", "data": "synthetic",
-                "config": dict(desc, ao=("learned AO (MLP 60-64-64-1, BF16 tensor cores) with cone-march fallback"
-                                         if use_learned else "plain cone march") +
+                "config": dict(desc, ao=("learned AO (MLP 78-64-64-1 on cone samples, BF16 tensor cores) with "
+                                         "cone-march fallback" if use_learned else "plain cone march") +
                                         ", 8 cones x 32 steps, 3-level mip, gradient normals",
-                               l2="per-step working set ~0.6 GB > 126 MB L2 (no flush)"),
+                               l2=f"per-step working set ~{(f.n * 84 + V * 12) / 2 ** 30:.1f} GiB > 126 MiB L2 "
+                                  "(no flush)"),
                 "learned_vs_plain": {"plain_particles_per_s": ws * f.n / (ms_plain * 1e-3), "plain_ms": ms_plain,
                                      "learned_particles_per_s": ws * f.n / (ms_learn * 1e-3), "learned_ms": ms_learn,
                                      "speedup": ms_plain / ms_learn, "ao_rmse_learned_vs_plain": rmse,
@@ -460,7 +573,11 @@ def run_ours(args):
                                                   "steps": train_rep["steps"], "ms": train_rep["ms"]}},
                 "density_tile": {"tile": tune["tile"], "candidates_ms": {"x".join(map(str, c["tile"])): c["ms"]
                                                                          for c in tune["candidates"] if c["lanes"] == 1}},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "errors": errors, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "same_method_vs_cpu": None if cpu is None else {
+                    "note": "plain GPU pipeline / plain CPU pipeline (the reference arm runs the plain march)",
+                    "plain_gpu_particles_per_s": ws * f.n / (ms_plain * 1e-3), "cpu_particles_per_s": cpu["value"],
+                    "ratio": ws * f.n / (ms_plain * 1e-3) / cpu["value"]},
                 "gpu_launches": (launches_density + launches_ao) * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)
     ctx.close()
