@@ -181,7 +181,28 @@ typedef struct p2v_params {
                                shape (frames, sizes, pointers, parameters) repeats (1) */
     /* --- outputs --- */
     int32_t vector_grid;    /* aggregator 2: also build the outParticles / outInfo grid of p2v_get_vector_grid (0) */
+    /* --- AOSphereRenderer volume deposit (appended; AOSphereRenderer.cpp:83-124, 918-1221) --- */
+    int32_t aos_deposit;    /* p2v_aos_deposit: the CPU rule of createVolumeCPU (0) or the GLSL rule of createVolumeGLSL */
+    int32_t aos_clip;       /* "ao::clipData": the CPU rule drops particles with dot(p, n) - d >= 0 (0) */
+    float aos_clip_plane[4];/* the clip plane as the renderer's clipDat: unit normal n and d = dot(point, n) (0) */
+    int32_t ao_normals;     /* p2v_ao_normals: where the AO modes take each particle's normal (P2V_NORMALS_LIST) */
 } p2v_params;
+
+/* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,
+ * AOSphereRenderer.cpp:918-1021): inner voxel trunc(u * s_inner) clamped to [0, s_inner - 1], stored at +1 inside
+ * the one-voxel border, with the optional clip-plane discard. GLSL (createVolumeGLSL, :1026-1221, and
+ * volume_updateVolume.vert.glsl:22-46): x and y floor(u * s_inner) clamped to [0, s_inner] written without the
+ * +1 (the point lands on a pixel corner; a fragment is taken for the pixel centre on the square's lower edge),
+ * z binned on the host into slice trunc(u * s_inner) (at most s_inner - 1; below the box: slice 0) + 1; no clip. */
+typedef enum p2v_aos_deposit { P2V_AOS_DEPOSIT_CPU = 0, P2V_AOS_DEPOSIT_GLSL = 1 } p2v_aos_deposit;
+
+/* Normals of the AO modes. LIST: the lists' per-particle directions (DIRDATA_FLOAT_XYZ, p2v_particle_list.normals).
+ * GRADIENT: computed on the device from this frame's density grid, for particle data without directions: the
+ * unit vector down the density gradient, -grad(rho) / |grad(rho)|, with grad(rho) the node grid's central
+ * differences (periodic along cyclic axes, one-sided first differences at the faces of open ones) interpolated
+ * trilinearly at the particle's position (clamped into the node range); a vanishing gradient gives a zero
+ * normal (AO 1). Needs a scalar grid (aggregator 0 or 1). */
+typedef enum p2v_ao_normals { P2V_NORMALS_LIST = 0, P2V_NORMALS_GRADIENT = 1 } p2v_ao_normals;
 
 typedef struct p2v_stats {
     uint64_t particles_in;       /* records presented */

@@ -239,6 +239,67 @@ __global__ void __launch_bounds__(256) sort_particles_kernel(const uint32_t* __r
     }
 }
 
+// Normals from the density grid (P2V_NORMALS_GRADIENT): -grad(rho) at the particle, normalised. grad(rho) at
+// node i along axis a is (v[i + 1] - v[i - 1]) / (2 h) with the neighbours wrapped on a cyclic axis, and the
+// one-sided first differences (v[1] - v[0]) / h, (v[s-1] - v[s-2]) / h at the faces of an open one; the node
+// gradients are interpolated trilinearly at u = (p - min) / h clamped into [0, s - 1].
+__device__ __forceinline__ float node_grad(const float* __restrict__ g, int64_t base, int64_t stride, int i, int s,
+                                           int cyc, float ih) {
+    if (s < 2)
+        return 0.0f;
+    int lo = i - 1, hi = i + 1;
+    float scale = 0.5f * ih;
+    if (cyc) {
+        lo = lo < 0 ? lo + s : lo;
+        hi = hi >= s ? hi - s : hi;
+    } else if (i == 0) {
+        lo = 0;
+        scale = ih;
+    } else if (i == s - 1) {
+        hi = s - 1;
+        scale = ih;
+    }
+    return (__ldg(g + base + hi * stride) - __ldg(g + base + lo * stride)) * scale;
+}
+
+__global__ void __launch_bounds__(256) gradient_normals_kernel(const GridGeo geo, const float* __restrict__ grid,
+    const float4* __restrict__ xyzr, uint32_t n, float4* __restrict__ nrm) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n)
+        return;
+    const float4 p = xyzr[j];
+    const float pc[3] = {p.x, p.y, p.z};
+    int i0[3], i1[3];
+    float f[3], ih[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ih[a] = 1.0f / geo.hf[a];
+        float u = (pc[a] - geo.minf[a]) * ih[a];
+        u = fminf(fmaxf(u, 0.0f), (float) (geo.s[a] - 1));  // a NaN coordinate becomes 0 (fmaxf)
+        const int k = min((int) u, geo.s[a] - 1);
+        i0[a] = k;
+        i1[a] = min(k + 1, geo.s[a] - 1);
+        f[a] = u - (float) k;
+    }
+    const int64_t sx = geo.s[0], sxy = (int64_t) geo.s[0] * geo.s[1];
+    float gr[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int x = (c & 1) ? i1[0] : i0[0], y = (c & 2) ? i1[1] : i0[1], z = (c & 4) ? i1[2] : i0[2];
+        const float w = ((c & 1) ? f[0] : 1.0f - f[0]) * ((c & 2) ? f[1] : 1.0f - f[1]) * ((c & 4) ? f[2] : 1.0f - f[2]);
+        gr[0] += w * node_grad(grid, z * sxy + y * sx, 1, x, geo.s[0], geo.cyc[0], ih[0]);
+        gr[1] += w * node_grad(grid, z * sxy + x, sx, y, geo.s[1], geo.cyc[1], ih[1]);
+        gr[2] += w * node_grad(grid, y * sx + x, sxy, z, geo.s[2], geo.cyc[2], ih[2]);
+    }
+    const float l2 = gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2];
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (l2 > 0.0f && isfinite(l2)) {
+        const float il = -rsqrtf(l2);
+        out = make_float4(gr[0] * il, gr[1] * il, gr[2] * il, 0.0f);
+    }
+    nrm[j] = out;
+}
+
 // ---------------------------------------------------------------------------------------------
 // AOSphere volume: nearest inner voxel, (4/3 pi r^3 / voxel volume) * genFac, summed exactly in
 // 64-bit fixed point (2^-32) so the result does not depend on the particle order.
@@ -253,16 +314,38 @@ __global__ void __launch_bounds__(256) aosphere_deposit_kernel(const AOSpherePar
         return;
     const float pc[3] = {p.x, p.y, p.z};
     int c[3];
+    if (!ap.glsl_rule) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        // AOSphereRenderer.cpp:964-980: int(((p - min) / range) * s_inner), clamped to [0, s_inner - 1]
-        const float q = ((pc[a] - ap.minOS[a]) / ap.rangeOS[a]) * static_cast<float>(ap.si[a]);
-        int v = (int) fminf(fmaxf(q, -2147483520.0f), 2147483520.0f);
-        c[a] = v < 0 ? 0 : (v >= ap.si[a] ? ap.si[a] - 1 : v);
+        for (int a = 0; a < 3; ++a) {
+            // AOSphereRenderer.cpp:964-980: int(((p - min) / range) * s_inner), clamped to [0, s_inner - 1]
+            const float q = __fmul_rn(__fdiv_rn(__fsub_rn(pc[a], ap.minOS[a]), ap.rangeOS[a]), (float) ap.si[a]);
+            const int v = (int) fminf(fmaxf(q, -2147483520.0f), 2147483520.0f);
+            c[a] = (v < 0 ? 0 : (v >= ap.si[a] ? ap.si[a] - 1 : v)) + 1;  // inside the one-voxel border
+        }
+        if (ap.clip) {
+            // :982-991: the particle is dropped when dot(pos, n) - d >= 0 (vislib's Dot: a running sum)
+            const float od = __fadd_rn(__fadd_rn(__fmul_rn(pc[0], ap.clip_plane[0]), __fmul_rn(pc[1], ap.clip_plane[1])),
+                                       __fmul_rn(pc[2], ap.clip_plane[2]));
+            if (__fsub_rn(od, ap.clip_plane[3]) >= 0.0f)
+                return;
+        }
+    } else {
+        // volume_updateVolume.vert.glsl:22: clamp(floor(((p - min) / range) * s_inner), 0, s_inner) in x and y, the
+        // point's pixel (no border offset); z: the host's slice binning (AOSphereRenderer.cpp:1129-1131), layer + 1
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+            const float q = __fmul_rn(__fdiv_rn(__fsub_rn(pc[a], ap.minOS[a]), ap.rangeOS[a]), (float) ap.si[a]);
+            const float fl = fminf(fmaxf(floorf(q), 0.0f), (float) ap.si[a]);
+            c[a] = (int) fl;
+        }
+        const float qz = __fmul_rn(__fdiv_rn(__fsub_rn(pc[2], ap.minOS[2]), ap.rangeOS[2]), (float) ap.si[2]);
+        const int vz = (int) fminf(fmaxf(qz, -2147483520.0f), 2147483520.0f);
+        c[2] = max(0, min(vz, ap.si[2] - 1)) + 1;
     }
+    // (4/3) pi r^3 (the CPU's float(M_PI) and the shader's 3.14159265 are the same float)
     const float spVol = 4.0f / 3.0f * 3.14159265358979f * p.w * p.w * p.w;
     const float val = (spVol / ap.voxel_vol) * ap.gen_fac;
-    const int64_t idx = (c[0] + 1) + ((int64_t) (c[1] + 1) + (int64_t) (c[2] + 1) * ap.s[1]) * ap.s[0];
+    const int64_t idx = c[0] + ((int64_t) c[1] + (int64_t) c[2] * ap.s[1]) * ap.s[0];
     atomicAdd(acc + idx, (unsigned long long) __float2ull_rn(val * 4294967296.0f));
 }
 
@@ -394,6 +477,14 @@ cudaError_t launch_sort_particles(const uint32_t* order, uint32_t n, const float
         return cudaSuccess;
     const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
     sort_particles_kernel<<<grd, 256, 0, st>>>(order, n, xyzr, nrm, xyzr_s, nrm_s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradient_normals(const GridGeo& geo, const float* grid, const float4* xyzr, uint32_t n, float4* nrm,
+                                    cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    gradient_normals_kernel<<<ceil_div(n, 256), 256, 0, st>>>(geo, grid, xyzr, n, nrm);
     return cudaGetLastError();
 }
 

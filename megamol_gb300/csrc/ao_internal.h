@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include "p2v_common.cuh"
+
 namespace p2v {
 
 constexpr int MAX_CONES = 16;
@@ -41,6 +43,9 @@ struct AOSphereParams {
     float minOS[3], rangeOS[3];    // clip box
     float voxel_vol, gen_fac, eval_fac;
     float origin[3], ext[3], sampd[3];  // posOrigin, posExtents, aoSampDist
+    int glsl_rule;                 // deposit: 0 = createVolumeCPU's voxel rule, 1 = createVolumeGLSL's
+    int clip;                      // CPU rule: drop particles on the far side of the clip plane
+    float clip_plane[4];           // unit normal, d
 };
 
 // MDAO occupancy volume geometry (uniforms of mdao_volume.geom/frag.glsl, MDAOVolumeGenerator.cpp:139-164)
@@ -68,6 +73,9 @@ cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const fl
     uint32_t n, const uint32_t* n_dev, const uint32_t* out_order, float* ao, cudaStream_t st);
 cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc,
     float* tex, const uint32_t* order, const float4* nrm, int mode, float* ao, int sms, cudaStream_t st);
+// unit normals down the density gradient of `grid` (geometry geo) at xyzr[j], into nrm[j] (P2V_NORMALS_GRADIENT)
+cudaError_t launch_gradient_normals(const GridGeo& geo, const float* grid, const float4* xyzr, uint32_t n, float4* nrm,
+    cudaStream_t st);
 cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,
     cudaStream_t st);
 

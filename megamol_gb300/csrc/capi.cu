@@ -569,13 +569,18 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_UPLOAD], st));
     // ---- normals for AO, on the side stream: needed only by the AO stage ----
     const bool want_ao = P.ao_mode != P2V_AO_NONE;
+    const bool list_normals = P.ao_normals == P2V_NORMALS_LIST;  // else computed from the grid in the AO stage
     cudaStream_t side = pp.side;
     if (want_ao) {
+        if (P.ao_normals != P2V_NORMALS_LIST && P.ao_normals != P2V_NORMALS_GRADIENT)
+            return fail(P2V_EINVAL, "ao_normals %d is not a p2v_ao_normals", P.ao_normals);
+        if (!list_normals && agg == 2)
+            return fail(P2V_EINVAL, "gradient normals need a scalar grid (aggregator 0 or 1)");
         P2V_CUDA_TRY(nrm.ensure(sizeof(float4) * (N + 1)));
         P2V_CUDA_TRY(ao.ensure(sizeof(float) * (N + 1)));
         // every check before the fork: an error return must not leave work on the side stream
         uint64_t nbytes = 0;
-        for (uint32_t l = 0; l < fr->list_count; ++l) {
+        for (uint32_t l = 0; l < fr->list_count && list_normals; ++l) {
             const p2v_particle_list& L = fr->lists[l];
             if (L.vertex_type == P2V_VERTDATA_NONE || L.count == 0)
                 continue;
@@ -593,7 +598,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_FORK], st));
         P2V_CUDA_TRY(cudaStreamWaitEvent(side, pp.sev[SEV_FORK], 0));
         uint64_t noff = 0;
-        for (uint32_t l = 0; l < fr->list_count; ++l) {
+        for (uint32_t l = 0; l < fr->list_count && list_normals; ++l) {
             const p2v_particle_list& L = fr->lists[l];
             if (L.vertex_type == P2V_VERTDATA_NONE)
                 continue;
@@ -1060,15 +1065,24 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
     const p2v_params& P = prm;
     // the cone-march stages run on sorted copies of the positions and normals (coalesced whatever the input
     // order) and scatter the AO back to input order at the end
-    // (the binning's last pass wrote the sorted positions when it knew the frame would march cones)
+    // (the binning's last pass wrote the sorted positions when it knew the frame would march cones); gradient
+    // normals are computed in sorted order from the sorted positions
     auto to_sorted = [&]() -> cudaError_t {
         cudaError_t e = pp.xyzr_s.ensure(sizeof(float4) * ((size_t) n + 1));
         if (e == cudaSuccess)
             e = pp.nrm_s.ensure(sizeof(float4) * ((size_t) n + 1));
-        if (e == cudaSuccess)
-            e = launch_sort_particles(order, n, pp.xyzr_sorted ? nullptr : xyzr.as<float4>(), nrm.as<float4>(),
-                                      pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), sms, st);
-        return e;
+        if (e != cudaSuccess)
+            return e;
+        if (P.ao_normals == P2V_NORMALS_GRADIENT) {
+            if (!pp.xyzr_sorted)
+                e = launch_sort_particles(order, n, xyzr.as<float4>(), nrm.as<float4>(), pp.xyzr_s.as<float4>(),
+                                          pp.nrm_s.as<float4>(), sms, st);
+            if (e == cudaSuccess)
+                e = launch_gradient_normals(g, dgrid, pp.xyzr_s.as<float4>(), n, pp.nrm_s.as<float4>(), st);
+            return e;
+        }
+        return launch_sort_particles(order, n, pp.xyzr_sorted ? nullptr : xyzr.as<float4>(), nrm.as<float4>(),
+                                     pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), sms, st);
     };
     if (P.ao_mode == P2V_AO_CONE) {
         ConeParams cp{};
@@ -1136,7 +1150,15 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
                        (ap.rangeOS[2] / static_cast<float>(ap.si[2]));
         ap.gen_fac = P.aos_gen_fac;
         ap.eval_fac = P.aos_eval_fac;
+        if (P.aos_deposit != P2V_AOS_DEPOSIT_CPU && P.aos_deposit != P2V_AOS_DEPOSIT_GLSL)
+            return fail(P2V_EINVAL, "aos_deposit %d is not a p2v_aos_deposit", P.aos_deposit);
+        ap.glsl_rule = P.aos_deposit == P2V_AOS_DEPOSIT_GLSL ? 1 : 0;
+        ap.clip = P.aos_clip && !ap.glsl_rule ? 1 : 0;  // createVolumeGLSL has no clip discard
+        for (int k = 0; k < 4; ++k)
+            ap.clip_plane[k] = P.aos_clip_plane[k];
         const size_t nv = (size_t) ap.s[0] * ap.s[1] * ap.s[2];
+        if (P.ao_normals == P2V_NORMALS_GRADIENT)  // the taps read the normals in input order
+            P2V_CUDA_TRY(launch_gradient_normals(g, dgrid, xyzr.as<float4>(), n, nrm.as<float4>(), st));
         P2V_CUDA_TRY(aos_acc.ensure(sizeof(unsigned long long) * nv));
         P2V_CUDA_TRY(aos_tex.ensure(sizeof(float) * nv));
         P2V_CUDA_TRY(launch_aosphere(ap, xyzr.as<float4>(), n, aos_acc.as<unsigned long long>(), aos_tex.as<float>(),
@@ -1451,6 +1473,11 @@ void p2v_params_default(p2v_params* p) {
     p->batch_lanes = 0;
     p->batch_graph = 1;
     p->vector_grid = 0;
+    p->aos_deposit = P2V_AOS_DEPOSIT_CPU;  // AOSphereRenderer "vol::gen" (0 = CPU)
+    p->aos_clip = 0;                       // "ao::clipData" (false)
+    for (float& c : p->aos_clip_plane)
+        c = 0.0f;
+    p->ao_normals = P2V_NORMALS_LIST;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {

@@ -30,6 +30,8 @@ KERNEL_BUMP, KERNEL_GAUSS3 = 0, 1
 ACCUM_EXACT, ACCUM_KAHAN = 0, 1
 AO_NONE, AO_CONE, AO_AOSPHERE_AXES, AO_AOSPHERE_NORMAL, AO_LEARNED = range(5)
 AOVOL_DENSITY, AOVOL_MDAO = 0, 1
+AOS_DEPOSIT_CPU, AOS_DEPOSIT_GLSL = 0, 1
+NORMALS_LIST, NORMALS_GRADIENT = 0, 1
 STATUS_NAMES = {0: "P2V_OK", 1: "P2V_EINVAL", 2: "P2V_ENOMEM", 3: "P2V_ECUDA", 4: "P2V_ETIMEOUT", 5: "P2V_EDOMAIN",
                 6: "P2V_EUNSUPPORTED"}
 
@@ -55,6 +57,8 @@ class Params(C.Structure):
         ("aos_step_len", C.c_float), ("aos_gen_fac", C.c_float), ("aos_eval_fac", C.c_float),
         ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("tile_z", C.c_int32),
         ("batch_lanes", C.c_int32), ("batch_graph", C.c_int32), ("vector_grid", C.c_int32),
+        ("aos_deposit", C.c_int32), ("aos_clip", C.c_int32), ("aos_clip_plane", C.c_float * 4),
+        ("ao_normals", C.c_int32),
     ]
 
 
@@ -351,6 +355,9 @@ class Context:
         for k, v in kw.items():
             if not hasattr(self.params, k):
                 raise AttributeError(f"unknown parameter {k}")
+            cur = getattr(self.params, k)
+            if isinstance(cur, C.Array):
+                v = type(cur)(*v)
             setattr(self.params, k, v)
         self._check(self.lib.p2v_set_params(self.h, C.byref(self.params)))
 

@@ -37,7 +37,8 @@ def run_ao(ctx, f, normals, **params):
     base = dict(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], normalize=1, sigma=1.0, cyclX=1, cyclY=1, cyclZ=1,
                 accumulate=p2v.ACCUM_EXACT, forSurfaceReconstruction=0, mass_normalize=0, kernel=p2v.KERNEL_BUMP,
                 ao_volume=p2v.AOVOL_DENSITY, ao_volume_scale=1.0, ao_cones=3, ao_steps=0, ao_levels=0,
-                ao_apex_deg=50.0, ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1)
+                ao_apex_deg=50.0, ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1,
+                aos_deposit=p2v.AOS_DEPOSIT_CPU, aos_clip=0, aos_clip_plane=[0.0] * 4, ao_normals=p2v.NORMALS_LIST)
     base.update(params)
     ctx.set_params(**base)
     ao = np.full(f.n, np.nan, np.float32)
@@ -107,6 +108,62 @@ def test_aosphere_vs_fp64(ctx, mode):
     ref = oracle.aosphere_ao_f64(tex, f.bbox, f.xyzr, nrm, 0 if mode == p2v.AO_AOSPHERE_AXES else 1, 0.5, 1.0)
     d = np.abs(ao.astype(np.float64) - ref)
     assert d.max() <= 1e-5 * max(1.0, np.abs(ref).max()), d.max()
+
+
+@pytest.mark.parametrize("mode", [p2v.AO_AOSPHERE_AXES, p2v.AO_AOSPHERE_NORMAL])
+@pytest.mark.parametrize("rule, plane", [(p2v.AOS_DEPOSIT_GLSL, None), (p2v.AOS_DEPOSIT_CPU, "oblique"),
+                                         (p2v.AOS_DEPOSIT_CPU, "unset")])
+def test_aosphere_deposit_rules_vs_fp64(ctx, mode, rule, plane):
+    """The two deposit rules of AOSphereRenderer against the FP64 restatement: createVolumeGLSL's (the point's
+    pixel: floor clamped to [0, s_inner] in x and y, the host's z slice + 1) and createVolumeCPU's with the
+    ao::clipData discard, for an oblique plane through the box centre and for the renderer's plane when no
+    clip plane is connected (all zeros: dot - d = 0 >= 0 drops every particle, so the volume stays empty and
+    AO is 1, up to the rounding of the normal's squared length)."""
+    f = frame(n=20_000, seed=26)
+    nrm = synth.random_normals(f.n, 10)
+    s = (22, 26, 18)
+    cp = None
+    if plane == "oblique":
+        nv = np.array([0.3, -0.5, 0.81], np.float32)
+        nv /= np.linalg.norm(nv)
+        ctr = 0.5 * (np.array(f.bbox[:3], np.float32) + np.array(f.bbox[3:], np.float32))
+        cp = [float(nv[0]), float(nv[1]), float(nv[2]), float(np.dot(ctr, nv))]
+    elif plane == "unset":
+        cp = [0.0, 0.0, 0.0, 0.0]
+    ao, _, _ = run_ao(ctx, f, nrm, ao_mode=mode, aos_sizex=s[0], aos_sizey=s[1], aos_sizez=s[2], aos_step_len=0.5,
+                      aos_gen_fac=1.0, aos_eval_fac=1.0, aos_deposit=rule, aos_clip=int(cp is not None),
+                      aos_clip_plane=cp if cp is not None else [0.0] * 4)
+    tex = oracle.aosphere_volume_f64(f.xyzr, f.bbox, s, 1.0, glsl_rule=rule, clip_plane=cp)
+    ref = oracle.aosphere_ao_f64(tex, f.bbox, f.xyzr, nrm, 0 if mode == p2v.AO_AOSPHERE_AXES else 1, 0.5, 1.0)
+    d = np.abs(ao.astype(np.float64) - ref)
+    assert d.max() <= 1e-5 * max(1.0, np.abs(ref).max()), d.max()
+    if plane == "unset":
+        assert np.all(tex == 0) and np.abs(ao - 1.0).max() <= 1e-6  # |n|^2 = 1 up to rounding
+    else:
+        assert tex.sum() > 0
+
+
+@pytest.mark.parametrize("mode", [p2v.AO_CONE, p2v.AO_AOSPHERE_AXES])
+def test_library_gradient_normals_match_host_normals(ctx, mode):
+    """P2V_NORMALS_GRADIENT computes each particle's normal on the device from the frame's density grid (-grad rho,
+    central differences, periodic on cyclic axes, trilinear at the particle). The AO it gives equals the AO of
+    the same normals computed on the host (synth.gradient_normals, FP64) and passed as list normals: the cone
+    march runs without early exit, so the difference is the normals' rounding only."""
+    f = synth.lj_liquid(cells=20, res=48, seed=33)
+    ctx.set_params(sizex=48, sizey=48, sizez=48, normalize=1, ao_mode=p2v.AO_NONE, ao_normals=p2v.NORMALS_LIST)
+    vol = np.empty(48 ** 3, np.float32)
+    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
+    nrm = synth.gradient_normals(f.xyzr, vol.reshape(48, 48, 48), f.bbox)
+    extra = dict(ao_cones=8, ao_steps=32, ao_levels=3, ao_early_exit=0) if mode == p2v.AO_CONE else \
+        dict(aos_sizex=20, aos_sizey=20, aos_sizez=20)
+    host, _, _ = run_ao(ctx, f, nrm, ao_mode=mode, ao_normals=p2v.NORMALS_LIST, **extra)
+    ctx.set_params(ao_normals=p2v.NORMALS_GRADIENT)
+    ao = np.full(f.n, np.nan, np.float32)
+    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, ao_out=ao)], f.bbox)  # no list normals
+    ctx.set_params(ao_normals=p2v.NORMALS_LIST)
+    d = np.abs(ao.astype(np.float64) - host)
+    assert np.isfinite(ao).all()
+    assert np.sqrt(np.mean(d ** 2)) <= 1e-5 and d.max() <= 1e-3, (np.sqrt(np.mean(d ** 2)), d.max())
 
 
 def test_gradient_normals_ao_pipeline_lj_small(ctx):
