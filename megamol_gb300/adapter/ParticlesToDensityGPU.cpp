@@ -10,14 +10,17 @@
 
 #include "mmcore/param/BoolParam.h"
 #include "mmcore/param/EnumParam.h"
+#include "mmcore/param/FilePathParam.h"
 #include "mmcore/param/FloatParam.h"
 #include "mmcore/param/IntParam.h"
 #include "mmcore/utility/log/Log.h"
+#include "mmstd/renderer/CallClipPlane.h"
 
 using namespace megamol;
 using namespace megamol::p2v_gb300;
 using core::param::BoolParam;
 using core::param::EnumParam;
+using core::param::FilePathParam;
 using core::param::FloatParam;
 using core::param::IntParam;
 
@@ -42,6 +45,21 @@ ParticlesToDensityGPU::ParticlesToDensityGPU()
         , aoOffsetSlot("ao::offset", "Offset from the surface")
         , aoStrengthSlot("ao::strength", "Strength")
         , aoConeLengthSlot("ao::coneLength", "Cone length")
+        , aoVolumeSlot("ao::volume", "Volume the cone march samples: the density grid or MDAO's occupancy volume")
+        , aoVolumeScaleSlot("ao::volumeScale", "Density to occlusion scale of the density grid (saturated at 1)")
+        , aoNormalsSlot("ao::normals", "Particle normals: the input's directions or the density gradient")
+        , aoModelSlot("ao::model", "Network file of the learned AO (p2v_mlp_save)")
+        , mdaoVolSizeSlot("ambient occlusion::volumeSize", "Ambient Occlusion: Longest volume edge")
+        , mdaoHighPrecisionSlot("ambient occlusion::highPrecisionTexture", "Ambient Occlusion: Use high precision textures")
+        , aosSizeXSlot("vol::sizex", "The size of the volume in numbers of voxels")
+        , aosSizeYSlot("vol::sizey", "The size of the volume in numbers of voxels")
+        , aosSizeZSlot("vol::sizez", "The size of the volume in numbers of voxels")
+        , aosGenSlot("vol::gen", "The generation method")
+        , aosStepLenSlot("ao::stepLen", "The access step length in voxels")
+        , aosGenFacSlot("vol::genFac", "The generation factor (influence factor of a single sphere on a voxel)")
+        , aosEvalFacSlot("ao::evalFac", "The evaluation factor (influence factor of a single voxel on a sphere)")
+        , aosClipDataSlot("ao::clipData", "Clip ao data")
+        , getClipPlaneSlot("getclipplane", "Connects to a clipping plane module")
         , outDataSlot("outData", "Provides a density volume for the particles")
         , outParticlesSlot("outParticles", "Provides particles forming a regular grid with the sampled values")
         , outInfoSlot("outInfo", "Provides information which can be used for visualization and filtering")
@@ -101,6 +119,47 @@ ParticlesToDensityGPU::ParticlesToDensityGPU()
     MakeSlotAvailable(&aoStrengthSlot);
     aoConeLengthSlot << new FloatParam(0.8f, 0.01f, 1.0f);
     MakeSlotAvailable(&aoConeLengthSlot);
+    auto* av = new EnumParam(P2V_AOVOL_DENSITY);
+    av->SetTypePair(P2V_AOVOL_DENSITY, "Density grid");
+    av->SetTypePair(P2V_AOVOL_MDAO, "MDAO occupancy");
+    aoVolumeSlot << av;
+    MakeSlotAvailable(&aoVolumeSlot);
+    aoVolumeScaleSlot << new FloatParam(1.0f, 0.0f);
+    MakeSlotAvailable(&aoVolumeScaleSlot);
+    auto* an = new EnumParam(P2V_NORMALS_LIST);
+    an->SetTypePair(P2V_NORMALS_LIST, "Input directions");
+    an->SetTypePair(P2V_NORMALS_GRADIENT, "Density gradient");
+    aoNormalsSlot << an;
+    MakeSlotAvailable(&aoNormalsSlot);
+    aoModelSlot << new FilePathParam("");
+    MakeSlotAvailable(&aoModelSlot);
+    // SphereRenderer.cpp:205,214
+    mdaoVolSizeSlot << new IntParam(128, 1, 1024);
+    MakeSlotAvailable(&mdaoVolSizeSlot);
+    mdaoHighPrecisionSlot << new BoolParam(false);
+    MakeSlotAvailable(&mdaoHighPrecisionSlot);
+    // AOSphereRenderer.cpp:86-118
+    aosSizeXSlot << new IntParam(32, 4);
+    MakeSlotAvailable(&aosSizeXSlot);
+    aosSizeYSlot << new IntParam(32, 4);
+    MakeSlotAvailable(&aosSizeYSlot);
+    aosSizeZSlot << new IntParam(32, 4);
+    MakeSlotAvailable(&aosSizeZSlot);
+    auto* gen = new EnumParam(P2V_AOS_DEPOSIT_CPU);
+    gen->SetTypePair(P2V_AOS_DEPOSIT_CPU, "CPU");
+    gen->SetTypePair(P2V_AOS_DEPOSIT_GLSL, "GPU (GLSL)");
+    aosGenSlot << gen;
+    MakeSlotAvailable(&aosGenSlot);
+    aosStepLenSlot << new FloatParam(0.5f, 0.0f);
+    MakeSlotAvailable(&aosStepLenSlot);
+    aosGenFacSlot << new FloatParam(1.0f, 0.0f);
+    MakeSlotAvailable(&aosGenFacSlot);
+    aosEvalFacSlot << new FloatParam(1.0f, 0.0f);
+    MakeSlotAvailable(&aosEvalFacSlot);
+    aosClipDataSlot << new BoolParam(false);
+    MakeSlotAvailable(&aosClipDataSlot);
+    getClipPlaneSlot.SetCompatibleCall<core::view::CallClipPlaneDescription>();
+    MakeSlotAvailable(&getClipPlaneSlot);
 
     using VDC = geocalls::VolumetricDataCall;
     outDataSlot.SetCallback(VDC::ClassName(), VDC::FunctionName(VDC::IDX_GET_DATA),
@@ -157,7 +216,10 @@ void ParticlesToDensityGPU::release() {
 bool ParticlesToDensityGPU::anythingDirty() const {
     for (auto* s : {&aggregatorSlot, &xResSlot, &yResSlot, &zResSlot, &cyclXSlot, &cyclYSlot, &cyclZSlot,
              &normalizeSlot, &sigmaSlot, &kernelSlot, &massNormSlot, &aoModeSlot, &aoConesSlot, &aoStepsSlot,
-             &aoLevelsSlot, &aoApexSlot, &aoOffsetSlot, &aoStrengthSlot, &aoConeLengthSlot})
+             &aoLevelsSlot, &aoApexSlot, &aoOffsetSlot, &aoStrengthSlot, &aoConeLengthSlot, &aoVolumeSlot,
+             &aoVolumeScaleSlot, &aoNormalsSlot, &aoModelSlot, &mdaoVolSizeSlot, &mdaoHighPrecisionSlot, &aosSizeXSlot,
+             &aosSizeYSlot, &aosSizeZSlot, &aosGenSlot, &aosStepLenSlot, &aosGenFacSlot, &aosEvalFacSlot,
+             &aosClipDataSlot})
         if (s->IsDirty())
             return true;
     return false;
@@ -166,7 +228,10 @@ bool ParticlesToDensityGPU::anythingDirty() const {
 void ParticlesToDensityGPU::resetDirty() {
     for (auto* s : {&aggregatorSlot, &xResSlot, &yResSlot, &zResSlot, &cyclXSlot, &cyclYSlot, &cyclZSlot,
              &normalizeSlot, &sigmaSlot, &kernelSlot, &massNormSlot, &aoModeSlot, &aoConesSlot, &aoStepsSlot,
-             &aoLevelsSlot, &aoApexSlot, &aoOffsetSlot, &aoStrengthSlot, &aoConeLengthSlot})
+             &aoLevelsSlot, &aoApexSlot, &aoOffsetSlot, &aoStrengthSlot, &aoConeLengthSlot, &aoVolumeSlot,
+             &aoVolumeScaleSlot, &aoNormalsSlot, &aoModelSlot, &mdaoVolSizeSlot, &mdaoHighPrecisionSlot, &aosSizeXSlot,
+             &aosSizeYSlot, &aosSizeZSlot, &aosGenSlot, &aosStepLenSlot, &aosGenFacSlot, &aosEvalFacSlot,
+             &aosClipDataSlot})
         s->ResetDirty();
 }
 
@@ -246,9 +311,45 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
     prm.ao_offset = aoOffsetSlot.Param<FloatParam>()->Value();
     prm.ao_strength = aoStrengthSlot.Param<FloatParam>()->Value();
     prm.ao_cone_length = aoConeLengthSlot.Param<FloatParam>()->Value();
+    prm.ao_volume = aoVolumeSlot.Param<EnumParam>()->Value();
+    prm.ao_volume_scale = aoVolumeScaleSlot.Param<FloatParam>()->Value();
+    prm.ao_normals = aoNormalsSlot.Param<EnumParam>()->Value();
+    prm.mdao_volume_size = mdaoVolSizeSlot.Param<IntParam>()->Value();
+    prm.mdao_unorm8 = mdaoHighPrecisionSlot.Param<BoolParam>()->Value() ? 0 : 1;  // R8 unless high precision
+    prm.aos_sizex = aosSizeXSlot.Param<IntParam>()->Value();
+    prm.aos_sizey = aosSizeYSlot.Param<IntParam>()->Value();
+    prm.aos_sizez = aosSizeZSlot.Param<IntParam>()->Value();
+    prm.aos_deposit = aosGenSlot.Param<EnumParam>()->Value();
+    prm.aos_step_len = aosStepLenSlot.Param<FloatParam>()->Value();
+    prm.aos_gen_fac = aosGenFacSlot.Param<FloatParam>()->Value();
+    prm.aos_eval_fac = aosEvalFacSlot.Param<FloatParam>()->Value();
+    prm.aos_clip = aosClipDataSlot.Param<BoolParam>()->Value();
+    // the clip plane as AOSphereRenderer reads it (:273-287): unit normal and d = dot(point, normal), all zeros
+    // without a connected clip-plane module
+    auto* ccp = getClipPlaneSlot.CallAs<core::view::CallClipPlane>();
+    if (ccp != nullptr && (*ccp)(0)) {
+        const auto& pl = ccp->GetPlane();
+        const auto n = pl.Normal();
+        const auto pt = pl.Point();
+        prm.aos_clip_plane[0] = n.X();
+        prm.aos_clip_plane[1] = n.Y();
+        prm.aos_clip_plane[2] = n.Z();
+        prm.aos_clip_plane[3] = pt.X() * n.X() + pt.Y() * n.Y() + pt.Z() * n.Z();
+    }
     prm.vector_grid = prm.aggregator == 2;
     if (p2v_set_params(ctx, &prm) != P2V_OK)
         return false;
+    // the learned AO's network, loaded when the file parameter names a new file
+    const std::string model = aoModelSlot.Param<FilePathParam>()->Value().string();
+    if (!model.empty() && model != loadedModel) {
+        if (p2v_mlp_load(ctx, model.c_str()) != P2V_OK) {
+            char msg[512];
+            p2v_get_last_error(ctx, msg, sizeof(msg));
+            core::utility::log::Log::DefaultLog.WriteError("ParticlesToDensityGPU: %s", msg);
+            return false;
+        }
+        loadedModel = model;
+    }
 
     const unsigned int nl = in->GetParticleListCount();
     std::vector<p2v_particle_list> lists(nl);
@@ -274,8 +375,10 @@ bool ParticlesToDensityGPU::recompute(geocalls::MultiParticleDataCall* in) {
             L.normal_stride = p.GetDirDataStride();
         }
         if (prm.ao_mode != P2V_AO_NONE) {
-            L.normals = static_cast<const float*>(p.GetDirData());
-            L.normal_stride = p.GetDirDataStride();
+            if (prm.ao_normals == P2V_NORMALS_LIST) {
+                L.normals = static_cast<const float*>(p.GetDirData());
+                L.normal_stride = p.GetDirDataStride();
+            }
             ao[i].resize(p.GetCount());
             L.ao_out = ao[i].data();
         }

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <array>
+#include <string>
 #include <vector>
 
 #include "datatools/table/TableDataCall.h"
@@ -65,6 +66,16 @@ private:
     // additions of this module
     core::param::ParamSlot kernelSlot, massNormSlot, aoModeSlot, aoConesSlot, aoStepsSlot, aoLevelsSlot, aoApexSlot,
         aoOffsetSlot, aoStrengthSlot, aoConeLengthSlot;
+    // the AO source: the volume the cone march samples, its scale, the normals, the learned AO's network file
+    core::param::ParamSlot aoVolumeSlot, aoVolumeScaleSlot, aoNormalsSlot, aoModelSlot;
+    // MDAO (SphereRenderer.cpp:193-214): "ambient occlusion::volumeSize", "ambient occlusion::highPrecisionTexture"
+    core::param::ParamSlot mdaoVolSizeSlot, mdaoHighPrecisionSlot;
+    // AOSphereRenderer (AOSphereRenderer.cpp:57-124): "vol::sizex/y/z", "vol::gen", "ao::stepLen", "vol::genFac",
+    // "ao::evalFac", "ao::clipData"
+    core::param::ParamSlot aosSizeXSlot, aosSizeYSlot, aosSizeZSlot, aosGenSlot, aosStepLenSlot, aosGenFacSlot,
+        aosEvalFacSlot, aosClipDataSlot;
+    core::CallerSlot getClipPlaneSlot;  // "getclipplane" (AOSphereRenderer.cpp:54,273-287)
+    std::string loadedModel;
 
     core::CalleeSlot outDataSlot;
     core::CalleeSlot outParticlesSlot;
