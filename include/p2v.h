@@ -186,6 +186,11 @@ typedef struct p2v_params {
     int32_t aos_clip;       /* "ao::clipData": the CPU rule drops particles with dot(p, n) - d >= 0 (0) */
     float aos_clip_plane[4];/* the clip plane as the renderer's clipDat: unit normal n and d = dot(point, n) (0) */
     int32_t ao_normals;     /* p2v_ao_normals: where the AO modes take each particle's normal (P2V_NORMALS_LIST) */
+    /* --- bounded device waits --- */
+    int32_t mma_wait_polls; /* polls of the learned AO's tensor-core completion waits before the call gives up with
+                               P2V_ETIMEOUT; 0 = the default (2^20, about a second) */
+    int32_t test_hold_mma;  /* test hook: the learned AO's first MMA is not issued, so its bounded wait runs out and
+                               the call returns P2V_ETIMEOUT with the context still usable (0) */
 } p2v_params;
 
 /* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,

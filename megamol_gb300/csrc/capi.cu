@@ -1122,6 +1122,10 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         a.fallback = fb_list.as<uint32_t>();
         a.nfallback = &fs->ao_fallback;
         a.err = &fs->error;
+        if (P.mma_wait_polls < 0)
+            return fail(P2V_EINVAL, "mma_wait_polls must be >= 0");
+        a.wait_polls = (uint32_t) P.mma_wait_polls;
+        a.hold_mma = P.test_hold_mma ? 1 : 0;
         P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
         // the plain cone march for every particle whose features left the training range
         P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n,
@@ -1478,6 +1482,8 @@ void p2v_params_default(p2v_params* p) {
     for (float& c : p->aos_clip_plane)
         c = 0.0f;
     p->ao_normals = P2V_NORMALS_LIST;
+    p->mma_wait_polls = 0;
+    p->test_hold_mma = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {

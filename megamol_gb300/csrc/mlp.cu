@@ -403,7 +403,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // epilogue finishes layer 3 (64 -> 1) in FP32 with the sigmoid. The accumulators never occupy registers,
 // so four CTAs (32 warps, 64 registers each: more warps hide the texture latency better than the few
 // spilled registers cost) stay resident per SM. Every mbarrier wait
-// is bounded: on timeout the CTA records ERR_MMA_TIMEOUT, drains its MMAs (bounded) and frees TMEM.
+// is bounded: on timeout the CTA records ERR_MMA_TIMEOUT, drains its MMAs (bounded) and frees TMEM. The
+// poll count can be lowered (p2v_params.mma_wait_polls), and a test hook (p2v_params.test_hold_mma) leaves layer
+// 1 unissued so that its wait, on an arrival that never comes, runs out.
 // ---------------------------------------------------------------------------------------------
 namespace tc {
 constexpr int THREADS = 256;
@@ -467,8 +469,8 @@ __device__ __forceinline__ void fence_async_smem() {
 }
 
 // bounded wait for phase `phase` of an mbarrier; false when the budget ran out
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-    for (uint32_t i = 0; i < tc::WAIT_LIMIT; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t ok;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
@@ -571,6 +573,7 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
     const uint32_t a_s = smem_u32(sA), w1_s = smem_u32(sW1), w2_s = smem_u32(sW2);
     const float b3 = args.P[OFF_B3];
     const bool check = args.lo != nullptr && args.hi != nullptr;
+    const uint32_t polls = args.wait_polls ? args.wait_polls : tc::WAIT_LIMIT;
     uint32_t phase = 0;
     bool failed = false;
     const uint32_t ntiles = (args.n + tc::M - 1) / tc::M;
@@ -660,7 +663,7 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
         if (half == 0)
             oor = oor || s_flag[row] != 0u;
         // ---- layer 1: D[128 x 64] = A[128 x 80] W1^T ----
-        if (t == 0) {
+        if (t == 0 && !args.hold_mma) {
             tc_fence_after();
 #pragma unroll
             for (int kk = 0; kk < tc::KCH1 / 2; ++kk)
@@ -668,7 +671,7 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
                           kk > 0 ? 1u : 0u);
             umma_commit(mbar);
         }
-        failed = !mbar_wait(mbar, phase);
+        failed = !mbar_wait(mbar, phase, polls);
         phase ^= 1u;
         tc_fence_after();
         if (__syncthreads_or(failed))
@@ -698,7 +701,7 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
                           kk > 0 ? 1u : 0u);
             umma_commit(mbar);
         }
-        failed = !mbar_wait(mbar, phase);
+        failed = !mbar_wait(mbar, phase, polls);
         phase ^= 1u;
         tc_fence_after();
         if (__syncthreads_or(failed))
@@ -731,8 +734,10 @@ __global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpI
     if (failed) {
         if (t == 0 && args.err)
             atomicOr(args.err, ERR_MMA_TIMEOUT);
-        // drain: the phase that timed out may still complete; wait for it once more (bounded)
-        mbar_wait(mbar, phase ^ 1u);
+        // drain: the MMAs of the phase that timed out may still be running; wait for their completion once more
+        // with the full budget before TMEM is freed (nothing was issued under the test hook)
+        if (!args.hold_mma)
+            mbar_wait(mbar, phase ^ 1u, tc::WAIT_LIMIT);
     }
     tc_fence_before();
     __syncthreads();

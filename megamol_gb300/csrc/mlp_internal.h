@@ -50,6 +50,8 @@ struct MlpInferArgs {
     uint32_t* fallback;             // particle indices whose features left the training range (nullable)
     uint32_t* nfallback;
     uint32_t* err;                  // ERR_* bits (the tensor-core kernel's bounded waits)
+    uint32_t wait_polls;            // polls of each MMA-completion wait before it gives up (0: the default)
+    int hold_mma;                   // test hook: layer 1 is not issued, so its completion wait runs out
 };
 
 // One mip level of the AO volume as an 8-bit UNORM layered 2D texture of slice pairs: layer L holds z slices

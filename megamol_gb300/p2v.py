@@ -58,7 +58,7 @@ class Params(C.Structure):
         ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("tile_z", C.c_int32),
         ("batch_lanes", C.c_int32), ("batch_graph", C.c_int32), ("vector_grid", C.c_int32),
         ("aos_deposit", C.c_int32), ("aos_clip", C.c_int32), ("aos_clip_plane", C.c_float * 4),
-        ("ao_normals", C.c_int32),
+        ("ao_normals", C.c_int32), ("mma_wait_polls", C.c_int32), ("test_hold_mma", C.c_int32),
     ]
 
 

@@ -139,6 +139,26 @@ def test_fallback_outside_training_range_is_the_cone_march(ctx, trained):
     assert same >= nfb
 
 
+def test_mma_wait_runs_out_and_the_context_survives(ctx, trained):
+    """The tensor-core kernel's bounded completion wait: with the test hook its first MMA is never issued, so its
+    mbarrier gets no arrival; after mma_wait_polls polls every CTA records the timeout, frees its TMEM and
+    returns. p2v_run_frame reports P2V_ETIMEOUT, and the next frame on the same context runs normally and gives
+    the bits of a frame before the timeout."""
+    f = synth.lj_liquid(cells=16, res=40, seed=45)
+    nrm = with_normals(ctx, f)
+    before = ao_of(ctx, f, nrm, p2v.AO_LEARNED)
+    set_ao(ctx, f, p2v.AO_LEARNED, mma_wait_polls=64, test_hold_mma=1)
+    ao = np.empty(f.n, np.float32)
+    with pytest.raises(p2v.P2VError) as err:
+        ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm, ao_out=ao)], f.bbox)
+    assert err.value.status == p2v.ETIMEOUT
+    assert ctx.stats()["device_error"] != 0
+    ctx.set_params(mma_wait_polls=0, test_hold_mma=0)
+    after = ao_of(ctx, f, nrm, p2v.AO_LEARNED)
+    assert ctx.stats()["device_error"] == 0
+    assert np.array_equal(before, after)
+
+
 def test_save_load_roundtrip(ctx, trained, tmp_path):
     w = ctx.mlp_get_weights()
     path = str(tmp_path / "ao_mlp.bin")
