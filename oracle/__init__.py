@@ -24,7 +24,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libp2v_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_p2d.so")
-REFERENCE_TREE = os.environ.get("P2V_REFERENCE_TREE", "/root/reference")
+# The MegaMol source tree: P2V_REFERENCE_TREE when set, else a checkout named "reference" beside the repository.
+REFERENCE_TREE = os.environ.get("P2V_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                       "reference")
 
 BUMP, GAUSS3 = 0, 1
 
