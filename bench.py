@@ -155,23 +155,19 @@ def profile_traffic(name: str):
     return None
 
 
+# AO of every workload: 8 cones x 32 steps over a 3-level pyramid of the normalised density, normals down the
+# density gradient computed by the library on the device (ao_normals = 1, P2V_NORMALS_GRADIENT)
 AO_PARAMS = dict(ao_mode=1, ao_volume=0, ao_volume_scale=1.0, ao_cones=8, ao_steps=32, ao_levels=3, ao_apex_deg=50.0,
-                 ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1)
+                 ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1, ao_normals=1)
 
 
 def setup_frame(ctx, f, dparams=None):
-    """Density once (untimed) to derive the workload's normals: unit vectors down the density gradient."""
-    from megamol_gb300 import p2v, synth
+    """The frame's parameters: its grid, cyclic axes, min-max normalisation, the density kernel and the AO."""
+    from megamol_gb300 import p2v
 
     dp = dparams or dict(kernel=p2v.KERNEL_BUMP, sigma=1.0)
-    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], cyclX=1, cyclY=1, cyclZ=1, normalize=1,
-                   ao_mode=p2v.AO_NONE, **dp)
-    V = f.res[0] * f.res[1] * f.res[2]
-    vol = np.empty(V, np.float32)
-    ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
-    nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
+    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], cyclX=1, cyclY=1, cyclZ=1, normalize=1, **dp)
     ctx.set_params(**AO_PARAMS)
-    return vol.reshape(f.res[2], f.res[1], f.res[0]), nrm
 
 
 def cpu_reference_density(f, nthreads: int, kernel: int = 0):
@@ -218,12 +214,13 @@ def cone_kw(f) -> dict:
                 early_exit=AO_PARAMS["ao_early_exit"], border=0, sat_scale=AO_PARAMS["ao_volume_scale"])
 
 
-def cpu_pipeline(f, nthreads, nrm, kernel: int = 0):
+def cpu_pipeline(f, nthreads, kernel: int = 0):
     """One step of the CPU pipeline, every stage timed as it ran: the density on the full frame (the compiled
     reference module where present, else its bit-exact FP32 port), the mip pyramid of the normalised grid
-    (FP32, OpenMP) and the plain cone march (FP32 restatement of the shader in the GPU kernel's operation
-    order, OpenMP) on the AO sample. Returns a dict of measured seconds and particle counts; the step's
-    particles/s combines the measured stage rates: 1 / (t_density / N + t_mip / N + t_ao / S)."""
+    (FP32, OpenMP), and on the AO sample the gradient normals and the plain cone march (FP32 restatements of the
+    library's normals and of the shader in the GPU kernel's operation order, OpenMP). Returns a dict of measured
+    seconds and particle counts; the step's particles/s combines the measured stage rates:
+    1 / (t_density / N + t_mip / N + (t_normals + t_ao) / S)."""
     import oracle
 
     dt_d, kind, vol = cpu_reference_density(f, nthreads, kernel)
@@ -232,12 +229,15 @@ def cpu_pipeline(f, nthreads, nrm, kernel: int = 0):
     lv = oracle.mip_levels_f32(grid, AO_PARAMS["ao_levels"], AO_PARAMS["ao_volume_scale"], nthreads)
     dt_mip = time.perf_counter() - t0
     idx = ao_sample_index(f)
-    xs, ns = np.ascontiguousarray(f.xyzr[idx]), np.ascontiguousarray(nrm[idx])
+    xs = np.ascontiguousarray(f.xyzr[idx])
+    t0 = time.perf_counter()
+    ns = oracle.gradient_normals_f32(grid, f.bbox, f.res, xs, nthreads=nthreads)
+    dt_nrm = time.perf_counter() - t0
     bmin, bsize = cone_geometry(f)
     dirs = oracle.cone_dirs(AO_PARAMS["ao_cones"], np.deg2rad(np.float32(AO_PARAMS["ao_apex_deg"])))
     t0 = time.perf_counter()
     oracle.cone_ao_f32(lv, dirs, xs, ns, bmin, bsize, nthreads=nthreads, **cone_kw(f))
-    dt_ao = time.perf_counter() - t0
+    dt_ao = time.perf_counter() - t0 + dt_nrm
     rate = 1.0 / (dt_d / f.n + dt_mip / f.n + dt_ao / idx.size)
     return dict(value=rate, kind=kind, s_density=dt_d, s_mip=dt_mip, s_ao=dt_ao, particles=f.n,
                 ao_particles=int(idx.size), s_step=dt_d + dt_mip + dt_ao)
@@ -245,8 +245,8 @@ def cpu_pipeline(f, nthreads, nrm, kernel: int = 0):
 
 def cpu_sample_text(r: dict) -> str:
     return (f"measured stages per step: density on the full frame ({r['particles']} particles, "
-            f"{r['s_density']:.2f} s, {r['kind']}), mip pyramid of the full grid ({r['s_mip']:.2f} s), plain "
-            f"cone march (FP32 restatement, OpenMP) on {r['ao_particles']} evenly spaced particles "
+            f"{r['s_density']:.2f} s, {r['kind']}), mip pyramid of the full grid ({r['s_mip']:.2f} s), gradient "
+            f"normals + plain cone march (FP32 restatements, OpenMP) on {r['ao_particles']} evenly spaced particles "
             f"({r['s_ao']:.2f} s); particles/s = 1 / (t_density/N + t_mip/N + t_ao/N_ao), measured rates only")
 
 
@@ -261,13 +261,9 @@ def run_reference(args):
     f, desc = make_workload(args.workload)
     kern = density_params(desc)["kernel"]
     nthreads = os.cpu_count() or 1
-    from megamol_gb300 import synth
-
-    _, _, vol = cpu_reference_density(f, nthreads, kern)
-    nrm = synth.gradient_normals(f.xyzr, np.asarray(vol).reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
     for _ in range(max(0, args.warmup)):
-        cpu_pipeline(f, nthreads, nrm, kern)
-    runs = [cpu_pipeline(f, nthreads, nrm, kern) for _ in range(args.steps)]
+        cpu_pipeline(f, nthreads, kern)
+    runs = [cpu_pipeline(f, nthreads, kern) for _ in range(args.steps)]
     tot = {k: sum(r[k] for r in runs) for k in ("s_density", "s_mip", "s_ao", "s_step")}
     value = 1.0 / (tot["s_density"] / f.n + tot["s_mip"] / f.n + tot["s_ao"] / runs[0]["ao_particles"])
     cpu = dict(runs[0], **{k: v / args.steps for k, v in tot.items()})
@@ -275,7 +271,8 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot["s_step"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip, gradient normals"),
+            "config": dict(desc, ao="plain cone march 8 cones x 32 steps, 3-level mip, normals down the density "
+                                    "gradient"),
             "cpu_baseline": {"value": value, "unit": "particles/s", "cores": nthreads, "kind": runs[0]["kind"],
                              "sample": cpu_sample_text(cpu)},
             "stages_s_per_step": {k: tot[k] / args.steps for k in ("s_density", "s_mip", "s_ao")},
@@ -308,24 +305,20 @@ def train_learned_ao(ctx, f_main, dparams=None, workload: str = "mixed_phase_64M
     else:
         frames = [(make_workload(workload, rank=k)[0], 1_000_000, dparams or bump) for k in (100, 101)]
     for k, (f, npairs, dp) in enumerate(frames):
-        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1, **dp)
-        vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
-        ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
-        nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
-        ctx.set_params(**AO_PARAMS)
-        total = ctx.mlp_collect([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm)], f.bbox, npairs,
-                                seed=100 + k)
+        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], normalize=1, **dp)
+        ctx.set_params(**AO_PARAMS)  # the library's gradient normals: the lists carry none
+        total = ctx.mlp_collect([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, npairs, seed=100 + k)
     rep = ctx.mlp_train(seed=7)
     ctx.set_params(sizex=f_main.res[0], sizey=f_main.res[1], sizez=f_main.res[2], normalize=1, **(dparams or bump),
                    **AO_PARAMS)
     return total, rep
 
 
-def error_figures(ctx, f, dparams, nrm, ao_plain, ao_learned):
+def error_figures(ctx, f, dparams, ao_plain, ao_learned):
     """Errors of the timed frame against the FP64 oracle (untimed): the density of a z-slab (computed from the
     particles that reach it, un-normalised: max|a - b| / max|b| and RMS / max|b|), and the plain and learned
     AO on 2,000 evenly spaced particles against the FP64 cone march over the FP64 pyramid of the GPU's
-    normalised grid (max and RMS)."""
+    normalised grid, with the particles' gradient normals restated in FP32 from that grid (max and RMS)."""
     import oracle
     from megamol_gb300 import p2v, sharding
 
@@ -354,7 +347,8 @@ def error_figures(ctx, f, dparams, nrm, ao_plain, ao_learned):
     bmin, bsize = cone_geometry(f)
     lv = oracle.mip_chain_f64(grid, AO_PARAMS["ao_levels"], AO_PARAMS["ao_volume_scale"])
     dirs = oracle.cone_dirs(AO_PARAMS["ao_cones"], np.deg2rad(np.float32(AO_PARAMS["ao_apex_deg"])))
-    ref_ao = oracle.cone_ao_f64(lv, dirs, f.xyzr[idx], nrm[idx], bmin, bsize, **cone_kw(f))
+    nrm = oracle.gradient_normals_f32(grid, f.bbox, f.res, f.xyzr[idx], nthreads=nthreads)
+    ref_ao = oracle.cone_ao_f64(lv, dirs, f.xyzr[idx], nrm, bmin, bsize, **cone_kw(f))
     out = {"density_vs_fp64": den}
     for name, ao in (("plain_ao_vs_fp64", ao_plain), ("learned_ao_vs_fp64", ao_learned)):
         e = np.abs(ao[idx].astype(np.float64) - ref_ao)
@@ -436,14 +430,13 @@ def run_ours(args):
         pairs, train_rep = train_learned_ao(ctx, f, dparams, args.workload)
         if args.model:
             ctx.mlp_save(args.model)
-    grid0, nrm = setup_frame(ctx, f, dparams)
+    setup_frame(ctx, f, dparams)
     V = f.res[0] * f.res[1] * f.res[2]
     stream = torch.cuda.Stream()
     d_in = torch.from_numpy(f.xyzr).to(dev)
-    d_nrm = torch.from_numpy(nrm).to(dev)
     d_ao = torch.empty(f.n, dtype=torch.float32, device=dev)
     d_out = torch.empty(V, dtype=torch.float32, device=dev)
-    dev_lists = [p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=d_nrm, ao_out=d_ao)]
+    dev_lists = [p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, ao_out=d_ao)]
 
     def barrier():
         if ws > 1:
@@ -485,18 +478,17 @@ def run_ours(args):
 
     # ---- end to end through the public API, host buffers ----
     h_in = torch.from_numpy(f.xyzr).pin_memory()
-    h_nrm = torch.from_numpy(nrm).pin_memory()
     h_ao = torch.empty(f.n, dtype=torch.float32).pin_memory()
     h_out = torch.empty(V, dtype=torch.float32).pin_memory()
-    host_lists = [p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=h_nrm, ao_out=h_ao)]
+    host_lists = [p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, ao_out=h_ao)]
     e2e_steps = max(3, args.steps // 2)
     e2e_ms, _ = time_pipeline(ctx, host_lists, f.bbox, h_out, e2e_steps, 2, stream, torch, barrier, tag="e2e")
     e2e_ms = max_over_ranks(e2e_ms)
-    e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * (16 + 12)),
+    e2e = {"value": ws * f.n / (e2e_ms * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": int(f.n * 16),
            "d2h_bytes_per_step": int(V * 4 + f.n * 4), "ms_per_step": e2e_ms}
 
     # ---- errors of the timed frame against the FP64 oracle (untimed) ----
-    errors = error_figures(ctx, f, dparams, nrm, ao_plain, ao_learn) if rank == 0 else None
+    errors = error_figures(ctx, f, dparams, ao_plain, ao_learn) if rank == 0 else None
 
     # ---- roofline: algorithmic bytes per stage / its device time; the dominant stage's kernel ----
     peak, peak_kind = peaks()
@@ -539,7 +531,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1:
         nthreads = os.cpu_count() or 1
-        r = cpu_pipeline(f, nthreads, nrm, dparams["kernel"])
+        r = cpu_pipeline(f, nthreads, dparams["kernel"])
         cpu = {"value": r["value"], "unit": "particles/s", "cores": nthreads, "kind": r["kind"],
                "sample": cpu_sample_text(r)}
 
@@ -560,7 +552,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP: bf16 x bf16 -> f32)", "data": "synthetic",
                 "config": dict(desc, ao=("learned AO (MLP 78-64-64-1 on cone samples, BF16 tensor cores) with "
                                          "cone-march fallback" if use_learned else "plain cone march") +
-                                        ", 8 cones x 32 steps, 3-level mip, gradient normals",
+                                        ", 8 cones x 32 steps, 3-level mip, normals down the density gradient (library)",
                                l2=f"per-step working set ~{(f.n * 84 + V * 12) / 2 ** 30:.1f} GiB > 126 MiB L2 "
                                   "(no flush)"),
                 "learned_vs_plain": {"plain_particles_per_s": ws * f.n / (ms_plain * 1e-3), "plain_ms": ms_plain,
@@ -605,29 +597,23 @@ def run_batch_bench(args):
     dev = torch.cuda.current_device()
     traj = synth.trajectory(frames=64, seed=3 + 1000 * rank)
     ctx = p2v.Context(dev)
-    # setup (untimed): gradient normals from each frame's own density
+    # inputs (untimed): positions only, the normals come from each frame's own density inside the pipeline
     frames_dev, frames_host, total = [], [], 0
     for f in traj:
-        ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], ao_mode=p2v.AO_NONE, normalize=1,
-                       kernel=p2v.KERNEL_BUMP, sigma=1.0)
-        vol = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
-        ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, vol)
-        nrm = synth.gradient_normals(f.xyzr, vol.reshape(f.res[2], f.res[1], f.res[0]), f.bbox)
         V = f.res[0] * f.res[1] * f.res[2]
         d_in = torch.from_numpy(f.xyzr).to(dev)
-        d_n = torch.from_numpy(nrm).to(dev)
         d_ao = torch.empty(f.n, dtype=torch.float32, device=dev)
         d_out = torch.empty(V, dtype=torch.float32, device=dev)
-        frames_dev.append(dict(lists=[p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=d_n,
-                                                       ao_out=d_ao)], bbox=f.bbox, out=d_out, size=f.res))
+        frames_dev.append(dict(lists=[p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, ao_out=d_ao)],
+                               bbox=f.bbox, out=d_out, size=f.res))
         h_in = torch.from_numpy(f.xyzr).pin_memory()
-        h_n = torch.from_numpy(nrm).pin_memory()
         h_ao = torch.empty(f.n, dtype=torch.float32).pin_memory()
         h_out = torch.empty(V, dtype=torch.float32).pin_memory()
-        frames_host.append(dict(lists=[p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, normals=h_n,
-                                                        ao_out=h_ao)], bbox=f.bbox, out=h_out, size=f.res))
+        frames_host.append(dict(lists=[p2v.ParticleList(h_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, ao_out=h_ao)],
+                                bbox=f.bbox, out=h_out, size=f.res))
         total += f.n
-    ctx.set_params(normalize=1, batch_graph=1, tile_x=0, tile_y=0, tile_z=0, batch_lanes=0, **AO_PARAMS)
+    ctx.set_params(normalize=1, batch_graph=1, tile_x=0, tile_y=0, tile_z=0, batch_lanes=0, kernel=p2v.KERNEL_BUMP,
+                   sigma=1.0, **AO_PARAMS)
     tune = ctx.autotune_batch(frames_dev)
 
     def barrier():
@@ -671,7 +657,7 @@ def run_batch_bench(args):
         t = torch.tensor([ms, ms_e2e], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms, ms_e2e = float(t[0]), float(t[1])
-    h2d = sum(f.n * (16 + 12) for f in traj)
+    h2d = sum(f.n * 16 for f in traj)
     d2h = sum(f.n * 4 + f.res[0] * f.res[1] * f.res[2] * 4 for f in traj)
     if rank == 0:
         line = {"metric": "particles/s density+AO (batched trajectory)", "value": ws * total / (ms * 1e-3),
@@ -679,7 +665,7 @@ def run_batch_bench(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "trajectory_64", "frames": len(traj), "particles": total,
                            "particles_per_frame": "log-uniform [50k, 2M]", "grids": sorted({f.res[0] for f in traj}),
-                           "ao": "plain cone march, 8 cones x 32 steps, 3-level mip, gradient normals",
+                           "ao": "plain cone march, 8 cones x 32 steps, 3-level mip, normals down the density gradient (library)",
                            "l2": "per-step working set several GB > 126 MB L2 (no flush)"},
                 "batch": {"autotuned_tile": tune["tile"], "autotuned_lanes": tune["lanes"],
                           "ms_graph": ms, "ms_eager": ms_eager, "ms_frame_by_frame": ms_seq,

@@ -74,6 +74,9 @@ def lib() -> C.CDLL:
         f.p2vo_cone_steps.restype = C.c_int
         f.p2vo_cone_ao_f64.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_int32), C.c_int, C.c_void_p, C.c_int,
                                        C.POINTER(_ConeParams), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        f.p2vo_gradient_normals_f32.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                                C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.c_int64,
+                                                C.c_int, C.c_void_p]
         f.p2vo_mip_levels_f32.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_float, C.c_int,
                                           C.POINTER(C.c_void_p), C.c_int]
         f.p2vo_cone_ao_f32.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_int32), C.c_int, C.c_void_p, C.c_int,
@@ -527,6 +530,23 @@ def cone_ao_f64(levels, dirs, xyzr, normals, bounds_min, bounds_size, **kw) -> n
     cp = _cone_params(bounds_min, bounds_size, **kw)
     lib().p2vo_cone_ao_f64(ptrs, dims, len(lv), d.ctypes.data, d.shape[0], C.byref(cp), x.ctypes.data,
                            nrm.ctypes.data, x.shape[0], out.ctypes.data)
+    return out
+
+
+def gradient_normals_f32(grid, bbox, res, xyzr, cyclic=(1, 1, 1), nthreads: int = 1) -> np.ndarray:
+    """The library's P2V_NORMALS_GRADIENT normals restated in FP32 (OpenMP): unit vectors down the density
+    gradient of the node grid (z, y, x) at each particle, (n, 3) float32; zero where the gradient vanishes. The
+    node origin is the box minimum and the spacing the reference's float(|max - min|) / float(res - 1)."""
+    g = np.ascontiguousarray(grid, np.float32)
+    x = _xyzr(xyzr)
+    f = np.float32
+    h = [f(abs(f(bbox[a + 3]) - f(bbox[a]))) / f(res[a] - 1) for a in range(3)]
+    out = np.zeros((x.shape[0], 3), np.float32)
+    lib().p2vo_gradient_normals_f32(g.ctypes.data, (C.c_int32 * 3)(*[int(r) for r in res]),
+                                    (C.c_int32 * 3)(*[int(c) for c in cyclic]),
+                                    (C.c_float * 3)(*[float(bbox[a]) for a in range(3)]),
+                                    (C.c_float * 3)(*[float(v) for v in h]), x.ctypes.data, x.shape[0],
+                                    int(nthreads), out.ctypes.data)
     return out
 
 

@@ -636,6 +636,72 @@ extern "C" void p2vo_cone_ao_f32(const float* const* levels, const int32_t* ldim
     }
 }
 
+/* ------------------------------------------------------------------------------------------------
+ * Normals down the density gradient (the library's P2V_NORMALS_GRADIENT, restated in FP32 with OpenMP):
+ * -grad(rho) at each particle from the node grid's central differences (periodic along cyclic axes,
+ * one-sided first differences at the faces of open ones), trilinear at u = (p - min) / h clamped into the
+ * node range, normalised; zero where the gradient vanishes.
+ * ---------------------------------------------------------------------------------------------- */
+namespace {
+inline float node_grad_f32(const float* g, int64_t base, int64_t stride, int i, int s, int cyc, float ih) {
+    if (s < 2)
+        return 0.0f;
+    int lo = i - 1, hi = i + 1;
+    float scale = 0.5f * ih;
+    if (cyc) {
+        lo = lo < 0 ? lo + s : lo;
+        hi = hi >= s ? hi - s : hi;
+    } else if (i == 0) {
+        lo = 0;
+        scale = ih;
+    } else if (i == s - 1) {
+        hi = s - 1;
+        scale = ih;
+    }
+    return (g[base + hi * stride] - g[base + lo * stride]) * scale;
+}
+}  // namespace
+
+extern "C" void p2vo_gradient_normals_f32(const float* grid, const int32_t res[3], const int32_t cyc[3],
+    const float minf[3], const float h[3], const float* xyzr, int64_t n, int nthreads, float* out3) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t j = 0; j < n; ++j) {
+        const float* p = xyzr + 4 * j;
+        int i0[3], i1[3];
+        float f[3], ih[3];
+        for (int a = 0; a < 3; ++a) {
+            ih[a] = 1.0f / h[a];
+            float u = (p[a] - minf[a]) * ih[a];
+            u = std::min(std::max(u, 0.0f), (float) (res[a] - 1));
+            if (!(u == u))
+                u = 0.0f;
+            const int k = std::min((int) u, res[a] - 1);
+            i0[a] = k;
+            i1[a] = std::min(k + 1, res[a] - 1);
+            f[a] = u - (float) k;
+        }
+        const int64_t sx = res[0], sxy = (int64_t) res[0] * res[1];
+        float gr[3] = {0.0f, 0.0f, 0.0f};
+        for (int c = 0; c < 8; ++c) {
+            const int x = (c & 1) ? i1[0] : i0[0], y = (c & 2) ? i1[1] : i0[1], z = (c & 4) ? i1[2] : i0[2];
+            const float w = ((c & 1) ? f[0] : 1.0f - f[0]) * ((c & 2) ? f[1] : 1.0f - f[1]) * ((c & 4) ? f[2] : 1.0f - f[2]);
+            gr[0] += w * node_grad_f32(grid, z * sxy + y * sx, 1, x, res[0], cyc[0], ih[0]);
+            gr[1] += w * node_grad_f32(grid, z * sxy + x, sx, y, res[1], cyc[1], ih[1]);
+            gr[2] += w * node_grad_f32(grid, y * sx + x, sxy, z, res[2], cyc[2], ih[2]);
+        }
+        const float l2 = gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2];
+        float* o = out3 + 3 * j;
+        if (l2 > 0.0f && std::isfinite(l2)) {
+            const float il = -1.0f / std::sqrt(l2);
+            o[0] = gr[0] * il;
+            o[1] = gr[1] * il;
+            o[2] = gr[2] * il;
+        } else {
+            o[0] = o[1] = o[2] = 0.0f;
+        }
+    }
+}
+
 extern "C" void p2vo_aosphere_volume_ex_f64(const float* xyzr, int64_t n, const float clip[6], const int32_t s[3],
     float gen_fac, int glsl_rule, int use_clip, const float plane[4], double* tex) {
     // AOSphereRenderer.cpp:918-1021 (CPU rule) and :1026-1221 with volume_updateVolume.vert.glsl:22-46 (GLSL

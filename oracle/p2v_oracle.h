@@ -96,6 +96,11 @@ void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldims, int nle
 
 /* AOSphereRenderer volume deposit (AOSphereRenderer.cpp:918-1021): s = "vol::size" including the
  * 1-voxel zero border; tex gets (4/3 pi r^3 / voxel volume) * genFac in the inner voxel of each particle. */
+/* The library's gradient normals (P2V_NORMALS_GRADIENT) in FP32 with OpenMP: -grad(rho) / |grad(rho)| at each
+ * particle (out3: n x 3 floats) from the node grid (x fastest, res), cyclic flags, node origin minf and the
+ * reference spacing h per axis. */
+void p2vo_gradient_normals_f32(const float* grid, const int32_t res[3], const int32_t cyc[3], const float minf[3],
+    const float h[3], const float* xyzr, int64_t n, int nthreads, float* out3);
 /* AOSphere volume deposit with the renderer's two rules: glsl_rule 0 = createVolumeCPU (inner voxel +1, optional
  * clip-plane discard of particles with dot(p, n) - d >= 0), 1 = createVolumeGLSL (x, y: floor clamped to
  * [0, s_inner] without the border offset; z: slice trunc clamped to [0, s_inner - 1], + 1; no clip). */

@@ -68,3 +68,16 @@ def test_cone_features_known_answers():
     z = oracle.cone_features_f64([L * 0 for L in levels], dirs, t, lod, xyzr, nrm, (0, 0, 0), (1 / 32,) * 3)
     assert np.all(z[:, :ns] == 0)
     assert oracle.mlp_feature_steps(32) == [0, 4, 8, 12, 16, 19, 23, 27, 31]
+
+
+def test_gradient_normals_f32_match_host_normals():
+    """The FP32 restatement of the library's gradient normals (the CPU baseline's normals stage) against the
+    host's FP64 normals of the workloads (synth.gradient_normals): the same unit vectors up to rounding."""
+    f = synth.lj_liquid(cells=20, res=48, seed=33)
+    vol = oracle.density_f32(f.xyzr, f.bbox, f.res, (1, 1, 1), 1.0, oracle.BUMP, 2)
+    vol, _, _ = oracle.normalize_minmax_f32(vol)
+    g = vol.reshape(48, 48, 48)
+    a = oracle.gradient_normals_f32(g, f.bbox, f.res, f.xyzr, nthreads=2)
+    b = synth.gradient_normals(f.xyzr, g, f.bbox)
+    assert np.abs(np.linalg.norm(a, axis=1) - 1).max() <= 1e-5
+    assert np.abs(a - b).max() <= 1e-3 and np.sqrt(np.mean((a - b) ** 2)) <= 1e-5
