@@ -31,8 +31,8 @@ struct ConeParams {
     float4 dirs[MAX_CONES];        // xyz around +Y, w = cone width
     float t[MAX_STEPS], lod[MAX_STEPS];
     ConeLevel lv[MAX_LEVELS];
-    // learned AO: the march steps its features sample (per cone), and 8-bit paired-slice layered textures of
-    // the mip levels those samples read (0 = level not needed)
+    // learned AO: the march steps its features sample (per cone), and 8-bit 3D textures of the mip levels
+    // those samples read (0 = level not needed)
     int nfsteps;
     int fstep[MAX_FSTEPS];
     unsigned long long ftex[MAX_LEVELS];

@@ -50,21 +50,14 @@ __device__ __forceinline__ float sigmoidf_(float a) {
     return 1.0f / (1.0f + __expf(-a));
 }
 
-// GL LINEAR sample of one mip level at normalised point q through its paired-slice texture: one bilinear
-// fetch (CLAMP_TO_BORDER in x and y) returns slices z0 and z0 + 1 around the sample's z (layer z0 + 1), and
-// the z interpolation runs in FP32 with the sample's own fraction; layers outside the level are 0, as the
-// border. The texels are 8-bit UNORM (the MDAO volume's own R8 format) and the texture units weight x and y
-// with 8-bit fractions: the features feed a BF16 network and training pairs are extracted by the same code
-// (measured on the CPU: the same test RMSE as FP32 texels on the LJ, uniform and mixed-phase frames).
-__device__ __forceinline__ float feature_tex_sample(unsigned long long tex, int nz, float qx, float qy, float qz) {
-    const float zs = fmaf(qz, (float) nz, -0.5f);
-    const float z0f = floorf(zs);
-    const float fz = zs - z0f;
-    const int layer = (int) z0f + 1;
-    if (layer < 0 || layer > nz)
-        return 0.0f;
-    const float2 t = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, layer);
-    return fmaf(fz, t.y - t.x, t.x);
+// GL LINEAR sample of one mip level at normalised point q through its 3D texture: one trilinear fetch
+// (CLAMP_TO_BORDER with border 0, texel centres at (i + 0.5) / N). The texels are 8-bit UNORM (the MDAO volume's
+// own R8 format) and the texture units weight with 8-bit fractions: the features feed a BF16 network and
+// training pairs are extracted by the same code (measured on the CPU: the same test RMSE as FP32 texels on the
+// LJ, uniform and mixed-phase frames). A 3D texture keeps the samples of a warp's neighbouring particles in the
+// same cached blocks along z as well.
+__device__ __forceinline__ float feature_tex_sample(unsigned long long tex, float qx, float qy, float qz) {
+    return tex3D<float>((cudaTextureObject_t) tex, qx, qy, qz);
 }
 
 // Feature sample j of a cone with direction dir from normalised point u: the march's step fstep[j] at its
@@ -76,9 +69,9 @@ __device__ __forceinline__ float feature_sample(const ConeParams& cp, const floa
     const float qx = fmaf(t, dir[0], u[0]), qy = fmaf(t, dir[1], u[1]), qz = fmaf(t, dir[2], u[2]);
     const int l0 = min((int) lod, cp.nlevels - 1);
     const float fr = lod - (float) l0;
-    float v = feature_tex_sample(cp.ftex[l0], cp.lv[l0].d[2], qx, qy, qz);
+    float v = feature_tex_sample(cp.ftex[l0], qx, qy, qz);
     if (fr > 0.0f && l0 + 1 < cp.nlevels)
-        v = fmaf(fr, feature_tex_sample(cp.ftex[l0 + 1], cp.lv[l0 + 1].d[2], qx, qy, qz) - v, v);
+        v = fmaf(fr, feature_tex_sample(cp.ftex[l0 + 1], qx, qy, qz) - v, v);
     return v;
 }
 
@@ -105,26 +98,18 @@ __device__ __forceinline__ bool particle_frame(const ConeParams& cp, const float
     return true;
 }
 
-// Layer L of the paired texture = (slice L - 1, slice L) of level (dx, dy, dz), L in [0, dz], as 8-bit UNORM of
-// the texel clamped to [0, 1] (level-0 saturation clamp(v * sat, 0, 1) applied first when sat > 0).
+// Level (dx, dy, dz) into its 3D texture as 8-bit UNORM of the texel clamped to [0, 1] (level-0 saturation
+// clamp(v * sat, 0, 1) applied first when sat > 0).
 __global__ void __launch_bounds__(256) fill_feature_tex_kernel(const float* __restrict__ src, int dx, int dy, int dz,
                                                                float sat, unsigned long long surf) {
-    const int64_t n = (int64_t) dx * dy * (dz + 1);
+    const int64_t n = (int64_t) dx * dy * dz;
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
-        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), L = (int) (i / ((int64_t) dx * dy));
-        unsigned char q[2];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const int z = L - 1 + c;
-            float v = 0.0f;
-            if (z >= 0 && z < dz) {
-                v = src[((int64_t) z * dy + y) * dx + x];
-                if (sat > 0.0f)
-                    v = v * sat;
-            }
-            q[c] = (unsigned char) __float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f);
-        }
-        surf2DLayeredwrite(make_uchar2(q[0], q[1]), (cudaSurfaceObject_t) surf, x * (int) sizeof(uchar2), y, L);
+        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), z = (int) (i / ((int64_t) dx * dy));
+        float v = src[i];
+        if (sat > 0.0f)
+            v = v * sat;
+        const unsigned char q = (unsigned char) __float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f);
+        surf3Dwrite(q, (cudaSurfaceObject_t) surf, x * (int) sizeof(unsigned char), y, z);
     }
 }
 
@@ -758,10 +743,9 @@ cudaError_t FeatureTex::ensure(const int dims[3]) {
     if (arr && d[0] == dims[0] && d[1] == dims[1] && d[2] == dims[2])
         return cudaSuccess;
     release();
-    cudaChannelFormatDesc fmt = cudaCreateChannelDesc<uchar2>();
-    // dims[2] + 1 layers of slice pairs (slice L - 1, slice L)
-    cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2] + 1),
-                                      cudaArrayLayered | cudaArraySurfaceLoadStore);
+    cudaChannelFormatDesc fmt = cudaCreateChannelDesc<unsigned char>();
+    cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2]),
+                                      cudaArraySurfaceLoadStore);
     if (e != cudaSuccess) {
         arr = nullptr;
         return e;
@@ -805,7 +789,7 @@ void FeatureTex::release() {
 }
 
 cudaError_t launch_fill_feature_tex(const ConeLevel& L, float sat, const FeatureTex& t, cudaStream_t st) {
-    const int64_t n = (int64_t) L.d[0] * L.d[1] * (L.d[2] + 1);
+    const int64_t n = (int64_t) L.d[0] * L.d[1] * L.d[2];
     const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
     fill_feature_tex_kernel<<<grd, 256, 0, st>>>(L.v, L.d[0], L.d[1], L.d[2], sat, t.surf);
     return cudaGetLastError();

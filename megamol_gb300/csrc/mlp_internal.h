@@ -54,10 +54,8 @@ struct MlpInferArgs {
     int hold_mma;                   // test hook: layer 1 is not issued, so its completion wait runs out
 };
 
-// One mip level of the AO volume as an 8-bit UNORM layered 2D texture of slice pairs: layer L holds z slices
-// L - 1 (red) and L (green), so one bilinear fetch (GL LINEAR in x and y, CLAMP_TO_BORDER, normalised
-// coordinates) returns both slices around a sample's z. Written through a surface; the learned AO's features
-// sample it with the texture units.
+// One mip level of the AO volume as an 8-bit UNORM 3D texture (GL LINEAR, CLAMP_TO_BORDER, normalised
+// coordinates), written through a surface; the learned AO's features sample it with the texture units.
 struct FeatureTex {
     cudaArray_t arr = nullptr;
     unsigned long long tex = 0;   // cudaTextureObject_t
