@@ -191,6 +191,12 @@ typedef struct p2v_params {
                                P2V_ETIMEOUT; 0 = the default (2^20, about a second) */
     int32_t test_hold_mma;  /* test hook: the learned AO's first MMA is not issued, so its bounded wait runs out and
                                the call returns P2V_ETIMEOUT with the context still usable (0) */
+    /* --- z-slab output (a rank's share of one large frame) --- */
+    int32_t slab_z0, slab_z1; /* compute and return only grid planes [slab_z0, slab_z1) of the sizez planes; both 0 =
+                                 the whole grid. The node positions stay those of the whole grid; the returned volume
+                                 holds the slab (resolution z = slab_z1 - slab_z0, origin z moved to plane slab_z0),
+                                 its statistics and normalisation cover the slab only. Density and intensity
+                                 aggregators without AO (0, 0) */
 } p2v_params;
 
 /* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,
@@ -272,6 +278,16 @@ P2V_API p2v_status p2v_get_params(const p2v_ctx* ctx, p2v_params* p);
  * (a cudaStream_t, NULL = the context's stream): on return `vol` is filled and every host output is
  * written. Mirrors ParticlesToDensity::getDataCallback for IDX_GET_DATA. */
 P2V_API p2v_status p2v_run_frame(p2v_ctx* ctx, const p2v_frame* frame, p2v_volume* vol, void* stream);
+
+/* AO of a frame's particles against a density grid the caller supplies (sizex * sizey * sizez floats, x fastest,
+ * the nodes of the frame's box as p2v_run_frame places them; host or device memory per mem) instead of the grid
+ * of the frame's own particles: the grid the cone march and the AOSphere taps sample, and the gradient normals'
+ * grid. For a rank that holds only part of a frame's particles but the frame's whole (gathered) grid, and for
+ * callers that already hold a volume. No counterpart in the reference, whose AO samples a volume it builds itself
+ * (MDAOVolumeGenerator, AOSphereRenderer). Needs an AO mode, aggregator 0 and no z-slab; writes each list's
+ * ao_out. Synchronous on `stream` as p2v_run_frame. */
+P2V_API p2v_status p2v_run_ao_on_grid(p2v_ctx* ctx, const p2v_frame* frame, const float* grid, int32_t mem,
+                                      void* stream);
 
 /* Device pointer of the last density grid (valid until the next call on this context); the reference's
  * VolumetricDataCall cannot carry one, so this is an addition of this library. */

@@ -149,6 +149,7 @@ struct Pipe {
 struct FrameJob {
     uint64_t N = 0;
     int32_t res[3] = {0, 0, 0};
+    int32_t zlo = 0, zcount = 0;    // the z-slab the grid holds (zcount = res[2]: the whole grid)
     float bb[6] = {};
     const float* dgrid = nullptr;
     const uint32_t* order = nullptr;
@@ -197,6 +198,9 @@ struct p2v_ctx {
     int tuned_tile[3] = {0, 0, 0};
     int tuned_lanes = 0;
     // learned AO
+    // p2v_run_ao_on_grid: the density grid the AO stage reads instead of this frame's own (null: none)
+    const float* ext_grid = nullptr;
+    int ext_grid_mem = P2V_MEM_HOST;
     DevBuf mlp_P, mlp_m, mlp_v, mlp_g, mlp_part, mlp_ploss, mlp_loss, mlp_w1h, mlp_w2h, mlp_lo, mlp_hi, mlp_idx,
         mlp_y;
     DevBuf tX, tT;                       // collected training pairs
@@ -429,7 +433,19 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     g.nbins = (uint32_t) nb;
     g.sigma = P.sigma;
     g.kernel = P.kernel;
-    const uint64_t V = (uint64_t) res[0] * res[1] * res[2];
+    // the planes computed: a z-slab of the grid, or all of it
+    g.zlo = 0;
+    g.zhi = res[2];
+    if (P.slab_z0 != 0 || P.slab_z1 != 0) {
+        if (P.slab_z0 < 0 || P.slab_z1 <= P.slab_z0 || P.slab_z1 > res[2])
+            return fail(P2V_EINVAL, "slab [%d, %d) is not a non-empty range of the %d planes", P.slab_z0, P.slab_z1,
+                        res[2]);
+        if (agg == 2 || P.ao_mode != P2V_AO_NONE)
+            return fail(P2V_EUNSUPPORTED, "a z-slab serves the density and intensity aggregators without AO");
+        g.zlo = P.slab_z0;
+        g.zhi = P.slab_z1;
+    }
+    const uint64_t V = (uint64_t) res[0] * res[1] * (uint64_t) (g.zhi - g.zlo);
     const uint64_t VC = V * (uint64_t) comps;
 
     uint64_t N = 0;
@@ -686,7 +702,12 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     if (wnc)
         P2V_CUDA_TRY(launch_permute_weights(sb.vals[sb.result], pp.wts.as<float>(), pp.wsorted.as<float>(), n, wnc, sms,
                                             st));
-    {
+    if (ext_grid) {
+        // p2v_run_ao_on_grid: the caller's grid stands in for this frame's density (no gather, no statistics)
+        P2V_CUDA_TRY(cudaMemcpyAsync(dgrid, ext_grid, sizeof(float) * V,
+                                     ext_grid_mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                     st));
+    } else {
         // aggregator 0: the density; 1: the intensity-weighted sums; 2: three direction-weighted passes into
         // the interleaved vector volume and the plain kernel sums (the weights) into wsum
         const int passes = agg == 2 ? 4 : 1;
@@ -737,7 +758,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
             P2V_CUDA_TRY(launch_sort(vs, (uint32_t) V, 0xFFFFFFFFu, sms, st));
             vg_order = vs.vals[vs.result];
         }
-    } else {
+    } else if (!ext_grid) {
         P2V_CUDA_TRY(launch_finalize(tiles.as<TileStats>(), ntiles, fs, P.mass_normalize, P.normalize, 0.0, voxel_volume,
                                      st));
         P2V_CUDA_TRY(launch_normalize_modes(dgrid, V, fs, P.mass_normalize, P.normalize, sms, st));
@@ -788,6 +809,8 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     job.N = N;
     for (int a = 0; a < 3; ++a)
         job.res[a] = res[a];
+    job.zlo = g.zlo;
+    job.zcount = g.zhi - g.zlo;
     std::memcpy(job.bb, bb, sizeof(bb));
     job.dgrid = dgrid;
     job.order = sb.vals[sb.result];
@@ -836,6 +859,7 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
     pp.last_nbins = job.nbins;
     for (int a = 0; a < 3; ++a)
         last_res[a] = (uint64_t) res[a];
+    last_res[2] = (uint64_t) job.zcount;  // the planes the grid holds (a z-slab or all)
     stats = p2v_stats{};
     stats.particles_in = N;
     stats.particles_binned = hs.n_valid;
@@ -874,6 +898,11 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
             vol->extents[a] = rangef;
             vol->slice_dists[a] = rangef / static_cast<float>(res[a] - 1);
             vol->origin[a] = bb[a];
+        }
+        if (job.zcount != res[2]) {  // a z-slab: its planes, first plane and extent
+            vol->resolution[2] = (uint64_t) job.zcount;
+            vol->origin[2] = bb[2] + static_cast<float>(job.zlo) * vol->slice_dists[2];
+            vol->extents[2] = static_cast<float>(job.zcount - 1) * vol->slice_dists[2];
         }
         std::memcpy(vol->bbox, bb, sizeof(float) * 6);
         vol->components = (uint64_t) job.components;
@@ -1484,6 +1513,7 @@ void p2v_params_default(p2v_params* p) {
     p->ao_normals = P2V_NORMALS_LIST;
     p->mma_wait_polls = 0;
     p->test_hold_mma = 0;
+    p->slab_z0 = p->slab_z1 = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {
@@ -1559,6 +1589,19 @@ p2v_status p2v_run_frame(p2v_ctx* c, const p2v_frame* fr, p2v_volume* vol, void*
         return P2V_EINVAL;
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
     return c->run_frame(fr, vol, st);
+}
+
+p2v_status p2v_run_ao_on_grid(p2v_ctx* c, const p2v_frame* fr, const float* grid, int32_t mem, void* stream) {
+    if (!c || !fr || !grid || (mem != P2V_MEM_HOST && mem != P2V_MEM_DEVICE))
+        return P2V_EINVAL;
+    if (c->prm.ao_mode == P2V_AO_NONE || c->prm.aggregator != 0 || c->prm.slab_z0 != 0 || c->prm.slab_z1 != 0)
+        return c->fail(P2V_EINVAL, "p2v_run_ao_on_grid needs an AO mode, the density aggregator and no z-slab");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    c->ext_grid = grid;
+    c->ext_grid_mem = mem;
+    const p2v_status s = c->run_frame(fr, nullptr, st);
+    c->ext_grid = nullptr;
+    return s;
 }
 
 p2v_status p2v_run_batch(p2v_ctx* c, const p2v_batch_item* items, uint32_t count, p2v_stats* stats, void* stream) {

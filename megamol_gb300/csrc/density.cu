@@ -59,8 +59,9 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
     const int t = threadIdx.x;
     const int ty = t % TY;
     const int tz = t / TY;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-    const bool row_in = (y0 + ty < g.s[1]) && (z0 + tz < g.s[2]);
+    // tiles cover the slab [zlo, zhi) of the grid (z tile index offset by the slab's first tile)
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = (blockIdx.z + g.zlo / TZ) * TZ;
+    const bool row_in = (y0 + ty < g.s[1]) && (z0 + tz >= g.zlo) && (z0 + tz < g.zhi);
     const int T3[3] = {TX, TY, TZ};
 
 #pragma unroll
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(TY* TZ, 2) gather_kernel(GridGeo g, const floa
     double dsum = 0.0;
     float vmin = INFINITY, vmax = -INFINITY;
     if (row_in) {
-        float* out = grid + ((size_t) (z0 + tz) * g.s[1] + (y0 + ty)) * g.s[0] + x0;
+        float* out = grid + ((size_t) (z0 + tz - g.zlo) * g.s[1] + (y0 + ty)) * g.s[0] + x0;
 #pragma unroll
         for (int k = 0; k < TX; ++k) {
             if (x0 + k < g.s[0]) {
@@ -454,7 +455,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     const int t = threadIdx.x;
     const uint32_t lane = t & 31u;
     const uint32_t warp = t >> 5;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    // tiles cover the slab [zlo, zhi) of the grid (z tile index offset by the slab's first tile)
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = (blockIdx.z + g.zlo / TZ) * TZ;
     const int T3[3] = {TX, TY, TZ};
     const int o3[3] = {x0, y0, z0};
     for (int n = t; n < NN; n += NT) {
@@ -695,11 +697,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     float vmin = INFINITY, vmax = -INFINITY;
     for (int n = t; n < NN; n += NT) {
         const int x = n % TX, y = (n / TX) % TY, z = n / (TX * TY);
-        if (x0 + x < g.s[0] && y0 + y < g.s[1] && z0 + z < g.s[2]) {
+        if (x0 + x < g.s[0] && y0 + y < g.s[1] && z0 + z >= g.zlo && z0 + z < g.zhi) {
             const float v = ACC == ACC_FIXED_W ? __ll2float_rn((long long) acc64[n]) * winv
                             : ACC == ACC_DOUBLE ? __double2float_rn(accd[n])
                                                 : __ull2float_rn(((unsigned long long) acc_hi[n] << 32) | acc_lo[n]) * FIX_INV;
-            grid[(((size_t) (z0 + z) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)) * (size_t) ostride] = v;
+            grid[(((size_t) (z0 + z - g.zlo) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)) * (size_t) ostride] = v;
             dsum += (double) v;
             vmin = fminf(vmin, v);
             vmax = fmaxf(vmax, v);
@@ -853,8 +855,13 @@ size_t gather_smem_bytes(const GatherConfig& c) {
            (size_t) (2 * c.rmax + 1) * sizeof(uint32_t);
 }
 
+// z tiles of the slab [zlo, zhi): from the tile holding plane zlo to the one holding plane zhi - 1
+uint32_t gather_tiles_z(const GatherConfig& c, const GridGeo& g) {
+    return ceil_div((uint32_t) g.zhi, (uint32_t) c.tz) - (uint32_t) (g.zlo / c.tz);
+}
+
 uint32_t gather_tile_count(const GatherConfig& c, const GridGeo& g) {
-    return ceil_div(g.s[0], c.tx) * ceil_div(g.s[1], c.ty) * ceil_div(g.s[2], c.tz);
+    return ceil_div(g.s[0], c.tx) * ceil_div(g.s[1], c.ty) * gather_tiles_z(c, g);
 }
 
 namespace {
@@ -865,7 +872,7 @@ cudaError_t launch_tiles(K kern, const GatherConfig& c, const GridGeo& g, int nt
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess)
         return e;
-    dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), ceil_div(g.s[2], c.tz));
+    dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), gather_tiles_z(c, g));
     kern<<<grd, nt, smem, st>>>(g, rec_a, rec_b, start, grid, tiles, fs, c.rmax, w.w, w.wstride,
                                 w.ostride > 0 ? w.ostride : 1);
     return cudaGetLastError();
@@ -906,7 +913,7 @@ cudaError_t launch_gather(const GatherConfig& c, const GridGeo& g, const float4*
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess)
         return e;
-    dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), ceil_div(g.s[2], c.tz));
+    dim3 grd(ceil_div(g.s[0], c.tx), ceil_div(g.s[1], c.ty), gather_tiles_z(c, g));
     kern<<<grd, c.ty * c.tz, smem, st>>>(g, rec_a, rec_b, start, grid, tiles, fs, c.smax, c.rmax);
     return cudaGetLastError();
 }

@@ -28,6 +28,7 @@ struct GridGeo {
     int32_t kernel;      // 0 bump, 1 gauss3
     uint32_t nb[3];      // bins per axis = res + 2 (underflow and overflow bins)
     uint32_t nbins;      // nb[0]*nb[1]*nb[2]
+    int32_t zlo, zhi;    // the grid planes computed and written: [zlo, zhi) (a z-slab; 0, s[2] = all)
 };
 
 // Per-frame device scalars written by the binning stage and read by later stages.

@@ -59,6 +59,7 @@ class Params(C.Structure):
         ("batch_lanes", C.c_int32), ("batch_graph", C.c_int32), ("vector_grid", C.c_int32),
         ("aos_deposit", C.c_int32), ("aos_clip", C.c_int32), ("aos_clip_plane", C.c_float * 4),
         ("ao_normals", C.c_int32), ("mma_wait_polls", C.c_int32), ("test_hold_mma", C.c_int32),
+        ("slab_z0", C.c_int32), ("slab_z1", C.c_int32),
     ]
 
 
@@ -149,6 +150,7 @@ _SIGNATURES = {
                               C.POINTER(C.c_uint32), C.POINTER(C.c_float)], C.c_int),
     "p2v_host_alloc": ([C.c_uint64], C.c_void_p),
     "p2v_host_free": ([C.c_void_p], None),
+    "p2v_run_ao_on_grid": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int),
     "p2v_run_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p], C.c_int),
     "p2v_autotune_batch": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(TuneReportC)], C.c_int),
     "p2v_get_ao_volume": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_int32)],
@@ -451,6 +453,13 @@ class Context:
         return dict(resolution=list(vol.resolution), components=int(vol.components),
                     slice_dists=list(vol.slice_dists), origin=list(vol.origin), extents=list(vol.extents),
                     min_value=vol.min_value, max_value=vol.max_value, bbox=list(vol.bbox), data_hash=vol.data_hash)
+
+    def run_ao_on_grid(self, lists: Sequence[ParticleList], bbox, grid, clipbox=None, stream: int = 0):
+        """AO of the lists' particles (written to their ao_out) against `grid` (the frame's sizex * sizey * sizez
+        density, host numpy float32 or CUDA float32 tensor) instead of the grid of their own density."""
+        fr, keep = self._frame(lists, bbox, clipbox)
+        gp, gmem = _ptr(grid)
+        self._check(self.lib.p2v_run_ao_on_grid(self.h, C.byref(fr), C.c_void_p(gp), gmem, C.c_void_p(stream)))
 
     # ---- batches ----
     def _batch(self, frames):

@@ -71,11 +71,45 @@ def slab_worker(rank, world, cyclic, kernel, sigma):
     x[::50, 2] = rng.uniform(-3.0, 0.5, x[::50].shape[0])   # near and beyond the lower z face
     bbox, res = (0.0, 0.0, 0.0, 30.0, 30.0, 30.0), (28, 26, 31)
     cyc = (1, 1, 1) if cyclic else (0, 0, 0)
-    compute = lambda p: oracle.density_f32(p, bbox, res, cyclic=cyc, sigma=sigma, kernel=kernel, nthreads=1)
+    compute = lambda p, z0, z1: oracle.density_f32(p, bbox, res, cyclic=cyc, sigma=sigma, kernel=kernel,
+                                                   nthreads=1)[z0:z1]
     scale = 1.0 if kernel == oracle.BUMP else 3.0 * sigma
     slab, (z0, z1), gmin, gmax, gsum = sharding.run_slab(compute, x, bbox, res, bool(cyclic), rank, world,
                                                          normalize=True, support_scale=scale)
     return {"slab": slab, "z": np.array([z0, z1]), "stats": np.array([gmin, gmax, gsum])}
+
+
+AO_KW = dict(offset=0.01, strength=1.0, cone_length=0.8, steps=32, early_exit=1, border=0, sat_scale=1.0)
+
+
+def _ao_frame():
+    rng = np.random.default_rng(31)
+    n = 5000
+    x = np.empty((n, 4), np.float32)
+    x[:, :3] = rng.uniform(0.0, 30.0, (n, 3))
+    x[:, 3] = rng.uniform(0.5, 1.2, n)
+    return x, (0.0, 0.0, 0.0, 30.0, 30.0, 30.0), (24, 22, 26)
+
+
+def _oracle_ao_on_grid(bbox, res):
+    def ao_on_grid(particles, grid):
+        h = oracle.spacing_f64(bbox, res)
+        bmin = [bbox[a] - 0.5 * h[a] for a in range(3)]
+        bsize = [res[a] * h[a] for a in range(3)]
+        nrm = oracle.gradient_normals_f32(grid, bbox, res, particles)
+        lv = oracle.mip_chain_f64(grid, 3, 1.0)
+        dirs = oracle.cone_dirs(8, np.deg2rad(np.float32(50.0)))
+        return oracle.cone_ao_f64(lv, dirs, particles, nrm, bmin, bsize, shortest_edge=float(min(res)), max_lod=2.0,
+                                  **AO_KW)
+    return ao_on_grid
+
+
+def slab_ao_worker(rank, world):
+    x, bbox, res = _ao_frame()
+    compute = lambda p, z0, z1: oracle.density_f32(p, bbox, res, nthreads=1)[z0:z1]
+    slab, (z0, z1), ao, own = sharding.run_slab_ao(compute, _oracle_ao_on_grid(bbox, res), x, bbox, res, True, rank,
+                                                   world)
+    return {"slab": slab, "ao": ao, "own": own}
 
 
 def aggregate_worker(rank, world, op, comp):
@@ -138,6 +172,25 @@ def test_slab_decomposition_gloo(cyclic, kernel, sigma):
     for r in res:
         assert r["stats"][0] == mn and r["stats"][1] == mx
         assert abs(r["stats"][2] - full.astype(np.float64).sum()) <= 1e-9 * abs(full.astype(np.float64).sum())
+
+
+def test_slab_ao_gloo():
+    """AO across z-slab ranks: the gathered grid equals the single-process normalised grid, every particle has one
+    owner, and the owners' AO (cone march over the gathered grid, normals down its gradient) equals the
+    single-process AO of every particle bit for bit."""
+    res_ranks = spawn(slab_ao_worker, 2)
+    x, bbox, res = _ao_frame()
+    full = oracle.density_f32(x, bbox, res, nthreads=1)
+    norm, _, _ = oracle.normalize_minmax_f32(full)
+    grid = norm.reshape(full.shape)
+    ref = _oracle_ao_on_grid(bbox, res)(x, grid)
+    owners = np.stack([r["own"] for r in res_ranks])
+    assert np.all(owners.sum(0) == 1)
+    assert np.array_equal(np.concatenate([r["slab"] for r in res_ranks], 0), grid)
+    got = np.full(x.shape[0], np.nan)
+    for r in res_ranks:
+        got[r["own"]] = r["ao"]
+    assert np.array_equal(got, ref.astype(np.float32))
 
 
 @pytest.mark.parametrize("op,comp", [("sum", 1), ("max", 1), ("min", 3), ("prod", 1)])
