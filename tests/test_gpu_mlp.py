@@ -176,7 +176,7 @@ def test_cone_features_vs_fp64():
     the FP64 restatement (oracle.cone_features_f64): the AO pyramid as the GPU built it, rounded to the 8-bit
     UNORM texels the texture units read, sampled along each cone of the MDAO frame at the feature steps,
     linear within and between levels; then the unit normal and the surface point in volume coordinates. The
-    texture units weight x and y with 8-bit fractions, hence the tolerance. The 44^3 grid puts the steps on
+    texture units weight x, y and z with 8-bit fractions, hence the tolerance. The 44^3 grid puts the steps on
     all three levels, with level blends."""
     c = p2v.Context(0)
     try:
@@ -206,7 +206,9 @@ def test_cone_features_vs_fp64():
         e = np.abs(x[:, :ns].astype(np.float64) - ref[:, :ns])
         assert np.abs(x[:, ns:ns + 3] - ref[:, ns:ns + 3]).max() <= 1e-6
         assert np.abs(x[:, ns + 3:] - ref[:, ns + 3:]).max() <= 1e-5
-        assert e.max() <= 4e-3, e.max()
+        # 8-bit texels and 8-bit filter weights in x, y and z: each axis' weight moves a sample by up to 1/512 of
+        # the neighbouring texels' difference
+        assert e.max() <= 6e-3, e.max()
         assert np.sqrt(np.mean(e ** 2)) <= 5e-4, np.sqrt(np.mean(e ** 2))
     finally:
         c.close()
