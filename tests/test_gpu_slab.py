@@ -32,8 +32,8 @@ def ctx():
 
 
 def grid_of(ctx, f, **params):
-    ctx.set_params(sizex=f.res[0], sizey=f.res[1], sizez=f.res[2], normalize=0, ao_mode=p2v.AO_NONE, slab_z0=0,
-                   slab_z1=0, **params)
+    ctx.set_params(**{"sizex": f.res[0], "sizey": f.res[1], "sizez": f.res[2], "normalize": 0,
+                      "ao_mode": p2v.AO_NONE, "slab_z0": 0, "slab_z1": 0, **params})
     out = np.empty(f.res[0] * f.res[1] * f.res[2], np.float32)
     meta = ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR)], f.bbox, out)
     return out.reshape(f.res[2], f.res[1], f.res[0]), meta
