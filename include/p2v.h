@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 8
+#define P2V_ABI_VERSION 9
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -197,6 +197,16 @@ typedef struct p2v_params {
                                  holds the slab (resolution z = slab_z1 - slab_z0, origin z moved to plane slab_z0),
                                  its statistics and normalisation cover the slab only. Density and intensity
                                  aggregators without AO (0, 0) */
+    /* --- the persistent batch AO (appended) --- */
+    int32_t batch_persistent; /* p2v_run_batch with the cone march on the density (ao_mode P2V_AO_CONE, ao_volume
+                                 P2V_AOVOL_DENSITY, aggregator 0 or 1): the lanes run every frame up to its
+                                 normalised grid, then ONE persistent launch builds every frame's mip levels
+                                 and marches every frame's cones from a device-side work queue (1); 0 = each
+                                 lane runs its frames' AO kernels itself */
+    int32_t queue_wait_polls; /* polls of a queue item's dependency wait in that launch before the call gives up
+                                 with P2V_ETIMEOUT; 0 = the default (2^22, a second or more) */
+    int32_t test_hold_queue;  /* test hook: the first mip level the queue builds never reports its completion, so
+                                 the items that need it wait until queue_wait_polls runs out (0) */
 } p2v_params;
 
 /* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,
@@ -351,8 +361,10 @@ P2V_API p2v_status p2v_write_datraw(p2v_ctx* ctx, const char* prefix, uint32_t f
  * runs many frames (a trajectory's, of uneven particle counts and grid sizes) with the current parameters:
  * the frames are spread over batch_lanes concurrent pipelines (largest first, onto the least-loaded lane),
  * nothing waits for the device until the whole batch is queued, and with batch_graph the queued batch is
- * captured once as a CUDA graph and replayed by one launch while its shape repeats. Each frame's results
- * equal those of p2v_run_frame on the same frame bit for bit. */
+ * captured once as a CUDA graph and replayed by one launch while its shape repeats. With the cone march
+ * on the density and batch_persistent, every frame's AO stage (mip levels, gradient normals, cones) runs
+ * in one persistent launch over a device-side work queue after the lanes. Each frame's results equal those
+ * of p2v_run_frame on the same frame bit for bit. */
 typedef struct p2v_batch_item {
     const p2v_frame* frame;
     p2v_volume* volume;  /* the frame's grid and metadata; NULL or data == NULL: not returned */

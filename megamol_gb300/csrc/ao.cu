@@ -14,7 +14,7 @@
 #include <cstdint>
 
 #include "ao_internal.h"
-#include "cone_device.cuh"
+#include "cone_march.cuh"
 #include "p2v_common.cuh"
 
 namespace p2v {
@@ -31,120 +31,8 @@ __global__ void __launch_bounds__(256) mip_level_kernel(const float* __restrict_
         const int x = (int) (i % dx);
         const int y = (int) ((i / dx) % dy);
         const int z = (int) (i / ((int64_t) dx * dy));
-        const int x1 = min(2 * x + 1, sx - 1), y1 = min(2 * y + 1, sy - 1), z1 = min(2 * z + 1, sz - 1);
-        if (quantize) {
-            // R8 levels: children as 8-bit integers, the /8 rule rounded half up, stored as k/255
-            int k = 0;
-            for (int zz = 2 * z; zz <= z1; ++zz)
-                for (int yy = 2 * y; yy <= y1; ++yy)
-                    for (int xx = 2 * x; xx <= x1; ++xx)
-                        k += __float2int_rn(__ldg(src + ((int64_t) zz * sy + yy) * sx + xx) * 255.0f);
-            dst[i] = __fdiv_rn((float) ((k + 4) >> 3), 255.0f);
-            continue;
-        }
-        float acc = 0.0f;
-        for (int zz = 2 * z; zz <= z1; ++zz)
-            for (int yy = 2 * y; yy <= y1; ++yy)
-                for (int xx = 2 * x; xx <= x1; ++xx) {
-                    float v = __ldg(src + ((int64_t) zz * sy + yy) * sx + xx);
-                    if (sat_scale > 0.0f)
-                        v = fminf(fmaxf(v * sat_scale, 0.0f), 1.0f);
-                    acc += v;
-                }
-        dst[i] = acc * 0.125f;
+        dst[i] = mip_voxel<true>(src, sx, sy, sz, x, y, z, sat_scale, quantize);
     }
-}
-
-using Level = ConeLevel;
-
-// GL LINEAR filtering with texel centres at (i + 0.5) / N. border: 0 = CLAMP_TO_BORDER (0 outside),
-// 1 = CLAMP_TO_EDGE. sat > 0 saturates level-0 texels (the level-0 texture holds clamp(v*sat, 0, 1)).
-__device__ __forceinline__ float tex_fetch(const Level& L, int x, int y, int z, int border, float sat) {
-    if (border == 0) {
-        if ((unsigned) x >= (unsigned) L.d[0] || (unsigned) y >= (unsigned) L.d[1] || (unsigned) z >= (unsigned) L.d[2])
-            return 0.0f;
-    } else {
-        x = min(max(x, 0), L.d[0] - 1);
-        y = min(max(y, 0), L.d[1] - 1);
-        z = min(max(z, 0), L.d[2] - 1);
-    }
-    const float v = __ldg(L.v + ((int64_t) z * L.d[1] + y) * L.d[0] + x);
-    return sat > 0.0f ? fminf(fmaxf(v * sat, 0.0f), 1.0f) : v;
-}
-
-__device__ __forceinline__ float lerp_rn(float a, float b, float w) {
-    return __fmaf_rn(w, __fsub_rn(b, a), a);
-}
-
-__device__ __forceinline__ float saturate_if(float v, float sat) {
-    return sat > 0.0f ? fminf(fmaxf(v * sat, 0.0f), 1.0f) : v;
-}
-
-// One GL LINEAR sample. When the 2x2x2 block lies inside the level (the common case) the eight texels are
-// read from one base pointer without per-texel checks. The base offset and the z stride are 64-bit: a level
-// may hold more than 2^31 texels (an AOSphere volume of 2048^3, a density grid above 1290^3).
-__device__ __forceinline__ float trilinear(const Level& L, float ux, float uy, float uz, int border, float sat) {
-    // explicitly rounded operations: every kernel that inlines this gets the same bits
-    const float cx = __fmaf_rn(ux, L.fd[0], -0.5f), cy = __fmaf_rn(uy, L.fd[1], -0.5f);
-    const float cz = __fmaf_rn(uz, L.fd[2], -0.5f);
-    const float fx0 = floorf(cx), fy0 = floorf(cy), fz0 = floorf(cz);
-    const int x0 = (int) fx0, y0 = (int) fy0, z0 = (int) fz0;
-    const float fx = __fsub_rn(cx, fx0), fy = __fsub_rn(cy, fy0), fz = __fsub_rn(cz, fz0);
-    float c000, c100, c010, c110, c001, c101, c011, c111;
-    if (x0 >= 0 && y0 >= 0 && z0 >= 0 && x0 + 1 < L.d[0] && y0 + 1 < L.d[1] && z0 + 1 < L.d[2]) {
-        const int sy = L.d[0];
-        const int64_t sz = (int64_t) L.d[0] * L.d[1];
-        const float* b = L.v + (((int64_t) z0 * L.d[1] + y0) * L.d[0] + x0);
-        c000 = saturate_if(__ldg(b), sat);
-        c100 = saturate_if(__ldg(b + 1), sat);
-        c010 = saturate_if(__ldg(b + sy), sat);
-        c110 = saturate_if(__ldg(b + sy + 1), sat);
-        c001 = saturate_if(__ldg(b + sz), sat);
-        c101 = saturate_if(__ldg(b + sz + 1), sat);
-        c011 = saturate_if(__ldg(b + sz + sy), sat);
-        c111 = saturate_if(__ldg(b + sz + sy + 1), sat);
-    } else {
-        c000 = tex_fetch(L, x0, y0, z0, border, sat);
-        c100 = tex_fetch(L, x0 + 1, y0, z0, border, sat);
-        c010 = tex_fetch(L, x0, y0 + 1, z0, border, sat);
-        c110 = tex_fetch(L, x0 + 1, y0 + 1, z0, border, sat);
-        c001 = tex_fetch(L, x0, y0, z0 + 1, border, sat);
-        c101 = tex_fetch(L, x0 + 1, y0, z0 + 1, border, sat);
-        c011 = tex_fetch(L, x0, y0 + 1, z0 + 1, border, sat);
-        c111 = tex_fetch(L, x0 + 1, y0 + 1, z0 + 1, border, sat);
-    }
-    const float c00 = lerp_rn(c000, c100, fx), c10 = lerp_rn(c010, c110, fx);
-    const float c01 = lerp_rn(c001, c101, fx), c11 = lerp_rn(c011, c111, fx);
-    const float c0 = lerp_rn(c00, c10, fy), c1 = lerp_rn(c01, c11, fy);
-    return lerp_rn(c0, c1, fz);
-}
-
-// Visibility sample k of a cone: trilinear in the two levels around its lod, blended linearly
-// (LINEAR_MIPMAP_LINEAR).
-__device__ __forceinline__ float cone_sample(const ConeParams& cp, const float dir[3], const float u[3], int k) {
-    const float t = cp.t[k];
-    const float lod = cp.lod[k];
-    const float qx = __fmaf_rn(t, dir[0], u[0]), qy = __fmaf_rn(t, dir[1], u[1]), qz = __fmaf_rn(t, dir[2], u[2]);
-    const int l0 = min((int) lod, cp.nlevels - 1);
-    const float fr = __fsub_rn(lod, (float) l0);
-    float vis = trilinear(cp.lv[l0], qx, qy, qz, cp.border, l0 == 0 ? cp.sat : 0.0f);
-    if (fr > 0.0f && l0 + 1 < cp.nlevels)
-        vis = __fmaf_rn(fr, trilinear(cp.lv[l0 + 1], qx, qy, qz, cp.border, 0.0f), __fmul_rn(1.0f - fr, vis));
-    return vis;
-}
-
-// One cone of the MDAO march (mdao_deferred_fragment_ambocc.inc.glsl:30-51) from normalised point u.
-__device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const float u[3], const float ex[3],
-                                            const float nn[3], const float ez[3]) {
-    float dir[3];
-    cone_dir(cp, c, ex, nn, ez, dir);
-    float acc = 0.0f;
-    for (int k = 0; k < cp.nsteps; ++k) {
-        acc = __fmaf_rn(1.0f - acc, cone_sample(cp, dir, u, k), acc);
-        if (cp.early_exit && acc > 0.99f)
-            break;
-    }
-    return acc;
 }
 
 // One thread per particle: marches all cones (throughput: millions of particles). Particle i's data are
@@ -158,19 +46,7 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
         return;
     const uint32_t o = order ? order[i] : i;
     const uint32_t w = out_order ? out_order[i] : o;
-    const float4 p = xyzr[o];
-    const float4 nv = nrm[o];
-    float x[3], nn[3];
-    if (!surface_point(p, nv, x, nn)) {
-        ao[w] = 1.0f;  // no normal: no occlusion
-        return;
-    }
-    float u[3], ex[3], ez[3];
-    cone_frame(cp, x, nn, u, ex, ez);
-    float ambient = 0.0f;
-    for (int c = 0; c < cp.ncones; ++c)
-        ambient += march_cone(cp, c, u, ex, nn, ez);
-    ao[w] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+    ao[w] = cone_ao_at<true>(cp, xyzr[o], nrm[o]);
 }
 
 // The learned AO's fallback list (its length a device-side count, usually tiny): latency matters, so a
@@ -202,10 +78,10 @@ __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const Cone
         float acc = 0.0f;
         bool done = false;
         for (int k0 = 0; k0 < cp.nsteps && !done; k0 += 32) {
-            const float vis = k0 + lane < cp.nsteps ? cone_sample(cp, dir, u, k0 + lane) : 0.0f;
+            const float vis = k0 + lane < cp.nsteps ? cone_sample<true>(cp, dir, u, k0 + lane) : 0.0f;
             const int m = min(32, cp.nsteps - k0);
             for (int s = 0; s < m; ++s) {
-                acc = __fmaf_rn(1.0f - acc, __shfl_sync(0xffffffffu, vis, s), acc);
+                acc = __fmaf_rn(__fsub_rn(1.0f, acc), __shfl_sync(0xffffffffu, vis, s), acc);
                 if (cp.early_exit && acc > 0.99f) {
                     done = true;
                     break;
@@ -218,8 +94,8 @@ __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const Cone
         if (threadIdx.x == 0) {
             float ambient = 0.0f;
             for (int k = 0; k < cp.ncones; ++k)
-                ambient += s_acc[k];
-            ao[w] = 1.0f - fminf(fmaxf(cp.strength * ambient / (float) cp.ncones, 0.0f), 1.0f);
+                ambient = __fadd_rn(ambient, s_acc[k]);
+            ao[w] = cone_combine(cp, ambient);
         }
         __syncthreads();
     }
@@ -239,65 +115,13 @@ __global__ void __launch_bounds__(256) sort_particles_kernel(const uint32_t* __r
     }
 }
 
-// Normals from the density grid (P2V_NORMALS_GRADIENT): -grad(rho) at the particle, normalised. grad(rho) at
-// node i along axis a is (v[i + 1] - v[i - 1]) / (2 h) with the neighbours wrapped on a cyclic axis, and the
-// one-sided first differences (v[1] - v[0]) / h, (v[s-1] - v[s-2]) / h at the faces of an open one; the node
-// gradients are interpolated trilinearly at u = (p - min) / h clamped into [0, s - 1].
-__device__ __forceinline__ float node_grad(const float* __restrict__ g, int64_t base, int64_t stride, int i, int s,
-                                           int cyc, float ih) {
-    if (s < 2)
-        return 0.0f;
-    int lo = i - 1, hi = i + 1;
-    float scale = 0.5f * ih;
-    if (cyc) {
-        lo = lo < 0 ? lo + s : lo;
-        hi = hi >= s ? hi - s : hi;
-    } else if (i == 0) {
-        lo = 0;
-        scale = ih;
-    } else if (i == s - 1) {
-        hi = s - 1;
-        scale = ih;
-    }
-    return (__ldg(g + base + hi * stride) - __ldg(g + base + lo * stride)) * scale;
-}
-
+// Unit normals down the density gradient (P2V_NORMALS_GRADIENT), one thread per particle.
 __global__ void __launch_bounds__(256) gradient_normals_kernel(const GridGeo geo, const float* __restrict__ grid,
     const float4* __restrict__ xyzr, uint32_t n, float4* __restrict__ nrm) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n)
         return;
-    const float4 p = xyzr[j];
-    const float pc[3] = {p.x, p.y, p.z};
-    int i0[3], i1[3];
-    float f[3], ih[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        ih[a] = 1.0f / geo.hf[a];
-        float u = (pc[a] - geo.minf[a]) * ih[a];
-        u = fminf(fmaxf(u, 0.0f), (float) (geo.s[a] - 1));  // a NaN coordinate becomes 0 (fmaxf)
-        const int k = min((int) u, geo.s[a] - 1);
-        i0[a] = k;
-        i1[a] = min(k + 1, geo.s[a] - 1);
-        f[a] = u - (float) k;
-    }
-    const int64_t sx = geo.s[0], sxy = (int64_t) geo.s[0] * geo.s[1];
-    float gr[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int x = (c & 1) ? i1[0] : i0[0], y = (c & 2) ? i1[1] : i0[1], z = (c & 4) ? i1[2] : i0[2];
-        const float w = ((c & 1) ? f[0] : 1.0f - f[0]) * ((c & 2) ? f[1] : 1.0f - f[1]) * ((c & 4) ? f[2] : 1.0f - f[2]);
-        gr[0] += w * node_grad(grid, z * sxy + y * sx, 1, x, geo.s[0], geo.cyc[0], ih[0]);
-        gr[1] += w * node_grad(grid, z * sxy + x, sx, y, geo.s[1], geo.cyc[1], ih[1]);
-        gr[2] += w * node_grad(grid, y * sx + x, sxy, z, geo.s[2], geo.cyc[2], ih[2]);
-    }
-    const float l2 = gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2];
-    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (l2 > 0.0f && isfinite(l2)) {
-        const float il = -rsqrtf(l2);
-        out = make_float4(gr[0] * il, gr[1] * il, gr[2] * il, 0.0f);
-    }
-    nrm[j] = out;
+    nrm[j] = gradient_normal<true>(geo, grid, xyzr[j]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -369,7 +193,7 @@ __global__ void __launch_bounds__(128) aosphere_ao_kernel(const AOSphereParams a
         ao[o] = 1.0f;
         return;
     }
-    Level T;
+    ConeLevel T;
     T.v = tex;
     for (int a = 0; a < 3; ++a) {
         T.d[a] = ap.s[a];
@@ -387,7 +211,7 @@ __global__ void __launch_bounds__(128) aosphere_ao_kernel(const AOSphereParams a
         for (int a = 0; a < 3; ++a) {
             float q[3] = {aop[0], aop[1], aop[2]};
             q[a] += nn[a] > 0.0f ? aod[a] : -aod[a];
-            const float tap = 1.0f - trilinear(T, q[0], q[1], q[2], 1, 0.0f) * ap.eval_fac;
+            const float tap = 1.0f - trilinear<true>(T, q[0], q[1], q[2], 1, 0.0f) * ap.eval_fac;
             acc += nn[a] * nn[a] * tap;
         }
         ao[o] = acc;
@@ -395,7 +219,7 @@ __global__ void __launch_bounds__(128) aosphere_ao_kernel(const AOSphereParams a
         float q[3];
         for (int a = 0; a < 3; ++a)
             q[a] = (x[a] + nn[a] * ap.sampd[a] - ap.origin[a]) / ap.ext[a];
-        ao[o] = 1.0f - trilinear(T, q[0], q[1], q[2], 1, 0.0f) * ap.eval_fac;
+        ao[o] = 1.0f - trilinear<true>(T, q[0], q[1], q[2], 1, 0.0f) * ap.eval_fac;
     }
 }
 

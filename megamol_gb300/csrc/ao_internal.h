@@ -57,6 +57,49 @@ struct MdaoParams {
     int unorm8;                             // 1 = R8 texel values k/255, 0 = unquantised fractions
 };
 
+// ---- the persistent batch AO (p2v_run_batch, cone march on the density) ----
+// One frame's deferred AO stage: its cone march (lv[0] = the frame's density grid, lv[1..] mip levels the
+// batch kernel builds), its grid geometry for gradient normals, and its particles in sorted order.
+struct alignas(16) BatchAoFrame {
+    ConeParams cp;
+    GridGeo g;
+    const float* grid;       // the density grid (level 0 before saturation)
+    const float4* xyzr;      // positions and radii, sorted order
+    const float4* nrm;       // normals, sorted order; null: -grad(density) at each particle
+    const uint32_t* order;   // sorted position -> input index
+    float* ao;               // AO in input order
+    uint32_t n;
+};
+static_assert(sizeof(BatchAoFrame) % 16 == 0, "frame descriptors are copied as 16-byte words");
+
+enum : uint32_t { BSEG_MIP = 0, BSEG_AO = 1 };
+constexpr uint32_t BATCH_MIP_ITEM = 512;  // voxels of one mip item
+constexpr uint32_t BATCH_AO_ITEM = 128;   // particles of one AO item (one per thread)
+
+// A run of work items of one kind and frame. Items are numbered by tickets in queue order; a segment's
+// items start once its dependency (an earlier segment) has completed every item.
+struct BatchSeg {
+    uint32_t first;  // first ticket
+    uint32_t count;  // items
+    uint32_t frame;
+    uint32_t kind;   // BSEG_MIP: build mip level `level` from level - 1; BSEG_AO: cone march
+    int32_t level;
+    int32_t dep;     // segment index, -1 none
+};
+
+struct BatchQueueArgs {
+    const BatchAoFrame* frames;
+    const BatchSeg* segs;
+    uint32_t nseg, total;  // segments, tickets
+    uint32_t* words;       // [0] next ticket, [1] error (BATCH_ERR_*), [2 + s] completed items of segment s
+    uint32_t wait_polls;   // polls of a dependency before the wait gives up
+    int32_t hold_seg;      // test hook: this segment never reports its completion (-1 none)
+};
+constexpr uint32_t BATCH_ERR_TIMEOUT = 1;
+inline size_t batch_queue_words(uint32_t nseg) { return 2 + (size_t) nseg; }
+// zeroes the queue words and runs the queue with one resident block per free slot of every SM
+cudaError_t launch_batch_ao(const BatchQueueArgs& q, int sms, cudaStream_t st);
+
 // quantize = 1: the levels are R8 textures (texels k/255; out = ((sum k + 4) / 8) / 255)
 cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int quantize, int nlevels,
     float* const* out, int (*dims)[3], int sms, cudaStream_t st);

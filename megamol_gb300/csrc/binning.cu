@@ -415,6 +415,8 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
 
 // start[c] = first sorted position whose key is >= c, for c in [0, nbins]. Short gaps are filled by
 // the thread that sees them; gaps of 64 cells or more are queued for a block-wide fill.
+constexpr uint32_t GAP_CHUNK = 8192;
+
 __global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t nbins,
     uint32_t* __restrict__ start, uint4* __restrict__ gaps, uint32_t gap_cap, FrameScalars* __restrict__ fs,
     const FrameScalars* __restrict__ gate) {
@@ -431,11 +433,20 @@ __global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restr
             for (uint32_t c = lo; c <= hi; ++c)
                 start[c] = i;
         } else {
-            const uint32_t slot = atomicAdd(&fs->ngaps, 1u);
-            if (slot < gap_cap)
-                gaps[slot] = make_uint4(lo, hi, i, 0u);
-            else
-                atomicOr(&fs->error, ERR_GAP_OVERFLOW);
+            // a long run of empty cells: chunks of at most GAP_CHUNK cells, one block each in
+            // cell_gap_fill_kernel (a sparse grid can hold a single run of millions of cells). Runs are disjoint
+            // and longer than 64 cells, so the chunks number at most (nbins + 1) (1/GAP_CHUNK + 1/65), below
+            // the nbins / 64 + 2 entries the list holds
+            const uint32_t nch = (uint32_t) (((uint64_t) hi - lo + GAP_CHUNK) / GAP_CHUNK);
+            const uint32_t slot = atomicAdd(&fs->ngaps, nch);
+            for (uint32_t q = 0; q < nch; ++q) {
+                const uint64_t c0 = (uint64_t) lo + (uint64_t) q * GAP_CHUNK;
+                const uint64_t c1 = std::min<uint64_t>(hi, c0 + GAP_CHUNK - 1);
+                if ((uint64_t) slot + q < gap_cap)
+                    gaps[slot + q] = make_uint4((uint32_t) c0, (uint32_t) c1, i, 0u);
+                else
+                    atomicOr(&fs->error, ERR_GAP_OVERFLOW);
+            }
         }
     }
 }

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -145,6 +146,18 @@ struct Pipe {
     }
 };
 
+// One frame's buffers in a persistent batch: what the batch AO launch reads once every lane has finished
+// (the lane's own buffers serve its next frame meanwhile), and the frame's descriptor for that launch.
+struct BatchSlot {
+    DevBuf xyzr_s, order, nrm_s, ao, grid, mips;
+    BatchAoFrame* desc = nullptr;  // this frame's entry of the pinned descriptor table
+    bool deferred = false;         // the frame's AO stage was left to the batch launch
+    void release() {
+        for (DevBuf* b : {&xyzr_s, &order, &nrm_s, &ao, &grid, &mips})
+            b->release();
+    }
+};
+
 // Host-side state of a frame between its enqueue and its completion.
 struct FrameJob {
     uint64_t N = 0;
@@ -194,6 +207,15 @@ struct p2v_ctx {
     std::vector<uint8_t> b_graph_sig, b_eager_sig;
     std::vector<FrameJob> b_jobs;
     std::vector<int> b_lane_of;
+    // the persistent batch AO: per-frame buffers, pinned descriptor and segment tables, their device copies,
+    // the queue words and the pinned mirror of the queue's error word
+    std::vector<std::unique_ptr<BatchSlot>> b_slots;
+    BatchAoFrame* b_frames_h = nullptr;
+    size_t b_frames_cap = 0;
+    BatchSeg* b_segs_h = nullptr;
+    size_t b_segs_cap = 0;
+    DevBuf b_frames_d, b_segs_d, b_words;
+    uint32_t* b_err_h = nullptr;
     // autotuned choices (0 = none)
     int tuned_tile[3] = {0, 0, 0};
     int tuned_lanes = 0;
@@ -223,16 +245,22 @@ struct p2v_ctx {
 
     p2v_status run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t st);
     p2v_status enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol, cudaStream_t st, FrameScalars* h_out,
-                             bool timed, FrameJob& job);
+                             bool timed, FrameJob& job, BatchSlot* slot = nullptr);
     p2v_status finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol, p2v_stats& out);
     p2v_status run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
-                      uint32_t n, const uint32_t* order, cudaStream_t st);
+                      uint32_t n, const uint32_t* order, cudaStream_t st, BatchSlot* slot);
     p2v_status build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
-                          uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st);
+                          uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st, BatchSlot* slot);
+    p2v_status enqueue_batch_ao(const p2v_batch_item* items, uint32_t count, const std::vector<uint32_t>& byw,
+                                cudaStream_t st);
     p2v_status mlp_alloc();
     p2v_status prepare_features(Pipe& pp, ConeParams& cp, cudaStream_t st);
     p2v_status run_batch(const p2v_batch_item* items, uint32_t count, p2v_stats* out, cudaStream_t st,
                          bool allow_graph, float* ms_out);
+    bool batch_persistent_applies() const {
+        return prm.batch_persistent != 0 && prm.ao_mode == P2V_AO_CONE && prm.ao_volume == P2V_AOVOL_DENSITY &&
+               (prm.aggregator == 0 || prm.aggregator == 1);
+    }
     void drop_graph() {
         if (b_exec)
             cudaGraphExecDestroy(b_exec);
@@ -369,7 +397,7 @@ p2v_status p2v_ctx::run_frame(const p2v_frame* fr, p2v_volume* vol, cudaStream_t
 // Validate the frame and queue its whole pipeline on `st` using the buffers of `pp`; the frame scalars are
 // copied to the pinned slot h_out at the end. Nothing here waits for the device.
 p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol, cudaStream_t st,
-                                  FrameScalars* h_out, bool timed, FrameJob& job) {
+                                  FrameScalars* h_out, bool timed, FrameJob& job, BatchSlot* slot) {
     DevBuf &raw = pp.raw, &xyzr = pp.xyzr, &rec_a = pp.rec_a, &keys0 = pp.keys0,
            &keys1 = pp.keys1, &vals0 = pp.vals0, &vals1 = pp.vals1, &status = pp.status, &hist = pp.hist,
            &cstart = pp.cstart, &gaps = pp.gaps, &grid = pp.grid, &tiles = pp.tiles, &scal = pp.scal, &nrm = pp.nrm,
@@ -502,6 +530,9 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     const bool direct = vol && vol->data && vol->mem == P2V_MEM_DEVICE && vol->capacity >= VC;
     if (direct) {
         dgrid = vol->data;
+    } else if (slot) {  // read by the batch AO launch after the lane has moved on
+        P2V_CUDA_TRY(slot->grid.ensure(sizeof(float) * VC));
+        dgrid = slot->grid.as<float>();
     } else {
         P2V_CUDA_TRY(grid.ensure(sizeof(float) * VC));
         dgrid = grid.as<float>();
@@ -688,13 +719,22 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     // the cone-march stages read the positions in sorted order: the binning's last pass writes them
     pp.xyzr_sorted = P.ao_mode == P2V_AO_CONE || P.ao_mode == P2V_AO_LEARNED;
     if (pp.xyzr_sorted) {
-        P2V_CUDA_TRY(pp.xyzr_s.ensure(sizeof(float4) * ((size_t) n + 1)));
-        sb.xyzr_out = pp.xyzr_s.as<float4>();
+        DevBuf& xs = slot ? slot->xyzr_s : pp.xyzr_s;
+        P2V_CUDA_TRY(xs.ensure(sizeof(float4) * ((size_t) n + 1)));
+        sb.xyzr_out = xs.as<float4>();
     }
     sb.geo = g;
     P2V_CUDA_TRY(launch_bin_sort(sb, n, g, counting ? pp.bcount.as<uint32_t>() : nullptr, cstart.as<uint32_t>(),
                                  gaps.as<uint4>(), gap_cap, fs, sms, st));
     const uint32_t* skeys = sb.keys[sb.result];
+    if (slot) {
+        slot->deferred = false;
+        if (want_ao && n > 0) {  // the sorted order outlives the lane's sort buffers
+            P2V_CUDA_TRY(slot->order.ensure(sizeof(uint32_t) * ((size_t) n + 1)));
+            P2V_CUDA_TRY(cudaMemcpyAsync(slot->order.ptr, sb.vals[sb.result], sizeof(uint32_t) * n,
+                                         cudaMemcpyDeviceToDevice, st));
+        }
+    }
     if (timed)
         P2V_CUDA_TRY(cudaEventRecord(ev[EV_BIN], st));
 
@@ -776,7 +816,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         }
         P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_JOIN], side));
         P2V_CUDA_TRY(cudaStreamWaitEvent(st, pp.sev[SEV_NRM], 0));
-        const p2v_status as = run_ao(pp, fr, g, dgrid, bb, n, sb.vals[sb.result], st);
+        const p2v_status as = run_ao(pp, fr, g, dgrid, bb, n, sb.vals[sb.result], st, slot);
         if (as != P2V_OK) {
             cudaStreamWaitEvent(st, pp.sev[SEV_JOIN], 0);  // no side work left outside st (graph capture)
             return as;
@@ -788,7 +828,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     // ---- outputs ----
     if (grid_out && !want_ao)
         P2V_CUDA_TRY(cudaMemcpyAsync(vol->data, dgrid, sizeof(float) * VC, grid_kind, st));
-    if (want_ao) {
+    if (want_ao && !(slot && slot->deferred)) {  // a deferred frame's AO is copied out after the batch launch
         uint64_t aoff = 0;
         for (uint32_t l = 0; l < fr->list_count; ++l) {
             const p2v_particle_list& L = fr->lists[l];
@@ -942,8 +982,9 @@ void mdao_dims(const float clip[6], int vol_size, int dims[3], float& shortest, 
 }
 
 p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid,
-                               const float bb[6], uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st) {
-    DevBuf &xyzr = pp.xyzr, &mips = pp.mips, &mdao_acc = pp.mdao_acc, &mdao_vol = pp.mdao_vol;
+                               const float bb[6], uint32_t n, const uint32_t* order, ConeParams& cp, cudaStream_t st,
+                               BatchSlot* slot) {
+    DevBuf &xyzr = pp.xyzr, &mips = slot ? slot->mips : pp.mips, &mdao_acc = pp.mdao_acc, &mdao_vol = pp.mdao_vol;
     const p2v_params& P = prm;
     if (P.ao_volume != P2V_AOVOL_DENSITY && P.ao_volume != P2V_AOVOL_MDAO)
         return fail(P2V_EINVAL, "ao_volume %d is not a p2v_ao_volume", P.ao_volume);
@@ -951,6 +992,8 @@ p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, 
         return fail(P2V_EINVAL, "ao_cones must lie in [1, %d]", MAX_CONES);
     cp = ConeParams{};
     const bool mdao = P.ao_volume == P2V_AOVOL_MDAO;
+    if (mdao && slot)
+        return fail(P2V_EUNSUPPORTED, "the batch AO launch marches the density, not the MDAO volume");
     int d0[3];
     float shortest = 0.0f, max_lod = 0.0f;
     int L = 0;
@@ -1026,6 +1069,7 @@ p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, 
     if ((uint64_t) d0[0] * d0[1] * d0[2] >= (1ull << 31))
         return fail(P2V_EUNSUPPORTED, "AO volume %dx%dx%d exceeds 2^31 texels", d0[0], d0[1], d0[2]);
     // level 0 is the density grid (saturated on the fly) or the MDAO volume; levels 1.. are built here
+    // each level starts on a 128-byte boundary
     size_t need = 0;
     int d[MAX_LEVELS][3];
     for (int a = 0; a < 3; ++a)
@@ -1033,7 +1077,7 @@ p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, 
     for (int l = 1; l < L; ++l) {
         for (int a = 0; a < 3; ++a)
             d[l][a] = std::max(1, d[l - 1][a] / 2);
-        need += (size_t) d[l][0] * d[l][1] * d[l][2];
+        need += ((size_t) d[l][0] * d[l][1] * d[l][2] + 31) & ~size_t(31);
     }
     P2V_CUDA_TRY(mips.ensure(sizeof(float) * (need + 1)));
     float* lvp[MAX_LEVELS];
@@ -1041,10 +1085,11 @@ p2v_status p2v_ctx::build_cone(Pipe& pp, const p2v_frame* fr, const GridGeo& g, 
     size_t off = 0;
     for (int l = 1; l < L; ++l) {
         lvp[l] = mips.as<float>() + off;
-        off += (size_t) d[l][0] * d[l][1] * d[l][2];
+        off += ((size_t) d[l][0] * d[l][1] * d[l][2] + 31) & ~size_t(31);
     }
     int dims[MAX_LEVELS][3];
-    P2V_CUDA_TRY(launch_mip_levels(level0, d0, cp.sat, mdao && P.mdao_unorm8 ? 1 : 0, L, lvp, dims, sms, st));
+    if (!slot)  // a batch frame's levels are built by the batch AO launch
+        P2V_CUDA_TRY(launch_mip_levels(level0, d0, cp.sat, mdao && P.mdao_unorm8 ? 1 : 0, L, lvp, dims, sms, st));
     for (int l = 0; l < L; ++l) {
         cp.lv[l].v = lvp[l];
         for (int a = 0; a < 3; ++a) {
@@ -1088,7 +1133,7 @@ p2v_status p2v_ctx::prepare_features(Pipe& pp, ConeParams& cp, cudaStream_t st) 
 }
 
 p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, const float* dgrid, const float bb[6],
-                           uint32_t n, const uint32_t* order, cudaStream_t st) {
+                           uint32_t n, const uint32_t* order, cudaStream_t st, BatchSlot* slot) {
     DevBuf &xyzr = pp.xyzr, &nrm = pp.nrm, &ao = pp.ao, &scal = pp.scal, &fb_list = pp.fb_list,
            &aos_acc = pp.aos_acc, &aos_tex = pp.aos_tex;
     const p2v_params& P = prm;
@@ -1115,9 +1160,31 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
     };
     if (P.ao_mode == P2V_AO_CONE) {
         ConeParams cp{};
-        const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st);
+        const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st, slot);
         if (bs != P2V_OK)
             return bs;
+        if (slot) {
+            // the batch AO launch builds the levels and marches the cones (gradient normals computed there)
+            const bool list = P.ao_normals == P2V_NORMALS_LIST;
+            if (list && n > 0) {
+                P2V_CUDA_TRY(slot->nrm_s.ensure(sizeof(float4) * ((size_t) n + 1)));
+                P2V_CUDA_TRY(launch_sort_particles(order, n, nullptr, nrm.as<float4>(), nullptr,
+                                                   slot->nrm_s.as<float4>(), sms, st));
+            }
+            P2V_CUDA_TRY(slot->ao.ensure(sizeof(float) * ((size_t) n + 1)));
+            BatchAoFrame& d = *slot->desc;
+            d = BatchAoFrame{};
+            d.cp = cp;
+            d.g = g;
+            d.grid = dgrid;
+            d.xyzr = slot->xyzr_s.as<float4>();
+            d.nrm = list ? slot->nrm_s.as<float4>() : nullptr;
+            d.order = slot->order.as<uint32_t>();
+            d.ao = slot->ao.as<float>();
+            d.n = n;
+            slot->deferred = true;
+            return P2V_OK;
+        }
         P2V_CUDA_TRY(to_sorted());
         P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr, order,
                                     ao.as<float>(), st));
@@ -1127,7 +1194,7 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         if (!mlp_ready)
             return fail(P2V_EINVAL, "learned AO: no trained network (p2v_mlp_train or p2v_mlp_load first)");
         ConeParams cp{};
-        const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st);
+        const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st, nullptr);
         if (bs != P2V_OK)
             return bs;
         const p2v_status ps = prepare_features(pp, cp, st);
@@ -1222,6 +1289,96 @@ bool graph_safe_host(const void* p) {
 }
 
 }  // namespace
+
+// The persistent batch AO (after every lane has finished its frames): the work queue of every deferred
+// frame, mip levels first (level 1 of every frame, then level 2, ...; a level's segment depends on the level
+// below it), then each frame's cone march (depending on its last level), largest frames first; the tables
+// are uploaded from pinned memory, the queue runs in one launch, and the frames' AO is copied to the lists'
+// outputs.
+p2v_status p2v_ctx::enqueue_batch_ao(const p2v_batch_item* items, uint32_t count, const std::vector<uint32_t>& byw,
+                                     cudaStream_t st) {
+    if (prm.queue_wait_polls < 0)
+        return fail(P2V_EINVAL, "queue_wait_polls must be >= 0");
+    std::vector<BatchSeg> segs;
+    std::vector<std::array<int, MAX_LEVELS>> seg_of(count);
+    int maxL = 0;
+    for (uint32_t f = 0; f < count; ++f) {
+        seg_of[f].fill(-1);
+        const BatchSlot& sl = *b_slots[f];
+        if (sl.deferred && sl.desc->n > 0)
+            maxL = std::max(maxL, sl.desc->cp.nlevels);
+    }
+    uint32_t tick = 0;
+    for (int l = 1; l < maxL; ++l)
+        for (uint32_t f : byw) {
+            const BatchSlot& sl = *b_slots[f];
+            if (!sl.deferred || sl.desc->n == 0 || l >= sl.desc->cp.nlevels)
+                continue;
+            const ConeLevel& lv = sl.desc->cp.lv[l];
+            const uint64_t nv = (uint64_t) lv.d[0] * lv.d[1] * lv.d[2];
+            const uint32_t cnt = (uint32_t) ((nv + BATCH_MIP_ITEM - 1) / BATCH_MIP_ITEM);
+            seg_of[f][l] = (int) segs.size();
+            segs.push_back(BatchSeg{tick, cnt, f, BSEG_MIP, l, l >= 2 ? seg_of[f][l - 1] : -1});
+            tick += cnt;
+        }
+    const int hold = prm.test_hold_queue && !segs.empty() ? 0 : -1;
+    for (uint32_t f : byw) {
+        const BatchSlot& sl = *b_slots[f];
+        if (!sl.deferred || sl.desc->n == 0)
+            continue;
+        const uint32_t cnt = (sl.desc->n + BATCH_AO_ITEM - 1) / BATCH_AO_ITEM;
+        const int L = sl.desc->cp.nlevels;
+        segs.push_back(BatchSeg{tick, cnt, f, BSEG_AO, 0, L >= 2 ? seg_of[f][L - 1] : -1});
+        tick += cnt;
+    }
+    if (b_segs_cap < segs.size()) {
+        P2V_CUDA_TRY(cudaStreamSynchronize(st));
+        if (b_segs_h)
+            cudaFreeHost(b_segs_h);
+        b_segs_h = nullptr;
+        b_segs_cap = 0;
+        P2V_CUDA_TRY(cudaMallocHost(&b_segs_h, sizeof(BatchSeg) * segs.size()));
+        b_segs_cap = segs.size();
+    }
+    if (!segs.empty())
+        std::memcpy(b_segs_h, segs.data(), sizeof(BatchSeg) * segs.size());
+    P2V_CUDA_TRY(b_frames_d.ensure(sizeof(BatchAoFrame) * count));
+    P2V_CUDA_TRY(b_segs_d.ensure(sizeof(BatchSeg) * (segs.size() + 1)));
+    P2V_CUDA_TRY(b_words.ensure(sizeof(uint32_t) * batch_queue_words((uint32_t) segs.size())));
+    P2V_CUDA_TRY(cudaMemcpyAsync(b_frames_d.ptr, b_frames_h, sizeof(BatchAoFrame) * count, cudaMemcpyHostToDevice, st));
+    if (!segs.empty())
+        P2V_CUDA_TRY(cudaMemcpyAsync(b_segs_d.ptr, b_segs_h, sizeof(BatchSeg) * segs.size(), cudaMemcpyHostToDevice,
+                                     st));
+    BatchQueueArgs q{};
+    q.frames = b_frames_d.as<BatchAoFrame>();
+    q.segs = b_segs_d.as<BatchSeg>();
+    q.nseg = (uint32_t) segs.size();
+    q.total = tick;
+    q.words = b_words.as<uint32_t>();
+    q.wait_polls = prm.queue_wait_polls > 0 ? (uint32_t) prm.queue_wait_polls : (1u << 22);
+    q.hold_seg = hold;
+    P2V_CUDA_TRY(launch_batch_ao(q, sms, st));
+    P2V_CUDA_TRY(cudaMemcpyAsync(b_err_h, b_words.as<uint32_t>() + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    for (uint32_t f = 0; f < count; ++f) {
+        const BatchSlot& sl = *b_slots[f];
+        if (!sl.deferred)
+            continue;
+        const p2v_frame* fr = items[f].frame;
+        uint64_t aoff = 0;
+        for (uint32_t l = 0; l < fr->list_count; ++l) {
+            const p2v_particle_list& Lst = fr->lists[l];
+            if (Lst.vertex_type == P2V_VERTDATA_NONE)
+                continue;
+            if (Lst.ao_out && Lst.count > 0)
+                P2V_CUDA_TRY(cudaMemcpyAsync(Lst.ao_out, sl.ao.as<float>() + aoff, sizeof(float) * Lst.count,
+                                             Lst.mem == P2V_MEM_DEVICE ? cudaMemcpyDeviceToDevice
+                                                                       : cudaMemcpyDeviceToHost,
+                                             st));
+            aoff += Lst.count;
+        }
+    }
+    return P2V_OK;
+}
 
 // A batch: frames sorted by work (particles plus a share of the grid) and dealt, largest first, to the
 // least-loaded of L lanes; every lane queues its frames on its own stream, forked from and joined back into
@@ -1320,15 +1477,37 @@ p2v_status p2v_ctx::run_batch(const p2v_batch_item* items, uint32_t count, p2v_s
     }
     const bool use_graph = allow_graph && prm.batch_graph != 0 && pinned;
     const bool replay = use_graph && b_exec && sig == b_graph_sig;
+    const bool pers = batch_persistent_applies();
+    if (pers && !replay) {
+        // per-frame buffers and the pinned descriptor table (sized before any capture begins)
+        while (b_slots.size() < count)
+            b_slots.push_back(std::make_unique<BatchSlot>());
+        if (b_frames_cap < count) {
+            P2V_CUDA_TRY(cudaStreamSynchronize(st));
+            if (b_frames_h)
+                cudaFreeHost(b_frames_h);
+            b_frames_h = nullptr;
+            b_frames_cap = 0;
+            P2V_CUDA_TRY(cudaMallocHost(&b_frames_h, sizeof(BatchAoFrame) * count));
+            b_frames_cap = count;
+        }
+        if (!b_err_h)
+            P2V_CUDA_TRY(cudaMallocHost(&b_err_h, sizeof(uint32_t)));
+        for (uint32_t f = 0; f < count; ++f) {
+            b_slots[f]->desc = b_frames_h + f;
+            b_slots[f]->deferred = false;
+        }
+    }
     P2V_CUDA_TRY(cudaEventRecord(b_t0, st));
     if (replay) {
         P2V_CUDA_TRY(cudaGraphLaunch(b_exec, st));
     } else {
+        // an eager run may grow (reallocate) buffers a captured graph points to: a graph is replayed only
+        // while no other batch ran since its capture
+        drop_graph();
         const bool capture = use_graph && sig == b_eager_sig;
-        if (capture) {
-            drop_graph();
+        if (capture)
             P2V_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        }
         b_jobs.assign(count, FrameJob{});
         p2v_status es = P2V_OK;
         cudaError_t ce = cudaEventRecord(b_events[L], st);
@@ -1345,7 +1524,8 @@ p2v_status p2v_ctx::run_batch(const p2v_batch_item* items, uint32_t count, p2v_s
             if (it.size[2] > 0)
                 prm.sizez = it.size[2];
             Pipe& pp = *lanes[lane_of[f]];
-            es = enqueue_frame(pp, it.frame, it.volume, pp.stream, b_scal + f, false, b_jobs[f]);
+            es = enqueue_frame(pp, it.frame, it.volume, pp.stream, b_scal + f, false, b_jobs[f],
+                               pers ? b_slots[f].get() : nullptr);
             prm = saved;
         }
         for (int l = 0; l < L && ce == cudaSuccess; ++l) {
@@ -1353,6 +1533,8 @@ p2v_status p2v_ctx::run_batch(const p2v_batch_item* items, uint32_t count, p2v_s
             if (ce == cudaSuccess)
                 ce = cudaStreamWaitEvent(st, b_events[l], 0);
         }
+        if (pers && es == P2V_OK && ce == cudaSuccess)
+            es = enqueue_batch_ao(items, count, byw, st);
         if (capture) {
             cudaGraph_t g = nullptr;
             const cudaError_t ee = cudaStreamEndCapture(st, &g);
@@ -1388,6 +1570,11 @@ p2v_status p2v_ctx::run_batch(const p2v_batch_item* items, uint32_t count, p2v_s
     // ---- per-frame results ----
     p2v_status first_err = P2V_OK;
     std::string first_msg;
+    if (pers && *b_err_h != 0) {
+        first_err = P2V_ETIMEOUT;
+        first_msg = "batch AO queue: a work item's dependency wait gave up (queue_wait_polls " +
+                    std::to_string(prm.queue_wait_polls) + "); the batch's AO is invalid";
+    }
     uint64_t parts = 0;
     for (uint32_t f = 0; f < count; ++f) {
         p2v_stats fsx{};
@@ -1514,6 +1701,9 @@ void p2v_params_default(p2v_params* p) {
     p->mma_wait_polls = 0;
     p->test_hold_mma = 0;
     p->slab_z0 = p->slab_z1 = 0;
+    p->batch_persistent = 1;
+    p->queue_wait_polls = 0;
+    p->test_hold_queue = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {
@@ -1560,6 +1750,17 @@ void p2v_destroy(p2v_ctx* c) {
     for (auto& l : c->lanes)
         l->release();
     c->lanes.clear();
+    for (auto& sl : c->b_slots)
+        sl->release();
+    c->b_slots.clear();
+    for (DevBuf* b : {&c->b_frames_d, &c->b_segs_d, &c->b_words})
+        b->release();
+    if (c->b_frames_h)
+        cudaFreeHost(c->b_frames_h);
+    if (c->b_segs_h)
+        cudaFreeHost(c->b_segs_h);
+    if (c->b_err_h)
+        cudaFreeHost(c->b_err_h);
     for (DevBuf* b : {&c->mlp_P, &c->mlp_m, &c->mlp_v, &c->mlp_g, &c->mlp_part, &c->mlp_ploss, &c->mlp_loss,
                       &c->mlp_w1h, &c->mlp_w2h, &c->mlp_lo, &c->mlp_hi, &c->mlp_idx, &c->mlp_y, &c->tX, &c->tT})
         b->release();

@@ -131,3 +131,89 @@ def test_empty_and_single_frame_batches(ctx):
     frames, outs = batch_frames(traj, False)
     ctx.run_batch(frames)
     assert np.array_equal(outs[0][0], refs[0][0])
+
+
+def reference_with(ctx, traj, params):
+    refs = []
+    for f, size, nrm in traj:
+        ctx.set_params(sizex=size[0], sizey=size[1], sizez=size[2], **params)
+        vol = np.empty(size[0] * size[1] * size[2], np.float32)
+        ao = np.full(f.n, np.nan, np.float32)
+        ctx.run_frame([p2v.ParticleList(f.xyzr, p2v.VERTDATA_FLOAT_XYZR, normals=nrm, ao_out=ao)], f.bbox, vol)
+        refs.append((vol, ao))
+    return refs
+
+
+@pytest.mark.parametrize("normals", [p2v.NORMALS_LIST, p2v.NORMALS_GRADIENT])
+@pytest.mark.parametrize("graph", [0, 1])
+def test_persistent_batch_ao_equals_run_frame(ctx, normals, graph):
+    """The persistent batch AO launch (every frame's mip levels and cone march taken from one device-side work
+    queue after the lanes) gives every frame the grid and AO bits of p2v_run_frame, with list normals and with
+    normals down the density gradient, eagerly and (graph) captured and replayed. ao_levels = 0: the whole
+    pyramid, so every frame's march waits on a chain of five to seven levels."""
+    traj = small_trajectory(k=7, seed=45)
+    params = dict(AO, ao_levels=0, ao_normals=normals)
+    refs = reference_with(ctx, traj, params)
+    ctx.set_params(batch_lanes=3, batch_graph=graph, batch_persistent=1, **params)
+    frames, outs = batch_frames(traj, True)
+    for rep in range(3):  # eager; then (graph) captured; replayed
+        for vol, ao in outs:
+            vol.fill(np.nan)
+            ao.fill(np.nan)
+        ctx.run_batch(frames)
+        for k, ((vol, ao), (rvol, rao)) in enumerate(zip(outs, refs)):
+            assert np.array_equal(vol, rvol), (rep, k)
+            assert np.array_equal(ao, rao), (rep, k)
+    ctx.set_params(ao_normals=p2v.NORMALS_LIST, ao_levels=3)
+
+
+def test_persistent_and_lane_batches_agree_with_device_buffers(ctx):
+    """Device-resident lists and volumes (the volume doubles as the AO stage's level 0): the persistent launch
+    and the lanes' own AO kernels give the same bits."""
+    torch = pytest.importorskip("torch")
+    traj = small_trajectory(k=5, seed=46)
+    params = dict(AO, ao_normals=p2v.NORMALS_GRADIENT)
+    res = {}
+    for pers in (0, 1):
+        ctx.set_params(batch_lanes=2, batch_graph=1, batch_persistent=pers, **params)
+        frames, outs = [], []
+        for f, size, _ in traj:
+            d_in = torch.from_numpy(f.xyzr).cuda()
+            d_ao = torch.full((f.n,), float("nan"), device="cuda")
+            d_vol = torch.full((size[0] * size[1] * size[2],), float("nan"), device="cuda")
+            frames.append(dict(lists=[p2v.ParticleList(d_in, p2v.VERTDATA_FLOAT_XYZR, count=f.n, ao_out=d_ao)],
+                               bbox=f.bbox, out=d_vol, size=size))
+            outs.append((d_vol, d_ao))
+        for _ in range(3):
+            ctx.run_batch(frames)
+        torch.cuda.synchronize()
+        res[pers] = [(v.cpu().numpy(), a.cpu().numpy()) for v, a in outs]
+    for k, ((v0, a0), (v1, a1)) in enumerate(zip(res[0], res[1])):
+        assert np.array_equal(v0, v1), k
+        assert np.array_equal(a0, a1), k
+        assert not np.isnan(a1).any(), k
+    ctx.set_params(ao_normals=p2v.NORMALS_LIST)
+
+
+def test_queue_wait_runs_out_and_the_context_survives(ctx):
+    """The batch AO queue's bounded dependency wait: with the test hook the first mip level never reports its
+    completion, so the items that need it poll queue_wait_polls times, record the timeout and stop the queue.
+    p2v_run_batch reports P2V_ETIMEOUT; the next batch on the same context runs normally and gives the bits of
+    p2v_run_frame."""
+    traj = small_trajectory(k=4, seed=47)
+    params = dict(AO, ao_levels=0)
+    ctx.set_params(batch_lanes=2, batch_graph=0, batch_persistent=1, queue_wait_polls=2000, test_hold_queue=1,
+                   **params)
+    frames, _ = batch_frames(traj, True)
+    with pytest.raises(p2v.P2VError) as err:
+        ctx.run_batch(frames)
+    assert err.value.status == p2v.ETIMEOUT
+    ctx.set_params(queue_wait_polls=0, test_hold_queue=0)
+    refs = reference_with(ctx, traj, params)
+    ctx.set_params(batch_lanes=2, batch_graph=0, batch_persistent=1, **params)
+    frames, outs = batch_frames(traj, True)
+    ctx.run_batch(frames)
+    for k, ((vol, ao), (rvol, rao)) in enumerate(zip(outs, refs)):
+        assert np.array_equal(vol, rvol), k
+        assert np.array_equal(ao, rao), k
+    ctx.set_params(ao_levels=3)

@@ -98,3 +98,19 @@ def test_mixed_list_types(ctx):
 def test_lj_liquid_full_size(ctx):
     f = synth.lj_liquid(seed=2)
     assert check(ctx, f.xyzr, f.bbox, f.res) in COUNTING
+
+
+@pytest.mark.parametrize("n", [1, 2, 37])
+def test_long_empty_runs(ctx, n):
+    """A sparse frame on a 160^3 grid (4.3M cells): the cell starts of runs of up to millions of empty cells,
+    which the fill takes in chunks of 8192 cells."""
+    rng = np.random.default_rng(90 + n)
+    x = np.empty((n, 4), np.float32)
+    x[:, :3] = rng.uniform(0, 100, (n, 3))
+    x[:, 3] = 0.5
+    h = np.float32(100.0 / 159.0)
+    if n >= 2:  # the second particle 50 rows of cells after the first: a run of about 8100 cells between them
+        x[1, :3] = x[0, :3]
+        x[1, 1] += np.float32(50.0) * h
+        x[1, 0] = np.float32(0.25) * h
+    assert check(ctx, x, (0.0, 0.0, 0.0, 100.0, 100.0, 100.0), (160, 160, 160)) == 0   # the radix sort
