@@ -207,6 +207,10 @@ typedef struct p2v_params {
                                  with P2V_ETIMEOUT; 0 = the default (2^22, a second or more) */
     int32_t test_hold_queue;  /* test hook: the first mip level the queue builds never reports its completion, so
                                  the items that need it wait until queue_wait_polls runs out (0) */
+    int32_t sort_wait_polls;  /* polls of the binning radix sort's decoupled look-back before the frame gives up
+                                 with P2V_ETIMEOUT (the frame's grid is then empty); 0 = the default (2^22) */
+    int32_t test_hold_sort;   /* test hook: the second tile of the binning's first radix pass never publishes its
+                                 digit counts, so the tiles after it wait until sort_wait_polls runs out (0) */
 } p2v_params;
 
 /* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,

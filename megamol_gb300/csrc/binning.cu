@@ -249,16 +249,20 @@ __device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) {
 
 // One pass over digit (key >> shift) & (RADIX - 1). Tiles are taken in launch order from a counter; each
 // tile ranks its keys stably (warp match on the digit, per-warp digit counters), publishes its digit
-// counts, resolves its global offsets by decoupled look-back (bounded spins), stages the tile in digit
-// order in shared memory and writes runs of equal digits contiguously.
+// counts, resolves its global offsets by decoupled look-back, stages the tile in digit order in shared
+// memory and writes runs of equal digits contiguously.
+// The look-back waits are bounded (wait_polls polls of a predecessor that has published nothing). A wait
+// that runs out records ERR_LOOKBACK_TIMEOUT; every other wait then stops at its next poll and later passes
+// return at once. A tile that gave up adds only the counts it saw, so its destinations stay at or below the
+// true ones (inside the output); sort_sanitize_kernel then replaces the unfinished output by a valid one.
 template<bool GATHER, int BITS>
 __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_t* __restrict__ keys_in,
     const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n,
     int shift, const uint32_t* __restrict__ digit_offsets, uint32_t* __restrict__ tile_counter,
     uint32_t* __restrict__ status, uint32_t* __restrict__ err, const float4* __restrict__ xyzr_in,
     float4* __restrict__ rec_a, int4* __restrict__ rec_b, float4* __restrict__ xyzr_out, GridGeo geo,
-    const FrameScalars* __restrict__ gate) {
-    if (radix_skipped(gate))
+    const FrameScalars* __restrict__ gate, uint32_t wait_polls, int32_t hold_tile) {
+    if (radix_skipped(gate) || (ld_volatile(err) & ERR_LOOKBACK_TIMEOUT))
         return;
     constexpr int RADIX = 1 << BITS;
     constexpr uint32_t DMASK = RADIX - 1u;
@@ -328,7 +332,8 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
         count[e] = run;
         tsum += run;
         // publish the tile aggregate (or the inclusive prefix for tile 0) before looking back
-        st_volatile(status + (size_t) tile * RADIX + d, (tile == 0 ? FLAG_PRE : FLAG_AGG) | run);
+        if ((int32_t) tile != hold_tile)
+            st_volatile(status + (size_t) tile * RADIX + d, (tile == 0 ? FLAG_PRE : FLAG_AGG) | run);
     }
     // tile-local exclusive scan over digits (block scan of the per-thread digit sums)
     uint32_t incl = tsum;
@@ -362,10 +367,12 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
             while (t >= 0) {
                 const uint32_t sv = ld_volatile(status + (size_t) t * RADIX + d);
                 if ((sv & FLAG_MASK) == 0u) {
-                    if (++spins > SPIN_LIMIT) {
+                    if (++spins > wait_polls) {
                         atomicOr(err, ERR_LOOKBACK_TIMEOUT);
                         break;
                     }
+                    if (ld_volatile(err) & ERR_LOOKBACK_TIMEOUT)
+                        break;  // another wait gave up: the pass is void
                     continue;
                 }
                 excl += sv & COUNT_MASK;
@@ -373,7 +380,8 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
                     break;
                 --t;
             }
-            st_volatile(status + (size_t) tile * RADIX + d, FLAG_PRE | (excl + count[e]));
+            if ((int32_t) tile != hold_tile)
+                st_volatile(status + (size_t) tile * RADIX + d, FLAG_PRE | (excl + count[e]));
         }
         s_base[d] = digit_offsets[d] + excl;
     }
@@ -410,6 +418,19 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
             if (xyzr_out)
                 xyzr_out[dst] = p;
         }
+    }
+}
+
+// After a radix sort whose look-back gave up: every particle gets the invalid key nbins and the identity
+// order, a valid sorted state (an empty grid), so that no later stage indexes with unfinished output. The
+// frame reports P2V_ETIMEOUT.
+__global__ void __launch_bounds__(256) sort_sanitize_kernel(uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+    uint32_t n, uint32_t nbins, const uint32_t* __restrict__ err, const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate) || !(ld_volatile(err) & ERR_LOOKBACK_TIMEOUT))
+        return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        keys[i] = nbins;
+        vals[i] = i;
     }
 }
 
@@ -780,7 +801,8 @@ cudaError_t launch_onesweep_bits(uint32_t tiles, SortBuffers& b, int cur, uint32
     onesweep_kernel<GATHER, BITS><<<tiles, SORT_THREADS, smem, st>>>(b.keys[cur],
         (cur == 0 && b.implicit_vals0 && b.first_pass) ? nullptr : b.vals[cur], b.keys[cur ^ 1],
         b.vals[cur ^ 1], n, shift, offs, counter, b.status, b.err, GATHER ? b.xyzr_in : nullptr,
-        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, GATHER ? b.xyzr_out : nullptr, b.geo, gate);
+        GATHER ? b.rec_a : nullptr, GATHER ? b.rec_b : nullptr, GATHER ? b.xyzr_out : nullptr, b.geo, gate,
+        b.wait_polls ? b.wait_polls : SPIN_LIMIT, b.first_pass ? b.hold_tile : -1);
     return cudaSuccess;
 }
 
@@ -866,6 +888,8 @@ cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32
     if ((e = launch_sort(b, n, g.nbins, sms, st, gate, counting)) != cudaSuccess)
         return e;
     const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n + 1, 256), sms * 8));
+    if (n > 0)
+        sort_sanitize_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], b.vals[b.result], n, g.nbins, b.err, gate);
     cell_start_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, start, gaps, gap_cap, fs, gate);
     cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs, gate);
     count_valid_kernel<<<1, 1, 0, st>>>(start, g.nbins, fs);

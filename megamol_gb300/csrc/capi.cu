@@ -724,6 +724,10 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         sb.xyzr_out = xs.as<float4>();
     }
     sb.geo = g;
+    if (P.sort_wait_polls < 0)
+        return fail(P2V_EINVAL, "sort_wait_polls must be >= 0");
+    sb.wait_polls = (uint32_t) P.sort_wait_polls;
+    sb.hold_tile = P.test_hold_sort ? 1 : -1;
     P2V_CUDA_TRY(launch_bin_sort(sb, n, g, counting ? pp.bcount.as<uint32_t>() : nullptr, cstart.as<uint32_t>(),
                                  gaps.as<uint4>(), gap_cap, fs, sms, st));
     const uint32_t* skeys = sb.keys[sb.result];
@@ -1704,6 +1708,8 @@ void p2v_params_default(p2v_params* p) {
     p->batch_persistent = 1;
     p->queue_wait_polls = 0;
     p->test_hold_queue = 0;
+    p->sort_wait_polls = 0;
+    p->test_hold_sort = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {

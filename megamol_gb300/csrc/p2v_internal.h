@@ -38,6 +38,8 @@ struct SortBuffers {
     int result;            // index of the buffers holding the sorted output
     bool implicit_vals0;   // vals[0] holds no input values: the first pass takes the identity (indices)
     bool first_pass;       // set by launch_sort for its own bookkeeping
+    uint32_t wait_polls = 0;  // polls of a look-back wait before the sort gives up (0: SPIN_LIMIT)
+    int32_t hold_tile = -1;   // test hook: this tile of the first pass never publishes its counts (-1 none)
 };
 
 cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,

@@ -114,3 +114,40 @@ def test_long_empty_runs(ctx, n):
         x[1, 1] += np.float32(50.0) * h
         x[1, 0] = np.float32(0.25) * h
     assert check(ctx, x, (0.0, 0.0, 0.0, 100.0, 100.0, 100.0), (160, 160, 160)) == 0   # the radix sort
+
+
+@pytest.mark.parametrize("with_ao", [False, True])
+def test_lookback_wait_runs_out_and_the_context_survives(ctx, with_ao):
+    """The radix sort's bounded decoupled look-back: with the test hook the second tile of the first pass never
+    publishes its digit counts, so the tiles after it poll sort_wait_polls times, record the timeout, and the
+    sort's unfinished output is replaced by a valid one (every particle in the invalid cell, identity order)
+    before a later stage reads it. p2v_run_frame reports P2V_ETIMEOUT; the next frame on the same context gives
+    the bits of a frame before the timeout. with_ao: the AO stages (mip levels, gradient normals, cone march)
+    run on that output as well."""
+    rng = np.random.default_rng(95)
+    n = 30_000  # 8 sort tiles of 4096 keys; 102^3 cells > 64 n: the radix sort alone
+    x = np.empty((n, 4), np.float32)
+    x[:, :3] = rng.uniform(0, 50, (n, 3))
+    x[:, 3] = rng.uniform(0.4, 0.6, n)
+    bbox = (0.0, 0.0, 0.0, 50.0, 50.0, 50.0)
+    ao_params = dict(ao_mode=p2v.AO_CONE, ao_volume=p2v.AOVOL_DENSITY, ao_volume_scale=1.0, ao_cones=8,
+                     ao_steps=32, ao_levels=3, ao_normals=p2v.NORMALS_GRADIENT) if with_ao else dict(ao_mode=p2v.AO_NONE)
+
+    def frame():
+        ctx.set_params(sizex=100, sizey=100, sizez=100, normalize=1, forSurfaceReconstruction=0, **ao_params)
+        vol = np.full(100 ** 3, np.nan, np.float32)
+        ao = np.full(n, np.nan, np.float32)
+        ctx.run_frame([p2v.ParticleList(x, p2v.VERTDATA_FLOAT_XYZR, ao_out=ao if with_ao else None)], bbox, vol)
+        return vol, ao
+
+    before = frame()
+    assert ctx.stats()["cell_max_count"] == 0  # the radix path
+    ctx.set_params(sort_wait_polls=1000, test_hold_sort=1)
+    with pytest.raises(p2v.P2VError) as err:
+        frame()
+    assert err.value.status == p2v.ETIMEOUT
+    ctx.set_params(sort_wait_polls=0, test_hold_sort=0)
+    after = frame()
+    assert np.array_equal(before[0], after[0])
+    assert np.array_equal(before[1], after[1], equal_nan=True)
+    ctx.set_params(ao_mode=p2v.AO_NONE, ao_normals=p2v.NORMALS_LIST)
