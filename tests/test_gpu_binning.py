@@ -125,7 +125,7 @@ def test_lookback_wait_runs_out_and_the_context_survives(ctx, with_ao):
     the bits of a frame before the timeout. with_ao: the AO stages (mip levels, gradient normals, cone march)
     run on that output as well."""
     rng = np.random.default_rng(95)
-    n = 30_000  # 8 sort tiles of 4096 keys; 102^3 cells > 64 n: the radix sort alone
+    n = 30_000  # 8 sort tiles of 4096 keys; 162^3 cells > 64 n: the radix sort alone
     x = np.empty((n, 4), np.float32)
     x[:, :3] = rng.uniform(0, 50, (n, 3))
     x[:, 3] = rng.uniform(0.4, 0.6, n)
@@ -134,8 +134,8 @@ def test_lookback_wait_runs_out_and_the_context_survives(ctx, with_ao):
                      ao_steps=32, ao_levels=3, ao_normals=p2v.NORMALS_GRADIENT) if with_ao else dict(ao_mode=p2v.AO_NONE)
 
     def frame():
-        ctx.set_params(sizex=100, sizey=100, sizez=100, normalize=1, forSurfaceReconstruction=0, **ao_params)
-        vol = np.full(100 ** 3, np.nan, np.float32)
+        ctx.set_params(sizex=160, sizey=160, sizez=160, normalize=1, forSurfaceReconstruction=0, **ao_params)
+        vol = np.full(160 ** 3, np.nan, np.float32)
         ao = np.full(n, np.nan, np.float32)
         ctx.run_frame([p2v.ParticleList(x, p2v.VERTDATA_FLOAT_XYZR, ao_out=ao if with_ao else None)], bbox, vol)
         return vol, ao
