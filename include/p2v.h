@@ -211,6 +211,7 @@ typedef struct p2v_params {
                                  with P2V_ETIMEOUT (the frame's grid is then empty); 0 = the default (2^22) */
     int32_t test_hold_sort;   /* test hook: the second tile of the binning's first radix pass never publishes its
                                  digit counts, so the tiles after it wait until sort_wait_polls runs out (0) */
+    int32_t ao_march;         /* p2v_ao_march: the kernel of the plain cone march (P2V_AO_MARCH_THREAD) */
 } p2v_params;
 
 /* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,
@@ -228,6 +229,9 @@ typedef enum p2v_aos_deposit { P2V_AOS_DEPOSIT_CPU = 0, P2V_AOS_DEPOSIT_GLSL = 1
  * trilinearly at the particle's position (clamped into the node range); a vanishing gradient gives a zero
  * normal (AO 1). Needs a scalar grid (aggregator 0 or 1). */
 typedef enum p2v_ao_normals { P2V_NORMALS_LIST = 0, P2V_NORMALS_GRADIENT = 1 } p2v_ao_normals;
+/* The plain cone march's kernel (both give the same bits): one thread marches all cones of a particle, or
+ * one warp per cone of a particle with its lanes taking the cone's steps. */
+typedef enum p2v_ao_march { P2V_AO_MARCH_THREAD = 0, P2V_AO_MARCH_WARP = 1 } p2v_ao_march;
 
 typedef struct p2v_stats {
     uint64_t particles_in;       /* records presented */

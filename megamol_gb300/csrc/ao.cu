@@ -49,20 +49,22 @@ __global__ void __launch_bounds__(128) cone_ao_kernel(const ConeParams cp, const
     ao[w] = cone_ao_at<true>(cp, xyzr[o], nrm[o]);
 }
 
-// The learned AO's fallback list (its length a device-side count, usually tiny): latency matters, so a
-// block takes one particle with one warp per cone, and the lanes of a warp take the cone's samples (32 at a
-// time: the step positions are tabulated, so all samples load at once). Every lane then runs the march's
-// recurrence over the shuffled samples in step order with the same early exit, the block's first thread
-// adds the cones in cone order: the result has the bits of cone_ao_kernel. A bounded grid strides over the
-// list.
+// One warp per cone: a block takes one particle with one warp per cone, and the lanes of a warp take the
+// cone's samples (32 at a time: the step positions are tabulated, so all samples load at once). Every lane
+// then runs the march's recurrence over the shuffled samples in step order with the same early exit, the
+// block's first thread adds the cones in cone order: the result has the bits of cone_ao_kernel. A bounded
+// grid strides over the particles: the learned AO's fallback list (list and its device-side length n_dev,
+// usually tiny, where latency matters), or a whole frame (no list: particle i; P2V_AO_MARCH_WARP), where
+// every lane stays busy whatever step its cone ends at, at the price of the samples past the early exit.
 __global__ void __launch_bounds__(32 * MAX_CONES) cone_ao_list_kernel(const ConeParams cp,
     const uint32_t* __restrict__ list, const float4* __restrict__ xyzr, const float4* __restrict__ nrm, uint32_t n,
     const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ out_order, float* __restrict__ ao) {
     __shared__ float s_acc[MAX_CONES];
     const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-    n = min(n, *n_dev);
+    if (n_dev)
+        n = min(n, *n_dev);
     for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
-        const uint32_t o = list[i];
+        const uint32_t o = list ? list[i] : i;
         const float4 p = xyzr[o];
         const float4 nv = nrm[o];
         float x[3], nn[3];
@@ -263,6 +265,16 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
         for (int a = 0; a < 3; ++a)
             sd[a] = dd[a];
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cone_ao_warp(const ConeParams& cp, const float4* xyzr, const float4* nrm, uint32_t n,
+    const uint32_t* out_order, float* ao, int sms, cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    const int threads = 32 * cp.ncones;
+    const unsigned grd = (unsigned) std::min<uint64_t>(n, (uint64_t) sms * std::max(1, 2048 / threads));
+    cone_ao_list_kernel<<<grd, threads, 0, st>>>(cp, nullptr, xyzr, nrm, n, nullptr, out_order, ao);
     return cudaGetLastError();
 }
 

@@ -114,6 +114,9 @@ cudaError_t launch_sort_particles(const uint32_t* order, uint32_t n, const float
 // when out_order is given (sorted copies in, input order out), else to ao[that index]
 cudaError_t launch_cone_ao(const ConeParams& cp, const uint32_t* order, const float4* xyzr, const float4* nrm,
     uint32_t n, const uint32_t* n_dev, const uint32_t* out_order, float* ao, cudaStream_t st);
+// the whole frame with one warp per cone of a particle (the bits of launch_cone_ao)
+cudaError_t launch_cone_ao_warp(const ConeParams& cp, const float4* xyzr, const float4* nrm, uint32_t n,
+    const uint32_t* out_order, float* ao, int sms, cudaStream_t st);
 cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32_t n, unsigned long long* acc,
     float* tex, const uint32_t* order, const float4* nrm, int mode, float* ao, int sms, cudaStream_t st);
 // unit normals down the density gradient of `grid` (geometry geo) at xyzr[j], into nrm[j] (P2V_NORMALS_GRADIENT)

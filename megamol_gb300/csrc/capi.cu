@@ -259,7 +259,7 @@ struct p2v_ctx {
                          bool allow_graph, float* ms_out);
     bool batch_persistent_applies() const {
         return prm.batch_persistent != 0 && prm.ao_mode == P2V_AO_CONE && prm.ao_volume == P2V_AOVOL_DENSITY &&
-               (prm.aggregator == 0 || prm.aggregator == 1);
+               prm.ao_march == P2V_AO_MARCH_THREAD && (prm.aggregator == 0 || prm.aggregator == 1);
     }
     void drop_graph() {
         if (b_exec)
@@ -1190,8 +1190,12 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
             return P2V_OK;
         }
         P2V_CUDA_TRY(to_sorted());
-        P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr, order,
-                                    ao.as<float>(), st));
+        if (P.ao_march == P2V_AO_MARCH_WARP)
+            P2V_CUDA_TRY(launch_cone_ao_warp(cp, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, order, ao.as<float>(),
+                                             sms, st));
+        else
+            P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr, order,
+                                        ao.as<float>(), st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_LEARNED) {
@@ -1710,6 +1714,7 @@ void p2v_params_default(p2v_params* p) {
     p->test_hold_queue = 0;
     p->sort_wait_polls = 0;
     p->test_hold_sort = 0;
+    p->ao_march = P2V_AO_MARCH_THREAD;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {

@@ -32,6 +32,7 @@ AO_NONE, AO_CONE, AO_AOSPHERE_AXES, AO_AOSPHERE_NORMAL, AO_LEARNED = range(5)
 AOVOL_DENSITY, AOVOL_MDAO = 0, 1
 AOS_DEPOSIT_CPU, AOS_DEPOSIT_GLSL = 0, 1
 NORMALS_LIST, NORMALS_GRADIENT = 0, 1
+AO_MARCH_THREAD, AO_MARCH_WARP = 0, 1
 STATUS_NAMES = {0: "P2V_OK", 1: "P2V_EINVAL", 2: "P2V_ENOMEM", 3: "P2V_ECUDA", 4: "P2V_ETIMEOUT", 5: "P2V_EDOMAIN",
                 6: "P2V_EUNSUPPORTED"}
 
@@ -61,7 +62,7 @@ class Params(C.Structure):
         ("ao_normals", C.c_int32), ("mma_wait_polls", C.c_int32), ("test_hold_mma", C.c_int32),
         ("slab_z0", C.c_int32), ("slab_z1", C.c_int32),
         ("batch_persistent", C.c_int32), ("queue_wait_polls", C.c_int32), ("test_hold_queue", C.c_int32),
-        ("sort_wait_polls", C.c_int32), ("test_hold_sort", C.c_int32),
+        ("sort_wait_polls", C.c_int32), ("test_hold_sort", C.c_int32), ("ao_march", C.c_int32),
     ]
 
 

@@ -38,7 +38,8 @@ def run_ao(ctx, f, normals, **params):
                 accumulate=p2v.ACCUM_EXACT, forSurfaceReconstruction=0, mass_normalize=0, kernel=p2v.KERNEL_BUMP,
                 ao_volume=p2v.AOVOL_DENSITY, ao_volume_scale=1.0, ao_cones=3, ao_steps=0, ao_levels=0,
                 ao_apex_deg=50.0, ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1,
-                aos_deposit=p2v.AOS_DEPOSIT_CPU, aos_clip=0, aos_clip_plane=[0.0] * 4, ao_normals=p2v.NORMALS_LIST)
+                aos_deposit=p2v.AOS_DEPOSIT_CPU, aos_clip=0, aos_clip_plane=[0.0] * 4, ao_normals=p2v.NORMALS_LIST,
+                ao_march=p2v.AO_MARCH_THREAD)
     base.update(params)
     ctx.set_params(**base)
     ao = np.full(f.n, np.nan, np.float32)
@@ -178,3 +179,19 @@ def test_gradient_normals_ao_pipeline_lj_small(ctx):
     ref = cone_oracle(f, vol2, nrm, 8, 32, 3)
     d = np.abs(ao - ref)
     assert np.sqrt(np.mean(d ** 2)) <= 1e-5 and d.max() <= 2e-3
+
+
+@pytest.mark.parametrize("early_exit,steps", [(1, 32), (0, 32), (1, 0), (1, 40)])
+def test_warp_march_equals_thread_march(ctx, early_exit, steps):
+    """P2V_AO_MARCH_WARP (one warp per cone of a particle, its lanes taking the steps 32 at a time, the march's
+    recurrence replayed over the shuffled samples) gives the bits of the thread-per-particle march, with and
+    without early exit, with the step table of the reference's growth rule (steps 0) and with more than 32
+    steps (two rounds of lanes)."""
+    f = synth.lj_liquid(cells=20, res=48, seed=36)
+    nrm = synth.random_normals(f.n, 37)
+    nrm[::97] = 0.0  # particles without a normal: AO 1
+    kw = dict(ao_cones=8, ao_steps=steps, ao_levels=3, ao_early_exit=early_exit, ao_mode=p2v.AO_CONE)
+    a, _, _ = run_ao(ctx, f, nrm, ao_march=p2v.AO_MARCH_THREAD, **kw)
+    b, _, _ = run_ao(ctx, f, nrm, ao_march=p2v.AO_MARCH_WARP, **kw)
+    assert np.array_equal(a, b)
+    assert (b[::97] == 1.0).all()
