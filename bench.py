@@ -594,10 +594,10 @@ def run_ours(args):
 def run_batch_bench(args):
     """Batched-trajectory workload: 64 frames of 1-8 Gaussian blobs, particle counts log-uniform in
     [50k, 2M], grids 64^3-256^3 matched to extent, density + plain cone AO (8 cones x 32 steps, 3 levels,
-    gradient normals). One step = the whole batch through p2v_run_batch (one CUDA-graph launch: the lanes'
-    binning and density, then one persistent launch for every frame's AO); the autotuner picks the density
-    tile and the lane count first. Also reported: the same frames one p2v_run_frame call after another, the
-    batch without its graph, and the batch with each lane running its own AO kernels."""
+    gradient normals). One step = the whole batch through p2v_run_batch (one CUDA-graph launch); the
+    autotuner picks the density tile, the lane count and the batch AO form (one persistent launch for every
+    frame's AO after the lanes, or the lanes' own AO kernels) first. Also reported: the same frames one
+    p2v_run_frame call after another, the batch without its graph, and both batch AO forms."""
     import torch
 
     from megamol_gb300 import p2v, synth
@@ -635,7 +635,7 @@ def run_batch_bench(args):
             import torch.distributed as dist
             dist.barrier()
 
-    def timed(frames, steps, warmup, graph=True, persistent=1):
+    def timed(frames, steps, warmup, graph=True, persistent=-1):
         ctx.set_params(batch_graph=1 if graph else 0, batch_persistent=persistent)
         for _ in range(warmup):
             ctx.run_batch(frames)
@@ -654,6 +654,7 @@ def run_batch_bench(args):
     ms = timed(frames_dev, args.steps, max(args.warmup, 3))
     sampler.__exit__()
     ms_eager = timed(frames_dev, max(3, args.steps // 4), 2, graph=False)
+    ms_pers = timed(frames_dev, max(3, args.steps // 2), 3, persistent=1)
     ms_lanes = timed(frames_dev, max(3, args.steps // 2), 3, persistent=0)
     ms_e2e = timed(frames_host, max(3, args.steps // 2), 3)
     # the same frames one p2v_run_frame after another (stream-synchronous per frame)
@@ -688,10 +689,13 @@ def run_batch_bench(args):
                            "ao": "plain cone march, 8 cones x 32 steps, 3-level mip, normals down the density gradient (library)",
                            "l2": "per-step working set several GB > 126 MB L2 (no flush)"},
                 "batch": {"autotuned_tile": tune["tile"], "autotuned_lanes": tune["lanes"],
+                          "autotuned_persistent_ao": tune["persistent"],
                           "ms_graph": ms, "ms_eager": ms_eager, "ms_frame_by_frame": ms_seq,
-                          "ms_lanes_ao_graph": ms_lanes, "speedup_vs_frame_by_frame": ms_seq / ms,
-                          "note": "ms_graph / ms_eager: the AO of every frame in one persistent queue launch "
-                                  "after the lanes; ms_lanes_ao_graph: each lane runs its frames' AO kernels"},
+                          "ms_persistent_ao_graph": ms_pers, "ms_lanes_ao_graph": ms_lanes,
+                          "speedup_vs_frame_by_frame": ms_seq / ms,
+                          "note": "ms_graph / ms_eager: the autotuned configuration; ms_persistent_ao_graph: the "
+                                  "AO of every frame in one persistent queue launch after the lanes; "
+                                  "ms_lanes_ao_graph: each lane runs its frames' AO kernels"},
                 "e2e": {"value": ws * total / (ms_e2e * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e},
                 "gpu_launches": None, "clocks": sampler.summary()}

@@ -199,10 +199,12 @@ typedef struct p2v_params {
                                  aggregators without AO (0, 0) */
     /* --- the persistent batch AO (appended) --- */
     int32_t batch_persistent; /* p2v_run_batch with the cone march on the density (ao_mode P2V_AO_CONE, ao_volume
-                                 P2V_AOVOL_DENSITY, aggregator 0 or 1): the lanes run every frame up to its
-                                 normalised grid, then ONE persistent launch builds every frame's mip levels
-                                 and marches every frame's cones from a device-side work queue (1); 0 = each
-                                 lane runs its frames' AO kernels itself */
+                                 P2V_AOVOL_DENSITY, ao_march P2V_AO_MARCH_THREAD, aggregator 0 or 1): 1 = the
+                                 lanes run every frame up to its normalised grid, then ONE persistent launch
+                                 builds every frame's mip levels and marches every frame's cones from a
+                                 device-side work queue; 0 = each lane runs its frames' AO kernels itself
+                                 (overlapping them with other frames' binning and density); -1 = the choice of
+                                 p2v_autotune_batch, 0 before it has run (-1) */
     int32_t queue_wait_polls; /* polls of a queue item's dependency wait in that launch before the call gives up
                                  with P2V_ETIMEOUT; 0 = the default (2^22, a second or more) */
     int32_t test_hold_queue;  /* test hook: the first mip level the queue builds never reports its completion, so
@@ -394,10 +396,13 @@ typedef struct p2v_tune_report {
     int32_t cand_tile[P2V_TUNE_MAX][3];
     int32_t cand_lanes[P2V_TUNE_MAX];
     float cand_ms[P2V_TUNE_MAX];
+    int32_t persistent;               /* chosen batch AO: 1 the persistent launch, 0 the lanes' own kernels */
+    int32_t cand_persistent[P2V_TUNE_MAX];
 } p2v_tune_report;
 
-/* Time every compiled density tile x lane count on this batch (CUDA events, one warm-up run each) and keep
- * the fastest for later calls whose tile_x / batch_lanes are 0. rep (nullable) receives the table. */
+/* Time every compiled density tile x lane count (x, where the persistent batch AO applies, both batch AO
+ * forms) on this batch (CUDA events, one warm-up run each) and keep the fastest for later calls whose
+ * tile_x / batch_lanes are 0 and batch_persistent is -1. rep (nullable) receives the table. */
 P2V_API p2v_status p2v_autotune_batch(p2v_ctx* ctx, const p2v_batch_item* items, uint32_t count,
                                       p2v_tune_report* rep);
 

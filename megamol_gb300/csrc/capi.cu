@@ -219,6 +219,7 @@ struct p2v_ctx {
     // autotuned choices (0 = none)
     int tuned_tile[3] = {0, 0, 0};
     int tuned_lanes = 0;
+    int tuned_persistent = 0;
     // learned AO
     // p2v_run_ao_on_grid: the density grid the AO stage reads instead of this frame's own (null: none)
     const float* ext_grid = nullptr;
@@ -257,9 +258,15 @@ struct p2v_ctx {
     p2v_status prepare_features(Pipe& pp, ConeParams& cp, cudaStream_t st);
     p2v_status run_batch(const p2v_batch_item* items, uint32_t count, p2v_stats* out, cudaStream_t st,
                          bool allow_graph, float* ms_out);
+    // the AO stage of a batch can run as the persistent launch (cone march of the density, one thread per
+    // particle, a scalar grid)
+    bool batch_persistent_possible() const {
+        return prm.ao_mode == P2V_AO_CONE && prm.ao_volume == P2V_AOVOL_DENSITY && prm.ao_march == P2V_AO_MARCH_THREAD &&
+               (prm.aggregator == 0 || prm.aggregator == 1);
+    }
     bool batch_persistent_applies() const {
-        return prm.batch_persistent != 0 && prm.ao_mode == P2V_AO_CONE && prm.ao_volume == P2V_AOVOL_DENSITY &&
-               prm.ao_march == P2V_AO_MARCH_THREAD && (prm.aggregator == 0 || prm.aggregator == 1);
+        const bool want = prm.batch_persistent < 0 ? tuned_persistent > 0 : prm.batch_persistent != 0;
+        return want && batch_persistent_possible();
     }
     void drop_graph() {
         if (b_exec)
@@ -1709,7 +1716,7 @@ void p2v_params_default(p2v_params* p) {
     p->mma_wait_polls = 0;
     p->test_hold_mma = 0;
     p->slab_z0 = p->slab_z1 = 0;
-    p->batch_persistent = 1;
+    p->batch_persistent = -1;
     p->queue_wait_polls = 0;
     p->test_hold_queue = 0;
     p->sort_wait_polls = 0;
@@ -1835,35 +1842,40 @@ p2v_status p2v_autotune_batch(p2v_ctx* c, const p2v_batch_item* items, uint32_t 
     const p2v_params saved = c->prm;
     const int saved_tile[3] = {c->tuned_tile[0], c->tuned_tile[1], c->tuned_tile[2]};
     const int saved_lanes = c->tuned_lanes;
+    const int npers = c->batch_persistent_possible() ? 2 : 1;
     float best = INFINITY;
-    int bt = -1, bl = -1, nc = 0;
+    int bt = -1, bl = -1, bp = 0, nc = 0;
     p2v_status st = P2V_OK;
     for (int t = 0; t < 3 && st == P2V_OK; ++t)
-        for (int l : lane_opts) {
-            c->prm.tile_x = c->prm.tile_y = c->prm.tile_z = 0;
-            c->prm.batch_lanes = l;
-            c->tuned_tile[0] = tiles[t][0];
-            c->tuned_tile[1] = tiles[t][1];
-            c->tuned_tile[2] = tiles[t][2];
-            float ms = 0.0f;
-            st = c->run_batch(items, count, nullptr, c->own_stream, false, nullptr);  // warm-up, sizes buffers
-            if (st == P2V_OK)
-                st = c->run_batch(items, count, nullptr, c->own_stream, false, &ms);
-            if (st != P2V_OK)
-                break;
-            if (rep && nc < P2V_TUNE_MAX) {
-                for (int a = 0; a < 3; ++a)
-                    rep->cand_tile[nc][a] = tiles[t][a];
-                rep->cand_lanes[nc] = l;
-                rep->cand_ms[nc] = ms;
+        for (int l : lane_opts)
+            for (int pers = 0; pers < npers && st == P2V_OK; ++pers) {
+                c->prm.tile_x = c->prm.tile_y = c->prm.tile_z = 0;
+                c->prm.batch_lanes = l;
+                c->prm.batch_persistent = pers;
+                c->tuned_tile[0] = tiles[t][0];
+                c->tuned_tile[1] = tiles[t][1];
+                c->tuned_tile[2] = tiles[t][2];
+                float ms = 0.0f;
+                st = c->run_batch(items, count, nullptr, c->own_stream, false, nullptr);  // warm-up, sizes buffers
+                if (st == P2V_OK)
+                    st = c->run_batch(items, count, nullptr, c->own_stream, false, &ms);
+                if (st != P2V_OK)
+                    break;
+                if (rep && nc < P2V_TUNE_MAX) {
+                    for (int a = 0; a < 3; ++a)
+                        rep->cand_tile[nc][a] = tiles[t][a];
+                    rep->cand_lanes[nc] = l;
+                    rep->cand_ms[nc] = ms;
+                    rep->cand_persistent[nc] = pers;
+                }
+                ++nc;
+                if (ms < best) {
+                    best = ms;
+                    bt = t;
+                    bl = l;
+                    bp = pers;
+                }
             }
-            ++nc;
-            if (ms < best) {
-                best = ms;
-                bt = t;
-                bl = l;
-            }
-        }
     c->prm = saved;
     if (st != P2V_OK || bt < 0) {
         c->tuned_tile[0] = saved_tile[0];
@@ -1875,11 +1887,13 @@ p2v_status p2v_autotune_batch(p2v_ctx* c, const p2v_batch_item* items, uint32_t 
     for (int a = 0; a < 3; ++a)
         c->tuned_tile[a] = tiles[bt][a];
     c->tuned_lanes = bl;
+    c->tuned_persistent = bp;
     c->drop_graph();
     if (rep) {
         for (int a = 0; a < 3; ++a)
             rep->tile[a] = tiles[bt][a];
         rep->lanes = bl;
+        rep->persistent = bp;
         rep->ms_best = best;
         rep->candidates = std::min(nc, P2V_TUNE_MAX);
     }

@@ -104,7 +104,8 @@ NOALLOC_MAX_VOXELS = 262144  # P2V_NOALLOC_MAX_VOXELS: voxels of p2v_aosphere_ao
 class TuneReportC(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("tile", C.c_int32 * 3), ("lanes", C.c_int32), ("ms_best", C.c_float),
                 ("candidates", C.c_int32), ("cand_tile", (C.c_int32 * 3) * TUNE_MAX),
-                ("cand_lanes", C.c_int32 * TUNE_MAX), ("cand_ms", C.c_float * TUNE_MAX)]
+                ("cand_lanes", C.c_int32 * TUNE_MAX), ("cand_ms", C.c_float * TUNE_MAX),
+                ("persistent", C.c_int32), ("cand_persistent", C.c_int32 * TUNE_MAX)]
 
 
 class VolumeC(C.Structure):
@@ -504,9 +505,9 @@ class Context:
         rep.struct_size = C.sizeof(TuneReportC)
         self._check(self.lib.p2v_autotune_batch(self.h, C.cast(items, C.c_void_p), len(frames), C.byref(rep)))
         n = rep.candidates
-        return dict(tile=list(rep.tile), lanes=rep.lanes, ms_best=rep.ms_best,
-                    candidates=[dict(tile=list(rep.cand_tile[k]), lanes=rep.cand_lanes[k], ms=rep.cand_ms[k])
-                                for k in range(n)])
+        return dict(tile=list(rep.tile), lanes=rep.lanes, persistent=rep.persistent, ms_best=rep.ms_best,
+                    candidates=[dict(tile=list(rep.cand_tile[k]), lanes=rep.cand_lanes[k], ms=rep.cand_ms[k],
+                                     persistent=rep.cand_persistent[k]) for k in range(n)])
 
     def stats(self) -> dict:
         s = StatsC()

@@ -22,6 +22,7 @@ int main(void) {
     F(p2v_params, sort_wait_polls); F(p2v_params, test_hold_sort); F(p2v_params, ao_march);
     F(p2v_batch_item, volume); F(p2v_batch_item, size);
     F(p2v_tune_report, ms_best); F(p2v_tune_report, cand_lanes); F(p2v_tune_report, cand_ms);
+    F(p2v_tune_report, persistent); F(p2v_tune_report, cand_persistent);
     F(p2v_particle_list, count); F(p2v_particle_list, mem); F(p2v_particle_list, ao_out);
     F(p2v_frame, frame_id); F(p2v_frame, lists);
     F(p2v_volume, resolution); F(p2v_volume, min_value); F(p2v_volume, data_hash);

@@ -74,7 +74,7 @@ def test_params_default_mirror_reference_slots(lib):
     assert p.ao_cones == 3 and abs(p.ao_apex_deg - 50) < 1e-6 and abs(p.ao_offset - 0.01) < 1e-7
     assert abs(p.ao_cone_length - 0.8) < 1e-7 and p.mdao_volume_size == 128
     assert p.batch_lanes == 0 and p.batch_graph == 1 and p.vector_grid == 0
-    assert p.batch_persistent == 1 and p.queue_wait_polls == 0 and p.test_hold_queue == 0
+    assert p.batch_persistent == -1 and p.queue_wait_polls == 0 and p.test_hold_queue == 0
     assert p.sort_wait_polls == 0 and p.test_hold_sort == 0 and p.ao_march == p2v.AO_MARCH_THREAD
     assert lib.p2v_abi_version() == 9
 

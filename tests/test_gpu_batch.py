@@ -122,6 +122,28 @@ def test_autotune_picks_a_measured_configuration(ctx):
         assert np.array_equal(vol, rvol)
 
 
+def test_autotune_chooses_the_batch_ao_form(ctx):
+    """With the cone march on the density the autotuner also times both batch AO forms (the persistent launch
+    and the lanes' own kernels): 24 candidates; batch_persistent = -1 then follows its choice, and either form
+    gives the bits of p2v_run_frame."""
+    traj = small_trajectory(k=5, seed=61)
+    params = dict(AO, ao_normals=p2v.NORMALS_GRADIENT)
+    ctx.set_params(batch_lanes=0, tile_x=0, tile_y=0, tile_z=0, batch_persistent=-1, **params)
+    frames, outs = batch_frames(traj, True)
+    rep = ctx.autotune_batch(frames)
+    assert len(rep["candidates"]) == 24
+    assert {c["persistent"] for c in rep["candidates"]} == {0, 1}
+    assert rep["persistent"] in (0, 1)
+    assert rep["ms_best"] == min(c["ms"] for c in rep["candidates"])
+    refs = reference_with(ctx, traj, params)
+    ctx.set_params(batch_lanes=0, tile_x=0, tile_y=0, tile_z=0, batch_persistent=-1, **params)
+    ctx.run_batch(frames)
+    for k, ((vol, ao), (rvol, rao)) in enumerate(zip(outs, refs)):
+        assert np.array_equal(vol, rvol), k
+        assert np.array_equal(ao, rao), k
+    ctx.set_params(ao_normals=p2v.NORMALS_LIST, ao_mode=p2v.AO_NONE)
+
+
 def test_empty_and_single_frame_batches(ctx):
     ctx.set_params(batch_lanes=4, ao_mode=p2v.AO_NONE)
     meta, stats = ctx.run_batch([])
