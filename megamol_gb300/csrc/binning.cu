@@ -434,13 +434,18 @@ __global__ void __launch_bounds__(256) sort_sanitize_kernel(uint32_t* __restrict
     }
 }
 
-// start[c] = first sorted position whose key is >= c, for c in [0, nbins]. Short gaps are filled by
-// the thread that sees them; gaps of 64 cells or more are queued for a block-wide fill.
+// start[c] = first sorted position whose key is >= c, for c in [0, nbins], in two balanced steps with
+// coalesced stores. (1) The start of every CELL_BLOCK-th cell, bstart[b] = start[CELL_BLOCK b], from the
+// boundaries of the sorted keys: boundary i (between keys[i-1] and keys[i]) starts the cells
+// (keys[i-1], keys[i]], so the blocks whose first cell lies there; a run of 32 or more such blocks (a long
+// stretch of empty cells) is queued in chunks for cell_gap_fill_kernel. (2) Every cell c: the keys of its
+// block lie in [bstart[b], bstart[b+1]) (up to n for the last block), start[c] is the first of them >= c.
 constexpr uint32_t GAP_CHUNK = 8192;
+constexpr uint32_t CELL_BLOCK = 64;
 
-__global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t nbins,
-    uint32_t* __restrict__ start, uint4* __restrict__ gaps, uint32_t gap_cap, FrameScalars* __restrict__ fs,
-    const FrameScalars* __restrict__ gate) {
+__global__ void __launch_bounds__(256) block_starts_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+    uint32_t nbins, uint32_t* __restrict__ bstart, uint4* __restrict__ gaps, uint32_t gap_cap,
+    FrameScalars* __restrict__ fs, const FrameScalars* __restrict__ gate) {
     if (radix_skipped(gate))
         return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
@@ -450,19 +455,21 @@ __global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restr
             hi = nbins;
         if (lo > hi)
             continue;
-        if (hi - lo < 64u) {
-            for (uint32_t c = lo; c <= hi; ++c)
-                start[c] = i;
+        const uint32_t b0 = (uint32_t) (((uint64_t) lo + CELL_BLOCK - 1) / CELL_BLOCK), b1 = hi / CELL_BLOCK;
+        if (b0 > b1)
+            continue;
+        if (b1 - b0 < 32u) {
+            for (uint32_t bb = b0; bb <= b1; ++bb)
+                bstart[bb] = i;
         } else {
-            // a long run of empty cells: chunks of at most GAP_CHUNK cells, one block each in
-            // cell_gap_fill_kernel (a sparse grid can hold a single run of millions of cells). Runs are disjoint
-            // and longer than 64 cells, so the chunks number at most (nbins + 1) (1/GAP_CHUNK + 1/65), below
-            // the nbins / 64 + 2 entries the list holds
-            const uint32_t nch = (uint32_t) (((uint64_t) hi - lo + GAP_CHUNK) / GAP_CHUNK);
+            // chunks of at most GAP_CHUNK blocks, one CTA each in cell_gap_fill_kernel. Runs are disjoint and
+            // longer than 32 blocks, so the chunks number at most nblk (1/GAP_CHUNK + 1/33), far below the
+            // nbins / 64 + 2 entries the list holds
+            const uint32_t nch = (uint32_t) (((uint64_t) b1 - b0 + GAP_CHUNK) / GAP_CHUNK);
             const uint32_t slot = atomicAdd(&fs->ngaps, nch);
             for (uint32_t q = 0; q < nch; ++q) {
-                const uint64_t c0 = (uint64_t) lo + (uint64_t) q * GAP_CHUNK;
-                const uint64_t c1 = std::min<uint64_t>(hi, c0 + GAP_CHUNK - 1);
+                const uint64_t c0 = (uint64_t) b0 + (uint64_t) q * GAP_CHUNK;
+                const uint64_t c1 = std::min<uint64_t>(b1, c0 + GAP_CHUNK - 1);
                 if ((uint64_t) slot + q < gap_cap)
                     gaps[slot + q] = make_uint4((uint32_t) c0, (uint32_t) c1, i, 0u);
                 else
@@ -470,6 +477,26 @@ __global__ void __launch_bounds__(256) cell_start_kernel(const uint32_t* __restr
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(256) cell_starts_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+    uint32_t nbins, const uint32_t* __restrict__ bstart, uint32_t nblk, uint32_t* __restrict__ start,
+    const FrameScalars* __restrict__ gate) {
+    if (radix_skipped(gate))
+        return;
+    const uint64_t c = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+    if (c > nbins)
+        return;
+    const uint32_t b = (uint32_t) (c / CELL_BLOCK);
+    uint32_t lo = bstart[b], hi = b + 1 < nblk ? bstart[b + 1] : n;
+    while (lo < hi) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if ((uint64_t) keys[mid] < c)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    start[c] = lo;
 }
 
 __global__ void __launch_bounds__(256) cell_gap_fill_kernel(const uint4* __restrict__ gaps, uint32_t gap_cap,
@@ -858,8 +885,13 @@ size_t bin_scan_words(uint32_t nbins) {
     return (size_t) ceil_div(nbins + 1, SCAN_TILE);
 }
 
+uint32_t cell_block_count(uint32_t nbins) {
+    return (uint32_t) (((uint64_t) nbins + CELL_BLOCK) / CELL_BLOCK);  // blocks of cells 0 .. nbins
+}
+
 cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32_t* counts, uint32_t* start,
-                            uint4* gaps, uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st) {
+                            uint32_t* bstart, uint4* gaps, uint32_t gap_cap, FrameScalars* fs, int sms,
+                            cudaStream_t st) {
     const uint32_t nb = g.nbins + 1;
     cudaError_t e;
     const bool counting = counts != nullptr && n > 0;
@@ -890,8 +922,11 @@ cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32
     const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n + 1, 256), sms * 8));
     if (n > 0)
         sort_sanitize_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], b.vals[b.result], n, g.nbins, b.err, gate);
-    cell_start_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, start, gaps, gap_cap, fs, gate);
-    cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs, gate);
+    const uint32_t nblk = cell_block_count(g.nbins);
+    block_starts_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, bstart, gaps, gap_cap, fs, gate);
+    cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, bstart, fs, gate);
+    cell_starts_kernel<<<(unsigned) (((uint64_t) g.nbins + 256) / 256), 256, 0, st>>>(b.keys[b.result], n, g.nbins,
+                                                                                      bstart, nblk, start, gate);
     count_valid_kernel<<<1, 1, 0, st>>>(start, g.nbins, fs);
     return cudaGetLastError();
 }

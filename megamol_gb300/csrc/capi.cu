@@ -71,6 +71,7 @@ struct Pipe {
     DevBuf nrm, ao, mips, aos_acc, aos_tex, mdao_acc, mdao_vol, fb_list, wts, wsorted, wsum;
     DevBuf vdens, vdirs, vkeys0, vkeys1, vvals0, vvals1, vout;  // the vector aggregator's grid outputs
     DevBuf bcount;                         // particles per cell (the counting sort)
+    DevBuf bstart;                         // start of every 64th cell (the radix path's cell starts)
     DevBuf xyzr_s, nrm_s;                  // positions and normals in sorted order (the cone AO stages)
     bool xyzr_sorted = false;              // the binning of this frame wrote xyzr_s
     FeatureTex ftex[MAX_LEVELS];           // the learned AO's feature levels as paired-slice textures
@@ -119,7 +120,7 @@ struct Pipe {
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &xyzr_s, &nrm_s})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &bstart, &xyzr_s, &nrm_s})
             b->release();
         for (FeatureTex& t : ftex)
             t.release();
@@ -735,8 +736,9 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         return fail(P2V_EINVAL, "sort_wait_polls must be >= 0");
     sb.wait_polls = (uint32_t) P.sort_wait_polls;
     sb.hold_tile = P.test_hold_sort ? 1 : -1;
+    P2V_CUDA_TRY(pp.bstart.ensure(4 * ((size_t) cell_block_count(g.nbins) + 1)));
     P2V_CUDA_TRY(launch_bin_sort(sb, n, g, counting ? pp.bcount.as<uint32_t>() : nullptr, cstart.as<uint32_t>(),
-                                 gaps.as<uint4>(), gap_cap, fs, sms, st));
+                                 pp.bstart.as<uint32_t>(), gaps.as<uint4>(), gap_cap, fs, sms, st));
     const uint32_t* skeys = sb.keys[sb.result];
     if (slot) {
         slot->deferred = false;

@@ -60,8 +60,10 @@ size_t bin_scan_words(uint32_t nbins);
 // gather records, and the cell start table (nbins + 1 entries). counts (nbins + 1 words) selects the
 // counting sort by cell, whose per-cell ordering handles cells of up to 32 particles; a fuller cell sends
 // the frame through the radix sort on the device. counts == nullptr: the radix sort alone.
+// bstart: cell_block_count(nbins) words of scratch (the radix path's start of every 64th cell)
 cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32_t* counts, uint32_t* start,
-    uint4* gaps, uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st);
+    uint32_t* bstart, uint4* gaps, uint32_t gap_cap, FrameScalars* fs, int sms, cudaStream_t st);
+uint32_t cell_block_count(uint32_t nbins);
 
 // Density gather configuration chosen on the host.
 enum GatherMode { GATHER_EXACT = 0, GATHER_KAHAN = 1 };
