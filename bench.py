@@ -63,6 +63,14 @@ def make_workload(name: str, rank: int = 0):
         desc = dict(workload="uniform_100k", particles=f.n, grid=list(f.res), radius=0.5,
                     kernel="gauss3 sigma=r (cut at 3 sigma)", cyclic=True)
         return f, desc
+    if name == "uniform_2M":
+        # the same structure at 2M particles (a profiling size for the sparse gather: ~1 GB on the device)
+        n = 2_000_000
+        scale = (n / 100_000) ** (1.0 / 3.0)
+        f = synth.uniform(n=n, edge=100.0 * scale, res=int(round(128 * scale)), seed=1 + rank)
+        desc = dict(workload="uniform_2M", particles=f.n, grid=list(f.res), radius=0.5,
+                    kernel="gauss3 sigma=r (cut at 3 sigma)", cyclic=True)
+        return f, desc
     if name == "uniform_16M":
         # the learned-AO inference set: 16M particles of the small case's structure, box scaled to keep the
         # number density and the voxel size
@@ -299,7 +307,7 @@ def train_learned_ao(ctx, f_main, dparams=None, workload: str = "mixed_phase_64M
         frames += [(synth.uniform(n=100_000, seed=10 + k), 100_000, bump) for k in range(10)]
     elif workload == "uniform_100k":
         frames = [(make_workload(workload, rank=100 + k)[0], 100_000, gauss) for k in range(12)]
-    elif workload == "uniform_16M":
+    elif workload in ("uniform_16M", "uniform_2M"):
         frames = [(synth.uniform(n=100_000, seed=10 + k), 100_000, gauss) for k in range(10)]
         frames += [(synth.lj_liquid(seed=s), 500_000, bump) for s in (3, 4)]
     else:
