@@ -80,6 +80,14 @@ def make_workload(name: str, rank: int = 0):
         desc = dict(workload="uniform_16M", particles=f.n, grid=list(f.res), radius=0.5,
                     kernel="gauss3 sigma=r (cut at 3 sigma)", cyclic=True)
         return f, desc
+    if name == "mixed_phase_16M":
+        # the default frame's structure and grid at a quarter of its particles (a profiling size for the radix
+        # binning: sort passes above the L2 size, ~3 GB on the device)
+        f = synth.mixed_phase(n=16_000_000, seed=5 + rank)
+        desc = dict(workload="mixed_phase_16M", particles=f.n, grid=list(f.res),
+                    phases="FCC slab (a=1.12, jitter 0.05) + uniform gas at 1/20 density",
+                    radii="0.5/0.8/1.2 in 6:3:1", kernel="bump sigma=1 (reference rbf)", cyclic=True)
+        return f, desc
     if name == "mixed_phase_64M":
         f = synth.mixed_phase(seed=5 + rank)
         desc = dict(workload="mixed_phase_64M", particles=f.n, grid=list(f.res),

@@ -434,18 +434,24 @@ __global__ void __launch_bounds__(256) sort_sanitize_kernel(uint32_t* __restrict
     }
 }
 
-// start[c] = first sorted position whose key is >= c, for c in [0, nbins], in two balanced steps with
-// coalesced stores. (1) The start of every CELL_BLOCK-th cell, bstart[b] = start[CELL_BLOCK b], from the
-// boundaries of the sorted keys: boundary i (between keys[i-1] and keys[i]) starts the cells
-// (keys[i-1], keys[i]], so the blocks whose first cell lies there; a run of 32 or more such blocks (a long
-// stretch of empty cells) is queued in chunks for cell_gap_fill_kernel. (2) Every cell c: the keys of its
-// block lie in [bstart[b], bstart[b+1]) (up to n for the last block), start[c] is the first of them >= c.
+// start[c] = first sorted position whose key is >= c, for c in [0, nbins]. Boundary i of the sorted keys
+// (between keys[i-1] and keys[i]) starts the cells (keys[i-1], keys[i]]. boundary_starts_kernel<G> writes
+// the start of every G-th cell there: out[b] = start[G b] for the b whose cell G b lies in that range; a run
+// of more than RUN (64 cells, 32 blocks) is queued in chunks of at most GAP_CHUNK for cell_gap_fill_kernel
+// (a sparse grid holds runs of millions of empty cells). Runs are disjoint and longer than RUN, so the
+// chunks number at most (nbins / G + 1) (1/GAP_CHUNK + 1/(RUN + 1)), below the nbins / 64 + 2 entries the
+// list holds. Dense frames (fewer than 8 cells per particle) take G = 1: the table directly. Sparse frames
+// take G = CELL_BLOCK, then cell_starts_kernel: every cell searches the keys of its block, which lie in
+// [out[b], out[b+1]) (up to n for the last block), and its thread stores start[c] (coalesced; per-boundary
+// threads would write gaps of tens of cells each, one scattered sector per store).
 constexpr uint32_t GAP_CHUNK = 8192;
 constexpr uint32_t CELL_BLOCK = 64;
 
-__global__ void __launch_bounds__(256) block_starts_kernel(const uint32_t* __restrict__ keys, uint32_t n,
-    uint32_t nbins, uint32_t* __restrict__ bstart, uint4* __restrict__ gaps, uint32_t gap_cap,
+template<uint32_t G>
+__global__ void __launch_bounds__(256) boundary_starts_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+    uint32_t nbins, uint32_t* __restrict__ out, uint4* __restrict__ gaps, uint32_t gap_cap,
     FrameScalars* __restrict__ fs, const FrameScalars* __restrict__ gate) {
+    constexpr uint32_t RUN = G == 1 ? 64u : 32u;
     if (radix_skipped(gate))
         return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
@@ -455,16 +461,13 @@ __global__ void __launch_bounds__(256) block_starts_kernel(const uint32_t* __res
             hi = nbins;
         if (lo > hi)
             continue;
-        const uint32_t b0 = (uint32_t) (((uint64_t) lo + CELL_BLOCK - 1) / CELL_BLOCK), b1 = hi / CELL_BLOCK;
+        const uint32_t b0 = (uint32_t) (((uint64_t) lo + G - 1) / G), b1 = hi / G;
         if (b0 > b1)
             continue;
-        if (b1 - b0 < 32u) {
+        if (b1 - b0 < RUN) {
             for (uint32_t bb = b0; bb <= b1; ++bb)
-                bstart[bb] = i;
+                out[bb] = i;
         } else {
-            // chunks of at most GAP_CHUNK blocks, one CTA each in cell_gap_fill_kernel. Runs are disjoint and
-            // longer than 32 blocks, so the chunks number at most nblk (1/GAP_CHUNK + 1/33), far below the
-            // nbins / 64 + 2 entries the list holds
             const uint32_t nch = (uint32_t) (((uint64_t) b1 - b0 + GAP_CHUNK) / GAP_CHUNK);
             const uint32_t slot = atomicAdd(&fs->ngaps, nch);
             for (uint32_t q = 0; q < nch; ++q) {
@@ -922,11 +925,18 @@ cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32
     const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n + 1, 256), sms * 8));
     if (n > 0)
         sort_sanitize_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], b.vals[b.result], n, g.nbins, b.err, gate);
-    const uint32_t nblk = cell_block_count(g.nbins);
-    block_starts_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, bstart, gaps, gap_cap, fs, gate);
-    cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, bstart, fs, gate);
-    cell_starts_kernel<<<(unsigned) (((uint64_t) g.nbins + 256) / 256), 256, 0, st>>>(b.keys[b.result], n, g.nbins,
-                                                                                      bstart, nblk, start, gate);
+    if ((uint64_t) g.nbins < 8ull * n) {
+        boundary_starts_kernel<1><<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, start, gaps, gap_cap, fs, gate);
+        cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs, gate);
+    } else {
+        const uint32_t nblk = cell_block_count(g.nbins);
+        boundary_starts_kernel<CELL_BLOCK><<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, bstart, gaps, gap_cap,
+                                                                 fs, gate);
+        cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, bstart, fs, gate);
+        cell_starts_kernel<<<(unsigned) (((uint64_t) g.nbins + 256) / 256), 256, 0, st>>>(b.keys[b.result], n,
+                                                                                          g.nbins, bstart, nblk, start,
+                                                                                          gate);
+    }
     count_valid_kernel<<<1, 1, 0, st>>>(start, g.nbins, fs);
     return cudaGetLastError();
 }
