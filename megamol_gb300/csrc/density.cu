@@ -651,13 +651,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                         const int bx = (int) s_part[6][ow];
                                         const int row = (int) s_part[8][ow] + (zl * TY + yl) * TX;
                                         const float pw = WEIGHTED ? __uint_as_float(s_part[9][ow]) : 0.0f;
-                                        // only the row's chord of the support: nodes with |xl + d0x| < w, w the
-                                        // half chord in cells, widened by 0.1 % + 1e-3 cells so that every node
-                                        // it drops fails the d2 < eps2 test below as well (the same sums)
-                                        const float w = __fmaf_rn(sqrtf(eps2 - dyz) * g.ihh[0], 1.001f, 1e-3f);
-                                        const int xa = max(0, (int) floorf(-d0x - w));
-                                        const int xb = min(bx - 1, (int) ceilf(w - d0x));
-                                        for (int xl = xa; xl <= xb; ++xl) {
+                                        for (int xl = 0; xl < bx; ++xl) {
                                             const float dx = g.hhi[0] * (static_cast<float>(xl) + d0x);
                                             const float d2 = __fmaf_rn(dx, dx, dyz);
                                             if (!(d2 < eps2))
