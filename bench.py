@@ -39,7 +39,12 @@ def parse():
     ap.add_argument("--workload", default="mixed_phase_64M")
     ap.add_argument("--model", default=None,
                     help="learned-AO network file: loaded when it exists (no training), else written after training")
-    return ap.parse_args()
+    ap.add_argument("--ao-brick-order", type=int, default=None, choices=[0, 1],
+                    help="the AO stages' particle order: 1 brick-major, 0 cell order (default: the library's)")
+    args = ap.parse_args()
+    if args.ao_brick_order is not None:
+        AO_PARAMS["ao_brick_order"] = args.ao_brick_order
+    return args
 
 
 def dist_info():

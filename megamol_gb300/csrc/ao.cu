@@ -247,7 +247,53 @@ __global__ void __launch_bounds__(256) pack_normals_kernel(const uint8_t* __rest
     nrm[offset + i] = make_float4(v[0], v[1], v[2], 0.0f);
 }
 
+// Brick-major key of a sorted particle from its cell key: bricks of 16 x 4 x 4 cells in (z, y, x) order,
+// the cells inside a brick in (z, y, x) order; the invalid bin nbins keeps the largest key.
+__global__ void __launch_bounds__(256) brick_keys_kernel(const uint32_t* __restrict__ cell_keys, uint32_t n,
+    uint32_t nb0, uint32_t nb1, uint32_t nbins, uint32_t* __restrict__ out) {
+    const uint32_t nbx = (nb0 + 15) / 16, nby = (nb1 + 3) / 4;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t c = cell_keys[j];
+        if (c >= nbins) {
+            out[j] = 0xFFFFFFFFu;
+            continue;
+        }
+        const uint32_t x = c % nb0, y = (c / nb0) % nb1, z = c / (nb0 * nb1);
+        out[j] = ((((z >> 2) * nby + (y >> 2)) * nbx + (x >> 4)) << 8) | ((z & 3u) << 6) | ((y & 3u) << 4) | (x & 15u);
+    }
+}
+
+__global__ void __launch_bounds__(256) permute_ao_inputs_kernel(const uint32_t* __restrict__ perm, uint32_t n,
+    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, const uint32_t* __restrict__ order,
+    float4* __restrict__ xyzr_b, float4* __restrict__ nrm_b, uint32_t* __restrict__ order_b) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t s = perm[j];
+        xyzr_b[j] = xyzr[s];
+        nrm_b[j] = nrm[s];
+        order_b[j] = order[s];
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_brick_keys(const uint32_t* cell_keys, uint32_t n, const GridGeo& g, uint32_t* out, int sms,
+                              cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
+    brick_keys_kernel<<<grd, 256, 0, st>>>(cell_keys, n, g.nb[0], g.nb[1], g.nbins, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_permute_ao_inputs(const uint32_t* perm, uint32_t n, const float4* xyzr, const float4* nrm,
+                                     const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b, int sms,
+                                     cudaStream_t st) {
+    if (n == 0)
+        return cudaSuccess;
+    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
+    permute_ao_inputs_kernel<<<grd, 256, 0, st>>>(perm, n, xyzr, nrm, order, xyzr_b, nrm_b, order_b);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale, int quantize, int nlevels,
     float* const* out, int (*dims)[3], int sms, cudaStream_t st) {

@@ -73,6 +73,7 @@ struct Pipe {
     DevBuf bcount;                         // particles per cell (the counting sort)
     DevBuf bstart;                         // start of every 64th cell (the radix path's cell starts)
     DevBuf xyzr_s, nrm_s;                  // positions and normals in sorted order (the cone AO stages)
+    DevBuf bk0, bk1, bv0, bv1, xyzr_b, nrm_b, ord_b;  // the AO stages' brick order (ao_brick_order)
     bool xyzr_sorted = false;              // the binning of this frame wrote xyzr_s
     FeatureTex ftex[MAX_LEVELS];           // the learned AO's feature levels as paired-slice textures
     cudaEvent_t ev[EV_COUNT] = {};
@@ -120,7 +121,8 @@ struct Pipe {
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &bstart, &xyzr_s, &nrm_s})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &bstart, &xyzr_s, &nrm_s, &bk0, &bk1, &bv0, &bv1, &xyzr_b,
+                          &nrm_b, &ord_b})
             b->release();
         for (FeatureTex& t : ftex)
             t.release();
@@ -1171,6 +1173,50 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         return launch_sort_particles(order, n, pp.xyzr_sorted ? nullptr : xyzr.as<float4>(), nrm.as<float4>(),
                                      pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), sms, st);
     };
+    // with ao_brick_order the cone-march stages take the sorted particles in brick-major order (bricks of
+    // 16 x 4 x 4 cells): neighbouring threads then sample neighbouring texels along all three axes
+    const float4* axyzr = nullptr;
+    const float4* anrm = nullptr;
+    const uint32_t* aorder = order;
+    auto ao_inputs = [&]() -> cudaError_t {
+        axyzr = pp.xyzr_s.as<float4>();
+        anrm = pp.nrm_s.as<float4>();
+        aorder = order;
+        if (!P.ao_brick_order || n == 0)
+            return cudaSuccess;
+        for (DevBuf* b : {&pp.bk0, &pp.bk1, &pp.bv0, &pp.bv1, &pp.ord_b}) {
+            const cudaError_t e = b->ensure(sizeof(uint32_t) * ((size_t) n + 1));
+            if (e != cudaSuccess)
+                return e;
+        }
+        cudaError_t e = pp.xyzr_b.ensure(sizeof(float4) * ((size_t) n + 1));
+        if (e == cudaSuccess)
+            e = pp.nrm_b.ensure(sizeof(float4) * ((size_t) n + 1));
+        if (e == cudaSuccess)
+            e = launch_keys_from_starts(pp.cstart.as<uint32_t>(), g.nbins, n, pp.bk1.as<uint32_t>(), sms, st);
+        if (e == cudaSuccess)
+            e = launch_brick_keys(pp.bk1.as<uint32_t>(), n, g, pp.bk0.as<uint32_t>(), sms, st);
+        if (e != cudaSuccess)
+            return e;
+        SortBuffers bsrt{};
+        bsrt.keys[0] = pp.bk0.as<uint32_t>();
+        bsrt.keys[1] = pp.bk1.as<uint32_t>();
+        bsrt.vals[0] = pp.bv0.as<uint32_t>();
+        bsrt.vals[1] = pp.bv1.as<uint32_t>();
+        bsrt.hist = pp.hist.as<uint32_t>();
+        bsrt.status = pp.status.as<uint32_t>();
+        bsrt.err = &scal.as<FrameScalars>()->error;
+        bsrt.implicit_vals0 = true;
+        e = launch_sort(bsrt, n, 0xFFFFFFFFu, sms, st);
+        if (e == cudaSuccess)
+            e = launch_permute_ao_inputs(bsrt.vals[bsrt.result], n, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(),
+                                         order, pp.xyzr_b.as<float4>(), pp.nrm_b.as<float4>(),
+                                         pp.ord_b.as<uint32_t>(), sms, st);
+        axyzr = pp.xyzr_b.as<float4>();
+        anrm = pp.nrm_b.as<float4>();
+        aorder = pp.ord_b.as<uint32_t>();
+        return e;
+    };
     if (P.ao_mode == P2V_AO_CONE) {
         ConeParams cp{};
         const p2v_status bs = build_cone(pp, fr, g, dgrid, bb, n, order, cp, st, slot);
@@ -1199,12 +1245,11 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
             return P2V_OK;
         }
         P2V_CUDA_TRY(to_sorted());
+        P2V_CUDA_TRY(ao_inputs());
         if (P.ao_march == P2V_AO_MARCH_WARP)
-            P2V_CUDA_TRY(launch_cone_ao_warp(cp, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, order, ao.as<float>(),
-                                             sms, st));
+            P2V_CUDA_TRY(launch_cone_ao_warp(cp, axyzr, anrm, n, aorder, ao.as<float>(), sms, st));
         else
-            P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n, nullptr, order,
-                                        ao.as<float>(), st));
+            P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, axyzr, anrm, n, nullptr, aorder, ao.as<float>(), st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_LEARNED) {
@@ -1226,12 +1271,13 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         a.lo = mlp_has_range ? mlp_lo.as<float>() : nullptr;
         a.hi = mlp_has_range ? mlp_hi.as<float>() : nullptr;
         P2V_CUDA_TRY(to_sorted());
+        P2V_CUDA_TRY(ao_inputs());
         a.n = n;
         a.order = nullptr;  // sorted copies: position j is sorted position j
-        a.xyzr = pp.xyzr_s.as<float4>();
-        a.nrm = pp.nrm_s.as<float4>();
+        a.xyzr = axyzr;
+        a.nrm = anrm;
         a.y = ao.as<float>();
-        a.out_order = order;
+        a.out_order = aorder;
         a.fallback = fb_list.as<uint32_t>();
         a.nfallback = &fs->ao_fallback;
         a.err = &fs->error;
@@ -1241,8 +1287,8 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         a.hold_mma = P.test_hold_mma ? 1 : 0;
         P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
         // the plain cone march for every particle whose features left the training range
-        P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), n,
-                                    &fs->ao_fallback, order, ao.as<float>(), st));
+        P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), axyzr, anrm, n, &fs->ao_fallback, aorder,
+                                    ao.as<float>(), st));
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_AOSPHERE_AXES || P.ao_mode == P2V_AO_AOSPHERE_NORMAL) {
@@ -1724,6 +1770,7 @@ void p2v_params_default(p2v_params* p) {
     p->sort_wait_polls = 0;
     p->test_hold_sort = 0;
     p->ao_march = P2V_AO_MARCH_THREAD;
+    p->ao_brick_order = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {

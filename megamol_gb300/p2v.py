@@ -63,6 +63,7 @@ class Params(C.Structure):
         ("slab_z0", C.c_int32), ("slab_z1", C.c_int32),
         ("batch_persistent", C.c_int32), ("queue_wait_polls", C.c_int32), ("test_hold_queue", C.c_int32),
         ("sort_wait_polls", C.c_int32), ("test_hold_sort", C.c_int32), ("ao_march", C.c_int32),
+        ("ao_brick_order", C.c_int32),
     ]
 
 

@@ -19,7 +19,7 @@ int main(void) {
     F(p2v_params, tile_z); F(p2v_params, batch_graph); F(p2v_params, vector_grid);
     F(p2v_params, aos_deposit); F(p2v_params, aos_clip_plane); F(p2v_params, ao_normals); F(p2v_params, test_hold_mma); F(p2v_params, slab_z1);
     F(p2v_params, batch_persistent); F(p2v_params, queue_wait_polls); F(p2v_params, test_hold_queue);
-    F(p2v_params, sort_wait_polls); F(p2v_params, test_hold_sort); F(p2v_params, ao_march);
+    F(p2v_params, sort_wait_polls); F(p2v_params, test_hold_sort); F(p2v_params, ao_march); F(p2v_params, ao_brick_order);
     F(p2v_batch_item, volume); F(p2v_batch_item, size);
     F(p2v_tune_report, ms_best); F(p2v_tune_report, cand_lanes); F(p2v_tune_report, cand_ms);
     F(p2v_tune_report, persistent); F(p2v_tune_report, cand_persistent);

@@ -39,7 +39,7 @@ def run_ao(ctx, f, normals, **params):
                 ao_volume=p2v.AOVOL_DENSITY, ao_volume_scale=1.0, ao_cones=3, ao_steps=0, ao_levels=0,
                 ao_apex_deg=50.0, ao_offset=0.01, ao_strength=1.0, ao_cone_length=0.8, ao_early_exit=1,
                 aos_deposit=p2v.AOS_DEPOSIT_CPU, aos_clip=0, aos_clip_plane=[0.0] * 4, ao_normals=p2v.NORMALS_LIST,
-                ao_march=p2v.AO_MARCH_THREAD)
+                ao_march=p2v.AO_MARCH_THREAD, ao_brick_order=0)
     base.update(params)
     ctx.set_params(**base)
     ao = np.full(f.n, np.nan, np.float32)
@@ -195,3 +195,18 @@ def test_warp_march_equals_thread_march(ctx, early_exit, steps):
     b, _, _ = run_ao(ctx, f, nrm, ao_march=p2v.AO_MARCH_WARP, **kw)
     assert np.array_equal(a, b)
     assert (b[::97] == 1.0).all()
+
+
+@pytest.mark.parametrize("march", [p2v.AO_MARCH_THREAD, p2v.AO_MARCH_WARP])
+def test_brick_order_gives_the_same_bits(ctx, march):
+    """ao_brick_order: the cone march takes the sorted particles in brick-major order (a radix sort of brick
+    keys, then a permutation of positions, normals and output indices); every particle's AO keeps its bits."""
+    f = synth.lj_liquid(cells=24, res=64, seed=38)
+    nrm = synth.random_normals(f.n, 39)
+    kw = dict(ao_cones=8, ao_steps=32, ao_levels=3, ao_mode=p2v.AO_CONE, ao_march=march)
+    a, _, _ = run_ao(ctx, f, nrm, ao_brick_order=0, **kw)
+    b, _, _ = run_ao(ctx, f, nrm, ao_brick_order=1, **kw)
+    assert np.array_equal(a, b)
+    c, _, _ = run_ao(ctx, f, nrm, ao_brick_order=1, ao_normals=p2v.NORMALS_GRADIENT, **kw)
+    d, _, _ = run_ao(ctx, f, nrm, ao_brick_order=0, ao_normals=p2v.NORMALS_GRADIENT, **kw)
+    assert np.array_equal(c, d)

@@ -236,3 +236,14 @@ def test_learned_ao_uniform_100k_gauss3():
         assert rmse <= 0.02, (rmse, rep, c.stats()["ao_fallback"])
     finally:
         c.close()
+
+
+def test_brick_order_gives_the_same_bits(ctx, trained):
+    """ao_brick_order: the learned AO (features, tensor-core inference, fallback march) takes the sorted particles
+    in brick-major order; every particle's AO keeps its bits."""
+    f = synth.lj_liquid(cells=24, res=64, seed=47)
+    nrm = with_normals(ctx, f)
+    a = ao_of(ctx, f, nrm, p2v.AO_LEARNED, ao_brick_order=0)
+    b = ao_of(ctx, f, nrm, p2v.AO_LEARNED, ao_brick_order=1)
+    ctx.set_params(ao_brick_order=0)
+    assert np.array_equal(a, b)
