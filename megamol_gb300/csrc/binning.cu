@@ -400,23 +400,47 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) onesweep_kernel(const uint32_
     }
     __syncthreads();
     const uint32_t tile_n = n - base < (uint32_t) SORT_TILE ? n - base : (uint32_t) SORT_TILE;
-    for (uint32_t j = tid; j < tile_n; j += SORT_THREADS) {
-        const uint32_t kk = s_keys[j];
-        const uint32_t dd = (kk >> shift) & DMASK;
-        const uint32_t dst = s_base[dd] + (j - s_local[dd]);
-        keys_out[dst] = kk;
-        const uint32_t vv = s_vals[j];
-        vals_out[dst] = vv;
-        if (GATHER) {
-            // last pass: emit the particle's gather record (and its xyzr) in sorted order
-            const float4 p = xyzr_in[vv];
-            float4 A;
-            int4 B;
-            make_record(p, geo, A, B);
-            rec_a[REC_STRIDE * (size_t) dst] = A;
-            rec_b[REC_STRIDE * (size_t) dst] = B;
-            if (xyzr_out)
-                xyzr_out[dst] = p;
+    if (!GATHER) {
+        for (uint32_t j = tid; j < tile_n; j += SORT_THREADS) {
+            const uint32_t kk = s_keys[j];
+            const uint32_t dd = (kk >> shift) & DMASK;
+            const uint32_t dst = s_base[dd] + (j - s_local[dd]);
+            keys_out[dst] = kk;
+            vals_out[dst] = s_vals[j];
+        }
+        return;
+    }
+    // last pass: emit every particle's gather record (and its xyzr) in sorted order. The xyzr reads are
+    // scattered (input order): each thread issues GATHER_BATCH of them before it uses the first, so that
+    // enough reads are in flight to cover their latency
+    constexpr int GATHER_BATCH = 4;
+    for (uint32_t j0 = tid; j0 < tile_n; j0 += GATHER_BATCH * SORT_THREADS) {
+        uint32_t dst[GATHER_BATCH], vv[GATHER_BATCH];
+        float4 p[GATHER_BATCH];
+#pragma unroll
+        for (int q = 0; q < GATHER_BATCH; ++q) {
+            const uint32_t j = j0 + q * SORT_THREADS;
+            if (j < tile_n) {
+                const uint32_t kk = s_keys[j];
+                const uint32_t dd = (kk >> shift) & DMASK;
+                dst[q] = s_base[dd] + (j - s_local[dd]);
+                vv[q] = s_vals[j];
+                keys_out[dst[q]] = kk;
+                vals_out[dst[q]] = vv[q];
+                p[q] = xyzr_in[vv[q]];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < GATHER_BATCH; ++q) {
+            if (j0 + q * SORT_THREADS < tile_n) {
+                float4 A;
+                int4 B;
+                make_record(p[q], geo, A, B);
+                rec_a[REC_STRIDE * (size_t) dst[q]] = A;
+                rec_b[REC_STRIDE * (size_t) dst[q]] = B;
+                if (xyzr_out)
+                    xyzr_out[dst[q]] = p[q];
+            }
         }
     }
 }
