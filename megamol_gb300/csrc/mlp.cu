@@ -50,14 +50,27 @@ __device__ __forceinline__ float sigmoidf_(float a) {
     return 1.0f / (1.0f + __expf(-a));
 }
 
-// GL LINEAR sample of one mip level at normalised point q through its 3D texture: one trilinear fetch
-// (CLAMP_TO_BORDER with border 0, texel centres at (i + 0.5) / N). The texels are 8-bit UNORM (the MDAO volume's
-// own R8 format) and the texture units weight with 8-bit fractions: the features feed a BF16 network and
-// training pairs are extracted by the same code (measured on the CPU: the same test RMSE as FP32 texels on the
-// LJ, uniform and mixed-phase frames). A 3D texture keeps the samples of a warp's neighbouring particles in the
-// same cached blocks along z as well.
-__device__ __forceinline__ float feature_tex_sample(unsigned long long tex, float qx, float qy, float qz) {
-    return tex3D<float>((cudaTextureObject_t) tex, qx, qy, qz);
+// GL LINEAR sample of one mip level (dz slices) at normalised point q (CLAMP_TO_BORDER with border 0, texel
+// centres at (i + 0.5) / N) through its paired-slice layered texture: layer z holds the texels of slices z
+// and z + 1 (0 past the last) as two 8-bit UNORM channels (the MDAO volume's own R8 format), so one bilinear
+// fetch returns both slices around the sample, x and y weighted by the texture units with 8-bit fractions;
+// the z weight is applied in FP32. The features feed a BF16 network and training pairs are extracted by the
+// same code (measured on the CPU: the same test RMSE as FP32 texels on the LJ, uniform and mixed-phase frames).
+__device__ __forceinline__ float feature_tex_sample(unsigned long long tex, float fdz, int dz, float qx, float qy,
+                                                    float qz) {
+    const float cz = fmaf(qz, fdz, -0.5f);
+    const float z0f = floorf(cz);
+    const float fz = cz - z0f;
+    const int z0 = (int) z0f;
+    if (z0 >= 0 && z0 < dz) {
+        const float2 p = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, z0);
+        return fmaf(fz, p.y - p.x, p.x);
+    }
+    if (z0 == -1) {  // between the border and slice 0
+        const float2 p = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, 0);
+        return fz * p.x;
+    }
+    return 0.0f;
 }
 
 // Feature sample j of a cone with direction dir from normalised point u: the march's step fstep[j] at its
@@ -69,9 +82,9 @@ __device__ __forceinline__ float feature_sample(const ConeParams& cp, const floa
     const float qx = fmaf(t, dir[0], u[0]), qy = fmaf(t, dir[1], u[1]), qz = fmaf(t, dir[2], u[2]);
     const int l0 = min((int) lod, cp.nlevels - 1);
     const float fr = lod - (float) l0;
-    float v = feature_tex_sample(cp.ftex[l0], qx, qy, qz);
+    float v = feature_tex_sample(cp.ftex[l0], cp.lv[l0].fd[2], cp.lv[l0].d[2], qx, qy, qz);
     if (fr > 0.0f && l0 + 1 < cp.nlevels)
-        v = fmaf(fr, feature_tex_sample(cp.ftex[l0 + 1], qx, qy, qz) - v, v);
+        v = fmaf(fr, feature_tex_sample(cp.ftex[l0 + 1], cp.lv[l0 + 1].fd[2], cp.lv[l0 + 1].d[2], qx, qy, qz) - v, v);
     return v;
 }
 
@@ -98,18 +111,24 @@ __device__ __forceinline__ bool particle_frame(const ConeParams& cp, const float
     return true;
 }
 
-// Level (dx, dy, dz) into its 3D texture as 8-bit UNORM of the texel clamped to [0, 1] (level-0 saturation
+// Level (dx, dy, dz) into its paired-slice layered texture: texel (x, y) of layer z = the 8-bit UNORM values
+// of slices z and z + 1 (0 past the last slice), each texel clamped to [0, 1] (level-0 saturation
 // clamp(v * sat, 0, 1) applied first when sat > 0).
+__device__ __forceinline__ unsigned char unorm8(float v, float sat) {
+    if (sat > 0.0f)
+        v = v * sat;
+    return (unsigned char) __float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f);
+}
+
 __global__ void __launch_bounds__(256) fill_feature_tex_kernel(const float* __restrict__ src, int dx, int dy, int dz,
                                                                float sat, unsigned long long surf) {
     const int64_t n = (int64_t) dx * dy * dz;
+    const int64_t plane = (int64_t) dx * dy;
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
-        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), z = (int) (i / ((int64_t) dx * dy));
-        float v = src[i];
-        if (sat > 0.0f)
-            v = v * sat;
-        const unsigned char q = (unsigned char) __float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f);
-        surf3Dwrite(q, (cudaSurfaceObject_t) surf, x * (int) sizeof(unsigned char), y, z);
+        const int x = (int) (i % dx), y = (int) ((i / dx) % dy), z = (int) (i / plane);
+        const unsigned char lo = unorm8(src[i], sat);
+        const unsigned char hi = z + 1 < dz ? unorm8(src[i + plane], sat) : (unsigned char) 0;
+        surf2DLayeredwrite(make_uchar2(lo, hi), (cudaSurfaceObject_t) surf, x * (int) sizeof(uchar2), y, z);
     }
 }
 
@@ -743,9 +762,9 @@ cudaError_t FeatureTex::ensure(const int dims[3]) {
     if (arr && d[0] == dims[0] && d[1] == dims[1] && d[2] == dims[2])
         return cudaSuccess;
     release();
-    cudaChannelFormatDesc fmt = cudaCreateChannelDesc<unsigned char>();
+    cudaChannelFormatDesc fmt = cudaCreateChannelDesc<uchar2>();
     cudaError_t e = cudaMalloc3DArray(&arr, &fmt, make_cudaExtent(dims[0], dims[1], dims[2]),
-                                      cudaArraySurfaceLoadStore);
+                                      cudaArrayLayered | cudaArraySurfaceLoadStore);
     if (e != cudaSuccess) {
         arr = nullptr;
         return e;
