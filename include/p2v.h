@@ -214,9 +214,10 @@ typedef struct p2v_params {
     int32_t test_hold_sort;   /* test hook: the second tile of the binning's first radix pass never publishes its
                                  digit counts, so the tiles after it wait until sort_wait_polls runs out (0) */
     int32_t ao_march;         /* p2v_ao_march: the kernel of the plain cone march (P2V_AO_MARCH_THREAD) */
-    int32_t ao_brick_order;   /* the cone march and the learned AO take the particles in brick-major order (bricks of
-                                 16 x 4 x 4 cells) instead of cell order: neighbouring threads sample neighbouring
-                                 texels along all three axes; the same AO bits (0) */
+    int32_t ao_brick_order;   /* 1: the cone march and the learned AO take the particles in brick-major order (bricks
+                                 of 16 x 4 x 4 cells) instead of cell order, so that neighbouring threads sample
+                                 neighbouring texels along all three axes; 0: cell order; -1: brick order for the
+                                 plain cone march only. The same AO bits either way (-1) */
 } p2v_params;
 
 /* AOSphere volume deposit rule: which voxel a particle's volume goes to. CPU (createVolumeCPU,

@@ -247,51 +247,174 @@ __global__ void __launch_bounds__(256) pack_normals_kernel(const uint8_t* __rest
     nrm[offset + i] = make_float4(v[0], v[1], v[2], 0.0f);
 }
 
-// Brick-major key of a sorted particle from its cell key: bricks of 16 x 4 x 4 cells in (z, y, x) order,
-// the cells inside a brick in (z, y, x) order; the invalid bin nbins keeps the largest key.
-__global__ void __launch_bounds__(256) brick_keys_kernel(const uint32_t* __restrict__ cell_keys, uint32_t n,
-    uint32_t nb0, uint32_t nb1, uint32_t nbins, uint32_t* __restrict__ out) {
-    const uint32_t nbx = (nb0 + 15) / 16, nby = (nb1 + 3) / 4;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t c = cell_keys[j];
-        if (c >= nbins) {
-            out[j] = 0xFFFFFFFFu;
-            continue;
-        }
-        const uint32_t x = c % nb0, y = (c / nb0) % nb1, z = c / (nb0 * nb1);
-        out[j] = ((((z >> 2) * nby + (y >> 2)) * nbx + (x >> 4)) << 8) | ((z & 3u) << 6) | ((y & 3u) << 4) | (x & 15u);
+// ---------------------------------------------------------------------------------------------
+// Brick-major order of the sorted particles (ao_brick_order): bricks of 16 x 4 x 4 cells in (z, y, x) order,
+// inside a brick the cells in (z, y, x) order. The cell-sorted particles of one brick row (its 16 cells of one
+// (z, y)) are contiguous, so the order is a stable reordering of row segments: segment s = brick * 16 +
+// lz * 4 + ly holds the cells x in [16 bx, 16 bx + 16) of row (z, y) = (4 bz + lz, 4 by + ly). Its particles
+// lie at [start[k0], start[k0 + 16]) of the cell order; the exclusive scan of the segments' counts gives their
+// place in brick order. Particles of the invalid bin (the tail of the cell order) keep their places.
+// ---------------------------------------------------------------------------------------------
+struct BrickGeo {
+    uint32_t nb0, nb1, nb2, nbx, nby;
+};
+
+__device__ __forceinline__ bool brick_segment(const BrickGeo& bg, uint32_t s, uint32_t& k0, uint32_t& len) {
+    const uint32_t brick = s >> 4, lz = (s >> 2) & 3u, ly = s & 3u;
+    const uint32_t bx = brick % bg.nbx, by = (brick / bg.nbx) % bg.nby, bz = brick / (bg.nbx * bg.nby);
+    const uint32_t z = 4 * bz + lz, y = 4 * by + ly, x0 = 16 * bx;
+    if (z >= bg.nb2 || y >= bg.nb1)
+        return false;
+    k0 = (z * bg.nb1 + y) * bg.nb0 + x0;
+    len = min(16u, bg.nb0 - x0);
+    return true;
+}
+
+constexpr int BSCAN_THREADS = 256, BSCAN_ITEMS = 16, BSCAN_TILE = BSCAN_THREADS * BSCAN_ITEMS;
+
+// segment counts, and the sum of every tile of BSCAN_TILE segments
+__global__ void __launch_bounds__(BSCAN_THREADS) brick_counts_kernel(const uint32_t* __restrict__ start, BrickGeo bg,
+    uint32_t nseg, uint32_t* __restrict__ cnt, uint32_t* __restrict__ tsum) {
+    __shared__ uint32_t s_sum[BSCAN_THREADS / 32];
+    uint32_t sum = 0;
+    for (int e = 0; e < BSCAN_ITEMS; ++e) {
+        const uint32_t s = blockIdx.x * BSCAN_TILE + e * BSCAN_THREADS + threadIdx.x;
+        if (s >= nseg)
+            break;
+        uint32_t k0, len, c = 0;
+        if (brick_segment(bg, s, k0, len))
+            c = start[k0 + len] - start[k0];
+        cnt[s] = c;
+        sum += c;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0)
+        s_sum[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < BSCAN_THREADS / 32; ++w)
+            sum += s_sum[w];
+        tsum[blockIdx.x] = sum;
     }
 }
 
-__global__ void __launch_bounds__(256) permute_ao_inputs_kernel(const uint32_t* __restrict__ perm, uint32_t n,
+// exclusive scan of the tile sums in place (one block)
+__global__ void __launch_bounds__(1024) brick_tile_scan_kernel(uint32_t* __restrict__ tsum, uint32_t ntiles) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0)
+        s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < ntiles; base += 1024) {
+        const uint32_t i = base + tid;
+        const uint32_t x = i < ntiles ? tsum[i] : 0u;
+        uint32_t incl = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        if (lane == 31)
+            s_warp[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t ws = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o)
+                    ws += t;
+            }
+            s_warp[lane] = ws;
+        }
+        __syncthreads();
+        const uint32_t carry = s_carry;
+        if (i < ntiles)
+            tsum[i] = carry + (w > 0 ? s_warp[w - 1] : 0u) + incl - x;
+        __syncthreads();
+        if (tid == 0)
+            s_carry = carry + s_warp[31];
+        __syncthreads();
+    }
+}
+
+// every segment's particles to their brick-order places (the tile's prefix + the scan inside the tile); the
+// invalid tail copied in place
+__global__ void __launch_bounds__(BSCAN_THREADS) brick_permute_kernel(const uint32_t* __restrict__ start, BrickGeo bg,
+    uint32_t nseg, uint32_t nbins, uint32_t n, const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ tsum,
     const float4* __restrict__ xyzr, const float4* __restrict__ nrm, const uint32_t* __restrict__ order,
     float4* __restrict__ xyzr_b, float4* __restrict__ nrm_b, uint32_t* __restrict__ order_b) {
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t s = perm[j];
-        xyzr_b[j] = xyzr[s];
-        nrm_b[j] = nrm[s];
-        order_b[j] = order[s];
+    __shared__ uint32_t s_warp[BSCAN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    // this thread's segments: BSCAN_ITEMS consecutive ones, so that the in-tile scan is a thread-local run
+    const uint32_t s0 = blockIdx.x * BSCAN_TILE + tid * BSCAN_ITEMS;
+    uint32_t c[BSCAN_ITEMS], sum = 0;
+#pragma unroll
+    for (int e = 0; e < BSCAN_ITEMS; ++e) {
+        c[e] = s0 + e < nseg ? cnt[s0 + e] : 0u;
+        sum += c[e];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+            incl += t;
+    }
+    if (lane == 31)
+        s_warp[w] = incl;
+    __syncthreads();
+    uint32_t dst = tsum[blockIdx.x] + incl - sum;
+    for (int k = 0; k < w; ++k)
+        dst += s_warp[k];
+    for (int e = 0; e < BSCAN_ITEMS; ++e) {
+        uint32_t k0, len;
+        if (c[e] != 0u && brick_segment(bg, s0 + e, k0, len)) {
+            const uint32_t src = start[k0];
+            for (uint32_t i = 0; i < c[e]; ++i) {
+                xyzr_b[dst + i] = xyzr[src + i];
+                nrm_b[dst + i] = nrm[src + i];
+                order_b[dst + i] = order[src + i];
+            }
+        }
+        dst += c[e];
+    }
+    for (uint32_t j = start[nbins] + blockIdx.x * blockDim.x + tid; j < n; j += gridDim.x * blockDim.x) {
+        xyzr_b[j] = xyzr[j];
+        nrm_b[j] = nrm[j];
+        order_b[j] = order[j];
     }
 }
 
 }  // namespace
 
-cudaError_t launch_brick_keys(const uint32_t* cell_keys, uint32_t n, const GridGeo& g, uint32_t* out, int sms,
-                              cudaStream_t st) {
-    if (n == 0)
-        return cudaSuccess;
-    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
-    brick_keys_kernel<<<grd, 256, 0, st>>>(cell_keys, n, g.nb[0], g.nb[1], g.nbins, out);
-    return cudaGetLastError();
+BrickPlan brick_plan(const GridGeo& g) {
+    BrickPlan p{};
+    p.nb[0] = g.nb[0];
+    p.nb[1] = g.nb[1];
+    p.nb[2] = g.nb[2];
+    const uint64_t nbx = (g.nb[0] + 15) / 16, nby = (g.nb[1] + 3) / 4, nbz = (g.nb[2] + 3) / 4;
+    p.nseg = nbx * nby * nbz * 16;
+    p.ntiles = (p.nseg + BSCAN_TILE - 1) / BSCAN_TILE;
+    return p;
 }
 
-cudaError_t launch_permute_ao_inputs(const uint32_t* perm, uint32_t n, const float4* xyzr, const float4* nrm,
-                                     const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b, int sms,
-                                     cudaStream_t st) {
+cudaError_t launch_brick_order(const BrickPlan& p, const uint32_t* start, uint32_t nbins, uint32_t n,
+                               uint32_t* cnt, uint32_t* tsum, const float4* xyzr, const float4* nrm,
+                               const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b,
+                               cudaStream_t st) {
     if (n == 0)
         return cudaSuccess;
-    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
-    permute_ao_inputs_kernel<<<grd, 256, 0, st>>>(perm, n, xyzr, nrm, order, xyzr_b, nrm_b, order_b);
+    BrickGeo bg{p.nb[0], p.nb[1], p.nb[2], (p.nb[0] + 15) / 16, (p.nb[1] + 3) / 4};
+    const uint32_t nseg = (uint32_t) p.nseg, ntiles = (uint32_t) p.ntiles;
+    brick_counts_kernel<<<ntiles, BSCAN_THREADS, 0, st>>>(start, bg, nseg, cnt, tsum);
+    brick_tile_scan_kernel<<<1, 1024, 0, st>>>(tsum, ntiles);
+    brick_permute_kernel<<<ntiles, BSCAN_THREADS, 0, st>>>(start, bg, nseg, nbins, n, cnt, tsum, xyzr, nrm, order,
+                                                           xyzr_b, nrm_b, order_b);
     return cudaGetLastError();
 }
 

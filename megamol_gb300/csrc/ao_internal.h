@@ -122,13 +122,18 @@ cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32
 // unit normals down the density gradient of `grid` (geometry geo) at xyzr[j], into nrm[j] (P2V_NORMALS_GRADIENT)
 cudaError_t launch_gradient_normals(const GridGeo& geo, const float* grid, const float4* xyzr, uint32_t n, float4* nrm,
     cudaStream_t st);
-// brick-major keys (bricks of 16 x 4 x 4 cells) of sorted particles from their cell keys; invalid last
-cudaError_t launch_brick_keys(const uint32_t* cell_keys, uint32_t n, const GridGeo& g, uint32_t* out, int sms,
-                              cudaStream_t st);
-// xyzr_b[j] = xyzr[perm[j]], nrm_b[j] = nrm[perm[j]], order_b[j] = order[perm[j]]
-cudaError_t launch_permute_ao_inputs(const uint32_t* perm, uint32_t n, const float4* xyzr, const float4* nrm,
-                                     const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b, int sms,
-                                     cudaStream_t st);
+// Brick-major order of the cell-sorted particles (bricks of 16 x 4 x 4 cells): cnt needs nseg words, tsum
+// ntiles; xyzr_b[j] = xyzr[src], nrm_b[j] = nrm[src], order_b[j] = order[src] for the particle src of brick
+// order position j. start: the cell start table (nbins + 1 entries).
+struct BrickPlan {
+    uint32_t nb[3];
+    uint64_t nseg, ntiles;
+};
+BrickPlan brick_plan(const GridGeo& g);
+cudaError_t launch_brick_order(const BrickPlan& p, const uint32_t* start, uint32_t nbins, uint32_t n,
+                               uint32_t* cnt, uint32_t* tsum, const float4* xyzr, const float4* nrm,
+                               const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b,
+                               cudaStream_t st);
 cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,
     cudaStream_t st);
 

@@ -73,7 +73,7 @@ struct Pipe {
     DevBuf bcount;                         // particles per cell (the counting sort)
     DevBuf bstart;                         // start of every 64th cell (the radix path's cell starts)
     DevBuf xyzr_s, nrm_s;                  // positions and normals in sorted order (the cone AO stages)
-    DevBuf bk0, bk1, bv0, bv1, xyzr_b, nrm_b, ord_b;  // the AO stages' brick order (ao_brick_order)
+    DevBuf bk0, bk1, xyzr_b, nrm_b, ord_b;  // the AO stages' brick order (ao_brick_order)
     bool xyzr_sorted = false;              // the binning of this frame wrote xyzr_s
     FeatureTex ftex[MAX_LEVELS];           // the learned AO's feature levels as paired-slice textures
     cudaEvent_t ev[EV_COUNT] = {};
@@ -121,8 +121,8 @@ struct Pipe {
             cudaStreamSynchronize(stream);
         for (DevBuf* b : {&raw, &xyzr, &rec_a, &keys0, &keys1, &vals0, &vals1, &status, &hist, &cstart, &gaps,
                           &grid, &tiles, &scal, &nrm, &ao, &mips, &aos_acc, &aos_tex, &mdao_acc, &mdao_vol, &fb_list,
-                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &bstart, &xyzr_s, &nrm_s, &bk0, &bk1, &bv0, &bv1, &xyzr_b,
-                          &nrm_b, &ord_b})
+                          &wts, &wsorted, &wsum, &vdens, &vdirs, &vkeys0, &vkeys1, &vvals0, &vvals1, &vout, &bcount, &bstart, &xyzr_s, &nrm_s, &bk0, &bk1, &xyzr_b, &nrm_b,
+                          &ord_b})
             b->release();
         for (FeatureTex& t : ftex)
             t.release();
@@ -1173,8 +1173,9 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         return launch_sort_particles(order, n, pp.xyzr_sorted ? nullptr : xyzr.as<float4>(), nrm.as<float4>(),
                                      pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), sms, st);
     };
-    // with ao_brick_order the cone-march stages take the sorted particles in brick-major order (bricks of
-    // 16 x 4 x 4 cells): neighbouring threads then sample neighbouring texels along all three axes
+    // the cone-march stages can take the sorted particles in brick-major order (bricks of 16 x 4 x 4 cells):
+    // neighbouring threads then sample neighbouring texels along all three axes. ao_brick_order -1: for the
+    // plain march (measured faster), not for the learned AO (its texture fetches gained nothing)
     const float4* axyzr = nullptr;
     const float4* anrm = nullptr;
     const uint32_t* aorder = order;
@@ -1182,36 +1183,25 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         axyzr = pp.xyzr_s.as<float4>();
         anrm = pp.nrm_s.as<float4>();
         aorder = order;
-        if (!P.ao_brick_order || n == 0)
+        const bool bricks = P.ao_brick_order > 0 || (P.ao_brick_order < 0 && P.ao_mode == P2V_AO_CONE);
+        if (!bricks || n == 0)
             return cudaSuccess;
-        for (DevBuf* b : {&pp.bk0, &pp.bk1, &pp.bv0, &pp.bv1, &pp.ord_b}) {
-            const cudaError_t e = b->ensure(sizeof(uint32_t) * ((size_t) n + 1));
-            if (e != cudaSuccess)
-                return e;
-        }
-        cudaError_t e = pp.xyzr_b.ensure(sizeof(float4) * ((size_t) n + 1));
+        const BrickPlan bp = brick_plan(g);
+        if (bp.nseg >= (1ull << 32))
+            return cudaErrorInvalidValue;
+        cudaError_t e = pp.bk0.ensure(sizeof(uint32_t) * (bp.nseg + 1));
+        if (e == cudaSuccess)
+            e = pp.bk1.ensure(sizeof(uint32_t) * (bp.ntiles + 1));
+        if (e == cudaSuccess)
+            e = pp.ord_b.ensure(sizeof(uint32_t) * ((size_t) n + 1));
+        if (e == cudaSuccess)
+            e = pp.xyzr_b.ensure(sizeof(float4) * ((size_t) n + 1));
         if (e == cudaSuccess)
             e = pp.nrm_b.ensure(sizeof(float4) * ((size_t) n + 1));
         if (e == cudaSuccess)
-            e = launch_keys_from_starts(pp.cstart.as<uint32_t>(), g.nbins, n, pp.bk1.as<uint32_t>(), sms, st);
-        if (e == cudaSuccess)
-            e = launch_brick_keys(pp.bk1.as<uint32_t>(), n, g, pp.bk0.as<uint32_t>(), sms, st);
-        if (e != cudaSuccess)
-            return e;
-        SortBuffers bsrt{};
-        bsrt.keys[0] = pp.bk0.as<uint32_t>();
-        bsrt.keys[1] = pp.bk1.as<uint32_t>();
-        bsrt.vals[0] = pp.bv0.as<uint32_t>();
-        bsrt.vals[1] = pp.bv1.as<uint32_t>();
-        bsrt.hist = pp.hist.as<uint32_t>();
-        bsrt.status = pp.status.as<uint32_t>();
-        bsrt.err = &scal.as<FrameScalars>()->error;
-        bsrt.implicit_vals0 = true;
-        e = launch_sort(bsrt, n, 0xFFFFFFFFu, sms, st);
-        if (e == cudaSuccess)
-            e = launch_permute_ao_inputs(bsrt.vals[bsrt.result], n, pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(),
-                                         order, pp.xyzr_b.as<float4>(), pp.nrm_b.as<float4>(),
-                                         pp.ord_b.as<uint32_t>(), sms, st);
+            e = launch_brick_order(bp, pp.cstart.as<uint32_t>(), g.nbins, n, pp.bk0.as<uint32_t>(),
+                                   pp.bk1.as<uint32_t>(), pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), order,
+                                   pp.xyzr_b.as<float4>(), pp.nrm_b.as<float4>(), pp.ord_b.as<uint32_t>(), st);
         axyzr = pp.xyzr_b.as<float4>();
         anrm = pp.nrm_b.as<float4>();
         aorder = pp.ord_b.as<uint32_t>();
@@ -1770,7 +1760,7 @@ void p2v_params_default(p2v_params* p) {
     p->sort_wait_polls = 0;
     p->test_hold_sort = 0;
     p->ao_march = P2V_AO_MARCH_THREAD;
-    p->ao_brick_order = 0;
+    p->ao_brick_order = -1;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {

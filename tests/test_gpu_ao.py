@@ -199,8 +199,9 @@ def test_warp_march_equals_thread_march(ctx, early_exit, steps):
 
 @pytest.mark.parametrize("march", [p2v.AO_MARCH_THREAD, p2v.AO_MARCH_WARP])
 def test_brick_order_gives_the_same_bits(ctx, march):
-    """ao_brick_order: the cone march takes the sorted particles in brick-major order (a radix sort of brick
-    keys, then a permutation of positions, normals and output indices); every particle's AO keeps its bits."""
+    """ao_brick_order: the cone march takes the sorted particles in brick-major order (bricks of 16 x 4 x 4
+    cells: a stable reordering of the cell order's row segments); every particle's AO keeps its bits. The
+    frame's 66^3 cells leave partial bricks along every axis."""
     f = synth.lj_liquid(cells=24, res=64, seed=38)
     nrm = synth.random_normals(f.n, 39)
     kw = dict(ao_cones=8, ao_steps=32, ao_levels=3, ao_mode=p2v.AO_CONE, ao_march=march)
