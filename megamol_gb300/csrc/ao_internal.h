@@ -31,7 +31,7 @@ struct ConeParams {
     float4 dirs[MAX_CONES];        // xyz around +Y, w = cone width
     float t[MAX_STEPS], lod[MAX_STEPS];
     ConeLevel lv[MAX_LEVELS];
-    // learned AO: the march steps its features sample (per cone), and 8-bit 3D textures of the mip levels
+    // learned AO: the march steps its features sample (per cone), and 8-bit paired-slice textures of the mip levels
     // those samples read (0 = level not needed)
     int nfsteps;
     int fstep[MAX_FSTEPS];

@@ -1140,6 +1140,13 @@ p2v_status p2v_ctx::prepare_features(Pipe& pp, ConeParams& cp, cudaStream_t st) 
         if (l >= cp.nlevels || !need[l])
             continue;
         const ConeLevel& L = cp.lv[l];
+        // the feature textures are layered (one layer per z slice): the device's layer limit bounds sizez
+        int max_layers = 0, max_w = 0;
+        P2V_CUDA_TRY(cudaDeviceGetAttribute(&max_layers, cudaDevAttrMaxTexture2DLayeredLayers, device));
+        P2V_CUDA_TRY(cudaDeviceGetAttribute(&max_w, cudaDevAttrMaxTexture2DLayeredWidth, device));
+        if (L.d[2] > max_layers || L.d[0] > max_w || L.d[1] > max_w)
+            return fail(P2V_EUNSUPPORTED, "learned AO: mip level %d is %dx%dx%d; its feature texture allows at most %d "
+                        "slices of %d x %d texels", l, L.d[0], L.d[1], L.d[2], max_layers, max_w, max_w);
         P2V_CUDA_TRY(pp.ftex[l].ensure(L.d));
         P2V_CUDA_TRY(launch_fill_feature_tex(L, l == 0 ? cp.sat : 0.0f, pp.ftex[l], st));
         cp.ftex[l] = pp.ftex[l].tex;

@@ -54,8 +54,10 @@ struct MlpInferArgs {
     int hold_mma;                   // test hook: layer 1 is not issued, so its completion wait runs out
 };
 
-// One mip level of the AO volume as an 8-bit UNORM 3D texture (GL LINEAR, CLAMP_TO_BORDER, normalised
-// coordinates), written through a surface; the learned AO's features sample it with the texture units.
+// One mip level of the AO volume as a paired-slice layered texture: layer z holds slices z and z + 1 as two
+// 8-bit UNORM channels (GL LINEAR in x and y, CLAMP_TO_BORDER, normalised coordinates), written through a
+// surface; the learned AO's features sample it with the texture units (one bilinear fetch per sample, the z
+// weight applied in FP32).
 struct FeatureTex {
     cudaArray_t arr = nullptr;
     unsigned long long tex = 0;   // cudaTextureObject_t
