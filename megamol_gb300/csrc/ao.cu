@@ -16,6 +16,7 @@
 #include "ao_internal.h"
 #include "cone_march.cuh"
 #include "p2v_common.cuh"
+#include "particle_record.cuh"
 
 namespace p2v {
 
@@ -342,12 +343,9 @@ __global__ void __launch_bounds__(1024) brick_tile_scan_kernel(uint32_t* __restr
     }
 }
 
-// every segment's particles to their brick-order places (the tile's prefix + the scan inside the tile); the
-// invalid tail copied in place
-__global__ void __launch_bounds__(BSCAN_THREADS) brick_permute_kernel(const uint32_t* __restrict__ start, BrickGeo bg,
-    uint32_t nseg, uint32_t nbins, uint32_t n, const uint32_t* __restrict__ cnt, const uint32_t* __restrict__ tsum,
-    const float4* __restrict__ xyzr, const float4* __restrict__ nrm, const uint32_t* __restrict__ order,
-    float4* __restrict__ xyzr_b, float4* __restrict__ nrm_b, uint32_t* __restrict__ order_b) {
+// the segments' brick-order offsets in place of their counts: the tile's prefix + the scan inside the tile
+__global__ void __launch_bounds__(BSCAN_THREADS) brick_offsets_kernel(uint32_t nseg, uint32_t* __restrict__ cnt,
+                                                                      const uint32_t* __restrict__ tsum) {
     __shared__ uint32_t s_warp[BSCAN_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     // this thread's segments: BSCAN_ITEMS consecutive ones, so that the in-tile scan is a thread-local run
@@ -368,25 +366,40 @@ __global__ void __launch_bounds__(BSCAN_THREADS) brick_permute_kernel(const uint
     if (lane == 31)
         s_warp[w] = incl;
     __syncthreads();
-    uint32_t dst = tsum[blockIdx.x] + incl - sum;
+    uint32_t run = tsum[blockIdx.x] + incl - sum;
     for (int k = 0; k < w; ++k)
-        dst += s_warp[k];
+        run += s_warp[k];
+#pragma unroll
     for (int e = 0; e < BSCAN_ITEMS; ++e) {
-        uint32_t k0, len;
-        if (c[e] != 0u && brick_segment(bg, s0 + e, k0, len)) {
-            const uint32_t src = start[k0];
-            for (uint32_t i = 0; i < c[e]; ++i) {
-                xyzr_b[dst + i] = xyzr[src + i];
-                nrm_b[dst + i] = nrm[src + i];
-                order_b[dst + i] = order[src + i];
-            }
-        }
-        dst += c[e];
+        if (s0 + e < nseg)
+            cnt[s0 + e] = run;
+        run += c[e];
     }
-    for (uint32_t j = start[nbins] + blockIdx.x * blockDim.x + tid; j < n; j += gridDim.x * blockDim.x) {
-        xyzr_b[j] = xyzr[j];
-        nrm_b[j] = nrm[j];
-        order_b[j] = order[j];
+}
+
+// One thread per sorted particle (balanced however crowded a cell is): its segment from its record's floor
+// cell (the bin key's own cell: clamped to the border cells), its place = the segment's offset + its rank
+// in the segment's cell-order run. Particles of the invalid bin (the tail of the cell order) keep theirs.
+__global__ void __launch_bounds__(256) brick_scatter_kernel(const uint32_t* __restrict__ start,
+    const int4* __restrict__ rec_b, BrickGeo bg, uint32_t nbins, uint32_t n, const uint32_t* __restrict__ off,
+    int3 s3, const float4* __restrict__ xyzr, const float4* __restrict__ nrm, const uint32_t* __restrict__ order,
+    float4* __restrict__ xyzr_b, float4* __restrict__ nrm_b, uint32_t* __restrict__ order_b) {
+    const uint32_t nvalid = start[nbins];
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        uint32_t d = j;
+        if (j < nvalid) {
+            const int4 B = rec_b[(size_t) REC_STRIDE * j];
+            const uint32_t x = (uint32_t) (min(max(B.x, -1), s3.x) + 1);
+            const uint32_t y = (uint32_t) (min(max(B.y, -1), s3.y) + 1);
+            const uint32_t z = (uint32_t) (min(max(B.z, -1), s3.z) + 1);
+            const uint32_t seg = ((((z >> 2) * bg.nby + (y >> 2)) * bg.nbx + (x >> 4)) << 4) | ((z & 3u) << 2) | (y & 3u);
+            const uint32_t k0 = (z * bg.nb1 + y) * bg.nb0 + (x & ~15u);
+            d = off[seg] + (j - start[k0]);
+        }
+        xyzr_b[d] = xyzr[j];
+        if (nrm)
+            nrm_b[d] = nrm[j];
+        order_b[d] = order[j];
     }
 }
 
@@ -403,9 +416,9 @@ BrickPlan brick_plan(const GridGeo& g) {
     return p;
 }
 
-cudaError_t launch_brick_order(const BrickPlan& p, const uint32_t* start, uint32_t nbins, uint32_t n,
-                               uint32_t* cnt, uint32_t* tsum, const float4* xyzr, const float4* nrm,
-                               const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b,
+cudaError_t launch_brick_order(const BrickPlan& p, const GridGeo& g, const uint32_t* start, const int4* rec_b,
+                               uint32_t n, uint32_t* cnt, uint32_t* tsum, const float4* xyzr, const float4* nrm,
+                               const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b, int sms,
                                cudaStream_t st) {
     if (n == 0)
         return cudaSuccess;
@@ -413,8 +426,10 @@ cudaError_t launch_brick_order(const BrickPlan& p, const uint32_t* start, uint32
     const uint32_t nseg = (uint32_t) p.nseg, ntiles = (uint32_t) p.ntiles;
     brick_counts_kernel<<<ntiles, BSCAN_THREADS, 0, st>>>(start, bg, nseg, cnt, tsum);
     brick_tile_scan_kernel<<<1, 1024, 0, st>>>(tsum, ntiles);
-    brick_permute_kernel<<<ntiles, BSCAN_THREADS, 0, st>>>(start, bg, nseg, nbins, n, cnt, tsum, xyzr, nrm, order,
-                                                           xyzr_b, nrm_b, order_b);
+    brick_offsets_kernel<<<ntiles, BSCAN_THREADS, 0, st>>>(nseg, cnt, tsum);
+    const unsigned grd = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n, 256), (uint32_t) sms * 16));
+    brick_scatter_kernel<<<grd, 256, 0, st>>>(start, rec_b, bg, g.nbins, n, cnt, make_int3(g.s[0], g.s[1], g.s[2]),
+                                              xyzr, nrm, order, xyzr_b, nrm_b, order_b);
     return cudaGetLastError();
 }
 

@@ -123,16 +123,17 @@ cudaError_t launch_aosphere(const AOSphereParams& ap, const float4* xyzr, uint32
 cudaError_t launch_gradient_normals(const GridGeo& geo, const float* grid, const float4* xyzr, uint32_t n, float4* nrm,
     cudaStream_t st);
 // Brick-major order of the cell-sorted particles (bricks of 16 x 4 x 4 cells): cnt needs nseg words, tsum
-// ntiles; xyzr_b[j] = xyzr[src], nrm_b[j] = nrm[src], order_b[j] = order[src] for the particle src of brick
-// order position j. start: the cell start table (nbins + 1 entries).
+// ntiles; xyzr_b[j] = xyzr[src], nrm_b[j] = nrm[src] (nrm nullable), order_b[j] = order[src] for the particle
+// src of brick order position j. start: the cell start table (nbins + 1 entries); rec_b: the sorted particles'
+// gather records (their floor cells).
 struct BrickPlan {
     uint32_t nb[3];
     uint64_t nseg, ntiles;
 };
 BrickPlan brick_plan(const GridGeo& g);
-cudaError_t launch_brick_order(const BrickPlan& p, const uint32_t* start, uint32_t nbins, uint32_t n,
-                               uint32_t* cnt, uint32_t* tsum, const float4* xyzr, const float4* nrm,
-                               const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b,
+cudaError_t launch_brick_order(const BrickPlan& p, const GridGeo& g, const uint32_t* start, const int4* rec_b,
+                               uint32_t n, uint32_t* cnt, uint32_t* tsum, const float4* xyzr, const float4* nrm,
+                               const uint32_t* order, float4* xyzr_b, float4* nrm_b, uint32_t* order_b, int sms,
                                cudaStream_t st);
 cudaError_t launch_pack_normals(const void* src, uint32_t stride, uint64_t count, uint64_t offset, float4* nrm,
     cudaStream_t st);

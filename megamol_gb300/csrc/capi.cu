@@ -153,10 +153,11 @@ struct Pipe {
 // (the lane's own buffers serve its next frame meanwhile), and the frame's descriptor for that launch.
 struct BatchSlot {
     DevBuf xyzr_s, order, nrm_s, ao, grid, mips;
+    DevBuf xyzr_b, ord_b, nrm_b;   // the march's brick order (ao_brick_order)
     BatchAoFrame* desc = nullptr;  // this frame's entry of the pinned descriptor table
     bool deferred = false;         // the frame's AO stage was left to the batch launch
     void release() {
-        for (DevBuf* b : {&xyzr_s, &order, &nrm_s, &ao, &grid, &mips})
+        for (DevBuf* b : {&xyzr_s, &order, &nrm_s, &ao, &grid, &mips, &xyzr_b, &ord_b, &nrm_b})
             b->release();
     }
 };
@@ -1206,9 +1207,10 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         if (e == cudaSuccess)
             e = pp.nrm_b.ensure(sizeof(float4) * ((size_t) n + 1));
         if (e == cudaSuccess)
-            e = launch_brick_order(bp, pp.cstart.as<uint32_t>(), g.nbins, n, pp.bk0.as<uint32_t>(),
-                                   pp.bk1.as<uint32_t>(), pp.xyzr_s.as<float4>(), pp.nrm_s.as<float4>(), order,
-                                   pp.xyzr_b.as<float4>(), pp.nrm_b.as<float4>(), pp.ord_b.as<uint32_t>(), st);
+            e = launch_brick_order(bp, g, pp.cstart.as<uint32_t>(), reinterpret_cast<const int4*>(pp.rec_a.as<float4>() + 1),
+                                   n, pp.bk0.as<uint32_t>(), pp.bk1.as<uint32_t>(), pp.xyzr_s.as<float4>(),
+                                   pp.nrm_s.as<float4>(), order, pp.xyzr_b.as<float4>(), pp.nrm_b.as<float4>(),
+                                   pp.ord_b.as<uint32_t>(), sms, st);
         axyzr = pp.xyzr_b.as<float4>();
         anrm = pp.nrm_b.as<float4>();
         aorder = pp.ord_b.as<uint32_t>();
@@ -1238,6 +1240,24 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
             d.order = slot->order.as<uint32_t>();
             d.ao = slot->ao.as<float>();
             d.n = n;
+            if (P.ao_brick_order != 0 && n > 0) {  // the march in brick order (the same bits)
+                const BrickPlan bp = brick_plan(g);
+                P2V_CUDA_TRY(pp.bk0.ensure(sizeof(uint32_t) * (bp.nseg + 1)));
+                P2V_CUDA_TRY(pp.bk1.ensure(sizeof(uint32_t) * (bp.ntiles + 1)));
+                P2V_CUDA_TRY(slot->xyzr_b.ensure(sizeof(float4) * ((size_t) n + 1)));
+                P2V_CUDA_TRY(slot->ord_b.ensure(sizeof(uint32_t) * ((size_t) n + 1)));
+                if (list)
+                    P2V_CUDA_TRY(slot->nrm_b.ensure(sizeof(float4) * ((size_t) n + 1)));
+                P2V_CUDA_TRY(launch_brick_order(bp, g, pp.cstart.as<uint32_t>(),
+                                                reinterpret_cast<const int4*>(pp.rec_a.as<float4>() + 1), n,
+                                                pp.bk0.as<uint32_t>(), pp.bk1.as<uint32_t>(), slot->xyzr_s.as<float4>(),
+                                                d.nrm, slot->order.as<uint32_t>(), slot->xyzr_b.as<float4>(),
+                                                list ? slot->nrm_b.as<float4>() : nullptr, slot->ord_b.as<uint32_t>(),
+                                                sms, st));
+                d.xyzr = slot->xyzr_b.as<float4>();
+                d.nrm = list ? slot->nrm_b.as<float4>() : nullptr;
+                d.order = slot->ord_b.as<uint32_t>();
+            }
             slot->deferred = true;
             return P2V_OK;
         }
