@@ -476,21 +476,23 @@ def run_ours(args):
     # both pipelines below use the winner ----
     ctx.set_params(ao_mode=p2v.AO_NONE, tile_x=0, tile_y=0, tile_z=0)
     tune = ctx.autotune_batch([dict(lists=dev_lists, bbox=f.bbox, out=d_out, size=f.res)])
-    # ---- plain cone-march pipeline: both march kernels (the same bits), the faster is the baseline ----
-    ctx.set_params(ao_mode=p2v.AO_CONE, ao_march=p2v.AO_MARCH_WARP)
-    ms_plain_w, st_plain_w = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch,
-                                           barrier, tag="plain_warp")
-    ms_plain_w = max_over_ranks(ms_plain_w)
-    ao_plain_w = d_ao.cpu().numpy().copy()
-    ctx.set_params(ao_march=p2v.AO_MARCH_THREAD)
-    ms_plain_t, st_plain_t = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch,
-                                           barrier, tag="plain")
-    ms_plain_t = max_over_ranks(ms_plain_t)
-    ao_plain = d_ao.cpu().numpy().copy()
-    if not np.array_equal(ao_plain, ao_plain_w):
-        raise SystemExit("the two plain march kernels disagree")
-    plain_kernel = "thread" if ms_plain_t <= ms_plain_w else "warp"
-    ms_plain, st_plain = (ms_plain_t, st_plain_t) if plain_kernel == "thread" else (ms_plain_w, st_plain_w)
+    # ---- plain cone-march pipeline: both march kernels and both particle orders (the same bits); the fastest
+    # is the baseline ----
+    plain_runs = {}
+    for kern, order, tag in (("warp", 0, "plain_warp"), ("thread", 1, "plain_brick"), ("thread", 0, "plain")):
+        ctx.set_params(ao_mode=p2v.AO_CONE, ao_march=p2v.AO_MARCH_WARP if kern == "warp" else p2v.AO_MARCH_THREAD,
+                       ao_brick_order=order)
+        ms_k, st_k = time_pipeline(ctx, dev_lists, f.bbox, d_out, args.steps, args.warmup, stream, torch, barrier,
+                                   tag=tag)
+        plain_runs[tag] = (max_over_ranks(ms_k), st_k, d_ao.cpu().numpy().copy())
+    ctx.set_params(ao_march=p2v.AO_MARCH_THREAD, ao_brick_order=AO_PARAMS.get("ao_brick_order", 0))
+    ao_plain = plain_runs["plain"][2]
+    if not all(np.array_equal(ao_plain, r[2]) for r in plain_runs.values()):
+        raise SystemExit("the plain march variants disagree")
+    plain_best = min(plain_runs, key=lambda k: plain_runs[k][0])
+    ms_plain, st_plain = plain_runs[plain_best][0], plain_runs[plain_best][1]
+    plain_kernel = {"plain": "thread per particle, cell order", "plain_brick": "thread per particle, brick order",
+                    "plain_warp": "warp per cone, cell order"}[plain_best]
     # ---- learned-AO pipeline (MLP, cone-march fallback) ----
     ctx.set_params(ao_mode=p2v.AO_LEARNED)
     sampler = ClockSampler(dev)
@@ -592,9 +594,13 @@ def run_ours(args):
                                      "fallback_particles": int(st_learn["ao_fallback"]),
                                      "plain_ao_ms": st_plain["ms_ao"], "learned_ao_ms": st_learn["ms_ao"],
                                      "plain_march_kernel": plain_kernel,
-                                     "plain_ms_by_kernel": {"thread_per_particle": ms_plain_t, "warp_per_cone": ms_plain_w},
-                                     "plain_ao_ms_by_kernel": {"thread_per_particle": st_plain_t["ms_ao"],
-                                                               "warp_per_cone": st_plain_w["ms_ao"]},
+                                     "plain_ms_by_kernel": {"thread_per_particle": plain_runs["plain"][0],
+                                                            "thread_per_particle_brick_order": plain_runs["plain_brick"][0],
+                                                            "warp_per_cone": plain_runs["plain_warp"][0]},
+                                     "plain_ao_ms_by_kernel": {k2: plain_runs[k1][1]["ms_ao"] for k1, k2 in (
+                                         ("plain", "thread_per_particle"),
+                                         ("plain_brick", "thread_per_particle_brick_order"),
+                                         ("plain_warp", "warp_per_cone"))},
                                      "training": {"pairs": pairs, "val_rmse": train_rep["val_rmse"],
                                                   "steps": train_rep["steps"], "ms": train_rep["ms"]}},
                 "density_tile": {"tile": tune["tile"], "candidates_ms": {"x".join(map(str, c["tile"])): c["ms"]

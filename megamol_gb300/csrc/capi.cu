@@ -1183,7 +1183,7 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
     };
     // the cone-march stages can take the sorted particles in brick-major order (bricks of 16 x 4 x 4 cells):
     // neighbouring threads then sample neighbouring texels along all three axes. ao_brick_order -1: for the
-    // plain march (measured faster), not for the learned AO (its texture fetches gained nothing)
+    // plain march only (faster on uniform frames; the learned AO's texture fetches gained nothing)
     const float4* axyzr = nullptr;
     const float4* anrm = nullptr;
     const uint32_t* aorder = order;
@@ -1787,7 +1787,7 @@ void p2v_params_default(p2v_params* p) {
     p->sort_wait_polls = 0;
     p->test_hold_sort = 0;
     p->ao_march = P2V_AO_MARCH_THREAD;
-    p->ao_brick_order = -1;
+    p->ao_brick_order = 0;
 }
 
 p2v_status p2v_create(p2v_ctx** out, int device) {
