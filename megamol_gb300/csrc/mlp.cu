@@ -411,8 +411,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // poll count can be lowered (p2v_params.mma_wait_polls), and a test hook (p2v_params.test_hold_mma) leaves layer
 // 1 unissued so that its wait, on an arrival that never comes, runs out.
 // ---------------------------------------------------------------------------------------------
+#ifndef P2V_MLP_CTAS
+#define P2V_MLP_CTAS 4  // resident inference CTAs per SM (64 registers per thread at 4)
+#endif
 namespace tc {
 constexpr int THREADS = 256;
+constexpr int CTAS = P2V_MLP_CTAS;
 constexpr int M = 128;                         // particles per tile (MMA M, TMEM lanes)
 constexpr int KCH1 = MLP_KP / 8;               // 16-byte core-matrix columns of layer 1's K (10)
 constexpr int KCH2 = MLP_H / 8;                // of layer 2's K (8)
@@ -514,7 +518,7 @@ __device__ __forceinline__ void st_shared_v2(uint8_t* p, uint32_t a, uint32_t b)
 }
 
 template<bool FEATURES_IN>
-__global__ void __launch_bounds__(tc::THREADS, 4) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
+__global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     uint8_t* sA = tc_smem;
     uint8_t* sW1 = tc_smem + tc::A_BYTES;
@@ -866,9 +870,9 @@ cudaError_t launch_mlp_infer(const MlpInferArgs& a, const ConeParams& cp, bool f
         return cudaSuccess;
     static_assert(tc::DYN_SMEM <= 227 * 1024, "tensor-core tile does not fit in shared memory");
     const uint32_t ntiles = (a.n + tc::M - 1) / tc::M;
-    // four resident CTAs per SM (41 KB of shared memory and 64 registers per thread each; 4 x 64 TMEM
-    // columns of 512): one wave
-    const unsigned grid = (unsigned) std::min<uint32_t>(ntiles, (uint32_t) sms * 4);
+    // tc::CTAS resident CTAs per SM (41 KB of shared memory each, the registers the launch bounds leave, 64 TMEM
+    // columns each of 512): one wave
+    const unsigned grid = (unsigned) std::min<uint32_t>(ntiles, (uint32_t) sms * tc::CTAS);
     cudaError_t e;
     if (features_in) {
         e = cudaFuncSetAttribute(mlp_infer_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::DYN_SMEM);
