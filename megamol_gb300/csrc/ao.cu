@@ -25,14 +25,16 @@ namespace {
 // ---------------------------------------------------------------------------------------------
 // mip pyramid: level l+1 voxel = sum of the children 2g .. min(2g+1, N-1), divided by 8 always
 // ---------------------------------------------------------------------------------------------
+// One thread per voxel of the coarser level in 32-bit index arithmetic (an AO volume holds fewer than 2^31
+// texels, so every level above level 0 fewer than 2^28).
 __global__ void __launch_bounds__(256) mip_level_kernel(const float* __restrict__ src, int sx, int sy, int sz,
     float* __restrict__ dst, int dx, int dy, int dz, float sat_scale, int quantize) {
-    const int64_t n = (int64_t) dx * dy * dz;
-    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
-        const int x = (int) (i % dx);
-        const int y = (int) ((i / dx) % dy);
-        const int z = (int) (i / ((int64_t) dx * dy));
-        dst[i] = mip_voxel<true>(src, sx, sy, sz, x, y, z, sat_scale, quantize);
+    const uint32_t n = (uint32_t) dx * (uint32_t) dy * (uint32_t) dz;
+    const uint32_t pxy = (uint32_t) dx * (uint32_t) dy;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t z = i / pxy, r = i - z * pxy;
+        const uint32_t y = r / (uint32_t) dx, x = r - y * (uint32_t) dx;
+        dst[i] = mip_voxel<true>(src, sx, sy, sz, (int) x, (int) y, (int) z, sat_scale, quantize);
     }
 }
 

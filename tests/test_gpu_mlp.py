@@ -247,3 +247,20 @@ def test_brick_order_gives_the_same_bits(ctx, trained):
     b = ao_of(ctx, f, nrm, p2v.AO_LEARNED, ao_brick_order=1)
     ctx.set_params(ao_brick_order=0)
     assert np.array_equal(a, b)
+
+
+def test_learned_ao_with_gradient_normals(ctx, trained):
+    """P2V_NORMALS_GRADIENT with the learned AO: the inference kernel computes each particle's normal from the
+    density grid (the function of the gradient-normals kernel) and stores the fallback particles' normals for
+    the cone march. Against the same frame with the host's FP64 gradient normals passed as list normals the
+    normals differ in their last bits only: the AO agrees to 2e-3 RMS (features rounded to BF16)."""
+    f = synth.lj_liquid(cells=24, res=64, seed=48)
+    nrm = with_normals(ctx, f)
+    a = ao_of(ctx, f, nrm, p2v.AO_LEARNED)
+    b = ao_of(ctx, f, None, p2v.AO_LEARNED, ao_normals=p2v.NORMALS_GRADIENT)
+    c = ao_of(ctx, f, None, p2v.AO_LEARNED, ao_normals=p2v.NORMALS_GRADIENT, ao_brick_order=1)
+    ctx.set_params(ao_normals=p2v.NORMALS_LIST, ao_brick_order=0)
+    assert np.isfinite(b).all()
+    assert np.array_equal(b, c)
+    d = np.abs(a.astype(np.float64) - b)
+    assert np.sqrt(np.mean(d ** 2)) <= 2e-3 and d.max() <= 0.1, (np.sqrt(np.mean(d ** 2)), d.max())
