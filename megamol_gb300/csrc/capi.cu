@@ -1187,7 +1187,7 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
     const float4* axyzr = nullptr;
     const float4* anrm = nullptr;
     const uint32_t* aorder = order;
-    auto ao_inputs = [&](bool with_nrm) -> cudaError_t {
+    auto ao_inputs = [&]() -> cudaError_t {
         axyzr = pp.xyzr_s.as<float4>();
         anrm = pp.nrm_s.as<float4>();
         aorder = order;
@@ -1209,8 +1209,8 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         if (e == cudaSuccess)
             e = launch_brick_order(bp, g, pp.cstart.as<uint32_t>(), reinterpret_cast<const int4*>(pp.rec_a.as<float4>() + 1),
                                    n, pp.bk0.as<uint32_t>(), pp.bk1.as<uint32_t>(), pp.xyzr_s.as<float4>(),
-                                   with_nrm ? pp.nrm_s.as<float4>() : nullptr, order, pp.xyzr_b.as<float4>(),
-                                   pp.nrm_b.as<float4>(), pp.ord_b.as<uint32_t>(), sms, st);
+                                   pp.nrm_s.as<float4>(), order, pp.xyzr_b.as<float4>(), pp.nrm_b.as<float4>(),
+                                   pp.ord_b.as<uint32_t>(), sms, st);
         axyzr = pp.xyzr_b.as<float4>();
         anrm = pp.nrm_b.as<float4>();
         aorder = pp.ord_b.as<uint32_t>();
@@ -1262,7 +1262,7 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
             return P2V_OK;
         }
         P2V_CUDA_TRY(to_sorted());
-        P2V_CUDA_TRY(ao_inputs(true));
+        P2V_CUDA_TRY(ao_inputs());
         if (P.ao_march == P2V_AO_MARCH_WARP)
             P2V_CUDA_TRY(launch_cone_ao_warp(cp, axyzr, anrm, n, aorder, ao.as<float>(), sms, st));
         else
@@ -1287,22 +1287,12 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         a.w2h = mlp_w2h.as<__nv_bfloat16>();
         a.lo = mlp_has_range ? mlp_lo.as<float>() : nullptr;
         a.hi = mlp_has_range ? mlp_hi.as<float>() : nullptr;
-        // gradient normals are computed inside the inference kernel (the fallback particles' ones are stored for
-        // the cone march); list normals are sorted first
-        const bool grad = P.ao_normals == P2V_NORMALS_GRADIENT && pp.xyzr_sorted;
-        if (grad) {
-            P2V_CUDA_TRY(pp.nrm_s.ensure(sizeof(float4) * ((size_t) n + 1)));
-            a.grid = dgrid;
-            a.geo = g;
-        } else {
-            P2V_CUDA_TRY(to_sorted());
-        }
-        P2V_CUDA_TRY(ao_inputs(!grad));
-        a.nrm_out = const_cast<float4*>(anrm);
+        P2V_CUDA_TRY(to_sorted());
+        P2V_CUDA_TRY(ao_inputs());
         a.n = n;
         a.order = nullptr;  // sorted copies: position j is sorted position j
         a.xyzr = axyzr;
-        a.nrm = grad ? nullptr : anrm;
+        a.nrm = anrm;
         a.y = ao.as<float>();
         a.out_order = aorder;
         a.fallback = fb_list.as<uint32_t>();

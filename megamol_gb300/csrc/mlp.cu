@@ -21,7 +21,7 @@
 #include <cstdint>
 
 #include "ao_internal.h"
-#include "cone_march.cuh"
+#include "cone_device.cuh"
 #include "mlp_internal.h"
 #include "p2v_common.cuh"
 
@@ -531,7 +531,6 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
     __shared__ uint32_t s_tmem;
     __shared__ float s_part[tc::M];
     __shared__ uint32_t s_flag[tc::M];
-    __shared__ float4 s_nrm[tc::M];  // gradient normals of the tile's particles (args.grid)
 
     const int t = threadIdx.x;
     const int row = t & (tc::M - 1), half = t >> 7;
@@ -614,18 +613,10 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
             }
         } else {
             float u[3] = {0, 0, 0}, nn[3] = {0, 0, 0}, ex[3], ez[3];
-            if (valid)
+            if (valid) {
                 o = args.order ? args.order[pi] : pi;
-            if (args.grid) {
-                // the first half computes its particle's normal from the grid (the function of the gradient
-                // normals kernel, so the same bits), the second half takes it from shared memory
-                if (half == 0)
-                    s_nrm[row] = valid ? gradient_normal<true>(args.geo, args.grid, args.xyzr[o])
-                                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                __syncthreads();
+                valid = particle_frame(cp, args.xyzr[o], args.nrm[o], u, nn, ex, ez);
             }
-            if (valid)
-                valid = particle_frame(cp, args.xyzr[o], args.grid ? s_nrm[row] : args.nrm[o], u, nn, ex, ez);
             // this half's cones 4 h .. 4 h + 3 = features 36 h .. 36 h + 35 (K positions equal feature indices)
             constexpr int HALF_F = MLP_SAMPLES / 2;  // 36
             float fv[HALF_F];
@@ -741,8 +732,6 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
                 args.y[wo] = 1.0f;  // no normal / invalid particle: unoccluded, as the cone march
             } else if (oor && args.fallback) {
                 args.fallback[atomicAdd(args.nfallback, 1u)] = oo;
-                if (!FEATURES_IN && args.grid && args.nrm_out)
-                    args.nrm_out[oo] = s_nrm[row];  // the cone march of the fallback list reads it
                 if (FEATURES_IN)
                     args.y[wo] = y;
             } else {

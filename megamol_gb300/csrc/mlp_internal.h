@@ -42,12 +42,7 @@ struct MlpInferArgs {
     // extracted features (inference on particles)
     const uint32_t* order;          // sorted position -> particle index
     const float4* xyzr;
-    const float4* nrm;              // the particles' normals (sorted order), unless `grid` is given
-    // grid non-null: each particle's normal is computed in the kernel as -grad(grid) (P2V_NORMALS_GRADIENT);
-    // the normals of the particles that fall back to the cone march are stored to nrm_out (sorted order)
-    const float* grid;
-    GridGeo geo;
-    float4* nrm_out;
+    const float4* nrm;
     // given features (tests)
     const float* X;
     float* y;                       // output, indexed by particle (or by row for given features)

@@ -250,10 +250,9 @@ def test_brick_order_gives_the_same_bits(ctx, trained):
 
 
 def test_learned_ao_with_gradient_normals(ctx, trained):
-    """P2V_NORMALS_GRADIENT with the learned AO: the inference kernel computes each particle's normal from the
-    density grid (the function of the gradient-normals kernel) and stores the fallback particles' normals for
-    the cone march. Against the same frame with the host's FP64 gradient normals passed as list normals the
-    normals differ in their last bits only: the AO agrees to 2e-3 RMS (features rounded to BF16)."""
+    """P2V_NORMALS_GRADIENT with the learned AO (normals down the density gradient computed by the library,
+    also in brick order). Against the same frame with the host's FP64 gradient normals passed as list normals
+    the normals differ in their last bits only: the AO agrees to 2e-3 RMS (features rounded to BF16)."""
     f = synth.lj_liquid(cells=24, res=64, seed=48)
     nrm = with_normals(ctx, f)
     a = ao_of(ctx, f, nrm, p2v.AO_LEARNED)
