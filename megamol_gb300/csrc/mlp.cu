@@ -491,17 +491,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint32_
     return false;
 }
 
-// 16 consecutive TMEM columns of this thread's lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
+// 32 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+          "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+          "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 16; ++j)
+    for (int j = 0; j < 32; ++j)
         v[j] = __uint_as_float(r[j]);
 }
 
@@ -511,61 +515,6 @@ __device__ __forceinline__ void st_shared_v4(uint8_t* p, uint32_t a, uint32_t b,
 
 __device__ __forceinline__ void st_shared_v2(uint8_t* p, uint32_t a, uint32_t b) {
     *reinterpret_cast<uint2*>(p) = make_uint2(a, b);
-}
-
-// Store the BF16 pairs pk[0 .. NP) at K positions K0, K0 + 2, ... of row `row` (K0 even) with the widest
-// aligned shared-memory stores (a pair never straddles a core-matrix row: K0 + 2 e is even).
-template<int K0, int NP>
-__device__ __forceinline__ void store_pairs(uint8_t* sA, int row, const uint32_t* pk) {
-    int k = K0, i = 0;
-#pragma unroll
-    for (int step = 0; step < NP; ++step) {
-        if (i >= NP)
-            break;
-        if (k % 8 == 0 && NP - i >= 4) {
-            st_shared_v4(sA + canon_off(row, k, tc::SBO1), pk[i], pk[i + 1], pk[i + 2], pk[i + 3]);
-            k += 8;
-            i += 4;
-        } else if (k % 4 == 0 && NP - i >= 2) {
-            st_shared_v2(sA + canon_off(row, k, tc::SBO1), pk[i], pk[i + 1]);
-            k += 4;
-            i += 2;
-        } else {
-            *reinterpret_cast<uint32_t*>(sA + canon_off(row, k, tc::SBO1)) = pk[i];
-            k += 2;
-            i += 1;
-        }
-    }
-}
-
-// The features of cones K0 / 9 and K0 / 9 + 1 (K positions K0 .. K0 + 17, the feature indices) into the A tile
-// as BF16 pairs; true when one of them lies outside the training range. Two cones at a time keep 18 features
-// live instead of a half's 36.
-template<int K0>
-__device__ __forceinline__ bool feature_pair_of_cones(const ConeParams& cp, bool valid, const float u[3],
-    const float nn[3], const float ex[3], const float ez[3], uint8_t* sA, int row, bool check,
-    const __nv_bfloat162* sLo2, const __nv_bfloat162* sHi2) {
-    static_assert(K0 % 18 == 0, "two cones of MLP_FSTEPS = 9 features");
-    float fv[2 * MLP_FSTEPS];
-    if (valid) {
-        cone_features(cp, K0 / MLP_FSTEPS, u, nn, ex, ez, fv);
-        cone_features(cp, K0 / MLP_FSTEPS + 1, u, nn, ex, ez, fv + MLP_FSTEPS);
-    } else {
-#pragma unroll
-        for (int j = 0; j < 2 * MLP_FSTEPS; ++j)
-            fv[j] = 0.0f;
-    }
-    bool oor = false;
-    uint32_t pk[MLP_FSTEPS];
-#pragma unroll
-    for (int e = 0; e < MLP_FSTEPS; ++e) {
-        const __nv_bfloat162 v2 = __floats2bfloat162_rn(fv[2 * e], fv[2 * e + 1]);
-        if (check && valid)
-            oor |= !(__hble2(sLo2[K0 / 2 + e], v2) && __hble2(v2, sHi2[K0 / 2 + e]));
-        pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
-    }
-    store_pairs<K0, MLP_FSTEPS>(sA, row, pk);
-    return oor;
 }
 
 template<bool FEATURES_IN>
@@ -668,15 +617,41 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
                 o = args.order ? args.order[pi] : pi;
                 valid = particle_frame(cp, args.xyzr[o], args.nrm[o], u, nn, ex, ez);
             }
-            // this half's cones 4 h .. 4 h + 3 = features 36 h .. 36 h + 35 (K positions equal feature indices),
-            // two cones at a time
+            // this half's cones 4 h .. 4 h + 3 = features 36 h .. 36 h + 35 (K positions equal feature indices)
+            constexpr int HALF_F = MLP_SAMPLES / 2;  // 36
+            float fv[HALF_F];
+#pragma unroll
+            for (int cc = 0; cc < MLP_CONES / 2; ++cc) {
+                if (valid)
+                    cone_features(cp, (MLP_CONES / 2) * half + cc, u, nn, ex, ez, fv + cc * MLP_FSTEPS);
+                else
+#pragma unroll
+                    for (int j = 0; j < MLP_FSTEPS; ++j)
+                        fv[cc * MLP_FSTEPS + j] = 0.0f;
+            }
+            uint32_t pk[HALF_F / 2];
+#pragma unroll
+            for (int e = 0; e < HALF_F / 2; ++e) {
+                const __nv_bfloat162 v2 = __floats2bfloat162_rn(fv[2 * e], fv[2 * e + 1]);
+                if (check && valid)
+                    oor |= !in_range((HALF_F / 2) * half + e, v2);
+                pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
+            }
             if (half == 0) {
-                oor |= feature_pair_of_cones<0>(cp, valid, u, nn, ex, ez, sA, row, check, sLo2, sHi2);
-                oor |= feature_pair_of_cones<18>(cp, valid, u, nn, ex, ez, sA, row, check, sLo2, sHi2);
+                // K 0..31 (chunks 0..3) and K 32..35 (the first half of chunk 4)
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    st_shared_v4(sA + canon_off(row, 8 * c, tc::SBO1), pk[4 * c], pk[4 * c + 1], pk[4 * c + 2],
+                                 pk[4 * c + 3]);
+                st_shared_v2(sA + canon_off(row, 32, tc::SBO1), pk[16], pk[17]);
             } else {
-                oor |= feature_pair_of_cones<36>(cp, valid, u, nn, ex, ez, sA, row, check, sLo2, sHi2);
-                oor |= feature_pair_of_cones<54>(cp, valid, u, nn, ex, ez, sA, row, check, sLo2, sHi2);
-                // chunk 9: the normal, the surface point and two zeros (K 72..79)
+                // K 36..39 (the second half of chunk 4), K 40..71 (chunks 5..8), then chunk 9: the normal, the
+                // surface point and two zeros (K 72..79)
+                st_shared_v2(sA + canon_off(row, 36, tc::SBO1), pk[0], pk[1]);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    st_shared_v4(sA + canon_off(row, 40 + 8 * c, tc::SBO1), pk[2 + 4 * c], pk[3 + 4 * c],
+                                 pk[4 + 4 * c], pk[5 + 4 * c]);
                 const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
                 const __nv_bfloat162 n2u0 = __floats2bfloat162_rn(nn[2], u[0]);
                 const __nv_bfloat162 u12 = __floats2bfloat162_rn(u[1], u[2]);
@@ -709,22 +684,18 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
         tc_fence_after();
         if (__syncthreads_or(failed))
             break;
-        // hidden layer 1 -> A tile (K = 64 layout): columns 32 half .. 32 half + 31 of row `row`, read from TMEM
-        // 16 at a time (fewer live registers)
+        float v[32];
+        tmem_ld32(taddr, v);
+        // hidden layer 1 -> A tile (K = 64 layout): columns 32 half .. 32 half + 31 of row `row`
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-            float v[16];
-            tmem_ld16(taddr + 16u * hh, v);
+        for (int c = 0; c < 4; ++c) {
+            uint32_t pk[4];
 #pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                uint32_t pk[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int j = 8 * c + 2 * e, col = 32 * half + 16 * hh + j;
-                    pk[e] = pack_bf16(silu_fast(v[j] + sB1[col]), silu_fast(v[j + 1] + sB1[col + 1]));
-                }
-                st_shared_v4(sA + canon_off(row, 32 * half + 16 * hh + 8 * c, tc::SBO2), pk[0], pk[1], pk[2], pk[3]);
+            for (int e = 0; e < 4; ++e) {
+                const int j = 8 * c + 2 * e;
+                pk[e] = pack_bf16(silu_fast(v[j] + sB1[32 * half + j]), silu_fast(v[j + 1] + sB1[32 * half + j + 1]));
             }
+            st_shared_v4(sA + canon_off(row, 32 * half + 8 * c, tc::SBO2), pk[0], pk[1], pk[2], pk[3]);
         }
         fence_async_smem();
         tc_fence_before();
@@ -743,18 +714,12 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
         tc_fence_after();
         if (__syncthreads_or(failed))
             break;
-        // ---- layer 3 (64 -> 1) in FP32: each half sums its 32 columns in column order ----
+        tmem_ld32(taddr, v);
+        // ---- layer 3 (64 -> 1) in FP32: each half sums its 32 columns ----
         float z = 0.0f;
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-            float v[16];
-            tmem_ld16(taddr + 16u * hh, v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = 32 * half + 16 * hh + j;
-                z = fmaf(silu_fast(v[j] + sB2[col]), sW3[col], z);
-            }
-        }
+        for (int j = 0; j < 32; ++j)
+            z = fmaf(silu_fast(v[j] + sB2[32 * half + j]), sW3[32 * half + j], z);
         if (half == 1)
             s_part[row] = z;
         tc_fence_before();
