@@ -62,15 +62,13 @@ __device__ __forceinline__ float feature_tex_sample(unsigned long long tex, floa
     const float z0f = floorf(cz);
     const float fz = cz - z0f;
     const int z0 = (int) z0f;
-    if (z0 >= 0 && z0 < dz) {
-        const float2 p = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, z0);
-        return fmaf(fz, p.y - p.x, p.x);
-    }
-    if (z0 == -1) {  // between the border and slice 0
-        const float2 p = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, 0);
-        return fz * p.x;
-    }
-    return 0.0f;
+    // branch-free (every sample fetches, so the fetches of a particle issue back to back): the layer clamped
+    // into the texture; below slice 0 the pair is (border 0, slice 0), past the last slice (0, 0)
+    const float2 p = tex2DLayered<float2>((cudaTextureObject_t) tex, qx, qy, min(max(z0, 0), dz - 1));
+    const bool inside = z0 >= 0 && z0 < dz;
+    const float lo = inside ? p.x : 0.0f;
+    const float hi = inside ? p.y : (z0 == -1 ? p.x : 0.0f);
+    return fmaf(fz, hi - lo, lo);
 }
 
 // Feature sample j of a cone with direction dir from normalised point u: the march's step fstep[j] at its
