@@ -140,16 +140,8 @@ __device__ __forceinline__ float march_cone(const ConeParams& cp, int c, const f
     float dir[3];
     cone_dir(cp, c, ex, nn, ez, dir);
     float acc = 0.0f;
-    // two steps' samples are taken before either is used (their loads overlap); the recurrence and the early
-    // exit then run in step order, so the result is that of a step-by-step march (the second sample of a
-    // pair past the exit, or past the last step, is taken and not used)
-    for (int k = 0; k < cp.nsteps; k += 2) {
-        const float s0 = cone_sample<NC>(cp, dir, u, k);
-        const float s1 = cone_sample<NC>(cp, dir, u, min(k + 1, cp.nsteps - 1));
-        acc = __fmaf_rn(__fsub_rn(1.0f, acc), s0, acc);
-        if ((cp.early_exit && acc > 0.99f) || k + 1 >= cp.nsteps)
-            break;
-        acc = __fmaf_rn(__fsub_rn(1.0f, acc), s1, acc);
+    for (int k = 0; k < cp.nsteps; ++k) {
+        acc = __fmaf_rn(__fsub_rn(1.0f, acc), cone_sample<NC>(cp, dir, u, k), acc);
         if (cp.early_exit && acc > 0.99f)
             break;
     }
