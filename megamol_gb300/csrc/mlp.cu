@@ -515,6 +515,31 @@ __device__ __forceinline__ void st_shared_v2(uint8_t* p, uint32_t a, uint32_t b)
     *reinterpret_cast<uint2*>(p) = make_uint2(a, b);
 }
 
+// Store the BF16 pairs pk[0 .. NP) at K positions K0, K0 + 2, ... of row `row` (K0 even) with the widest
+// aligned shared-memory stores (a pair never straddles a core-matrix row: K0 + 2 e is even).
+template<int K0, int NP>
+__device__ __forceinline__ void store_pairs(uint8_t* sA, int row, const uint32_t* pk) {
+    int k = K0, i = 0;
+#pragma unroll
+    for (int step = 0; step < NP; ++step) {
+        if (i >= NP)
+            break;
+        if (k % 8 == 0 && NP - i >= 4) {
+            st_shared_v4(sA + canon_off(row, k, tc::SBO1), pk[i], pk[i + 1], pk[i + 2], pk[i + 3]);
+            k += 8;
+            i += 4;
+        } else if (k % 4 == 0 && NP - i >= 2) {
+            st_shared_v2(sA + canon_off(row, k, tc::SBO1), pk[i], pk[i + 1]);
+            k += 4;
+            i += 2;
+        } else {
+            *reinterpret_cast<uint32_t*>(sA + canon_off(row, k, tc::SBO1)) = pk[i];
+            k += 2;
+            i += 1;
+        }
+    }
+}
+
 template<bool FEATURES_IN>
 __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(const MlpInferArgs args, const ConeParams cp) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
@@ -615,7 +640,8 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
                 o = args.order ? args.order[pi] : pi;
                 valid = particle_frame(cp, args.xyzr[o], args.nrm[o], u, nn, ex, ez);
             }
-            // this half's cones 4 h .. 4 h + 3 = features 36 h .. 36 h + 35 (K positions equal feature indices)
+            // this half's cones 4 h .. 4 h + 3 = features HALF_F h .. HALF_F (h + 1) - 1 (K positions equal
+            // feature indices)
             constexpr int HALF_F = MLP_SAMPLES / 2;  // 36
             float fv[HALF_F];
 #pragma unroll
@@ -636,25 +662,19 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
                 pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
             }
             if (half == 0) {
-                // K 0..31 (chunks 0..3) and K 32..35 (the first half of chunk 4)
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    st_shared_v4(sA + canon_off(row, 8 * c, tc::SBO1), pk[4 * c], pk[4 * c + 1], pk[4 * c + 2],
-                                 pk[4 * c + 3]);
-                st_shared_v2(sA + canon_off(row, 32, tc::SBO1), pk[16], pk[17]);
+                store_pairs<0, HALF_F / 2>(sA, row, pk);
             } else {
-                // K 36..39 (the second half of chunk 4), K 40..71 (chunks 5..8), then chunk 9: the normal, the
-                // surface point and two zeros (K 72..79)
-                st_shared_v2(sA + canon_off(row, 36, tc::SBO1), pk[0], pk[1]);
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    st_shared_v4(sA + canon_off(row, 40 + 8 * c, tc::SBO1), pk[2 + 4 * c], pk[3 + 4 * c],
-                                 pk[4 + 4 * c], pk[5 + 4 * c]);
+                store_pairs<HALF_F, HALF_F / 2>(sA, row, pk);
+                // then the normal, the surface point and two zeros (K MLP_SAMPLES .. MLP_SAMPLES + 7), and zeros up
+                // to MLP_KP
                 const __nv_bfloat162 n01 = __floats2bfloat162_rn(nn[0], nn[1]);
                 const __nv_bfloat162 n2u0 = __floats2bfloat162_rn(nn[2], u[0]);
                 const __nv_bfloat162 u12 = __floats2bfloat162_rn(u[1], u[2]);
                 st_shared_v4(sA + canon_off(row, MLP_SAMPLES, tc::SBO1), *reinterpret_cast<const uint32_t*>(&n01),
                              *reinterpret_cast<const uint32_t*>(&n2u0), *reinterpret_cast<const uint32_t*>(&u12), 0u);
+#pragma unroll
+                for (int k = MLP_SAMPLES + 8; k < MLP_KP; k += 8)
+                    st_shared_v4(sA + canon_off(row, k, tc::SBO1), 0u, 0u, 0u, 0u);
                 if (valid && check)
                     oor |= !(in_range(MLP_SAMPLES / 2, n01) && in_range(MLP_SAMPLES / 2 + 1, n2u0) &&
                              in_range(MLP_SAMPLES / 2 + 2, u12));

@@ -6,19 +6,25 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "../../include/p2v.h"
 #include "ao_internal.h"
 
 namespace p2v {
 
 // Features: the cone march's own samples, for each of MLP_CONES cones at MLP_FSTEPS of its steps (cone-major:
 // feature c * MLP_FSTEPS + j), then the unit normal and the surface point in normalised volume coordinates.
+#ifndef P2V_MLP_FSTEPS_BUILD
+#define P2V_MLP_FSTEPS_BUILD P2V_MLP_FSTEPS
+#endif
 constexpr int MLP_CONES = 8;
-constexpr int MLP_FSTEPS = 9;
+constexpr int MLP_FSTEPS = P2V_MLP_FSTEPS_BUILD;
 constexpr int MLP_SAMPLES = MLP_CONES * MLP_FSTEPS;   // 72
 constexpr int MLP_IN = MLP_SAMPLES + 6;               // 78
 static_assert(MLP_FSTEPS <= MAX_FSTEPS, "feature step table too small");
-// The tensor-core tile holds feature i at K position i; K 78, 79 are zero (MLP_KP = 80, five MMAs of K = 16).
-constexpr int MLP_KP = 80;
+static_assert(MLP_SAMPLES % 8 == 0, "the normal and the surface point start a core-matrix column");
+// The tensor-core tile holds feature i at K position i; K MLP_IN .. MLP_KP - 1 are zero (MLP_KP = 80: five MMAs
+// of K = 16).
+constexpr int MLP_KP = (MLP_IN + 15) / 16 * 16;
 __host__ __device__ constexpr int mlp_feature_at(int k) {
     return k < MLP_IN ? k : -1;
 }
