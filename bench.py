@@ -582,7 +582,7 @@ def run_ours(args):
         line = {"metric": "particles/s density+AO", "value": value, "unit": "particles/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP: bf16 x bf16 -> f32)", "data": "synthetic",
-                "config": dict(desc, ao=("learned AO (MLP 78-64-64-1 on cone samples, BF16 tensor cores) with "
+                "config": dict(desc, ao=("learned AO (MLP 54-64-64-1 on cone samples, BF16 tensor cores) with "
                                          "cone-march fallback" if use_learned else "plain cone march") +
                                         ", 8 cones x 32 steps, 3-level mip, normals down the density gradient (library)",
                                l2=f"per-step working set ~{(f.n * 84 + V * 12) / 2 ** 30:.1f} GiB > 126 MiB L2 "

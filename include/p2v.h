@@ -260,13 +260,13 @@ typedef struct p2v_stats {
  * march's steps (step round(j (steps - 1) / (P2V_MLP_FSTEPS - 1)) for feature j), each at the step's own mip
  * level (linear between the two levels around its lod); cone-major (feature c * P2V_MLP_FSTEPS + j). Then the
  * unit normal and the surface point in normalised volume coordinates; P2V_MLP_INPUTS values. The learned AO
- * therefore needs ao_cones = P2V_MLP_CONES. Network 78 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid. Parameter
- * vector: W1[64][78], b1[64], W2[64][64], b2[64], w3[64], b3. */
+ * therefore needs ao_cones = P2V_MLP_CONES. Network 54 -> 64 -> 64 -> 1 with SiLU, SiLU, sigmoid. Parameter
+ * vector: W1[64][54], b1[64], W2[64][64], b2[64], w3[64], b3. */
 #define P2V_MLP_CONES 8
-#define P2V_MLP_FSTEPS 9
-#define P2V_MLP_INPUTS 78
+#define P2V_MLP_FSTEPS 6
+#define P2V_MLP_INPUTS 54
 #define P2V_MLP_HIDDEN 64
-#define P2V_MLP_PARAMS 9281
+#define P2V_MLP_PARAMS 7745
 
 typedef struct p2v_train_params {
     uint32_t struct_size;   /* sizeof(p2v_train_params); set by p2v_train_params_default */

@@ -1727,7 +1727,7 @@ cudaError_t grow_keep(DevBuf& b, size_t need, size_t used) {
     return e;
 }
 
-constexpr char MLP_MAGIC[8] = {'P', '2', 'V', 'M', 'L', 'P', '0', '2'};
+constexpr char MLP_MAGIC[8] = {'P', '2', 'V', 'M', 'L', 'P', '0', '3'};
 #if P2V_MLP_FSTEPS_BUILD == P2V_MLP_FSTEPS  // (an experimental build may change the step count)
 static_assert(P2V_MLP_INPUTS == MLP_IN && P2V_MLP_HIDDEN == MLP_H && P2V_MLP_PARAMS == MLP_NPARAM &&
                   P2V_MLP_CONES == MLP_CONES && P2V_MLP_FSTEPS == MLP_FSTEPS,

@@ -1,9 +1,9 @@
 // Learned AO: a small MLP that stands in for the cone march.
 //
-// Input (78): the cone march's own visibility samples, read by the texture units: for each of the 8 cones, in
-// the particle's MDAO cone frame, the volume at 9 of the march's steps (spread evenly over the step table),
+// Input (54): the cone march's own visibility samples, read by the texture units: for each of the 8 cones, in
+// the particle's MDAO cone frame, the volume at 6 of the march's steps (spread evenly over the step table),
 // each at the step's own mip level (LINEAR_MIPMAP_LINEAR between the two levels around its lod); then the
-// unit normal and the surface point in normalised volume coordinates. Network 78 -> 64 -> 64 -> 1, SiLU,
+// unit normal and the surface point in normalised volume coordinates. Network 54 -> 64 -> 64 -> 1, SiLU,
 // SiLU, sigmoid: it learns how the march's 32 steps, early exit and cone average turn these samples into AO.
 // Training: FP32 forward/backward kernels per CTA with a fixed-order reduction of the per-CTA gradients,
 // then Adam; pairs come from the plain cone march. Inference: BF16 weights and features, FP32 accumulation
@@ -398,7 +398,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // Inference on the 5th-generation tensor cores (tcgen05). One CTA of 256 threads takes 128 particles per
 // tile. Threads t and t + 128 extract the cone samples of particle t (cones 0-3 and 4-7) straight into the A
 // tile (BF16, canonical no-swizzle K-major layout in shared memory, feature i at K position i); one thread
-// issues the layer-1 MMAs (M = 128, N = 64, K = 80) into 64 TMEM columns and commits
+// issues the layer-1 MMAs (M = 128, N = 64, K = 64) into 64 TMEM columns and commits
 // them to an mbarrier. The epilogue reads TMEM
 // (warp w: lanes 32 (w % 4).., columns 32 (w / 4)..), adds the bias, applies SiLU and writes the hidden
 // layer back into the A tile as layer 2's A operand; layer 2 (K = 64) reuses the TMEM columns, and its
@@ -416,11 +416,11 @@ namespace tc {
 constexpr int THREADS = 256;
 constexpr int CTAS = P2V_MLP_CTAS;
 constexpr int M = 128;                         // particles per tile (MMA M, TMEM lanes)
-constexpr int KCH1 = MLP_KP / 8;               // 16-byte core-matrix columns of layer 1's K (10)
+constexpr int KCH1 = MLP_KP / 8;               // 16-byte core-matrix columns of layer 1's K (8)
 constexpr int KCH2 = MLP_H / 8;                // of layer 2's K (8)
 constexpr int SBO1 = KCH1 * 128;               // bytes between 8-row core-matrix groups, layer 1
 constexpr int SBO2 = KCH2 * 128;               // layer 2
-constexpr int A_BYTES = (M / 8) * SBO1;        // 20480: features; later the hidden layer (16384 B)
+constexpr int A_BYTES = (M / 8) * SBO1;        // 16384: features; later the hidden layer (16384 B)
 constexpr int W1_BYTES = (MLP_H / 8) * SBO1;   // 10240
 constexpr int W2_BYTES = (MLP_H / 8) * SBO2;   // 8192
 constexpr int DYN_SMEM = A_BYTES + W1_BYTES + W2_BYTES;
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
             }
             // this half's cones 4 h .. 4 h + 3 = features HALF_F h .. HALF_F (h + 1) - 1 (K positions equal
             // feature indices)
-            constexpr int HALF_F = MLP_SAMPLES / 2;  // 36
+            constexpr int HALF_F = MLP_SAMPLES / 2;  // 24
             float fv[HALF_F];
 #pragma unroll
             for (int cc = 0; cc < MLP_CONES / 2; ++cc) {
@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
         __syncthreads();
         if (half == 0)
             oor = oor || s_flag[row] != 0u;
-        // ---- layer 1: D[128 x 64] = A[128 x 80] W1^T ----
+        // ---- layer 1: D[128 x 64] = A[128 x MLP_KP] W1^T ----
         if (t == 0 && !args.hold_mma) {
             tc_fence_after();
 #pragma unroll

@@ -18,11 +18,11 @@ namespace p2v {
 #endif
 constexpr int MLP_CONES = 8;
 constexpr int MLP_FSTEPS = P2V_MLP_FSTEPS_BUILD;
-constexpr int MLP_SAMPLES = MLP_CONES * MLP_FSTEPS;   // 72
-constexpr int MLP_IN = MLP_SAMPLES + 6;               // 78
+constexpr int MLP_SAMPLES = MLP_CONES * MLP_FSTEPS;   // 48
+constexpr int MLP_IN = MLP_SAMPLES + 6;               // 54
 static_assert(MLP_FSTEPS <= MAX_FSTEPS, "feature step table too small");
 static_assert(MLP_SAMPLES % 8 == 0, "the normal and the surface point start a core-matrix column");
-// The tensor-core tile holds feature i at K position i; K MLP_IN .. MLP_KP - 1 are zero (MLP_KP = 80: five MMAs
+// The tensor-core tile holds feature i at K position i; K MLP_IN .. MLP_KP - 1 are zero (MLP_KP = 64: four MMAs
 // of K = 16).
 constexpr int MLP_KP = (MLP_IN + 15) / 16 * 16;
 __host__ __device__ constexpr int mlp_feature_at(int k) {

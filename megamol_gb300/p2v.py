@@ -136,7 +136,7 @@ class TrainReport(C.Structure):
                 ("final_loss", C.c_float), ("val_rmse", C.c_float), ("val_max_err", C.c_float), ("ms", C.c_double)]
 
 
-MLP_CONES, MLP_FSTEPS, MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 8, 9, 78, 64, 9281
+MLP_CONES, MLP_FSTEPS, MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 8, 6, 54, 64, 7745
 
 # Every entry point include/p2v.h declares, with its ctypes signature.
 _SIGNATURES = {

@@ -607,8 +607,8 @@ def aosphere_ao_f64(tex, clip, xyzr, normals, mode=0, step_len=0.5, eval_fac=1.0
     return out
 
 
-MLP_IN, MLP_HIDDEN = 78, 64
-MLP_CONES, MLP_FSTEPS = 8, 9
+MLP_IN, MLP_HIDDEN = 54, 64
+MLP_CONES, MLP_FSTEPS = 8, 6
 
 
 def mlp_feature_steps(nsteps: int, fsteps: int = MLP_FSTEPS) -> list[int]:

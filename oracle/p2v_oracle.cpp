@@ -798,7 +798,7 @@ extern "C" void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], cons
  * ---------------------------------------------------------------------------------------------- */
 extern "C" void p2vo_mlp_f64(const double* P, const float* x, const float* t, int64_t n, double* grads, double* loss,
     double* y) {
-    const int IN = 78, H = 64;
+    const int IN = 54, H = 64;
     const double* W1 = P;
     const double* b1 = W1 + H * IN;
     const double* W2 = b1 + H;

@@ -113,8 +113,8 @@ void p2vo_aosphere_volume_f64(const float* xyzr, int64_t n, const float clip[6],
 void p2vo_aosphere_ao_f64(const double* tex, const int32_t s[3], const float clip[6], float step_len, float eval_fac,
     const float* xyzr, const float* nrm, int64_t n, int mode, double* ao);
 
-/* Learned-AO MLP 78 -> 64 -> 64 -> 1 (SiLU, SiLU, sigmoid), FP64 reference for gradient checks.
- * params: W1[64][78], b1[64], W2[64][64], b2[64], w3[64], b3 (9281 values). Loss = mean((y - t)^2).
+/* Learned-AO MLP 54 -> 64 -> 64 -> 1 (SiLU, SiLU, sigmoid), FP64 reference for gradient checks.
+ * params: W1[64][54], b1[64], W2[64][64], b2[64], w3[64], b3 (7745 values). Loss = mean((y - t)^2).
  * grads (may be NULL) receives dLoss/dparams; y (may be NULL) the predictions. */
 void p2vo_mlp_f64(const double* params, const float* x, const float* t, int64_t n, double* grads, double* loss,
     double* y);

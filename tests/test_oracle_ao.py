@@ -67,7 +67,8 @@ def test_cone_features_known_answers():
     assert np.allclose(x[:, ns + 3:], (xyzr[:, :3] + xyzr[:, 3:] * n) / 32)
     z = oracle.cone_features_f64([L * 0 for L in levels], dirs, t, lod, xyzr, nrm, (0, 0, 0), (1 / 32,) * 3)
     assert np.all(z[:, :ns] == 0)
-    assert oracle.mlp_feature_steps(32) == [0, 4, 8, 12, 16, 19, 23, 27, 31]
+    assert oracle.mlp_feature_steps(32) == [0, 6, 12, 19, 25, 31]
+    assert oracle.mlp_feature_steps(32, 9) == [0, 4, 8, 12, 16, 19, 23, 27, 31]
 
 
 def test_gradient_normals_f32_match_host_normals():
