@@ -409,6 +409,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // poll count can be lowered (p2v_params.mma_wait_polls), and a test hook (p2v_params.test_hold_mma) leaves layer
 // 1 unissued so that its wait, on an arrival that never comes, runs out.
 // ---------------------------------------------------------------------------------------------
+#ifndef P2V_MLP_PACK_PER_CONE
+#define P2V_MLP_PACK_PER_CONE 1  // with an even step count, pack each cone's features as soon as it is sampled
+#endif
 #ifndef P2V_MLP_CTAS
 #define P2V_MLP_CTAS 4  // resident inference CTAs per SM (64 registers per thread at 4)
 #endif
@@ -643,23 +646,46 @@ __global__ void __launch_bounds__(tc::THREADS, tc::CTAS) mlp_infer_tc_kernel(con
             // this half's cones 4 h .. 4 h + 3 = features HALF_F h .. HALF_F (h + 1) - 1 (K positions equal
             // feature indices)
             constexpr int HALF_F = MLP_SAMPLES / 2;  // 24
-            float fv[HALF_F];
-#pragma unroll
-            for (int cc = 0; cc < MLP_CONES / 2; ++cc) {
-                if (valid)
-                    cone_features(cp, (MLP_CONES / 2) * half + cc, u, nn, ex, ez, fv + cc * MLP_FSTEPS);
-                else
-#pragma unroll
-                    for (int j = 0; j < MLP_FSTEPS; ++j)
-                        fv[cc * MLP_FSTEPS + j] = 0.0f;
-            }
             uint32_t pk[HALF_F / 2];
+            if constexpr (MLP_FSTEPS % 2 == 0 && P2V_MLP_PACK_PER_CONE) {
+                // an even step count: a cone's features pair up among themselves, so each cone is packed as soon
+                // as it is sampled (fewer live registers)
 #pragma unroll
-            for (int e = 0; e < HALF_F / 2; ++e) {
-                const __nv_bfloat162 v2 = __floats2bfloat162_rn(fv[2 * e], fv[2 * e + 1]);
-                if (check && valid)
-                    oor |= !in_range((HALF_F / 2) * half + e, v2);
-                pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
+                for (int cc = 0; cc < MLP_CONES / 2; ++cc) {
+                    float fv[MLP_FSTEPS];
+                    if (valid)
+                        cone_features(cp, (MLP_CONES / 2) * half + cc, u, nn, ex, ez, fv);
+                    else
+#pragma unroll
+                        for (int j = 0; j < MLP_FSTEPS; ++j)
+                            fv[j] = 0.0f;
+#pragma unroll
+                    for (int e = 0; e < MLP_FSTEPS / 2; ++e) {
+                        const int pe = cc * (MLP_FSTEPS / 2) + e;
+                        const __nv_bfloat162 v2 = __floats2bfloat162_rn(fv[2 * e], fv[2 * e + 1]);
+                        if (check && valid)
+                            oor |= !in_range((HALF_F / 2) * half + pe, v2);
+                        pk[pe] = *reinterpret_cast<const uint32_t*>(&v2);
+                    }
+                }
+            } else {
+                float fv[HALF_F];
+#pragma unroll
+                for (int cc = 0; cc < MLP_CONES / 2; ++cc) {
+                    if (valid)
+                        cone_features(cp, (MLP_CONES / 2) * half + cc, u, nn, ex, ez, fv + cc * MLP_FSTEPS);
+                    else
+#pragma unroll
+                        for (int j = 0; j < MLP_FSTEPS; ++j)
+                            fv[cc * MLP_FSTEPS + j] = 0.0f;
+                }
+#pragma unroll
+                for (int e = 0; e < HALF_F / 2; ++e) {
+                    const __nv_bfloat162 v2 = __floats2bfloat162_rn(fv[2 * e], fv[2 * e + 1]);
+                    if (check && valid)
+                        oor |= !in_range((HALF_F / 2) * half + e, v2);
+                    pk[e] = *reinterpret_cast<const uint32_t*>(&v2);
+                }
             }
             if (half == 0) {
                 store_pairs<0, HALF_F / 2>(sA, row, pk);
