@@ -415,6 +415,25 @@ constexpr int WP_FIELDS = 10;
 constexpr float FIX_SCALE = 4294967296.0f;          // 2^32
 constexpr float FIX_INV = 2.3283064365386963e-10f;  // 2^-32
 
+// The float nearest (ties to even) to the fixed-point sum hi:lo times 2^-32, from 32-bit integer operations
+// and one exact 32-bit conversion: the same value as __ull2float_rn(hi:lo) * 2^-32, without the 64-bit
+// conversion, which like FP64 arithmetic runs on the narrow FP64 pipe of this part. q receives the rounded
+// sum (v * 2^32, an integer).
+__device__ __forceinline__ float fixed_to_float(uint32_t hi, uint32_t lo, unsigned long long& q) {
+    const unsigned long long x = ((unsigned long long) hi << 32) | lo;
+    const int sh = 40 - __clzll(x);  // bits below a 24-bit significand (x == 0: -24)
+    if (sh <= 0) {
+        q = x;  // below 2^24: exact
+        return __uint2float_rn(lo) * FIX_INV;
+    }
+    unsigned long long m = x >> sh;
+    const unsigned long long rem = x & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    m += (rem > half || (rem == half && (m & 1ull))) ? 1ull : 0ull;  // m <= 2^24
+    q = m << sh;
+    // m * 2^(sh - 32): the significand converts exactly and the scale is a power of two (sh in [1, 40])
+    return __uint2float_rn((uint32_t) m) * __int_as_float((95 + sh) << 23);
+}
+
 // Particle-major gather with exact, order-independent accumulation. A CTA owns a tile of TX*TY*TZ
 // nodes held as 64-bit fixed-point sums in shared memory; for every cyclic image of the tile it walks
 // the sorted particle records of the surrounding cell rows (coalesced 16-byte loads), and each thread
@@ -432,6 +451,9 @@ constexpr float FIX_INV = 2.3283064365386963e-10f;  // 2^-32
 //               the arrival order only at the 1e-16 level, below the final rounding to FP32.
 // The result is written with stride ostride.
 constexpr int ACC_EXACT = 0, ACC_FIXED_W = 1, ACC_DOUBLE = 2;
+#ifndef P2V_GATHER_LANE_WALK
+#define P2V_GATHER_LANE_WALK 0  // 1: in the exact gather each lane walks its own particle's node box
+#endif
 template<int TX, int TY, int TZ, int NT, int ACC>
 __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, const float4* __restrict__ rec_a,
     const int4* __restrict__ rec_b, const uint32_t* __restrict__ start, float* __restrict__ grid,
@@ -447,6 +469,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     uint32_t* row_beg = acc_hi + NN;                        // [rmax]
     uint32_t* row_off = row_beg + rmax;                                      // [rmax + 1]
     __shared__ double s_dsum[NT / 32];
+    __shared__ unsigned long long s_isum[NT / 32], s_fsum[NT / 32];
     __shared__ float s_fmin[NT / 32], s_fmax[NT / 32];
     __shared__ Extent s_ex;
     __shared__ uint32_t s_part[WP_FIELDS][NT];
@@ -599,8 +622,46 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                     wp.iby = 1.0f / (float) bw[1];
                                     if (WEIGHTED)
                                         wp.w = wts ? __ldg(wts + (size_t) j * wstride) : 1.0f;
+#if P2V_GATHER_LANE_WALK
+                                    // each lane walks its own particle's box: rows in support, then x
+                                    if (ACC == ACC_EXACT) {
+                                        for (int zl = 0; zl < bw[2]; ++zl) {
+                                            const float dz = g.hhi[2] * (static_cast<float>(zl) + wp.d0[2]);
+                                            for (int yl = 0; yl < bw[1]; ++yl) {
+                                                const float dy = g.hhi[1] * (static_cast<float>(yl) + wp.d0[1]);
+                                                const float dyz = __fmaf_rn(dy, dy, dz * dz);
+                                                if (!(dyz < wp.eps2))
+                                                    continue;
+                                                const int row = wp.node0 + (zl * TY + yl) * TX;
+                                                for (int xl = 0; xl < bw[0]; ++xl) {
+                                                    const float dx = g.hhi[0] * (static_cast<float>(xl) + wp.d0[0]);
+                                                    const float d2 = __fmaf_rn(dx, dx, dyz);
+                                                    if (!(d2 < wp.eps2))
+                                                        continue;
+                                                    float v;
+                                                    if (bump) {
+                                                        const float w = __fmaf_rn(-d2, wp.inv, 1.0f);
+                                                        v = w > 0.0f ? __expf(-__fdividef(1.0f, w)) : 0.0f;
+                                                    } else {
+                                                        v = fmaxf(__expf(-d2 * wp.inv) - E45, 0.0f);
+                                                    }
+                                                    const uint32_t q = __float2uint_rn(v * FIX_SCALE);
+                                                    if (q != 0u) {
+                                                        const uint32_t old = atomicAdd(acc_lo + row + xl, q);
+                                                        if (old + q < old)
+                                                            atomicAdd(acc_hi + row + xl, 1u);
+                                                    }
+                                                }
+                                            }
+                                        }
+                                    }
+#endif
                                 }
                             }
+#if P2V_GATHER_LANE_WALK
+                            if (ACC == ACC_EXACT)
+                                continue;
+#endif
                             // exclusive prefix of the row counts over the warp
                             uint32_t incl = nb;
 #pragma unroll
@@ -695,28 +756,45 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     __syncthreads();
 
     // ---- write the tile (x fastest, coalesced) and its statistics ----
+    // The density's tile sum is exact in integers: every output value is a multiple of 2^-32, and the
+    // integer and fractional parts of the rounded sums are added separately (each below 2^44 for a tile), so
+    // no node pays an FP64 conversion and add (the FP64 pipe of this part is 1/64 of the FP32 rate).
     double dsum = 0.0;
+    unsigned long long isum = 0ull, fsum = 0ull;
     float vmin = INFINITY, vmax = -INFINITY;
     for (int n = t; n < NN; n += NT) {
         const int x = n % TX, y = (n / TX) % TY, z = n / (TX * TY);
         if (x0 + x < g.s[0] && y0 + y < g.s[1] && z0 + z >= g.zlo && z0 + z < g.zhi) {
-            const float v = ACC == ACC_FIXED_W ? __ll2float_rn((long long) acc64[n]) * winv
-                            : ACC == ACC_DOUBLE ? __double2float_rn(accd[n])
-                                                : __ull2float_rn(((unsigned long long) acc_hi[n] << 32) | acc_lo[n]) * FIX_INV;
+            float v;
+            if (ACC == ACC_EXACT) {
+                unsigned long long q;
+                v = fixed_to_float(acc_hi[n], acc_lo[n], q);
+                isum += q >> 32;
+                fsum += q & 0xFFFFFFFFull;
+            } else {
+                v = ACC == ACC_FIXED_W ? __ll2float_rn((long long) acc64[n]) * winv : __double2float_rn(accd[n]);
+                dsum += (double) v;
+            }
             grid[(((size_t) (z0 + z - g.zlo) * g.s[1] + (y0 + y)) * g.s[0] + (x0 + x)) * (size_t) ostride] = v;
-            dsum += (double) v;
             vmin = fminf(vmin, v);
             vmax = fmaxf(vmax, v);
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        if (ACC == ACC_EXACT) {
+            isum += __shfl_xor_sync(0xffffffffu, isum, o);
+            fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+        } else {
+            dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        }
         vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
         vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     }
     if ((t & 31) == 0) {
         s_dsum[t >> 5] = dsum;
+        s_isum[t >> 5] = isum;
+        s_fsum[t >> 5] = fsum;
         s_fmin[t >> 5] = vmin;
         s_fmax[t >> 5] = vmax;
     }
@@ -724,9 +802,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
     if (t == 0) {
         for (int w = 1; w < NT / 32; ++w) {
             dsum += s_dsum[w];
+            isum += s_isum[w];
+            fsum += s_fsum[w];
             vmin = fminf(vmin, s_fmin[w]);
             vmax = fmaxf(vmax, s_fmax[w]);
         }
+        if (ACC == ACC_EXACT)
+            dsum = (double) isum + (double) fsum * 2.3283064365386963e-10;
         TileStats ts;
         ts.sum = dsum;
         ts.vmin = vmin;
