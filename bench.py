@@ -533,8 +533,9 @@ def run_ours(args):
     counting = nb + 1 <= 64 * f.n and 4 * (nb + 1) <= 128 * 2 ** 20  # the library's counting-sort rule
     radix_passes = 0 if counting else (key_bits + 8) // 9
     stage_bytes = {
-        # read xyzr, write key + index, the radix passes (8 B in, 8 B out each), the sorted records, cell starts
-        "ms_binning": f.n * (16 + 8 + 16 * radix_passes + 32) + nb * 8,
+        # read xyzr, write the key (+ the counting sort's rank), the radix passes (8 B in, 8 B out each; the first
+        # reads no index list), the sorted records, cell starts
+        "ms_binning": f.n * (16 + (4 + 16 * radix_passes - 4 if radix_passes else 8) + 32) + nb * 8,
         "ms_density": f.n * 16 + V * 4 + nb * 4,   # sorted records once, the grid written, cell starts
         "ms_normalize": V * 8,                      # statistics read + normalised write
         # mip levels read and written, positions + normals in, AO out, the levels read once

@@ -99,7 +99,8 @@ __global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, f
         const uint64_t o = L.offset + i;
         xyzr[o] = make_float4(x, y, z, r);
         keys[o] = key;
-        idx[o] = static_cast<uint32_t>(o);
+        if (idx)
+            idx[o] = static_cast<uint32_t>(o);
     }
     // block reduction: one atomic per block and quantity
 #pragma unroll

@@ -620,7 +620,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
                 raw_off += (bytes + 15) & ~uint64_t(15);
             }
         }
-        P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), vals0.as<uint32_t>(), fs, st));
+        P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), nullptr, fs, st));
         off += L.count;
     }
     if (timed)
@@ -721,6 +721,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     sb.keys[1] = keys1.as<uint32_t>();
     sb.vals[0] = vals0.as<uint32_t>();
     sb.vals[1] = vals1.as<uint32_t>();
+    sb.implicit_vals0 = true;  // no index list was packed: the first radix pass takes the identity
     sb.hist = hist.as<uint32_t>();
     sb.status = status.as<uint32_t>();
     sb.err = &fs->error;

@@ -451,9 +451,20 @@ __device__ __forceinline__ float fixed_to_float(uint32_t hi, uint32_t lo, unsign
 //               the arrival order only at the 1e-16 level, below the final rounding to FP32.
 // The result is written with stride ostride.
 constexpr int ACC_EXACT = 0, ACC_FIXED_W = 1, ACC_DOUBLE = 2;
-#ifndef P2V_GATHER_LANE_WALK
-#define P2V_GATHER_LANE_WALK 0  // 1: in the exact gather each lane walks its own particle's node box
-#endif
+
+// Sorted position of the f-th staged record: the row r with row_off[r] <= f < row_off[r + 1] holds it.
+__device__ __forceinline__ uint32_t locate_record(const uint32_t* row_off, const uint32_t* row_beg, int nrows,
+                                                  uint32_t f) {
+    int lo = 0, hi = nrows;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (row_off[mid] <= f)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return row_beg[lo] + (f - row_off[lo]);
+}
 template<int TX, int TY, int TZ, int NT, int ACC>
 __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, const float4* __restrict__ rec_a,
     const int4* __restrict__ rec_b, const uint32_t* __restrict__ start, float* __restrict__ grid,
@@ -560,22 +571,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                         // Each warp takes 32 consecutive records; every lane derives its particle's node
                         // box, then the warp walks the concatenated boxes 32 nodes at a time (a warp-level
                         // load-balanced search), so all lanes test nodes in lockstep.
+                        // the warp's next 32 records are located and loaded one iteration ahead (their
+                        // latency overlaps the current batch's nodes)
+                        uint32_t jn = 0;
+                        float4 An = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        int4 Bn = make_int4(0, 0, 0, 0);
+                        if (warp * 32 + lane < total) {
+                            jn = locate_record(row_off, row_beg, nrows, warp * 32 + lane);
+                            An = rec_a[REC_STRIDE * (size_t) jn];
+                            Bn = rec_b[REC_STRIDE * (size_t) jn];
+                        }
                         for (uint32_t base = warp * 32; base < total; base += NT) {
                             const uint32_t f = base + lane;
                             uint32_t nb = 0;
                             WarpPart wp;
+                            const uint32_t j = jn;
+                            const float4 A = An;
+                            const int4 B = Bn;
+                            if (f + NT < total) {
+                                jn = locate_record(row_off, row_beg, nrows, f + NT);
+                                An = rec_a[REC_STRIDE * (size_t) jn];
+                                Bn = rec_b[REC_STRIDE * (size_t) jn];
+                            }
                             if (f < total) {
-                                int lo = 0, hi = nrows;  // row r with row_off[r] <= f < row_off[r+1]
-                                while (hi - lo > 1) {
-                                    const int mid = (lo + hi) >> 1;
-                                    if (row_off[mid] <= f)
-                                        lo = mid;
-                                    else
-                                        hi = mid;
-                                }
-                                const uint32_t j = row_beg[lo] + (f - row_off[lo]);
-                                const float4 A = rec_a[REC_STRIDE * (size_t) j];
-                                const int4 B = rec_b[REC_STRIDE * (size_t) j];
                                 const float phi[3] = {A.x, A.y, A.z};
                                 const int cf[3] = {B.x, B.y, B.z};
                                 const uint32_t meta = (uint32_t) B.w;
@@ -622,46 +640,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) gather_fixed_kernel(GridGeo g, 
                                     wp.iby = 1.0f / (float) bw[1];
                                     if (WEIGHTED)
                                         wp.w = wts ? __ldg(wts + (size_t) j * wstride) : 1.0f;
-#if P2V_GATHER_LANE_WALK
-                                    // each lane walks its own particle's box: rows in support, then x
-                                    if (ACC == ACC_EXACT) {
-                                        for (int zl = 0; zl < bw[2]; ++zl) {
-                                            const float dz = g.hhi[2] * (static_cast<float>(zl) + wp.d0[2]);
-                                            for (int yl = 0; yl < bw[1]; ++yl) {
-                                                const float dy = g.hhi[1] * (static_cast<float>(yl) + wp.d0[1]);
-                                                const float dyz = __fmaf_rn(dy, dy, dz * dz);
-                                                if (!(dyz < wp.eps2))
-                                                    continue;
-                                                const int row = wp.node0 + (zl * TY + yl) * TX;
-                                                for (int xl = 0; xl < bw[0]; ++xl) {
-                                                    const float dx = g.hhi[0] * (static_cast<float>(xl) + wp.d0[0]);
-                                                    const float d2 = __fmaf_rn(dx, dx, dyz);
-                                                    if (!(d2 < wp.eps2))
-                                                        continue;
-                                                    float v;
-                                                    if (bump) {
-                                                        const float w = __fmaf_rn(-d2, wp.inv, 1.0f);
-                                                        v = w > 0.0f ? __expf(-__fdividef(1.0f, w)) : 0.0f;
-                                                    } else {
-                                                        v = fmaxf(__expf(-d2 * wp.inv) - E45, 0.0f);
-                                                    }
-                                                    const uint32_t q = __float2uint_rn(v * FIX_SCALE);
-                                                    if (q != 0u) {
-                                                        const uint32_t old = atomicAdd(acc_lo + row + xl, q);
-                                                        if (old + q < old)
-                                                            atomicAdd(acc_hi + row + xl, 1u);
-                                                    }
-                                                }
-                                            }
-                                        }
-                                    }
-#endif
                                 }
                             }
-#if P2V_GATHER_LANE_WALK
-                            if (ACC == ACC_EXACT)
-                                continue;
-#endif
                             // exclusive prefix of the row counts over the warp
                             uint32_t incl = nb;
 #pragma unroll

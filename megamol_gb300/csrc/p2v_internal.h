@@ -42,6 +42,7 @@ struct SortBuffers {
     int32_t hold_tile = -1;   // test hook: this tile of the first pass never publishes its counts (-1 none)
 };
 
+// idx (optional) receives the identity order of the packed particles.
 cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,
     FrameScalars* fs, cudaStream_t st);
 size_t sort_status_words(uint32_t n);
