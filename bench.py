@@ -385,7 +385,8 @@ def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, 
     The timed steps run inside an NVTX range named `tag` (profilers can restrict themselves to it)."""
     for _ in range(warmup):
         ctx.run_frame(lists, bbox, out, stream=stream.cuda_stream)
-    stage = {"ms_binning": 0.0, "ms_density": 0.0, "ms_normalize": 0.0, "ms_ao": 0.0, "ao_fallback": 0}
+    stage = {"ms_binning": 0.0, "ms_density": 0.0, "ms_normalize": 0.0, "ms_ao": 0.0, "ao_fallback": 0,
+             "ms_ao_kernel": 0.0, "ao_fetches": 0}
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     barrier()
@@ -405,23 +406,26 @@ def time_pipeline(ctx, lists, bbox, out, steps, warmup, stream, torch, barrier, 
     if sampler:
         sampler.__exit__()
     barrier()
-    return ev0.elapsed_time(ev1) / steps, {k: v / steps for k, v in stage.items()}
+    return ev0.elapsed_time(ev1) / steps, {k: v / steps for k, v in stage.items()}  # ao_fetches: per step too
 
 
 def feature_levels(f) -> int:
     """Mip levels the learned AO's feature samples read (one texture each): the step table of the cone march
     (geometric steps from offset + 1e-4 to the cone length, lod = log2(t * w * shortest edge) clamped to
-    [0, levels - 1], w = 2 tan(apex / 2)) at the 9 feature steps, two levels where a lod is fractional."""
+    [0, levels - 1], w = 2 tan(apex / 2)) at the MLP_FSTEPS feature steps, two levels where a lod is fractional."""
     import math
+
+    from megamol_gb300 import p2v
 
     t0 = AO_PARAMS["ao_offset"] + 1e-4
     n = AO_PARAMS["ao_steps"]
     g = (AO_PARAMS["ao_cone_length"] / t0) ** (1.0 / n)
     w = 2.0 * math.tan(math.radians(AO_PARAMS["ao_apex_deg"]) / 2)
     top = AO_PARAMS["ao_levels"] - 1
+    F = p2v.MLP_FSTEPS
     need = set()
-    for j in range(9):
-        k = int(math.floor(j * (n - 1) / 8 + 0.5))
+    for j in range(F):
+        k = int(math.floor(j * (n - 1) / (F - 1) + 0.5))
         lod = min(max(math.log2(t0 * g ** k * w * min(f.res)), 0.0), top)
         need.add(int(lod))
         if lod > int(lod) and int(lod) < top:
@@ -524,6 +528,7 @@ def run_ours(args):
 
     # ---- roofline: algorithmic bytes per stage / its device time; the dominant stage's kernel ----
     peak, peak_kind = peaks()
+    tex_peaks = (p2v.measure_texture_rate(0), p2v.measure_texture_rate(1)) if use_learned else (None, None)
     nb = (f.res[0] + 2) * (f.res[1] + 2) * (f.res[2] + 2)
     dims = [list(f.res)]
     for _ in range(1, AO_PARAMS["ao_levels"]):
@@ -554,6 +559,17 @@ def run_ours(args):
     dom = max(stages, key=lambda k: stages[k]["ms"])
     prof = {"ms_binning": "binning", "ms_density": "density_gather", "ms_normalize": "normalize",
             "ms_ao": "learned_ao" if use_learned else "cone_ao"}[dom]
+    if use_learned and st.get("ms_ao_kernel", 0.0) > 0.0 and st.get("ao_fetches", 0) > 0:
+        # the inference kernel is bound by the texture units' random-access rate, not by HBM: its fetches per
+        # second against the device's measured sample rates in the same texture format (incoherent lanes: every
+        # lane its own random point, as cone samples along per-particle normals; coherent: quads of adjacent
+        # texels)
+        fetches = float(f.n) * st["ao_fetches"]
+        stages["ms_ao"]["texture"] = {
+            "kernel": "p2v::mlp_infer_tc_kernel", "ms": st["ms_ao_kernel"], "fetches_per_particle": st["ao_fetches"],
+            "achieved_gsamples": fetches / (st["ms_ao_kernel"] * 1e-3) / 1e9,
+            "peak_incoherent_gsamples": tex_peaks[1], "peak_coherent_gsamples": tex_peaks[0],
+            "frac_of_incoherent": fetches / (st["ms_ao_kernel"] * 1e-3) / 1e9 / tex_peaks[1] if tex_peaks[1] else None}
     roofline = {"bound": "hbm", "kernel": stages[dom]["kernel"], "achieved": stages[dom]["achieved_gbs"],
                 "peak": peak, "unit": "GB/s", "frac": stages[dom]["frac"], "peak_kind": peak_kind,
                 "traffic": profile_traffic(f"{prof}_{args.workload}.md"),

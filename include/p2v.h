@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define P2V_ABI_VERSION 9
+#define P2V_ABI_VERSION 10
 
 #if defined(__GNUC__)
 #define P2V_API __attribute__((visibility("default")))
@@ -252,6 +252,9 @@ typedef struct p2v_stats {
     uint32_t ao_fallback;        /* learned AO: particles that fell back to the cone march */
     uint32_t cell_max_count;     /* binning: particles in the fullest cell when the counting sort by cell was
                                     tried (it takes frames whose cells hold at most 32), 0 = radix sort only */
+    uint32_t ao_fetches;         /* learned AO: texture fetches per particle of its inference kernel (0 otherwise) */
+    double ms_ao_kernel;         /* CUDA events around the AO stage's main kernel alone (the learned AO's inference
+                                    or the plain cone march; 0 for other AO modes or untimed frames) */
 } p2v_stats;
 
 /* Learned AO (no counterpart in the reference: its AO is the GLSL cone march). Features per particle: the

@@ -58,7 +58,7 @@ struct DevBuf {
     }
 };
 
-enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_COUNT };
+enum Ev { EV_START, EV_UPLOAD, EV_BIN, EV_DENSITY, EV_NORM, EV_AO, EV_DOWN, EV_AOK0, EV_AOK1, EV_COUNT };
 // fork/join events of a pipe's side stream: the normals upload runs under binning and density, the grid
 // download under AO
 enum SideEv { SEV_FORK, SEV_NRM, SEV_GRID, SEV_JOIN, SEV_COUNT };
@@ -75,6 +75,9 @@ struct Pipe {
     DevBuf xyzr_s, nrm_s;                  // positions and normals in sorted order (the cone AO stages)
     DevBuf bk0, bk1, xyzr_b, nrm_b, ord_b;  // the AO stages' brick order (ao_brick_order)
     bool xyzr_sorted = false;              // the binning of this frame wrote xyzr_s
+    bool timing = false;                   // this frame records stage events
+    bool aok = false;                      // EV_AOK0 / EV_AOK1 bracket this frame's main AO kernel
+    uint32_t ao_fetches = 0;               // texture fetches per particle of the learned AO's inference
     FeatureTex ftex[MAX_LEVELS];           // the learned AO's feature levels as paired-slice textures
     cudaEvent_t ev[EV_COUNT] = {};
     cudaEvent_t sev[SEV_COUNT] = {};
@@ -177,6 +180,8 @@ struct FrameJob {
     VectorGridGeo vg_geo{};
     FrameScalars* h_out = nullptr;  // pinned slot that receives the frame's scalars
     bool timed = false;             // stage events were recorded
+    bool aok = false;               // the main AO kernel was bracketed by events
+    uint32_t ao_fetches = 0;
 };
 
 __global__ void init_scalars_kernel(FrameScalars* fs) {
@@ -833,6 +838,9 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
         }
         P2V_CUDA_TRY(cudaEventRecord(pp.sev[SEV_JOIN], side));
         P2V_CUDA_TRY(cudaStreamWaitEvent(st, pp.sev[SEV_NRM], 0));
+        pp.timing = timed && !slot;
+        pp.aok = false;
+        pp.ao_fetches = 0;
         const p2v_status as = run_ao(pp, fr, g, dgrid, bb, n, sb.vals[sb.result], st, slot);
         if (as != P2V_OK) {
             cudaStreamWaitEvent(st, pp.sev[SEV_JOIN], 0);  // no side work left outside st (graph capture)
@@ -883,6 +891,8 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     job.vg_geo.normalize = P.normalize ? 1 : 0;
     job.h_out = h_out;
     job.timed = timed;
+    job.aok = want_ao && pp.aok;
+    job.ao_fetches = want_ao ? pp.ao_fetches : 0u;
     return P2V_OK;
 }
 
@@ -943,7 +953,10 @@ p2v_status p2v_ctx::finish_frame(Pipe& pp, const FrameJob& job, p2v_volume* vol,
     stats.ms_download = ms;
     cudaEventElapsedTime(&ms, ev[EV_START], ev[EV_DOWN]);
     stats.ms_total = ms;
+    if (job.aok && cudaEventElapsedTime(&ms, ev[EV_AOK0], ev[EV_AOK1]) == cudaSuccess)
+        stats.ms_ao_kernel = ms;
     }
+    stats.ao_fetches = job.ao_fetches;
     stats.device_error = hs.error;
     stats.ao_fallback = hs.ao_fallback;
     stats.cell_max_count = hs.bin_maxcount;
@@ -1264,10 +1277,16 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
         }
         P2V_CUDA_TRY(to_sorted());
         P2V_CUDA_TRY(ao_inputs());
+        if (pp.timing)
+            P2V_CUDA_TRY(cudaEventRecord(pp.ev[EV_AOK0], st));
         if (P.ao_march == P2V_AO_MARCH_WARP)
             P2V_CUDA_TRY(launch_cone_ao_warp(cp, axyzr, anrm, n, aorder, ao.as<float>(), sms, st));
         else
             P2V_CUDA_TRY(launch_cone_ao(cp, nullptr, axyzr, anrm, n, nullptr, aorder, ao.as<float>(), st));
+        if (pp.timing) {
+            P2V_CUDA_TRY(cudaEventRecord(pp.ev[EV_AOK1], st));
+            pp.aok = true;
+        }
         return P2V_OK;
     }
     if (P.ao_mode == P2V_AO_LEARNED) {
@@ -1303,7 +1322,20 @@ p2v_status p2v_ctx::run_ao(Pipe& pp, const p2v_frame* fr, const GridGeo& g, cons
             return fail(P2V_EINVAL, "mma_wait_polls must be >= 0");
         a.wait_polls = (uint32_t) P.mma_wait_polls;
         a.hold_mma = P.test_hold_mma ? 1 : 0;
+        // texture fetches per particle: one per feature sample, two where the sample's lod lies between levels
+        pp.ao_fetches = 0;
+        for (int j = 0; j < MLP_FSTEPS; ++j) {
+            const float lod = cp.lod[cp.fstep[j]];
+            const int l0 = std::min((int) lod, cp.nlevels - 1);
+            pp.ao_fetches += (uint32_t) MLP_CONES * ((lod - (float) l0 > 0.0f && l0 + 1 < cp.nlevels) ? 2u : 1u);
+        }
+        if (pp.timing)
+            P2V_CUDA_TRY(cudaEventRecord(pp.ev[EV_AOK0], st));
         P2V_CUDA_TRY(launch_mlp_infer(a, cp, false, sms, st));
+        if (pp.timing) {
+            P2V_CUDA_TRY(cudaEventRecord(pp.ev[EV_AOK1], st));
+            pp.aok = true;
+        }
         // the plain cone march for every particle whose features left the training range
         P2V_CUDA_TRY(launch_cone_ao(cp, fb_list.as<uint32_t>(), axyzr, anrm, n, &fs->ao_fallback, aorder,
                                     ao.as<float>(), st));

@@ -122,7 +122,8 @@ class StatsC(C.Structure):
                 ("mass_sum", C.c_double), ("ms_upload", C.c_double), ("ms_binning", C.c_double),
                 ("ms_density", C.c_double), ("ms_normalize", C.c_double), ("ms_ao", C.c_double),
                 ("ms_download", C.c_double), ("ms_total", C.c_double), ("device_error", C.c_uint32),
-                ("ao_fallback", C.c_uint32), ("cell_max_count", C.c_uint32)]
+                ("ao_fallback", C.c_uint32), ("cell_max_count", C.c_uint32), ("ao_fetches", C.c_uint32),
+                ("ms_ao_kernel", C.c_double)]
 
 
 class TrainParams(C.Structure):
@@ -181,6 +182,8 @@ _SIGNATURES = {
     "p2v_mlp_infer": ([C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int),
     "p2v_aosphere_ao_noalloc": ([C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_int32),
                                  C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+    # include/p2v_measure.h
+    "p2v_measure_texture_rate": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
 }
 
 _lib: Optional[C.CDLL] = None
@@ -200,6 +203,16 @@ def library(path: str = LIB_PATH) -> C.CDLL:
             f.restype = res
         _lib = lib
     return _lib
+
+
+def measure_texture_rate(pattern: int) -> float:
+    """G texture samples/s of the current device in the learned AO's feature format: pattern 0 = coherent quads,
+    1 = every lane its own random point (p2v_measure_texture_rate)."""
+    v = C.c_double(0.0)
+    st = library().p2v_measure_texture_rate(int(pattern), C.byref(v))
+    if st != OK:
+        raise P2VError(st, "p2v_measure_texture_rate failed")
+    return float(v.value)
 
 
 def default_params() -> Params:

@@ -26,7 +26,8 @@ int main(void) {
     F(p2v_particle_list, count); F(p2v_particle_list, mem); F(p2v_particle_list, ao_out);
     F(p2v_frame, frame_id); F(p2v_frame, lists);
     F(p2v_volume, resolution); F(p2v_volume, min_value); F(p2v_volume, data_hash);
-    F(p2v_stats, mass_sum); F(p2v_stats, ms_total); F(p2v_stats, ao_fallback); F(p2v_stats, cell_max_count);
+    F(p2v_stats, mass_sum); F(p2v_stats, ms_total); F(p2v_stats, ao_fallback); F(p2v_stats, cell_max_count); F(p2v_stats, ao_fetches);
+    F(p2v_stats, ms_ao_kernel);
     printf("\"end\": 0}\n");
     return 0;
 }

@@ -77,7 +77,7 @@ def test_params_default_mirror_reference_slots(lib):
     assert p.batch_persistent == -1 and p.queue_wait_polls == 0 and p.test_hold_queue == 0
     assert p.sort_wait_polls == 0 and p.test_hold_sort == 0 and p.ao_march == p2v.AO_MARCH_THREAD
     assert p.ao_brick_order == 0
-    assert lib.p2v_abi_version() == 9
+    assert lib.p2v_abi_version() == 10
 
 
 def test_create_without_device_fails_cleanly(lib):

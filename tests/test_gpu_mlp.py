@@ -263,3 +263,21 @@ def test_learned_ao_with_gradient_normals(ctx, trained):
     assert np.array_equal(b, c)
     d = np.abs(a.astype(np.float64) - b)
     assert np.sqrt(np.mean(d ** 2)) <= 2e-3 and d.max() <= 0.1, (np.sqrt(np.mean(d ** 2)), d.max())
+
+
+def test_ao_kernel_timing_and_texture_rates(ctx, trained):
+    """The frame statistics bracket the AO stage's main kernel alone (the inference, or the plain march) and
+    count the inference's texture fetches per particle; the texture-rate probe the benchmark divides by
+    reports the units' coherent rate above their incoherent one."""
+    f = synth.lj_liquid(cells=32, res=80, seed=43)
+    nrm = with_normals(ctx, f)
+    ao_of(ctx, f, nrm, p2v.AO_LEARNED)
+    st = ctx.stats()
+    per_sample = st["ao_fetches"] / p2v.MLP_CONES
+    assert st["ao_fetches"] % p2v.MLP_CONES == 0 and p2v.MLP_FSTEPS <= per_sample <= 2 * p2v.MLP_FSTEPS, st
+    assert 0.0 < st["ms_ao_kernel"] <= st["ms_ao"], st
+    ao_of(ctx, f, nrm, p2v.AO_CONE)
+    st = ctx.stats()
+    assert st["ao_fetches"] == 0 and 0.0 < st["ms_ao_kernel"] <= st["ms_ao"], st
+    coherent, incoherent = p2v.measure_texture_rate(0), p2v.measure_texture_rate(1)
+    assert coherent > incoherent > 0.0, (coherent, incoherent)
