@@ -55,11 +55,33 @@ __device__ __forceinline__ uint32_t lane_id() {
     return threadIdx.x & 31u;
 }
 
+// True when the particle's kernel support holds no grid node along some axis, by a margin that the density
+// gather's own node ranges cannot contradict: the gather would add nothing for it. q: the particle's position
+// in cells, (p - min) / h as the bin key takes it. In node units the nodes around the particle lie at in-cell
+// offsets 0 and 1 from its offset phi = q - floor(q); neither is inside the support when phi and 1 - phi both
+// exceed eps / h by 1e-3 plus the rounding of q and of a position the gather forms from a cell up to twice the
+// grid size away (the gather's exactly rounded in-cell offset differs from phi by less than that).
+__device__ __forceinline__ bool support_misses_nodes(const float q[3], float r, const GridGeo& g) {
+    const float eps = g.kernel == 0 ? g.sigma * r : 3.0f * (g.sigma * r);
+    bool miss = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float phi = q[a] - floorf(q[a]);
+        const float eh = eps * g.ihh[a];
+        const float m = 1e-3f + 1e-6f * static_cast<float>(g.s[a]) + 4e-7f * fabsf(q[a]);
+        miss = miss || (phi - eh > m && (1.0f - phi) - eh > m);
+    }
+    return miss;
+}
+
 // Grid-stride over the list: each thread packs several particles and keeps running reductions, so the
-// frame-wide maxima and counts cost one atomic per block rather than per 256 particles.
+// frame-wide maxima and counts cost one atomic per block rather than per 256 particles. empty_flag (a power of
+// two above every cell key, or 0): added to the key of a particle whose support holds no node, so that the
+// sort puts those particles after every other (in cell order) and the cell start table, which the density
+// gather walks, leaves them out.
 template<class T, int NC, bool ALIGNED>
 __global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, float4* __restrict__ xyzr,
-    uint32_t* __restrict__ keys, uint32_t* __restrict__ idx, FrameScalars* __restrict__ fs) {
+    uint32_t* __restrict__ keys, uint32_t* __restrict__ idx, FrameScalars* __restrict__ fs, uint32_t empty_flag) {
     __shared__ int32_t s_cmin[3][8], s_cmax[3][8];
     __shared__ uint32_t s_rmax[8], s_drop[8];
     int32_t cell[3] = {INT32_MAX, INT32_MAX, INT32_MAX};
@@ -76,9 +98,11 @@ __global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, f
         bool valid = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(r) && r > 0.0f;
         uint32_t bin[3];
         int32_t c[3];
+        float qa[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const float q = (p[a] - g.minf[a]) / g.hf[a];
+            qa[a] = q;
             valid = valid && fabsf(q) < 1073741824.0f;
             c[a] = clamp_cell(q);
             const int32_t b = c[a] < -1 ? -1 : (c[a] > g.s[a] ? g.s[a] : c[a]);
@@ -93,6 +117,8 @@ __global__ void __launch_bounds__(256) pack_keys_kernel(ListDesc L, GridGeo g, f
                 cellhi[a] = max(cellhi[a], c[a]);
             }
             rbits = max(rbits, __float_as_uint(r));
+            if (empty_flag && support_misses_nodes(qa, r, g))
+                key |= empty_flag;
         } else {
             ++drop;
         }
@@ -532,6 +558,74 @@ __global__ void __launch_bounds__(256) boundary_starts_kernel(const uint32_t* __
     }
 }
 
+// The dense table (G = 1) with coalesced stores: a warp takes 32 consecutive boundaries, scans the lengths of
+// their runs of up to RUN cells, and its lanes then write the cells of all 32 runs together (consecutive lanes,
+// consecutive cells; each lane finds the boundary owning its cell by a binary search over the scanned lengths).
+// Longer runs go to the gap list as in boundary_starts_kernel. Per-thread run loops stored one scattered
+// sector per cell and lane; the cells a boundary owns get longer when particles whose support holds no node
+// are sorted behind the others.
+__global__ void __launch_bounds__(256) boundary_starts_dense_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+    uint32_t nbins, uint32_t* __restrict__ out, uint4* __restrict__ gaps, uint32_t gap_cap,
+    FrameScalars* __restrict__ fs, const FrameScalars* __restrict__ gate) {
+    constexpr uint32_t RUN = 64u;
+    if (radix_skipped(gate))
+        return;
+    const uint32_t lane = lane_id();
+    const uint64_t wstride = (uint64_t) gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t) blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base <= n; base += wstride) {
+        const uint64_t i64 = base + lane;
+        uint32_t lo = 1u, hi = 0u;  // empty run
+        if (i64 <= n) {
+            const uint32_t i = (uint32_t) i64;
+            lo = i == 0 ? 0u : keys[i - 1] + 1u;
+            hi = i == n ? nbins : keys[i];
+            if (hi > nbins)
+                hi = nbins;
+        }
+        uint32_t len = lo <= hi ? hi - lo + 1u : 0u;
+        if (len > RUN) {
+            const uint32_t i = (uint32_t) i64;
+            const uint32_t nch = (uint32_t) (((uint64_t) len - 1 + GAP_CHUNK) / GAP_CHUNK);
+            const uint32_t slot = atomicAdd(&fs->ngaps, nch);
+            for (uint32_t q = 0; q < nch; ++q) {
+                const uint64_t c0 = (uint64_t) lo + (uint64_t) q * GAP_CHUNK;
+                const uint64_t c1 = std::min<uint64_t>(hi, c0 + GAP_CHUNK - 1);
+                if ((uint64_t) slot + q < gap_cap)
+                    gaps[slot + q] = make_uint4((uint32_t) c0, (uint32_t) c1, i, 0u);
+                else
+                    atomicOr(&fs->error, ERR_GAP_OVERFLOW);
+            }
+            len = 0u;
+        }
+        uint32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t) o)
+                incl += t;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t pre = incl - len;  // first cell slot of this lane's run
+        for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            // owner: the last lane whose run starts at or before slot j (lanes with empty runs share the next
+            // lane's start and are passed over: the search ends on the last of equal starts)
+            uint32_t ow = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const uint32_t cand = ow + step;
+                const uint32_t pc = __shfl_sync(0xffffffffu, pre, cand);
+                if (pc <= j)
+                    ow = cand;
+            }
+            const uint32_t olo = __shfl_sync(0xffffffffu, lo, ow);
+            const uint32_t opre = __shfl_sync(0xffffffffu, pre, ow);
+            if (j < total)
+                out[olo + (j - opre)] = (uint32_t) (base + ow);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) cell_starts_kernel(const uint32_t* __restrict__ keys, uint32_t n,
     uint32_t nbins, const uint32_t* __restrict__ bstart, uint32_t nblk, uint32_t* __restrict__ start,
     const FrameScalars* __restrict__ gate) {
@@ -815,7 +909,7 @@ __global__ void count_valid_kernel(const uint32_t* __restrict__ start, uint32_t 
 // host launchers
 // ---------------------------------------------------------------------------------------------
 cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,
-    FrameScalars* fs, cudaStream_t st) {
+    FrameScalars* fs, uint32_t empty_flag, cudaStream_t st) {
     if (L.count == 0)
         return cudaSuccess;
     const dim3 block(256);
@@ -826,30 +920,30 @@ cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, 
     case 1: {  // FLOAT_XYZ
         bool al = (addr % 4 == 0) && (L.stride % 4 == 0);
         if (al)
-            pack_keys_kernel<float, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<float, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
         else
-            pack_keys_kernel<float, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<float, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
     } break;
     case 2: {  // FLOAT_XYZR
         bool al = (addr % 4 == 0) && (L.stride % 4 == 0);
         if (al)
-            pack_keys_kernel<float, 4, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<float, 4, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
         else
-            pack_keys_kernel<float, 4, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<float, 4, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
     } break;
     case 3: {  // SHORT_XYZ
         bool al = (addr % 2 == 0) && (L.stride % 2 == 0);
         if (al)
-            pack_keys_kernel<uint16_t, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<uint16_t, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
         else
-            pack_keys_kernel<uint16_t, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<uint16_t, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
     } break;
     case 4: {  // DOUBLE_XYZ
         bool al = (addr % 8 == 0) && (L.stride % 8 == 0);
         if (al)
-            pack_keys_kernel<double, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<double, 3, true><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
         else
-            pack_keys_kernel<double, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs);
+            pack_keys_kernel<double, 3, false><<<grid, block, 0, st>>>(L, g, xyzr, keys, idx, fs, empty_flag);
     } break;
     default:
         return cudaErrorInvalidValue;
@@ -867,6 +961,16 @@ size_t sort_hist_words() {
 
 int sort_passes(uint32_t max_key) {
     return sort_plan(max_key).passes;
+}
+
+uint32_t sort_empty_flag(uint32_t max_key) {
+    int nb = 0;
+    while (nb < 32 && (max_key >> nb) != 0u)
+        ++nb;
+    if (nb >= 31)
+        return 0u;
+    const uint32_t flag = 1u << nb;
+    return sort_plan(flag | (flag - 1u)).passes == sort_plan(max_key).passes ? flag : 0u;
 }
 
 template<bool GATHER, int BITS>
@@ -970,13 +1074,14 @@ cudaError_t launch_bin_sort(SortBuffers& b, uint32_t n, const GridGeo& g, uint32
     // the radix path: alone, or as the fallback (gated) when a cell holds more than BIN_CELL_MAX particles;
     // with the counting sort its pass count is odd so both leave the sorted keys in buffer 1
     const FrameScalars* gate = counting ? fs : nullptr;
-    if ((e = launch_sort(b, n, g.nbins, sms, st, gate, counting)) != cudaSuccess)
+    const uint32_t max_key = b.empty_flag ? (b.empty_flag | (b.empty_flag - 1u)) : g.nbins;
+    if ((e = launch_sort(b, n, max_key, sms, st, gate, counting)) != cudaSuccess)
         return e;
     const unsigned grid = (unsigned) std::max<uint32_t>(1u, std::min<uint32_t>(ceil_div(n + 1, 256), sms * 8));
     if (n > 0)
         sort_sanitize_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], b.vals[b.result], n, g.nbins, b.err, gate);
     if ((uint64_t) g.nbins < 8ull * n) {
-        boundary_starts_kernel<1><<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, start, gaps, gap_cap, fs, gate);
+        boundary_starts_dense_kernel<<<grid, 256, 0, st>>>(b.keys[b.result], n, g.nbins, start, gaps, gap_cap, fs, gate);
         cell_gap_fill_kernel<<<sms * 2, 256, 0, st>>>(gaps, gap_cap, start, fs, gate);
     } else {
         const uint32_t nblk = cell_block_count(g.nbins);

@@ -536,6 +536,10 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
                           4ull * ((uint64_t) g.nbins + 1) <= COUNTING_TABLE_MAX_BYTES;
     if (counting)
         P2V_CUDA_TRY(pp.bcount.ensure(4 * ((size_t) g.nbins + 1)));
+    // the radix path sorts particles whose support holds no node after all others (a key bit above the cells),
+    // so the density gather never visits them; the AO stages' brick order reads the cell table for every
+    // particle and keeps plain cell keys
+    const uint32_t empty_flag = (!counting && P.ao_brick_order == 0) ? sort_empty_flag(g.nbins) : 0u;
     P2V_CUDA_TRY(status.ensure(4 * (std::max(sort_status_words(n), bin_scan_words(g.nbins)) + 256)));
     P2V_CUDA_TRY(hist.ensure(4 * sort_hist_words()));
     P2V_CUDA_TRY(cstart.ensure(4 * ((size_t) g.nbins + 1)));
@@ -625,7 +629,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
                 raw_off += (bytes + 15) & ~uint64_t(15);
             }
         }
-        P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), nullptr, fs, st));
+        P2V_CUDA_TRY(launch_pack_keys(d, g, xyzr.as<float4>(), keys0.as<uint32_t>(), nullptr, fs, empty_flag, st));
         off += L.count;
     }
     if (timed)
@@ -727,6 +731,7 @@ p2v_status p2v_ctx::enqueue_frame(Pipe& pp, const p2v_frame* fr, p2v_volume* vol
     sb.vals[0] = vals0.as<uint32_t>();
     sb.vals[1] = vals1.as<uint32_t>();
     sb.implicit_vals0 = true;  // no index list was packed: the first radix pass takes the identity
+    sb.empty_flag = empty_flag;
     sb.hist = hist.as<uint32_t>();
     sb.status = status.as<uint32_t>();
     sb.err = &fs->error;

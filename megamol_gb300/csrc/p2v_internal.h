@@ -38,13 +38,18 @@ struct SortBuffers {
     int result;            // index of the buffers holding the sorted output
     bool implicit_vals0;   // vals[0] holds no input values: the first pass takes the identity (indices)
     bool first_pass;       // set by launch_sort for its own bookkeeping
+    uint32_t empty_flag = 0;  // key bit of the particles whose support holds no node (radix path), 0 = none
     uint32_t wait_polls = 0;  // polls of a look-back wait before the sort gives up (0: SPIN_LIMIT)
     int32_t hold_tile = -1;   // test hook: this tile of the first pass never publishes its counts (-1 none)
 };
 
-// idx (optional) receives the identity order of the packed particles.
+// idx (optional) receives the identity order of the packed particles. empty_flag: 0, or the bit that
+// sort_empty_flag returns, added to the keys of particles whose support holds no grid node.
 cudaError_t launch_pack_keys(const ListDesc& L, const GridGeo& g, float4* xyzr, uint32_t* keys, uint32_t* idx,
-    FrameScalars* fs, cudaStream_t st);
+    FrameScalars* fs, uint32_t empty_flag, cudaStream_t st);
+// The power of two above every cell key (max_key) that marks particles whose support holds no node, or 0 when
+// the extra key bit would cost the radix sort a pass.
+uint32_t sort_empty_flag(uint32_t max_key);
 size_t sort_status_words(uint32_t n);
 size_t sort_hist_words();
 int sort_passes(uint32_t max_key);

@@ -689,6 +689,25 @@ def bin_keys(xyzr, bbox, res) -> tuple[np.ndarray, int]:
     return keys, nbins
 
 
+def support_misses_nodes_f64(xyzr, bbox, res, sigma=1.0, kernel=0) -> np.ndarray:
+    """Particles whose kernel support (radius sigma r, bump, or 3 sigma r, Gaussian) holds no grid node along
+    some axis, in FP64 without margin: nodes at bbox min + k h, h = |max - min| / (res - 1). The library's
+    radix binning sorts such particles after all others (it flags them with a margin, so every particle it
+    flags is one of these)."""
+    x = np.asarray(xyzr, np.float64).reshape(-1, 4)
+    eps = (1.0 if kernel == 0 else 3.0) * sigma * x[:, 3]
+    miss = np.zeros(x.shape[0], bool)
+    with np.errstate(invalid="ignore"):
+        for a in range(3):
+            lo, hi = float(bbox[a]), float(bbox[a + 3])
+            h = abs(hi - lo) / (res[a] - 1)
+            q = (x[:, a] - lo) / h
+            phi = q - np.floor(q)
+            eh = eps / h
+            miss |= (phi > eh) & (1.0 - phi > eh)
+    return miss
+
+
 def binning(xyzr, bbox, res):
     """Stable sort of the bin keys (np.argsort kind="stable"): (sorted keys, permutation, cell starts of the
     nbins + 1 bins)."""

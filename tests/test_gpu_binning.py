@@ -27,6 +27,21 @@ def check(ctx, xyzr, bbox, res, lists=None):
     ctx.run_frame(lists or [p2v.ParticleList(xyzr, p2v.VERTDATA_FLOAT_XYZR)], bbox, None)
     keys, order, start = ctx.binning()
     rk, ro, rs = oracle.binning(xyzr, bbox, res)
+    nbins = rs.size - 1
+    if keys.size and keys.max() > nbins:
+        # the radix path sorts the particles whose support holds no node after all others, by a key bit above
+        # the cells: each of them must miss every node (FP64), and the order must be the stable sort by
+        # (that bit, cell)
+        flag = 1 << int(nbins).bit_length()
+        n = keys.size
+        pf = np.zeros(n, bool)
+        pf[order[keys > nbins]] = True
+        assert np.all(oracle.support_misses_nodes_f64(xyzr, bbox, res)[pf])
+        ck = np.empty(n, np.uint32)
+        ck[ro] = rk
+        ro = np.lexsort((np.arange(n), ck, pf)).astype(np.uint32)
+        rk = (ck[ro] | np.where(pf[ro], flag, 0)).astype(np.uint32)
+        rs = np.searchsorted(rk, np.arange(nbins + 1, dtype=np.int64), side="left").astype(np.uint32)
     assert np.array_equal(keys, rk)
     assert np.array_equal(order, ro)
     assert np.array_equal(start, rs)

@@ -199,3 +199,38 @@ def test_lj_liquid_full_size(ctx, seed, accumulate):
     assert err <= 1e-6, err
     st = ctx.stats()
     assert st["particles_binned"] == f.n and st["device_error"] == 0
+
+
+@pytest.mark.parametrize("cyclic", [(1, 1, 1), (0, 0, 0)])
+def test_particles_whose_support_misses_every_node(ctx, cyclic):
+    """A frame of flat voxels (3.1 units in z against radii of 0.3-0.9, as in the mixed-phase frame) on the
+    radix path (86 cells per particle): the binning sorts the particles whose support holds no node after all
+    others and the gather never visits them. The grid is bit-identical to the one of plain cell keys (the AO
+    brick order keeps them) and matches the FP64 oracle."""
+    rng = np.random.default_rng(77)
+    n = 40_000
+    x = np.empty((n, 4), np.float32)
+    x[:, :2] = rng.uniform(0, 40, (n, 2))
+    x[:, 2] = rng.uniform(0, 400, n)
+    x[:, 3] = rng.uniform(0.3, 0.9, n)
+    bbox, res = (0.0, 0.0, 0.0, 40.0, 40.0, 400.0), (160, 160, 129)
+    L = [p2v.ParticleList(x, p2v.VERTDATA_FLOAT_XYZR)]
+    ctx.set_params(ao_brick_order=0)
+    flagged, _ = run(ctx, L, bbox, res, cyclic=cyclic)
+    flagged = flagged.copy()
+    keys, order, start = ctx.binning()
+    nbins = start.size - 1
+    assert ctx.stats()["cell_max_count"] == 0  # the radix path
+    miss = oracle.support_misses_nodes_f64(x, bbox, res)
+    pf = np.zeros(n, bool)
+    pf[order[keys > nbins]] = True
+    assert pf.sum() > 0.3 * n and np.all(miss[pf]), (pf.sum(), miss.sum())
+    ctx.set_params(ao_brick_order=1)
+    try:
+        plain, _ = run(ctx, L, bbox, res, cyclic=cyclic)
+        assert ctx.binning()[0].max() <= nbins
+    finally:
+        ctx.set_params(ao_brick_order=0)
+    assert np.array_equal(flagged.view(np.uint32), plain.view(np.uint32))
+    v64 = oracle.density_f64(x, bbox, res, cyclic, 1.0, oracle.BUMP, NT)
+    assert maxrel(flagged, v64) <= 1e-6
