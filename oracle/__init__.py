@@ -130,7 +130,7 @@ def density_f32(xyzr, bbox, res, cyclic=(1, 1, 1), sigma=1.0, kernel=BUMP, nthre
 
 
 def density_f64(xyzr, bbox, res, cyclic=(1, 1, 1), sigma=1.0, kernel=BUMP, nthreads=1) -> np.ndarray:
-    """FP64 restatement (the error judge); raw sums, shape (z, y, x)."""
+    """FP64 restatement (the error reference); raw sums, shape (z, y, x)."""
     a = _xyzr(xyzr)
     out = np.zeros((res[2], res[1], res[0]), np.float64)
     g = _grid(bbox, res, cyclic, sigma)
@@ -567,7 +567,7 @@ def mip_levels_f32(l0: np.ndarray, nlevels: int, sat_scale: float = 0.0, nthread
 
 def cone_ao_f32(levels, dirs, xyzr, normals, bounds_min, bounds_size, nthreads: int = 1, **kw) -> np.ndarray:
     """Cone-marched AO per particle in FP32 with OpenMP, the GPU kernel's operation order (the CPU baseline's
-    timing stand-in; the error judge is cone_ao_f64). `levels` as mip_levels_f32 returns them."""
+    timing stand-in; the error reference is cone_ao_f64). `levels` as mip_levels_f32 returns them."""
     lv = [np.ascontiguousarray(L, np.float32) for L in levels]
     ptrs = (C.c_void_p * len(lv))(*[L.ctypes.data for L in lv])
     dims = (C.c_int32 * (3 * len(lv)))(*[d for L in lv for d in (L.shape[2], L.shape[1], L.shape[0])])

@@ -496,7 +496,7 @@ extern "C" void p2vo_cone_ao_f64(const double* const* levels, const int32_t* ldi
  * FP32 cone pipeline (the CPU baseline's timing stand-in for the GLSL march, OpenMP): the MDAO pyramid
  * of a float volume (level 1 built from the saturated texels clamp(v * scale, 0, 1)) and the march in
  * FP32 with the GPU kernel's operation order (fused multiply-adds where it fuses, level 0 saturated on
- * the fly). The error judge stays the FP64 march above.
+ * the fly). The error reference stays the FP64 march above.
  * ---------------------------------------------------------------------------------------------- */
 extern "C" void p2vo_mip_levels_f32(const float* l0, const int32_t d0[3], float sat_scale, int nlevels,
                                     float* const* out, int nthreads) {

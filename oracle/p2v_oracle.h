@@ -45,7 +45,7 @@ int p2vo_density_f32(const float* xyzr, int64_t n, const p2vo_grid* g, int kerne
 
 /* FP64 restatement: the reference's integer decisions (cell, footprint, wrap) made with its float
  * expressions, every value (node positions, distances, kernel) evaluated in double with the exact
- * grid spacing (right-left)/(res-1). The GPU path is judged against this. */
+ * grid spacing (right-left)/(res-1). The GPU path's error is measured against this. */
 int p2vo_density_f64(const float* xyzr, int64_t n, const p2vo_grid* g, int kernel, int nthreads, double* out);
 
 /* Weighted createVolumeCPU: nc weights per particle (w[j * nc + c]); out holds nc interleaved components.

@@ -100,7 +100,7 @@ def test_training_converges(trained):
 
 
 def test_learned_ao_matches_cone_march_and_is_faster(ctx, trained):
-    """On a frame the network never saw: AO RMSE <= 0.02 against the plain cone march (the benchmark spec's bar),
+    """On a frame the network never saw: AO RMSE <= 0.02 against the plain cone march (the accuracy bar),
     well below the constant predictor's, and an AO stage faster than the march it replaces."""
     f = synth.lj_liquid(cells=32, res=80, seed=43)
     nrm = with_normals(ctx, f)

@@ -1,5 +1,5 @@
 """CPU tests of the oracle itself: the FP32 restatement must reproduce the reference module's golden
-outputs bit for bit, and the FP64 judge must agree with them within the reference's own float error."""
+outputs bit for bit, and the FP64 restatement must agree with them within the reference's own float error."""
 import numpy as np
 import pytest
 
@@ -25,7 +25,7 @@ def test_restatement_f32_bitexact_vs_reference_golden(name):
 
 
 @pytest.mark.parametrize("name", NAMES)
-def test_fp64_judge_close_to_reference_golden(name):
+def test_fp64_restatement_close_to_reference_golden(name):
     c = G.load(name)
     xyzr = G.case_xyzr(c)
     bbox, res = G.grid(c)

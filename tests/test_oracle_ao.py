@@ -1,5 +1,5 @@
 """CPU checks of the AO restatements in the oracle: the FP32 cone pipeline (the CPU baseline's timing
-stand-in) against the FP64 judge, and known answers of the learned AO's FP64 feature restatement."""
+stand-in) against the FP64 restatement, and known answers of the learned AO's FP64 feature restatement."""
 import numpy as np
 
 import oracle
