@@ -1,7 +1,7 @@
 """CPU oracle for the particle-to-volume path — TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this package,
-and only as the checker / the timed CPU baseline. The shipped GPU library never calls it.
+and only to check results / as the timed CPU baseline. The shipped GPU library never calls it.
 
 Native libraries back it (all built by ``oracle/Makefile``):
 

@@ -1,5 +1,5 @@
 /*
- * p2v_oracle.h — CPU restatement of MegaMol's particle-to-volume path, used ONLY as the checker.
+ * p2v_oracle.h — CPU restatement of MegaMol's particle-to-volume path, used ONLY to check results.
  *
  * TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
  * this library. The shipped GPU library never calls it.
