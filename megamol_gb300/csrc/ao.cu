@@ -27,14 +27,31 @@ namespace {
 // ---------------------------------------------------------------------------------------------
 // One thread per voxel of the coarser level in 32-bit index arithmetic (an AO volume holds fewer than 2^31
 // texels, so every level above level 0 fewer than 2^28).
+// pairs: the finer level's rows have an even length and start 8-byte aligned, so the two children of a voxel
+// along x load as one float2 (the same values added in the same order as mip_voxel's loop: the same bits).
 __global__ void __launch_bounds__(256) mip_level_kernel(const float* __restrict__ src, int sx, int sy, int sz,
-    float* __restrict__ dst, int dx, int dy, int dz, float sat_scale, int quantize) {
+    float* __restrict__ dst, int dx, int dy, int dz, float sat_scale, int quantize, int pairs) {
     const uint32_t n = (uint32_t) dx * (uint32_t) dy * (uint32_t) dz;
     const uint32_t pxy = (uint32_t) dx * (uint32_t) dy;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t z = i / pxy, r = i - z * pxy;
         const uint32_t y = r / (uint32_t) dx, x = r - y * (uint32_t) dx;
-        dst[i] = mip_voxel<true>(src, sx, sy, sz, (int) x, (int) y, (int) z, sat_scale, quantize);
+        if (pairs && !quantize) {
+            const int y1 = min(2 * (int) y + 1, sy - 1), z1 = min(2 * (int) z + 1, sz - 1);
+            float acc = 0.0f;
+            for (int zz = 2 * (int) z; zz <= z1; ++zz)
+                for (int yy = 2 * (int) y; yy <= y1; ++yy) {
+                    float2 v = __ldg(reinterpret_cast<const float2*>(src + ((int64_t) zz * sy + yy) * sx + 2 * x));
+                    if (sat_scale > 0.0f) {
+                        v.x = fminf(fmaxf(__fmul_rn(v.x, sat_scale), 0.0f), 1.0f);
+                        v.y = fminf(fmaxf(__fmul_rn(v.y, sat_scale), 0.0f), 1.0f);
+                    }
+                    acc = __fadd_rn(__fadd_rn(acc, v.x), v.y);
+                }
+            dst[i] = __fmul_rn(acc, 0.125f);
+        } else {
+            dst[i] = mip_voxel<true>(src, sx, sy, sz, (int) x, (int) y, (int) z, sat_scale, quantize);
+        }
     }
 }
 
@@ -443,8 +460,9 @@ cudaError_t launch_mip_levels(const float* l0, const int d0[3], float sat_scale,
         int dd[3] = {max(1, sd[0] / 2), max(1, sd[1] / 2), max(1, sd[2] / 2)};
         const int64_t nv = (int64_t) dd[0] * dd[1] * dd[2];
         const unsigned grd = (unsigned) std::max<int64_t>(1, std::min<int64_t>((nv + 255) / 256, (int64_t) sms * 32));
+        const int pairs = (sd[0] % 2 == 0) && (reinterpret_cast<uintptr_t>(src) % 8 == 0);
         mip_level_kernel<<<grd, 256, 0, st>>>(src, sd[0], sd[1], sd[2], out[l], dd[0], dd[1], dd[2],
-                                              l == 1 ? sat_scale : 0.0f, quantize);
+                                              l == 1 ? sat_scale : 0.0f, quantize, pairs);
         for (int a = 0; a < 3; ++a)
             dims[l][a] = dd[a];
         src = out[l];
