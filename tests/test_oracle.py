@@ -125,3 +125,17 @@ def test_mip_constant_volume():
     assert m2.shape == (2, 1, 1) and np.allclose(m2, 0.5)
     m3 = oracle.mip_step_f64(np.full((4, 1, 2), 0.5))  # y is already 1: only 4 children, still /8
     assert m3.shape == (2, 1, 1) and np.allclose(m3, 0.5 * 4 / 8)
+
+
+def test_support_misses_nodes_known_answers():
+    """The FP64 test of a support holding no grid node (nodes at 0, 1, ..., 10 on every axis, h = 1): a
+    particle midway between two node planes in z with radius 0.3 misses every node, one within its radius
+    of a plane does not, and the Gaussian kernel's support (3 sigma r) reaches the planes."""
+    bbox, res = (0.0, 0.0, 0.0, 10.0, 10.0, 10.0), (11, 11, 11)
+    x = np.array([[2.0, 3.0, 4.5, 0.3],     # z midway: |4.5 - 4| = |5 - 4.5| = 0.5 > 0.3
+                  [2.0, 3.0, 4.25, 0.3],    # 0.25 from the plane z = 4
+                  [2.0, 3.0, 4.5, 0.6],     # radius beyond half the spacing
+                  [2.5, 3.5, 4.5, 0.45]],   # midway on every axis
+                 np.float32)
+    assert oracle.support_misses_nodes_f64(x, bbox, res).tolist() == [True, False, False, True]
+    assert oracle.support_misses_nodes_f64(x, bbox, res, sigma=1.0, kernel=1).tolist() == [False] * 4
