@@ -575,6 +575,9 @@ def run_ours(args):
                 "traffic": profile_traffic(f"{prof}_{args.workload}.md"),
                 "algorithmic_bytes": stages[dom]["algorithmic_bytes"], "ms_per_launch": stages[dom]["ms"],
                 "stages": stages}
+    if "texture" in stages[dom]:
+        roofline["note"] = ("HBM is not this stage's bound: its inference kernel is bound by the texture units' "
+                            "incoherent sample rate (stages.%s.texture.frac_of_incoherent)" % dom)
 
     # ---- CPU baseline (rank 0, N=1 only): one measured step of the CPU pipeline ----
     cpu = None
